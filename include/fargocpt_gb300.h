@@ -1,0 +1,245 @@
+/*
+ * fargocpt_gb300 — C ABI of the GB300 (sm_103a) engine for FargoCPT's
+ * per-timestep gas-hydrodynamics step on the 2D polar staggered grid.
+ *
+ * The engine owns every hydro field in HBM.  The caller (FargoCPT's C++
+ * driver, or any host that keeps the N-body system, configuration and I/O)
+ * hands in planet positions and scalars each step and reads back dt and
+ * disk-on-planet forces; whole fields cross the boundary only on request
+ * (initialisation, snapshots, restarts).
+ *
+ * Layout contract (identical to FargoCPT's t_polargrid, src/polargrid.h:111-133):
+ *   row-major double, ring-major: cell(nr, naz) = naz + nr * naz_count,
+ *   azimuth contiguous.  Scalar grids have nrad rows, vector grids
+ *   (V_RADIAL, V_RADIAL0, TAU_R_PHI) have nrad + 1 rows.  nrad counts the two
+ *   ghost rings exactly like FargoCPT's "Nrad" key (src/init.cpp:93-100).
+ *
+ * Every entry point returns FGPU_OK (0) or a negative fgpu_status; the text of
+ * the last error of a handle is available from fgpu_last_error().  A handle is
+ * not thread-safe; all of its work is ordered on one CUDA stream.
+ */
+#ifndef FARGOCPT_GB300_H
+#define FARGOCPT_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FGPU_ABI_VERSION 1
+
+typedef enum fgpu_status {
+    FGPU_OK = 0,
+    FGPU_ERR_BAD_ARG = -1,   /* invalid handle, size, enum or option      */
+    FGPU_ERR_OOM = -2,       /* device allocation failed                  */
+    FGPU_ERR_CUDA = -3,      /* a CUDA call failed (text in last_error)   */
+    FGPU_ERR_UNSUPPORTED = -4, /* option outside the GPU path's scope     */
+    FGPU_ERR_NONFINITE = -5, /* NaN/Inf found by fgpu_check_finite        */
+    FGPU_ERR_NO_DEVICE = -6  /* no CUDA device or the kernels are absent  */
+} fgpu_status;
+
+/* Fields, named after FargoCPT's t_data::t_polargrid_type (src/data.h:17-86). */
+typedef enum fgpu_field {
+    FGPU_SIGMA = 0,
+    FGPU_V_RADIAL = 1,      /* vector grid: nrad + 1 rows */
+    FGPU_V_AZIMUTHAL = 2,
+    FGPU_ENERGY = 3,
+    FGPU_SIGMA0 = 4,        /* damping / reference values */
+    FGPU_V_RADIAL0 = 5,     /* vector grid */
+    FGPU_V_AZIMUTHAL0 = 6,
+    FGPU_ENERGY0 = 7,
+    FGPU_SOUNDSPEED = 8,
+    FGPU_SCALE_HEIGHT = 9,
+    FGPU_PRESSURE = 10,
+    FGPU_TEMPERATURE = 11,
+    FGPU_VISCOSITY = 12,
+    FGPU_QPLUS = 13,
+    FGPU_QMINUS = 14,
+    FGPU_POTENTIAL = 15,
+    FGPU_DIV_V = 16,
+    FGPU_TAU_R_R = 17,
+    FGPU_TAU_PHI_PHI = 18,
+    FGPU_TAU_R_PHI = 19,    /* vector grid */
+    FGPU_Q_R = 20,
+    FGPU_Q_PHI = 21,
+    FGPU_FIELD_COUNT = 22
+} fgpu_field;
+
+/* Per-field ghost-ring boundary hooks (src/boundary_conditions/config.cpp:86-330). */
+typedef enum fgpu_bc {
+    FGPU_BC_NONE = 0,
+    FGPU_BC_ZEROGRADIENT = 1,  /* zero_gradient.cpp:39-90 */
+    FGPU_BC_OUTFLOW = 2,       /* outflow.cpp:16-57 (v_radial only) */
+    FGPU_BC_REFERENCE = 3,     /* reference.cpp:17-88 */
+    FGPU_BC_KEPLERIAN = 4      /* keplerian_azimuthal.cpp:18-59 (v_azimuthal only) */
+} fgpu_bc;
+
+/* Damping kinds (src/boundary_conditions/boundary_conditions.h:93-99). */
+typedef enum fgpu_damping {
+    FGPU_DAMP_NONE = 0,
+    FGPU_DAMP_REFERENCE = 1,   /* damping.cpp:311-427 */
+    FGPU_DAMP_ZERO = 2,        /* damping.cpp:429-549 */
+    FGPU_DAMP_MEAN = 3         /* damping.cpp:551-617, 682-752 */
+} fgpu_damping;
+
+/* Index of a damped quantity in fgpu_params.damping_inner/outer, in the order
+ * of FargoCPT's damping_vector (damping.cpp:214-271). */
+enum { FGPU_DQ_VRAD = 0, FGPU_DQ_VAZI = 1, FGPU_DQ_SIGMA = 2, FGPU_DQ_ENERGY = 3 };
+
+enum { FGPU_EOS_ISOTHERMAL = 0, FGPU_EOS_IDEAL = 1 };
+enum { FGPU_SPACING_ARITHMETIC = 0, FGPU_SPACING_LOGARITHMIC = 1 };
+enum { FGPU_ARTVISC_NONE = 0, FGPU_ARTVISC_SN = 1, FGPU_ARTVISC_TW = 2 };
+enum { FGPU_LIMITER_VANLEER = 0, FGPU_LIMITER_MC = 1 };
+enum { FGPU_BETA_REF_ZERO = 0, FGPU_BETA_REF_REFERENCE = 1,
+       FGPU_BETA_REF_DISKMODEL = 2, FGPU_BETA_REF_FLOOR = 3 };
+enum { FGPU_PRECISION_FP64 = 0, FGPU_PRECISION_FP32_MIXED = 1 };
+
+/*
+ * Flat parameter block: the subset of FargoCPT's parameters:: namespace and
+ * globals that the hydro step reads, already converted to code units by the
+ * caller (src/parameters.cpp, src/Interpret.cpp, src/constants.cpp).
+ */
+typedef struct fgpu_params {
+    int nrad;               /* Nrad incl. 2 ghost rings (parameters.cpp:506) */
+    int naz;                /* Naz (parameters.cpp:507) */
+    int eos;                /* FGPU_EOS_* (Interpret.cpp:398-460) */
+    int art_visc;           /* FGPU_ARTVISC_* (parameters.cpp:637-655) */
+    int art_visc_dissipation;
+    int flux_limiter;       /* FGPU_LIMITER_* (TransportEuler.cpp:306-337) */
+    int fast_transport;     /* 1: FARGO (Interpret.cpp:158-171) */
+    int heating_viscous;    /* HeatingViscous (parameters.cpp:560) */
+    int cooling_beta;       /* CoolingBetaLocal (parameters.cpp:439) */
+    int cooling_beta_reference; /* FGPU_BETA_REF_* (parameters.cpp:451-463) */
+    int damping;            /* Damping (damping.cpp:188) */
+    int damping_inner[4];   /* FGPU_DAMP_* per FGPU_DQ_* */
+    int damping_outer[4];
+    int bc_sigma_inner, bc_sigma_outer;   /* FGPU_BC_* */
+    int bc_energy_inner, bc_energy_outer;
+    int bc_vrad_inner, bc_vrad_outer;
+    int bc_vaz_inner, bc_vaz_outer;
+    int precision;          /* FGPU_PRECISION_* */
+    int reserved_i[7];
+
+    double gamma;           /* AdiabaticIndex */
+    double mu;              /* mean molecular weight */
+    double aspect_ratio;    /* AspectRatio h0 */
+    double flaring_index;   /* FlaringIndex */
+    double viscous_alpha;   /* ViscousAlpha (> 0 selects alpha viscosity) */
+    double constant_viscosity; /* used when viscous_alpha <= 0 */
+    double art_visc_factor; /* ArtificialViscosityFactor */
+    double radial_viscosity_factor;
+    double heating_viscous_factor;
+    double cfl;             /* CFL */
+    double cfl_max_var;     /* CFLmaxVar */
+    double heating_cooling_cfl_limit;
+    double sigma0;          /* Sigma0 */
+    double sigma_floor;     /* SigmaFloor (multiples of sigma0) */
+    double thickness_smoothing; /* ThicknessSmoothing */
+    double cooling_beta_value;  /* CoolingBeta */
+    double cooling_beta_ramp_up;/* CoolingBetaRampUp */
+    double minimum_temperature; /* code units */
+    double maximum_temperature; /* code units */
+    double G;               /* constants::G in code units */
+    double R_gas;           /* constants::R in code units */
+    double sigma_sb;        /* constants::sigma in code units */
+    double c_light;         /* constants::c in code units */
+    double hydro_center_mass;
+    double damping_inner_limit;
+    double damping_outer_limit;
+    double damping_time_factor;
+    double damping_time_radius_outer;
+    double vaz_inner_keplerian_factor;
+    double vaz_outer_keplerian_factor;
+    double rmin, rmax;      /* RMIN, RMAX */
+    int radial_spacing;     /* FGPU_SPACING_* (used for damping ring search) */
+    int reserved_j;
+    double reserved_d[8];
+} fgpu_params;
+
+/* One N-body object as the gas sees it (src/Pframeforce.cpp:24-35). */
+typedef struct fgpu_body {
+    double x, y;            /* position in the hydro frame */
+    double mass;            /* ramped mass, t_planet::get_rampup_mass(t) */
+    double r_sm;            /* Klahr cubic smoothing radius
+                               (roche radius * distance * factor), 0 = off */
+    double a;               /* distance from the origin, t_planet::get_r() */
+} fgpu_body;
+
+typedef struct fgpu_engine fgpu_engine;
+
+/* Fills radii[0 .. nrad + 1] with the interface radii FargoCPT builds in
+ * init_radialarrays (src/init.cpp:93-110): Radii[n] for n = 0 .. nrad + 1.
+ * Host-only helper; needs no device. */
+int fgpu_grid_radii(int spacing, double rmin, double rmax, int nrad,
+		    double *radii);
+
+/* Creates an engine on the current CUDA device.  radii: nrad + 2 values
+ * (FargoCPT's Radii[0 .. nrad + 1]).  Replaces the allocations of
+ * t_data::set_size (src/data.cpp), InitTransport (src/TransportEuler.cpp:57)
+ * and init_radialarrays (src/init.cpp:178-225). */
+int fgpu_create(const fgpu_params *params, const double *radii,
+		fgpu_engine **out);
+int fgpu_destroy(fgpu_engine *eng);
+const char *fgpu_last_error(const fgpu_engine *eng);
+/* CUDA stream (cudaStream_t) that orders all work of the handle. */
+int fgpu_get_stream(const fgpu_engine *eng, void **stream);
+
+/* Host <-> device copies of whole fields; rows must be the field's row count
+ * (nrad or nrad + 1) and cols == naz.  Synchronous with respect to the host. */
+int fgpu_upload_field(fgpu_engine *eng, int field, const double *host,
+		      int rows, int cols);
+int fgpu_download_field(fgpu_engine *eng, int field, double *host, int rows,
+			int cols);
+
+/* Per-step N-body state seen by the gas: bodies[0] is the central object.
+ * indirect_x/y: refframe::IndirectTerm (src/frame_of_reference.cpp:166-170);
+ * omega_frame: refframe::OmegaFrame.  Replaces the g_xpl/g_ypl/g_mpl set-up of
+ * CalculateNbodyPotential (src/Pframeforce.cpp:24-35). */
+int fgpu_set_bodies(fgpu_engine *eng, int n, const fgpu_body *bodies,
+		    double indirect_x, double indirect_y, double omega_frame);
+
+/* init_euler (src/SourceEuler.cpp:251-285): derived quantities (c_s, P, T, H,
+ * nu) and the heating/cooling rates the first CFL call reads
+ * (compute_heating_cooling_for_CFL, src/SourceEuler.cpp:1410-1450). */
+int fgpu_init_euler(fgpu_engine *eng, double t);
+
+/* recalculate_derived_disk_quantities (src/SourceEuler.cpp:225-249). */
+int fgpu_recalculate_derived(fgpu_engine *eng, double t);
+
+/* cfl::condition_cfl (src/cfl.cpp:185-382): the global CFL time step. */
+int fgpu_condition_cfl(fgpu_engine *eng, double *dt_out);
+
+/* boundary_conditions::apply_boundary_condition
+ * (src/boundary_conditions/boundary_conditions.cpp:65-114). */
+int fgpu_apply_boundary_condition(fgpu_engine *eng, double t, double dt,
+				  int final);
+
+/* The gas part of sim::step_Euler (src/simulation.cpp:170-265):
+ * CalculateNbodyPotential, update_with_sourceterms,
+ * update_with_artificial_viscosity, recalculate_viscosity,
+ * compute_viscous_stress_tensor, update_velocities_with_viscosity, SubStep3,
+ * apply_boundary_condition(final=false), Transport,
+ * apply_boundary_condition(final=true), recalculate_derived_disk_quantities.
+ * t is sim::time at the start of the step.  Asynchronous. */
+int fgpu_step_euler(fgpu_engine *eng, double dt, double t);
+
+/* ComputeDiskOnPlanetAccel (src/Force.cpp:23-122) for body k: accel[0..1]
+ * receive the x/y acceleration of the disk on the body. */
+int fgpu_disk_on_planet_accel(fgpu_engine *eng, int k, double accel[2]);
+
+/* quantities::gas_total_mass (src/quantities.cpp:51-74) over the active rings. */
+int fgpu_total_mass(fgpu_engine *eng, double *mass);
+
+/* Scans the evolved fields for NaN/Inf; returns FGPU_ERR_NONFINITE and the
+ * first bad (field, ring, azimuth) when one is found. */
+int fgpu_check_finite(fgpu_engine *eng, int *field, int *nr, int *naz);
+
+/* Blocks until all queued work of the handle is done. */
+int fgpu_synchronize(fgpu_engine *eng);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FARGOCPT_GB300_H */

@@ -1,0 +1,299 @@
+"""Generates the golden fixtures of tests/golden/ by running the FargoCPT
+reference itself.
+
+Needs the reference sources (default /root/reference/src) and builds them with
+oracle/ref/Makefile (parity flags: -O2 -fno-fast-math -ffp-contract=off) into
+oracle/_ref/parity/fargocpt.  Each case writes a FargoCPT setup file plus a
+seeded initial surface density (loaded by the reference via
+``SigmaCondition: 2D``), runs the reference, and stores in <case>.npz:
+
+* radii (Radii[0 .. Nrad+1]), the code-unit constants of constants.yml;
+* the fields of snapshot 0 (initial state) and of the selected snapshots;
+* the simulation time of every monitor output and the N-body positions and
+  disk torques FargoCPT writes to monitor/nbody<k>.dat at each of them.
+
+The generating setups are recorded next to the fixtures (<case>.yml) and the
+engine parameters in <case>.json.  Run from the repository root:
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import math
+import os
+import re
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from fargocpt_gb300.abi import BC, DAMP, BETA_REF  # noqa: E402
+
+REF_SRC = os.environ.get("FARGO_REFERENCE_SRC", "/root/reference/src")
+REF_EXE = os.path.join(REPO, "oracle", "_ref", "parity", "fargocpt")
+
+COMMON = dict(
+    l0="1 au", m0="1 solMass", mu=2.35, Sigma0=1e-3,
+    ThicknessSmoothing=0.6, Integrator="Euler", InitializeVradialZero="yes",
+    FirstDT=1.0, CFL=0.5, Frame="Fixed", HydroFrameCenter="primary",
+    IndirectTermMode=1, DiskFeedback="no", RadialSpacing="Logarithmic",
+    WriteDiskQuantities="no", Nmonitor=1,
+)
+
+# Each case: FargoCPT keys, grid, planet (or None), snapshots to keep.
+CASES = {
+    # C1-like: locally isothermal, one planet, SN art. visc, wave damping
+    "iso_planet_fixed_dt": dict(
+        keys=dict(SigmaSlope=0.5, AspectRatio=0.05, FlaringIndex=0.0,
+                  EquationOfState="Isothermal", ViscousAlpha=1e-3,
+                  ArtificialViscosity="SN", Transport="FARGO",
+                  InnerBoundary="outflow", OuterBoundary="reference",
+                  Damping="yes", DampingInnerLimit=1.1, DampingOuterLimit=0.9,
+                  DampingTimeFactor=1.0,
+                  DampingSurfaceDensityInner="Reference",
+                  DampingSurfaceDensityOuter="Reference",
+                  DampingVRadialInner="Reference", DampingVRadialOuter="Reference",
+                  DampingVAzimuthalInner="Reference",
+                  DampingVAzimuthalOuter="Reference",
+                  MonitorTimestep=0.002, Nsnapshots=20),
+        nrad=20, naz=48, rmin=0.4, rmax=2.5, planet=1e-3, keep=[1, 2, 5, 10, 20]),
+    # C2-like: adiabatic, beta cooling, SN with sqrt(2), flaring, planet
+    "adi_planet_fixed_dt": dict(
+        keys=dict(SigmaSlope=1.0, AspectRatio=0.05, FlaringIndex=0.25,
+                  EquationOfState="Ideal", AdiabaticIndex=1.4, ViscousAlpha=1e-3,
+                  ArtificialViscosity="SN", ArtificialViscosityFactor=1.41421356,
+                  CoolingBetaLocal="yes", CoolingBeta=10,
+                  Transport="FARGO",
+                  InnerBoundary="zerogradient", OuterBoundary="outflow",
+                  Damping="yes", DampingInnerLimit=1.15, DampingOuterLimit=0.85,
+                  DampingTimeFactor=0.5,
+                  DampingSurfaceDensityInner="Reference",
+                  DampingSurfaceDensityOuter="Reference",
+                  DampingVRadialInner="Reference", DampingVRadialOuter="Reference",
+                  DampingVAzimuthalInner="Reference",
+                  DampingVAzimuthalOuter="Reference",
+                  DampingEnergyInner="Reference", DampingEnergyOuter="Reference",
+                  MonitorTimestep=0.002, Nsnapshots=20),
+        nrad=20, naz=48, rmin=0.3, rmax=3.0, planet=1e-3, keep=[1, 2, 5, 10, 20]),
+    # CFL-limited, star only: exercises condition_cfl and the monitor clamp
+    "iso_star_cfl": dict(
+        keys=dict(SigmaSlope=0.5, AspectRatio=0.05, FlaringIndex=0.0,
+                  EquationOfState="Isothermal", ViscousAlpha=1e-3,
+                  ArtificialViscosity="SN", Transport="FARGO",
+                  InnerBoundary="zerogradient", OuterBoundary="zerogradient",
+                  Damping="yes", DampingInnerLimit=1.1, DampingOuterLimit=0.9,
+                  DampingSurfaceDensityInner="Reference",
+                  DampingSurfaceDensityOuter="Zero",
+                  DampingVRadialInner="Zero", DampingVRadialOuter="Reference",
+                  DampingVAzimuthalInner="Mean", DampingVAzimuthalOuter="Reference",
+                  MonitorTimestep=0.5, Nsnapshots=4),
+        nrad=16, naz=40, rmin=0.4, rmax=2.5, planet=None, keep=[1, 2, 3, 4]),
+    # CFL-limited adiabatic, MC limiter, standard (non-FARGO) transport
+    "adi_star_cfl_mc_std": dict(
+        keys=dict(SigmaSlope=1.0, AspectRatio=0.05, FlaringIndex=0.25,
+                  EquationOfState="Ideal", AdiabaticIndex=1.4, ViscousAlpha=3e-3,
+                  ArtificialViscosity="SN", CoolingBetaLocal="yes", CoolingBeta=10,
+                  FluxLimiter="mc", Transport="Standard",
+                  InnerBoundary="outflow", OuterBoundary="zerogradient",
+                  Damping="yes", DampingInnerLimit=1.1, DampingOuterLimit=0.9,
+                  DampingSurfaceDensityInner="Reference",
+                  DampingSurfaceDensityOuter="Reference",
+                  DampingEnergyInner="Mean", DampingEnergyOuter="Reference",
+                  MonitorTimestep=0.05, Nsnapshots=3),
+        nrad=16, naz=40, rmin=0.3, rmax=3.0, planet=None, keep=[1, 2, 3]),
+}
+
+
+def build_reference():
+    if not os.path.isdir(REF_SRC):
+        raise SystemExit(f"reference sources not found at {REF_SRC}")
+    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle", "ref"),
+                    "VARIANT=parity", f"REF={REF_SRC}", "-j8"], check=True)
+
+
+def log_radii(nrad, rmin, rmax):
+    q = math.pow(rmax / rmin, 1.0 / (nrad - 2.0))
+    return np.array([rmin * math.pow(q, n - 1.0) for n in range(nrad + 2)])
+
+
+def read_yaml_values(path):
+    """Tiny reader for FargoCPT's constants.yml / units.yml blocks."""
+    out, cur = {}, None
+    for line in open(path):
+        if not line.strip() or line.startswith("#"):
+            continue
+        if not line.startswith(" "):
+            cur = line.strip().rstrip(":")
+            out[cur] = {}
+        else:
+            k, _, v = line.strip().partition(":")
+            out[cur][k.strip()] = v.strip()
+    return out
+
+
+def engine_params(case, consts, temp_unit):
+    k = {**COMMON, **case["keys"]}
+    adi = k["EquationOfState"].lower() in ("ideal", "adiabatic")
+    inner, outer = k["InnerBoundary"].lower(), k["OuterBoundary"].lower()
+
+    def composite(name):   # boundary_conditions/config.cpp:344-430
+        return {"zerogradient": ("zerogradient", "zerogradient", "zerogradient"),
+                "outflow": ("zerogradient", "zerogradient", "outflow"),
+                "reference": ("reference", "reference", "reference")}[name]
+
+    si, ei, vi = composite(inner)
+    so, eo, vo = composite(outer)
+
+    def damp(key):
+        v = str(k.get(key, "None")).lower()[0]
+        return {"n": 0, "r": 1, "i": 1, "y": 1, "m": 3, "z": 2}[v]
+
+    return dict(
+        nrad=case["nrad"], naz=case["naz"], eos=1 if adi else 0,
+        art_visc=1 if k.get("ArtificialViscosity", "SN").upper() == "SN" else 0,
+        art_visc_dissipation=1, flux_limiter=1 if k.get("FluxLimiter", "") == "mc" else 0,
+        fast_transport=1 if k["Transport"].lower().startswith("f") else 0,
+        heating_viscous=1, cooling_beta=1 if k.get("CoolingBetaLocal") == "yes" else 0,
+        cooling_beta_reference=BETA_REF["zero"], damping=1,
+        damping_inner=[damp("DampingVRadialInner"), damp("DampingVAzimuthalInner"),
+                       damp("DampingSurfaceDensityInner"), damp("DampingEnergyInner")],
+        damping_outer=[damp("DampingVRadialOuter"), damp("DampingVAzimuthalOuter"),
+                       damp("DampingSurfaceDensityOuter"), damp("DampingEnergyOuter")],
+        bc_sigma_inner=BC[si], bc_sigma_outer=BC[so],
+        # energy_inner reads the outer composite's name (config.cpp:146)
+        bc_energy_inner=BC[eo], bc_energy_outer=BC[eo],
+        bc_vrad_inner=BC[vi], bc_vrad_outer=BC[vo],
+        bc_vaz_inner=BC["keplerian"], bc_vaz_outer=BC["keplerian"],
+        precision=0,
+        gamma=float(k.get("AdiabaticIndex", 1.4)), mu=float(k["mu"]),
+        aspect_ratio=float(k["AspectRatio"]), flaring_index=float(k["FlaringIndex"]),
+        viscous_alpha=float(k["ViscousAlpha"]), constant_viscosity=0.0,
+        art_visc_factor=float(k.get("ArtificialViscosityFactor", 1.41)),
+        radial_viscosity_factor=1.0, heating_viscous_factor=1.0,
+        cfl=float(k["CFL"]), cfl_max_var=1.1, heating_cooling_cfl_limit=10.0,
+        sigma0=float(k["Sigma0"]), sigma_floor=1e-9,
+        thickness_smoothing=float(k["ThicknessSmoothing"]),
+        cooling_beta_value=float(k.get("CoolingBeta", 1.0)), cooling_beta_ramp_up=0.0,
+        minimum_temperature=3.0 / temp_unit, maximum_temperature=1.0e300 / temp_unit,
+        G=float(consts["gravitational constant"]["code value"]),
+        R_gas=float(consts["specific gas constant"]["code value"]),
+        sigma_sb=float(consts["Stefan-Boltzmann constant"]["code value"]),
+        c_light=float(consts["speed of light"]["code value"]),
+        hydro_center_mass=1.0,
+        damping_inner_limit=float(k["DampingInnerLimit"]),
+        damping_outer_limit=float(k["DampingOuterLimit"]),
+        damping_time_factor=float(k.get("DampingTimeFactor", 1.0)),
+        damping_time_radius_outer=float(case["rmax"]),
+        vaz_inner_keplerian_factor=1.0, vaz_outer_keplerian_factor=1.0,
+        rmin=float(case["rmin"]), rmax=float(case["rmax"]), radial_spacing=1,
+    )
+
+
+def write_setup(case, path, seed):
+    nrad, naz = case["nrad"], case["naz"]
+    radii = log_radii(nrad, case["rmin"], case["rmax"])
+    rinf, rsup = radii[:nrad], radii[1:nrad + 1]
+    rmed = 2.0 / 3.0 * (rsup ** 3 - rinf ** 3) / (rsup ** 2 - rinf ** 2)
+    rng = np.random.default_rng(seed)
+    slope = case["keys"]["SigmaSlope"]
+    sigma = 1e-3 * rmed[:, None] ** -slope * (1 + 1e-3 * rng.uniform(-1, 1, (nrad, naz)))
+    sigma.astype("<f8").tofile(os.path.join(path, "sigma_init.dat"))
+    keys = {**COMMON, **case["keys"], "Nrad": nrad, "Naz": naz,
+            "Rmin": case["rmin"], "Rmax": case["rmax"],
+            "SigmaCondition": "2D", "SigmaFilename": "sigma_init.dat",
+            "OutputDir": "out"}
+    lines = [f"{k}: {v}" for k, v in keys.items()]
+    lines.append("nbody:")
+    lines.append("- name: star\n  semi-major axis: 0.0\n  mass: 1.0")
+    if case["planet"] is not None:
+        lines.append(f"- name: planet\n  semi-major axis: 1.0\n  mass: {case['planet']}\n"
+                     "  eccentricity: 0.0")
+    text = "\n".join(lines) + "\n"
+    with open(os.path.join(path, "setup.yml"), "w") as f:
+        f.write(text)
+    return text
+
+
+def read_snapshot(out, n, nrad, naz):
+    d = os.path.join(out, "snapshots", str(n))
+
+    def rd(name, rows):
+        return np.fromfile(os.path.join(d, name), dtype="<f8").reshape(rows, naz)
+
+    return dict(SIGMA=rd("Sigma.dat", nrad), V_RADIAL=rd("vrad.dat", nrad + 1),
+                V_AZIMUTHAL=rd("vazi.dat", nrad), ENERGY=rd("energy.dat", nrad))
+
+
+def read_nbody(out, k):
+    rows = []
+    for line in open(os.path.join(out, "monitor", f"nbody{k}.dat")):
+        if line.startswith("#") or not line.strip():
+            continue
+        rows.append([float(x) for x in line.split()])
+    a = np.array(rows)
+    # columns (nbody/planet.cpp:361-372): snapshot, monitor, x, y, vx, vy,
+    # mass, time, omega_frame, ..., torque (18)
+    return dict(x=a[:, 2], y=a[:, 3], mass=a[:, 6], time=a[:, 7], torque=a[:, 18])
+
+
+def make_case(name, case, seed):
+    tmp = tempfile.mkdtemp(prefix=f"golden_{name}_")
+    try:
+        text = write_setup(case, tmp, seed)
+        r = subprocess.run([REF_EXE, "start", "setup.yml"], cwd=tmp,
+                           capture_output=True, text=True, timeout=600,
+                           env={**os.environ, "OMP_NUM_THREADS": "1"})
+        if r.returncode != 0:
+            print(r.stdout[-3000:], r.stderr[-3000:])
+            raise SystemExit(f"reference run {name} failed")
+        out = os.path.join(tmp, "out")
+        nrad, naz = case["nrad"], case["naz"]
+        used = np.loadtxt(os.path.join(out, "used_rad.dat"))
+        radii = log_radii(nrad, case["rmin"], case["rmax"])
+        assert np.array_equal(used, radii[:nrad + 1]), "radii formula mismatch"
+        consts = read_yaml_values(os.path.join(out, "constants.yml"))
+        units = read_yaml_values(os.path.join(out, "units.yml"))
+        temp_unit = float(units["temperature"]["cgs value"])
+        params = engine_params(case, consts, temp_unit)
+        arrays = {"radii": radii}
+        snap0 = read_snapshot(out, 0, nrad, naz)
+        for k, v in snap0.items():
+            arrays[f"s0_{k}"] = v
+        for n in case["keep"]:
+            for k, v in read_snapshot(out, n, nrad, naz).items():
+                arrays[f"s{n}_{k}"] = v
+        nb = 2 if case["planet"] is not None else 1
+        for k in range(nb):
+            for key, v in read_nbody(out, k).items():
+                arrays[f"body{k}_{key}"] = v
+        arrays["keep"] = np.array(case["keep"])
+        meta = dict(params=params, first_dt=float(COMMON["FirstDT"]),
+                    monitor_timestep=float(case["keys"]["MonitorTimestep"]),
+                    nsnapshots=int(case["keys"]["Nsnapshots"]), nbodies=nb,
+                    seed=seed, reference_log_tail=r.stdout.splitlines()[-1])
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **arrays)
+        with open(os.path.join(HERE, f"{name}.json"), "w") as f:
+            json.dump(meta, f, indent=1, sort_keys=True)
+        with open(os.path.join(HERE, f"{name}.yml"), "w") as f:
+            f.write("# FargoCPT setup that produced the fixture (sigma file: seeded noise)\n")
+            f.write(text)
+        print(f"{name}: ok ({meta['reference_log_tail']})")
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+
+
+def main():
+    build_reference()
+    for i, (name, case) in enumerate(CASES.items()):
+        make_case(name, case, seed=1000 + i)
+
+
+if __name__ == "__main__":
+    main()
