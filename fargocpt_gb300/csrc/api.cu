@@ -1,0 +1,689 @@
+// C ABI of the GB300 hydro engine (include/fargocpt_gb300.h).
+//
+// Host side: owns the device buffers, computes the per-ring metric tables with
+// the expressions of FargoCPT's init_radialarrays (src/init.cpp:188-225) so the
+// device sees bit-identical metric values, resolves boundary and damping
+// set-up, and sequences the kernels of one hydro step on the handle's stream.
+#include "../../include/fargocpt_gb300.h"
+#include "hydro.cuh"
+#include "kernels.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+using namespace fgpu;
+
+struct fgpu_engine {
+    fgpu_params p;
+    int nr = 0, nz = 0;
+    size_t cells = 0, vcells = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+
+    double *field[FGPU_FIELD_COUNT] = {};
+    double *sigma_alt = nullptr, *vr_alt = nullptr, *vaz_alt = nullptr, *energy_alt = nullptr;
+    double *mom[4] = {};
+    double *ring_ws = nullptr;
+    size_t az_smem = 0;
+    int az_block = 256;
+    int radial_chunk = 16;
+
+    double *tables_mem = nullptr;
+    Tables tabs{};
+    double *damp_mem = nullptr;
+    int *damp_rings = nullptr;
+    int n_damp_rings = 0;
+    double *partial = nullptr, *red_out = nullptr;
+    unsigned long long *d_dtmin = nullptr, *d_bad = nullptr;
+    double *h_pinned = nullptr;
+
+    Geo geo{};
+    Phys ph{};
+    Bodies bodies{};
+    BcSpec bc{};
+    Damping dm{};
+    bool cfl_valid = false;
+    std::vector<double> host_radii;
+};
+
+#define CK(call)                                                                  \
+    do {                                                                          \
+        cudaError_t e_ = (call);                                                  \
+        if (e_ != cudaSuccess) {                                                  \
+            eng->err = std::string(#call) + ": " + cudaGetErrorString(e_);       \
+            return FGPU_ERR_CUDA;                                                 \
+        }                                                                         \
+    } while (0)
+
+static bool is_vector_field(int f)
+{
+    return f == FGPU_V_RADIAL || f == FGPU_V_RADIAL0 || f == FGPU_TAU_R_PHI;
+}
+
+static int field_rows(const fgpu_engine *e, int f) { return is_vector_field(f) ? e->nr + 1 : e->nr; }
+
+extern "C" int fgpu_grid_radii(int spacing, double rmin, double rmax, int nrad, double *radii)
+{
+    if (!radii || nrad < 4 || !(rmax > rmin) || !(rmin > 0.0)) return FGPU_ERR_BAD_ARG;
+    if (spacing == FGPU_SPACING_LOGARITHMIC) {
+        // init.cpp:93-100
+        const double q = std::pow((rmax / rmin), 1.0 / ((double)nrad - 2.0));
+        for (int n = 0; n <= nrad + 1; ++n) radii[n] = rmin * std::pow(q, (double)n - 1.0);
+    } else if (spacing == FGPU_SPACING_ARITHMETIC) {
+        // init.cpp:103-110
+        const double interval = (rmax - rmin) / (double)(nrad - 2.0);
+        for (int n = 0; n <= nrad + 1; ++n) radii[n] = rmin + interval * (double)(n - 1.0);
+    } else {
+        return FGPU_ERR_BAD_ARG;
+    }
+    return FGPU_OK;
+}
+
+extern "C" const char *fgpu_last_error(const fgpu_engine *eng)
+{
+    return eng ? eng->err.c_str() : "null engine";
+}
+
+extern "C" int fgpu_get_stream(const fgpu_engine *eng, void **stream)
+{
+    if (!eng || !stream) return FGPU_ERR_BAD_ARG;
+    *stream = (void *)eng->stream;
+    return FGPU_OK;
+}
+
+// ------------------------------------------------------------------------
+// damping ring search (find_cell_id.cpp:222-452 with NDEBUG clamping)
+// ------------------------------------------------------------------------
+static int cell_id(const fgpu_engine *e, const std::vector<double> &Rmed, double r, bool rinf)
+{
+    const fgpu_params &p = e->p;
+    int id;
+    if (p.radial_spacing == FGPU_SPACING_LOGARITHMIC) {
+        const double g = std::pow(p.rmax / p.rmin, 1.0 / ((double)p.nrad - 2.0));
+        const double ilg = 1.0 / std::log(g);
+        if (rinf) {
+            id = (int)std::floor(std::log(r / p.rmin) * ilg) + 1;
+        } else {
+            const double oc = 3.0 / 2.0 / p.rmin * (1 - std::pow(g, 2.0)) / (1 - std::pow(g, 3.0));
+            id = (int)std::floor(std::log(r * oc) * ilg) + 1;
+        }
+    } else {
+        const double g = ((double)p.nrad - 2.0) / (p.rmax - p.rmin);
+        id = (int)std::floor((r - p.rmin) * g) + 1;
+        if (!rinf && id >= 0 && id <= e->nr && Rmed[id] > r) id--;
+    }
+    if (id < 0) id = 0;
+    if (id > e->nr - 1) id = e->nr - 1;
+    return id;
+}
+
+static int clamp_id(int id, bool vec, int nr)
+{
+    const int mx = nr - (vec ? 0 : 1);
+    return std::min(std::max(id, 0), mx);
+}
+
+static double omega_kepler(const fgpu_params &p, double r)
+{
+    return std::sqrt(p.G * p.hydro_center_mass / (r * r * r));  // Theo.cpp:246-249
+}
+
+static int validate(const fgpu_params *p, std::string &why)
+{
+    if (p->nrad < 6 || p->naz < 8) { why = "nrad >= 6 and naz >= 8 required"; return FGPU_ERR_BAD_ARG; }
+    if (p->naz > 8192) { why = "naz > 8192 not supported by the azimuthal kernel"; return FGPU_ERR_UNSUPPORTED; }
+    if (p->eos != FGPU_EOS_ISOTHERMAL && p->eos != FGPU_EOS_IDEAL) { why = "eos"; return FGPU_ERR_BAD_ARG; }
+    if (p->art_visc == FGPU_ARTVISC_TW) { why = "Tscharnuter-Winkler artificial viscosity is not on the GPU path"; return FGPU_ERR_UNSUPPORTED; }
+    if (p->art_visc != FGPU_ARTVISC_NONE && p->art_visc != FGPU_ARTVISC_SN) { why = "art_visc"; return FGPU_ERR_BAD_ARG; }
+    if (p->precision != FGPU_PRECISION_FP64) { why = "only the FP64 precision form is built"; return FGPU_ERR_UNSUPPORTED; }
+    if (p->radial_spacing != FGPU_SPACING_LOGARITHMIC && p->radial_spacing != FGPU_SPACING_ARITHMETIC) { why = "radial_spacing"; return FGPU_ERR_BAD_ARG; }
+    const int bcs[8] = {p->bc_sigma_inner, p->bc_sigma_outer, p->bc_energy_inner, p->bc_energy_outer,
+                        p->bc_vrad_inner, p->bc_vrad_outer, p->bc_vaz_inner, p->bc_vaz_outer};
+    for (int k = 0; k < 8; ++k) {
+        if (bcs[k] < FGPU_BC_NONE || bcs[k] > FGPU_BC_KEPLERIAN) { why = "boundary kind"; return FGPU_ERR_BAD_ARG; }
+    }
+    for (int q = 0; q < 4; ++q) {
+        if (p->damping_inner[q] < 0 || p->damping_inner[q] > FGPU_DAMP_MEAN ||
+            p->damping_outer[q] < 0 || p->damping_outer[q] > FGPU_DAMP_MEAN) {
+            why = "damping kind"; return FGPU_ERR_BAD_ARG;
+        }
+    }
+    if (!(p->cfl > 0) || !(p->G > 0) || !(p->hydro_center_mass > 0)) { why = "cfl, G, mass must be > 0"; return FGPU_ERR_BAD_ARG; }
+    return FGPU_OK;
+}
+
+static int setup_tables(fgpu_engine *eng, const double *radii)
+{
+    const fgpu_params &p = eng->p;
+    const int nr = eng->nr, nz = eng->nz;
+    const int R = nr + 2;
+    const double dphi = 2.0 * M_PI / (double)nz;      // Interpret.cpp:230
+    const double invdphi = (double)nz / (2.0 * M_PI); // Interpret.cpp:231
+    eng->geo = Geo{nr, nz, dphi, invdphi};
+    enum { RINF, RSUP, RMED, SURF, INVRMED, INVSURF, INVDIFFRMED, INVDIFFRSUP, INVDIFFRSUPRB,
+           INVRINF, RINFSQ, TWOOVER, OMEGAK, INVOMEGAK, CSISO, INVDXSRC, INVDXTHETA, EMODEL,
+           NTAB };
+    std::vector<double> h((size_t)NTAB * R, 0.0);
+    auto T = [&](int k) { return h.data() + (size_t)k * R; };
+    for (int n = 0; n <= nr; ++n) {
+        T(RINF)[n] = radii[n];
+        T(RSUP)[n] = radii[n + 1];
+        double rm = 2.0 / 3.0 * (std::pow(T(RSUP)[n], 3) - std::pow(T(RINF)[n], 3));
+        rm = rm / (std::pow(T(RSUP)[n], 2) - std::pow(T(RINF)[n], 2));
+        T(RMED)[n] = rm;
+        T(SURF)[n] = M_PI * (std::pow(T(RSUP)[n], 2) - std::pow(T(RINF)[n], 2)) / (double)nz;
+        T(INVRMED)[n] = 1.0 / rm;
+        T(INVSURF)[n] = 1.0 / T(SURF)[n];
+        T(INVDIFFRSUP)[n] = 1.0 / (T(RSUP)[n] - T(RINF)[n]);
+        T(INVDIFFRSUPRB)[n] = 1.0 / ((T(RSUP)[n] - T(RINF)[n]) * rm);
+        T(INVRINF)[n] = 1.0 / T(RINF)[n];
+        T(RINFSQ)[n] = std::pow(T(RINF)[n], 2);
+        T(OMEGAK)[n] = omega_kepler(p, rm);
+        T(INVOMEGAK)[n] = 1.0 / omega_kepler(p, rm);
+        {   // compute_sound_speed_normal, isothermal branch (SourceEuler.cpp:983-990)
+            const double vK = std::sqrt(p.G * p.hydro_center_mass / rm);
+            const double hh = p.aspect_ratio * std::pow(rm, p.flaring_index);
+            T(CSISO)[n] = hh * vK;
+        }
+        T(INVDXSRC)[n] = 2.0 / (dphi * (T(RSUP)[n] + T(RINF)[n]));
+        T(INVDXTHETA)[n] = 1.0 / (dphi * rm);
+        T(EMODEL)[n] = 1.0 / (p.gamma - 1.0) * std::pow(p.aspect_ratio, 2) *
+                       std::pow(rm, 2.0 * p.flaring_index - 1.0) * p.G * p.hydro_center_mass;
+    }
+    for (int n = 1; n <= nr; ++n) T(INVDIFFRMED)[n] = 1.0 / (T(RMED)[n] - T(RMED)[n - 1]);
+    for (int n = 0; n < nr; ++n) {
+        T(TWOOVER)[n] = 2.0 / (std::pow(T(RINF)[n + 1], 2) - std::pow(T(RINF)[n], 2));
+    }
+    std::vector<double> cs(nz), sn(nz);
+    for (int j = 0; j < nz; ++j) {
+        cs[j] = std::cos(dphi * (double)j);  // SideEuler.cpp:56-61
+        sn[j] = std::sin(dphi * (double)j);
+    }
+    const size_t bytes = sizeof(double) * ((size_t)NTAB * R + 2 * (size_t)nz);
+    CK(cudaMalloc(&eng->tables_mem, bytes));
+    CK(cudaMemcpy(eng->tables_mem, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice));
+    double *tc = eng->tables_mem + (size_t)NTAB * R;
+    CK(cudaMemcpy(tc, cs.data(), sizeof(double) * nz, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(tc + nz, sn.data(), sizeof(double) * nz, cudaMemcpyHostToDevice));
+    auto D = [&](int k) -> const double * { return eng->tables_mem + (size_t)k * R; };
+    Tables &t = eng->tabs;
+    t.Rinf = D(RINF); t.Rsup = D(RSUP); t.Rmed = D(RMED); t.Surf = D(SURF);
+    t.InvRmed = D(INVRMED); t.InvSurf = D(INVSURF); t.InvDiffRmed = D(INVDIFFRMED);
+    t.InvDiffRsup = D(INVDIFFRSUP); t.InvDiffRsupRb = D(INVDIFFRSUPRB); t.InvRinf = D(INVRINF);
+    t.RinfSq = D(RINFSQ); t.TwoOverDRa2 = D(TWOOVER); t.OmegaK = D(OMEGAK);
+    t.InvOmegaK = D(INVOMEGAK); t.CsIso = D(CSISO); t.InvDxSrc = D(INVDXSRC);
+    t.InvDxTheta = D(INVDXTHETA); t.EModel = D(EMODEL);
+    t.cosj = tc; t.sinj = tc + nz;
+
+    // boundary hooks
+    BcSpec &bc = eng->bc;
+    bc.sigma_in = p.bc_sigma_inner; bc.sigma_out = p.bc_sigma_outer;
+    bc.energy_in = p.bc_energy_inner; bc.energy_out = p.bc_energy_outer;
+    bc.vr_in = p.bc_vrad_inner; bc.vr_out = p.bc_vrad_outer;
+    bc.vaz_in = p.bc_vaz_inner; bc.vaz_out = p.bc_vaz_outer;
+    bc.vk_in = std::sqrt(p.G * p.hydro_center_mass / T(RMED)[0]);        // Theo.cpp:207-211
+    bc.vk_out = std::sqrt(p.G * p.hydro_center_mass / T(RMED)[nr - 1]);
+    bc.kep_in = p.vaz_inner_keplerian_factor; bc.kep_out = p.vaz_outer_keplerian_factor;
+
+    // damping (damping.cpp:311-752)
+    std::vector<double> Rmed(T(RMED), T(RMED) + R);
+    std::vector<double> fac((size_t)4 * (nr + 1), 0.0);  // inner S, outer S, inner V, outer V
+    for (int vec = 0; vec < 2; ++vec) {
+        const double *radius = vec ? T(RINF) : T(RMED);
+        double *fi = fac.data() + (size_t)(vec ? 2 : 0) * (nr + 1);
+        double *fo = fi + (nr + 1);
+        for (int n = 0; n <= nr; ++n) {
+            fi[n] = std::pow((radius[n] - p.rmin * p.damping_inner_limit) /
+                                 (p.rmin - p.rmin * p.damping_inner_limit), 2);
+            fo[n] = std::pow((radius[n] - p.rmax * p.damping_outer_limit) /
+                                 (p.rmax - p.rmax * p.damping_outer_limit), 2);
+        }
+    }
+    CK(cudaMalloc(&eng->damp_mem, sizeof(double) * fac.size()));
+    CK(cudaMemcpy(eng->damp_mem, fac.data(), sizeof(double) * fac.size(), cudaMemcpyHostToDevice));
+    const int dq_field[4] = {FGPU_V_RADIAL, FGPU_V_AZIMUTHAL, FGPU_SIGMA, FGPU_ENERGY};
+    std::vector<char> ring_on(nr + 1, 0);
+    for (int q = 0; q < 4; ++q) {
+        DampQ &d = eng->dm.q[q];
+        const bool vec = is_vector_field(dq_field[q]);
+        const double *radius = vec ? T(RINF) : T(RMED);
+        d.vector = vec;
+        d.is_density = dq_field[q] == FGPU_SIGMA;
+        d.kind_in = p.damping ? p.damping_inner[q] : 0;
+        d.kind_out = p.damping ? p.damping_outer[q] : 0;
+        d.active_in = (p.damping_inner_limit > 1.0) && (radius[0] < p.rmin * p.damping_inner_limit);
+        d.limit_in = vec ? clamp_id(cell_id(eng, Rmed, p.rmin * p.damping_inner_limit, true), true, nr)
+                         : clamp_id(cell_id(eng, Rmed, p.rmin * p.damping_inner_limit, false), false, nr);
+        const int maxr = vec ? nr : nr - 1;
+        d.active_out = (p.damping_outer_limit < 1.0) && (radius[maxr] > p.rmax * p.damping_outer_limit);
+        d.limit_out = vec ? clamp_id(cell_id(eng, Rmed, p.rmax * p.damping_outer_limit, true) + 1, true, nr)
+                          : clamp_id(cell_id(eng, Rmed, p.rmax * p.damping_outer_limit, false) + 1, false, nr);
+        d.tau_in = p.damping_time_factor * 2.0 * M_PI / omega_kepler(p, p.rmin);
+        d.tau_out = p.damping_time_factor * 2.0 * M_PI / omega_kepler(p, p.damping_time_radius_outer);
+        d.x0_zero_in = d.is_density ? p.sigma_floor * p.sigma0 : 0.0;
+        d.fac_in = eng->damp_mem + (size_t)(vec ? 2 : 0) * (nr + 1);
+        d.fac_out = d.fac_in + (nr + 1);
+        const int size = vec ? nr + 1 : nr;
+        if (d.kind_in && d.active_in) for (int n = 0; n <= d.limit_in; ++n) ring_on[n] = 1;
+        if (d.kind_out && d.active_out) for (int n = d.limit_out; n < size; ++n) ring_on[n] = 1;
+    }
+    std::vector<int> rings;
+    for (int n = 0; n <= nr; ++n) if (ring_on[n]) rings.push_back(n);
+    eng->n_damp_rings = (int)rings.size();
+    if (!rings.empty()) {
+        CK(cudaMalloc(&eng->damp_rings, sizeof(int) * rings.size()));
+        CK(cudaMemcpy(eng->damp_rings, rings.data(), sizeof(int) * rings.size(), cudaMemcpyHostToDevice));
+    }
+
+    // physics constants
+    Phys &ph = eng->ph;
+    ph.adiabatic = p.eos == FGPU_EOS_IDEAL;
+    ph.art_visc_sn = p.art_visc == FGPU_ARTVISC_SN;
+    ph.dissipation = p.art_visc_dissipation;
+    ph.limiter_mc = p.flux_limiter == FGPU_LIMITER_MC;
+    ph.fast_transport = p.fast_transport;
+    ph.heating_viscous = p.heating_viscous;
+    ph.cooling_beta = p.cooling_beta;
+    ph.beta_ref = p.cooling_beta_reference;
+    ph.gamma = p.gamma;
+    ph.gm1 = p.gamma - 1.0;
+    ph.g_gm1 = p.gamma * (p.gamma - 1.0);
+    ph.sqrt_gamma = std::sqrt(p.gamma);
+    ph.mu = p.mu;
+    ph.alpha = p.viscous_alpha;
+    ph.constant_viscosity = p.constant_viscosity;
+    ph.C2 = std::pow(p.art_visc_factor, 2);
+    ph.four_C2 = 4.0 * std::pow(p.art_visc_factor, 2);
+    ph.rvf = p.radial_viscosity_factor;
+    ph.hvf = p.heating_viscous_factor;
+    ph.cfl = p.cfl;
+    ph.inv_hc_limit = 1.0 / p.heating_cooling_cfl_limit;
+    ph.sigma_min = p.sigma_floor * p.sigma0;
+    ph.sigma_floor10 = 10.0 * p.sigma0 * p.sigma_floor;
+    ph.eps_smooth = p.thickness_smoothing;
+    ph.tmin = p.minimum_temperature;
+    ph.tmax = p.maximum_temperature;
+    ph.Rgas = p.R_gas;
+    ph.sigma_sb = p.sigma_sb;
+    ph.c_light = p.c_light;
+    ph.G = p.G;
+    ph.Mc = p.hydro_center_mass;
+    ph.c_v_inv = p.mu / p.R_gas * (p.gamma - 1.0);
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_create(const fgpu_params *params, const double *radii, fgpu_engine **out)
+{
+    if (!params || !radii || !out) return FGPU_ERR_BAD_ARG;
+    *out = nullptr;
+    std::string why;
+    int rc = validate(params, why);
+    if (rc != FGPU_OK) {
+        fprintf(stderr, "fgpu_create: %s\n", why.c_str());
+        return rc;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return FGPU_ERR_NO_DEVICE;
+    }
+    fgpu_engine *eng = new (std::nothrow) fgpu_engine();
+    if (!eng) return FGPU_ERR_OOM;
+    eng->p = *params;
+    eng->nr = params->nrad;
+    eng->nz = params->naz;
+    eng->cells = (size_t)eng->nr * eng->nz;
+    eng->vcells = (size_t)(eng->nr + 1) * eng->nz;
+    eng->host_radii.assign(radii, radii + eng->nr + 2);
+    auto fail = [&](int code) {
+        fprintf(stderr, "fgpu_create: %s\n", eng->err.c_str());
+        fgpu_destroy(eng);
+        return code;
+    };
+    if (cudaStreamCreateWithFlags(&eng->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        eng->err = "stream";
+        return fail(FGPU_ERR_CUDA);
+    }
+    for (int f = 0; f < FGPU_FIELD_COUNT; ++f) {
+        const size_t n = (size_t)field_rows(eng, f) * eng->nz;
+        if (cudaMalloc(&eng->field[f], n * sizeof(double)) != cudaSuccess) {
+            eng->err = "out of device memory (fields)";
+            return fail(FGPU_ERR_OOM);
+        }
+        cudaMemset(eng->field[f], 0, n * sizeof(double));
+    }
+    double **alts[4] = {&eng->sigma_alt, &eng->vr_alt, &eng->vaz_alt, &eng->energy_alt};
+    for (int k = 0; k < 4; ++k) {
+        const size_t n = k == 1 ? eng->vcells : eng->cells;
+        if (cudaMalloc(alts[k], n * sizeof(double)) != cudaSuccess) {
+            eng->err = "out of device memory (state)";
+            return fail(FGPU_ERR_OOM);
+        }
+        cudaMemset(*alts[k], 0, n * sizeof(double));
+    }
+    for (int k = 0; k < 4; ++k) {
+        if (cudaMalloc(&eng->mom[k], eng->cells * sizeof(double)) != cudaSuccess) {
+            eng->err = "out of device memory (momenta)";
+            return fail(FGPU_ERR_OOM);
+        }
+    }
+    if (cudaMalloc(&eng->partial, sizeof(double) * 5 * (size_t)eng->nr) != cudaSuccess ||
+        cudaMalloc(&eng->red_out, sizeof(double) * 8) != cudaSuccess ||
+        cudaMalloc(&eng->d_dtmin, sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMalloc(&eng->d_bad, sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMallocHost(&eng->h_pinned, sizeof(double) * 16) != cudaSuccess) {
+        eng->err = "out of memory (reductions)";
+        return fail(FGPU_ERR_OOM);
+    }
+    rc = setup_tables(eng, radii);
+    if (rc != FGPU_OK) return fail(rc);
+
+    // azimuthal transport: whole ring in shared memory when it fits
+    eng->az_block = std::max(128, std::min(1024, ((eng->nz + 7) / 8 + 31) / 32 * 32));
+    eng->az_smem = azimuthal_smem_bytes(eng->nz);
+    if (eng->az_smem > 220 * 1024) {
+        if (cudaMalloc(&eng->ring_ws, eng->az_smem * (size_t)eng->nr) != cudaSuccess) {
+            eng->err = "out of device memory (ring workspace)";
+            return fail(FGPU_ERR_OOM);
+        }
+    } else if (eng->az_smem > 48 * 1024) {
+        if (prepare_azimuthal(eng->az_smem) != cudaSuccess) {
+            eng->err = "cannot reserve shared memory for the azimuthal kernel";
+            return fail(FGPU_ERR_CUDA);
+        }
+    }
+    if (cudaStreamSynchronize(eng->stream) != cudaSuccess) {
+        eng->err = cudaGetErrorString(cudaGetLastError());
+        return fail(FGPU_ERR_CUDA);
+    }
+    *out = eng;
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_destroy(fgpu_engine *eng)
+{
+    if (!eng) return FGPU_ERR_BAD_ARG;
+    if (eng->stream) cudaStreamSynchronize(eng->stream);
+    for (int f = 0; f < FGPU_FIELD_COUNT; ++f) cudaFree(eng->field[f]);
+    cudaFree(eng->sigma_alt); cudaFree(eng->vr_alt); cudaFree(eng->vaz_alt); cudaFree(eng->energy_alt);
+    for (int k = 0; k < 4; ++k) cudaFree(eng->mom[k]);
+    cudaFree(eng->ring_ws); cudaFree(eng->tables_mem); cudaFree(eng->damp_mem);
+    cudaFree(eng->damp_rings); cudaFree(eng->partial); cudaFree(eng->red_out);
+    cudaFree(eng->d_dtmin); cudaFree(eng->d_bad);
+    if (eng->h_pinned) cudaFreeHost(eng->h_pinned);
+    if (eng->stream) cudaStreamDestroy(eng->stream);
+    delete eng;
+    return FGPU_OK;
+}
+
+static Launch launch_of(const fgpu_engine *eng)
+{
+    Launch L;
+    L.g = eng->geo;
+    L.t = eng->tabs;
+    L.ph = eng->ph;
+    L.stream = eng->stream;
+    L.bx = 128;
+    return L;
+}
+
+static State state_of(fgpu_engine *eng)
+{
+    State s;
+    double **f = eng->field;
+    s.sigma = f[FGPU_SIGMA]; s.vr = f[FGPU_V_RADIAL]; s.vaz = f[FGPU_V_AZIMUTHAL];
+    s.energy = f[FGPU_ENERGY]; s.sigma0 = f[FGPU_SIGMA0]; s.vr0 = f[FGPU_V_RADIAL0];
+    s.vaz0 = f[FGPU_V_AZIMUTHAL0]; s.energy0 = f[FGPU_ENERGY0]; s.cs = f[FGPU_SOUNDSPEED];
+    s.H = f[FGPU_SCALE_HEIGHT]; s.P = f[FGPU_PRESSURE]; s.T = f[FGPU_TEMPERATURE];
+    s.nu = f[FGPU_VISCOSITY]; s.qplus = f[FGPU_QPLUS]; s.qminus = f[FGPU_QMINUS];
+    s.pot = f[FGPU_POTENTIAL]; s.divv = f[FGPU_DIV_V]; s.trr = f[FGPU_TAU_R_R];
+    s.tpp = f[FGPU_TAU_PHI_PHI]; s.trp = f[FGPU_TAU_R_PHI]; s.qr = f[FGPU_Q_R];
+    s.qphi = f[FGPU_Q_PHI];
+    return s;
+}
+
+static int check_launch(fgpu_engine *eng)
+{
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        eng->err = std::string("kernel launch: ") + cudaGetErrorString(e);
+        return FGPU_ERR_CUDA;
+    }
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_upload_field(fgpu_engine *eng, int field, const double *host, int rows, int cols)
+{
+    if (!eng || !host || field < 0 || field >= FGPU_FIELD_COUNT) return FGPU_ERR_BAD_ARG;
+    if (rows != field_rows(eng, field) || cols != eng->nz) {
+        eng->err = "upload_field: shape mismatch";
+        return FGPU_ERR_BAD_ARG;
+    }
+    CK(cudaMemcpyAsync(eng->field[field], host, sizeof(double) * (size_t)rows * cols,
+                       cudaMemcpyHostToDevice, eng->stream));
+    CK(cudaStreamSynchronize(eng->stream));
+    eng->cfl_valid = false;
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_download_field(fgpu_engine *eng, int field, double *host, int rows, int cols)
+{
+    if (!eng || !host || field < 0 || field >= FGPU_FIELD_COUNT) return FGPU_ERR_BAD_ARG;
+    if (rows != field_rows(eng, field) || cols != eng->nz) {
+        eng->err = "download_field: shape mismatch";
+        return FGPU_ERR_BAD_ARG;
+    }
+    CK(cudaMemcpyAsync(host, eng->field[field], sizeof(double) * (size_t)rows * cols,
+                       cudaMemcpyDeviceToHost, eng->stream));
+    CK(cudaStreamSynchronize(eng->stream));
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_set_bodies(fgpu_engine *eng, int n, const fgpu_body *bodies, double ix,
+                               double iy, double omega_frame)
+{
+    if (!eng || n < 0 || n > kMaxBodies || (n > 0 && !bodies)) return FGPU_ERR_BAD_ARG;
+    Bodies &b = eng->bodies;
+    b.n = n;
+    for (int k = 0; k < n; ++k) {
+        b.x[k] = bodies[k].x;
+        b.y[k] = bodies[k].y;
+        b.m[k] = bodies[k].mass;
+        b.rsm[k] = bodies[k].r_sm;
+        b.a[k] = bodies[k].a;
+    }
+    b.ix = ix;
+    b.iy = iy;
+    b.omega_frame = omega_frame;
+    return FGPU_OK;
+}
+
+static double beta_inv_at(const fgpu_params &p, double t)
+{
+    // thermal_relaxation, SourceEuler.cpp:645-653
+    double beta_inv = 1 / p.cooling_beta_value;
+    if (p.cooling_beta_ramp_up > 0.0) {
+        const double ramp = 1 - std::exp(-std::pow(2 * t / p.cooling_beta_ramp_up, 2));
+        beta_inv = beta_inv * ramp;
+    }
+    return beta_inv;
+}
+
+extern "C" int fgpu_init_euler(fgpu_engine *eng, double t)
+{
+    if (!eng) return FGPU_ERR_BAD_ARG;
+    Launch L = launch_of(eng);
+    State s = state_of(eng);
+    launch_derived_cfl(L, 1 | 2, s, nullptr);
+    if (eng->ph.adiabatic) {
+        // compute_heating_cooling_for_CFL, SourceEuler.cpp:1410-1450
+        launch_stress(L, s.sigma, s.vr, s.vaz, s.nu, s.divv, s.trr, s.tpp, s.trp);
+        launch_viscous(L, 0.0, beta_inv_at(eng->p, t), 2, s);
+    }
+    eng->cfl_valid = false;
+    return check_launch(eng);
+}
+
+extern "C" int fgpu_recalculate_derived(fgpu_engine *eng, double t)
+{
+    (void)t;
+    if (!eng) return FGPU_ERR_BAD_ARG;
+    Launch L = launch_of(eng);
+    launch_derived_cfl(L, 1, state_of(eng), nullptr);
+    eng->cfl_valid = false;
+    return check_launch(eng);
+}
+
+extern "C" int fgpu_condition_cfl(fgpu_engine *eng, double *dt_out)
+{
+    if (!eng || !dt_out) return FGPU_ERR_BAD_ARG;
+    if (!eng->cfl_valid) {
+        CK(cudaMemsetAsync(eng->d_dtmin, 0x7f, sizeof(unsigned long long), eng->stream));
+        launch_derived_cfl(launch_of(eng), 4, state_of(eng), eng->d_dtmin);
+        int rc = check_launch(eng);
+        if (rc) return rc;
+        eng->cfl_valid = true;
+    }
+    CK(cudaMemcpyAsync(eng->h_pinned, eng->d_dtmin, sizeof(double), cudaMemcpyDeviceToHost,
+                       eng->stream));
+    CK(cudaStreamSynchronize(eng->stream));
+    *dt_out = eng->h_pinned[0];
+    return FGPU_OK;
+}
+
+static void ghost(fgpu_engine *eng, const Launch &L)
+{
+    launch_ghost(L, eng->bc, eng->bodies.omega_frame, state_of(eng));
+}
+
+extern "C" int fgpu_apply_boundary_condition(fgpu_engine *eng, double t, double dt, int final)
+{
+    (void)t;
+    if (!eng) return FGPU_ERR_BAD_ARG;
+    Launch L = launch_of(eng);
+    if (final && eng->p.damping) {
+        launch_damping(L, eng->dm, dt, eng->damp_rings, eng->n_damp_rings, state_of(eng));
+    }
+    ghost(eng, L);
+    eng->cfl_valid = false;
+    return check_launch(eng);
+}
+
+extern "C" int fgpu_step_euler(fgpu_engine *eng, double dt, double t)
+{
+    if (!eng || !(dt > 0.0)) return FGPU_ERR_BAD_ARG;
+    Launch L = launch_of(eng);
+    const double omf = eng->bodies.omega_frame;
+    double **f = eng->field;
+    const bool adi = eng->ph.adiabatic;
+
+    // CalculateNbodyPotential (simulation.cpp:170-174)
+    launch_potential(L, eng->bodies, f[FGPU_SCALE_HEIGHT], f[FGPU_POTENTIAL]);
+    // update_with_sourceterms (simulation.cpp:190): momentum updates
+    launch_source(L, dt, omf, f[FGPU_SIGMA], f[FGPU_PRESSURE], f[FGPU_POTENTIAL],
+                  f[FGPU_V_RADIAL], f[FGPU_V_AZIMUTHAL], eng->vr_alt, eng->vaz_alt);
+    std::swap(f[FGPU_V_RADIAL], eng->vr_alt);
+    std::swap(f[FGPU_V_AZIMUTHAL], eng->vaz_alt);
+    State s = state_of(eng);
+    // compression heating + artificial viscosity (simulation.cpp:190-194)
+    if (adi || eng->ph.art_visc_sn) {
+        launch_artvisc_q(L, dt, s.sigma, s.vr, s.vaz, s.energy, s.qr, s.qphi);
+        launch_artvisc_v(L, dt, s.sigma, s.energy, s.qr, s.qphi, s.vr, s.vaz, s.cs, s.H, s.nu);
+    }
+    // viscous stress and velocity update, SubStep3 (simulation.cpp:196-203)
+    launch_stress(L, s.sigma, s.vr, s.vaz, s.nu, s.divv, s.trr, s.tpp, s.trp);
+    launch_viscous(L, dt, beta_inv_at(eng->p, t), adi ? 7 : 1, s);
+    // apply_boundary_condition(final = false) (simulation.cpp:213)
+    ghost(eng, L);
+    // Transport (simulation.cpp:215-217)
+    launch_transport_radial(L, dt, omf, eng->radial_chunk, s.sigma, s.vr, s.vaz, s.energy,
+                            eng->mom, eng->energy_alt, eng->sigma_alt);
+    launch_transport_azimuthal(L, dt, eng->az_block, eng->mom, eng->energy_alt, eng->sigma_alt,
+                               s.vaz, eng->ring_ws, eng->az_smem);
+    launch_finish(L, omf, eng->mom, eng->sigma_alt, eng->energy_alt, s.vr, eng->vr_alt,
+                  eng->vaz_alt, s.sigma, s.energy);
+    std::swap(f[FGPU_V_RADIAL], eng->vr_alt);
+    std::swap(f[FGPU_V_AZIMUTHAL], eng->vaz_alt);
+    s = state_of(eng);
+    // apply_boundary_condition(final = true) (simulation.cpp:244)
+    if (eng->p.damping) {
+        launch_damping(L, eng->dm, dt, eng->damp_rings, eng->n_damp_rings, s);
+    }
+    ghost(eng, L);
+    // recalculate_derived_disk_quantities (simulation.cpp:265) + the next CFL
+    CK(cudaMemsetAsync(eng->d_dtmin, 0x7f, sizeof(unsigned long long), eng->stream));
+    launch_derived_cfl(L, 1 | 4, s, eng->d_dtmin);
+    eng->cfl_valid = true;
+    return check_launch(eng);
+}
+
+extern "C" int fgpu_disk_on_planet_accel(fgpu_engine *eng, int k, double accel[2])
+{
+    if (!eng || !accel || k < 0 || k >= eng->bodies.n) return FGPU_ERR_BAD_ARG;
+    const Bodies &b = eng->bodies;
+    // inner/outer split at the body's distance from the origin (t_planet::get_r);
+    // the cubic smoothing radius is the same r_sm the gas feels
+    launch_disk_force(launch_of(eng), b.x[k], b.y[k], b.a[k], b.rsm[k], eng->field[FGPU_SIGMA],
+                      eng->field[FGPU_SCALE_HEIGHT], eng->partial, eng->red_out);
+    int rc = check_launch(eng);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(eng->h_pinned, eng->red_out, sizeof(double) * 5, cudaMemcpyDeviceToHost,
+                       eng->stream));
+    CK(cudaStreamSynchronize(eng->stream));
+    accel[0] = eng->h_pinned[0] + eng->h_pinned[2];
+    accel[1] = eng->h_pinned[1] + eng->h_pinned[3];
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_total_mass(fgpu_engine *eng, double *mass)
+{
+    if (!eng || !mass) return FGPU_ERR_BAD_ARG;
+    launch_disk_force(launch_of(eng), 0.0, 0.0, 0.0, 0.0, eng->field[FGPU_SIGMA],
+                      eng->field[FGPU_SCALE_HEIGHT], eng->partial, eng->red_out);
+    int rc = check_launch(eng);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(eng->h_pinned, eng->red_out, sizeof(double) * 5, cudaMemcpyDeviceToHost,
+                       eng->stream));
+    CK(cudaStreamSynchronize(eng->stream));
+    *mass = eng->h_pinned[4];
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_check_finite(fgpu_engine *eng, int *field, int *nr, int *naz)
+{
+    if (!eng) return FGPU_ERR_BAD_ARG;
+    const int fields[4] = {FGPU_SIGMA, FGPU_V_RADIAL, FGPU_V_AZIMUTHAL, FGPU_ENERGY};
+    Launch L = launch_of(eng);
+    for (int k = 0; k < 4; ++k) {
+        const int f = fields[k];
+        const size_t n = (size_t)field_rows(eng, f) * eng->nz;
+        CK(cudaMemsetAsync(eng->d_bad, 0xff, sizeof(unsigned long long), eng->stream));
+        launch_check_finite(L, eng->field[f], n, eng->d_bad);
+        CK(cudaMemcpyAsync(eng->h_pinned, eng->d_bad, sizeof(unsigned long long),
+                           cudaMemcpyDeviceToHost, eng->stream));
+        CK(cudaStreamSynchronize(eng->stream));
+        unsigned long long bad;
+        std::memcpy(&bad, eng->h_pinned, sizeof(bad));
+        if (bad != ~0ull) {
+            if (field) *field = f;
+            if (nr) *nr = (int)(bad / eng->nz);
+            if (naz) *naz = (int)(bad % eng->nz);
+            return FGPU_ERR_NONFINITE;
+        }
+    }
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_synchronize(fgpu_engine *eng)
+{
+    if (!eng) return FGPU_ERR_BAD_ARG;
+    CK(cudaStreamSynchronize(eng->stream));
+    return FGPU_OK;
+}

@@ -1,0 +1,90 @@
+// Device-side data structures shared by the GB300 hydro kernels and the C ABI.
+//
+// Layout (FargoCPT's t_polargrid, src/polargrid.h:111-133): row-major double,
+// ring-major, cell(i, j) = j + i * nz, azimuth contiguous.  Scalar grids have
+// nr rows, vector grids (v_radial, tau_r_phi) nr + 1 rows.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fgpu {
+
+constexpr int kMaxBodies = 16;
+
+// Per-ring metric tables, uploaded once (host computes them with the same
+// expressions FargoCPT's init_radialarrays uses, src/init.cpp:188-225, so the
+// device sees bit-identical values).
+struct Tables {
+    const double *Rinf, *Rsup, *Rmed, *Surf, *InvRmed, *InvSurf, *InvDiffRmed,
+        *InvDiffRsup, *InvDiffRsupRb, *InvRinf;
+    const double *RinfSq;      // pow(Rinf, 2)
+    const double *TwoOverDRa2; // 2 / (pow(Ra[i+1],2) - pow(Ra[i],2))
+    const double *OmegaK;      // calculate_omega_kepler(Rmed)
+    const double *InvOmegaK;   // 1 / calculate_omega_kepler(Rmed)
+    const double *CsIso;       // isothermal c_s per ring (SourceEuler.cpp:983-990)
+    const double *InvDxSrc;    // 2 / (dphi (Rsup + Rinf))  (SourceEuler.cpp:387)
+    const double *InvDxTheta;  // 1 / (dphi Rmed)
+    const double *EModel;      // beta-cooling disk-model energy per unit sigma
+    const double *cosj, *sinj; // cos / sin (dphi j)
+};
+
+struct Geo {
+    int nr, nz;
+    double dphi, invdphi;
+};
+
+// Physics switches and constants (a flat copy of the fgpu_params subset the
+// kernels read, plus host-precomputed products).
+struct Phys {
+    int adiabatic, art_visc_sn, dissipation, limiter_mc, fast_transport;
+    int heating_viscous, cooling_beta, beta_ref;
+    double gamma, gm1, g_gm1, sqrt_gamma, mu, alpha, constant_viscosity;
+    double C2;            // pow(ArtificialViscosityFactor, 2)
+    double rvf, hvf, cfl, inv_hc_limit, sigma_min, sigma_floor10;
+    double eps_smooth;    // ThicknessSmoothing
+    double tmin, tmax, Rgas, sigma_sb, c_light, G, Mc;
+    double c_v_inv;       // mu / R * (gamma - 1)
+    double four_C2;       // 4 * pow(C, 2)
+    double cool_const;    // 2 * 4 * sigma_sb / c (SubStep3 alpha, pre-folded order kept)
+};
+
+struct Bodies {
+    int n;
+    double x[kMaxBodies], y[kMaxBodies], m[kMaxBodies], rsm[kMaxBodies], a[kMaxBodies];
+    double ix, iy;        // indirect term
+    double omega_frame;
+};
+
+// Ghost-ring hooks of one step (FGPU_BC_* per field and side).
+struct BcSpec {
+    int sigma_in, sigma_out, energy_in, energy_out, vr_in, vr_out, vaz_in, vaz_out;
+    double vk_in, vk_out;       // compute_v_kepler(Rmed[0]) , (Rmed[nr-1])
+    double kep_in, kep_out;     // keplerian factors
+};
+
+// Damping set-up of one quantity (boundary_conditions/damping.cpp:311-752).
+struct DampQ {
+    int kind_in, kind_out;      // FGPU_DAMP_*
+    int active_in, active_out;
+    int limit_in, limit_out;    // ring limits
+    int vector;                 // uses Rinf (v_radial) instead of Rmed
+    int is_density;
+    double tau_in, tau_out;
+    double x0_zero_in;          // X0 of "zero" damping at the inner edge
+    const double *fac_in, *fac_out; // per-ring pow((r - r_lim)/(r_edge - r_lim), 2)
+};
+
+struct Damping {
+    DampQ q[4];                 // v_radial, v_azimuthal, sigma, energy
+};
+
+// Pointers of the evolved state and the work arrays of one step.
+struct State {
+    double *sigma, *vr, *vaz, *energy;        // current state
+    double *sigma0, *vr0, *vaz0, *energy0;    // reference values
+    double *cs, *H, *P, *T, *nu, *qplus, *qminus, *pot;
+    double *divv, *trr, *tpp, *trp, *qr, *qphi;
+};
+
+}  // namespace fgpu

@@ -1,0 +1,49 @@
+// Host-side launchers of the FP64 hydro kernels (kernels_fp64.cu).
+#pragma once
+
+#include "hydro.cuh"
+
+#include <stddef.h>
+
+namespace fgpu {
+
+struct Launch {
+    Geo g;
+    Tables t;
+    Phys ph;
+    cudaStream_t stream;
+    int bx;  // threads per block along the azimuth for cell kernels
+};
+
+void launch_potential(const Launch &L, const Bodies &b, const double *H, double *pot);
+void launch_source(const Launch &L, double dt, double omf, const double *S, const double *P,
+                   const double *pot, const double *vr_in, const double *vaz_in, double *vr_out,
+                   double *vaz_out);
+void launch_artvisc_q(const Launch &L, double dt, const double *S, const double *vr,
+                      const double *vaz, double *E, double *Qr, double *Qp);
+void launch_artvisc_v(const Launch &L, double dt, const double *S, const double *E,
+                      const double *Qr, const double *Qp, double *vr, double *vaz, double *cs,
+                      double *H, double *nu);
+void launch_stress(const Launch &L, const double *S, const double *vr, const double *vaz,
+                   const double *nu, double *divv, double *trr, double *tpp, double *trp);
+void launch_viscous(const Launch &L, double dt, double beta_inv, int mode, const State &s);
+void launch_ghost(const Launch &L, const BcSpec &bc, double omf, const State &s);
+void launch_transport_radial(const Launch &L, double dt, double omf, int chunk, const double *S,
+                             const double *vr, const double *vaz, const double *E,
+                             double *const mom[4], double *E_out, double *S_out);
+size_t azimuthal_smem_bytes(int nz);
+cudaError_t prepare_azimuthal(size_t smem);
+void launch_transport_azimuthal(const Launch &L, double dt, int block, double *const mom[4],
+                                double *E, double *S, const double *vaz, double *ring_ws,
+                                size_t smem);
+void launch_finish(const Launch &L, double omf, double *const mom[4], const double *S_t,
+                   const double *E_t, const double *vr_in, double *vr_out, double *vaz_out,
+                   double *S_out, double *E_out);
+void launch_damping(const Launch &L, const Damping &dm, double dt, const int *rings, int nrings,
+                    const State &s);
+void launch_derived_cfl(const Launch &L, int mode, const State &s, unsigned long long *dt_min);
+void launch_disk_force(const Launch &L, double px, double py, double pa, double rsm,
+                       const double *S, const double *H, double *partial, double *out);
+void launch_check_finite(const Launch &L, const double *x, size_t n, unsigned long long *bad);
+
+}  // namespace fgpu

@@ -1,0 +1,1182 @@
+// FP64 kernels of the GB300 hydro step.
+//
+// Each kernel restates one or more phases of FargoCPT's sim::step_Euler
+// (reference src/simulation.cpp:148-267) with the reference's expression
+// order, so the FP64 path reproduces the reference's own FP64 results to
+// round-off.  Work is fused where the fusion recomputes nothing: GB300's FP64
+// rate is low, so every FP64 operation is done once and intermediates that
+// several neighbours reuse go through HBM/L2 instead of being recomputed.
+#include "hydro.cuh"
+#include "kernels.h"
+
+#include <math.h>
+
+namespace fgpu {
+
+#define CELL(i, j) ((size_t)(i) * (size_t)nz + (size_t)(j))
+
+__device__ __forceinline__ int jnext(int j, int nz) { return j == nz - 1 ? 0 : j + 1; }
+__device__ __forceinline__ int jprev(int j, int nz) { return j == 0 ? nz - 1 : j - 1; }
+
+// van_leer_lim / MC_lim, src/TransportEuler.cpp:306-337
+__device__ __forceinline__ double flux_limiter(double a, double b, int mc)
+{
+    if (mc) {
+        double mm = 0.0;
+        if (a * b > 0.0) mm = fabs(a) < fabs(b) ? a : b;
+        const double c = 0.5 * (a + b), d = 2.0 * mm;
+        if (c * d > 0.0) return fabs(c) < fabs(d) ? c : d;
+        return 0.0;
+    }
+    if (a * b > 0.0) return 2.0 * a * b / (a + b);
+    return 0.0;
+}
+
+// assure_temperature_range, src/SourceEuler.cpp:136-202
+__device__ __forceinline__ double temperature_floor(double e, double sigma, const Phys &ph)
+{
+    const double emin = ph.tmin * sigma / ph.mu * ph.Rgas / ph.gm1;
+    const double emax = ph.tmax * sigma / ph.mu * ph.Rgas / ph.gm1;
+    if (!(e > emin)) e = emin;
+    if (!(e < emax)) e = emax;
+    return e;
+}
+
+// ---------------------------------------------------------------------------
+// CalculateNbodyPotential, src/Pframeforce.cpp:21-86
+// ---------------------------------------------------------------------------
+__global__ void k_potential(Geo g, Tables t, Phys ph, Bodies b, const double *__restrict__ H,
+                            double *__restrict__ pot)
+{
+    const int nz = g.nz;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;
+    if (j >= nz) return;
+    const double x = t.Rmed[i] * t.cosj[j];
+    const double y = t.Rmed[i] * t.sinj[j];
+    const double smooth = ph.eps_smooth * H[CELL(i, j)];
+    double acc = 0.0;
+    for (int k = 0; k < b.n; ++k) {
+        const double dx = x - b.x[k];
+        const double dy = y - b.y[k];
+        const double dist_2 = dx * dx + dy * dy;
+        const double d_sm = sqrt(dist_2 + smooth * smooth);
+        double fk = 1.0;
+        const double r_sm = b.rsm[k];
+        if (r_sm > 0.0 && d_sm < r_sm) {
+            const double q = d_sm / r_sm;
+            fk = pow(q, 4.0) - 2.0 * pow(q, 3.0) + 2.0 * q;
+        }
+        acc += -ph.G * b.m[k] / d_sm * fk;
+    }
+    acc += -b.ix * x - b.iy * y;
+    pot[CELL(i, j)] = acc;
+}
+
+// ---------------------------------------------------------------------------
+// momentum_update_radial / momentum_update_azimuthal,
+// src/SourceEuler.cpp:325-428.  Out of place: v_r needs the old v_phi.
+// ---------------------------------------------------------------------------
+__global__ void k_source(Geo g, Tables t, double dt, double omega_frame,
+                         const double *__restrict__ S, const double *__restrict__ P,
+                         const double *__restrict__ pot, const double *__restrict__ vr_in,
+                         const double *__restrict__ vaz_in, double *__restrict__ vr_out,
+                         double *__restrict__ vaz_out)
+{
+    const int nz = g.nz, nr = g.nr;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;  // 0 .. nr
+    if (j >= nz) return;
+    // v_radial rows One_no_ghost_vr (2) .. MaxMo_no_ghost_vr (nr - 1)
+    double vr = vr_in[CELL(i, j)];
+    if (i >= 2 && i < nr - 1) {
+        double gradp = 2.0 / (S[CELL(i, j)] + S[CELL(i - 1, j)]);
+        gradp *= (P[CELL(i, j)] - P[CELL(i - 1, j)]);
+        gradp *= t.InvDiffRmed[i];
+        const double gradphi = (pot[CELL(i, j)] - pot[CELL(i - 1, j)]) * t.InvDiffRmed[i];
+        const int jn = jnext(j, nz);
+        const double vsum = vaz_in[CELL(i, j)] + vaz_in[CELL(i, jn)] +
+                            vaz_in[CELL(i - 1, j)] + vaz_in[CELL(i - 1, jn)];
+        const double vt = 0.25 * vsum + t.Rinf[i] * omega_frame;
+        const double vt2 = vt * vt;
+        const double centrifugal = vt2 * t.InvRinf[i];
+        vr += dt * (-gradp - gradphi + centrifugal);
+    }
+    vr_out[CELL(i, j)] = vr;
+    if (i < nr) {
+        // v_azimuthal rows Zero_no_ghost (1) .. Max_no_ghost (nr - 1)
+        double va = vaz_in[CELL(i, j)];
+        if (i >= 1 && i < nr - 1) {
+            const int jp = jprev(j, nz);
+            const double invdx = t.InvDxSrc[i];
+            const double gradp = 2.0 / (S[CELL(i, j)] + S[CELL(i, jp)]) *
+                                 (P[CELL(i, j)] - P[CELL(i, jp)]) * invdx;
+            const double gradphi = (pot[CELL(i, j)] - pot[CELL(i, jp)]) * invdx;
+            va = va + dt * (-gradp - gradphi);
+        }
+        vaz_out[CELL(i, j)] = va;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// compression_heating (SourceEuler.cpp:459-493) and the first half of
+// update_with_artificial_viscosity_SN (artificial_viscosity.cpp:148-207):
+// q_r, q_phi and the energy update, then the temperature floor
+// (artificial_viscosity.cpp:19-21).
+// ---------------------------------------------------------------------------
+__global__ void k_artvisc_q(Geo g, Tables t, Phys ph, double dt, const double *__restrict__ S,
+                            const double *__restrict__ vr, const double *__restrict__ vaz,
+                            double *__restrict__ E, double *__restrict__ Qr,
+                            double *__restrict__ Qp)
+{
+    const int nz = g.nz, nr = g.nr;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;  // 0 .. nr - 1
+    if (j >= nz) return;
+    const int jn = jnext(j, nz);
+    const size_t c = CELL(i, j);
+    const double vr0 = vr[c], vr1 = vr[CELL(i + 1, j)];
+    const double va0 = vaz[c], va1 = vaz[CELL(i, jn)];
+    double e = 0.0;
+    if (ph.adiabatic) {
+        e = E[c];
+        if (i < nr - 1) {
+            const double div_v = (vr1 * t.Rinf[i + 1] - vr0 * t.Rinf[i]) * t.InvDiffRsupRb[i] +
+                                 (va1 - va0) * g.invdphi * t.InvRmed[i];
+            e = e * exp(-ph.gm1 * dt * div_v);
+        }
+    }
+    if (ph.art_visc_sn) {
+        const double sig = S[c];
+        const double dv_r = vr1 - vr0;
+        const double qr = dv_r < 0.0 ? ph.C2 * sig * (dv_r * dv_r) : 0.0;
+        const double dv_p = va1 - va0;
+        const double qp = dv_p < 0.0 ? ph.C2 * sig * (dv_p * dv_p) : 0.0;
+        Qr[c] = qr;
+        Qp[c] = qp;
+        if (ph.adiabatic && ph.dissipation && i >= 1 && i < nr - 1) {
+            e = e - dt * qr * dv_r * t.InvDiffRsup[i] - dt * qp * dv_p * t.InvDxTheta[i];
+        }
+    }
+    if (ph.adiabatic) {
+        if (ph.dissipation) e = temperature_floor(e, S[c], ph);
+        E[c] = e;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Second half of update_with_artificial_viscosity_SN (velocity updates,
+// artificial_viscosity.cpp:209-248) and recalculate_viscosity
+// (SourceEuler.cpp:205-223: c_s, H, nu for the ideal EOS).
+// ---------------------------------------------------------------------------
+__global__ void k_artvisc_v(Geo g, Tables t, Phys ph, double dt, const double *__restrict__ S,
+                            const double *__restrict__ E, const double *__restrict__ Qr,
+                            const double *__restrict__ Qp, double *__restrict__ vr,
+                            double *__restrict__ vaz, double *__restrict__ cs,
+                            double *__restrict__ H, double *__restrict__ nu)
+{
+    const int nz = g.nz, nr = g.nr;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;  // 0 .. nr - 1
+    if (j >= nz) return;
+    const size_t c = CELL(i, j);
+    if (ph.art_visc_sn) {
+        if (i >= 2 && i < nr - 1) {
+            vr[c] = vr[c] - dt * 2.0 / (S[c] + S[CELL(i - 1, j)]) * (Qr[c] - Qr[CELL(i - 1, j)]) *
+                                t.InvDiffRmed[i];
+        }
+        if (i >= 1 && i < nr - 1) {
+            const int jp = jprev(j, nz);
+            vaz[c] = vaz[c] - dt * 2.0 / (S[c] + S[CELL(i, jp)]) * (Qp[c] - Qp[CELL(i, jp)]) *
+                                  t.InvDxTheta[i];
+        }
+    }
+    if (ph.adiabatic) {
+        // compute_sound_speed_normal / compute_scale_height_old / update_viscosity
+        const double c_s = sqrt(ph.g_gm1 * E[c] / S[c]);
+        const double h = c_s / ph.sqrt_gamma * t.InvOmegaK[i];
+        cs[c] = c_s;
+        H[c] = h;
+        nu[c] = ph.alpha > 0 ? ph.alpha * h * c_s : ph.constant_viscosity;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// viscosity::compute_viscous_stress_tensor, src/viscosity/viscosity.cpp:139-254
+// ---------------------------------------------------------------------------
+__global__ void k_stress(Geo g, Tables t, const double *__restrict__ S, const double *__restrict__ vr,
+                         const double *__restrict__ vaz, const double *__restrict__ nu,
+                         double *__restrict__ divv, double *__restrict__ trr,
+                         double *__restrict__ tpp, double *__restrict__ trp)
+{
+    const int nz = g.nz, nr = g.nr;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;  // 0 .. nr - 1
+    if (j >= nz) return;
+    const size_t c = CELL(i, j);
+    const int jn = jnext(j, nz);
+    const double vr0 = vr[c], vr1 = vr[CELL(i + 1, j)];
+    const double va0 = vaz[c], va1 = vaz[CELL(i, jn)];
+    const double n = nu[c], sg = S[c];
+    const double dv = (vr1 * t.Rinf[i + 1] - vr0 * t.Rinf[i]) * t.InvDiffRsupRb[i] +
+                      (va1 - va0) * g.invdphi * t.InvRmed[i];
+    divv[c] = dv;
+    const double drr = (vr1 - vr0) * t.InvDiffRsup[i];
+    trr[c] = 2.0 * n * sg * (drr - 1.0 / 3.0 * dv);
+    const double dpp = (va1 - va0) * g.invdphi * t.InvRmed[i] + 0.5 * (vr1 + vr0) * t.InvRmed[i];
+    tpp[c] = 2.0 * n * sg * (dpp - 1.0 / 3.0 * dv);
+    if (i >= 1) {
+        const int jp = jprev(j, nz);
+        const double dvazirdr = (va0 * t.InvRmed[i] - vaz[CELL(i - 1, j)] * t.InvRmed[i - 1]) *
+                                t.InvDiffRmed[i];
+        const double dvrdphi = (vr0 - vr[CELL(i, jp)]) * g.invdphi;
+        const double drp = t.Rinf[i] * dvazirdr + dvrdphi * t.InvRinf[i];
+        const double n4 = 0.25 * (n + nu[CELL(i - 1, j)] + nu[CELL(i, jp)] + nu[CELL(i - 1, jp)]);
+        const double s4 = 0.25 * (sg + S[CELL(i - 1, j)] + S[CELL(i, jp)] + S[CELL(i - 1, jp)]);
+        trp[c] = n4 * s4 * drp;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// update_velocities_with_viscosity (viscosity.cpp:355-421) fused with SubStep3
+// (SourceEuler.cpp:859-954: beta cooling, viscous heating, energy update,
+// temperature floor).  mode bit 1: velocities, bit 2: heating/cooling rates,
+// bit 4: energy update (init_euler's compute_heating_cooling_for_CFL uses 2).
+// ---------------------------------------------------------------------------
+__global__ void k_viscous(Geo g, Tables t, Phys ph, double dt, double beta_inv, int mode,
+                          const double *__restrict__ S, const double *__restrict__ trr,
+                          const double *__restrict__ tpp, const double *__restrict__ trp,
+                          const double *__restrict__ divv, const double *__restrict__ nu,
+                          const double *__restrict__ H, const double *__restrict__ S0,
+                          const double *__restrict__ E0, double *__restrict__ vr,
+                          double *__restrict__ vaz, double *__restrict__ E,
+                          double *__restrict__ qplus, double *__restrict__ qminus)
+{
+    const int nz = g.nz, nr = g.nr;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;  // 0 .. nr - 1
+    if (j >= nz) return;
+    const size_t c = CELL(i, j);
+    const int jp = jprev(j, nz), jn = jnext(j, nz);
+    if (mode & 1) {
+        if (i >= 1 && i < nr - 1) {
+            const double sigma_avg = 0.5 * (S[c] + S[CELL(i, jp)]);
+            const double dVp = dt * t.InvRmed[i] / (sigma_avg) *
+                               (t.TwoOverDRa2[i] * (t.RinfSq[i + 1] * trp[CELL(i + 1, j)] -
+                                                    t.RinfSq[i] * trp[c]) +
+                                (tpp[c] - tpp[CELL(i, jp)]) * g.invdphi);
+            vaz[c] += dVp;
+        }
+        if (i >= 2 && i < nr - 1) {
+            const double sigma_avg = 0.5 * (S[c] + S[CELL(i - 1, j)]);
+            const double dVr =
+                dt / (sigma_avg)*ph.rvf * 2.0 / (t.Rmed[i] + t.Rmed[i - 1]) *
+                ((t.Rmed[i] * trr[c] - t.Rmed[i - 1] * trr[CELL(i - 1, j)]) * t.InvDiffRmed[i] +
+                 (trp[CELL(i, jn)] - trp[c]) * g.invdphi - 0.5 * (tpp[c] + tpp[CELL(i - 1, j)]));
+            vr[c] += dVr;
+        }
+    }
+    if (!(mode & 6) || !ph.adiabatic) return;
+    double qp = 0.0, qm = 0.0;
+    const double e = E[c];
+    const double sig = S[c];
+    const bool active = i >= 1 && i < nr - 1;
+    if (active) {
+        if (ph.cooling_beta) {
+            // thermal_relaxation, SourceEuler.cpp:632-690
+            double delta_E = e;
+            if (ph.beta_ref == 1) {
+                delta_E -= E0[c] / S0[c] * sig;
+            } else if (ph.beta_ref == 2) {
+                delta_E -= t.EModel[i] * sig;
+            } else if (ph.beta_ref == 3) {
+                delta_E -= ph.tmin * sig / ph.mu * ph.Rgas / ph.gm1;
+            }
+            qm = 0.0 + delta_E * t.OmegaK[i] * beta_inv;
+        }
+        if (ph.heating_viscous) {
+            // viscous_heating, SourceEuler.cpp:496-536
+            const double n = nu[c];
+            if (n != 0.0) {
+                const double tau_r_phi = 0.25 * (trp[c] + trp[CELL(i + 1, j)] + trp[CELL(i, jn)] +
+                                                 trp[CELL(i + 1, jn)]);
+                const double t_rr = trr[c], t_pp = tpp[c], d = divv[c];
+                double q = 1.0 / (2.0 * n * sig) *
+                           (t_rr * t_rr + 2 * (tau_r_phi * tau_r_phi) + t_pp * t_pp);
+                q += (2.0 / 9.0) * n * sig * (d * d);
+                q *= ph.hvf;
+                qp = 0.0 + q;
+            }
+        }
+        // radiative alpha factor, SourceEuler.cpp:905-912
+        const double x = ph.mu * ph.gm1 / (ph.Rgas * sig);
+        const double x2 = x * x;
+        const double inv_pow4 = x2 * x2;
+        const double alpha = 1.0 + 2.0 * H[c] * 4.0 * ph.sigma_sb / ph.c_light * inv_pow4 * (e * e * e);
+        qp /= alpha;
+        qm /= alpha;
+    }
+    if (mode & 4) {
+        double e_new = e;
+        if (active) {
+            e_new = e + dt * (qp - qm);
+            if (sig < ph.sigma_floor10) {
+                // TAU_EFF is zero on this path: the equilibrium energy is 0
+                qm = qp;
+                e_new = 0.0;
+            }
+        }
+        E[c] = temperature_floor(e_new, sig, ph);
+    }
+    qplus[c] = qp;
+    qminus[c] = qm;
+}
+
+// ---------------------------------------------------------------------------
+// Ghost-ring hooks of apply_boundary_condition (boundary_conditions.cpp:65-114)
+// ---------------------------------------------------------------------------
+__device__ void ghost_hook(double *x, const double *x0, int kind, int outer, int vec, int nr,
+                           int nz, int j, double vk, double kep, double rmed_edge, double omf)
+{
+    const int irad = vec ? nr : nr - 1;  // get_max_radial()
+    switch (kind) {
+    case 1:  // zero_gradient.cpp:14-90
+        if (!outer) {
+            if (vec) {
+                x[CELL(0, j)] = x[CELL(2, j)];
+                x[CELL(1, j)] = x[CELL(2, j)];
+            } else {
+                x[CELL(0, j)] = x[CELL(1, j)];
+            }
+        } else {
+            if (vec) {
+                x[CELL(irad, j)] = x[CELL(irad - 2, j)];
+                x[CELL(irad - 1, j)] = x[CELL(irad - 2, j)];
+            } else {
+                x[CELL(irad, j)] = x[CELL(irad - 1, j)];
+            }
+        }
+        break;
+    case 2:  // outflow.cpp:16-57
+        if (!outer) {
+            if (x[CELL(2, j)] > 0.0) {
+                x[CELL(1, j)] = 0.0;
+                x[CELL(0, j)] = 0.0;
+            } else {
+                x[CELL(1, j)] = x[CELL(2, j)];
+                x[CELL(0, j)] = x[CELL(2, j)];
+            }
+        } else {
+            if (x[CELL(irad - 2, j)] < 0.0) {
+                x[CELL(irad - 1, j)] = 0.0;
+                x[CELL(irad, j)] = 0.0;
+            } else {
+                x[CELL(irad - 1, j)] = x[CELL(irad - 2, j)];
+                x[CELL(irad, j)] = x[CELL(irad - 2, j)];
+            }
+        }
+        break;
+    case 3:  // reference.cpp:17-88
+        if (!outer) {
+            x[CELL(0, j)] = x0[CELL(0, j)];
+            if (vec) x[CELL(1, j)] = x0[CELL(1, j)];
+        } else {
+            x[CELL(irad, j)] = x0[CELL(irad, j)];
+            if (vec) x[CELL(irad - 1, j)] = x0[CELL(irad - 1, j)];
+        }
+        break;
+    case 4: {  // keplerian_azimuthal.cpp:18-59
+        const int i = outer ? irad : 0;
+        x[CELL(i, j)] = kep * vk - rmed_edge * omf;
+        break;
+    }
+    default:
+        break;
+    }
+}
+
+__global__ void k_ghost(Geo g, Tables t, BcSpec bc, double omf, State s)
+{
+    const int nz = g.nz, nr = g.nr;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nz) return;
+    ghost_hook(s.sigma, s.sigma0, bc.sigma_in, 0, 0, nr, nz, j, 0, 0, 0, 0);
+    ghost_hook(s.sigma, s.sigma0, bc.sigma_out, 1, 0, nr, nz, j, 0, 0, 0, 0);
+    ghost_hook(s.energy, s.energy0, bc.energy_in, 0, 0, nr, nz, j, 0, 0, 0, 0);
+    ghost_hook(s.energy, s.energy0, bc.energy_out, 1, 0, nr, nz, j, 0, 0, 0, 0);
+    ghost_hook(s.vr, s.vr0, bc.vr_in, 0, 1, nr, nz, j, 0, 0, 0, 0);
+    ghost_hook(s.vr, s.vr0, bc.vr_out, 1, 1, nr, nz, j, 0, 0, 0, 0);
+    ghost_hook(s.vaz, s.vaz0, bc.vaz_in, 0, 0, nr, nz, j, bc.vk_in, bc.kep_in, t.Rmed[0], omf);
+    ghost_hook(s.vaz, s.vaz0, bc.vaz_out, 1, 0, nr, nz, j, bc.vk_out, bc.kep_out, t.Rmed[nr - 1],
+               omf);
+}
+
+// ---------------------------------------------------------------------------
+// Radial transport, OneWindRad (TransportEuler.cpp:138-167) with
+// compute_momenta_from_velocities (:471-493), compute_star_radial (:349-406)
+// and VanLeerRadial (:545-620).  One thread sweeps one azimuth column over a
+// chunk of rings with a register window, so every interface value is formed
+// once; neighbouring chunks overlap by the 2-ring stencil halo only.
+// Quantities: 0..3 momenta, 4 energy, 5 sigma (sigma is advected last, with
+// the pre-transport sigma as the reference density).
+// ---------------------------------------------------------------------------
+struct RadWin {
+    double w[4];   // specific quantity at rings k-1 .. k+2 relative to the interface k
+    double dq[2];  // limited slope at k-1, k
+};
+
+template <int NQ>
+__device__ __forceinline__ void rad_load_ring(int i, int j, int nz, int nr, const double *S,
+                                              const double *vr, const double *vaz,
+                                              const double *E, double omf, const Tables &t,
+                                              double *q /* NQ+1: quantities, last = sigma */)
+{
+    const double sg = S[CELL(i, j)];
+    const double r = t.Rmed[i];
+    q[0] = sg * vr[CELL(i + 1, j)];
+    q[1] = sg * vr[CELL(i, j)];
+    q[2] = sg * (vaz[CELL(i, jnext(j, nz))] + r * omf) * r;
+    q[3] = sg * (vaz[CELL(i, j)] + r * omf) * r;
+    if (NQ == 5) q[4] = E[CELL(i, j)];
+    q[NQ] = sg;
+}
+
+template <int NQ>
+__global__ void k_transport_radial(Geo g, Tables t, double dt, double omf, int mc, int chunk,
+                                   const double *__restrict__ S, const double *__restrict__ vr,
+                                   const double *__restrict__ vaz, const double *__restrict__ E,
+                                   double *__restrict__ mom0, double *__restrict__ mom1,
+                                   double *__restrict__ mom2, double *__restrict__ mom3,
+                                   double *__restrict__ E_out, double *__restrict__ S_out)
+{
+    const int nz = g.nz, nr = g.nr;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nz) return;
+    const int i0 = blockIdx.y * chunk;
+    if (i0 >= nr) return;
+    const int i1 = min(i0 + chunk, nr);
+    const double dtdphi = dt * g.dphi;
+
+    // window over rings k-2 .. k+1 for the interface k: raw quantities and
+    // specific quantities (quantity / sigma)
+    double qv[4][NQ + 1];   // rings k-2, k-1, k, k+1
+    bool have[4];
+    for (int s = 0; s < 4; ++s) {
+        const int ring = i0 - 2 + s;
+        have[s] = ring >= 0 && ring < nr;
+        if (have[s]) {
+            rad_load_ring<NQ>(ring, j, nz, nr, S, vr, vaz, E, omf, t, qv[s]);
+        } else {
+            for (int q = 0; q <= NQ; ++q) qv[s][q] = 0.0;
+        }
+    }
+    // limited slope of quantity q (specific for q < NQ, sigma for q == NQ) at
+    // ring `ring` from window slots (s-1, s, s+1)
+    auto slope = [&](int s, int ring, int q) -> double {
+        if (ring <= 0 || ring >= nr - 1) return 0.0;
+        double a, b, c;
+        if (q < NQ) {
+            a = qv[s - 1][q] / qv[s - 1][NQ];
+            b = qv[s][q] / qv[s][NQ];
+            c = qv[s + 1][q] / qv[s + 1][NQ];
+        } else {
+            a = qv[s - 1][NQ];
+            b = qv[s][NQ];
+            c = qv[s + 1][NQ];
+        }
+        const double dqm = (b - a) * t.InvDiffRmed[ring];
+        const double dqp = (c - b) * t.InvDiffRmed[ring + 1];
+        return flux_limiter(dqp, dqm, mc);
+    };
+
+    double flux_prev[NQ + 1];
+    double q_prev[NQ + 1];
+    for (int k = i0; k <= i1; ++k) {
+        // interface k uses rings k-1 (slot 1) and k (slot 2); slopes need
+        // slots 0..3
+        double flux[NQ + 1];
+        if (k == 0 || k >= nr) {
+            for (int q = 0; q <= NQ; ++q) flux[q] = 0.0;
+        } else {
+            const double v = vr[CELL(k, j)];
+            // DensityStar (compute_star_radial on sigma)
+            double sstar;
+            if (v > 0.0) {
+                const double dqs = slope(1, k - 1, NQ);
+                sstar = qv[1][NQ] + (t.Rmed[k] - t.Rmed[k - 1] - v * dt) * 0.5 * dqs;
+            } else {
+                const double dqs = slope(2, k, NQ);
+                sstar = qv[2][NQ] - (t.Rmed[k + 1] - t.Rmed[k] + v * dt) * 0.5 * dqs;
+            }
+            const double base = dtdphi * t.Rinf[k];
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) {
+                double qstar;
+                if (v > 0.0) {
+                    const double dq = slope(1, k - 1, q);
+                    qstar = qv[1][q] / qv[1][NQ] + (t.Rmed[k] - t.Rmed[k - 1] - v * dt) * 0.5 * dq;
+                } else {
+                    const double dq = slope(2, k, q);
+                    qstar = qv[2][q] / qv[2][NQ] - (t.Rmed[k + 1] - t.Rmed[k] + v * dt) * 0.5 * dq;
+                }
+                flux[q] = base * qstar * sstar * v;
+            }
+            // sigma: specific quantity is exactly 1
+            flux[NQ] = base * 1.0 * sstar * v;
+        }
+        if (k > i0) {
+            const int i = k - 1;
+            const double invs = t.InvSurf[i];
+            const size_t c = CELL(i, j);
+            const double n0 = q_prev[0] + (flux_prev[0] - flux[0]) * invs;
+            const double n1 = q_prev[1] + (flux_prev[1] - flux[1]) * invs;
+            const double n2 = q_prev[2] + (flux_prev[2] - flux[2]) * invs;
+            const double n3 = q_prev[3] + (flux_prev[3] - flux[3]) * invs;
+            mom0[c] = n0;
+            mom1[c] = n1;
+            mom2[c] = n2;
+            mom3[c] = n3;
+            if (NQ == 5) E_out[c] = q_prev[4] + (flux_prev[4] - flux[4]) * invs;
+            S_out[c] = q_prev[NQ] + (flux_prev[NQ] - flux[NQ]) * invs;
+        }
+        if (k < i1) {
+            for (int q = 0; q <= NQ; ++q) {
+                flux_prev[q] = flux[q];
+                q_prev[q] = qv[2][q];
+            }
+            // shift the window by one ring
+            for (int s = 0; s < 3; ++s) {
+                have[s] = have[s + 1];
+                for (int q = 0; q <= NQ; ++q) qv[s][q] = qv[s + 1][q];
+            }
+            const int ring = k + 2;
+            have[3] = ring < nr;
+            if (have[3]) {
+                rad_load_ring<NQ>(ring, j, nz, nr, S, vr, vaz, E, omf, t, qv[3]);
+            } else {
+                for (int q = 0; q <= NQ; ++q) qv[3][q] = 0.0;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Block reductions
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_min(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Sum over the block; result valid in every thread.
+__device__ double block_sum(double v, double *red)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        double x = lane < nw ? red[lane] : 0.0;
+        x = warp_sum(x);
+        if (lane == 0) red[32] = x;
+    }
+    __syncthreads();
+    return red[32];
+}
+
+__device__ double block_min(double v, double *red)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+    v = warp_min(v);
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        double x = lane < nw ? red[lane] : 1.0e300;
+        x = warp_min(x);
+        if (lane == 0) red[32] = x;
+    }
+    __syncthreads();
+    return red[32];
+}
+
+// ---------------------------------------------------------------------------
+// Azimuthal transport with FARGO orbital advection, OneWindTheta
+// (TransportEuler.cpp:270-288): ring mean, ComputeConstantResidual (:207-236),
+// QuantitiesAdvection with the residual then the uniform velocity (:292-304,
+// ComputeStarTheta :416-466, VanLeerTheta :630-664) and AdvectSHIFT
+// (:238-268).  One CTA owns one ring; the ring's sigma, sigma*, velocity,
+// specific quantity and slopes live in shared memory (or in a per-ring global
+// workspace when the ring is too long for shared memory).
+// ---------------------------------------------------------------------------
+struct RingArrays {
+    double *S, *SS, *V, *W, *D;
+};
+
+__device__ void ring_star_theta(const double *Q, const double *V, double *D, double *QS,
+                                double dt, double dxtheta, double invdxtheta, int nz, int mc,
+                                bool uniform, double vconst)
+{
+    for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+        const int jp = j == nz - 1 ? 0 : j + 1;
+        const int jm = j == 0 ? nz - 1 : j - 1;
+        const double dqm = Q[j] - Q[jm];
+        const double dqp = Q[jp] - Q[j];
+        D[j] = 0.5 * flux_limiter(dqp, dqm, mc) * invdxtheta;
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+        const int jm = j == 0 ? nz - 1 : j - 1;
+        const double ksi = (uniform ? vconst : V[j]) * dt;
+        if (ksi > 0.0) {
+            QS[j] = Q[jm] + (dxtheta - ksi) * D[jm];
+        } else {
+            QS[j] = Q[j] - (dxtheta + ksi) * D[j];
+        }
+    }
+    __syncthreads();
+}
+
+// One QuantitiesAdvection pass over the ring (sigma is in R.S on entry and
+// is replaced by its advected value on exit).
+__device__ void ring_advection_pass(RingArrays R, double *const *qptr, int nq, size_t row,
+                                    double dt, double dxtheta, double invdxtheta, double dxrad,
+                                    double invsurf, int nz, int mc, bool uniform, double vconst)
+{
+    // DensityStar from sigma, then every quantity divided by DENSITY_INT = sigma
+    ring_star_theta(R.S, R.V, R.D, R.SS, dt, dxtheta, invdxtheta, nz, mc, uniform, vconst);
+    for (int q = 0; q < nq; ++q) {
+        double *Q = qptr[q] + row;
+        for (int j = threadIdx.x; j < nz; j += blockDim.x) R.W[j] = Q[j] / R.S[j];
+        __syncthreads();
+        // QRStar into W after slopes in D: reuse ring_star_theta with W -> W
+        for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+            const int jp = j == nz - 1 ? 0 : j + 1;
+            const int jm = j == 0 ? nz - 1 : j - 1;
+            const double dqm = R.W[j] - R.W[jm];
+            const double dqp = R.W[jp] - R.W[j];
+            R.D[j] = 0.5 * flux_limiter(dqp, dqm, mc) * invdxtheta;
+        }
+        __syncthreads();
+        double f[8];
+        int n = 0;
+        for (int j = threadIdx.x; j < nz; j += blockDim.x, ++n) {
+            const int jm = j == 0 ? nz - 1 : j - 1;
+            const double v = uniform ? vconst : R.V[j];
+            const double ksi = v * dt;
+            double qs;
+            if (ksi > 0.0) {
+                qs = R.W[jm] + (dxtheta - ksi) * R.D[jm];
+            } else {
+                qs = R.W[j] - (dxtheta + ksi) * R.D[j];
+            }
+            f[n] = dxrad * qs * R.SS[j] * v;
+        }
+        __syncthreads();
+        n = 0;
+        for (int j = threadIdx.x; j < nz; j += blockDim.x, ++n) R.W[j] = f[n];
+        __syncthreads();
+        for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+            const int jp = j == nz - 1 ? 0 : j + 1;
+            double varq = R.W[j];
+            varq -= R.W[jp];
+            Q[j] += varq * invsurf;
+        }
+        __syncthreads();
+    }
+    // sigma last: its specific quantity is exactly 1, so QRStar == 1
+    {
+        double f[8];
+        int n = 0;
+        for (int j = threadIdx.x; j < nz; j += blockDim.x, ++n) {
+            const double v = uniform ? vconst : R.V[j];
+            f[n] = dxrad * 1.0 * R.SS[j] * v;
+        }
+        __syncthreads();
+        n = 0;
+        for (int j = threadIdx.x; j < nz; j += blockDim.x, ++n) R.W[j] = f[n];
+        __syncthreads();
+        for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+            const int jp = j == nz - 1 ? 0 : j + 1;
+            double varq = R.W[j];
+            varq -= R.W[jp];
+            R.S[j] += varq * invsurf;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_transport_azimuthal(Geo g, Tables t, double dt, int mc, int fast, int nq,
+                                      const double *__restrict__ vaz, double *mom0, double *mom1,
+                                      double *mom2, double *mom3, double *E, double *S,
+                                      double *ring_ws)
+{
+    extern __shared__ double smem[];
+    __shared__ double red[33];
+    const int nz = g.nz;
+    const int i = blockIdx.x;
+    const size_t row = (size_t)i * nz;
+    double *base = ring_ws ? ring_ws + (size_t)i * 5 * nz : smem;
+    RingArrays R{base, base + nz, base + 2 * nz, base + 3 * nz, base + 4 * nz};
+
+    // compute_average_azimuthal_velocity, :174-189
+    double part = 0.0;
+    for (int j = threadIdx.x; j < nz; j += blockDim.x) part += vaz[row + j];
+    const double vmean = block_sum(part, red) / (double)nz;
+    // ComputeConstantResidual, :207-236
+    const double Ntilde = vmean * t.InvRmed[i] * dt * g.invdphi;
+    const double Nround = floor(Ntilde + 0.5);
+    const int nshift = (int)Nround;
+    const double invdt = 1.0 / dt;
+    const double vt = (Ntilde - Nround) * t.Rmed[i] * invdt * g.dphi;
+    for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+        double vres = vaz[row + j] - vmean;
+        if (!fast) vres = vt + vres;
+        R.V[j] = vres;
+        R.S[j] = S[row + j];
+    }
+    __syncthreads();
+
+    double *qptr[5] = {mom0, mom1, mom2, mom3, E};
+    const double dxtheta = g.dphi * t.Rmed[i];
+    const double invdxtheta = 1.0 / dxtheta;
+    const double dxrad = (t.Rsup[i] - t.Rinf[i]) * dt;
+    const double invsurf = t.InvSurf[i];
+    ring_advection_pass(R, qptr, nq, row, dt, dxtheta, invdxtheta, dxrad, invsurf, nz, mc, false,
+                        0.0);
+    if (fast) {
+        ring_advection_pass(R, qptr, nq, row, dt, dxtheta, invdxtheta, dxrad, invsurf, nz, mc,
+                            true, vt);
+    }
+    // AdvectSHIFT of every quantity, sigma last
+    for (int q = 0; q <= nq; ++q) {
+        double *Q = q < nq ? qptr[q] + row : nullptr;
+        if (Q) {
+            for (int j = threadIdx.x; j < nz; j += blockDim.x) R.W[j] = Q[j];
+        } else {
+            for (int j = threadIdx.x; j < nz; j += blockDim.x) R.W[j] = R.S[j];
+        }
+        __syncthreads();
+        double *out = Q ? Q : S + row;
+        for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+            int ji = j - nshift;
+            ji %= nz;
+            if (ji < 0) ji += nz;
+            out[j] = R.W[ji];
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// compute_velocities_from_momenta (TransportEuler.cpp:498-535), the sigma
+// floor (assure_minimum_value, SourceEuler.cpp:102-134) and the temperature
+// floor (Transport, TransportEuler.cpp:122-127).  Reads the transported
+// buffers, writes the new state buffers.
+// ---------------------------------------------------------------------------
+__global__ void k_finish(Geo g, Tables t, Phys ph, double omf, const double *__restrict__ mom0,
+                         const double *__restrict__ mom1, const double *__restrict__ mom2,
+                         const double *__restrict__ mom3, const double *__restrict__ S_t,
+                         const double *__restrict__ E_t, const double *__restrict__ vr_in,
+                         double *__restrict__ vr_out, double *__restrict__ vaz_out,
+                         double *__restrict__ S_out, double *__restrict__ E_out)
+{
+    const int nz = g.nz, nr = g.nr;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;  // 0 .. nr
+    if (j >= nz) return;
+    const size_t c = CELL(i, j);
+    if (i == nr) {
+        vr_out[c] = vr_in[c];
+        return;
+    }
+    const double s = S_t[c];
+    if (i == 0) {
+        vr_out[c] = 0.0;
+    } else {
+        const size_t cm = CELL(i - 1, j);
+        vr_out[c] = (mom0[cm] + mom1[c]) / (S_t[cm] + s);
+    }
+    const int jm = jprev(j, nz);
+    const size_t cjm = CELL(i, jm);
+    vaz_out[c] = (mom2[cjm] + mom3[c]) / (S_t[cjm] + s) * t.InvRmed[i] - t.Rmed[i] * omf;
+    const double sf = s < ph.sigma_min ? ph.sigma_min : s;
+    S_out[c] = sf;
+    if (ph.adiabatic) E_out[c] = temperature_floor(E_t[c], sf, ph);
+}
+
+// ---------------------------------------------------------------------------
+// damping (boundary_conditions/damping.cpp:311-752, :754-776): one CTA per
+// ring of the damping zones; the "mean" kind writes X0(ring, 0) like the
+// reference does.
+// ---------------------------------------------------------------------------
+__device__ void damp_ring(double *X, double *X0, const DampQ &d, int i, int nz, int outer,
+                          double dt, double *red)
+{
+    const int kind = outer ? d.kind_out : d.kind_in;
+    const size_t row = (size_t)i * nz;
+    double x0c = 0.0;
+    if (kind == 3) {
+        double part = 0.0;
+        for (int j = threadIdx.x; j < nz; j += blockDim.x) part += X[row + j];
+        const double mean = block_sum(part, red) / nz;
+        if (threadIdx.x == 0) X0[row] = mean;
+        x0c = mean;
+    } else if (kind == 2) {
+        x0c = outer ? 0.0 : d.x0_zero_in;
+    }
+    const double factor = outer ? d.fac_out[i] : d.fac_in[i];
+    const double tau = outer ? d.tau_out : d.tau_in;
+    const double ef = exp(-dt * factor / tau);
+    for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+        const double x0 = kind == 1 ? X0[row + j] : x0c;
+        X[row + j] = (X[row + j] - x0) * ef + x0;
+    }
+    __syncthreads();
+}
+
+__global__ void k_damping(Geo g, Damping dm, double dt, const int *__restrict__ rings,
+                          State s)
+{
+    __shared__ double red[33];
+    const int nz = g.nz, nr = g.nr;
+    const int i = rings[blockIdx.x];
+    double *X[4] = {s.vr, s.vaz, s.sigma, s.energy};
+    double *X0[4] = {s.vr0, s.vaz0, s.sigma0, s.energy0};
+    for (int q = 0; q < 4; ++q) {
+        const DampQ &d = dm.q[q];
+        const int size = d.vector ? nr + 1 : nr;
+        if (d.kind_in != 0 && d.active_in && i <= d.limit_in) {
+            damp_ring(X[q], X0[q], d, i, nz, 0, dt, red);
+        }
+        if (d.kind_out != 0 && d.active_out && i >= d.limit_out && i < size) {
+            damp_ring(X[q], X0[q], d, i, nz, 1, dt, red);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// recalculate_derived_disk_quantities (SourceEuler.cpp:225-249) fused with
+// cfl::condition_cfl (cfl.cpp:185-382).  One CTA per ring; the ring means of
+// v_phi for rings i and i + 1 are block reductions; the step minimum is an
+// atomic min on the ordered bit pattern of the (positive) dt.
+// mode bit 1: derived quantities (bit 2: include T, c_s, H for init),
+// bit 4: CFL.
+// ---------------------------------------------------------------------------
+__global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const double *__restrict__ S,
+                              const double *__restrict__ E, const double *__restrict__ vr,
+                              const double *__restrict__ vaz, const double *__restrict__ qplus,
+                              const double *__restrict__ qminus, double *__restrict__ cs,
+                              double *__restrict__ H, double *__restrict__ P,
+                              double *__restrict__ T, double *__restrict__ nu,
+                              unsigned long long *__restrict__ dt_min)
+{
+    __shared__ double red[33];
+    const int nz = g.nz, nr = g.nr;
+    const int i = blockIdx.x;
+    const size_t row = (size_t)i * nz;
+    const bool do_cfl = (mode & 4) != 0;
+    double vm0 = 0.0, vm1 = 0.0;
+    if (do_cfl && i < nr - 1) {
+        double p0 = 0.0, p1 = 0.0;
+        for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+            p0 += vaz[row + j];
+            p1 += vaz[row + nz + j];
+        }
+        vm0 = block_sum(p0, red) / (double)nz;
+        vm1 = block_sum(p1, red) / (double)nz;
+    }
+    const double dxR = t.Rsup[i] - t.Rinf[i];
+    const double dxA = t.Rmed[i] * g.dphi;
+    const double cell = dxR < dxA ? dxR : dxA;
+    double local = 1.0e300;
+    if (do_cfl && i == 0) {
+        const double denom = fabs(vm0 * t.InvRmed[0] - vm1 * t.InvRmed[1]) + 1.0e-100;
+        local = ph.cfl * g.dphi / denom;
+    }
+    const bool cfl_ring = do_cfl && i >= 1 && i < nr - 1;
+    if (cfl_ring) {
+        const double denom = fabs(vm0 * t.InvRmed[i] - vm1 * t.InvRmed[i + 1]) + 1.0e-100;
+        local = ph.cfl * g.dphi / denom;
+    }
+    for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+        const size_t c = row + j;
+        double c_s, n;
+        if (mode & 1) {
+            const double sg = S[c];
+            if (ph.adiabatic) {
+                const double e = E[c];
+                T[c] = ph.c_v_inv * e / sg;
+                c_s = sqrt(ph.g_gm1 * e / sg);
+                const double h = c_s / ph.sqrt_gamma * t.InvOmegaK[i];
+                cs[c] = c_s;
+                H[c] = h;
+                P[c] = ph.gm1 * e;
+                n = ph.alpha > 0 ? ph.alpha * h * c_s : ph.constant_viscosity;
+            } else {
+                c_s = t.CsIso[i];
+                const double h = c_s * t.InvOmegaK[i];
+                P[c] = sg * (c_s * c_s);
+                if (mode & 2) {
+                    cs[c] = c_s;
+                    H[c] = h;
+                    T[c] = ph.mu / ph.Rgas * P[c] / sg;
+                }
+                n = ph.alpha > 0 ? ph.alpha * h * c_s : ph.constant_viscosity;
+            }
+            nu[c] = n;
+        } else {
+            c_s = cs[c];
+            n = nu[c];
+        }
+        if (cfl_ring) {
+            const double va = vaz[c];
+            const double vres = ph.fast_transport ? va - vm0 : va;
+            const double invdt1 = c_s / cell;
+            const double invdt2 = vr[c] / dxR;
+            const double invdt3 = vres / dxA;
+            const double vr1 = vr[c + nz];
+            const double va1 = vaz[row + (j == nz - 1 ? 0 : j + 1)];
+            double invdt4;
+            if (sn) {
+                double dvR = vr1 - vr[c];
+                double dvA = va1 - va;
+                dvR = dvR > 0.0 ? 0.0 : -dvR;
+                dvA = dvA > 0.0 ? 0.0 : -dvA;
+                const double a = dvR / dxR, b = dvA / dxA;
+                invdt4 = ph.four_C2 * (a > b ? a : b);
+            } else {
+                const double eps_rr = (vr1 - vr[c]) * t.InvDiffRsup[i];
+                const double eps_pp = t.InvRmed[i] * ((va1 - va) * g.invdphi + 0.5 * (vr1 + vr[c]));
+                const double d = eps_rr + eps_pp;
+                const double mdiv = -(d < 0.0 ? d : 0.0);
+                invdt4 = ph.four_C2 * mdiv;
+            }
+            const double invdt5 = 4.0 * n / (cell * cell);
+            double invdt6 = 0.0;
+            if (ph.adiabatic) {
+                invdt6 = ph.inv_hc_limit * fabs((qplus[c] - qminus[c]) / E[c]);
+            }
+            const double dt_cell =
+                ph.cfl / sqrt(invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 +
+                              invdt4 * invdt4 + invdt5 * invdt5 + invdt6 * invdt6);
+            local = fmin(local, dt_cell);
+        }
+    }
+    if (do_cfl) {
+        const double m = block_min(local, red);
+        if (threadIdx.x == 0 && m < 1.0e300) {
+            atomicMin(dt_min, (unsigned long long)__double_as_longlong(m));
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// ComputeDiskOnPlanetAccel (src/Force.cpp:23-122) with CorrectDiskSelfgravity
+// (the ring mean of sigma subtracted, Pframeforce.cpp:175-190), and
+// gas_total_mass (quantities.cpp:51-74).  One CTA per active ring writes its
+// partial sums; k_reduce_rows adds them in ring order with compensation.
+// ---------------------------------------------------------------------------
+__global__ void k_disk_force(Geo g, Tables t, Phys ph, double px, double py, double pa,
+                             double rsm, const double *__restrict__ S,
+                             const double *__restrict__ H, double *__restrict__ partial)
+{
+    __shared__ double red[33];
+    const int nz = g.nz;
+    const int i = blockIdx.x + 1;  // radial_first_active .. radial_active_size - 1
+    const size_t row = (size_t)i * nz;
+    double ps = 0.0;
+    for (int j = threadIdx.x; j < nz; j += blockDim.x) ps += S[row + j];
+    const double sigma1d = block_sum(ps, red) / nz;
+    double ax = 0.0, ay = 0.0, mass = 0.0;
+    for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+        const double smooth = ph.eps_smooth * H[row + j];
+        const double xc = t.Rmed[i] * t.cosj[j];
+        const double yc = t.Rmed[i] * t.sinj[j];
+        const double cellmass = t.Surf[i] * (S[row + j] - sigma1d);
+        const double dx = xc - px, dy = yc - py;
+        const double d2 = dx * dx + dy * dy;
+        const double dsm2 = d2 + smooth * smooth;
+        const double dsm = sqrt(dsm2);
+        const double inv3 = 1.0 / (dsm2 * dsm);
+        double fk = 1.0;
+        if (rsm > 0.0 && dsm < rsm) {
+            const double q = dsm / rsm;
+            fk = -(3.0 * pow(q, 4.0) - 4.0 * pow(q, 3.0));
+        }
+        ax += ph.G * cellmass * dx * inv3 * fk;
+        ay += ph.G * cellmass * dy * inv3 * fk;
+        mass += t.Surf[i] * S[row + j];
+    }
+    ax = block_sum(ax, red);
+    ay = block_sum(ay, red);
+    mass = block_sum(mass, red);
+    if (threadIdx.x == 0) {
+        const bool inner = t.Rmed[i] < pa;
+        double *p = partial + (size_t)blockIdx.x * 5;
+        p[0] = inner ? ax : 0.0;
+        p[1] = inner ? ay : 0.0;
+        p[2] = inner ? 0.0 : ax;
+        p[3] = inner ? 0.0 : ay;
+        p[4] = mass;
+    }
+}
+
+// Kahan-compensated sum of `rows` records of `width` doubles, in order.
+__global__ void k_reduce_rows(const double *__restrict__ partial, int rows, int width,
+                              double *__restrict__ out)
+{
+    const int w = threadIdx.x;
+    if (w >= width) return;
+    double s = 0.0, comp = 0.0;
+    for (int r = 0; r < rows; ++r) {
+        const double y = partial[(size_t)r * width + w] - comp;
+        const double tt = s + y;
+        comp = (tt - s) - y;
+        s = tt;
+    }
+    out[w] = s;
+}
+
+// NaN/Inf scan of one field: records the first bad flat index (atomicMin).
+__global__ void k_check_finite(const double *__restrict__ x, size_t n, unsigned long long *bad)
+{
+    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n && !isfinite(x[k])) atomicMin(bad, (unsigned long long)k);
+}
+
+// ---------------------------------------------------------------------------
+// host-side launchers
+// ---------------------------------------------------------------------------
+static inline dim3 grid2d(int nz, int rows, int bx) { return dim3((nz + bx - 1) / bx, rows); }
+
+void launch_potential(const Launch &L, const Bodies &b, const double *H, double *pot)
+{
+    k_potential<<<grid2d(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(L.g, L.t, L.ph, b, H, pot);
+}
+
+void launch_source(const Launch &L, double dt, double omf, const double *S, const double *P,
+                   const double *pot, const double *vr_in, const double *vaz_in, double *vr_out,
+                   double *vaz_out)
+{
+    k_source<<<grid2d(L.g.nz, L.g.nr + 1, L.bx), L.bx, 0, L.stream>>>(
+        L.g, L.t, dt, omf, S, P, pot, vr_in, vaz_in, vr_out, vaz_out);
+}
+
+void launch_artvisc_q(const Launch &L, double dt, const double *S, const double *vr,
+                      const double *vaz, double *E, double *Qr, double *Qp)
+{
+    k_artvisc_q<<<grid2d(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(L.g, L.t, L.ph, dt, S, vr,
+                                                                      vaz, E, Qr, Qp);
+}
+
+void launch_artvisc_v(const Launch &L, double dt, const double *S, const double *E,
+                      const double *Qr, const double *Qp, double *vr, double *vaz, double *cs,
+                      double *H, double *nu)
+{
+    k_artvisc_v<<<grid2d(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(L.g, L.t, L.ph, dt, S, E, Qr,
+                                                                      Qp, vr, vaz, cs, H, nu);
+}
+
+void launch_stress(const Launch &L, const double *S, const double *vr, const double *vaz,
+                   const double *nu, double *divv, double *trr, double *tpp, double *trp)
+{
+    k_stress<<<grid2d(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(L.g, L.t, S, vr, vaz, nu, divv,
+                                                                   trr, tpp, trp);
+}
+
+void launch_viscous(const Launch &L, double dt, double beta_inv, int mode, const State &s)
+{
+    k_viscous<<<grid2d(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(
+        L.g, L.t, L.ph, dt, beta_inv, mode, s.sigma, s.trr, s.tpp, s.trp, s.divv, s.nu, s.H,
+        s.sigma0, s.energy0, s.vr, s.vaz, s.energy, s.qplus, s.qminus);
+}
+
+void launch_ghost(const Launch &L, const BcSpec &bc, double omf, const State &s)
+{
+    k_ghost<<<(L.g.nz + 127) / 128, 128, 0, L.stream>>>(L.g, L.t, bc, omf, s);
+}
+
+void launch_transport_radial(const Launch &L, double dt, double omf, int chunk, const double *S,
+                             const double *vr, const double *vaz, const double *E,
+                             double *const mom[4], double *E_out, double *S_out)
+{
+    const int chunks = (L.g.nr + chunk - 1) / chunk;
+    const int bx = 64;
+    dim3 grid((L.g.nz + bx - 1) / bx, chunks);
+    if (L.ph.adiabatic) {
+        k_transport_radial<5><<<grid, bx, 0, L.stream>>>(L.g, L.t, dt, omf, L.ph.limiter_mc, chunk,
+                                                         S, vr, vaz, E, mom[0], mom[1], mom[2],
+                                                         mom[3], E_out, S_out);
+    } else {
+        k_transport_radial<4><<<grid, bx, 0, L.stream>>>(L.g, L.t, dt, omf, L.ph.limiter_mc, chunk,
+                                                         S, vr, vaz, E, mom[0], mom[1], mom[2],
+                                                         mom[3], E_out, S_out);
+    }
+}
+
+size_t azimuthal_smem_bytes(int nz) { return (size_t)5 * nz * sizeof(double); }
+
+cudaError_t prepare_azimuthal(size_t smem)
+{
+    return cudaFuncSetAttribute(k_transport_azimuthal,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+void launch_transport_azimuthal(const Launch &L, double dt, int block, double *const mom[4],
+                                double *E, double *S, const double *vaz, double *ring_ws,
+                                size_t smem)
+{
+    const int nq = L.ph.adiabatic ? 5 : 4;
+    k_transport_azimuthal<<<L.g.nr, block, ring_ws ? 0 : smem, L.stream>>>(
+        L.g, L.t, dt, L.ph.limiter_mc, L.ph.fast_transport, nq, vaz, mom[0], mom[1], mom[2],
+        mom[3], E, S, ring_ws);
+}
+
+void launch_finish(const Launch &L, double omf, double *const mom[4], const double *S_t,
+                   const double *E_t, const double *vr_in, double *vr_out, double *vaz_out,
+                   double *S_out, double *E_out)
+{
+    k_finish<<<grid2d(L.g.nz, L.g.nr + 1, L.bx), L.bx, 0, L.stream>>>(
+        L.g, L.t, L.ph, omf, mom[0], mom[1], mom[2], mom[3], S_t, E_t, vr_in, vr_out, vaz_out,
+        S_out, E_out);
+}
+
+void launch_damping(const Launch &L, const Damping &dm, double dt, const int *rings, int nrings,
+                    const State &s)
+{
+    if (nrings <= 0) return;
+    k_damping<<<nrings, 256, 0, L.stream>>>(L.g, dm, dt, rings, s);
+}
+
+void launch_derived_cfl(const Launch &L, int mode, const State &s, unsigned long long *dt_min)
+{
+    k_derived_cfl<<<L.g.nr, 256, 0, L.stream>>>(L.g, L.t, L.ph, mode, L.ph.art_visc_sn, s.sigma,
+                                                s.energy, s.vr, s.vaz, s.qplus, s.qminus, s.cs,
+                                                s.H, s.P, s.T, s.nu, dt_min);
+}
+
+void launch_disk_force(const Launch &L, double px, double py, double pa, double rsm,
+                       const double *S, const double *H, double *partial, double *out)
+{
+    const int rows = L.g.nr - 2;
+    k_disk_force<<<rows, 256, 0, L.stream>>>(L.g, L.t, L.ph, px, py, pa, rsm, S, H, partial);
+    k_reduce_rows<<<1, 32, 0, L.stream>>>(partial, rows, 5, out);
+}
+
+void launch_check_finite(const Launch &L, const double *x, size_t n, unsigned long long *bad)
+{
+    const int bx = 256;
+    k_check_finite<<<(unsigned)((n + bx - 1) / bx), bx, 0, L.stream>>>(x, n, bad);
+}
+
+}  // namespace fgpu

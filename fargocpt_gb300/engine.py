@@ -1,0 +1,141 @@
+"""Python front end of the GB300 engine's C ABI.
+
+Method names follow FargoCPT's hydro functions (reference src/SourceEuler.h,
+src/TransportEuler.h, src/cfl.h, src/Force.h) so that a run loop written
+against the reference's call sequence drives the engine unchanged.  Every
+call goes through libfargocpt_gb300.so; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from .abi import (FIELDS, STATUS_NAMES, VECTOR_FIELDS, FgpuBody, FgpuParams,
+                  load_library)
+
+
+class EngineError(RuntimeError):
+    pass
+
+
+def grid_radii(spacing: int, rmin: float, rmax: float, nrad: int) -> np.ndarray:
+    """FargoCPT's Radii[0 .. nrad+1] (init.cpp:93-110), computed by the library."""
+    lib = load_library()
+    out = np.empty(nrad + 2, dtype=np.float64)
+    rc = lib.fgpu_grid_radii(spacing, rmin, rmax, nrad, out.ctypes.data_as(C.POINTER(C.c_double)))
+    if rc != 0:
+        raise EngineError(f"fgpu_grid_radii: {STATUS_NAMES.get(rc, rc)}")
+    return out
+
+
+class Engine:
+    """One disk resident in HBM.  Not thread-safe; all work on one stream."""
+
+    def __init__(self, params: FgpuParams, radii):
+        self.lib = load_library()
+        self.params = params
+        self.nr, self.nz = params.nrad, params.naz
+        r = np.ascontiguousarray(radii, dtype=np.float64)
+        if r.size < self.nr + 2:
+            raise ValueError("radii must hold nrad + 2 values")
+        self._radii = r
+        h = C.c_void_p()
+        rc = self.lib.fgpu_create(C.byref(params), r.ctypes.data_as(C.POINTER(C.c_double)),
+                                  C.byref(h))
+        if rc != 0:
+            raise EngineError(f"fgpu_create: {STATUS_NAMES.get(rc, rc)}")
+        self.h = h
+
+    # -- lifetime -----------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc != 0:
+            msg = self.lib.fgpu_last_error(self.h)
+            raise EngineError(f"{what}: {STATUS_NAMES.get(rc, rc)}: "
+                              f"{msg.decode() if msg else ''}")
+
+    @property
+    def stream(self) -> int:
+        p = C.c_void_p()
+        self._check(self.lib.fgpu_get_stream(self.h, C.byref(p)), "fgpu_get_stream")
+        return p.value or 0
+
+    # -- fields -------------------------------------------------------------
+    def rows(self, name):
+        return self.nr + 1 if name in VECTOR_FIELDS else self.nr
+
+    def set_field(self, name, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        if a.shape != (self.rows(name), self.nz):
+            raise ValueError(f"{name}: shape {a.shape} != {(self.rows(name), self.nz)}")
+        self._check(self.lib.fgpu_upload_field(self.h, FIELDS[name],
+                                               a.ctypes.data_as(C.POINTER(C.c_double)),
+                                               a.shape[0], a.shape[1]), f"upload {name}")
+
+    def get_field(self, name):
+        a = np.empty((self.rows(name), self.nz), dtype=np.float64)
+        self._check(self.lib.fgpu_download_field(self.h, FIELDS[name],
+                                                 a.ctypes.data_as(C.POINTER(C.c_double)),
+                                                 a.shape[0], a.shape[1]), f"download {name}")
+        return a
+
+    # -- per-step host state ------------------------------------------------
+    def set_bodies(self, bodies, ix, iy, omega_frame=0.0):
+        arr = (FgpuBody * max(1, len(bodies)))()
+        for k, b in enumerate(bodies):
+            vals = list(b) + [0.0] * (5 - len(b))
+            arr[k] = FgpuBody(*vals)
+        self._check(self.lib.fgpu_set_bodies(self.h, len(bodies), arr, ix, iy, omega_frame),
+                    "fgpu_set_bodies")
+
+    # -- hydro functions ----------------------------------------------------
+    def init_euler(self, t):
+        self._check(self.lib.fgpu_init_euler(self.h, t), "fgpu_init_euler")
+
+    def recalculate_derived(self, t):
+        self._check(self.lib.fgpu_recalculate_derived(self.h, t), "fgpu_recalculate_derived")
+
+    def condition_cfl(self) -> float:
+        out = C.c_double()
+        self._check(self.lib.fgpu_condition_cfl(self.h, C.byref(out)), "fgpu_condition_cfl")
+        return out.value
+
+    def apply_boundary_condition(self, t, dt, final):
+        self._check(self.lib.fgpu_apply_boundary_condition(self.h, t, dt, 1 if final else 0),
+                    "fgpu_apply_boundary_condition")
+
+    def step_euler(self, dt, t):
+        self._check(self.lib.fgpu_step_euler(self.h, dt, t), "fgpu_step_euler")
+
+    def disk_on_planet_accel(self, k):
+        out = (C.c_double * 2)()
+        self._check(self.lib.fgpu_disk_on_planet_accel(self.h, k, out),
+                    "fgpu_disk_on_planet_accel")
+        return out[0], out[1]
+
+    def total_mass(self):
+        out = C.c_double()
+        self._check(self.lib.fgpu_total_mass(self.h, C.byref(out)), "fgpu_total_mass")
+        return out.value
+
+    def check_finite(self):
+        f, i, j = C.c_int(), C.c_int(), C.c_int()
+        rc = self.lib.fgpu_check_finite(self.h, C.byref(f), C.byref(i), C.byref(j))
+        if rc == -5:
+            return (f.value, i.value, j.value)
+        self._check(rc, "fgpu_check_finite")
+        return None
+
+    def synchronize(self):
+        self._check(self.lib.fgpu_synchronize(self.h), "fgpu_synchronize")

@@ -1,0 +1,80 @@
+"""The C-ABI library without a GPU: it loads, exports every symbol of
+include/fargocpt_gb300.h, computes the reference's radii on the host, and
+reports a missing device instead of falling back to the CPU."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from fargocpt_gb300 import abi
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_symbols():
+    text = open(os.path.join(REPO, "include", "fargocpt_gb300.h")).read()
+    return sorted(set(re.findall(r"\b(fgpu_[a-z_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(abi.LIB_PATH):
+        from fargocpt_gb300.build import build
+        build()
+    return abi.load_library()
+
+
+def test_exports_every_declared_symbol(lib):
+    declared = _declared_symbols()
+    assert set(declared) == set(abi.EXPORTED_SYMBOLS)
+    for name in declared:
+        assert hasattr(lib, name), name
+
+
+def test_grid_radii_matches_reference_formula(lib):
+    from golden_runner import load_case
+    meta, arrays = load_case("iso_planet_fixed_dt")
+    p = meta["params"]
+    out = np.empty(p["nrad"] + 2)
+    rc = lib.fgpu_grid_radii(1, p["rmin"], p["rmax"], p["nrad"],
+                             out.ctypes.data_as(C.POINTER(C.c_double)))
+    assert rc == 0
+    assert np.array_equal(out, arrays["radii"])
+
+
+def test_bad_arguments_are_rejected(lib):
+    out = np.empty(8)
+    assert lib.fgpu_grid_radii(7, 0.4, 2.5, 6, out.ctypes.data_as(C.POINTER(C.c_double))) == -1
+    assert lib.fgpu_grid_radii(1, 2.5, 0.4, 6, out.ctypes.data_as(C.POINTER(C.c_double))) == -1
+    h = C.c_void_p()
+    p = abi.FgpuParams()
+    p.nrad, p.naz = 3, 8
+    assert lib.fgpu_create(C.byref(p), out.ctypes.data_as(C.POINTER(C.c_double)), C.byref(h)) == -1
+    assert lib.fgpu_destroy(None) == -1
+
+
+def test_unsupported_options_are_reported(lib):
+    from gpu_cases import make_params
+    out = np.zeros(40)
+    h = C.c_void_p()
+    p, _ = make_params(16, 32, art_visc=abi.ARTVISC_TW)
+    assert lib.fgpu_create(C.byref(p), out.ctypes.data_as(C.POINTER(C.c_double)), C.byref(h)) == -4
+    p, _ = make_params(16, 9000)
+    assert lib.fgpu_create(C.byref(p), out.ctypes.data_as(C.POINTER(C.c_double)), C.byref(h)) == -4
+
+
+def test_no_device_is_an_error_not_a_fallback(lib):
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    from gpu_cases import make_params
+    p, d = make_params(16, 32)
+    radii = np.linspace(0.4, 2.5, 18)
+    h = C.c_void_p()
+    rc = lib.fgpu_create(C.byref(p), radii.ctypes.data_as(C.POINTER(C.c_double)), C.byref(h))
+    assert rc == -6
