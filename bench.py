@@ -1,0 +1,317 @@
+"""Benchmark of the GB300 hydro step: cell-updates/s on FargoCPT's adiabatic
+disk (512 x 1536, the configuration the metric is quoted on).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config c2]
+    python bench.py --impl reference ...     # the CPU restatement, all host cores
+
+One step = one FargoCPT Euler hydro step (sim::step_Euler's gas part plus the
+CFL dt for the next step) over the whole disk.  value: device time of the
+steps (CUDA events on the engine's stream, L2 flushed before every timed step,
+fields resident in HBM).  e2e: wall time of the drop-in call sequence a C++
+driver makes every step through the C ABI (CFL read-back, N-body state in,
+step, disk force on the planet read back).  Multi-GPU runs are independent
+replicas (the path does not shard across GPUs here).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+# Compulsory HBM bytes per cell of each kernel of the FP64 adiabatic step
+# (unique fields read + written, 8 B each); see the design doc.
+KERNEL_BYTES_PER_CELL = {
+    "potential": 16, "source": 56, "artvisc_q": 56, "artvisc_v": 88, "stress": 64,
+    "viscous_substep3": 120, "ghost_pre": 0, "transport_radial": 80,
+    "transport_azimuthal": 104, "finish": 80, "damping": 0, "ghost_post": 0,
+    "derived_cfl": 88,
+}
+STEP_BYTES_PER_CELL = {"adiabatic": 64, "isothermal": 48}   # one read + write of the state
+KERNELS_PER_STEP = 15   # 13 step kernels + 2 disk-force kernels
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--config", default="c2")
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+def peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            m = json.load(f)
+        return float(m["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.rows, self.proc = [], None
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            if len(r) >= 9:
+                for k, n in enumerate(names):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.rows)}
+
+
+def load_disk(backend, fields, nbody):
+    for k, a in fields.items():
+        backend.set_field(k, a)
+        backend.set_field(k + "0", a)
+    b = nbody.bodies(0.0)
+    ix, iy = nbody.indirect(b)
+    backend.set_bodies(b, ix, iy, 0.0)
+    backend.init_euler(0.0)
+    backend.apply_boundary_condition(0.0, 0.0, False)
+
+
+def cpu_baseline(cfg_name, seconds, threads=None):
+    """The oracle (CPU restatement of the reference's step) on this host's
+    cores over a bounded sample of the same workload."""
+    from fargocpt_gb300 import setups
+    from oracle.oracle_py import OracleState, build_oracle, set_threads
+
+    build_oracle()
+    cores = set_threads(threads or os.cpu_count() or 1)
+    params, d, radii, fields, nbody = setups.build(cfg_name)
+    o = OracleState(params, radii)
+    load_disk(o, fields, nbody)
+    cells = d["nrad"] * d["naz"]
+    t, steps, t0 = 0.0, 0, time.perf_counter()
+    while True:
+        dt = o.condition_cfl()
+        b = nbody.bodies(t)
+        ix, iy = nbody.indirect(b)
+        o.set_bodies(b, ix, iy, 0.0)
+        o.step_euler(dt, t)
+        o.disk_on_planet_accel(1)
+        t += dt
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds and steps >= 2:
+            break
+    return {"value": cells * steps / el, "unit": "cell-updates/s", "cores": cores,
+            "kind": "port", "sample": f"{steps} full steps of {cfg_name} "
+            f"({d['nrad']}x{d['naz']}) in {el:.1f} s"}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    cb = cpu_baseline(args.config, args.cpu_seconds)
+    from fargocpt_gb300 import setups
+    c = setups.CONFIGS[args.config]
+    line = {
+        "impl": "reference", "metric": "cell-updates/s/GPU, plain FP64 vs mixed-precision "
+        "& batched at stated error", "value": cb["value"], "unit": cb["unit"],
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": c["nrad"] * c["naz"] / cb["value"] * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(args.config),
+        "cpu_baseline": cb,
+        "e2e": {"value": cb["value"], "unit": cb["unit"], "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def workload_config(name):
+    from fargocpt_gb300 import setups
+    c = setups.CONFIGS[name]
+    return {"workload": f"FargoCPT {'adiabatic' if c['adiabatic'] else 'locally isothermal'} "
+            f"disk {c['nrad']}x{c['naz']} (incl. 2 ghost rings), r in [{c['rmin']}, {c['rmax']}], "
+            f"{len(c['planets'])} planet(s), FARGO, SN art. visc, alpha=1e-3"
+            + (", beta cooling 10" if c["adiabatic"] else "") + ", FP64",
+            "nrad": c["nrad"], "naz": c["naz"], "precision": "fp64",
+            "l2": "flushed (256 MB write) before every timed step"}
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if args.impl == "gb300" else "gloo")
+    if args.impl == "reference":
+        run_reference(args, rank)
+        if dist is not None:
+            dist.barrier()
+        return
+
+    import numpy as np
+    import torch
+
+    from fargocpt_gb300.build import build
+    if rank == 0:
+        build()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.set_device(local)
+    from fargocpt_gb300 import setups
+    from fargocpt_gb300.engine import Engine
+
+    params, d, radii, fields, nbody = setups.build(args.config)
+    eng = Engine(params, radii)
+    load_disk(eng, fields, nbody)
+    cells = d["nrad"] * d["naz"]
+    stream = torch.cuda.ExternalStream(eng.stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    t = 0.0
+
+    def one_step(timed_events=None):
+        nonlocal t
+        dt = eng.condition_cfl()
+        b = nbody.bodies(t)
+        ix, iy = nbody.indirect(b)
+        eng.set_bodies(b, ix, iy, 0.0)
+        if timed_events is not None:
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                timed_events[0].record(stream)
+        eng.step_euler(dt, t)
+        if timed_events is not None:
+            timed_events[1].record(stream)
+        eng.disk_on_planet_accel(1)
+        t += dt
+
+    for _ in range(args.warmup):
+        one_step()
+    eng.synchronize()
+
+    # device time of the steps, L2 flushed before each
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    sampler = ClockSampler(local)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    for k in range(args.steps):
+        one_step(ev[k])
+    eng.synchronize()
+    torch.cuda.synchronize()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(step_ms)
+
+    # end to end through the C ABI: the drop-in call sequence, wall clock
+    if dist is not None:
+        dist.barrier()
+    eng.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        one_step()
+    eng.synchronize()
+    e2e_s = time.perf_counter() - t0
+    clocks = sampler.stop()
+
+    # per-kernel time of the same steps (phase timing on)
+    eng.set_phase_timing(True)
+    for _ in range(args.steps):
+        one_step()
+    phases, nsteps = eng.phase_times()
+    eng.set_phase_timing(False)
+    assert eng.check_finite() is None, "non-finite state after the benchmark"
+
+    if dist is not None:
+        tt = torch.tensor([total_ms, e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms, e2e_s = float(tt[0]), float(tt[1])
+    if rank != 0:
+        return
+
+    value = world * cells * args.steps / (total_ms * 1e-3)
+    e2e = world * cells * args.steps / e2e_s
+    peak, peak_src = peaks()
+    dom = max(phases, key=phases.get)
+    dom_ms = phases[dom] / max(1, nsteps)
+    dom_bytes = KERNEL_BYTES_PER_CELL.get(dom, 0) * cells
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    kind = "adiabatic" if d["eos"] == 1 else "isothermal"
+    step_achieved = STEP_BYTES_PER_CELL[kind] * cells * args.steps / (total_ms * 1e-3) / 1e9
+    line = {
+        "metric": "cell-updates/s/GPU, plain FP64 vs mixed-precision & batched at stated error",
+        "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(args.config),
+        "e2e": {"value": e2e, "unit": "cell-updates/s",
+                "h2d_bytes_per_step": 2 * 40,   # fgpu_body x2 passed as kernel arguments
+                "d2h_bytes_per_step": 8 + 40},  # CFL dt + disk-force partial sums
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
+                     "traffic": None,
+                     "bytes_per_cell": KERNEL_BYTES_PER_CELL.get(dom, 0),
+                     "ms_per_launch": dom_ms},
+        "roofline_step": {"achieved": step_achieved, "peak": peak, "unit": "GB/s",
+                          "frac": step_achieved / peak,
+                          "bytes_per_cell": STEP_BYTES_PER_CELL[kind]},
+        "phase_ms_per_step": {k: v / max(1, nsteps) for k, v in phases.items()},
+        "gpu_launches": args.steps * KERNELS_PER_STEP,
+        "clocks": clocks,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args.config, args.cpu_seconds)
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

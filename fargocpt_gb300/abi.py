@@ -119,7 +119,7 @@ EXPORTED_SYMBOLS = [
     "fgpu_set_bodies", "fgpu_init_euler", "fgpu_recalculate_derived",
     "fgpu_condition_cfl", "fgpu_apply_boundary_condition", "fgpu_step_euler",
     "fgpu_disk_on_planet_accel", "fgpu_total_mass", "fgpu_check_finite",
-    "fgpu_synchronize",
+    "fgpu_synchronize", "fgpu_set_phase_timing", "fgpu_phase_times", "fgpu_phase_name",
 ]
 
 
@@ -146,6 +146,9 @@ def _declare(lib: C.CDLL) -> C.CDLL:
         "fgpu_total_mass": ([vp, dp], C.c_int),
         "fgpu_check_finite": ([vp, P(C.c_int), P(C.c_int), P(C.c_int)], C.c_int),
         "fgpu_synchronize": ([vp], C.c_int),
+        "fgpu_set_phase_timing": ([vp, C.c_int], C.c_int),
+        "fgpu_phase_times": ([vp, dp, C.c_int, P(C.c_int), P(C.c_int)], C.c_int),
+        "fgpu_phase_name": ([C.c_int], C.c_char_p),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

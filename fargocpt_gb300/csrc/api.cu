@@ -51,7 +51,44 @@ struct fgpu_engine {
     Damping dm{};
     bool cfl_valid = false;
     std::vector<double> host_radii;
+
+    // phase timing: one row of events per recorded step
+    bool timing = false;
+    std::vector<std::vector<cudaEvent_t>> ev_rows;
+    std::vector<cudaEvent_t> ev_free;
+    int ev_cursor = 0;
 };
+
+static const char *kPhaseNames[] = {
+    "potential", "source", "artvisc_q", "artvisc_v", "stress", "viscous_substep3",
+    "ghost_pre", "transport_radial", "transport_azimuthal", "finish", "damping",
+    "ghost_post", "derived_cfl"};
+constexpr int kPhases = sizeof(kPhaseNames) / sizeof(kPhaseNames[0]);
+
+static cudaEvent_t take_event(fgpu_engine *e)
+{
+    if (!e->ev_free.empty()) {
+        cudaEvent_t ev = e->ev_free.back();
+        e->ev_free.pop_back();
+        return ev;
+    }
+    cudaEvent_t ev;
+    cudaEventCreate(&ev);
+    return ev;
+}
+
+// Marks the end of phase `k` of the current step (k = -1 opens the step).
+static void mark(fgpu_engine *e, int k)
+{
+    if (!e->timing) return;
+    if (k < 0) {
+        e->ev_rows.emplace_back();
+        e->ev_rows.back().reserve(kPhases + 1);
+    }
+    cudaEvent_t ev = take_event(e);
+    cudaEventRecord(ev, e->stream);
+    e->ev_rows.back().push_back(ev);
+}
 
 #define CK(call)                                                                  \
     do {                                                                          \
@@ -411,6 +448,9 @@ extern "C" int fgpu_destroy(fgpu_engine *eng)
 {
     if (!eng) return FGPU_ERR_BAD_ARG;
     if (eng->stream) cudaStreamSynchronize(eng->stream);
+    for (auto &row : eng->ev_rows)
+        for (auto ev : row) cudaEventDestroy(ev);
+    for (auto ev : eng->ev_free) cudaEventDestroy(ev);
     for (int f = 0; f < FGPU_FIELD_COUNT; ++f) cudaFree(eng->field[f]);
     cudaFree(eng->sigma_alt); cudaFree(eng->vr_alt); cudaFree(eng->vaz_alt); cudaFree(eng->energy_alt);
     for (int k = 0; k < 4; ++k) cudaFree(eng->mom[k]);
@@ -584,42 +624,59 @@ extern "C" int fgpu_step_euler(fgpu_engine *eng, double dt, double t)
     double **f = eng->field;
     const bool adi = eng->ph.adiabatic;
 
+    mark(eng, -1);
     // CalculateNbodyPotential (simulation.cpp:170-174)
     launch_potential(L, eng->bodies, f[FGPU_SCALE_HEIGHT], f[FGPU_POTENTIAL]);
+    mark(eng, 0);
     // update_with_sourceterms (simulation.cpp:190): momentum updates
     launch_source(L, dt, omf, f[FGPU_SIGMA], f[FGPU_PRESSURE], f[FGPU_POTENTIAL],
                   f[FGPU_V_RADIAL], f[FGPU_V_AZIMUTHAL], eng->vr_alt, eng->vaz_alt);
     std::swap(f[FGPU_V_RADIAL], eng->vr_alt);
     std::swap(f[FGPU_V_AZIMUTHAL], eng->vaz_alt);
+    mark(eng, 1);
     State s = state_of(eng);
     // compression heating + artificial viscosity (simulation.cpp:190-194)
     if (adi || eng->ph.art_visc_sn) {
         launch_artvisc_q(L, dt, s.sigma, s.vr, s.vaz, s.energy, s.qr, s.qphi);
+        mark(eng, 2);
         launch_artvisc_v(L, dt, s.sigma, s.energy, s.qr, s.qphi, s.vr, s.vaz, s.cs, s.H, s.nu);
+        mark(eng, 3);
+    } else {
+        mark(eng, 2);
+        mark(eng, 3);
     }
     // viscous stress and velocity update, SubStep3 (simulation.cpp:196-203)
     launch_stress(L, s.sigma, s.vr, s.vaz, s.nu, s.divv, s.trr, s.tpp, s.trp);
+    mark(eng, 4);
     launch_viscous(L, dt, beta_inv_at(eng->p, t), adi ? 7 : 1, s);
+    mark(eng, 5);
     // apply_boundary_condition(final = false) (simulation.cpp:213)
     ghost(eng, L);
+    mark(eng, 6);
     // Transport (simulation.cpp:215-217)
     launch_transport_radial(L, dt, omf, eng->radial_chunk, s.sigma, s.vr, s.vaz, s.energy,
                             eng->mom, eng->energy_alt, eng->sigma_alt);
+    mark(eng, 7);
     launch_transport_azimuthal(L, dt, eng->az_block, eng->mom, eng->energy_alt, eng->sigma_alt,
                                s.vaz, eng->ring_ws, eng->az_smem);
+    mark(eng, 8);
     launch_finish(L, omf, eng->mom, eng->sigma_alt, eng->energy_alt, s.vr, eng->vr_alt,
                   eng->vaz_alt, s.sigma, s.energy);
     std::swap(f[FGPU_V_RADIAL], eng->vr_alt);
     std::swap(f[FGPU_V_AZIMUTHAL], eng->vaz_alt);
+    mark(eng, 9);
     s = state_of(eng);
     // apply_boundary_condition(final = true) (simulation.cpp:244)
     if (eng->p.damping) {
         launch_damping(L, eng->dm, dt, eng->damp_rings, eng->n_damp_rings, s);
     }
+    mark(eng, 10);
     ghost(eng, L);
+    mark(eng, 11);
     // recalculate_derived_disk_quantities (simulation.cpp:265) + the next CFL
     CK(cudaMemsetAsync(eng->d_dtmin, 0x7f, sizeof(unsigned long long), eng->stream));
     launch_derived_cfl(L, 1 | 4, s, eng->d_dtmin);
+    mark(eng, 12);
     eng->cfl_valid = true;
     return check_launch(eng);
 }
@@ -685,5 +742,41 @@ extern "C" int fgpu_synchronize(fgpu_engine *eng)
 {
     if (!eng) return FGPU_ERR_BAD_ARG;
     CK(cudaStreamSynchronize(eng->stream));
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_set_phase_timing(fgpu_engine *eng, int enable)
+{
+    if (!eng) return FGPU_ERR_BAD_ARG;
+    eng->timing = enable != 0;
+    return FGPU_OK;
+}
+
+extern "C" const char *fgpu_phase_name(int k)
+{
+    return (k >= 0 && k < kPhases) ? kPhaseNames[k] : nullptr;
+}
+
+extern "C" int fgpu_phase_times(fgpu_engine *eng, double *ms, int capacity, int *count,
+                                int *steps)
+{
+    if (!eng || !ms || capacity < kPhases) return FGPU_ERR_BAD_ARG;
+    CK(cudaStreamSynchronize(eng->stream));
+    for (int k = 0; k < kPhases; ++k) ms[k] = 0.0;
+    int n = 0;
+    for (auto &row : eng->ev_rows) {
+        if ((int)row.size() == kPhases + 1) {
+            for (int k = 0; k < kPhases; ++k) {
+                float t = 0.f;
+                CK(cudaEventElapsedTime(&t, row[k], row[k + 1]));
+                ms[k] += t;
+            }
+            ++n;
+        }
+        for (auto ev : row) eng->ev_free.push_back(ev);
+    }
+    eng->ev_rows.clear();
+    if (count) *count = kPhases;
+    if (steps) *steps = n;
     return FGPU_OK;
 }

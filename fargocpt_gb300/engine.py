@@ -137,5 +137,19 @@ class Engine:
         self._check(rc, "fgpu_check_finite")
         return None
 
+    def set_phase_timing(self, enable: bool):
+        self._check(self.lib.fgpu_set_phase_timing(self.h, 1 if enable else 0),
+                    "fgpu_set_phase_timing")
+
+    def phase_times(self):
+        """{phase: summed ms} over the steps recorded since the last call, and
+        the number of steps."""
+        buf = (C.c_double * 64)()
+        n, steps = C.c_int(), C.c_int()
+        self._check(self.lib.fgpu_phase_times(self.h, buf, 64, C.byref(n), C.byref(steps)),
+                    "fgpu_phase_times")
+        return ({self.lib.fgpu_phase_name(k).decode(): buf[k] for k in range(n.value)},
+                steps.value)
+
     def synchronize(self):
         self._check(self.lib.fgpu_synchronize(self.h), "fgpu_synchronize")

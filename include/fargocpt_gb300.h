@@ -238,6 +238,18 @@ int fgpu_check_finite(fgpu_engine *eng, int *field, int *nr, int *naz);
 /* Blocks until all queued work of the handle is done. */
 int fgpu_synchronize(fgpu_engine *eng);
 
+/* Phase timing (no counterpart in the reference, whose only timer is the
+ * wall clock per step, src/logging.cpp:179-201): when enabled, every
+ * fgpu_step_euler records CUDA events between its kernels on the handle's
+ * stream.  fgpu_phase_times waits for the recorded steps, writes the summed
+ * milliseconds of each phase into ms[0 .. count-1] (count = number of
+ * phases, at most capacity), the number of steps into *steps, and clears the
+ * record.  fgpu_phase_name(k) names phase k. */
+int fgpu_set_phase_timing(fgpu_engine *eng, int enable);
+int fgpu_phase_times(fgpu_engine *eng, double *ms, int capacity, int *count,
+		     int *steps);
+const char *fgpu_phase_name(int k);
+
 #ifdef __cplusplus
 }
 #endif

@@ -22,8 +22,9 @@ def make_params(nrad, naz, adiabatic=False, **over):
         radial_viscosity_factor=1.0, heating_viscous_factor=1.0, cfl=0.5, cfl_max_var=1.1,
         heating_cooling_cfl_limit=10.0, sigma0=1e-3, sigma_floor=1e-9,
         thickness_smoothing=0.6, cooling_beta_value=10.0, cooling_beta_ramp_up=0.0,
-        minimum_temperature=2.811621e-05, maximum_temperature=9.372e294,
-        G=1.0, R_gas=1.0000000000000004, sigma_sb=2.0e-15, c_light=10065.167938321798,
+        minimum_temperature=2.811616511825056e-05, maximum_temperature=9.372055039416854e+294,
+        G=1.0, R_gas=1.0000000000000004, sigma_sb=468.30692052083845,
+        c_light=10065.167938321798,
         hydro_center_mass=1.0, damping_inner_limit=1.1, damping_outer_limit=0.9,
         damping_time_factor=1.0, damping_time_radius_outer=2.5,
         vaz_inner_keplerian_factor=1.0, vaz_outer_keplerian_factor=1.0,
