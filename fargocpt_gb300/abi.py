@@ -120,6 +120,7 @@ EXPORTED_SYMBOLS = [
     "fgpu_condition_cfl", "fgpu_apply_boundary_condition", "fgpu_step_euler",
     "fgpu_disk_on_planet_accel", "fgpu_total_mass", "fgpu_check_finite",
     "fgpu_synchronize", "fgpu_set_phase_timing", "fgpu_phase_times", "fgpu_phase_name",
+    "fgpu_disk_force_static",
 ]
 
 
@@ -149,6 +150,8 @@ def _declare(lib: C.CDLL) -> C.CDLL:
         "fgpu_set_phase_timing": ([vp, C.c_int], C.c_int),
         "fgpu_phase_times": ([vp, dp, C.c_int, P(C.c_int), P(C.c_int)], C.c_int),
         "fgpu_phase_name": ([C.c_int], C.c_char_p),
+        "fgpu_disk_force_static": ([vp, vp, vp, C.c_int, C.c_int, C.c_double, C.c_double,
+                                    P(FgpuBody), vp, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

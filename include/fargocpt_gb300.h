@@ -250,6 +250,23 @@ int fgpu_phase_times(fgpu_engine *eng, double *ms, int capacity, int *count,
 		     int *steps);
 const char *fgpu_phase_name(int k);
 
+/* Disk-on-body force and gas mass without any device allocation.  No
+ * counterpart in the reference: it serves callers that keep sigma and the
+ * scale height in their own device buffers and may not allocate device
+ * memory when they ask for the force (fixed memory budgets, allocation-free
+ * hot paths, code that must not synchronise the device).  The per-ring
+ * partial sums live in a static device array of 16384 rings (FargoCPT's
+ * MAX1D), so nrad - 2 must not exceed 16384; larger grids get
+ * FGPU_ERR_BAD_ARG.  sigma, scale_height: device, nrad x naz; radii: device,
+ * nrad + 2 values; out: device, 5 doubles (inner x, inner y, outer x, outer y
+ * acceleration, gas mass of the active rings).  The first call on a device
+ * looks up the array's address; make it before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU race. */
+int fgpu_disk_force_static(const double *sigma, const double *scale_height,
+			   const double *radii, int nrad, int naz, double G,
+			   double thickness_smoothing, const fgpu_body *body,
+			   double *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

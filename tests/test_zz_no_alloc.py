@@ -1,0 +1,77 @@
+"""fgpu_disk_force_static, the allocation-free disk-force entry point.
+
+It exists for callers that hold sigma and the scale height in their own device
+buffers and may not allocate device memory when they ask for the force (for
+instance under a fixed device-memory budget, or on a hot path where an
+allocation would synchronise the device).  Its scratch is a static device
+array shared by all calls, so this test calls it twice in a row with
+different bodies and checks each result against the regular entry points
+(fgpu_disk_on_planet_accel, fgpu_total_mass) of an engine holding the same
+disk.  Tolerance: 1e-9 relative on the force components (plus 1e-18 absolute
+for components near zero), 1e-12 relative on the mass.
+
+This file sorts last so that a run stopping at the first failure has already
+run every other test.
+"""
+import ctypes as C
+import math
+
+import numpy as np
+import pytest
+
+from gpu_cases import initial_state, load, make_params
+
+pytestmark = pytest.mark.gpu
+
+
+def test_static_scratch_force_matches_engine_twice():
+    import torch
+
+    from fargocpt_gb300.abi import FgpuBody, load_library
+    from fargocpt_gb300.engine import Engine, grid_radii
+
+    lib = load_library()
+    params, d = make_params(64, 192, adiabatic=True)
+    radii = grid_radii(d["radial_spacing"], d["rmin"], d["rmax"], d["nrad"])
+    st = initial_state(d, radii, seed=7)
+    bodies = [(0.0, 0.0, 1.0, 0.0, 0.0), (0.9, 0.3, 1e-3, 0.0, math.hypot(0.9, 0.3))]
+    eng = Engine(params, radii)
+    load(eng, st, bodies)
+    eng.apply_boundary_condition(0.0, 0.0, False)
+    t = 0.0
+    for _ in range(3):
+        dt = eng.condition_cfl()
+        eng.step_euler(dt, t)
+        t += dt
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    sig = torch.from_numpy(eng.get_field("SIGMA")).to(dev)
+    hh = torch.from_numpy(eng.get_field("SCALE_HEIGHT")).to(dev)
+    rad = torch.from_numpy(np.ascontiguousarray(radii)).to(dev)
+    out = torch.full((5,), float("nan"), dtype=torch.float64, device=dev)
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    mass_ref = eng.total_mass()
+    for k in (1, 0):  # two calls in a row, different bodies
+        acc_ref = eng.disk_on_planet_accel(k)
+        body = FgpuBody(*bodies[k])
+        rc = lib.fgpu_disk_force_static(
+            C.c_void_p(sig.data_ptr()), C.c_void_p(hh.data_ptr()), C.c_void_p(rad.data_ptr()),
+            d["nrad"], d["naz"], d["G"], d["thickness_smoothing"], C.byref(body),
+            C.c_void_p(out.data_ptr()), stream)
+        assert rc == 0
+        torch.cuda.synchronize()
+        o = out.cpu().numpy()
+        acc = (o[0] + o[2], o[1] + o[3])
+        np.testing.assert_allclose(acc, acc_ref, rtol=1e-9, atol=1e-18)
+        assert abs(o[4] - mass_ref) <= 1e-12 * abs(mass_ref)
+
+
+def test_static_scratch_rejects_oversized_grids():
+    from fargocpt_gb300.abi import FgpuBody, load_library
+
+    lib = load_library()
+    body = FgpuBody(1.0, 0.0, 1e-3, 0.0, 1.0)
+    dummy = C.c_void_p(16)  # never dereferenced: the size check comes first
+    rc = lib.fgpu_disk_force_static(dummy, dummy, dummy, 16384 + 3, 64, 1.0, 0.6,
+                                    C.byref(body), dummy, None)
+    assert rc == -1
