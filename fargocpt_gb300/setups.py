@@ -105,16 +105,16 @@ class CircularPlanets:
 
 
 CONFIGS = {
-    # BASELINE configs[0]: locally isothermal, one planet
+    # locally isothermal 128 x 384 disk, one planet
     "c1": dict(nrad=128, naz=384, rmin=0.4, rmax=2.5, adiabatic=False, slope=0.5,
                flaring=0.0, planets=[(1e-3, 1.0, 0.0)]),
-    # BASELINE configs[1]: adiabatic, beta cooling, SN art. visc, one planet
+    # adiabatic 512 x 1536 disk, beta cooling, SN art. visc, one planet
     "c2": dict(nrad=512, naz=1536, rmin=0.3, rmax=3.0, adiabatic=True, slope=1.0,
                flaring=0.25, planets=[(1e-3, 1.0, 0.0)]),
-    # BASELINE configs[2] grid with configs[0] physics
+    # locally isothermal 1024 x 3072 disk, one planet
     "c3": dict(nrad=1024, naz=3072, rmin=0.4, rmax=2.5, adiabatic=False, slope=0.5,
                flaring=0.0, planets=[(1e-3, 1.0, 0.0)]),
-    # BASELINE configs[4]: large adiabatic disk with three planets
+    # large adiabatic 2048 x 6144 disk with three planets
     "c5": dict(nrad=2048, naz=6144, rmin=0.3, rmax=5.0, adiabatic=True, slope=1.0,
                flaring=0.25, planets=[(1e-3, 1.0, 0.0), (3e-4, 1.6, 2.1), (1e-4, 2.5, 4.2)]),
 }
