@@ -175,7 +175,7 @@ static double omega_kepler(const fgpu_params &p, double r)
 static int validate(const fgpu_params *p, std::string &why)
 {
     if (p->nrad < 6 || p->naz < 8) { why = "nrad >= 6 and naz >= 8 required"; return FGPU_ERR_BAD_ARG; }
-    if (p->naz > 8192) { why = "naz > 8192 not supported by the azimuthal kernel"; return FGPU_ERR_UNSUPPORTED; }
+    if (p->naz > 8192) { why = "naz > 8192 not supported by the azimuthal kernel (16 cells x 512 threads per ring)"; return FGPU_ERR_UNSUPPORTED; }
     if (p->eos != FGPU_EOS_ISOTHERMAL && p->eos != FGPU_EOS_IDEAL) { why = "eos"; return FGPU_ERR_BAD_ARG; }
     if (p->art_visc == FGPU_ARTVISC_TW) { why = "Tscharnuter-Winkler artificial viscosity is not on the GPU path"; return FGPU_ERR_UNSUPPORTED; }
     if (p->art_visc != FGPU_ARTVISC_NONE && p->art_visc != FGPU_ARTVISC_SN) { why = "art_visc"; return FGPU_ERR_BAD_ARG; }
@@ -206,7 +206,7 @@ static int setup_tables(fgpu_engine *eng, const double *radii)
     eng->geo = Geo{nr, nz, dphi, invdphi};
     enum { RINF, RSUP, RMED, SURF, INVRMED, INVSURF, INVDIFFRMED, INVDIFFRSUP, INVDIFFRSUPRB,
            INVRINF, RINFSQ, TWOOVER, OMEGAK, INVOMEGAK, CSISO, INVDXSRC, INVDXTHETA, EMODEL,
-           NTAB };
+           HFACADI, INVCELL, INVCELL2, TWOOVERRMEDSUM, NTAB };
     std::vector<double> h((size_t)NTAB * R, 0.0);
     auto T = [&](int k) { return h.data() + (size_t)k * R; };
     for (int n = 0; n <= nr; ++n) {
@@ -233,7 +233,13 @@ static int setup_tables(fgpu_engine *eng, const double *radii)
         T(INVDXTHETA)[n] = 1.0 / (dphi * rm);
         T(EMODEL)[n] = 1.0 / (p.gamma - 1.0) * std::pow(p.aspect_ratio, 2) *
                        std::pow(rm, 2.0 * p.flaring_index - 1.0) * p.G * p.hydro_center_mass;
+        T(HFACADI)[n] = 1.0 / omega_kepler(p, rm) / std::sqrt(p.gamma);
+        const double dxr = T(RSUP)[n] - T(RINF)[n], dxa = rm * dphi;
+        const double cell = std::min(dxr, dxa);
+        T(INVCELL)[n] = 1.0 / cell;
+        T(INVCELL2)[n] = 1.0 / (cell * cell);
     }
+    for (int n = 1; n <= nr; ++n) T(TWOOVERRMEDSUM)[n] = 2.0 / (T(RMED)[n] + T(RMED)[n - 1]);
     for (int n = 1; n <= nr; ++n) T(INVDIFFRMED)[n] = 1.0 / (T(RMED)[n] - T(RMED)[n - 1]);
     for (int n = 0; n < nr; ++n) {
         T(TWOOVER)[n] = 2.0 / (std::pow(T(RINF)[n + 1], 2) - std::pow(T(RINF)[n], 2));
@@ -256,7 +262,8 @@ static int setup_tables(fgpu_engine *eng, const double *radii)
     t.InvDiffRsup = D(INVDIFFRSUP); t.InvDiffRsupRb = D(INVDIFFRSUPRB); t.InvRinf = D(INVRINF);
     t.RinfSq = D(RINFSQ); t.TwoOverDRa2 = D(TWOOVER); t.OmegaK = D(OMEGAK);
     t.InvOmegaK = D(INVOMEGAK); t.CsIso = D(CSISO); t.InvDxSrc = D(INVDXSRC);
-    t.InvDxTheta = D(INVDXTHETA); t.EModel = D(EMODEL);
+    t.InvDxTheta = D(INVDXTHETA); t.EModel = D(EMODEL); t.HFacAdi = D(HFACADI);
+    t.InvCell = D(INVCELL); t.InvCell2 = D(INVCELL2); t.TwoOverRmedSum = D(TWOOVERRMEDSUM);
     t.cosj = tc; t.sinj = tc + nz;
 
     // boundary hooks
@@ -353,6 +360,10 @@ static int setup_tables(fgpu_engine *eng, const double *radii)
     ph.G = p.G;
     ph.Mc = p.hydro_center_mass;
     ph.c_v_inv = p.mu / p.R_gas * (p.gamma - 1.0);
+    ph.cool_const = 2.0 * 4.0 * p.sigma_sb / p.c_light;
+    ph.mu_gm1_over_R = p.mu * (p.gamma - 1.0) / p.R_gas;
+    ph.emin_fac = p.minimum_temperature / p.mu * p.R_gas / (p.gamma - 1.0);
+    ph.emax_fac = p.maximum_temperature / p.mu * p.R_gas / (p.gamma - 1.0);
     return FGPU_OK;
 }
 
@@ -423,14 +434,19 @@ extern "C" int fgpu_create(const fgpu_params *params, const double *radii, fgpu_
     if (rc != FGPU_OK) return fail(rc);
 
     // azimuthal transport: whole ring in shared memory when it fits
-    eng->az_block = std::max(128, std::min(1024, ((eng->nz + 7) / 8 + 31) / 32 * 32));
+    {
+        const int per = azimuthal_cells_per_thread(eng->nz);
+        eng->az_block = std::max(128, std::min(512, ((eng->nz + per - 1) / per + 31) / 32 * 32));
+    }
     eng->az_smem = azimuthal_smem_bytes(eng->nz);
     if (eng->az_smem > 220 * 1024) {
         if (cudaMalloc(&eng->ring_ws, eng->az_smem * (size_t)eng->nr) != cudaSuccess) {
             eng->err = "out of device memory (ring workspace)";
             return fail(FGPU_ERR_OOM);
         }
-    } else if (eng->az_smem > 48 * 1024) {
+    } else {
+        // the kernel also has static shared memory: opt in for the dynamic size
+        // whatever it is
         if (prepare_azimuthal(eng->az_smem) != cudaSuccess) {
             eng->err = "cannot reserve shared memory for the azimuthal kernel";
             return fail(FGPU_ERR_CUDA);

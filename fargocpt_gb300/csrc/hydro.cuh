@@ -26,6 +26,10 @@ struct Tables {
     const double *InvDxSrc;    // 2 / (dphi (Rsup + Rinf))  (SourceEuler.cpp:387)
     const double *InvDxTheta;  // 1 / (dphi Rmed)
     const double *EModel;      // beta-cooling disk-model energy per unit sigma
+    const double *HFacAdi;     // 1 / (Omega_K sqrt(gamma)): H = c_s * HFacAdi (ideal EOS)
+    const double *InvCell;     // 1 / min(Rsup - Rinf, Rmed dphi)  (cfl.cpp:223-225)
+    const double *InvCell2;    // InvCell^2
+    const double *TwoOverRmedSum; // 2 / (Rmed[i] + Rmed[i-1])  (viscosity.cpp:407)
     const double *cosj, *sinj; // cos / sin (dphi j)
 };
 
@@ -46,7 +50,9 @@ struct Phys {
     double tmin, tmax, Rgas, sigma_sb, c_light, G, Mc;
     double c_v_inv;       // mu / R * (gamma - 1)
     double four_C2;       // 4 * pow(C, 2)
-    double cool_const;    // 2 * 4 * sigma_sb / c (SubStep3 alpha, pre-folded order kept)
+    double cool_const;    // 2 * 4 * sigma_sb / c (SubStep3's radiative alpha)
+    double mu_gm1_over_R; // mu (gamma - 1) / R
+    double emin_fac, emax_fac; // Tmin|Tmax / mu * R / (gamma - 1)
 };
 
 struct Bodies {

@@ -32,6 +32,7 @@ void launch_transport_radial(const Launch &L, double dt, double omf, int chunk, 
                              const double *vr, const double *vaz, const double *E,
                              double *const mom[4], double *E_out, double *S_out);
 size_t azimuthal_smem_bytes(int nz);
+int azimuthal_cells_per_thread(int nz);
 cudaError_t prepare_azimuthal(size_t smem);
 void launch_transport_azimuthal(const Launch &L, double dt, int block, double *const mom[4],
                                 double *E, double *S, const double *vaz, double *ring_ws,

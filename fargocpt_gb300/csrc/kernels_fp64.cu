@@ -18,25 +18,66 @@ namespace fgpu {
 __device__ __forceinline__ int jnext(int j, int nz) { return j == nz - 1 ? 0 : j + 1; }
 __device__ __forceinline__ int jprev(int j, int nz) { return j == 0 ? nz - 1 : j - 1; }
 
+// Sign and magnitude tests on the bit pattern run on the integer pipe, which
+// GB300 has plenty of, instead of the FP64 pipe, which it has little of.
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ bool positive(double x)
+{
+    // x > 0 for finite x
+    return dbits(x) > 0;
+}
+// a * b > 0 for finite a, b (both non-zero, same sign)
+__device__ __forceinline__ bool same_sign_nonzero(double a, double b)
+{
+    const long long ia = dbits(a), ib = dbits(b);
+    const long long m = 0x7fffffffffffffffll;
+    return ((ia ^ ib) >= 0) && (ia & m) != 0 && (ib & m) != 0;
+}
+// |a| < |b| for finite a, b
+__device__ __forceinline__ bool abs_less(double a, double b)
+{
+    const long long m = 0x7fffffffffffffffll;
+    return (dbits(a) & m) < (dbits(b) & m);
+}
+
+// Reciprocal by Newton-Raphson iteration r <- r (2 - b r), written as
+// e = 1 - b r, r <- r + r e, from the hardware's approximate reciprocal
+// (PTX rcp.approx.ftz.f64).  Two iterations square the seed's relative error
+// twice, which takes any seed better than 2^-14 below double rounding; the
+// quotient a * (1/b) is then within two units in the last place of a / b.
+// Used for divisors that are normal numbers (densities, sums of slopes).
+__device__ __forceinline__ double fast_rcp(double b)
+{
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(b));
+    double e = fma(-b, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-b, r, 1.0);
+    r = fma(r, e, r);
+    return r;
+}
+__device__ __forceinline__ double fast_div(double a, double b) { return a * fast_rcp(b); }
+
 // van_leer_lim / MC_lim, src/TransportEuler.cpp:306-337
 __device__ __forceinline__ double flux_limiter(double a, double b, int mc)
 {
     if (mc) {
-        double mm = 0.0;
-        if (a * b > 0.0) mm = fabs(a) < fabs(b) ? a : b;
+        const double mm = same_sign_nonzero(a, b) ? (abs_less(a, b) ? a : b) : 0.0;
         const double c = 0.5 * (a + b), d = 2.0 * mm;
-        if (c * d > 0.0) return fabs(c) < fabs(d) ? c : d;
+        if (same_sign_nonzero(c, d)) return abs_less(c, d) ? c : d;
         return 0.0;
     }
-    if (a * b > 0.0) return 2.0 * a * b / (a + b);
+    if (same_sign_nonzero(a, b)) return fast_div(2.0 * a * b, a + b);
     return 0.0;
 }
 
-// assure_temperature_range, src/SourceEuler.cpp:136-202
+// assure_temperature_range, src/SourceEuler.cpp:136-202: the bounds are
+// Tmin/max * sigma / mu * R / (gamma - 1); the constant factor is folded on
+// the host.
 __device__ __forceinline__ double temperature_floor(double e, double sigma, const Phys &ph)
 {
-    const double emin = ph.tmin * sigma / ph.mu * ph.Rgas / ph.gm1;
-    const double emax = ph.tmax * sigma / ph.mu * ph.Rgas / ph.gm1;
+    const double emin = sigma * ph.emin_fac;
+    const double emax = sigma * ph.emax_fac;
     if (!(e > emin)) e = emin;
     if (!(e < emax)) e = emax;
     return e;
@@ -60,14 +101,18 @@ __global__ void k_potential(Geo g, Tables t, Phys ph, Bodies b, const double *__
         const double dx = x - b.x[k];
         const double dy = y - b.y[k];
         const double dist_2 = dx * dx + dy * dy;
-        const double d_sm = sqrt(dist_2 + smooth * smooth);
+        const double d2 = dist_2 + smooth * smooth;
+        const double inv_d = rsqrt(d2);
         double fk = 1.0;
         const double r_sm = b.rsm[k];
-        if (r_sm > 0.0 && d_sm < r_sm) {
-            const double q = d_sm / r_sm;
-            fk = pow(q, 4.0) - 2.0 * pow(q, 3.0) + 2.0 * q;
+        if (r_sm > 0.0) {
+            const double d_sm = d2 * inv_d;
+            if (d_sm < r_sm) {
+                const double q = d_sm / r_sm;
+                fk = q * q * q * q - 2.0 * (q * q * q) + 2.0 * q;
+            }
         }
-        acc += -ph.G * b.m[k] / d_sm * fk;
+        acc += -ph.G * b.m[k] * inv_d * fk;
     }
     acc += -b.ix * x - b.iy * y;
     pot[CELL(i, j)] = acc;
@@ -90,7 +135,7 @@ __global__ void k_source(Geo g, Tables t, double dt, double omega_frame,
     // v_radial rows One_no_ghost_vr (2) .. MaxMo_no_ghost_vr (nr - 1)
     double vr = vr_in[CELL(i, j)];
     if (i >= 2 && i < nr - 1) {
-        double gradp = 2.0 / (S[CELL(i, j)] + S[CELL(i - 1, j)]);
+        double gradp = 2.0 * fast_rcp(S[CELL(i, j)] + S[CELL(i - 1, j)]);
         gradp *= (P[CELL(i, j)] - P[CELL(i - 1, j)]);
         gradp *= t.InvDiffRmed[i];
         const double gradphi = (pot[CELL(i, j)] - pot[CELL(i - 1, j)]) * t.InvDiffRmed[i];
@@ -109,7 +154,7 @@ __global__ void k_source(Geo g, Tables t, double dt, double omega_frame,
         if (i >= 1 && i < nr - 1) {
             const int jp = jprev(j, nz);
             const double invdx = t.InvDxSrc[i];
-            const double gradp = 2.0 / (S[CELL(i, j)] + S[CELL(i, jp)]) *
+            const double gradp = 2.0 * fast_rcp(S[CELL(i, j)] + S[CELL(i, jp)]) *
                                  (P[CELL(i, j)] - P[CELL(i, jp)]) * invdx;
             const double gradphi = (pot[CELL(i, j)] - pot[CELL(i, jp)]) * invdx;
             va = va + dt * (-gradp - gradphi);
@@ -182,19 +227,19 @@ __global__ void k_artvisc_v(Geo g, Tables t, Phys ph, double dt, const double *_
     const size_t c = CELL(i, j);
     if (ph.art_visc_sn) {
         if (i >= 2 && i < nr - 1) {
-            vr[c] = vr[c] - dt * 2.0 / (S[c] + S[CELL(i - 1, j)]) * (Qr[c] - Qr[CELL(i - 1, j)]) *
-                                t.InvDiffRmed[i];
+            vr[c] = vr[c] - dt * 2.0 * fast_rcp(S[c] + S[CELL(i - 1, j)]) *
+                                (Qr[c] - Qr[CELL(i - 1, j)]) * t.InvDiffRmed[i];
         }
         if (i >= 1 && i < nr - 1) {
             const int jp = jprev(j, nz);
-            vaz[c] = vaz[c] - dt * 2.0 / (S[c] + S[CELL(i, jp)]) * (Qp[c] - Qp[CELL(i, jp)]) *
-                                  t.InvDxTheta[i];
+            vaz[c] = vaz[c] - dt * 2.0 * fast_rcp(S[c] + S[CELL(i, jp)]) *
+                                  (Qp[c] - Qp[CELL(i, jp)]) * t.InvDxTheta[i];
         }
     }
     if (ph.adiabatic) {
         // compute_sound_speed_normal / compute_scale_height_old / update_viscosity
-        const double c_s = sqrt(ph.g_gm1 * E[c] / S[c]);
-        const double h = c_s / ph.sqrt_gamma * t.InvOmegaK[i];
+        const double c_s = sqrt(ph.g_gm1 * fast_div(E[c], S[c]));
+        const double h = c_s * t.HFacAdi[i];
         cs[c] = c_s;
         H[c] = h;
         nu[c] = ph.alpha > 0 ? ph.alpha * h * c_s : ph.constant_viscosity;
@@ -261,7 +306,7 @@ __global__ void k_viscous(Geo g, Tables t, Phys ph, double dt, double beta_inv, 
     if (mode & 1) {
         if (i >= 1 && i < nr - 1) {
             const double sigma_avg = 0.5 * (S[c] + S[CELL(i, jp)]);
-            const double dVp = dt * t.InvRmed[i] / (sigma_avg) *
+            const double dVp = fast_div(dt * t.InvRmed[i], sigma_avg) *
                                (t.TwoOverDRa2[i] * (t.RinfSq[i + 1] * trp[CELL(i + 1, j)] -
                                                     t.RinfSq[i] * trp[c]) +
                                 (tpp[c] - tpp[CELL(i, jp)]) * g.invdphi);
@@ -270,7 +315,7 @@ __global__ void k_viscous(Geo g, Tables t, Phys ph, double dt, double beta_inv, 
         if (i >= 2 && i < nr - 1) {
             const double sigma_avg = 0.5 * (S[c] + S[CELL(i - 1, j)]);
             const double dVr =
-                dt / (sigma_avg)*ph.rvf * 2.0 / (t.Rmed[i] + t.Rmed[i - 1]) *
+                fast_div(dt, sigma_avg) * ph.rvf * t.TwoOverRmedSum[i] *
                 ((t.Rmed[i] * trr[c] - t.Rmed[i - 1] * trr[CELL(i - 1, j)]) * t.InvDiffRmed[i] +
                  (trp[CELL(i, jn)] - trp[c]) * g.invdphi - 0.5 * (tpp[c] + tpp[CELL(i - 1, j)]));
             vr[c] += dVr;
@@ -286,11 +331,11 @@ __global__ void k_viscous(Geo g, Tables t, Phys ph, double dt, double beta_inv, 
             // thermal_relaxation, SourceEuler.cpp:632-690
             double delta_E = e;
             if (ph.beta_ref == 1) {
-                delta_E -= E0[c] / S0[c] * sig;
+                delta_E -= fast_div(E0[c], S0[c]) * sig;
             } else if (ph.beta_ref == 2) {
                 delta_E -= t.EModel[i] * sig;
             } else if (ph.beta_ref == 3) {
-                delta_E -= ph.tmin * sig / ph.mu * ph.Rgas / ph.gm1;
+                delta_E -= sig * ph.emin_fac;
             }
             qm = 0.0 + delta_E * t.OmegaK[i] * beta_inv;
         }
@@ -301,7 +346,7 @@ __global__ void k_viscous(Geo g, Tables t, Phys ph, double dt, double beta_inv, 
                 const double tau_r_phi = 0.25 * (trp[c] + trp[CELL(i + 1, j)] + trp[CELL(i, jn)] +
                                                  trp[CELL(i + 1, jn)]);
                 const double t_rr = trr[c], t_pp = tpp[c], d = divv[c];
-                double q = 1.0 / (2.0 * n * sig) *
+                double q = fast_rcp(2.0 * n * sig) *
                            (t_rr * t_rr + 2 * (tau_r_phi * tau_r_phi) + t_pp * t_pp);
                 q += (2.0 / 9.0) * n * sig * (d * d);
                 q *= ph.hvf;
@@ -309,12 +354,13 @@ __global__ void k_viscous(Geo g, Tables t, Phys ph, double dt, double beta_inv, 
             }
         }
         // radiative alpha factor, SourceEuler.cpp:905-912
-        const double x = ph.mu * ph.gm1 / (ph.Rgas * sig);
+        const double x = ph.mu_gm1_over_R * fast_rcp(sig);
         const double x2 = x * x;
         const double inv_pow4 = x2 * x2;
-        const double alpha = 1.0 + 2.0 * H[c] * 4.0 * ph.sigma_sb / ph.c_light * inv_pow4 * (e * e * e);
-        qp /= alpha;
-        qm /= alpha;
+        const double alpha = 1.0 + H[c] * ph.cool_const * inv_pow4 * (e * e * e);
+        const double inv_alpha = fast_rcp(alpha);
+        qp *= inv_alpha;
+        qm *= inv_alpha;
     }
     if (mode & 4) {
         double e_new = e;
@@ -420,27 +466,31 @@ __global__ void k_ghost(Geo g, Tables t, BcSpec bc, double omf, State s)
 // Quantities: 0..3 momenta, 4 energy, 5 sigma (sigma is advected last, with
 // the pre-transport sigma as the reference density).
 // ---------------------------------------------------------------------------
-struct RadWin {
-    double w[4];   // specific quantity at rings k-1 .. k+2 relative to the interface k
-    double dq[2];  // limited slope at k-1, k
-};
-
+// Specific quantities of ring i (quantity / sigma, TransportEuler.cpp:550-551
+// via divise_polargrid, SideEuler.cpp:27-41): the momenta's specific values
+// are the velocities themselves; energy needs one division.  Slot NQ holds
+// sigma, whose star value is built from sigma itself (compute_star_radial on
+// Density, :140).
 template <int NQ>
-__device__ __forceinline__ void rad_load_ring(int i, int j, int nz, int nr, const double *S,
-                                              const double *vr, const double *vaz,
-                                              const double *E, double omf, const Tables &t,
-                                              double *q /* NQ+1: quantities, last = sigma */)
+__device__ __forceinline__ void rad_ring(int i, int j, int nz, const double *S, const double *vr,
+                                         const double *vaz, const double *E, double omf,
+                                         const Tables &t, double *w, double &sig)
 {
     const double sg = S[CELL(i, j)];
     const double r = t.Rmed[i];
-    q[0] = sg * vr[CELL(i + 1, j)];
-    q[1] = sg * vr[CELL(i, j)];
-    q[2] = sg * (vaz[CELL(i, jnext(j, nz))] + r * omf) * r;
-    q[3] = sg * (vaz[CELL(i, j)] + r * omf) * r;
-    if (NQ == 5) q[4] = E[CELL(i, j)];
-    q[NQ] = sg;
+    w[0] = vr[CELL(i + 1, j)];
+    w[1] = vr[CELL(i, j)];
+    w[2] = (vaz[CELL(i, jnext(j, nz))] + r * omf) * r;
+    w[3] = (vaz[CELL(i, j)] + r * omf) * r;
+    if (NQ == 5) w[4] = fast_div(E[CELL(i, j)], sg);
+    w[NQ] = sg;
+    sig = sg;
 }
 
+// One thread streams one azimuth column through a chunk of rings.  For every
+// ring it forms the specific quantities and their limited slopes once; the
+// interface between ring k-1 and k takes its upwind star value from ring k-1
+// or k, so each flux is computed exactly once.
 template <int NQ>
 __global__ void k_transport_radial(Geo g, Tables t, double dt, double omf, int mc, int chunk,
                                    const double *__restrict__ S, const double *__restrict__ vr,
@@ -449,6 +499,7 @@ __global__ void k_transport_radial(Geo g, Tables t, double dt, double omf, int m
                                    double *__restrict__ mom2, double *__restrict__ mom3,
                                    double *__restrict__ E_out, double *__restrict__ S_out)
 {
+    constexpr int NW = NQ + 1;
     const int nz = g.nz, nr = g.nr;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= nz) return;
@@ -457,104 +508,116 @@ __global__ void k_transport_radial(Geo g, Tables t, double dt, double omf, int m
     const int i1 = min(i0 + chunk, nr);
     const double dtdphi = dt * g.dphi;
 
-    // window over rings k-2 .. k+1 for the interface k: raw quantities and
-    // specific quantities (quantity / sigma)
-    double qv[4][NQ + 1];   // rings k-2, k-1, k, k+1
-    bool have[4];
-    for (int s = 0; s < 4; ++s) {
-        const int ring = i0 - 2 + s;
-        have[s] = ring >= 0 && ring < nr;
-        if (have[s]) {
-            rad_load_ring<NQ>(ring, j, nz, nr, S, vr, vaz, E, omf, t, qv[s]);
-        } else {
-            for (int q = 0; q <= NQ; ++q) qv[s][q] = 0.0;
-        }
-    }
-    // limited slope of quantity q (specific for q < NQ, sigma for q == NQ) at
-    // ring `ring` from window slots (s-1, s, s+1)
-    auto slope = [&](int s, int ring, int q) -> double {
+    // rolling state: specific quantities of rings k-1 (wa) and k (wb), their
+    // limited slopes (da, db), the upward difference of ring k (ub), the
+    // sigma of ring k-1 / k
+    double wa[NW] = {}, wb[NW] = {}, da[NW] = {}, db[NW] = {}, ub[NW] = {};
+    double sa = 0.0, sb = 0.0;
+
+    // slope of ring `ring` from its down/up differences (compute_star_radial,
+    // :357-367: zero on the first and last ring)
+    auto lim = [&](int ring, double up, double down) -> double {
         if (ring <= 0 || ring >= nr - 1) return 0.0;
-        double a, b, c;
-        if (q < NQ) {
-            a = qv[s - 1][q] / qv[s - 1][NQ];
-            b = qv[s][q] / qv[s][NQ];
-            c = qv[s + 1][q] / qv[s + 1][NQ];
-        } else {
-            a = qv[s - 1][NQ];
-            b = qv[s][NQ];
-            c = qv[s + 1][NQ];
-        }
-        const double dqm = (b - a) * t.InvDiffRmed[ring];
-        const double dqp = (c - b) * t.InvDiffRmed[ring + 1];
-        return flux_limiter(dqp, dqm, mc);
+        return flux_limiter(up, down, mc);
     };
 
-    double flux_prev[NQ + 1];
-    double q_prev[NQ + 1];
-    for (int k = i0; k <= i1; ++k) {
-        // interface k uses rings k-1 (slot 1) and k (slot 2); slopes need
-        // slots 0..3
-        double flux[NQ + 1];
-        if (k == 0 || k >= nr) {
-            for (int q = 0; q <= NQ; ++q) flux[q] = 0.0;
-        } else {
-            const double v = vr[CELL(k, j)];
-            // DensityStar (compute_star_radial on sigma)
-            double sstar;
-            if (v > 0.0) {
-                const double dqs = slope(1, k - 1, NQ);
-                sstar = qv[1][NQ] + (t.Rmed[k] - t.Rmed[k - 1] - v * dt) * 0.5 * dqs;
-            } else {
-                const double dqs = slope(2, k, NQ);
-                sstar = qv[2][NQ] - (t.Rmed[k + 1] - t.Rmed[k] + v * dt) * 0.5 * dqs;
-            }
-            const double base = dtdphi * t.Rinf[k];
+    // prime rings k-1 = i0-1 and k = i0 (their slopes need rings i0-2 .. i0+1)
+    {
+        double wm2[NW] = {}, wtmp[NW] = {}, s_tmp = 0.0;
+        const int r0 = i0 - 1;
+        if (r0 - 1 >= 0) rad_ring<NQ>(r0 - 1, j, nz, S, vr, vaz, E, omf, t, wm2, s_tmp);
+        if (r0 >= 0) rad_ring<NQ>(r0, j, nz, S, vr, vaz, E, omf, t, wa, sa);
+        rad_ring<NQ>(i0, j, nz, S, vr, vaz, E, omf, t, wb, sb);
+        double downa[NW];
 #pragma unroll
-            for (int q = 0; q < NQ; ++q) {
-                double qstar;
-                if (v > 0.0) {
-                    const double dq = slope(1, k - 1, q);
-                    qstar = qv[1][q] / qv[1][NQ] + (t.Rmed[k] - t.Rmed[k - 1] - v * dt) * 0.5 * dq;
-                } else {
-                    const double dq = slope(2, k, q);
-                    qstar = qv[2][q] / qv[2][NQ] - (t.Rmed[k + 1] - t.Rmed[k] + v * dt) * 0.5 * dq;
-                }
-                flux[q] = base * qstar * sstar * v;
-            }
-            // sigma: specific quantity is exactly 1
-            flux[NQ] = base * 1.0 * sstar * v;
+        for (int q = 0; q < NW; ++q) {
+            downa[q] = (r0 - 1 >= 0 && r0 >= 0) ? (wa[q] - wm2[q]) * t.InvDiffRmed[r0] : 0.0;
+            ub[q] = r0 >= 0 ? (wb[q] - wa[q]) * t.InvDiffRmed[i0] : 0.0;  // up of k-1 = down of k
         }
-        if (k > i0) {
-            const int i = k - 1;
-            const double invs = t.InvSurf[i];
-            const size_t c = CELL(i, j);
-            const double n0 = q_prev[0] + (flux_prev[0] - flux[0]) * invs;
-            const double n1 = q_prev[1] + (flux_prev[1] - flux[1]) * invs;
-            const double n2 = q_prev[2] + (flux_prev[2] - flux[2]) * invs;
-            const double n3 = q_prev[3] + (flux_prev[3] - flux[3]) * invs;
-            mom0[c] = n0;
-            mom1[c] = n1;
-            mom2[c] = n2;
-            mom3[c] = n3;
-            if (NQ == 5) E_out[c] = q_prev[4] + (flux_prev[4] - flux[4]) * invs;
-            S_out[c] = q_prev[NQ] + (flux_prev[NQ] - flux[NQ]) * invs;
+        const bool has_next = i0 + 1 < nr;
+        if (has_next) rad_ring<NQ>(i0 + 1, j, nz, S, vr, vaz, E, omf, t, wtmp, s_tmp);
+#pragma unroll
+        for (int q = 0; q < NW; ++q) {
+            da[q] = r0 >= 0 ? lim(r0, ub[q], downa[q]) : 0.0;
+            const double up = has_next ? (wtmp[q] - wb[q]) * t.InvDiffRmed[i0 + 1] : 0.0;
+            db[q] = lim(i0, up, ub[q]);
+            ub[q] = up;
         }
-        if (k < i1) {
-            for (int q = 0; q <= NQ; ++q) {
-                flux_prev[q] = flux[q];
-                q_prev[q] = qv[2][q];
-            }
-            // shift the window by one ring
-            for (int s = 0; s < 3; ++s) {
-                have[s] = have[s + 1];
-                for (int q = 0; q <= NQ; ++q) qv[s][q] = qv[s + 1][q];
-            }
-            const int ring = k + 2;
-            have[3] = ring < nr;
-            if (have[3]) {
-                rad_load_ring<NQ>(ring, j, nz, nr, S, vr, vaz, E, omf, t, qv[3]);
+        // keep ring i0+1 for the first shift
+#pragma unroll
+        for (int q = 0; q < NW; ++q) wm2[q] = wtmp[q];
+        // wm2 now holds ring k+1; stash it in registers via the loop below
+        double flux_prev[NW], q_prev[NW];
+        double wn[NW];
+#pragma unroll
+        for (int q = 0; q < NW; ++q) wn[q] = wm2[q];
+        double sn = has_next ? S[CELL(i0 + 1, j)] : 0.0;
+
+        for (int k = i0; k <= i1; ++k) {
+            // flux through the interface k (between rings k-1 and k)
+            double flux[NW];
+            if (k == 0 || k >= nr) {
+#pragma unroll
+                for (int q = 0; q < NW; ++q) flux[q] = 0.0;
             } else {
-                for (int q = 0; q <= NQ; ++q) qv[3][q] = 0.0;
+                const double v = vr[CELL(k, j)];
+                const double base = dtdphi * t.Rinf[k];
+                const double vdt = v * dt;
+                double sstar;
+                const bool up = positive(v);
+                // DensityStar, then QRStar of every specific quantity
+                if (up) {
+                    const double f = (t.Rmed[k] - t.Rmed[k - 1] - vdt) * 0.5;
+                    sstar = wa[NQ] + f * da[NQ];
+#pragma unroll
+                    for (int q = 0; q < NQ; ++q) flux[q] = base * (wa[q] + f * da[q]) * sstar * v;
+                } else {
+                    const double f = (t.Rmed[k + 1] - t.Rmed[k] + vdt) * 0.5;
+                    sstar = wb[NQ] - f * db[NQ];
+#pragma unroll
+                    for (int q = 0; q < NQ; ++q) flux[q] = base * (wb[q] - f * db[q]) * sstar * v;
+                }
+                flux[NQ] = base * sstar * v;
+            }
+            if (k > i0) {
+                // VanLeerRadial update of ring k-1 (:586-591)
+                const int i = k - 1;
+                const double invs = t.InvSurf[i];
+                const size_t c = CELL(i, j);
+                mom0[c] = q_prev[0] + (flux_prev[0] - flux[0]) * invs;
+                mom1[c] = q_prev[1] + (flux_prev[1] - flux[1]) * invs;
+                mom2[c] = q_prev[2] + (flux_prev[2] - flux[2]) * invs;
+                mom3[c] = q_prev[3] + (flux_prev[3] - flux[3]) * invs;
+                if (NQ == 5) E_out[c] = q_prev[4] + (flux_prev[4] - flux[4]) * invs;
+                S_out[c] = q_prev[NQ] + (flux_prev[NQ] - flux[NQ]) * invs;
+            }
+            if (k < i1) {
+                // conserved quantities of ring k for its update at interface k+1
+#pragma unroll
+                for (int q = 0; q < NW; ++q) flux_prev[q] = flux[q];
+                q_prev[0] = sb * wb[0];
+                q_prev[1] = sb * wb[1];
+                q_prev[2] = sb * wb[2];
+                q_prev[3] = sb * wb[3];
+                if (NQ == 5) q_prev[4] = E[CELL(k, j)];
+                q_prev[NQ] = sb;
+                // advance: ring k becomes k-1, ring k+1 becomes k
+                const bool more = k + 2 < nr;
+                double w2[NW], s2 = 0.0;
+                if (more) rad_ring<NQ>(k + 2, j, nz, S, vr, vaz, E, omf, t, w2, s2);
+#pragma unroll
+                for (int q = 0; q < NW; ++q) {
+                    wa[q] = wb[q];
+                    da[q] = db[q];
+                    wb[q] = wn[q];
+                    const double up = more ? (w2[q] - wn[q]) * t.InvDiffRmed[k + 2] : 0.0;
+                    db[q] = lim(k + 1, up, ub[q]);
+                    ub[q] = up;
+                    wn[q] = more ? w2[q] : 0.0;
+                }
+                sa = sb;
+                sb = sn;
+                sn = s2;
             }
         }
     }
@@ -618,104 +681,118 @@ __device__ double block_min(double v, double *red)
 // specific quantity and slopes live in shared memory (or in a per-ring global
 // workspace when the ring is too long for shared memory).
 // ---------------------------------------------------------------------------
-struct RingArrays {
-    double *S, *SS, *V, *W, *D;
-};
+// Each thread owns the cells j = threadIdx.x + n * blockDim.x, n < PER.
 
-__device__ void ring_star_theta(const double *Q, const double *V, double *D, double *QS,
-                                double dt, double dxtheta, double invdxtheta, int nz, int mc,
-                                bool uniform, double vconst)
-{
-    for (int j = threadIdx.x; j < nz; j += blockDim.x) {
-        const int jp = j == nz - 1 ? 0 : j + 1;
-        const int jm = j == 0 ? nz - 1 : j - 1;
-        const double dqm = Q[j] - Q[jm];
-        const double dqp = Q[jp] - Q[j];
-        D[j] = 0.5 * flux_limiter(dqp, dqm, mc) * invdxtheta;
-    }
-    __syncthreads();
-    for (int j = threadIdx.x; j < nz; j += blockDim.x) {
-        const int jm = j == 0 ? nz - 1 : j - 1;
-        const double ksi = (uniform ? vconst : V[j]) * dt;
-        if (ksi > 0.0) {
-            QS[j] = Q[jm] + (dxtheta - ksi) * D[jm];
-        } else {
-            QS[j] = Q[j] - (dxtheta + ksi) * D[j];
-        }
-    }
-    __syncthreads();
-}
-
-// One QuantitiesAdvection pass over the ring (sigma is in R.S on entry and
-// is replaced by its advected value on exit).
-__device__ void ring_advection_pass(RingArrays R, double *const *qptr, int nq, size_t row,
-                                    double dt, double dxtheta, double invdxtheta, double dxrad,
+// One QuantitiesAdvection pass (TransportEuler.cpp:292-304) over the ring:
+// DensityStar from sigma (ComputeStarTheta, :416-466), then VanLeerTheta
+// (:630-664) for every quantity with DENSITY_INT = sigma, sigma last.  S holds
+// sigma on entry and its advected value on exit.  v[n] is the owned cells'
+// velocity (ignored when uniform).
+template <int PER>
+__device__ void ring_advection_pass(double *S, double *SS, double *W, double *D,
+                                    double *const *qrow, int nq, const double *v, double dt,
+                                    double dxtheta, double half_invdx, double dxrad,
                                     double invsurf, int nz, int mc, bool uniform, double vconst)
 {
-    // DensityStar from sigma, then every quantity divided by DENSITY_INT = sigma
-    ring_star_theta(R.S, R.V, R.D, R.SS, dt, dxtheta, invdxtheta, nz, mc, uniform, vconst);
+    const int tid = threadIdx.x, bs = blockDim.x;
+    double invs[PER], f[PER];
+    // DensityStar
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = tid + n * bs;
+        if (j < nz) {
+            const int jp = j == nz - 1 ? 0 : j + 1;
+            const int jm = j == 0 ? nz - 1 : j - 1;
+            D[j] = flux_limiter(S[jp] - S[j], S[j] - S[jm], mc) * half_invdx;
+            invs[n] = fast_rcp(S[j]);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = tid + n * bs;
+        if (j < nz) {
+            const int jm = j == 0 ? nz - 1 : j - 1;
+            const double vv = uniform ? vconst : v[n];
+            const double ksi = vv * dt;
+            SS[j] = positive(vv) ? S[jm] + (dxtheta - ksi) * D[jm] : S[j] - (dxtheta + ksi) * D[j];
+        }
+    }
+    __syncthreads();
     for (int q = 0; q < nq; ++q) {
-        double *Q = qptr[q] + row;
-        for (int j = threadIdx.x; j < nz; j += blockDim.x) R.W[j] = Q[j] / R.S[j];
-        __syncthreads();
-        // QRStar into W after slopes in D: reuse ring_star_theta with W -> W
-        for (int j = threadIdx.x; j < nz; j += blockDim.x) {
-            const int jp = j == nz - 1 ? 0 : j + 1;
-            const int jm = j == 0 ? nz - 1 : j - 1;
-            const double dqm = R.W[j] - R.W[jm];
-            const double dqp = R.W[jp] - R.W[j];
-            R.D[j] = 0.5 * flux_limiter(dqp, dqm, mc) * invdxtheta;
+        double *Q = qrow[q];
+#pragma unroll
+        for (int n = 0; n < PER; ++n) {
+            const int j = tid + n * bs;
+            if (j < nz) W[j] = Q[j] * invs[n];
         }
         __syncthreads();
-        double f[8];
-        int n = 0;
-        for (int j = threadIdx.x; j < nz; j += blockDim.x, ++n) {
-            const int jm = j == 0 ? nz - 1 : j - 1;
-            const double v = uniform ? vconst : R.V[j];
-            const double ksi = v * dt;
-            double qs;
-            if (ksi > 0.0) {
-                qs = R.W[jm] + (dxtheta - ksi) * R.D[jm];
-            } else {
-                qs = R.W[j] - (dxtheta + ksi) * R.D[j];
+#pragma unroll
+        for (int n = 0; n < PER; ++n) {
+            const int j = tid + n * bs;
+            if (j < nz) {
+                const int jp = j == nz - 1 ? 0 : j + 1;
+                const int jm = j == 0 ? nz - 1 : j - 1;
+                D[j] = flux_limiter(W[jp] - W[j], W[j] - W[jm], mc) * half_invdx;
             }
-            f[n] = dxrad * qs * R.SS[j] * v;
         }
         __syncthreads();
-        n = 0;
-        for (int j = threadIdx.x; j < nz; j += blockDim.x, ++n) R.W[j] = f[n];
-        __syncthreads();
-        for (int j = threadIdx.x; j < nz; j += blockDim.x) {
-            const int jp = j == nz - 1 ? 0 : j + 1;
-            double varq = R.W[j];
-            varq -= R.W[jp];
-            Q[j] += varq * invsurf;
+#pragma unroll
+        for (int n = 0; n < PER; ++n) {
+            const int j = tid + n * bs;
+            if (j < nz) {
+                const int jm = j == 0 ? nz - 1 : j - 1;
+                const double vv = uniform ? vconst : v[n];
+                const double ksi = vv * dt;
+                const double qs = positive(vv) ? W[jm] + (dxtheta - ksi) * D[jm]
+                                               : W[j] - (dxtheta + ksi) * D[j];
+                f[n] = dxrad * qs * SS[j] * vv;
+            }
         }
         __syncthreads();
-    }
-    // sigma last: its specific quantity is exactly 1, so QRStar == 1
-    {
-        double f[8];
-        int n = 0;
-        for (int j = threadIdx.x; j < nz; j += blockDim.x, ++n) {
-            const double v = uniform ? vconst : R.V[j];
-            f[n] = dxrad * 1.0 * R.SS[j] * v;
+#pragma unroll
+        for (int n = 0; n < PER; ++n) {
+            const int j = tid + n * bs;
+            if (j < nz) W[j] = f[n];
         }
         __syncthreads();
-        n = 0;
-        for (int j = threadIdx.x; j < nz; j += blockDim.x, ++n) R.W[j] = f[n];
-        __syncthreads();
-        for (int j = threadIdx.x; j < nz; j += blockDim.x) {
-            const int jp = j == nz - 1 ? 0 : j + 1;
-            double varq = R.W[j];
-            varq -= R.W[jp];
-            R.S[j] += varq * invsurf;
+#pragma unroll
+        for (int n = 0; n < PER; ++n) {
+            const int j = tid + n * bs;
+            if (j < nz) {
+                const int jp = j == nz - 1 ? 0 : j + 1;
+                Q[j] += (W[j] - W[jp]) * invsurf;
+            }
         }
         __syncthreads();
     }
+    // sigma: its specific quantity is exactly 1, so QRStar == 1
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = tid + n * bs;
+        if (j < nz) W[j] = dxrad * SS[j] * (uniform ? vconst : v[n]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = tid + n * bs;
+        if (j < nz) {
+            const int jp = j == nz - 1 ? 0 : j + 1;
+            f[n] = S[j] + (W[j] - W[jp]) * invsurf;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = tid + n * bs;
+        if (j < nz) S[j] = f[n];
+    }
+    __syncthreads();
 }
 
-__global__ void k_transport_azimuthal(Geo g, Tables t, double dt, int mc, int fast, int nq,
+template <int PER>
+__global__ void __launch_bounds__(512) k_transport_azimuthal(Geo g, Tables t, double dt, int mc,
+                                                             int fast, int nq,
                                       const double *__restrict__ vaz, double *mom0, double *mom1,
                                       double *mom2, double *mom3, double *E, double *S,
                                       double *ring_ws)
@@ -724,54 +801,70 @@ __global__ void k_transport_azimuthal(Geo g, Tables t, double dt, int mc, int fa
     __shared__ double red[33];
     const int nz = g.nz;
     const int i = blockIdx.x;
+    const int tid = threadIdx.x, bs = blockDim.x;
     const size_t row = (size_t)i * nz;
-    double *base = ring_ws ? ring_ws + (size_t)i * 5 * nz : smem;
-    RingArrays R{base, base + nz, base + 2 * nz, base + 3 * nz, base + 4 * nz};
+    double *base = ring_ws ? ring_ws + (size_t)i * 4 * nz : smem;
+    double *Sr = base, *SS = base + nz, *W = base + 2 * nz, *D = base + 3 * nz;
 
     // compute_average_azimuthal_velocity, :174-189
+    double vown[PER];
     double part = 0.0;
-    for (int j = threadIdx.x; j < nz; j += blockDim.x) part += vaz[row + j];
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = tid + n * bs;
+        if (j < nz) {
+            vown[n] = vaz[row + j];
+            part += vown[n];
+        }
+    }
     const double vmean = block_sum(part, red) / (double)nz;
-    // ComputeConstantResidual, :207-236
+    // ComputeConstantResidual, :207-236: FP64 shift phase of the ring
     const double Ntilde = vmean * t.InvRmed[i] * dt * g.invdphi;
     const double Nround = floor(Ntilde + 0.5);
     const int nshift = (int)Nround;
     const double invdt = 1.0 / dt;
     const double vt = (Ntilde - Nround) * t.Rmed[i] * invdt * g.dphi;
-    for (int j = threadIdx.x; j < nz; j += blockDim.x) {
-        double vres = vaz[row + j] - vmean;
-        if (!fast) vres = vt + vres;
-        R.V[j] = vres;
-        R.S[j] = S[row + j];
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = tid + n * bs;
+        if (j < nz) {
+            double vres = vown[n] - vmean;
+            if (!fast) vres = vt + vres;
+            vown[n] = vres;
+            Sr[j] = S[row + j];
+        }
     }
     __syncthreads();
 
-    double *qptr[5] = {mom0, mom1, mom2, mom3, E};
+    double *qrow[5] = {mom0 + row, mom1 + row, mom2 + row, mom3 + row, E + row};
     const double dxtheta = g.dphi * t.Rmed[i];
-    const double invdxtheta = 1.0 / dxtheta;
+    const double half_invdx = 0.5 * (1.0 / dxtheta);
     const double dxrad = (t.Rsup[i] - t.Rinf[i]) * dt;
     const double invsurf = t.InvSurf[i];
-    ring_advection_pass(R, qptr, nq, row, dt, dxtheta, invdxtheta, dxrad, invsurf, nz, mc, false,
-                        0.0);
+    ring_advection_pass<PER>(Sr, SS, W, D, qrow, nq, vown, dt, dxtheta, half_invdx, dxrad,
+                             invsurf, nz, mc, false, 0.0);
     if (fast) {
-        ring_advection_pass(R, qptr, nq, row, dt, dxtheta, invdxtheta, dxrad, invsurf, nz, mc,
-                            true, vt);
+        ring_advection_pass<PER>(Sr, SS, W, D, qrow, nq, vown, dt, dxtheta, half_invdx, dxrad,
+                                 invsurf, nz, mc, true, vt);
     }
     // AdvectSHIFT of every quantity, sigma last
     for (int q = 0; q <= nq; ++q) {
-        double *Q = q < nq ? qptr[q] + row : nullptr;
-        if (Q) {
-            for (int j = threadIdx.x; j < nz; j += blockDim.x) R.W[j] = Q[j];
-        } else {
-            for (int j = threadIdx.x; j < nz; j += blockDim.x) R.W[j] = R.S[j];
+        double *Q = q < nq ? qrow[q] : S + row;
+        const double *src = q < nq ? qrow[q] : Sr;
+#pragma unroll
+        for (int n = 0; n < PER; ++n) {
+            const int j = tid + n * bs;
+            if (j < nz) W[j] = src[j];
         }
         __syncthreads();
-        double *out = Q ? Q : S + row;
-        for (int j = threadIdx.x; j < nz; j += blockDim.x) {
-            int ji = j - nshift;
-            ji %= nz;
-            if (ji < 0) ji += nz;
-            out[j] = R.W[ji];
+#pragma unroll
+        for (int n = 0; n < PER; ++n) {
+            const int j = tid + n * bs;
+            if (j < nz) {
+                int ji = (j - nshift) % nz;
+                if (ji < 0) ji += nz;
+                Q[j] = W[ji];
+            }
         }
         __syncthreads();
     }
@@ -804,11 +897,11 @@ __global__ void k_finish(Geo g, Tables t, Phys ph, double omf, const double *__r
         vr_out[c] = 0.0;
     } else {
         const size_t cm = CELL(i - 1, j);
-        vr_out[c] = (mom0[cm] + mom1[c]) / (S_t[cm] + s);
+        vr_out[c] = fast_div(mom0[cm] + mom1[c], S_t[cm] + s);
     }
     const int jm = jprev(j, nz);
     const size_t cjm = CELL(i, jm);
-    vaz_out[c] = (mom2[cjm] + mom3[c]) / (S_t[cjm] + s) * t.InvRmed[i] - t.Rmed[i] * omf;
+    vaz_out[c] = fast_div(mom2[cjm] + mom3[c], S_t[cjm] + s) * t.InvRmed[i] - t.Rmed[i] * omf;
     const double sf = s < ph.sigma_min ? ph.sigma_min : s;
     S_out[c] = sf;
     if (ph.adiabatic) E_out[c] = temperature_floor(E_t[c], sf, ph);
@@ -915,9 +1008,10 @@ __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const 
             const double sg = S[c];
             if (ph.adiabatic) {
                 const double e = E[c];
-                T[c] = ph.c_v_inv * e / sg;
-                c_s = sqrt(ph.g_gm1 * e / sg);
-                const double h = c_s / ph.sqrt_gamma * t.InvOmegaK[i];
+                const double es = fast_div(e, sg);
+                T[c] = ph.c_v_inv * es;
+                c_s = sqrt(ph.g_gm1 * es);
+                const double h = c_s * t.HFacAdi[i];
                 cs[c] = c_s;
                 H[c] = h;
                 P[c] = ph.gm1 * e;
@@ -929,7 +1023,7 @@ __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const 
                 if (mode & 2) {
                     cs[c] = c_s;
                     H[c] = h;
-                    T[c] = ph.mu / ph.Rgas * P[c] / sg;
+                    T[c] = ph.mu / ph.Rgas * P[c] / sg;  // init only
                 }
                 n = ph.alpha > 0 ? ph.alpha * h * c_s : ph.constant_viscosity;
             }
@@ -941,9 +1035,9 @@ __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const 
         if (cfl_ring) {
             const double va = vaz[c];
             const double vres = ph.fast_transport ? va - vm0 : va;
-            const double invdt1 = c_s / cell;
-            const double invdt2 = vr[c] / dxR;
-            const double invdt3 = vres / dxA;
+            const double invdt1 = c_s * t.InvCell[i];
+            const double invdt2 = vr[c] * t.InvDiffRsup[i];
+            const double invdt3 = vres * t.InvDxTheta[i];
             const double vr1 = vr[c + nz];
             const double va1 = vaz[row + (j == nz - 1 ? 0 : j + 1)];
             double invdt4;
@@ -952,8 +1046,8 @@ __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const 
                 double dvA = va1 - va;
                 dvR = dvR > 0.0 ? 0.0 : -dvR;
                 dvA = dvA > 0.0 ? 0.0 : -dvA;
-                const double a = dvR / dxR, b = dvA / dxA;
-                invdt4 = ph.four_C2 * (a > b ? a : b);
+                const double a = dvR * t.InvDiffRsup[i], b = dvA * t.InvDxTheta[i];
+                invdt4 = ph.four_C2 * (dbits(a) > dbits(b) ? a : b);
             } else {
                 const double eps_rr = (vr1 - vr[c]) * t.InvDiffRsup[i];
                 const double eps_pp = t.InvRmed[i] * ((va1 - va) * g.invdphi + 0.5 * (vr1 + vr[c]));
@@ -961,15 +1055,16 @@ __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const 
                 const double mdiv = -(d < 0.0 ? d : 0.0);
                 invdt4 = ph.four_C2 * mdiv;
             }
-            const double invdt5 = 4.0 * n / (cell * cell);
+            const double invdt5 = 4.0 * n * t.InvCell2[i];
             double invdt6 = 0.0;
             if (ph.adiabatic) {
-                invdt6 = ph.inv_hc_limit * fabs((qplus[c] - qminus[c]) / E[c]);
+                invdt6 = ph.inv_hc_limit * fabs(fast_div(qplus[c] - qminus[c], E[c]));
             }
             const double dt_cell =
-                ph.cfl / sqrt(invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 +
-                              invdt4 * invdt4 + invdt5 * invdt5 + invdt6 * invdt6);
-            local = fmin(local, dt_cell);
+                fast_div(ph.cfl, sqrt(invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 +
+                                      invdt4 * invdt4 + invdt5 * invdt5 + invdt6 * invdt6));
+            // positive doubles order like their bit patterns
+            if (dbits(dt_cell) < dbits(local)) local = dt_cell;
         }
     }
     if (do_cfl) {
@@ -1006,12 +1101,15 @@ __global__ void k_disk_force(Geo g, Tables t, Phys ph, double px, double py, dou
         const double dx = xc - px, dy = yc - py;
         const double d2 = dx * dx + dy * dy;
         const double dsm2 = d2 + smooth * smooth;
-        const double dsm = sqrt(dsm2);
-        const double inv3 = 1.0 / (dsm2 * dsm);
+        const double rinv = rsqrt(dsm2);
+        const double inv3 = rinv * rinv * rinv;
         double fk = 1.0;
-        if (rsm > 0.0 && dsm < rsm) {
-            const double q = dsm / rsm;
-            fk = -(3.0 * pow(q, 4.0) - 4.0 * pow(q, 3.0));
+        if (rsm > 0.0) {
+            const double dsm = dsm2 * rinv;
+            if (dsm < rsm) {
+                const double q = dsm / rsm;
+                fk = -(3.0 * (q * q * q * q) - 4.0 * (q * q * q));
+            }
         }
         ax += ph.G * cellmass * dx * inv3 * fk;
         ay += ph.G * cellmass * dy * inv3 * fk;
@@ -1124,12 +1222,23 @@ void launch_transport_radial(const Launch &L, double dt, double omf, int chunk, 
     }
 }
 
-size_t azimuthal_smem_bytes(int nz) { return (size_t)5 * nz * sizeof(double); }
+size_t azimuthal_smem_bytes(int nz) { return (size_t)4 * nz * sizeof(double); }
+
+// Cells per thread of the azimuthal kernel: blocks stay at <= 512 threads so
+// that the per-thread cell arrays fit 128 registers.
+int azimuthal_cells_per_thread(int nz) { return nz <= 2048 ? 4 : (nz <= 4096 ? 8 : 16); }
 
 cudaError_t prepare_azimuthal(size_t smem)
 {
-    return cudaFuncSetAttribute(k_transport_azimuthal,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_transport_azimuthal<4>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_transport_azimuthal<8>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_transport_azimuthal<16>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return e;
 }
 
 void launch_transport_azimuthal(const Launch &L, double dt, int block, double *const mom[4],
@@ -1137,9 +1246,20 @@ void launch_transport_azimuthal(const Launch &L, double dt, int block, double *c
                                 size_t smem)
 {
     const int nq = L.ph.adiabatic ? 5 : 4;
-    k_transport_azimuthal<<<L.g.nr, block, ring_ws ? 0 : smem, L.stream>>>(
-        L.g, L.t, dt, L.ph.limiter_mc, L.ph.fast_transport, nq, vaz, mom[0], mom[1], mom[2],
-        mom[3], E, S, ring_ws);
+    const size_t dyn = ring_ws ? 0 : smem;
+    const int per = azimuthal_cells_per_thread(L.g.nz);
+#define AZ_LAUNCH(P)                                                                          \
+    k_transport_azimuthal<P><<<L.g.nr, block, dyn, L.stream>>>(                               \
+        L.g, L.t, dt, L.ph.limiter_mc, L.ph.fast_transport, nq, vaz, mom[0], mom[1], mom[2], \
+        mom[3], E, S, ring_ws)
+    if (per == 4) {
+        AZ_LAUNCH(4);
+    } else if (per == 8) {
+        AZ_LAUNCH(8);
+    } else {
+        AZ_LAUNCH(16);
+    }
+#undef AZ_LAUNCH
 }
 
 void launch_finish(const Launch &L, double omf, double *const mom[4], const double *S_t,

@@ -54,9 +54,9 @@ def test_gpu_vs_oracle_cfl_steps(adiabatic, nrad, naz):
     assert abs(g.total_mass() - o.total_mass()) <= 1e-13 * abs(o.total_mass())
 
 
-@pytest.mark.parametrize("naz", [1536, 6144])
+@pytest.mark.parametrize("naz", [1536, 7680])
 def test_azimuthal_kernel_variants(naz):
-    # naz = 1536 runs the ring in > 48 KB of shared memory, 6144 in the
+    # naz = 1536 runs the ring in > 48 KB of shared memory, 7680 in the
     # global per-ring workspace
     params, d = make_params(8, naz, adiabatic=True)
     (o, dto), (g, dtg) = run_both(params, d, steps=3, planet=False)
