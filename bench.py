@@ -181,6 +181,87 @@ def workload_config(name):
             "l2": "flushed (256 MB write) before every timed step"}
 
 
+def measure(args, precision, cfg_name, torch, dist, local):
+    """Times `args.steps` steps of one precision form; returns a dict."""
+    from fargocpt_gb300 import setups
+    from fargocpt_gb300.abi import params_from_dict
+    from fargocpt_gb300.engine import Engine
+
+    params, d, radii, fields, nbody = setups.build(cfg_name)
+    if precision == "fp32":
+        d = dict(d)
+        d["precision"] = 1
+        params = params_from_dict(d)
+    eng = Engine(params, radii)
+    load_disk(eng, fields, nbody)
+    cells = d["nrad"] * d["naz"]
+    stream = torch.cuda.ExternalStream(eng.stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    state = {"t": 0.0}
+
+    def one_step(timed_events=None):
+        t = state["t"]
+        dt = eng.condition_cfl()
+        b = nbody.bodies(t)
+        ix, iy = nbody.indirect(b)
+        eng.set_bodies(b, ix, iy, 0.0)
+        if timed_events is not None:
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                timed_events[0].record(stream)
+        eng.step_euler(dt, t)
+        if timed_events is not None:
+            timed_events[1].record(stream)
+        eng.disk_on_planet_accel(1)
+        state["t"] = t + dt
+
+    for _ in range(args.warmup):
+        one_step()
+    eng.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        one_step(ev[k])
+    eng.synchronize()
+    torch.cuda.synchronize()
+    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+    if dist is not None:
+        dist.barrier()
+    eng.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        one_step()
+    eng.synchronize()
+    e2e_s = time.perf_counter() - t0
+    eng.set_phase_timing(True)
+    for _ in range(args.steps):
+        one_step()
+    phases, nsteps = eng.phase_times()
+    eng.set_phase_timing(False)
+    assert eng.check_finite() is None, "non-finite state after the benchmark"
+    return dict(total_ms=total_ms, e2e_s=e2e_s, phases=phases, nsteps=nsteps, cells=cells, d=d)
+
+
+def roofline(res, steps, bytes_scale):
+    peak, peak_src = peaks()
+    phases, nsteps, cells, d = res["phases"], res["nsteps"], res["cells"], res["d"]
+    dom = max(phases, key=phases.get)
+    dom_ms = phases[dom] / max(1, nsteps)
+    bpc = KERNEL_BYTES_PER_CELL.get(dom, 0) * bytes_scale
+    achieved = bpc * cells / (dom_ms * 1e-3) / 1e9
+    kind = "adiabatic" if d["eos"] == 1 else "isothermal"
+    sbpc = STEP_BYTES_PER_CELL[kind] * bytes_scale
+    step_achieved = sbpc * cells * steps / (res["total_ms"] * 1e-3) / 1e9
+    return ({"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+             "frac": achieved / peak, "peak_source": peak_src, "traffic": None,
+             "bytes_per_cell": bpc, "ms_per_launch": dom_ms},
+            {"achieved": step_achieved, "peak": peak, "unit": "GB/s",
+             "frac": step_achieved / peak, "bytes_per_cell": sbpc})
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -196,7 +277,6 @@ def main():
             dist.barrier()
         return
 
-    import numpy as np
     import torch
 
     from fargocpt_gb300.build import build
@@ -205,107 +285,50 @@ def main():
     if dist is not None:
         dist.barrier()
     torch.cuda.set_device(local)
-    from fargocpt_gb300 import setups
-    from fargocpt_gb300.engine import Engine
 
-    params, d, radii, fields, nbody = setups.build(args.config)
-    eng = Engine(params, radii)
-    load_disk(eng, fields, nbody)
-    cells = d["nrad"] * d["naz"]
-    stream = torch.cuda.ExternalStream(eng.stream)
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-
-    t = 0.0
-
-    def one_step(timed_events=None):
-        nonlocal t
-        dt = eng.condition_cfl()
-        b = nbody.bodies(t)
-        ix, iy = nbody.indirect(b)
-        eng.set_bodies(b, ix, iy, 0.0)
-        if timed_events is not None:
-            with torch.cuda.stream(stream):
-                flush.zero_()
-                timed_events[0].record(stream)
-        eng.step_euler(dt, t)
-        if timed_events is not None:
-            timed_events[1].record(stream)
-        eng.disk_on_planet_accel(1)
-        t += dt
-
-    for _ in range(args.warmup):
-        one_step()
-    eng.synchronize()
-
-    # device time of the steps, L2 flushed before each
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
     sampler = ClockSampler(local)
-    if dist is not None:
-        dist.barrier()
-    torch.cuda.synchronize()
     sampler.start()
-    for k in range(args.steps):
-        one_step(ev[k])
-    eng.synchronize()
-    torch.cuda.synchronize()
-    step_ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms = sum(step_ms)
-
-    # end to end through the C ABI: the drop-in call sequence, wall clock
-    if dist is not None:
-        dist.barrier()
-    eng.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        one_step()
-    eng.synchronize()
-    e2e_s = time.perf_counter() - t0
+    r64 = measure(args, "fp64", args.config, torch, dist, local)
+    r32 = measure(args, "fp32", args.config, torch, dist, local)
     clocks = sampler.stop()
 
-    # per-kernel time of the same steps (phase timing on)
-    eng.set_phase_timing(True)
-    for _ in range(args.steps):
-        one_step()
-    phases, nsteps = eng.phase_times()
-    eng.set_phase_timing(False)
-    assert eng.check_finite() is None, "non-finite state after the benchmark"
-
+    vals = [r64["total_ms"], r64["e2e_s"], r32["total_ms"], r32["e2e_s"]]
     if dist is not None:
-        tt = torch.tensor([total_ms, e2e_s], device="cuda", dtype=torch.float64)
+        tt = torch.tensor(vals, device="cuda", dtype=torch.float64)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms, e2e_s = float(tt[0]), float(tt[1])
+        vals = [float(x) for x in tt]
     if rank != 0:
         return
-
-    value = world * cells * args.steps / (total_ms * 1e-3)
-    e2e = world * cells * args.steps / e2e_s
-    peak, peak_src = peaks()
-    dom = max(phases, key=phases.get)
-    dom_ms = phases[dom] / max(1, nsteps)
-    dom_bytes = KERNEL_BYTES_PER_CELL.get(dom, 0) * cells
-    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
-    kind = "adiabatic" if d["eos"] == 1 else "isothermal"
-    step_achieved = STEP_BYTES_PER_CELL[kind] * cells * args.steps / (total_ms * 1e-3) / 1e9
+    cells = r64["cells"]
+    value = world * cells * args.steps / (vals[0] * 1e-3)
+    e2e = world * cells * args.steps / vals[1]
+    value32 = world * cells * args.steps / (vals[2] * 1e-3)
+    e2e32 = world * cells * args.steps / vals[3]
+    rl, rls = roofline(r64, args.steps, 1.0)
+    rl32, rls32 = roofline(r32, args.steps, 0.5)
     line = {
         "metric": "cell-updates/s/GPU, plain FP64 vs mixed-precision & batched at stated error",
         "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": vals[0] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(args.config),
         "e2e": {"value": e2e, "unit": "cell-updates/s",
-                "h2d_bytes_per_step": 2 * 40,   # fgpu_body x2 passed as kernel arguments
+                "h2d_bytes_per_step": 2 * 40,   # fgpu_body x2, passed as kernel arguments
                 "d2h_bytes_per_step": 8 + 40},  # CFL dt + disk-force partial sums
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
-                     "traffic": None,
-                     "bytes_per_cell": KERNEL_BYTES_PER_CELL.get(dom, 0),
-                     "ms_per_launch": dom_ms},
-        "roofline_step": {"achieved": step_achieved, "peak": peak, "unit": "GB/s",
-                          "frac": step_achieved / peak,
-                          "bytes_per_cell": STEP_BYTES_PER_CELL[kind]},
-        "phase_ms_per_step": {k: v / max(1, nsteps) for k, v in phases.items()},
-        "gpu_launches": args.steps * KERNELS_PER_STEP,
+        "roofline": rl,
+        "roofline_step": rls,
+        "phase_ms_per_step": {k: v / max(1, r64["nsteps"]) for k, v in r64["phases"].items()},
+        "fp32_mixed": {
+            "value": value32, "unit": "cell-updates/s", "ms_per_step": vals[2] / args.steps,
+            "e2e": {"value": e2e32, "unit": "cell-updates/s", "h2d_bytes_per_step": 80,
+                    "d2h_bytes_per_step": 4 + 40},
+            "speedup_vs_fp64": value32 / value,
+            "roofline": rl32, "roofline_step": rls32,
+            "phase_ms_per_step": {k: v / max(1, r32["nsteps"])
+                                  for k, v in r32["phases"].items()},
+            "error": "see python -m fargocpt_gb300.accuracy (relative L1/Linf vs FP64)",
+        },
+        "gpu_launches": 2 * args.steps * KERNELS_PER_STEP,
         "clocks": clocks,
     }
     if not args.no_cpu_baseline:

@@ -7,6 +7,7 @@
 #include "../../include/fargocpt_gb300.h"
 #include "hydro.cuh"
 #include "kernels.h"
+#include "fp32_engine.h"
 
 #include <cuda_runtime.h>
 
@@ -57,6 +58,8 @@ struct fgpu_engine {
     std::vector<std::vector<cudaEvent_t>> ev_rows;
     std::vector<cudaEvent_t> ev_free;
     int ev_cursor = 0;
+
+    fgpu32::Engine32 *e32 = nullptr;  // FP32-mixed form, when selected
 };
 
 static const char *kPhaseNames[] = {
@@ -179,7 +182,7 @@ static int validate(const fgpu_params *p, std::string &why)
     if (p->eos != FGPU_EOS_ISOTHERMAL && p->eos != FGPU_EOS_IDEAL) { why = "eos"; return FGPU_ERR_BAD_ARG; }
     if (p->art_visc == FGPU_ARTVISC_TW) { why = "Tscharnuter-Winkler artificial viscosity is not on the GPU path"; return FGPU_ERR_UNSUPPORTED; }
     if (p->art_visc != FGPU_ARTVISC_NONE && p->art_visc != FGPU_ARTVISC_SN) { why = "art_visc"; return FGPU_ERR_BAD_ARG; }
-    if (p->precision != FGPU_PRECISION_FP64) { why = "only the FP64 precision form is built"; return FGPU_ERR_UNSUPPORTED; }
+    if (p->precision != FGPU_PRECISION_FP64 && p->precision != FGPU_PRECISION_FP32_MIXED) { why = "precision"; return FGPU_ERR_BAD_ARG; }
     if (p->radial_spacing != FGPU_SPACING_LOGARITHMIC && p->radial_spacing != FGPU_SPACING_ARITHMETIC) { why = "radial_spacing"; return FGPU_ERR_BAD_ARG; }
     const int bcs[8] = {p->bc_sigma_inner, p->bc_sigma_outer, p->bc_energy_inner, p->bc_energy_outer,
                         p->bc_vrad_inner, p->bc_vrad_outer, p->bc_vaz_inner, p->bc_vaz_outer};
@@ -399,6 +402,31 @@ extern "C" int fgpu_create(const fgpu_params *params, const double *radii, fgpu_
         eng->err = "stream";
         return fail(FGPU_ERR_CUDA);
     }
+    if (params->precision == FGPU_PRECISION_FP32_MIXED) {
+        rc = setup_tables(eng, radii);
+        if (rc != FGPU_OK) return fail(rc);
+        eng->e32 = new (std::nothrow) fgpu32::Engine32();
+        if (!eng->e32) return fail(FGPU_ERR_OOM);
+        for (int q = 0; q < 4; ++q) {
+            const DampQ &d = eng->dm.q[q];
+            fgpu32::DampQSpec &sp = eng->e32->damp_spec[q];
+            sp.kind_in = d.kind_in; sp.kind_out = d.kind_out;
+            sp.active_in = d.active_in; sp.active_out = d.active_out;
+            sp.limit_in = d.limit_in; sp.limit_out = d.limit_out;
+            sp.tau_in = d.tau_in; sp.tau_out = d.tau_out;
+        }
+        eng->e32->mark_fn = [](void *ctx, int k) { mark((fgpu_engine *)ctx, k); };
+        eng->e32->mark_ctx = eng;
+        rc = eng->e32->create(*params, radii, eng->stream);
+        if (rc != FGPU_OK) {
+            eng->err = eng->e32->err;
+            return fail(rc);
+        }
+        *out = eng;
+        return FGPU_OK;
+    }
+    int rc2 = FGPU_OK;
+    (void)rc2;
     for (int f = 0; f < FGPU_FIELD_COUNT; ++f) {
         const size_t n = (size_t)field_rows(eng, f) * eng->nz;
         if (cudaMalloc(&eng->field[f], n * sizeof(double)) != cudaSuccess) {
@@ -464,6 +492,10 @@ extern "C" int fgpu_destroy(fgpu_engine *eng)
 {
     if (!eng) return FGPU_ERR_BAD_ARG;
     if (eng->stream) cudaStreamSynchronize(eng->stream);
+    if (eng->e32) {
+        eng->e32->destroy();
+        delete eng->e32;
+    }
     for (auto &row : eng->ev_rows)
         for (auto ev : row) cudaEventDestroy(ev);
     for (auto ev : eng->ev_free) cudaEventDestroy(ev);
@@ -522,6 +554,11 @@ extern "C" int fgpu_upload_field(fgpu_engine *eng, int field, const double *host
         eng->err = "upload_field: shape mismatch";
         return FGPU_ERR_BAD_ARG;
     }
+    if (eng->e32) {
+        int rc = eng->e32->upload(field, host, rows);
+        if (rc) eng->err = eng->e32->err;
+        return rc;
+    }
     CK(cudaMemcpyAsync(eng->field[field], host, sizeof(double) * (size_t)rows * cols,
                        cudaMemcpyHostToDevice, eng->stream));
     CK(cudaStreamSynchronize(eng->stream));
@@ -535,6 +572,11 @@ extern "C" int fgpu_download_field(fgpu_engine *eng, int field, double *host, in
     if (rows != field_rows(eng, field) || cols != eng->nz) {
         eng->err = "download_field: shape mismatch";
         return FGPU_ERR_BAD_ARG;
+    }
+    if (eng->e32) {
+        int rc = eng->e32->download(field, host, rows);
+        if (rc) eng->err = eng->e32->err;
+        return rc;
     }
     CK(cudaMemcpyAsync(host, eng->field[field], sizeof(double) * (size_t)rows * cols,
                        cudaMemcpyDeviceToHost, eng->stream));
@@ -558,6 +600,13 @@ extern "C" int fgpu_set_bodies(fgpu_engine *eng, int n, const fgpu_body *bodies,
     b.ix = ix;
     b.iy = iy;
     b.omega_frame = omega_frame;
+    if (eng->e32) {
+        if (omega_frame != 0.0) {
+            eng->err = "the FP32-mixed form runs in the fixed (non-rotating) frame";
+            return FGPU_ERR_UNSUPPORTED;
+        }
+        eng->e32->set_bodies(n, bodies, ix, iy);
+    }
     return FGPU_OK;
 }
 
@@ -572,9 +621,17 @@ static double beta_inv_at(const fgpu_params &p, double t)
     return beta_inv;
 }
 
+#define ROUTE32(expr)                           \
+    if (eng->e32) {                             \
+        int rc_ = (expr);                       \
+        if (rc_) eng->err = eng->e32->err;      \
+        return rc_;                             \
+    }
+
 extern "C" int fgpu_init_euler(fgpu_engine *eng, double t)
 {
     if (!eng) return FGPU_ERR_BAD_ARG;
+    ROUTE32(eng->e32->init_euler(t));
     Launch L = launch_of(eng);
     State s = state_of(eng);
     launch_derived_cfl(L, 1 | 2, s, nullptr);
@@ -591,6 +648,7 @@ extern "C" int fgpu_recalculate_derived(fgpu_engine *eng, double t)
 {
     (void)t;
     if (!eng) return FGPU_ERR_BAD_ARG;
+    ROUTE32(eng->e32->derived_cfl(1));
     Launch L = launch_of(eng);
     launch_derived_cfl(L, 1, state_of(eng), nullptr);
     eng->cfl_valid = false;
@@ -600,6 +658,7 @@ extern "C" int fgpu_recalculate_derived(fgpu_engine *eng, double t)
 extern "C" int fgpu_condition_cfl(fgpu_engine *eng, double *dt_out)
 {
     if (!eng || !dt_out) return FGPU_ERR_BAD_ARG;
+    ROUTE32(eng->e32->cfl(dt_out));
     if (!eng->cfl_valid) {
         CK(cudaMemsetAsync(eng->d_dtmin, 0x7f, sizeof(unsigned long long), eng->stream));
         launch_derived_cfl(launch_of(eng), 4, state_of(eng), eng->d_dtmin);
@@ -623,6 +682,7 @@ extern "C" int fgpu_apply_boundary_condition(fgpu_engine *eng, double t, double 
 {
     (void)t;
     if (!eng) return FGPU_ERR_BAD_ARG;
+    ROUTE32(eng->e32->boundary(dt, final != 0));
     Launch L = launch_of(eng);
     if (final && eng->p.damping) {
         launch_damping(L, eng->dm, dt, eng->damp_rings, eng->n_damp_rings, state_of(eng));
@@ -635,6 +695,7 @@ extern "C" int fgpu_apply_boundary_condition(fgpu_engine *eng, double t, double 
 extern "C" int fgpu_step_euler(fgpu_engine *eng, double dt, double t)
 {
     if (!eng || !(dt > 0.0)) return FGPU_ERR_BAD_ARG;
+    ROUTE32(eng->e32->step(dt, t));
     Launch L = launch_of(eng);
     const double omf = eng->bodies.omega_frame;
     double **f = eng->field;
@@ -701,6 +762,17 @@ extern "C" int fgpu_disk_on_planet_accel(fgpu_engine *eng, int k, double accel[2
 {
     if (!eng || !accel || k < 0 || k >= eng->bodies.n) return FGPU_ERR_BAD_ARG;
     const Bodies &b = eng->bodies;
+    if (eng->e32) {
+        double o[5];
+        int rc = eng->e32->disk_force(b.x[k], b.y[k], b.a[k], b.rsm[k], o);
+        if (rc) {
+            eng->err = eng->e32->err;
+            return rc;
+        }
+        accel[0] = o[0] + o[2];
+        accel[1] = o[1] + o[3];
+        return FGPU_OK;
+    }
     // inner/outer split at the body's distance from the origin (t_planet::get_r);
     // the cubic smoothing radius is the same r_sm the gas feels
     launch_disk_force(launch_of(eng), b.x[k], b.y[k], b.a[k], b.rsm[k], eng->field[FGPU_SIGMA],
@@ -718,6 +790,13 @@ extern "C" int fgpu_disk_on_planet_accel(fgpu_engine *eng, int k, double accel[2
 extern "C" int fgpu_total_mass(fgpu_engine *eng, double *mass)
 {
     if (!eng || !mass) return FGPU_ERR_BAD_ARG;
+    if (eng->e32) {
+        double o[5];
+        int rc = eng->e32->disk_force(0.0, 0.0, 0.0, 0.0, o);
+        if (rc) eng->err = eng->e32->err;
+        *mass = o[4];
+        return rc;
+    }
     launch_disk_force(launch_of(eng), 0.0, 0.0, 0.0, 0.0, eng->field[FGPU_SIGMA],
                       eng->field[FGPU_SCALE_HEIGHT], eng->partial, eng->red_out);
     int rc = check_launch(eng);
@@ -732,6 +811,7 @@ extern "C" int fgpu_total_mass(fgpu_engine *eng, double *mass)
 extern "C" int fgpu_check_finite(fgpu_engine *eng, int *field, int *nr, int *naz)
 {
     if (!eng) return FGPU_ERR_BAD_ARG;
+    ROUTE32(eng->e32->check_finite(field, nr, naz));
     const int fields[4] = {FGPU_SIGMA, FGPU_V_RADIAL, FGPU_V_AZIMUTHAL, FGPU_ENERGY};
     Launch L = launch_of(eng);
     for (int k = 0; k < 4; ++k) {

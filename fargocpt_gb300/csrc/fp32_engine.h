@@ -1,0 +1,139 @@
+// FP32-mixed form of the hydro step: device structures and the host engine
+// (kernels_fp32.cu).  The C ABI (api.cu) routes a handle created with
+// precision = FGPU_PRECISION_FP32_MIXED here.
+#pragma once
+
+#include "../../include/fargocpt_gb300.h"
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include <string>
+
+namespace fgpu32 {
+
+constexpr int kMaxBodies = 16;
+
+struct GeoF {
+    int nr, nz;
+    float dphi, invdphi;
+    double dphi_d, invdphi_d;
+};
+
+// Per-ring tables in FP32, plus the FP64 values the FP64 islands need.
+struct TablesF {
+    const float *Rinf, *Rsup, *Rmed, *Surf, *InvRmed, *InvSurf, *InvDiffRmed, *InvDiffRsup,
+        *InvDiffRsupRb, *InvRinf, *RinfSq, *TwoOverDRa2, *OmegaK, *InvOmegaK, *CsIso,
+        *InvDxSrc, *InvDxTheta, *EModel, *HFacAdi, *InvCell, *InvCell2, *TwoOverRmedSum;
+    // Keplerian reference terms
+    const float *Kbal;      // (v_K face)^2 / Rinf - dPhi_K/dr at interface i
+    const float *Aface;     // 0.5 (v_K(i) + v_K(i-1))
+    const float *Shear;     // d(v_K / r)/dr at interface i
+    const float *DJ;        // J_K(i-1) - J_K(i), J_K = r v_K
+    const float *JSlope;    // (J_K(i+1) - J_K(i)) / (Rmed(i+1) - Rmed(i))
+    const float *DRmed;     // Rmed(i) - Rmed(i-1)
+    const float *OmRefDiff; // v_K(i)/R(i) - v_K(i+1)/R(i+1)
+    const float *Vref;      // v_K(Rmed)
+    const double *Rmed_d, *InvRmed_d, *Vref_d, *Surf_d, *PhiK_d, *cos_d, *sin_d;
+};
+
+struct PhysF {
+    int adiabatic, art_visc_sn, dissipation, limiter_mc, fast_transport;
+    int heating_viscous, cooling_beta, beta_ref;
+    float gm1, g_gm1, mu, alpha, constant_viscosity, C2, four_C2, rvf, hvf, cfl, inv_hc_limit;
+    float sigma_min, sigma_floor10, eps_smooth, c_v_inv, mu_over_R, cool_const, mu_gm1_over_R;
+    float emin_fac, emax_fac;
+    double G_d;
+};
+
+struct BodiesF {
+    int n;
+    int star_at_origin;
+    double x[kMaxBodies], y[kMaxBodies], a[kMaxBodies];
+    float gm[kMaxBodies], rsm[kMaxBodies];
+    float gm_ref, ix, iy;
+};
+
+struct BcF {
+    int sigma_in, sigma_out, energy_in, energy_out, vr_in, vr_out, vaz_in, vaz_out;
+    float kep_in, kep_out;  // Keplerian-hook value of the residual
+    float zg_in, zg_out;    // zero-gradient offset of the residual between rings
+};
+
+struct DampQF {
+    int kind_in, kind_out, active_in, active_out, limit_in, limit_out, vector;
+    float tau_in, tau_out;
+    const float *fac_in, *fac_out;
+    const float *x0_zero_in, *x0_zero_out;  // per-ring X0 of the "zero" kind
+};
+struct DampingF {
+    DampQF q[4];
+};
+
+struct StateF {
+    float *sigma, *vr, *dv, *energy, *sigma0, *vr0, *dv0, *energy0;
+    float *sigma_lo;  // low part of the compensated sigma (sigma = sigma + sigma_lo)
+};
+
+// Damping ring set-up, computed by the FP64 set-up code (the same ring search).
+struct DampQSpec {
+    int kind_in = 0, kind_out = 0, active_in = 0, active_out = 0, limit_in = 0, limit_out = 0;
+    double tau_in = 1.0, tau_out = 1.0;
+};
+
+class Engine32 {
+  public:
+    int create(const fgpu_params &p, const double *radii, cudaStream_t stream);
+    void destroy();
+    int upload(int field, const double *host, int rows);
+    int download(int field, double *host, int rows);
+    void set_bodies(int n, const fgpu_body *b, double ix, double iy);
+    int init_euler(double t);
+    int derived_cfl(int mode);
+    int cfl(double *dt_out);
+    int boundary(double dt, bool final);
+    int step(double dt, double t);
+    int disk_force(double px, double py, double pa, double rsm, double out[5]);
+    int check_finite(int *field, int *nr_out, int *naz_out);
+
+    DampQSpec damp_spec[4];
+    std::string err;
+    // phase marker: called with -1 before the first kernel of a step and with
+    // the phase index after each phase (the FP64 form's phase list)
+    void (*mark_fn)(void *, int) = nullptr;
+    void *mark_ctx = nullptr;
+
+  private:
+    double beta_inv(double t) const;
+    const double *offset_of(int f) const;
+    StateF state();
+
+    fgpu_params p{};
+    cudaStream_t stream = nullptr;
+    int nr = 0, nz = 0;
+    size_t cells = 0, vcells = 0;
+    GeoF geo{};
+    TablesF tabs{};
+    PhysF phys{};
+    BodiesF bodies{};
+    BcF bc{};
+    DampingF dm{};
+    float *fld[FGPU_FIELD_COUNT] = {};
+    float *alt_sigma = nullptr, *alt_vr = nullptr, *alt_dv = nullptr, *alt_e = nullptr;
+    float *sigma_lo = nullptr, *alt_sigma_lo = nullptr;
+    float *mom[4] = {};
+    float *tab_f = nullptr;
+    double *tab_d = nullptr;
+    float *damp_mem = nullptr, *damp_aux = nullptr;
+    int *damp_rings = nullptr;
+    int n_rings = 0;
+    double *partial = nullptr, *red_out = nullptr, *stage = nullptr;
+    unsigned int *d_dtmin = nullptr;
+    unsigned long long *d_bad = nullptr;
+    double *h_pinned = nullptr;
+    int per = 4, az_block = 128;
+    size_t az_smem = 0;
+    bool cfl_valid = false;
+};
+
+}  // namespace fgpu32

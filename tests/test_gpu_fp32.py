@@ -1,0 +1,100 @@
+"""The FP32-mixed form (precision = FGPU_PRECISION_FP32_MIXED).
+
+Bars (relative, per field):
+* against the reference's FP64 snapshots (golden cases, <= 20 steps):
+  sigma, v_phi and e within 1e-5 L-infinity; v_r, a small difference of
+  large terms, within 1e-3 of its own maximum;
+* against the FP64 form on a 128 x 384 disk over 300 steps: sigma L1 <= 2e-6,
+  L-infinity <= 2e-5; v_phi residual about Keplerian L1 <= 5e-5;
+* the upload/download round trip keeps v_phi to FP32 precision of the
+  residual about Keplerian.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from golden_runner import CASES, EVOLVED, replay, rel_linf
+
+pytestmark = pytest.mark.gpu
+
+
+def _engine():
+    from fargocpt_gb300.engine import Engine
+    return Engine
+
+
+def rel_l1(a, b):
+    return float(np.sum(np.abs(a - b)) / np.sum(np.abs(b)))
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fp32_mixed_against_reference_snapshots(name):
+    snaps, times, torques, dts, arrays = replay(_engine(), name, {"precision": 1})
+    assert snaps
+    for n, fields in snaps.items():
+        for f in EVOLVED:
+            ref = arrays[f"s{n}_{f}"]
+            if not np.any(ref):
+                continue
+            err = rel_linf(fields[f], ref)
+            tol = 1e-3 if f == "V_RADIAL" else 1e-5
+            assert err <= tol, f"{name} snap {n} {f}: {err:.3e}"
+
+
+def test_fp32_mixed_against_fp64_form():
+    from fargocpt_gb300 import setups
+    from fargocpt_gb300.abi import params_from_dict
+    from fargocpt_gb300.engine import Engine
+
+    p64, d, radii, fields, nbody = setups.build("c1")
+    d32 = dict(d)
+    d32["precision"] = 1
+    engs = [Engine(p64, radii), Engine(params_from_dict(d32), radii)]
+    for e in engs:
+        for k, a in fields.items():
+            e.set_field(k, a)
+            e.set_field(k + "0", a)
+        b = nbody.bodies(0.0)
+        e.set_bodies(b, *nbody.indirect(b), 0.0)
+        e.init_euler(0.0)
+        e.apply_boundary_condition(0.0, 0.0, False)
+    t = 0.0
+    for _ in range(300):
+        dt = engs[0].condition_cfl()
+        b = nbody.bodies(t)
+        ix, iy = nbody.indirect(b)
+        for e in engs:
+            e.set_bodies(b, ix, iy, 0.0)
+            e.step_euler(dt, t)
+        t += dt
+    s64, s32 = engs[0].get_field("SIGMA"), engs[1].get_field("SIGMA")
+    assert rel_l1(s32, s64) <= 2e-6
+    assert rel_linf(s32, s64) <= 2e-5
+    nr = d["nrad"]
+    rinf, rsup = radii[:nr], radii[1:nr + 1]
+    rmed = 2.0 / 3.0 * (rsup ** 3 - rinf ** 3) / (rsup ** 2 - rinf ** 2)
+    vk = np.sqrt(1.0 / rmed)[:, None]
+    v64, v32 = engs[0].get_field("V_AZIMUTHAL"), engs[1].get_field("V_AZIMUTHAL")
+    assert rel_l1(v32 - vk, v64 - vk) <= 5e-5
+    assert engs[1].check_finite() is None
+
+
+def test_fp32_round_trip_keeps_residual_precision():
+    from fargocpt_gb300 import setups
+    from fargocpt_gb300.abi import params_from_dict
+    from fargocpt_gb300.engine import Engine
+
+    p64, d, radii, fields, nbody = setups.build("c1")
+    d32 = dict(d)
+    d32["precision"] = 1
+    e = Engine(params_from_dict(d32), radii)
+    v = fields["V_AZIMUTHAL"]
+    e.set_field("V_AZIMUTHAL", v)
+    back = e.get_field("V_AZIMUTHAL")
+    nr = d["nrad"]
+    rinf, rsup = radii[:nr], radii[1:nr + 1]
+    rmed = 2.0 / 3.0 * (rsup ** 3 - rinf ** 3) / (rsup ** 2 - rinf ** 2)
+    vk = np.sqrt(1.0 / rmed)[:, None]
+    res = v - vk
+    assert np.max(np.abs(back - v)) <= 1e-7 * np.max(np.abs(res))
