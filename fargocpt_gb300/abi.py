@@ -113,6 +113,37 @@ def params_to_dict(p: FgpuParams) -> dict:
     return out
 
 
+BATCH_KERNELS = ["potential", "source", "artvisc_q", "artvisc_v", "stress", "viscous",
+                 "ghost", "transport_radial", "transport_azimuthal", "finish", "damping",
+                 "derived_cfl"]
+
+
+class FgpuTile(C.Structure):
+    _fields_ = [("threads", C.c_int), ("rings", C.c_int)]
+
+
+class FgpuTiles(C.Structure):
+    _fields_ = [("k", FgpuTile * len(BATCH_KERNELS))]
+
+    def to_dict(self) -> dict:
+        return {n: [self.k[i].threads, self.k[i].rings] for i, n in enumerate(BATCH_KERNELS)}
+
+    @classmethod
+    def from_dict(cls, d: dict) -> "FgpuTiles":
+        t = cls()
+        for i, n in enumerate(BATCH_KERNELS):
+            t.k[i].threads, t.k[i].rings = int(d[n][0]), int(d[n][1])
+        return t
+
+
+class FgpuClock(C.Structure):
+    _fields_ = [("time", C.c_double), ("last_dt", C.c_double), ("t_end", C.c_double),
+                ("monitor_dt", C.c_double), ("cfl_max_var", C.c_double),
+                ("star_mass", C.c_double), ("n_monitor", C.c_int), ("steps", C.c_int),
+                ("active", C.c_int), ("n_planets", C.c_int), ("mass", C.c_double * 16),
+                ("a", C.c_double * 16), ("phase", C.c_double * 16)]
+
+
 EXPORTED_SYMBOLS = [
     "fgpu_grid_radii", "fgpu_create", "fgpu_destroy", "fgpu_last_error",
     "fgpu_get_stream", "fgpu_upload_field", "fgpu_download_field",
@@ -121,6 +152,9 @@ EXPORTED_SYMBOLS = [
     "fgpu_disk_on_planet_accel", "fgpu_total_mass", "fgpu_check_finite",
     "fgpu_synchronize", "fgpu_set_phase_timing", "fgpu_phase_times", "fgpu_phase_name",
     "fgpu_disk_force_static",
+    "fgpu_batch_create", "fgpu_batch_destroy", "fgpu_batch_last_error", "fgpu_batch_size",
+    "fgpu_batch_disk", "fgpu_batch_get_tiles", "fgpu_batch_set_tiles", "fgpu_batch_autotune",
+    "fgpu_batch_step", "fgpu_batch_set_clock", "fgpu_batch_get_clock", "fgpu_batch_run",
 ]
 
 
@@ -152,6 +186,18 @@ def _declare(lib: C.CDLL) -> C.CDLL:
         "fgpu_phase_name": ([C.c_int], C.c_char_p),
         "fgpu_disk_force_static": ([vp, vp, vp, C.c_int, C.c_int, C.c_double, C.c_double,
                                     P(FgpuBody), vp, vp], C.c_int),
+        "fgpu_batch_create": ([C.c_int, P(FgpuParams), P(dp), P(vp)], C.c_int),
+        "fgpu_batch_destroy": ([vp], C.c_int),
+        "fgpu_batch_last_error": ([vp], C.c_char_p),
+        "fgpu_batch_size": ([vp, P(C.c_int)], C.c_int),
+        "fgpu_batch_disk": ([vp, C.c_int, P(vp)], C.c_int),
+        "fgpu_batch_get_tiles": ([vp, P(FgpuTiles)], C.c_int),
+        "fgpu_batch_set_tiles": ([vp, P(FgpuTiles)], C.c_int),
+        "fgpu_batch_autotune": ([vp, C.c_int, P(FgpuTiles)], C.c_int),
+        "fgpu_batch_step": ([vp, dp, dp], C.c_int),
+        "fgpu_batch_set_clock": ([vp, C.c_int, P(FgpuClock)], C.c_int),
+        "fgpu_batch_get_clock": ([vp, C.c_int, P(FgpuClock)], C.c_int),
+        "fgpu_batch_run": ([vp, C.c_int, C.c_int, P(C.c_int)], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -60,6 +60,8 @@ struct fgpu_engine {
     int ev_cursor = 0;
 
     fgpu32::Engine32 *e32 = nullptr;  // FP32-mixed form, when selected
+    bool owns_stream = true;          // false for the disks of a batch
+    bool batch_owned = false;         // disks of a batch are freed by the batch
 };
 
 static const char *kPhaseNames[] = {
@@ -370,7 +372,10 @@ static int setup_tables(fgpu_engine *eng, const double *radii)
     return FGPU_OK;
 }
 
-extern "C" int fgpu_create(const fgpu_params *params, const double *radii, fgpu_engine **out)
+// Creates an engine on the given stream (owned by the caller), or on a new
+// stream of its own when shared is null.
+static int create_engine(const fgpu_params *params, const double *radii, cudaStream_t shared,
+                         fgpu_engine **out)
 {
     if (!params || !radii || !out) return FGPU_ERR_BAD_ARG;
     *out = nullptr;
@@ -398,7 +403,10 @@ extern "C" int fgpu_create(const fgpu_params *params, const double *radii, fgpu_
         fgpu_destroy(eng);
         return code;
     };
-    if (cudaStreamCreateWithFlags(&eng->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (shared) {
+        eng->stream = shared;
+        eng->owns_stream = false;
+    } else if (cudaStreamCreateWithFlags(&eng->stream, cudaStreamNonBlocking) != cudaSuccess) {
         eng->err = "stream";
         return fail(FGPU_ERR_CUDA);
     }
@@ -490,7 +498,7 @@ extern "C" int fgpu_create(const fgpu_params *params, const double *radii, fgpu_
 
 extern "C" int fgpu_destroy(fgpu_engine *eng)
 {
-    if (!eng) return FGPU_ERR_BAD_ARG;
+    if (!eng || eng->batch_owned) return FGPU_ERR_BAD_ARG;
     if (eng->stream) cudaStreamSynchronize(eng->stream);
     if (eng->e32) {
         eng->e32->destroy();
@@ -506,10 +514,34 @@ extern "C" int fgpu_destroy(fgpu_engine *eng)
     cudaFree(eng->damp_rings); cudaFree(eng->partial); cudaFree(eng->red_out);
     cudaFree(eng->d_dtmin); cudaFree(eng->d_bad);
     if (eng->h_pinned) cudaFreeHost(eng->h_pinned);
-    if (eng->stream) cudaStreamDestroy(eng->stream);
+    if (eng->stream && eng->owns_stream) cudaStreamDestroy(eng->stream);
     delete eng;
     return FGPU_OK;
 }
+
+extern "C" int fgpu_create(const fgpu_params *params, const double *radii, fgpu_engine **out)
+{
+    return create_engine(params, radii, nullptr, out);
+}
+
+namespace fgpu32 {
+// FP32-mixed disks of a batch: created on the batch's stream
+int create_disk(const fgpu_params *params, const double *radii, cudaStream_t stream,
+                fgpu_engine **out)
+{
+    if (!params || params->precision != FGPU_PRECISION_FP32_MIXED) return FGPU_ERR_UNSUPPORTED;
+    const int rc = create_engine(params, radii, stream, out);
+    if (rc == FGPU_OK) (*out)->batch_owned = true;
+    return rc;
+}
+int destroy_disk(fgpu_engine *eng)
+{
+    if (!eng) return FGPU_ERR_BAD_ARG;
+    eng->batch_owned = false;
+    return fgpu_destroy(eng);
+}
+Engine32 *engine32_of(fgpu_engine *eng) { return eng ? eng->e32 : nullptr; }
+}  // namespace fgpu32
 
 static Launch launch_of(const fgpu_engine *eng)
 {

@@ -1,0 +1,950 @@
+// Device bodies of the FP32-mixed hydro step, shared by the single-disk
+// kernels (kernels_fp32.cu) and the batched many-disk kernels
+// (batch_fp32.cu).  Each body updates one cell, one column or one ring of one
+// disk; the kernels around them only decide which disk, ring and column a
+// thread works on.  The storage conventions (residual v_phi about v_K(Rmed),
+// potential residual about -G M / Rmed, compensated sigma hi + lo) are
+// described at the top of kernels_fp32.cu.
+#pragma once
+
+#include "fp32_engine.h"
+
+#include <cuda_runtime.h>
+
+namespace fgpu32 {
+
+#define CELL(i, j) ((size_t)(i) * (size_t)nz + (size_t)(j))
+
+__device__ __forceinline__ int jnext(int j, int nz) { return j == nz - 1 ? 0 : j + 1; }
+__device__ __forceinline__ int jprev(int j, int nz) { return j == 0 ? nz - 1 : j - 1; }
+
+__device__ __forceinline__ float lim_f(float a, float b, int mc)
+{
+    if (mc) {
+        float mm = 0.f;
+        if (a * b > 0.f) mm = fabsf(a) < fabsf(b) ? a : b;
+        const float c = 0.5f * (a + b), d = 2.f * mm;
+        if (c * d > 0.f) return fabsf(c) < fabsf(d) ? c : d;
+        return 0.f;
+    }
+    if (a * b > 0.f) return __fdividef(2.f * a * b, a + b);
+    return 0.f;
+}
+
+// hi + lo + inc as a compensated pair: y = lo + inc is small next to hi, so
+// Fast2Sum (Dekker 1971) recovers the rounding error of hi + y exactly.
+__device__ __forceinline__ void comp_add(float &hi, float &lo, float inc)
+{
+    const float y = lo + inc;
+    const float s = hi + y;
+    lo = y - (s - hi);
+    hi = s;
+}
+
+__device__ __forceinline__ float tfloor(float e, float sigma, const PhysF &ph)
+{
+    const float emin = sigma * ph.emin_fac;
+    const float emax = sigma * ph.emax_fac;
+    if (!(e > emin)) e = emin;
+    if (!(e < emax)) e = emax;
+    return e;
+}
+
+__device__ __forceinline__ float warp_sum_f(float v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_sum_d(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_min_f(float v)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+template <typename T, T (*WARP)(T)>
+__device__ __forceinline__ T block_reduce(T v, T *red, T neutral)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+    v = WARP(v);
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        T x = lane < nw ? red[lane] : neutral;
+        x = WARP(x);
+        if (lane == 0) red[32] = x;
+    }
+    __syncthreads();
+    return red[32];
+}
+__device__ __forceinline__ double bsum_d(double v, double *red)
+{
+    return block_reduce<double, warp_sum_d>(v, red, 0.0);
+}
+__device__ __forceinline__ float bsum_f(float v, float *red)
+{
+    return block_reduce<float, warp_sum_f>(v, red, 0.f);
+}
+__device__ __forceinline__ float bmin_f(float v, float *red)
+{
+    return block_reduce<float, warp_min_f>(v, red, 3.0e38f);
+}
+
+// ---------------------------------------------------------------------------
+// Potential residual Phi - Phi_K (CalculateNbodyPotential, Pframeforce.cpp:21-86)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void potential_cell(const GeoF &g, const TablesF &t, const PhysF &ph,
+                                               const BodiesF &b, const float *__restrict__ H,
+                                               float *__restrict__ pot, int i, int j)
+{
+    const int nz = g.nz;
+    const double xd = t.Rmed_d[i] * t.cos_d[j];
+    const double yd = t.Rmed_d[i] * t.sin_d[j];
+    const float eps = ph.eps_smooth * H[CELL(i, j)];
+    const float s2 = eps * eps;
+    float acc = 0.f;
+    for (int k = 0; k < b.n; ++k) {
+        float term;
+        if (k == 0 && b.star_at_origin) {
+            // -G M / sqrt(r^2 + eps^2) + G M / r without cancellation:
+            // 1/r - 1/d = (d - r) / (r d) = eps^2 / ((d + r) r d)
+            const float r = t.Rmed[i];
+            const float d = sqrtf(r * r + s2);
+            term = b.gm[0] * s2 / ((d + r) * r * d);
+        } else {
+            const double dx = xd - b.x[k], dy = yd - b.y[k];
+            const float d2 = (float)(dx * dx + dy * dy) + s2;
+            const float inv_d = rsqrtf(d2);
+            float fk = 1.f;
+            if (b.rsm[k] > 0.f) {
+                const float dsm = d2 * inv_d;
+                if (dsm < b.rsm[k]) {
+                    const float q = dsm / b.rsm[k];
+                    fk = q * q * q * q - 2.f * q * q * q + 2.f * q;
+                }
+            }
+            if (k == 0) {
+                // central object off the origin: residual against -G M / r in FP64
+                term = (float)(-(double)b.gm[0] * fk / sqrt(dx * dx + dy * dy + (double)s2) +
+                               (double)b.gm_ref * t.InvRmed_d[i]);
+            } else {
+                term = -b.gm[k] * inv_d * fk;
+            }
+        }
+        acc += term;
+    }
+    acc += -b.ix * (float)xd - b.iy * (float)yd;
+    pot[CELL(i, j)] = acc;
+}
+
+// ---------------------------------------------------------------------------
+// momentum sources (SourceEuler.cpp:325-428) in residual form; rows 0..nr
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void source_cell(const GeoF &g, const TablesF &t, float dt,
+                                            const float *__restrict__ S,
+                                            const float *__restrict__ P,
+                                            const float *__restrict__ pot,
+                                            const float *__restrict__ vr_in,
+                                            const float *__restrict__ dv_in,
+                                            float *__restrict__ vr_out,
+                                            float *__restrict__ dv_out, int i, int j)
+{
+    const int nz = g.nz, nr = g.nr;
+    float vr = vr_in[CELL(i, j)];
+    if (i >= 2 && i < nr - 1) {
+        const float gradp = 2.f * __fdividef(P[CELL(i, j)] - P[CELL(i - 1, j)],
+                                             S[CELL(i, j)] + S[CELL(i - 1, j)]) *
+                            t.InvDiffRmed[i];
+        const float gradphi = (pot[CELL(i, j)] - pot[CELL(i - 1, j)]) * t.InvDiffRmed[i];
+        const int jn = jnext(j, nz);
+        const float d = 0.25f * (dv_in[CELL(i, j)] + dv_in[CELL(i, jn)] + dv_in[CELL(i - 1, j)] +
+                                 dv_in[CELL(i - 1, jn)]);
+        // vt^2 / r - dPhi_K/dr = Kbal + (2 A d + d^2) / Rinf
+        const float centri = t.Kbal[i] + (2.f * t.Aface[i] + d) * d * t.InvRinf[i];
+        vr += dt * (-gradp - gradphi + centri);
+    }
+    vr_out[CELL(i, j)] = vr;
+    if (i < nr) {
+        float v = dv_in[CELL(i, j)];
+        if (i >= 1 && i < nr - 1) {
+            const int jp = jprev(j, nz);
+            const float invdx = t.InvDxSrc[i];
+            const float gradp = 2.f * __fdividef(P[CELL(i, j)] - P[CELL(i, jp)],
+                                                 S[CELL(i, j)] + S[CELL(i, jp)]) * invdx;
+            const float gradphi = (pot[CELL(i, j)] - pot[CELL(i, jp)]) * invdx;
+            v = v + dt * (-gradp - gradphi);
+        }
+        dv_out[CELL(i, j)] = v;
+    }
+}
+
+// compression heating + SN q and energy update + T floor
+__device__ __forceinline__ void artvisc_q_cell(const GeoF &g, const TablesF &t, const PhysF &ph,
+                                               float dt, const float *__restrict__ S,
+                                               const float *__restrict__ vr,
+                                               const float *__restrict__ dv, float *__restrict__ E,
+                                               float *__restrict__ Qr, float *__restrict__ Qp,
+                                               int i, int j)
+{
+    const int nz = g.nz, nr = g.nr;
+    const size_t c = CELL(i, j);
+    const int jn = jnext(j, nz);
+    const float vr0 = vr[c], vr1 = vr[CELL(i + 1, j)];
+    const float dvp = dv[CELL(i, jn)] - dv[c];
+    float e = 0.f;
+    if (ph.adiabatic) {
+        e = E[c];
+        if (i < nr - 1) {
+            const float div_v = (vr1 * t.Rinf[i + 1] - vr0 * t.Rinf[i]) * t.InvDiffRsupRb[i] +
+                                dvp * g.invdphi * t.InvRmed[i];
+            e = e * __expf(-ph.gm1 * dt * div_v);
+        }
+    }
+    if (ph.art_visc_sn) {
+        const float sig = S[c];
+        const float dv_r = vr1 - vr0;
+        const float qr = dv_r < 0.f ? ph.C2 * sig * (dv_r * dv_r) : 0.f;
+        const float qp = dvp < 0.f ? ph.C2 * sig * (dvp * dvp) : 0.f;
+        Qr[c] = qr;
+        Qp[c] = qp;
+        if (ph.adiabatic && ph.dissipation && i >= 1 && i < nr - 1) {
+            e = e - dt * qr * dv_r * t.InvDiffRsup[i] - dt * qp * dvp * t.InvDxTheta[i];
+        }
+    }
+    if (ph.adiabatic) {
+        if (ph.dissipation) e = tfloor(e, S[c], ph);
+        E[c] = e;
+    }
+}
+
+__device__ __forceinline__ void artvisc_v_cell(const GeoF &g, const TablesF &t, const PhysF &ph,
+                                               float dt, const float *__restrict__ S,
+                                               const float *__restrict__ E,
+                                               const float *__restrict__ Qr,
+                                               const float *__restrict__ Qp, float *__restrict__ vr,
+                                               float *__restrict__ dv, float *__restrict__ cs,
+                                               float *__restrict__ H, float *__restrict__ nu, int i,
+                                               int j)
+{
+    const int nz = g.nz, nr = g.nr;
+    const size_t c = CELL(i, j);
+    if (ph.art_visc_sn) {
+        if (i >= 2 && i < nr - 1) {
+            vr[c] -= dt * 2.f * __fdividef(Qr[c] - Qr[CELL(i - 1, j)], S[c] + S[CELL(i - 1, j)]) *
+                     t.InvDiffRmed[i];
+        }
+        if (i >= 1 && i < nr - 1) {
+            const int jp = jprev(j, nz);
+            dv[c] -= dt * 2.f * __fdividef(Qp[c] - Qp[CELL(i, jp)], S[c] + S[CELL(i, jp)]) *
+                     t.InvDxTheta[i];
+        }
+    }
+    if (ph.adiabatic) {
+        const float c_s = sqrtf(ph.g_gm1 * __fdividef(E[c], S[c]));
+        const float h = c_s * t.HFacAdi[i];
+        cs[c] = c_s;
+        H[c] = h;
+        nu[c] = ph.alpha > 0.f ? ph.alpha * h * c_s : ph.constant_viscosity;
+    }
+}
+
+// stress tensor (viscosity.cpp:139-254); tau_r_phi adds the Keplerian shear
+__device__ __forceinline__ void stress_cell(const GeoF &g, const TablesF &t,
+                                            const float *__restrict__ S,
+                                            const float *__restrict__ vr,
+                                            const float *__restrict__ dv,
+                                            const float *__restrict__ nu, float *__restrict__ divv,
+                                            float *__restrict__ trr, float *__restrict__ tpp,
+                                            float *__restrict__ trp, int i, int j)
+{
+    const int nz = g.nz;
+    const size_t c = CELL(i, j);
+    const int jn = jnext(j, nz);
+    const float vr0 = vr[c], vr1 = vr[CELL(i + 1, j)];
+    const float dvp = dv[CELL(i, jn)] - dv[c];
+    const float n = nu[c], sg = S[c];
+    const float d = (vr1 * t.Rinf[i + 1] - vr0 * t.Rinf[i]) * t.InvDiffRsupRb[i] +
+                    dvp * g.invdphi * t.InvRmed[i];
+    divv[c] = d;
+    const float drr = (vr1 - vr0) * t.InvDiffRsup[i];
+    trr[c] = 2.f * n * sg * (drr - (1.f / 3.f) * d);
+    const float dpp = dvp * g.invdphi * t.InvRmed[i] + 0.5f * (vr1 + vr0) * t.InvRmed[i];
+    tpp[c] = 2.f * n * sg * (dpp - (1.f / 3.f) * d);
+    if (i >= 1) {
+        const int jp = jprev(j, nz);
+        const float dvazirdr =
+            t.Shear[i] + (dv[c] * t.InvRmed[i] - dv[CELL(i - 1, j)] * t.InvRmed[i - 1]) *
+                             t.InvDiffRmed[i];
+        const float dvrdphi = (vr0 - vr[CELL(i, jp)]) * g.invdphi;
+        const float drp = t.Rinf[i] * dvazirdr + dvrdphi * t.InvRinf[i];
+        const float n4 = 0.25f * (n + nu[CELL(i - 1, j)] + nu[CELL(i, jp)] + nu[CELL(i - 1, jp)]);
+        const float s4 = 0.25f * (sg + S[CELL(i - 1, j)] + S[CELL(i, jp)] + S[CELL(i - 1, jp)]);
+        trp[c] = n4 * s4 * drp;
+    }
+}
+
+// viscous velocity update + SubStep3.  mode bits: 1 velocities
+// (viscosity.cpp:355-421), 2 heating/cooling rates, 4 energy update
+// (SourceEuler.cpp:859-954)
+__device__ __forceinline__ void viscous_cell(
+    const GeoF &g, const TablesF &t, const PhysF &ph, float dt, float beta_inv, int mode,
+    const float *__restrict__ S, const float *__restrict__ trr, const float *__restrict__ tpp,
+    const float *__restrict__ trp, const float *__restrict__ divv, const float *__restrict__ nu,
+    const float *__restrict__ H, const float *__restrict__ S0, const float *__restrict__ E0,
+    float *__restrict__ vr, float *__restrict__ dv, float *__restrict__ E,
+    float *__restrict__ qplus, float *__restrict__ qminus, int i, int j)
+{
+    const int nz = g.nz, nr = g.nr;
+    const size_t c = CELL(i, j);
+    const int jp = jprev(j, nz), jn = jnext(j, nz);
+    if (mode & 1) {
+        if (i >= 1 && i < nr - 1) {
+            const float sa = 0.5f * (S[c] + S[CELL(i, jp)]);
+            dv[c] += __fdividef(dt * t.InvRmed[i], sa) *
+                     (t.TwoOverDRa2[i] * (t.RinfSq[i + 1] * trp[CELL(i + 1, j)] -
+                                          t.RinfSq[i] * trp[c]) +
+                      (tpp[c] - tpp[CELL(i, jp)]) * g.invdphi);
+        }
+        if (i >= 2 && i < nr - 1) {
+            const float sa = 0.5f * (S[c] + S[CELL(i - 1, j)]);
+            vr[c] += __fdividef(dt, sa) * ph.rvf * t.TwoOverRmedSum[i] *
+                     ((t.Rmed[i] * trr[c] - t.Rmed[i - 1] * trr[CELL(i - 1, j)]) * t.InvDiffRmed[i] +
+                      (trp[CELL(i, jn)] - trp[c]) * g.invdphi - 0.5f * (tpp[c] + tpp[CELL(i - 1, j)]));
+        }
+    }
+    if (!(mode & 6) || !ph.adiabatic) return;
+    float qp = 0.f, qm = 0.f;
+    const float e = E[c], sig = S[c];
+    const bool active = i >= 1 && i < nr - 1;
+    if (active) {
+        if (ph.cooling_beta) {
+            float dE = e;
+            if (ph.beta_ref == 1) dE -= __fdividef(E0[c], S0[c]) * sig;
+            else if (ph.beta_ref == 2) dE -= t.EModel[i] * sig;
+            else if (ph.beta_ref == 3) dE -= sig * ph.emin_fac;
+            qm = dE * t.OmegaK[i] * beta_inv;
+        }
+        if (ph.heating_viscous) {
+            const float n = nu[c];
+            if (n != 0.f) {
+                const float trpa = 0.25f * (trp[c] + trp[CELL(i + 1, j)] + trp[CELL(i, jn)] +
+                                            trp[CELL(i + 1, jn)]);
+                const float a = trr[c], b2 = tpp[c], dd = divv[c];
+                float q = __fdividef(a * a + 2.f * trpa * trpa + b2 * b2, 2.f * n * sig);
+                q += (2.f / 9.f) * n * sig * dd * dd;
+                qp = q * ph.hvf;
+            }
+        }
+        // radiative alpha: 1 + 8 sigma_SB / c * H * x^4 e^3 with
+        // x = mu (gamma-1) / (R sigma), evaluated as x * (x e)^3
+        const float x = __fdividef(ph.mu_gm1_over_R, sig);
+        const float xe = x * e;
+        const float alpha = 1.f + H[c] * ph.cool_const * x * (xe * xe * xe);
+        const float ia = __frcp_rn(alpha);
+        qp *= ia;
+        qm *= ia;
+    }
+    if (mode & 4) {
+        float en = e;
+        if (active) {
+            en = e + dt * (qp - qm);
+            if (sig < ph.sigma_floor10) {
+                qm = qp;
+                en = 0.f;
+            }
+        }
+        E[c] = tfloor(en, sig, ph);
+    }
+    qplus[c] = qp;
+    qminus[c] = qm;
+}
+
+// ghost rings (boundary_conditions.cpp:65-114); v_phi hooks work on the
+// residual, with the reference-profile offsets per ring
+__device__ __forceinline__ void ghost_f(float *x, const float *x0, int kind, int outer, int vec,
+                                        int nr, int nz, int j, float kep_value, float zg_offset)
+{
+    const int irad = vec ? nr : nr - 1;
+    switch (kind) {
+    case 1:
+        if (!outer) {
+            if (vec) {
+                x[CELL(0, j)] = x[CELL(2, j)];
+                x[CELL(1, j)] = x[CELL(2, j)];
+            } else {
+                x[CELL(0, j)] = x[CELL(1, j)] + zg_offset;
+            }
+        } else {
+            if (vec) {
+                x[CELL(irad, j)] = x[CELL(irad - 2, j)];
+                x[CELL(irad - 1, j)] = x[CELL(irad - 2, j)];
+            } else {
+                x[CELL(irad, j)] = x[CELL(irad - 1, j)] + zg_offset;
+            }
+        }
+        break;
+    case 2:
+        if (!outer) {
+            const float v2 = x[CELL(2, j)];
+            x[CELL(1, j)] = v2 > 0.f ? 0.f : v2;
+            x[CELL(0, j)] = v2 > 0.f ? 0.f : v2;
+        } else {
+            const float v2 = x[CELL(irad - 2, j)];
+            x[CELL(irad - 1, j)] = v2 < 0.f ? 0.f : v2;
+            x[CELL(irad, j)] = v2 < 0.f ? 0.f : v2;
+        }
+        break;
+    case 3:
+        if (!outer) {
+            x[CELL(0, j)] = x0[CELL(0, j)];
+            if (vec) x[CELL(1, j)] = x0[CELL(1, j)];
+        } else {
+            x[CELL(irad, j)] = x0[CELL(irad, j)];
+            if (vec) x[CELL(irad - 1, j)] = x0[CELL(irad - 1, j)];
+        }
+        break;
+    case 4:
+        x[CELL(outer ? irad : 0, j)] = kep_value;
+        break;
+    default:
+        break;
+    }
+}
+
+__device__ __forceinline__ void ghost_col(const GeoF &g, const BcF &bc, const StateF &s, int j)
+{
+    const int nz = g.nz, nr = g.nr;
+    ghost_f(s.sigma, s.sigma0, bc.sigma_in, 0, 0, nr, nz, j, 0.f, 0.f);
+    ghost_f(s.sigma, s.sigma0, bc.sigma_out, 1, 0, nr, nz, j, 0.f, 0.f);
+    // low part of sigma: copied by zero-gradient, cleared by reference hooks
+    if (bc.sigma_in == 1) s.sigma_lo[CELL(0, j)] = s.sigma_lo[CELL(1, j)];
+    else if (bc.sigma_in == 3) s.sigma_lo[CELL(0, j)] = 0.f;
+    if (bc.sigma_out == 1) s.sigma_lo[CELL(nr - 1, j)] = s.sigma_lo[CELL(nr - 2, j)];
+    else if (bc.sigma_out == 3) s.sigma_lo[CELL(nr - 1, j)] = 0.f;
+    ghost_f(s.energy, s.energy0, bc.energy_in, 0, 0, nr, nz, j, 0.f, 0.f);
+    ghost_f(s.energy, s.energy0, bc.energy_out, 1, 0, nr, nz, j, 0.f, 0.f);
+    ghost_f(s.vr, s.vr0, bc.vr_in, 0, 1, nr, nz, j, 0.f, 0.f);
+    ghost_f(s.vr, s.vr0, bc.vr_out, 1, 1, nr, nz, j, 0.f, 0.f);
+    ghost_f(s.dv, s.dv0, bc.vaz_in, 0, 0, nr, nz, j, bc.kep_in, bc.zg_in);
+    ghost_f(s.dv, s.dv0, bc.vaz_out, 1, 0, nr, nz, j, bc.kep_out, bc.zg_out);
+}
+
+// ---------------------------------------------------------------------------
+// radial transport (TransportEuler.cpp:138-167, 349-406, 545-620) with the
+// residual angular momentum: quantities 0,1 radial momenta, 2,3 residual
+// angular momenta sigma r dv, [4 energy], last sigma.  The angular-momentum
+// slopes and the limiter act on the total specific angular momentum
+// J_K + r dv (J_K = r v_K per ring), the upwind star value is kept relative to
+// J_K of the upwind ring, and the Keplerian part J_K * mass-flux enters the
+// residual update through the per-ring differences of J_K.  One thread walks
+// column j through rings i0 .. i0 + chunk - 1 with a rolling window.
+// ---------------------------------------------------------------------------
+template <int NQ>
+__device__ __forceinline__ void rad_ring_f(int i, int j, int nz, const float *S, const float *vr,
+                                           const float *dv, const float *E, const TablesF &t,
+                                           float *w)
+{
+    const float sg = S[CELL(i, j)];
+    const float r = t.Rmed[i];
+    w[0] = vr[CELL(i + 1, j)];
+    w[1] = vr[CELL(i, j)];
+    w[2] = dv[CELL(i, jnext(j, nz))] * r;
+    w[3] = dv[CELL(i, j)] * r;
+    if (NQ == 5) w[4] = __fdividef(E[CELL(i, j)], sg);
+    w[NQ] = sg;
+}
+
+template <int NQ>
+__device__ __forceinline__ void radial_col(const GeoF &g, const TablesF &t, float dt, int mc,
+                                           int chunk, const float *__restrict__ S,
+                                           const float *__restrict__ vr,
+                                           const float *__restrict__ dv,
+                                           const float *__restrict__ E, float *__restrict__ m0,
+                                           float *__restrict__ m1, float *__restrict__ m2,
+                                           float *__restrict__ m3, float *__restrict__ E_out,
+                                           float *__restrict__ S_out,
+                                           const float *__restrict__ S_lo,
+                                           float *__restrict__ S_lo_out, int i0, int j)
+{
+    constexpr int NW = NQ + 1;
+    const int nz = g.nz, nr = g.nr;
+    if (i0 >= nr) return;
+    const int i1 = min(i0 + chunk, nr);
+    const float dtdphi = dt * g.dphi;
+
+    // upward difference of ring k (total slope for the angular momenta)
+    auto updiff = [&](int k, const float *wlo, const float *whi, int q) -> float {
+        float d = (whi[q] - wlo[q]) * t.InvDiffRmed[k + 1];
+        if (q == 2 || q == 3) d += t.JSlope[k];
+        return d;
+    };
+    auto lim = [&](int ring, float up, float down) -> float {
+        if (ring <= 0 || ring >= nr - 1) return 0.f;
+        return lim_f(up, down, mc);
+    };
+
+    float wa[NW] = {}, wb[NW] = {}, wn[NW] = {}, da[NW] = {}, db[NW] = {}, ub[NW] = {};
+    {
+        float wm2[NW] = {};
+        const int r0 = i0 - 1;
+        if (r0 - 1 >= 0) rad_ring_f<NQ>(r0 - 1, j, nz, S, vr, dv, E, t, wm2);
+        if (r0 >= 0) rad_ring_f<NQ>(r0, j, nz, S, vr, dv, E, t, wa);
+        rad_ring_f<NQ>(i0, j, nz, S, vr, dv, E, t, wb);
+        const bool has_next = i0 + 1 < nr;
+        if (has_next) rad_ring_f<NQ>(i0 + 1, j, nz, S, vr, dv, E, t, wn);
+#pragma unroll
+        for (int q = 0; q < NW; ++q) {
+            const float downa = (r0 - 1 >= 0) ? updiff(r0 - 1, wm2, wa, q) : 0.f;
+            const float upa = (r0 >= 0) ? updiff(r0, wa, wb, q) : 0.f;
+            da[q] = r0 >= 0 ? lim(r0, upa, downa) : 0.f;
+            const float upb = has_next ? updiff(i0, wb, wn, q) : 0.f;
+            db[q] = lim(i0, upb, upa);
+            ub[q] = upb;
+        }
+    }
+    float flux_prev[NW] = {}, q_prev[NW] = {};
+    float kep_prev = 0.f;  // Keplerian term of ring k-1 from interface k-1
+    for (int k = i0; k <= i1; ++k) {
+        float flux[NW];
+        float kep_lower = 0.f, kep_upper = 0.f;
+        if (k == 0 || k >= nr) {
+#pragma unroll
+            for (int q = 0; q < NW; ++q) flux[q] = 0.f;
+        } else {
+            const float v = vr[CELL(k, j)];
+            const float base = dtdphi * t.Rinf[k];
+            const float vdt = v * dt;
+            float sstar;
+            if (v > 0.f) {
+                const float f = (t.DRmed[k] - vdt) * 0.5f;
+                sstar = wa[NQ] + f * da[NQ];
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) flux[q] = base * (wa[q] + f * da[q]) * sstar * v;
+            } else {
+                const float f = (t.DRmed[k + 1] + vdt) * 0.5f;
+                sstar = wb[NQ] - f * db[NQ];
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) flux[q] = base * (wb[q] - f * db[q]) * sstar * v;
+            }
+            const float fs = base * sstar * v;
+            flux[NQ] = fs;
+            // J_K(upwind) - J_K(ring) times the mass flux, for the ring above
+            // (inflow from below) and the ring below (outflow upwards)
+            if (v > 0.f) kep_upper = t.DJ[k] * fs;
+            else kep_lower = -t.DJ[k] * fs;
+        }
+        if (k > i0) {
+            const int i = k - 1;
+            const float invs = t.InvSurf[i];
+            const size_t c = CELL(i, j);
+            m0[c] = q_prev[0] + (flux_prev[0] - flux[0]) * invs;
+            m1[c] = q_prev[1] + (flux_prev[1] - flux[1]) * invs;
+            m2[c] = q_prev[2] + (flux_prev[2] + kep_prev - flux[2] - kep_lower) * invs;
+            m3[c] = q_prev[3] + (flux_prev[3] + kep_prev - flux[3] - kep_lower) * invs;
+            if (NQ == 5) E_out[c] = q_prev[4] + (flux_prev[4] - flux[4]) * invs;
+            float hi = q_prev[NQ], lo = S_lo[c];
+            comp_add(hi, lo, (flux_prev[NQ] - flux[NQ]) * invs);
+            S_out[c] = hi;
+            S_lo_out[c] = lo;
+        }
+        if (k < i1) {
+#pragma unroll
+            for (int q = 0; q < NW; ++q) flux_prev[q] = flux[q];
+            kep_prev = kep_upper;
+            const float sb = wb[NQ];
+            q_prev[0] = sb * wb[0];
+            q_prev[1] = sb * wb[1];
+            q_prev[2] = sb * wb[2];
+            q_prev[3] = sb * wb[3];
+            if (NQ == 5) q_prev[4] = E[CELL(k, j)];
+            q_prev[NQ] = sb;
+            const bool more = k + 2 < nr;
+            float w2[NW] = {};
+            if (more) rad_ring_f<NQ>(k + 2, j, nz, S, vr, dv, E, t, w2);
+#pragma unroll
+            for (int q = 0; q < NW; ++q) {
+                wa[q] = wb[q];
+                da[q] = db[q];
+                wb[q] = wn[q];
+                const float up = more ? updiff(k + 1, wn, w2, q) : 0.f;
+                db[q] = lim(k + 1, up, ub[q]);
+                ub[q] = up;
+                wn[q] = w2[q];
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// azimuthal transport with FARGO (TransportEuler.cpp:174-304, 416-466,
+// 630-664): FP32 advection, FP64 ring mean and shift phase.  The residual
+// angular momentum is advected like any specific quantity (J_K is constant on
+// a ring, so its part cancels exactly).  One block per ring; thread tid owns
+// cells tid + n * blockDim.x, n < PER, which must cover the ring.
+// ---------------------------------------------------------------------------
+template <int PER>
+__device__ __forceinline__ void ring_pass_f(float *S, float *SS, float *W, float *D,
+                                            float *const *qrow, int nq, const float *v,
+                                            float *slo, float dt, float dxtheta,
+                                            float half_invdx, float dxrad, float invsurf, int nz,
+                                            int mc, bool uniform, float vconst)
+{
+    const int tid = threadIdx.x, bs = blockDim.x;
+    float invs[PER], f[PER];
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = tid + n * bs;
+        if (j < nz) {
+            const int jp = j == nz - 1 ? 0 : j + 1, jm = j == 0 ? nz - 1 : j - 1;
+            D[j] = lim_f(S[jp] - S[j], S[j] - S[jm], mc) * half_invdx;
+            invs[n] = __frcp_rn(S[j]);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = tid + n * bs;
+        if (j < nz) {
+            const int jm = j == 0 ? nz - 1 : j - 1;
+            const float vv = uniform ? vconst : v[n];
+            const float ksi = vv * dt;
+            SS[j] = ksi > 0.f ? S[jm] + (dxtheta - ksi) * D[jm] : S[j] - (dxtheta + ksi) * D[j];
+        }
+    }
+    __syncthreads();
+    for (int q = 0; q < nq; ++q) {
+        float *Q = qrow[q];
+#pragma unroll
+        for (int n = 0; n < PER; ++n) {
+            const int j = tid + n * bs;
+            if (j < nz) W[j] = Q[j] * invs[n];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int n = 0; n < PER; ++n) {
+            const int j = tid + n * bs;
+            if (j < nz) {
+                const int jp = j == nz - 1 ? 0 : j + 1, jm = j == 0 ? nz - 1 : j - 1;
+                D[j] = lim_f(W[jp] - W[j], W[j] - W[jm], mc) * half_invdx;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int n = 0; n < PER; ++n) {
+            const int j = tid + n * bs;
+            if (j < nz) {
+                const int jm = j == 0 ? nz - 1 : j - 1;
+                const float vv = uniform ? vconst : v[n];
+                const float ksi = vv * dt;
+                const float qs = ksi > 0.f ? W[jm] + (dxtheta - ksi) * D[jm]
+                                           : W[j] - (dxtheta + ksi) * D[j];
+                f[n] = dxrad * qs * SS[j] * vv;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int n = 0; n < PER; ++n) {
+            const int j = tid + n * bs;
+            if (j < nz) W[j] = f[n];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int n = 0; n < PER; ++n) {
+            const int j = tid + n * bs;
+            if (j < nz) Q[j] += (W[j] - W[j == nz - 1 ? 0 : j + 1]) * invsurf;
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = tid + n * bs;
+        if (j < nz) W[j] = dxrad * SS[j] * (uniform ? vconst : v[n]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = tid + n * bs;
+        if (j < nz) {
+            f[n] = S[j];
+            comp_add(f[n], slo[n], (W[j] - W[j == nz - 1 ? 0 : j + 1]) * invsurf);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = tid + n * bs;
+        if (j < nz) S[j] = f[n];
+    }
+    __syncthreads();
+}
+
+// smf: 4 * nz floats of shared memory; red: 33 doubles of shared memory
+template <int PER>
+__device__ __forceinline__ void azimuthal_ring(const GeoF &g, const TablesF &t, double dt, int mc,
+                                               int fast, int nq, const float *__restrict__ dv,
+                                               float *m0, float *m1, float *m2, float *m3,
+                                               float *E, float *S, float *S_lo, int i, float *smf,
+                                               double *red)
+{
+    const int nz = g.nz;
+    const int tid = threadIdx.x, bs = blockDim.x;
+    const size_t row = (size_t)i * nz;
+    float *Sr = smf, *SS = smf + nz, *W = smf + 2 * nz, *D = smf + 3 * nz;
+
+    float vown[PER], slo[PER];
+    double part = 0.0;
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = tid + n * bs;
+        if (j < nz) {
+            vown[n] = dv[row + j];
+            part += (double)vown[n];
+        }
+    }
+    // ring mean of v_phi and the FARGO shift phase in FP64 (:174-236)
+    const double mean_dv = bsum_d(part, red) / (double)nz;
+    const double vmean = t.Vref_d[i] + mean_dv;
+    const double Ntilde = vmean * t.InvRmed_d[i] * dt * g.invdphi_d;
+    const double Nround = floor(Ntilde + 0.5);
+    const int nshift = (int)Nround;
+    const float vt = (float)((Ntilde - Nround) * t.Rmed_d[i] * (1.0 / dt) * g.dphi_d);
+    const float mdv = (float)mean_dv;
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = tid + n * bs;
+        if (j < nz) {
+            // residual about the ring mean (compute_residual_velocity, :194-205)
+            float vres = vown[n] - mdv;
+            if (!fast) vres = vt + vres;
+            vown[n] = vres;
+            Sr[j] = S[row + j];
+            slo[n] = S_lo[row + j];
+        }
+    }
+    __syncthreads();
+    float *qrow[5] = {m0 + row, m1 + row, m2 + row, m3 + row, E + row};
+    const float dxtheta = g.dphi * t.Rmed[i];
+    const float half_invdx = 0.5f / dxtheta;
+    const float dxrad = (t.Rsup[i] - t.Rinf[i]) * (float)dt;
+    const float invsurf = t.InvSurf[i];
+    ring_pass_f<PER>(Sr, SS, W, D, qrow, nq, vown, slo, (float)dt, dxtheta, half_invdx, dxrad,
+                     invsurf, nz, mc, false, 0.f);
+    if (fast) {
+        ring_pass_f<PER>(Sr, SS, W, D, qrow, nq, vown, slo, (float)dt, dxtheta, half_invdx, dxrad,
+                         invsurf, nz, mc, true, vt);
+    }
+    for (int q = 0; q <= nq; ++q) {
+        float *Q = q < nq ? qrow[q] : S + row;
+        const float *src = q < nq ? qrow[q] : Sr;
+#pragma unroll
+        for (int n = 0; n < PER; ++n) {
+            const int j = tid + n * bs;
+            if (j < nz) W[j] = src[j];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int n = 0; n < PER; ++n) {
+            const int j = tid + n * bs;
+            if (j < nz) {
+                int ji = (j - nshift) % nz;
+                if (ji < 0) ji += nz;
+                Q[j] = W[ji];
+            }
+        }
+        __syncthreads();
+    }
+    // the low part of sigma moves with it
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = tid + n * bs;
+        if (j < nz) W[j] = slo[n];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = tid + n * bs;
+        if (j < nz) {
+            int ji = (j - nshift) % nz;
+            if (ji < 0) ji += nz;
+            S_lo[row + j] = W[ji];
+        }
+    }
+    // the caller may reuse smf for the next ring
+    __syncthreads();
+}
+
+// velocities from momenta (:498-535), floors; rows 0..nr
+__device__ __forceinline__ void finish_cell(
+    const GeoF &g, const TablesF &t, const PhysF &ph, const float *__restrict__ m0,
+    const float *__restrict__ m1, const float *__restrict__ m2, const float *__restrict__ m3,
+    const float *__restrict__ S_t, const float *__restrict__ E_t, const float *__restrict__ vr_in,
+    float *__restrict__ vr_out, float *__restrict__ dv_out, float *__restrict__ S_out,
+    float *__restrict__ E_out, const float *__restrict__ Slo_t, float *__restrict__ Slo_out, int i,
+    int j)
+{
+    const int nz = g.nz, nr = g.nr;
+    const size_t c = CELL(i, j);
+    if (i == nr) {
+        vr_out[c] = vr_in[c];
+        return;
+    }
+    const float s = S_t[c];
+    if (i == 0) {
+        vr_out[c] = 0.f;
+    } else {
+        const size_t cm = CELL(i - 1, j);
+        vr_out[c] = __fdividef(m0[cm] + m1[c], S_t[cm] + s);
+    }
+    const size_t cjm = CELL(i, jprev(j, nz));
+    dv_out[c] = __fdividef(m2[cjm] + m3[c], S_t[cjm] + s) * t.InvRmed[i];
+    const bool floored = s < ph.sigma_min;
+    const float sf = floored ? ph.sigma_min : s;
+    S_out[c] = sf;
+    Slo_out[c] = floored ? 0.f : Slo_t[c];
+    if (ph.adiabatic) E_out[c] = tfloor(E_t[c], sf, ph);
+}
+
+// damping zones (damping.cpp:311-776); block-wide over ring i
+__device__ __forceinline__ void damp_ring_f(float *X, float *X0, const DampQF &d, int i, int nz,
+                                            int outer, float dt, float *red, float *Xlo)
+{
+    const int kind = outer ? d.kind_out : d.kind_in;
+    const size_t row = (size_t)i * nz;
+    float x0c = 0.f;
+    if (kind == 3) {
+        float part = 0.f;
+        for (int j = threadIdx.x; j < nz; j += blockDim.x) part += X[row + j];
+        const float mean = bsum_f(part, red) / nz;
+        if (threadIdx.x == 0) X0[row] = mean;
+        x0c = mean;
+    } else if (kind == 2) {
+        x0c = outer ? d.x0_zero_out[i] : d.x0_zero_in[i];
+    }
+    const float factor = outer ? d.fac_out[i] : d.fac_in[i];
+    const float tau = outer ? d.tau_out : d.tau_in;
+    const float ef = __expf(-dt * factor / tau);
+    for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+        const float x0 = kind == 1 ? X0[row + j] : x0c;
+        X[row + j] = (X[row + j] - x0) * ef + x0;
+        if (Xlo) Xlo[row + j] *= ef;
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ void damping_ring(const GeoF &g, const DampingF &dm, float dt,
+                                             const StateF &s, int i, float *red)
+{
+    const int nz = g.nz, nr = g.nr;
+    float *X[4] = {s.vr, s.dv, s.sigma, s.energy};
+    float *X0[4] = {s.vr0, s.dv0, s.sigma0, s.energy0};
+    for (int q = 0; q < 4; ++q) {
+        const DampQF &d = dm.q[q];
+        const int size = d.vector ? nr + 1 : nr;
+        float *lo = q == 2 ? s.sigma_lo : nullptr;
+        if (d.kind_in != 0 && d.active_in && i <= d.limit_in)
+            damp_ring_f(X[q], X0[q], d, i, nz, 0, dt, red, lo);
+        if (d.kind_out != 0 && d.active_out && i >= d.limit_out && i < size)
+            damp_ring_f(X[q], X0[q], d, i, nz, 1, dt, red, lo);
+    }
+}
+
+// derived quantities + CFL (SourceEuler.cpp:225-249, cfl.cpp:185-382); block-
+// wide over ring i.  mode bits: 1 derived quantities, 2 also c_s, H, T of the
+// isothermal disk, 4 CFL minimum into dt_min (float bits, atomicMin)
+__device__ __forceinline__ void derived_cfl_ring(
+    const GeoF &g, const TablesF &t, const PhysF &ph, int mode, const float *__restrict__ S,
+    const float *__restrict__ E, const float *__restrict__ vr, const float *__restrict__ dv,
+    const float *__restrict__ qplus, const float *__restrict__ qminus, float *__restrict__ cs,
+    float *__restrict__ H, float *__restrict__ P, float *__restrict__ T, float *__restrict__ nu,
+    unsigned int *__restrict__ dt_min, int i, float *red)
+{
+    const int nz = g.nz, nr = g.nr;
+    const size_t row = (size_t)i * nz;
+    const bool do_cfl = (mode & 4) != 0;
+    float md0 = 0.f, md1 = 0.f;
+    if (do_cfl && i < nr - 1) {
+        float p0 = 0.f, p1 = 0.f;
+        for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+            p0 += dv[row + j];
+            p1 += dv[row + nz + j];
+        }
+        md0 = bsum_f(p0, red) / (float)nz;
+        md1 = bsum_f(p1, red) / (float)nz;
+    }
+    float local = 3.0e38f;
+    if (do_cfl && i < nr - 1 && i >= 0 && (i == 0 || i < nr - 1)) {
+        // shear limit: |vm_i / R_i - vm_{i+1} / R_{i+1}| with vm = Vref + mean dv
+        const float denom = fabsf(t.OmRefDiff[i] + md0 * t.InvRmed[i] - md1 * t.InvRmed[i + 1]) +
+                            1.0e-30f;
+        local = ph.cfl * g.dphi / denom;
+    }
+    const bool cfl_ring = do_cfl && i >= 1 && i < nr - 1;
+    for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+        const size_t c = row + j;
+        float c_s, n;
+        if (mode & 1) {
+            const float sg = S[c];
+            if (ph.adiabatic) {
+                const float e = E[c];
+                const float es = __fdividef(e, sg);
+                T[c] = ph.c_v_inv * es;
+                c_s = sqrtf(ph.g_gm1 * es);
+                const float h = c_s * t.HFacAdi[i];
+                cs[c] = c_s;
+                H[c] = h;
+                P[c] = ph.gm1 * e;
+                n = ph.alpha > 0.f ? ph.alpha * h * c_s : ph.constant_viscosity;
+            } else {
+                c_s = t.CsIso[i];
+                const float h = c_s * t.InvOmegaK[i];
+                P[c] = sg * (c_s * c_s);
+                if (mode & 2) {
+                    cs[c] = c_s;
+                    H[c] = h;
+                    T[c] = ph.mu_over_R * P[c] / sg;
+                }
+                n = ph.alpha > 0.f ? ph.alpha * h * c_s : ph.constant_viscosity;
+            }
+            nu[c] = n;
+        } else {
+            c_s = cs[c];
+            n = nu[c];
+        }
+        if (cfl_ring) {
+            const float d0 = dv[c];
+            const float vres = ph.fast_transport ? d0 - md0 : t.Vref[i] + d0;
+            const float invdt1 = c_s * t.InvCell[i];
+            const float invdt2 = vr[c] * t.InvDiffRsup[i];
+            const float invdt3 = vres * t.InvDxTheta[i];
+            const float vr1 = vr[c + nz];
+            const float dvA = dv[row + (j == nz - 1 ? 0 : j + 1)] - d0;
+            float invdt4;
+            if (ph.art_visc_sn) {
+                const float a = fmaxf(vr[c] - vr1, 0.f) * t.InvDiffRsup[i];
+                const float b = fmaxf(-dvA, 0.f) * t.InvDxTheta[i];
+                invdt4 = ph.four_C2 * fmaxf(a, b);
+            } else {
+                const float eps_rr = (vr1 - vr[c]) * t.InvDiffRsup[i];
+                const float eps_pp = t.InvRmed[i] * (dvA * g.invdphi + 0.5f * (vr1 + vr[c]));
+                invdt4 = ph.four_C2 * fmaxf(-(eps_rr + eps_pp), 0.f);
+            }
+            const float invdt5 = 4.f * n * t.InvCell2[i];
+            float invdt6 = 0.f;
+            if (ph.adiabatic) invdt6 = ph.inv_hc_limit * fabsf(__fdividef(qplus[c] - qminus[c], E[c]));
+            const float s2 = invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 +
+                             invdt4 * invdt4 + invdt5 * invdt5 + invdt6 * invdt6;
+            local = fminf(local, ph.cfl * rsqrtf(s2));
+        }
+    }
+    if (do_cfl) {
+        const float m = bmin_f(local, red);
+        if (threadIdx.x == 0 && m < 3.0e38f) atomicMin(dt_min, __float_as_uint(m));
+    }
+}
+
+}  // namespace fgpu32

@@ -9,6 +9,7 @@
 #include <stddef.h>
 
 #include <string>
+#include <vector>
 
 namespace fgpu32 {
 
@@ -75,6 +76,44 @@ struct StateF {
     float *sigma_lo;  // low part of the compensated sigma (sigma = sigma + sigma_lo)
 };
 
+// Every buffer and constant one disk's step touches, as the batched kernels
+// read it from device memory.  s holds the step-start state (vr, dv buffers
+// A); the source terms write the B buffers, transport writes back to A, so
+// the buffers a step uses are the same every step (graph-capturable).
+struct DiskF {
+    GeoF g;
+    TablesF t;
+    PhysF ph;
+    BcF bc;
+    DampingF dm;
+    StateF s;
+    float *vr_b, *dv_b;
+    float *sigma_t, *energy_t, *sigma_lo_t;  // after radial transport
+    float *mom[4];
+    float *pot, *P, *cs, *H, *nu, *T, *Qr, *Qp, *divv, *trr, *tpp, *trp, *qplus, *qminus;
+    unsigned int *dtmin;
+    int damping, nq;
+};
+
+// The per-step inputs of one disk: dt (FP64 for the FARGO phase, FP32 for
+// the rest), the start time, the cooling rate factor and the bodies.
+struct StepF {
+    double dt, t;
+    float fdt, beta_inv;
+    int run, pad;
+    BodiesF b;
+};
+
+// Device-side run clock of one disk (sim::CalculateTimeStep and the monitor
+// clamp of sim::run, simulation.cpp:100-118, 505-558) and the circular
+// orbits its planets follow around the central star.
+struct ClockF {
+    double t, last_dt, t_end, monitor_dt, cfl_max_var;
+    double G, mstar, beta_inv0, beta_ramp;
+    int n_monitor, steps, active, n_planets;
+    double q[kMaxBodies], a[kMaxBodies], phase[kMaxBodies];
+};
+
 // Damping ring set-up, computed by the FP64 set-up code (the same ring search).
 struct DampQSpec {
     int kind_in = 0, kind_out = 0, active_in = 0, active_out = 0, limit_in = 0, limit_out = 0;
@@ -95,6 +134,19 @@ class Engine32 {
     int step(double dt, double t);
     int disk_force(double px, double py, double pa, double rsm, double out[5]);
     int check_finite(int *field, int *nr_out, int *naz_out);
+    // the device description used by the batched kernels
+    DiskF describe();
+    const BodiesF &current_bodies() const { return bodies; }
+    double beta_inv_at(double t) const { return beta_inv(t); }
+    int rings() const { return nr; }
+    int azimuthal() const { return nz; }
+    const int *damping_rings(int *n) const
+    {
+        *n = (p.damping && n_rings) ? n_rings : 0;
+        return host_damp_rings.data();
+    }
+    const fgpu_params &params() const { return p; }
+    void set_cfl_valid(bool v) { cfl_valid = v; }
 
     DampQSpec damp_spec[4];
     std::string err;
@@ -127,6 +179,7 @@ class Engine32 {
     float *damp_mem = nullptr, *damp_aux = nullptr;
     int *damp_rings = nullptr;
     int n_rings = 0;
+    std::vector<int> host_damp_rings;
     double *partial = nullptr, *red_out = nullptr, *stage = nullptr;
     unsigned int *d_dtmin = nullptr;
     unsigned long long *d_bad = nullptr;

@@ -47,8 +47,24 @@ class Engine:
             raise EngineError(f"fgpu_create: {STATUS_NAMES.get(rc, rc)}")
         self.h = h
 
+    @classmethod
+    def attach(cls, handle, params: FgpuParams, radii, owner) -> "Engine":
+        """Front end for a handle owned by someone else (a disk of a batch);
+        closing it leaves the handle alone."""
+        self = cls.__new__(cls)
+        self.lib = load_library()
+        self.params = params
+        self.nr, self.nz = params.nrad, params.naz
+        self._radii = np.ascontiguousarray(radii, dtype=np.float64)
+        self.h = handle
+        self._owner = owner
+        return self
+
     # -- lifetime -----------------------------------------------------------
     def close(self):
+        if getattr(self, "_owner", None) is not None:
+            self.h = None
+            return
         if getattr(self, "h", None):
             self.lib.fgpu_destroy(self.h)
             self.h = None

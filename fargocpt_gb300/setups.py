@@ -128,3 +128,30 @@ def build(name, seed=1234):
     fields = initial_fields(d, radii, c["slope"], seed)
     nbody = CircularPlanets(c["planets"])
     return params_from_dict(d), d, radii, fields, nbody
+
+
+# Sweep of independent locally isothermal disks: each draws its grid and
+# physics from the seed; the radial range and the rest of the set-up are the
+# 128 x 384 single-planet disk's.
+SWEEP_NR = (128, 192, 256, 384, 512)
+
+
+def sweep(n_disks=64, seed=4, nr_choices=SWEEP_NR, precision=1):
+    """n_disks setups-style tuples (params, dict, radii, fields, nbody):
+    Nr uniform in nr_choices with Naz = 3 Nr, alpha log-uniform in
+    [1e-4, 1e-2], planet mass ratio log-uniform in [1e-5, 3e-3] at r = 1,
+    aspect ratio uniform in [0.03, 0.07], sigma slope uniform in [0.5, 1.5]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_disks):
+        nr = int(rng.choice(nr_choices))
+        alpha = 10.0 ** rng.uniform(-4.0, -2.0)
+        q = 10.0 ** rng.uniform(math.log10(1e-5), math.log10(3e-3))
+        h = rng.uniform(0.03, 0.07)
+        slope = rng.uniform(0.5, 1.5)
+        d = base_params(nr, 3 * nr, 0.4, 2.5, adiabatic=False, alpha=alpha, h=h)
+        d["precision"] = precision
+        radii = log_radii(nr, 0.4, 2.5)
+        fields = initial_fields(d, radii, slope, seed * 1000 + k)
+        out.append((params_from_dict(d), d, radii, fields, CircularPlanets([(q, 1.0, 0.0)])))
+    return out

@@ -267,6 +267,98 @@ int fgpu_disk_force_static(const double *sigma, const double *scale_height,
 			   double thickness_smoothing, const fgpu_body *body,
 			   double *out, void *stream);
 
+/* ------------------------------------------------------------------------
+ * Batched many-disk form.  No counterpart in the reference, which runs one
+ * disk per process (src/main.cpp); a parameter sweep there is many runs.  A
+ * batch holds n independent FP32-mixed disks of any sizes; every phase of
+ * the step is one grid-stride launch over all disks, each disk with its own
+ * dt.  The per-disk handles of fgpu_batch_disk take every single-disk call
+ * (upload, download, bodies, init_euler, CFL, boundary, force, mass,
+ * finiteness) and share the batch's stream; they belong to the batch
+ * (fgpu_destroy refuses them).
+ * ---------------------------------------------------------------------- */
+typedef struct fgpu_batch fgpu_batch;
+
+/* Tile shape of one batched kernel: threads per block and, for the per-cell
+ * kernels, rings per block (cells per thread along the radius); for the
+ * radial transport, rings one thread walks.  Ring kernels (azimuthal
+ * transport, damping, CFL) use one block per ring; their cells per thread
+ * follow from threads and the longest ring. */
+typedef struct {
+	int threads;
+	int rings;
+} fgpu_tile;
+
+enum fgpu_batch_kernel {
+	FGPU_BK_POTENTIAL = 0,
+	FGPU_BK_SOURCE,
+	FGPU_BK_ARTVISC_Q,
+	FGPU_BK_ARTVISC_V,
+	FGPU_BK_STRESS,
+	FGPU_BK_VISCOUS,
+	FGPU_BK_GHOST,
+	FGPU_BK_TRANSPORT_RADIAL,
+	FGPU_BK_TRANSPORT_AZIMUTHAL,
+	FGPU_BK_FINISH,
+	FGPU_BK_DAMPING,
+	FGPU_BK_DERIVED_CFL,
+	FGPU_BK_COUNT
+};
+
+typedef struct {
+	fgpu_tile k[FGPU_BK_COUNT];
+} fgpu_tiles;
+
+/* Device-side run clock of one disk: FargoCPT's CalculateTimeStep
+ * (src/simulation.cpp:100-118) and the monitor-time clamp of sim::run
+ * (:505-558), evaluated on the GPU so that a captured sequence of steps needs
+ * no host round trip.  The star (star_mass, at the origin) holds n_planets
+ * planets on circular orbits: planet k at radius a[k], angular speed
+ * sqrt(G (star_mass + mass[k]) / a^3), initial angle phase[k]; the indirect
+ * term is the one of the star-centred frame.  A disk steps while
+ * time < t_end.  steps counts the steps taken; active is 1 while the disk
+ * still steps. */
+typedef struct {
+	double time, last_dt, t_end, monitor_dt, cfl_max_var;
+	double star_mass;
+	int n_monitor, steps, active, n_planets;
+	double mass[16], a[16], phase[16];
+} fgpu_clock;
+
+/* params[k], radii[k]: disk k as for fgpu_create; every disk must select
+ * FGPU_PRECISION_FP32_MIXED.  1 <= n <= 1024. */
+int fgpu_batch_create(int n, const fgpu_params *params,
+		      const double *const *radii, fgpu_batch **out);
+int fgpu_batch_destroy(fgpu_batch *b);
+const char *fgpu_batch_last_error(const fgpu_batch *b);
+int fgpu_batch_size(const fgpu_batch *b, int *n);
+int fgpu_batch_disk(fgpu_batch *b, int k, fgpu_engine **disk);
+
+/* Tile shapes in use; fgpu_batch_set_tiles checks and applies them (a
+ * captured step sequence is rebuilt).  fgpu_batch_autotune times candidate
+ * shapes of every kernel on the batch's current state with CUDA events
+ * (reps timed launches each), keeps the fastest, writes them to *best and
+ * restores the state it started from. */
+int fgpu_batch_get_tiles(const fgpu_batch *b, fgpu_tiles *tiles);
+int fgpu_batch_set_tiles(fgpu_batch *b, const fgpu_tiles *tiles);
+int fgpu_batch_autotune(fgpu_batch *b, int reps, fgpu_tiles *best);
+
+/* One step of every disk with host-given dt[k] and t[k] (dt[k] = 0 skips
+ * disk k) and the bodies last given to each disk's handle: fgpu_step_euler
+ * of all disks at once. */
+int fgpu_batch_step(fgpu_batch *b, const double *dt, const double *t);
+
+/* Device clock: set or read disk k's clock.  fgpu_batch_run advances every
+ * disk by up to max_steps steps with its own CFL dt, stopping disks at
+ * their t_end, as CUDA graphs of steps_per_graph steps (captured once and
+ * relaunched); *n_active receives the number of disks still below t_end.
+ * Before the first run the disks need their initial state, init_euler and
+ * a valid CFL time step (fgpu_condition_cfl), as FargoCPT's start-up has. */
+int fgpu_batch_set_clock(fgpu_batch *b, int k, const fgpu_clock *clock);
+int fgpu_batch_get_clock(fgpu_batch *b, int k, fgpu_clock *clock);
+int fgpu_batch_run(fgpu_batch *b, int max_steps, int steps_per_graph,
+		   int *n_active);
+
 #ifdef __cplusplus
 }
 #endif

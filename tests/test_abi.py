@@ -78,3 +78,36 @@ def test_no_device_is_an_error_not_a_fallback(lib):
     h = C.c_void_p()
     rc = lib.fgpu_create(C.byref(p), radii.ctypes.data_as(C.POINTER(C.c_double)), C.byref(h))
     assert rc == -6
+
+
+def test_batch_arguments_and_missing_device(lib):
+    from gpu_cases import make_params
+    radii = np.linspace(0.4, 2.5, 18)
+    rp = (C.POINTER(C.c_double) * 2)(*[radii.ctypes.data_as(C.POINTER(C.c_double))] * 2)
+    p, _ = make_params(16, 48)
+    ps = (abi.FgpuParams * 2)(p, p)
+    h = C.c_void_p()
+    assert lib.fgpu_batch_create(0, ps, rp, C.byref(h)) == -1
+    assert lib.fgpu_batch_create(2, ps, None, C.byref(h)) == -1
+    # the batched form is FP32-mixed only
+    assert lib.fgpu_batch_create(2, ps, rp, C.byref(h)) == -4
+    for q in ps:
+        q.precision = 1
+    assert lib.fgpu_batch_destroy(None) == -1
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return
+    except ImportError:
+        pass
+    assert lib.fgpu_batch_create(2, ps, rp, C.byref(h)) == -6
+
+
+def test_batch_tile_table_round_trips():
+    t = abi.FgpuTiles()
+    for i in range(len(abi.BATCH_KERNELS)):
+        t.k[i].threads, t.k[i].rings = 32 * (i + 1), i + 1
+    d = t.to_dict()
+    assert list(d) == abi.BATCH_KERNELS
+    back = abi.FgpuTiles.from_dict(d)
+    assert bytes(back) == bytes(t)
