@@ -11,6 +11,14 @@ fields resident in HBM).  e2e: wall time of the drop-in call sequence a C++
 driver makes every step through the C ABI (CFL read-back, N-body state in,
 step, disk force on the planet read back).  Multi-GPU runs are independent
 replicas (the path does not shard across GPUs here).
+
+Beside the FP64 headline the line carries the FP32-mixed form on the same
+disk (``fp32_mixed``) and the batched form (``batched``): 64 independent
+FP32-mixed disks of different sizes, each with its own CFL dt from the
+device clock, stepped by one launch per phase over all disks, the timed
+steps captured as one CUDA graph, tile shapes from the autotuner; it is
+compared with the FP64 form stepping the same disks one after another.
+``--forms`` limits the run to some of the forms (for profiling).
 """
 from __future__ import annotations
 
@@ -36,7 +44,7 @@ KERNEL_BYTES_PER_CELL = {
     "derived_cfl": 88,
 }
 STEP_BYTES_PER_CELL = {"adiabatic": 64, "isothermal": 48}   # one read + write of the state
-KERNELS_PER_STEP = 15   # 13 step kernels + 2 disk-force kernels
+KERNELS_IN_TIMED_STEP = 13   # the adiabatic step's kernels between the step's events
 
 
 def parse():
@@ -48,6 +56,12 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--forms", default="fp64,fp32,batch,fp64disks",
+                    help="comma list of the forms to time: fp64 (the headline), fp32 "
+                    "(FP32-mixed, same disk), batch (64-disk FP32-mixed sweep), fp64disks "
+                    "(the FP64 form on the sweep's disks, one after another)")
+    ap.add_argument("--batch-disks", type=int, default=64)
+    ap.add_argument("--no-autotune", action="store_true")
     return ap.parse_args()
 
 
@@ -245,6 +259,101 @@ def measure(args, precision, cfg_name, torch, dist, local):
     return dict(total_ms=total_ms, e2e_s=e2e_s, phases=phases, nsteps=nsteps, cells=cells, d=d)
 
 
+def measure_batch(args, torch, dist):
+    """The batched form on the sweep of independent locally isothermal disks
+    (Nr in {128..512}, Naz = 3 Nr, seeded physics): every disk with its own
+    CFL dt from the device clock, `args.steps` steps captured as one CUDA
+    graph; inputs (about 1.8 GB of fields) far exceed the 129 MB L2."""
+    import numpy as np
+
+    from fargocpt_gb300 import setups
+    from fargocpt_gb300.batch import Batch, orbits_to_time, start_disks
+
+    disks = setups.sweep(args.batch_disks, seed=4)
+    cells = np.array([x[0].nrad * x[0].naz for x in disks], dtype=np.float64)
+    b = Batch([x[0] for x in disks], [x[2] for x in disks])
+    t_end = orbits_to_time(2.0)
+    start_disks(b, disks, t_end=t_end, monitor_dt=t_end / 20)
+    t0 = time.perf_counter()
+    tiles = b.tiles() if args.no_autotune else b.autotune(reps=5)
+    tune_s = time.perf_counter() - t0
+    stream = torch.cuda.ExternalStream(b.disks[0].stream)
+
+    def steps():
+        return np.array([b.clock(k)["steps"] for k in range(b.n)], dtype=np.float64)
+
+    b.run(args.warmup, steps_per_graph=max(1, args.warmup))
+    b.run(args.steps, steps_per_graph=args.steps)   # captures the timed graph
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    s0 = steps()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.run(args.steps, steps_per_graph=args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    s1 = steps()
+    updates = float(np.sum((s1 - s0) * cells))
+    # end to end through the C ABI with host buffers: per step, every disk's
+    # CFL dt read back, its bodies and (dt, t) sent (fgpu_batch_step)
+    dts = np.empty(b.n)
+    ts = np.array([b.clock(k)["time"] for k in range(b.n)])
+    e2e_updates = 0.0
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
+        for k, (_, _, _, _, nbody) in enumerate(disks):
+            dts[k] = b.disks[k].condition_cfl()
+            bk = nbody.bodies(ts[k])
+            b.disks[k].set_bodies(bk, *nbody.indirect(bk), 0.0)
+        b.step(dts, ts)
+        ts += dts
+        e2e_updates += float(np.sum(cells))
+    e2e_s = time.perf_counter() - w0
+    for e in b.disks:
+        assert e.check_finite() is None, "non-finite state after the batched benchmark"
+    out = dict(ms=ms, updates=updates, e2e_s=e2e_s, e2e_updates=e2e_updates, tiles=tiles,
+               tune_s=tune_s, cells=float(np.sum(cells)), n=b.n,
+               nr=sorted(set(int(x[0].nrad) for x in disks)))
+    b.close()
+    return out, disks
+
+
+def measure_fp64_disks(disks, torch, steps=5, warmup=2):
+    """The FP64 form on the same disks, one engine after another (each disk
+    alone on the GPU, as FargoCPT runs one disk per process)."""
+    from fargocpt_gb300.abi import params_from_dict
+    from fargocpt_gb300.engine import Engine
+
+    total_ms, updates = 0.0, 0.0
+    for params, d, radii, fields, nbody in disks:
+        d64 = dict(d)
+        d64["precision"] = 0
+        eng = Engine(params_from_dict(d64), radii)
+        load_disk(eng, fields, nbody)
+        stream = torch.cuda.ExternalStream(eng.stream)
+        t = 0.0
+        for n in range(warmup + steps):
+            if n == warmup:
+                eng.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            dt = eng.condition_cfl()
+            b = nbody.bodies(t)
+            eng.set_bodies(b, *nbody.indirect(b), 0.0)
+            eng.step_euler(dt, t)
+            t += dt
+        e1 = torch.cuda.Event(enable_timing=True)
+        e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+        updates += steps * d["nrad"] * d["naz"]
+        eng.close()
+    return updates / (total_ms * 1e-3)
+
+
 def roofline(res, steps, bytes_scale):
     peak, peak_src = peaks()
     phases, nsteps, cells, d = res["phases"], res["nsteps"], res["cells"], res["d"]
@@ -286,26 +395,74 @@ def main():
         dist.barrier()
     torch.cuda.set_device(local)
 
+    forms = set(args.forms.split(","))
     sampler = ClockSampler(local)
     sampler.start()
-    r64 = measure(args, "fp64", args.config, torch, dist, local)
-    r32 = measure(args, "fp32", args.config, torch, dist, local)
+    r64 = measure(args, "fp64", args.config, torch, dist, local) if "fp64" in forms else None
+    r32 = measure(args, "fp32", args.config, torch, dist, local) if "fp32" in forms else None
+    rb, bdisks = measure_batch(args, torch, dist) if "batch" in forms else (None, None)
     clocks = sampler.stop()
+    fp64_same = (measure_fp64_disks(bdisks, torch)
+                 if rb is not None and "fp64disks" in forms else None)
 
-    vals = [r64["total_ms"], r64["e2e_s"], r32["total_ms"], r32["e2e_s"]]
+    vals = [r64["total_ms"] if r64 else 1.0, r64["e2e_s"] if r64 else 1.0,
+            r32["total_ms"] if r32 else 1.0, r32["e2e_s"] if r32 else 1.0,
+            rb["ms"] if rb else 1.0, rb["e2e_s"] if rb else 1.0]
     if dist is not None:
         tt = torch.tensor(vals, device="cuda", dtype=torch.float64)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         vals = [float(x) for x in tt]
     if rank != 0:
         return
+    batched = None
+    if rb is not None:
+        bvalue = world * rb["updates"] / (vals[4] * 1e-3)
+        peak, peak_src = peaks()
+        batched = {
+            "value": bvalue, "unit": "cell-updates/s", "ms_per_step": vals[4] / args.steps,
+            "workload": f"{rb['n']} independent locally isothermal FP32-mixed disks, Nr in "
+                        f"{rb['nr']}, Naz = 3 Nr, {rb['cells']:.0f} cells, own CFL dt each "
+                        "(device clock), seeded alpha/q/h/slope, steps as one CUDA graph, "
+                        "inputs larger than L2",
+            "e2e": {"value": world * rb["e2e_updates"] / vals[5], "unit": "cell-updates/s",
+                    "h2d_bytes_per_step": rb["n"] * (2 * 40 + 16),
+                    "d2h_bytes_per_step": rb["n"] * 8,
+                    "path": "host clock: per step every disk's CFL dt read, bodies and "
+                            "(dt, t) sent, fgpu_batch_step"},
+            "fp64_same_disks": fp64_same,
+            "speedup_vs_fp64_same_disks": bvalue / fp64_same if fp64_same else None,
+            "roofline_step": {"achieved": bvalue * 24 / 1e9, "peak": peak, "unit": "GB/s",
+                              "frac": bvalue * 24 / 1e9 / peak, "bytes_per_cell": 24,
+                              "peak_source": peak_src},
+            "tiles": rb["tiles"], "autotune_s": rb["tune_s"],
+            "gpu_launches": 14 * args.steps,
+            "error": "per disk the FP32-mixed arithmetic (bit-identical to the single-disk "
+                     "FP32-mixed engine); python -m fargocpt_gb300.accuracy gives its error",
+        }
+    if r64 is None:
+        print(json.dumps({"forms": sorted(forms), "batched": batched,
+                          "fp32_mixed_ms": vals[2] / args.steps if r32 else None,
+                          "clocks": clocks}))
+        return
     cells = r64["cells"]
     value = world * cells * args.steps / (vals[0] * 1e-3)
     e2e = world * cells * args.steps / vals[1]
-    value32 = world * cells * args.steps / (vals[2] * 1e-3)
-    e2e32 = world * cells * args.steps / vals[3]
     rl, rls = roofline(r64, args.steps, 1.0)
-    rl32, rls32 = roofline(r32, args.steps, 0.5)
+    fp32 = None
+    if r32 is not None:
+        value32 = world * cells * args.steps / (vals[2] * 1e-3)
+        e2e32 = world * cells * args.steps / vals[3]
+        rl32, rls32 = roofline(r32, args.steps, 0.5)
+        fp32 = {
+            "value": value32, "unit": "cell-updates/s", "ms_per_step": vals[2] / args.steps,
+            "e2e": {"value": e2e32, "unit": "cell-updates/s", "h2d_bytes_per_step": 80,
+                    "d2h_bytes_per_step": 4 + 40},
+            "speedup_vs_fp64": value32 / value,
+            "roofline": rl32, "roofline_step": rls32,
+            "phase_ms_per_step": {k: v / max(1, r32["nsteps"])
+                                  for k, v in r32["phases"].items()},
+            "error": "see python -m fargocpt_gb300.accuracy (relative L1/Linf vs FP64)",
+        }
     line = {
         "metric": "cell-updates/s/GPU, plain FP64 vs mixed-precision & batched at stated error",
         "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps,
@@ -318,17 +475,9 @@ def main():
         "roofline": rl,
         "roofline_step": rls,
         "phase_ms_per_step": {k: v / max(1, r64["nsteps"]) for k, v in r64["phases"].items()},
-        "fp32_mixed": {
-            "value": value32, "unit": "cell-updates/s", "ms_per_step": vals[2] / args.steps,
-            "e2e": {"value": e2e32, "unit": "cell-updates/s", "h2d_bytes_per_step": 80,
-                    "d2h_bytes_per_step": 4 + 40},
-            "speedup_vs_fp64": value32 / value,
-            "roofline": rl32, "roofline_step": rls32,
-            "phase_ms_per_step": {k: v / max(1, r32["nsteps"])
-                                  for k, v in r32["phases"].items()},
-            "error": "see python -m fargocpt_gb300.accuracy (relative L1/Linf vs FP64)",
-        },
-        "gpu_launches": 2 * args.steps * KERNELS_PER_STEP,
+        "fp32_mixed": fp32,
+        "batched": batched,
+        "gpu_launches": args.steps * KERNELS_IN_TIMED_STEP,
         "clocks": clocks,
     }
     if not args.no_cpu_baseline:
