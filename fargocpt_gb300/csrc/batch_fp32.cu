@@ -192,24 +192,27 @@ __global__ void b_transport_radial(const DiskF *__restrict__ D, const StepF *__r
     }
 }
 
-// azimuthal transport: one ring per block iteration; PER * blockDim.x covers
-// the longest ring of the batch; dynamic shared memory 4 * naz_max floats
+// azimuthal transport: one ring per block iteration, PER cells per thread
+// strided over the block; PER * blockDim.x covers the longest ring of the
+// batch; the transported quantities are staged in dynamic shared memory,
+// azimuthal_smem_floats(naz_max, nq_max, true) floats
 template <int PER>
 __global__ void __launch_bounds__(512) b_transport_azimuthal(const DiskF *__restrict__ D,
                                                              const StepF *__restrict__ S,
                                                              const int *__restrict__ start, int nd)
 {
-    extern __shared__ float smf[];
-    __shared__ double red[33];
+    extern __shared__ __align__(16) float smf[];
+    __shared__ float redf[33];
+    __shared__ long long redl[33];
     const int total = __ldg(start + nd);
     for (int item = blockIdx.x; item < total; item += gridDim.x) {
         const int d = disk_of(start, nd, item);
         if (!S[d].run) continue;
         const DiskF &k = D[d];
         const int i = item - __ldg(start + d);
-        azimuthal_ring<PER>(k.g, k.t, S[d].dt, k.ph.limiter_mc, k.ph.fast_transport, k.nq, k.dv_b,
+        azimuthal_ring<PER, true>(k.g, k.t, S[d].dt, k.ph.limiter_mc, k.ph.fast_transport, k.nq, k.dv_b,
                             k.mom[0], k.mom[1], k.mom[2], k.mom[3], k.energy_t, k.sigma_t,
-                            k.sigma_lo_t, i, smf, red);
+                            k.sigma_lo_t, i, smf, redf, redl);
     }
 }
 
@@ -218,11 +221,12 @@ __global__ void b_damping(const DiskF *__restrict__ D, const StepF *__restrict__
                           const int2 *__restrict__ items, int n)
 {
     __shared__ float red[33];
+    __shared__ long long redl[33];
     for (int it = blockIdx.x; it < n; it += gridDim.x) {
         const int2 w = items[it];
         if (!S[w.x].run) continue;
         const DiskF &k = D[w.x];
-        damping_ring(k.g, k.dm, S[w.x].fdt, k.s, w.y, red);
+        damping_ring(k.g, k.dm, S[w.x].fdt, k.s, w.y, red, redl);
     }
 }
 
@@ -231,6 +235,7 @@ __global__ void b_derived_cfl(const DiskF *__restrict__ D, const StepF *__restri
                               const int *__restrict__ start, int nd, int mode, int all)
 {
     __shared__ float red[33];
+    __shared__ long long redl[33];
     const int total = __ldg(start + nd);
     for (int item = blockIdx.x; item < total; item += gridDim.x) {
         const int d = disk_of(start, nd, item);
@@ -238,7 +243,7 @@ __global__ void b_derived_cfl(const DiskF *__restrict__ D, const StepF *__restri
         const DiskF &k = D[d];
         const int i = item - __ldg(start + d);
         derived_cfl_ring(k.g, k.t, k.ph, mode, k.s.sigma, k.s.energy, k.s.vr, k.s.dv, k.qplus,
-                         k.qminus, k.cs, k.H, k.P, k.T, k.nu, k.dtmin, i, red);
+                         k.qminus, k.cs, k.H, k.P, k.T, k.nu, k.dtmin, i, red, redl);
     }
 }
 
@@ -563,7 +568,8 @@ static void launch_kernel(fgpu_batch *b, int k, int ghost_b = 0)
         break;
     case FGPU_BK_FINISH: b_finish<<<g, th, 0, s>>>(D, S, b->table(k), nd, r); break;
     case FGPU_BK_DAMPING:
-        if (b->n_damp_items) b_damping<<<g, th, 0, s>>>(D, S, b->d_damp_items, b->n_damp_items);
+        if (b->n_damp_items)
+            b_damping<<<g, th, 0, s>>>(D, S, b->d_damp_items, b->n_damp_items);
         break;
     case FGPU_BK_DERIVED_CFL:
         b_derived_cfl<<<g, th, 0, s>>>(D, S, b->table(k), nd, 1 | 4, 0);
@@ -672,8 +678,10 @@ extern "C" int fgpu_batch_create(int n, const fgpu_params *params, const double 
         b->aux[k].star_is_centre = 0;
     }
     b->n_damp_items = (int)damp.size();
-    b->az_smem = (size_t)4 * b->nz_max * sizeof(float);
-    if (b->az_smem > 200 * 1024) {
+    int nq_max = 4;
+    for (int k = 0; k < n; ++k) nq_max = std::max(nq_max, desc[k].nq);
+    b->az_smem = azimuthal_smem_floats(b->nz_max, nq_max, true) * sizeof(float);
+    if (b->az_smem > kMaxRingSmem) {
         b->err = "ring too long for the batched azimuthal kernel";
         return fail(FGPU_ERR_UNSUPPORTED);
     }

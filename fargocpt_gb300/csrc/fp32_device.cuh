@@ -95,6 +95,54 @@ __device__ __forceinline__ float bmin_f(float v, float *red)
     return block_reduce<float, warp_min_f>(v, red, 3.0e38f);
 }
 
+__device__ __forceinline__ float warp_max_f(float v)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ long long warp_sum_ll(long long v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Ring sums that do not depend on the block's shape.  Every value is rounded
+// to a multiple of 2^-k and the resulting 64-bit integers are added; integer
+// addition is associative, so neither the tile shape a kernel runs with nor
+// the order of the threads changes a bit of the result.  k is the largest
+// exponent for which n values of at most the block's largest |x| stay below
+// 2^62 in total; the sum is then within n 2^-k (about 2^-51 n max|x|) of the
+// exact one.  Every thread of the block must call both steps.
+//
+// Step 1: the scale, from the block's largest |x| (an exact reduction).
+__device__ __forceinline__ int exact_sum_scale(float local_absmax, int n, float *redf)
+{
+    const float m = block_reduce<float, warp_max_f>(local_absmax, redf, 0.f);
+    int e = 0;
+    frexpf(m, &e);                // m < 2^e
+    const int ln = 32 - __clz(n);  // n < 2^ln
+    return 62 - e - ln;
+}
+__device__ __forceinline__ long long to_fixed(float x, int k) { return __float2ll_rn(ldexpf(x, k)); }
+// Step 2: the sum of the threads' integer partial sums.
+__device__ __forceinline__ double exact_sum_result(long long part, int k, long long *redl)
+{
+    const long long s = block_reduce<long long, warp_sum_ll>(part, redl, 0LL);
+    return ldexp((double)s, -k);
+}
+
+// Mean of row[0 .. n-1] (global memory, cells strided over the block).
+__device__ __forceinline__ float exact_row_mean(const float *row, int n, float *redf,
+                                                long long *redl)
+{
+    float m = 0.f;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) m = fmaxf(m, fabsf(row[j]));
+    const int k = exact_sum_scale(m, n, redf);
+    long long part = 0;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) part += to_fixed(row[j], k);
+    return (float)(exact_sum_result(part, k, redl) / (double)n);
+}
+
 // ---------------------------------------------------------------------------
 // Potential residual Phi - Phi_K (CalculateNbodyPotential, Pframeforce.cpp:21-86)
 // ---------------------------------------------------------------------------
@@ -683,31 +731,55 @@ __device__ __forceinline__ void ring_pass_f(float *S, float *SS, float *W, float
     __syncthreads();
 }
 
-// smf: 4 * nz floats of shared memory; red: 33 doubles of shared memory
-template <int PER>
+// Shared memory of azimuthal_ring: 4 ring-long work arrays, plus the nq
+// quantity rows when STAGE (then every row is read from HBM once, up front,
+// and the passes and the shift work in shared memory).
+__host__ __device__ constexpr size_t azimuthal_smem_floats(int nz, int nq, bool stage)
+{
+    return (size_t)(stage ? 4 + nq : 4) * (size_t)nz;
+}
+
+// smf: azimuthal_smem_floats(nz, nq, STAGE) floats of shared memory; redf: 33
+// floats, redl: 33 long longs (shared memory)
+template <int PER, bool STAGE>
 __device__ __forceinline__ void azimuthal_ring(const GeoF &g, const TablesF &t, double dt, int mc,
                                                int fast, int nq, const float *__restrict__ dv,
                                                float *m0, float *m1, float *m2, float *m3,
                                                float *E, float *S, float *S_lo, int i, float *smf,
-                                               double *red)
+                                               float *redf, long long *redl)
 {
     const int nz = g.nz;
     const int tid = threadIdx.x, bs = blockDim.x;
     const size_t row = (size_t)i * nz;
     float *Sr = smf, *SS = smf + nz, *W = smf + 2 * nz, *D = smf + 3 * nz;
+    float *grow[5] = {m0 + row, m1 + row, m2 + row, m3 + row, E + row};
+    float *qrow[5];
+#pragma unroll
+    for (int q = 0; q < 5; ++q) qrow[q] = STAGE ? smf + (size_t)(4 + q) * nz : grow[q];
 
     float vown[PER], slo[PER];
-    double part = 0.0;
+    float amax = 0.f;
 #pragma unroll
     for (int n = 0; n < PER; ++n) {
         const int j = tid + n * bs;
         if (j < nz) {
             vown[n] = dv[row + j];
-            part += (double)vown[n];
+            amax = fmaxf(amax, fabsf(vown[n]));
+            Sr[j] = S[row + j];
+            slo[n] = S_lo[row + j];
+            if (STAGE) {
+                for (int q = 0; q < nq; ++q) qrow[q][j] = grow[q][j];
+            }
         }
     }
-    // ring mean of v_phi and the FARGO shift phase in FP64 (:174-236)
-    const double mean_dv = bsum_d(part, red) / (double)nz;
+    // ring mean of v_phi, independent of the block's shape, and the FARGO
+    // shift phase in FP64 (:174-236)
+    const int ks = exact_sum_scale(amax, nz, redf);
+    long long part = 0;
+#pragma unroll
+    for (int n = 0; n < PER; ++n)
+        if (tid + n * bs < nz) part += to_fixed(vown[n], ks);
+    const double mean_dv = exact_sum_result(part, ks, redl) / (double)nz;
     const double vmean = t.Vref_d[i] + mean_dv;
     const double Ntilde = vmean * t.InvRmed_d[i] * dt * g.invdphi_d;
     const double Nround = floor(Ntilde + 0.5);
@@ -722,12 +794,8 @@ __device__ __forceinline__ void azimuthal_ring(const GeoF &g, const TablesF &t, 
             float vres = vown[n] - mdv;
             if (!fast) vres = vt + vres;
             vown[n] = vres;
-            Sr[j] = S[row + j];
-            slo[n] = S_lo[row + j];
         }
     }
-    __syncthreads();
-    float *qrow[5] = {m0 + row, m1 + row, m2 + row, m3 + row, E + row};
     const float dxtheta = g.dphi * t.Rmed[i];
     const float half_invdx = 0.5f / dxtheta;
     const float dxrad = (t.Rsup[i] - t.Rinf[i]) * (float)dt;
@@ -738,25 +806,44 @@ __device__ __forceinline__ void azimuthal_ring(const GeoF &g, const TablesF &t, 
         ring_pass_f<PER>(Sr, SS, W, D, qrow, nq, vown, slo, (float)dt, dxtheta, half_invdx, dxrad,
                          invsurf, nz, mc, true, vt);
     }
-    for (int q = 0; q <= nq; ++q) {
-        float *Q = q < nq ? qrow[q] : S + row;
-        const float *src = q < nq ? qrow[q] : Sr;
+    // the integer shift (AdvectSHIFT, :238-268): cell j takes cell j - nshift
+    const int ns = nshift % nz;
+    int src[PER];
 #pragma unroll
-        for (int n = 0; n < PER; ++n) {
-            const int j = tid + n * bs;
-            if (j < nz) W[j] = src[j];
-        }
-        __syncthreads();
+    for (int n = 0; n < PER; ++n) {
+        int ji = tid + n * bs - ns;
+        if (ji < 0) ji += nz;
+        else if (ji >= nz) ji -= nz;
+        src[n] = ji;
+    }
+    if (STAGE) {
+        // all rows are in shared memory: shift straight out of it
+        for (int q = 0; q <= nq; ++q) {
+            const float *from = q < nq ? qrow[q] : Sr;
+            float *to = q < nq ? grow[q] : S + row;
 #pragma unroll
-        for (int n = 0; n < PER; ++n) {
-            const int j = tid + n * bs;
-            if (j < nz) {
-                int ji = (j - nshift) % nz;
-                if (ji < 0) ji += nz;
-                Q[j] = W[ji];
+            for (int n = 0; n < PER; ++n) {
+                const int j = tid + n * bs;
+                if (j < nz) to[j] = from[src[n]];
             }
         }
-        __syncthreads();
+    } else {
+        for (int q = 0; q <= nq; ++q) {
+            float *Q = q < nq ? grow[q] : S + row;
+            const float *from = q < nq ? grow[q] : Sr;
+#pragma unroll
+            for (int n = 0; n < PER; ++n) {
+                const int j = tid + n * bs;
+                if (j < nz) W[j] = from[j];
+            }
+            __syncthreads();
+#pragma unroll
+            for (int n = 0; n < PER; ++n) {
+                const int j = tid + n * bs;
+                if (j < nz) Q[j] = W[src[n]];
+            }
+            __syncthreads();
+        }
     }
     // the low part of sigma moves with it
 #pragma unroll
@@ -768,11 +855,7 @@ __device__ __forceinline__ void azimuthal_ring(const GeoF &g, const TablesF &t, 
 #pragma unroll
     for (int n = 0; n < PER; ++n) {
         const int j = tid + n * bs;
-        if (j < nz) {
-            int ji = (j - nshift) % nz;
-            if (ji < 0) ji += nz;
-            S_lo[row + j] = W[ji];
-        }
+        if (j < nz) S_lo[row + j] = W[src[n]];
     }
     // the caller may reuse smf for the next ring
     __syncthreads();
@@ -810,16 +893,16 @@ __device__ __forceinline__ void finish_cell(
 }
 
 // damping zones (damping.cpp:311-776); block-wide over ring i
+// red: 33 floats, redl: 33 long longs (shared memory)
 __device__ __forceinline__ void damp_ring_f(float *X, float *X0, const DampQF &d, int i, int nz,
-                                            int outer, float dt, float *red, float *Xlo)
+                                            int outer, float dt, float *red, float *Xlo,
+                                            long long *redl)
 {
     const int kind = outer ? d.kind_out : d.kind_in;
     const size_t row = (size_t)i * nz;
     float x0c = 0.f;
     if (kind == 3) {
-        float part = 0.f;
-        for (int j = threadIdx.x; j < nz; j += blockDim.x) part += X[row + j];
-        const float mean = bsum_f(part, red) / nz;
+        const float mean = exact_row_mean(X + row, nz, red, redl);
         if (threadIdx.x == 0) X0[row] = mean;
         x0c = mean;
     } else if (kind == 2) {
@@ -837,7 +920,7 @@ __device__ __forceinline__ void damp_ring_f(float *X, float *X0, const DampQF &d
 }
 
 __device__ __forceinline__ void damping_ring(const GeoF &g, const DampingF &dm, float dt,
-                                             const StateF &s, int i, float *red)
+                                             const StateF &s, int i, float *red, long long *redl)
 {
     const int nz = g.nz, nr = g.nr;
     float *X[4] = {s.vr, s.dv, s.sigma, s.energy};
@@ -847,9 +930,9 @@ __device__ __forceinline__ void damping_ring(const GeoF &g, const DampingF &dm, 
         const int size = d.vector ? nr + 1 : nr;
         float *lo = q == 2 ? s.sigma_lo : nullptr;
         if (d.kind_in != 0 && d.active_in && i <= d.limit_in)
-            damp_ring_f(X[q], X0[q], d, i, nz, 0, dt, red, lo);
+            damp_ring_f(X[q], X0[q], d, i, nz, 0, dt, red, lo, redl);
         if (d.kind_out != 0 && d.active_out && i >= d.limit_out && i < size)
-            damp_ring_f(X[q], X0[q], d, i, nz, 1, dt, red, lo);
+            damp_ring_f(X[q], X0[q], d, i, nz, 1, dt, red, lo, redl);
     }
 }
 
@@ -861,20 +944,16 @@ __device__ __forceinline__ void derived_cfl_ring(
     const float *__restrict__ E, const float *__restrict__ vr, const float *__restrict__ dv,
     const float *__restrict__ qplus, const float *__restrict__ qminus, float *__restrict__ cs,
     float *__restrict__ H, float *__restrict__ P, float *__restrict__ T, float *__restrict__ nu,
-    unsigned int *__restrict__ dt_min, int i, float *red)
+    unsigned int *__restrict__ dt_min, int i, float *red, long long *redl)
 {
     const int nz = g.nz, nr = g.nr;
     const size_t row = (size_t)i * nz;
     const bool do_cfl = (mode & 4) != 0;
     float md0 = 0.f, md1 = 0.f;
     if (do_cfl && i < nr - 1) {
-        float p0 = 0.f, p1 = 0.f;
-        for (int j = threadIdx.x; j < nz; j += blockDim.x) {
-            p0 += dv[row + j];
-            p1 += dv[row + nz + j];
-        }
-        md0 = bsum_f(p0, red) / (float)nz;
-        md1 = bsum_f(p1, red) / (float)nz;
+        // ring means of dv, independent of the block's shape
+        md0 = exact_row_mean(dv + row, nz, red, redl);
+        md1 = exact_row_mean(dv + row + nz, nz, red, redl);
     }
     float local = 3.0e38f;
     if (do_cfl && i < nr - 1 && i >= 0 && (i == 0 || i < nr - 1)) {

@@ -14,6 +14,8 @@
 namespace fgpu32 {
 
 constexpr int kMaxBodies = 16;
+// dynamic shared memory a ring kernel may ask for (227 KB less static use)
+constexpr size_t kMaxRingSmem = 220 * 1024;
 
 struct GeoF {
     int nr, nz;
@@ -186,6 +188,7 @@ class Engine32 {
     double *h_pinned = nullptr;
     int per = 4, az_block = 128;
     size_t az_smem = 0;
+    bool az_stage = false;
     bool cfl_valid = false;
 };
 

@@ -25,6 +25,7 @@
 #include "../../include/fargocpt_gb300.h"
 #include "fp32_engine.h"
 #include "fp32_device.cuh"
+#include "reduce.cuh"
 
 #include <cuda_runtime.h>
 
@@ -125,7 +126,7 @@ __global__ void f_transport_radial(GeoF g, TablesF t, float dt, int mc, int chun
                    S_lo_out, blockIdx.y * chunk, j);
 }
 
-template <int PER>
+template <int PER, bool STAGE>
 __global__ void __launch_bounds__(512) f_transport_azimuthal(GeoF g, TablesF t, double dt, int mc,
                                                              int fast, int nq,
                                                              const float *__restrict__ dv,
@@ -133,10 +134,11 @@ __global__ void __launch_bounds__(512) f_transport_azimuthal(GeoF g, TablesF t, 
                                                              float *m3, float *E, float *S,
                                                              float *S_lo)
 {
-    extern __shared__ float smf[];
-    __shared__ double red[33];
-    azimuthal_ring<PER>(g, t, dt, mc, fast, nq, dv, m0, m1, m2, m3, E, S, S_lo, blockIdx.x, smf,
-                        red);
+    extern __shared__ __align__(16) float smf[];
+    __shared__ float redf[33];
+    __shared__ long long redl[33];
+    azimuthal_ring<PER, STAGE>(g, t, dt, mc, fast, nq, dv, m0, m1, m2, m3, E, S, S_lo,
+                               blockIdx.x, smf, redf, redl);
 }
 
 __global__ void f_finish(GeoF g, TablesF t, PhysF ph, const float *__restrict__ m0,
@@ -156,7 +158,8 @@ __global__ void f_finish(GeoF g, TablesF t, PhysF ph, const float *__restrict__ 
 __global__ void f_damping(GeoF g, DampingF dm, float dt, const int *__restrict__ rings, StateF s)
 {
     __shared__ float red[33];
-    damping_ring(g, dm, dt, s, rings[blockIdx.x], red);
+    __shared__ long long redl[33];
+    damping_ring(g, dm, dt, s, rings[blockIdx.x], red, redl);
 }
 
 __global__ void f_derived_cfl(GeoF g, TablesF t, PhysF ph, int mode, const float *__restrict__ S,
@@ -167,8 +170,9 @@ __global__ void f_derived_cfl(GeoF g, TablesF t, PhysF ph, int mode, const float
                               float *__restrict__ nu, unsigned int *__restrict__ dt_min)
 {
     __shared__ float red[33];
+    __shared__ long long redl[33];
     derived_cfl_ring(g, t, ph, mode, S, E, vr, dv, qplus, qminus, cs, H, P, T, nu, dt_min,
-                     blockIdx.x, red);
+                     blockIdx.x, red, redl);
 }
 
 // disk force on a body and gas mass: FP64 separations and accumulation
@@ -217,18 +221,11 @@ __global__ void f_disk_force(GeoF g, TablesF t, PhysF ph, double px, double py, 
     }
 }
 
+// one warp per component
 __global__ void f_reduce_rows(const double *__restrict__ partial, int rows, double *__restrict__ out)
 {
-    const int w = threadIdx.x;
-    if (w >= 5) return;
-    double s = 0.0, comp = 0.0;
-    for (int r = 0; r < rows; ++r) {
-        const double y = partial[(size_t)r * 5 + w] - comp;
-        const double tt = s + y;
-        comp = (tt - s) - y;
-        s = tt;
-    }
-    out[w] = s;
+    const int w = threadIdx.x >> 5;
+    if (w < 5) warp_compensated_rows(partial, rows, 5, w, out);
 }
 
 __global__ void f_check_finite(const float *__restrict__ x, size_t n, unsigned long long *bad)
@@ -515,21 +512,27 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
     // azimuthal kernel configuration
     per = nz <= 2048 ? 4 : (nz <= 4096 ? 8 : 16);
     az_block = std::max(128, std::min(512, ((nz + per - 1) / per + 31) / 32 * 32));
-    az_smem = (size_t)4 * nz * sizeof(float);
-    if (az_smem > 200 * 1024) {
+    // cells strided over the block; the transported quantities staged in
+    // shared memory when they fit in its 227 KB
+    const int nq = phys.adiabatic ? 5 : 4;
+    az_stage = azimuthal_smem_floats(nz, nq, true) * sizeof(float) <= kMaxRingSmem;
+    az_smem = azimuthal_smem_floats(nz, nq, az_stage) * sizeof(float);
+    if (az_smem > kMaxRingSmem) {
         err = "ring too long for the FP32 azimuthal kernel";
         return FGPU_ERR_UNSUPPORTED;
     }
-    cudaError_t e1 = cudaFuncSetAttribute(f_transport_azimuthal<4>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)az_smem);
-    cudaError_t e2 = cudaFuncSetAttribute(f_transport_azimuthal<8>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)az_smem);
-    cudaError_t e3 = cudaFuncSetAttribute(f_transport_azimuthal<16>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)az_smem);
-    if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
-        err = "cannot reserve shared memory for the FP32 azimuthal kernel";
-        return FGPU_ERR_CUDA;
+    const void *az_kernels[6] = {
+        (const void *)f_transport_azimuthal<4, false>, (const void *)f_transport_azimuthal<8, false>,
+        (const void *)f_transport_azimuthal<16, false>, (const void *)f_transport_azimuthal<4, true>,
+        (const void *)f_transport_azimuthal<8, true>, (const void *)f_transport_azimuthal<16, true>};
+    for (const void *fn : az_kernels) {
+        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)az_smem) !=
+            cudaSuccess) {
+            err = "cannot reserve shared memory for the FP32 azimuthal kernel";
+            return FGPU_ERR_CUDA;
+        }
     }
+
     CKF(cudaDeviceSynchronize());
     return FGPU_OK;
 }
@@ -770,13 +773,19 @@ int Engine32::step(double dt, double t)
     mark(7);
     {
         const int nq = adi ? 5 : 4;
-#define AZ32(P)                                                                                  \
-    f_transport_azimuthal<P><<<nr, az_block, az_smem, stream>>>(                                 \
+#define AZ32(P, ST)                                                                              \
+    f_transport_azimuthal<P, ST><<<nr, az_block, az_smem, stream>>>(                             \
         geo, tabs, dt, phys.limiter_mc, phys.fast_transport, nq, s.dv, mom[0], mom[1], mom[2],  \
         mom[3], alt_e, alt_sigma, alt_sigma_lo)
-        if (per == 4) AZ32(4);
-        else if (per == 8) AZ32(8);
-        else AZ32(16);
+        if (az_stage) {
+            if (per == 4) AZ32(4, true);
+            else if (per == 8) AZ32(8, true);
+            else AZ32(16, true);
+        } else {
+            if (per == 4) AZ32(4, false);
+            else if (per == 8) AZ32(8, false);
+            else AZ32(16, false);
+        }
 #undef AZ32
     }
     mark(8);
@@ -805,7 +814,7 @@ int Engine32::disk_force(double px, double py, double pa, double rsm, double out
     const int rows = nr - 2;
     f_disk_force<<<rows, 256, 0, stream>>>(geo, tabs, phys, px, py, pa, rsm, fld[FGPU_SIGMA],
                                            fld[FGPU_SCALE_HEIGHT], partial);
-    f_reduce_rows<<<1, 32, 0, stream>>>(partial, rows, red_out);
+    f_reduce_rows<<<1, 32 * 5, 0, stream>>>(partial, rows, red_out);
     CKF(cudaGetLastError());
     CKF(cudaMemcpyAsync(h_pinned, red_out, sizeof(double) * 5, cudaMemcpyDeviceToHost, stream));
     CKF(cudaStreamSynchronize(stream));

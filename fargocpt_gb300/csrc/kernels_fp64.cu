@@ -8,6 +8,7 @@
 // several neighbours reuse go through HBM/L2 instead of being recomputed.
 #include "hydro.cuh"
 #include "kernels.h"
+#include "reduce.cuh"
 
 #include <math.h>
 
@@ -1079,7 +1080,7 @@ __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const 
 // ComputeDiskOnPlanetAccel (src/Force.cpp:23-122) with CorrectDiskSelfgravity
 // (the ring mean of sigma subtracted, Pframeforce.cpp:175-190), and
 // gas_total_mass (quantities.cpp:51-74).  One CTA per active ring writes its
-// partial sums; k_reduce_rows adds them in ring order with compensation.
+// partial sums; k_reduce_rows adds them with compensation in a fixed order.
 // ---------------------------------------------------------------------------
 __global__ void k_disk_force(Geo g, Tables t, Phys ph, double px, double py, double pa,
                              double rsm, const double *__restrict__ S,
@@ -1130,19 +1131,12 @@ __global__ void k_disk_force(Geo g, Tables t, Phys ph, double px, double py, dou
 }
 
 // Kahan-compensated sum of `rows` records of `width` doubles, in order.
+// one warp per component
 __global__ void k_reduce_rows(const double *__restrict__ partial, int rows, int width,
                               double *__restrict__ out)
 {
-    const int w = threadIdx.x;
-    if (w >= width) return;
-    double s = 0.0, comp = 0.0;
-    for (int r = 0; r < rows; ++r) {
-        const double y = partial[(size_t)r * width + w] - comp;
-        const double tt = s + y;
-        comp = (tt - s) - y;
-        s = tt;
-    }
-    out[w] = s;
+    const int w = threadIdx.x >> 5;
+    if (w < width) warp_compensated_rows(partial, rows, width, w, out);
 }
 
 // NaN/Inf scan of one field: records the first bad flat index (atomicMin).
@@ -1290,7 +1284,7 @@ void launch_disk_force(const Launch &L, double px, double py, double pa, double 
 {
     const int rows = L.g.nr - 2;
     k_disk_force<<<rows, 256, 0, L.stream>>>(L.g, L.t, L.ph, px, py, pa, rsm, S, H, partial);
-    k_reduce_rows<<<1, 32, 0, L.stream>>>(partial, rows, 5, out);
+    k_reduce_rows<<<1, 32 * 5, 0, L.stream>>>(partial, rows, 5, out);
 }
 
 void launch_check_finite(const Launch &L, const double *x, size_t n, unsigned long long *bad)

@@ -326,7 +326,8 @@ typedef struct {
 } fgpu_clock;
 
 /* params[k], radii[k]: disk k as for fgpu_create; every disk must select
- * FGPU_PRECISION_FP32_MIXED.  1 <= n <= 1024. */
+ * FGPU_PRECISION_FP32_MIXED; the longest ring must fit the azimuthal
+ * transport's shared memory (naz <= 6144).  1 <= n <= 1024. */
 int fgpu_batch_create(int n, const fgpu_params *params,
 		      const double *const *radii, fgpu_batch **out);
 int fgpu_batch_destroy(fgpu_batch *b);
