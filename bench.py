@@ -44,6 +44,15 @@ KERNEL_BYTES_PER_CELL = {
     "derived_cfl": 88,
 }
 STEP_BYTES_PER_CELL = {"adiabatic": 64, "isothermal": 48}   # one read + write of the state
+# dram__bytes_read.sum + dram__bytes_write.sum per launch from one ncu capture
+# of the dominant kernels on the 512 x 1536 adiabatic disk (summaries and
+# commands in profiles/transport_kernels_c2_fp64.md and
+# profiles/transport_azimuthal_c2_fp32.md)
+NCU_DRAM_BYTES_C2 = {
+    ("fp64", "transport_azimuthal"): 44.128e6 + 0.389e6,
+    ("fp64", "transport_radial"): 25.255e6 + 0.525e6,
+    ("fp32", "transport_azimuthal"): 25.256e6 + 1.903e6,
+}
 KERNELS_IN_TIMED_STEP = 13   # the adiabatic step's kernels between the step's events
 
 
@@ -354,7 +363,7 @@ def measure_fp64_disks(disks, torch, steps=5, warmup=2):
     return updates / (total_ms * 1e-3)
 
 
-def roofline(res, steps, bytes_scale):
+def roofline(res, steps, bytes_scale, form, cfg_name):
     peak, peak_src = peaks()
     phases, nsteps, cells, d = res["phases"], res["nsteps"], res["cells"], res["d"]
     dom = max(phases, key=phases.get)
@@ -364,9 +373,10 @@ def roofline(res, steps, bytes_scale):
     kind = "adiabatic" if d["eos"] == 1 else "isothermal"
     sbpc = STEP_BYTES_PER_CELL[kind] * bytes_scale
     step_achieved = sbpc * cells * steps / (res["total_ms"] * 1e-3) / 1e9
+    traffic = NCU_DRAM_BYTES_C2.get((form, dom)) if cfg_name == "c2" else None
     return ({"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-             "frac": achieved / peak, "peak_source": peak_src, "traffic": None,
-             "bytes_per_cell": bpc, "ms_per_launch": dom_ms},
+             "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
+             "traffic_unit": "B per launch", "bytes_per_cell": bpc, "ms_per_launch": dom_ms},
             {"achieved": step_achieved, "peak": peak, "unit": "GB/s",
              "frac": step_achieved / peak, "bytes_per_cell": sbpc})
 
@@ -447,12 +457,15 @@ def main():
     cells = r64["cells"]
     value = world * cells * args.steps / (vals[0] * 1e-3)
     e2e = world * cells * args.steps / vals[1]
-    rl, rls = roofline(r64, args.steps, 1.0)
+    rl, rls = roofline(r64, args.steps, 1.0, "fp64", args.config)
+    # the FP64 kernels are bound by the FP64 pipe (75-81% busy, DRAM at 1%
+    # of peak in profiles/transport_kernels_c2_fp64.md)
+    rl["fp64_pipe_busy_pct_ncu"] = {"transport_azimuthal": 75.0, "transport_radial": 80.6}
     fp32 = None
     if r32 is not None:
         value32 = world * cells * args.steps / (vals[2] * 1e-3)
         e2e32 = world * cells * args.steps / vals[3]
-        rl32, rls32 = roofline(r32, args.steps, 0.5)
+        rl32, rls32 = roofline(r32, args.steps, 0.5, "fp32", args.config)
         fp32 = {
             "value": value32, "unit": "cell-updates/s", "ms_per_step": vals[2] / args.steps,
             "e2e": {"value": e2e32, "unit": "cell-updates/s", "h2d_bytes_per_step": 80,

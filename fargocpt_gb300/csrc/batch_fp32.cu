@@ -196,8 +196,10 @@ __global__ void b_transport_radial(const DiskF *__restrict__ D, const StepF *__r
 // strided over the block; PER * blockDim.x covers the longest ring of the
 // batch; the transported quantities are staged in dynamic shared memory,
 // azimuthal_smem_floats(naz_max, nq_max, true) floats
+// (two blocks per SM up to 4 cells per thread: 64 registers without spills)
 template <int PER>
-__global__ void __launch_bounds__(512) b_transport_azimuthal(const DiskF *__restrict__ D,
+__global__ void __launch_bounds__(512, PER <= 4 ? 2 : 1)
+    b_transport_azimuthal(const DiskF *__restrict__ D,
                                                              const StepF *__restrict__ S,
                                                              const int *__restrict__ start, int nd)
 {
