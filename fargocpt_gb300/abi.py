@@ -57,7 +57,7 @@ class FgpuParams(C.Structure):
         ("bc_energy_inner", C.c_int), ("bc_energy_outer", C.c_int),
         ("bc_vrad_inner", C.c_int), ("bc_vrad_outer", C.c_int),
         ("bc_vaz_inner", C.c_int), ("bc_vaz_outer", C.c_int),
-        ("precision", C.c_int), ("reserved_i", C.c_int * 7),
+        ("precision", C.c_int), ("integrator", C.c_int), ("reserved_i", C.c_int * 6),
         ("gamma", C.c_double), ("mu", C.c_double), ("aspect_ratio", C.c_double),
         ("flaring_index", C.c_double), ("viscous_alpha", C.c_double),
         ("constant_viscosity", C.c_double), ("art_visc_factor", C.c_double),
@@ -151,7 +151,7 @@ EXPORTED_SYMBOLS = [
     "fgpu_condition_cfl", "fgpu_apply_boundary_condition", "fgpu_step_euler",
     "fgpu_disk_on_planet_accel", "fgpu_total_mass", "fgpu_check_finite",
     "fgpu_synchronize", "fgpu_set_phase_timing", "fgpu_phase_times", "fgpu_phase_name",
-    "fgpu_disk_force_static",
+    "fgpu_disk_force_static", "fgpu_gas_kick", "fgpu_transport", "fgpu_compute_pressure",
     "fgpu_batch_create", "fgpu_batch_destroy", "fgpu_batch_last_error", "fgpu_batch_size",
     "fgpu_batch_disk", "fgpu_batch_get_tiles", "fgpu_batch_set_tiles", "fgpu_batch_autotune",
     "fgpu_batch_step", "fgpu_batch_set_clock", "fgpu_batch_get_clock", "fgpu_batch_run",
@@ -186,6 +186,9 @@ def _declare(lib: C.CDLL) -> C.CDLL:
         "fgpu_phase_name": ([C.c_int], C.c_char_p),
         "fgpu_disk_force_static": ([vp, vp, vp, C.c_int, C.c_int, C.c_double, C.c_double,
                                     P(FgpuBody), vp, vp], C.c_int),
+        "fgpu_gas_kick": ([vp, C.c_double, C.c_double], C.c_int),
+        "fgpu_transport": ([vp, C.c_double], C.c_int),
+        "fgpu_compute_pressure": ([vp], C.c_int),
         "fgpu_batch_create": ([C.c_int, P(FgpuParams), P(dp), P(vp)], C.c_int),
         "fgpu_batch_destroy": ([vp], C.c_int),
         "fgpu_batch_last_error": ([vp], C.c_char_p),

@@ -9,6 +9,16 @@ relative L-infinity (max |a - b| / max |b|) of sigma, v_r, v_phi, the v_phi
 residual about Keplerian, and e, plus the relative error of the disk torque on
 the planet.  The FP64 form itself agrees with FargoCPT's own FP64 build to
 1e-12 (tests/test_gpu_golden.py), so it stands in for the FP64 reference.
+
+    python -m fargocpt_gb300.accuracy --compare perturbed ...
+
+calibrates how much of that error any FP32 storage must incur: the second
+run is the FP64 form again, started from the same disk with v_r and the v_phi
+residual about Keplerian rounded once to FP32 (what the FP32-mixed form's
+upload does to them; its sigma is a compensated pair and stays exact), plus
+optional relative noise of the given size on sigma (--sigma-noise).  The
+difference it grows to is the flow's own amplification of FP32-sized
+perturbations.
 """
 from __future__ import annotations
 
@@ -29,28 +39,41 @@ def rel_linf(a, b):
     return float(np.max(np.abs(a - b)) / max(float(np.max(np.abs(b))), 1e-300))
 
 
-def run(config="c3", orbits=10.0, outputs=10, seed=1234, log=sys.stderr):
+def run(config="c3", orbits=10.0, outputs=10, seed=1234, log=sys.stderr, compare="fp32",
+        sigma_noise=0.0):
     from . import setups
     from .abi import params_from_dict
     from .engine import Engine
 
     p64, d, radii, fields, nbody = setups.build(config, seed=seed)
-    d32 = dict(d)
-    d32["precision"] = 1
-    engines = [Engine(p64, radii), Engine(params_from_dict(d32), radii)]
-    for e in engines:
-        for k, a in fields.items():
+    nr = d["nrad"]
+    rinf, rsup = radii[:nr], radii[1:nr + 1]
+    rmed = 2.0 / 3.0 * (rsup ** 3 - rinf ** 3) / (rsup ** 2 - rinf ** 2)
+    vk = np.sqrt(d["G"] * d["hydro_center_mass"] / rmed)[:, None]
+    second = dict(fields)
+    if compare == "fp32":
+        d32 = dict(d)
+        d32["precision"] = 1
+        p2 = params_from_dict(d32)
+    else:
+        p2 = p64
+        second["V_RADIAL"] = fields["V_RADIAL"].astype(np.float32).astype(np.float64)
+        res = (fields["V_AZIMUTHAL"] - vk).astype(np.float32).astype(np.float64)
+        second["V_AZIMUTHAL"] = vk + res
+        if sigma_noise > 0:
+            rng = np.random.default_rng(seed + 1)
+            second["SIGMA"] = fields["SIGMA"] * (1 + sigma_noise * rng.uniform(-1, 1,
+                                                                              fields["SIGMA"].shape))
+    engines = [Engine(p64, radii), Engine(p2, radii)]
+    for e, start in zip(engines, (fields, second)):
+        for k, a in start.items():
             e.set_field(k, a)
-            e.set_field(k + "0", a)
+            e.set_field(k + "0", fields[k])
         b = nbody.bodies(0.0)
         e.set_bodies(b, *nbody.indirect(b), 0.0)
         e.init_euler(0.0)
         e.apply_boundary_condition(0.0, 0.0, False)
     e64, e32 = engines
-    nr = d["nrad"]
-    rinf, rsup = radii[:nr], radii[1:nr + 1]
-    rmed = 2.0 / 3.0 * (rsup ** 3 - rinf ** 3) / (rsup ** 2 - rinf ** 2)
-    vk = np.sqrt(d["G"] * d["hydro_center_mass"] / rmed)[:, None]
     t_end = orbits * 2.0 * math.pi
     t, steps, t0 = 0.0, 0, time.time()
     history = []
@@ -90,6 +113,7 @@ def run(config="c3", orbits=10.0, outputs=10, seed=1234, log=sys.stderr):
         history.append(rec)
         print(json.dumps(rec), file=log, flush=True)
     return {"config": config, "grid": [d["nrad"], d["naz"]], "orbits": orbits,
+            "compare": compare, "sigma_noise": sigma_noise,
             "steps": steps, "seconds": time.time() - t0, "history": history,
             "final": history[-1]}
 
@@ -100,10 +124,12 @@ def main():
     ap.add_argument("--orbits", type=float, default=10.0)
     ap.add_argument("--outputs", type=int, default=10)
     ap.add_argument("--out", default=None)
+    ap.add_argument("--compare", default="fp32", choices=["fp32", "perturbed"])
+    ap.add_argument("--sigma-noise", type=float, default=0.0)
     a = ap.parse_args()
     from .build import build
     build()
-    res = run(a.config, a.orbits, a.outputs)
+    res = run(a.config, a.orbits, a.outputs, compare=a.compare, sigma_noise=a.sigma_noise)
     text = json.dumps(res, indent=1)
     if a.out:
         with open(a.out, "w") as f:

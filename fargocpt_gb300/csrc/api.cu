@@ -185,6 +185,7 @@ static int validate(const fgpu_params *p, std::string &why)
     if (p->art_visc == FGPU_ARTVISC_TW) { why = "Tscharnuter-Winkler artificial viscosity is not on the GPU path"; return FGPU_ERR_UNSUPPORTED; }
     if (p->art_visc != FGPU_ARTVISC_NONE && p->art_visc != FGPU_ARTVISC_SN) { why = "art_visc"; return FGPU_ERR_BAD_ARG; }
     if (p->precision != FGPU_PRECISION_FP64 && p->precision != FGPU_PRECISION_FP32_MIXED) { why = "precision"; return FGPU_ERR_BAD_ARG; }
+    if (p->integrator != FGPU_INTEGRATOR_EULER && p->integrator != FGPU_INTEGRATOR_LEAPFROG) { why = "integrator"; return FGPU_ERR_BAD_ARG; }
     if (p->radial_spacing != FGPU_SPACING_LOGARITHMIC && p->radial_spacing != FGPU_SPACING_ARITHMETIC) { why = "radial_spacing"; return FGPU_ERR_BAD_ARG; }
     const int bcs[8] = {p->bc_sigma_inner, p->bc_sigma_outer, p->bc_energy_inner, p->bc_energy_outer,
                         p->bc_vrad_inner, p->bc_vrad_outer, p->bc_vaz_inner, p->bc_vaz_outer};
@@ -353,6 +354,7 @@ static int setup_tables(fgpu_engine *eng, const double *radii)
     ph.rvf = p.radial_viscosity_factor;
     ph.hvf = p.heating_viscous_factor;
     ph.cfl = p.cfl;
+    ph.leapfrog = p.integrator == FGPU_INTEGRATOR_LEAPFROG;
     ph.inv_hc_limit = 1.0 / p.heating_cooling_cfl_limit;
     ph.sigma_min = p.sigma_floor * p.sigma0;
     ph.sigma_floor10 = 10.0 * p.sigma0 * p.sigma_floor;
@@ -724,16 +726,15 @@ extern "C" int fgpu_apply_boundary_condition(fgpu_engine *eng, double t, double 
     return check_launch(eng);
 }
 
-extern "C" int fgpu_step_euler(fgpu_engine *eng, double dt, double t)
+// The gas kick of step_Euler (simulation.cpp:170-203), and of each half of
+// step_LeapFrog (:312-331, :352-384): potential, source terms, artificial
+// viscosity, viscosity, stress, viscous update, SubStep3.
+static void gas_kick(fgpu_engine *eng, double dt, double t)
 {
-    if (!eng || !(dt > 0.0)) return FGPU_ERR_BAD_ARG;
-    ROUTE32(eng->e32->step(dt, t));
     Launch L = launch_of(eng);
     const double omf = eng->bodies.omega_frame;
     double **f = eng->field;
     const bool adi = eng->ph.adiabatic;
-
-    mark(eng, -1);
     // CalculateNbodyPotential (simulation.cpp:170-174)
     launch_potential(L, eng->bodies, f[FGPU_SCALE_HEIGHT], f[FGPU_POTENTIAL]);
     mark(eng, 0);
@@ -759,10 +760,15 @@ extern "C" int fgpu_step_euler(fgpu_engine *eng, double dt, double t)
     mark(eng, 4);
     launch_viscous(L, dt, beta_inv_at(eng->p, t), adi ? 7 : 1, s);
     mark(eng, 5);
-    // apply_boundary_condition(final = false) (simulation.cpp:213)
-    ghost(eng, L);
-    mark(eng, 6);
-    // Transport (simulation.cpp:215-217)
+}
+
+// Transport (TransportEuler.cpp; simulation.cpp:215-217)
+static void transport(fgpu_engine *eng, double dt)
+{
+    Launch L = launch_of(eng);
+    const double omf = eng->bodies.omega_frame;
+    double **f = eng->field;
+    State s = state_of(eng);
     launch_transport_radial(L, dt, omf, eng->radial_chunk, s.sigma, s.vr, s.vaz, s.energy,
                             eng->mom, eng->energy_alt, eng->sigma_alt);
     mark(eng, 7);
@@ -774,7 +780,20 @@ extern "C" int fgpu_step_euler(fgpu_engine *eng, double dt, double t)
     std::swap(f[FGPU_V_RADIAL], eng->vr_alt);
     std::swap(f[FGPU_V_AZIMUTHAL], eng->vaz_alt);
     mark(eng, 9);
-    s = state_of(eng);
+}
+
+extern "C" int fgpu_step_euler(fgpu_engine *eng, double dt, double t)
+{
+    if (!eng || !(dt > 0.0)) return FGPU_ERR_BAD_ARG;
+    ROUTE32(eng->e32->step(dt, t));
+    Launch L = launch_of(eng);
+    mark(eng, -1);
+    gas_kick(eng, dt, t);
+    // apply_boundary_condition(final = false) (simulation.cpp:213)
+    ghost(eng, L);
+    mark(eng, 6);
+    transport(eng, dt);
+    State s = state_of(eng);
     // apply_boundary_condition(final = true) (simulation.cpp:244)
     if (eng->p.damping) {
         launch_damping(L, eng->dm, dt, eng->damp_rings, eng->n_damp_rings, s);
@@ -787,6 +806,34 @@ extern "C" int fgpu_step_euler(fgpu_engine *eng, double dt, double t)
     launch_derived_cfl(L, 1 | 4, s, eng->d_dtmin);
     mark(eng, 12);
     eng->cfl_valid = true;
+    return check_launch(eng);
+}
+
+extern "C" int fgpu_gas_kick(fgpu_engine *eng, double dt, double t)
+{
+    if (!eng || !(dt > 0.0)) return FGPU_ERR_BAD_ARG;
+    ROUTE32(eng->e32->kick(dt, t));
+    gas_kick(eng, dt, t);
+    eng->cfl_valid = false;
+    return check_launch(eng);
+}
+
+extern "C" int fgpu_transport(fgpu_engine *eng, double dt)
+{
+    if (!eng || !(dt > 0.0)) return FGPU_ERR_BAD_ARG;
+    ROUTE32(eng->e32->transport(dt));
+    transport(eng, dt);
+    eng->cfl_valid = false;
+    return check_launch(eng);
+}
+
+extern "C" int fgpu_compute_pressure(fgpu_engine *eng)
+{
+    if (!eng) return FGPU_ERR_BAD_ARG;
+    ROUTE32(eng->e32->pressure());
+    Launch L = launch_of(eng);
+    launch_pressure(L, eng->field[FGPU_SIGMA], eng->field[FGPU_ENERGY],
+                    eng->field[FGPU_PRESSURE]);
     return check_launch(eng);
 }
 

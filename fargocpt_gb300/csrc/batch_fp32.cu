@@ -633,7 +633,9 @@ extern "C" int fgpu_batch_create(int n, const fgpu_params *params, const double 
     if (!params || !radii || n < 1 || n > 1024) return FGPU_ERR_BAD_ARG;
     for (int k = 0; k < n; ++k) {
         if (!radii[k]) return FGPU_ERR_BAD_ARG;
-        if (params[k].precision != FGPU_PRECISION_FP32_MIXED) return FGPU_ERR_UNSUPPORTED;
+        if (params[k].precision != FGPU_PRECISION_FP32_MIXED ||
+            params[k].integrator != FGPU_INTEGRATOR_EULER)
+            return FGPU_ERR_UNSUPPORTED;
     }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -767,6 +769,21 @@ extern "C" int fgpu_batch_set_tiles(fgpu_batch *b, const fgpu_tiles *tiles)
     return apply_tiles(b, *tiles);
 }
 
+// The batched kernels were given every disk's step buffers at creation; a
+// half step of a disk alone (fgpu_gas_kick without fgpu_transport) leaves its
+// velocities in the other pair.
+static int check_canonical(fgpu_batch *b)
+{
+    for (int k = 0; k < b->nd; ++k) {
+        if (!b->disks[k]->canonical()) {
+            b->err = "disk " + std::to_string(k) +
+                     " is between the kick and the transport of a step";
+            return FGPU_ERR_BAD_ARG;
+        }
+    }
+    return FGPU_OK;
+}
+
 extern "C" int fgpu_batch_step(fgpu_batch *b, const double *dt, const double *t)
 {
     if (!b || !dt || !t) return FGPU_ERR_BAD_ARG;
@@ -777,6 +794,7 @@ extern "C" int fgpu_batch_step(fgpu_batch *b, const double *dt, const double *t)
         }
     }
     CKB(cudaStreamSynchronize(b->stream));
+    if (int rc = check_canonical(b)) return rc;
     for (int k = 0; k < b->nd; ++k) {
         StepF &s = b->h_steps[k];
         s.dt = dt[k];
@@ -901,6 +919,7 @@ extern "C" int fgpu_batch_run(fgpu_batch *b, int max_steps, int steps_per_graph,
     if (!b || max_steps < 0 || steps_per_graph < 1 || steps_per_graph > 4096)
         return FGPU_ERR_BAD_ARG;
     CKB(cudaStreamSynchronize(b->stream));
+    if (int rc = check_canonical(b)) return rc;
     int done = 0;
     int active = -1;
     while (done < max_steps) {
@@ -1021,6 +1040,7 @@ extern "C" int fgpu_batch_autotune(fgpu_batch *b, int reps, fgpu_tiles *best)
 {
     if (!b || reps < 1 || reps > 1000) return FGPU_ERR_BAD_ARG;
     CKB(cudaStreamSynchronize(b->stream));
+    if (int rc = check_canonical(b)) return rc;
     // a valid step description for every disk: its current CFL dt and bodies
     for (int k = 0; k < b->nd; ++k) {
         double dt = 0.0;

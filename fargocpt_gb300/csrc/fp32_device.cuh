@@ -861,6 +861,22 @@ __device__ __forceinline__ void azimuthal_ring(const GeoF &g, const TablesF &t, 
     __syncthreads();
 }
 
+// compute_pressure (SourceEuler.cpp:1345-1376): P alone
+__device__ __forceinline__ void pressure_cell(const GeoF &g, const TablesF &t, const PhysF &ph,
+                                              const float *__restrict__ S,
+                                              const float *__restrict__ E, float *__restrict__ P,
+                                              int i, int j)
+{
+    const int nz = g.nz;
+    const size_t c = CELL(i, j);
+    if (ph.adiabatic) {
+        P[c] = ph.gm1 * E[c];
+    } else {
+        const float c_s = t.CsIso[i];
+        P[c] = S[c] * (c_s * c_s);
+    }
+}
+
 // velocities from momenta (:498-535), floors; rows 0..nr
 __device__ __forceinline__ void finish_cell(
     const GeoF &g, const TablesF &t, const PhysF &ph, const float *__restrict__ m0,
@@ -1012,9 +1028,15 @@ __device__ __forceinline__ void derived_cfl_ring(
                 const float eps_pp = t.InvRmed[i] * (dvA * g.invdphi + 0.5f * (vr1 + vr[c]));
                 invdt4 = ph.four_C2 * fmaxf(-(eps_rr + eps_pp), 0.f);
             }
-            const float invdt5 = 4.f * n * t.InvCell2[i];
+            float invdt5 = 4.f * n * t.InvCell2[i];
             float invdt6 = 0.f;
             if (ph.adiabatic) invdt6 = ph.inv_hc_limit * fabsf(__fdividef(qplus[c] - qminus[c], E[c]));
+            if (ph.leapfrog) {
+                // LeapFrog applies the source terms twice with dt/2 (cfl.cpp:254-317)
+                invdt4 *= 0.6f;
+                invdt5 *= 0.6f;
+                invdt6 *= 0.6f;
+            }
             const float s2 = invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 +
                              invdt4 * invdt4 + invdt5 * invdt5 + invdt6 * invdt6;
             local = fminf(local, ph.cfl * rsqrtf(s2));

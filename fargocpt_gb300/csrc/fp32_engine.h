@@ -43,6 +43,7 @@ struct TablesF {
 struct PhysF {
     int adiabatic, art_visc_sn, dissipation, limiter_mc, fast_transport;
     int heating_viscous, cooling_beta, beta_ref;
+    int leapfrog;  // LeapFrog integrator: three CFL limits x 0.6
     float gm1, g_gm1, mu, alpha, constant_viscosity, C2, four_C2, rvf, hvf, cfl, inv_hc_limit;
     float sigma_min, sigma_floor10, eps_smooth, c_v_inv, mu_over_R, cool_const, mu_gm1_over_R;
     float emin_fac, emax_fac;
@@ -134,6 +135,12 @@ class Engine32 {
     int cfl(double *dt_out);
     int boundary(double dt, bool final);
     int step(double dt, double t);
+    // the phases step_LeapFrog composes (simulation.cpp:276-459)
+    int kick(double dt, double t);
+    int transport(double dt);
+    int pressure();
+    // the step's buffers are the ones the batched kernels were given
+    bool canonical() const { return fld[FGPU_V_RADIAL] == vr_a && fld[FGPU_V_AZIMUTHAL] == dv_a; }
     int disk_force(double px, double py, double pa, double rsm, double out[5]);
     int check_finite(int *field, int *nr_out, int *naz_out);
     // the device description used by the batched kernels
@@ -174,6 +181,7 @@ class Engine32 {
     DampingF dm{};
     float *fld[FGPU_FIELD_COUNT] = {};
     float *alt_sigma = nullptr, *alt_vr = nullptr, *alt_dv = nullptr, *alt_e = nullptr;
+    float *vr_a = nullptr, *dv_a = nullptr;  // v_r, v_phi buffers at creation
     float *sigma_lo = nullptr, *alt_sigma_lo = nullptr;
     float *mom[4] = {};
     float *tab_f = nullptr;

@@ -43,6 +43,7 @@ struct Geo {
 struct Phys {
     int adiabatic, art_visc_sn, dissipation, limiter_mc, fast_transport;
     int heating_viscous, cooling_beta, beta_ref;
+    int leapfrog;         // LeapFrog integrator: three CFL limits x 0.6
     double gamma, gm1, g_gm1, sqrt_gamma, mu, alpha, constant_viscosity;
     double C2;            // pow(ArtificialViscosityFactor, 2)
     double rvf, hvf, cfl, inv_hc_limit, sigma_min, sigma_floor10;

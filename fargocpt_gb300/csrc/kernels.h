@@ -43,6 +43,7 @@ void launch_finish(const Launch &L, double omf, double *const mom[4], const doub
 void launch_damping(const Launch &L, const Damping &dm, double dt, const int *rings, int nrings,
                     const State &s);
 void launch_derived_cfl(const Launch &L, int mode, const State &s, unsigned long long *dt_min);
+void launch_pressure(const Launch &L, const double *S, const double *E, double *P);
 void launch_disk_force(const Launch &L, double px, double py, double pa, double rsm,
                        const double *S, const double *H, double *partial, double *out);
 void launch_check_finite(const Launch &L, const double *x, size_t n, unsigned long long *bad);

@@ -141,6 +141,14 @@ __global__ void __launch_bounds__(512) f_transport_azimuthal(GeoF g, TablesF t, 
                                blockIdx.x, smf, redf, redl);
 }
 
+__global__ void f_pressure(GeoF g, TablesF t, PhysF ph, const float *__restrict__ S,
+                           const float *__restrict__ E, float *__restrict__ P)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= g.nz) return;
+    pressure_cell(g, t, ph, S, E, P, blockIdx.y, j);
+}
+
 __global__ void f_finish(GeoF g, TablesF t, PhysF ph, const float *__restrict__ m0,
                          const float *__restrict__ m1, const float *__restrict__ m2,
                          const float *__restrict__ m3, const float *__restrict__ S_t,
@@ -403,6 +411,7 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
     ph.rvf = (float)p.radial_viscosity_factor;
     ph.hvf = (float)p.heating_viscous_factor;
     ph.cfl = (float)p.cfl;
+    ph.leapfrog = p.integrator == FGPU_INTEGRATOR_LEAPFROG;
     ph.inv_hc_limit = (float)(1.0 / p.heating_cooling_cfl_limit);
     ph.sigma_min = (float)(p.sigma_floor * p.sigma0);
     ph.sigma_floor10 = (float)(10.0 * p.sigma0 * p.sigma_floor);
@@ -425,6 +434,8 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
         CKF(cudaMalloc(&fld[f], n * sizeof(float)));
         CKF(cudaMemset(fld[f], 0, n * sizeof(float)));
     }
+    vr_a = fld[FGPU_V_RADIAL];
+    dv_a = fld[FGPU_V_AZIMUTHAL];
     CKF(cudaMalloc(&alt_sigma, cells * sizeof(float)));
     CKF(cudaMalloc(&alt_vr, vcells * sizeof(float)));
     CKF(cudaMalloc(&alt_dv, cells * sizeof(float)));
@@ -712,14 +723,16 @@ int Engine32::boundary(double dt, bool final)
     return FGPU_OK;
 }
 
-int Engine32::step(double dt, double t)
+// The gas kick: potential, source terms, artificial viscosity, viscosity,
+// stress, viscous update and SubStep3 (simulation.cpp:170-203).  Leaves the
+// updated velocities in the step's buffers.
+int Engine32::kick(double dt, double t)
 {
     const float fdt = (float)dt;
     const bool adi = phys.adiabatic;
     auto mark = [&](int k) {
         if (mark_fn) mark_fn(mark_ctx, k);
     };
-    mark(-1);
     f_potential<<<grid2(nz, nr), 128, 0, stream>>>(geo, tabs, phys, bodies, fld[FGPU_SCALE_HEIGHT],
                                                    fld[FGPU_POTENTIAL]);
     mark(0);
@@ -754,8 +767,21 @@ int Engine32::step(double dt, double t)
         fld[FGPU_SCALE_HEIGHT], s.sigma0, s.energy0, s.vr, s.dv, s.energy, fld[FGPU_QPLUS],
         fld[FGPU_QMINUS]);
     mark(5);
-    f_ghost<<<(nz + 127) / 128, 128, 0, stream>>>(geo, bc, s);
-    mark(6);
+    CKF(cudaGetLastError());
+    cfl_valid = false;
+    return FGPU_OK;
+}
+
+// Transport (TransportEuler.cpp): radial sweep, FARGO azimuthal transport,
+// velocities from momenta and floors.
+int Engine32::transport(double dt)
+{
+    const float fdt = (float)dt;
+    const bool adi = phys.adiabatic;
+    auto mark = [&](int k) {
+        if (mark_fn) mark_fn(mark_ctx, k);
+    };
+    StateF s = state();
     {
         const int chunk = 16;
         dim3 grid((nz + 63) / 64, (nr + chunk - 1) / chunk);
@@ -796,13 +822,38 @@ int Engine32::step(double dt, double t)
     std::swap(fld[FGPU_V_RADIAL], alt_vr);
     std::swap(fld[FGPU_V_AZIMUTHAL], alt_dv);
     mark(9);
-    s = state();
+    CKF(cudaGetLastError());
+    cfl_valid = false;
+    return FGPU_OK;
+}
+
+int Engine32::pressure()
+{
+    f_pressure<<<grid2(nz, nr), 128, 0, stream>>>(geo, tabs, phys, fld[FGPU_SIGMA],
+                                                  fld[FGPU_ENERGY], fld[FGPU_PRESSURE]);
+    CKF(cudaGetLastError());
+    return FGPU_OK;
+}
+
+int Engine32::step(double dt, double t)
+{
+    auto mark = [&](int k) {
+        if (mark_fn) mark_fn(mark_ctx, k);
+    };
+    mark(-1);
+    int rc = kick(dt, t);
+    if (rc) return rc;
+    f_ghost<<<(nz + 127) / 128, 128, 0, stream>>>(geo, bc, state());
+    mark(6);
+    rc = transport(dt);
+    if (rc) return rc;
+    StateF s = state();
     if (p.damping && n_rings)
-        f_damping<<<n_rings, 256, 0, stream>>>(geo, dm, fdt, damp_rings, s);
+        f_damping<<<n_rings, 256, 0, stream>>>(geo, dm, (float)dt, damp_rings, s);
     mark(10);
     f_ghost<<<(nz + 127) / 128, 128, 0, stream>>>(geo, bc, s);
     mark(11);
-    int rc = derived_cfl(1 | 4);
+    rc = derived_cfl(1 | 4);
     if (rc) return rc;
     mark(12);
     CKF(cudaGetLastError());

@@ -1056,10 +1056,16 @@ __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const 
                 const double mdiv = -(d < 0.0 ? d : 0.0);
                 invdt4 = ph.four_C2 * mdiv;
             }
-            const double invdt5 = 4.0 * n * t.InvCell2[i];
+            double invdt5 = 4.0 * n * t.InvCell2[i];
             double invdt6 = 0.0;
             if (ph.adiabatic) {
                 invdt6 = ph.inv_hc_limit * fabs(fast_div(qplus[c] - qminus[c], E[c]));
+            }
+            if (ph.leapfrog) {
+                // LeapFrog applies the source terms twice with dt/2 (cfl.cpp:254-317)
+                invdt4 *= 0.6;
+                invdt5 *= 0.6;
+                invdt6 *= 0.6;
             }
             const double dt_cell =
                 fast_div(ph.cfl, sqrt(invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 +
@@ -1270,6 +1276,29 @@ void launch_damping(const Launch &L, const Damping &dm, double dt, const int *ri
 {
     if (nrings <= 0) return;
     k_damping<<<nrings, 256, 0, L.stream>>>(L.g, dm, dt, rings, s);
+}
+
+// compute_pressure (SourceEuler.cpp:1345-1376): P alone, from sigma and c_s
+// (isothermal, axisymmetric c_s) or e (ideal EOS)
+__global__ void k_pressure(Geo g, Tables t, Phys ph, const double *__restrict__ S,
+                           const double *__restrict__ E, double *__restrict__ P)
+{
+    const int nz = g.nz;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;
+    if (j >= nz) return;
+    const size_t c = (size_t)i * nz + j;
+    if (ph.adiabatic) {
+        P[c] = ph.gm1 * E[c];
+    } else {
+        const double c_s = t.CsIso[i];
+        P[c] = S[c] * (c_s * c_s);
+    }
+}
+
+void launch_pressure(const Launch &L, const double *S, const double *E, double *P)
+{
+    k_pressure<<<dim3((L.g.nz + 127) / 128, L.g.nr), 128, 0, L.stream>>>(L.g, L.t, L.ph, S, E, P);
 }
 
 void launch_derived_cfl(const Launch &L, int mode, const State &s, unsigned long long *dt_min)

@@ -134,6 +134,16 @@ class Engine:
     def step_euler(self, dt, t):
         self._check(self.lib.fgpu_step_euler(self.h, dt, t), "fgpu_step_euler")
 
+    # the phases step_LeapFrog composes (simulation.cpp:276-459)
+    def gas_kick(self, dt, t):
+        self._check(self.lib.fgpu_gas_kick(self.h, dt, t), "fgpu_gas_kick")
+
+    def transport(self, dt):
+        self._check(self.lib.fgpu_transport(self.h, dt), "fgpu_transport")
+
+    def compute_pressure(self):
+        self._check(self.lib.fgpu_compute_pressure(self.h), "fgpu_compute_pressure")
+
     def disk_on_planet_accel(self, k):
         out = (C.c_double * 2)()
         self._check(self.lib.fgpu_disk_on_planet_accel(self.h, k, out),

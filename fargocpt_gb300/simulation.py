@@ -7,10 +7,13 @@ can be driven exactly like ``sim::run`` drives ``step_Euler``:
 * ``CalculateTimeStep`` (simulation.cpp:100-118): dt = min(CFLmaxVar * last_dt,
   CFL dt);
 * the clamp of the step to the next monitor time (simulation.cpp:526-540);
-* the monitor bookkeeping (simulation.cpp:544-550).
+* the monitor bookkeeping (simulation.cpp:544-550);
+* the gas part of step_LeapFrog (simulation.cpp:276-459) from the phase
+  functions (``gas_kick``, ``transport``, ``compute_pressure``).
 
 Any object with the hydro-step methods (``condition_cfl``, ``step_euler``,
-``apply_boundary_condition``, ``set_bodies``) can be driven; the product uses
+``apply_boundary_condition``, ``set_bodies``, and for LeapFrog the phase
+functions and ``recalculate_derived``) can be driven; the product uses
 :class:`fargocpt_gb300.engine.Engine`.
 """
 from __future__ import annotations
@@ -47,13 +50,38 @@ def start(hydro, clock: RunClock, cfl_max_var: float) -> None:
     calculate_time_step(hydro, clock, cfl_max_var)
 
 
+def step_leapfrog(hydro, dt: float, t: float, first, second) -> None:
+    """The gas part of step_LeapFrog (simulation.cpp:276-459): kick dt/2, the
+    boundary condition, transport over dt, the pressure of the transported
+    state, kick dt/2, then the final boundary condition (damping) and the
+    derived quantities.  first and second are (bodies, indirect_x,
+    indirect_y) for the two kicks: the host has drifted the bodies to the half
+    step before the first kick and recomputed the indirect term before the
+    second (:285-302, :338-342)."""
+    half = dt / 2
+    mid = t + half
+    hydro.set_bodies(first[0], first[1], first[2], 0.0)
+    hydro.gas_kick(half, t)
+    hydro.apply_boundary_condition(t, 0.0, False)
+    hydro.transport(dt)
+    hydro.set_bodies(second[0], second[1], second[2], 0.0)
+    hydro.compute_pressure()
+    hydro.gas_kick(half, mid)
+    hydro.apply_boundary_condition(t + dt, dt, True)
+    hydro.recalculate_derived(t + dt)
+
+
 def advance(hydro, clock: RunClock, *, cfl_max_var: float,
             monitor_timestep: float, t_final: float, max_steps: int = -1,
-            bodies=None, on_monitor=None) -> None:
-    """The loop of sim::run (simulation.cpp:505-558) with step_Euler.
+            bodies=None, on_monitor=None, integrator: str = "euler",
+            bodies_second=None) -> None:
+    """The loop of sim::run (simulation.cpp:505-558) with step_Euler or, for
+    integrator "leapfrog", step_LeapFrog's gas part.
 
     bodies(clock) -> (list_of_body_tuples, indirect_x, indirect_y) is called
-    before every step (the N-body state of the host at the start of the step);
+    before every step (the N-body state of the host at the start of the step;
+    for LeapFrog the state the first kick sees); bodies_second(clock, dt), for
+    LeapFrog, gives the second kick's (defaults to the first's);
     on_monitor(clock) after every step that lands on a monitor time.
     """
     while clock.time < t_final:
@@ -65,10 +93,15 @@ def advance(hydro, clock: RunClock, *, cfl_max_var: float,
         overshoot = cfl_dt > time_left
         almost_there = time_left < cfl_dt * (1 + 0.05)
         step_dt = time_left if (overshoot or almost_there) else cfl_dt
-        if bodies is not None:
-            b, ix, iy = bodies(clock)
-            hydro.set_bodies(b, ix, iy, 0.0)
-        hydro.step_euler(step_dt, clock.time)
+        if integrator == "leapfrog":
+            first = bodies(clock) if bodies is not None else ([], 0.0, 0.0)
+            second = bodies_second(clock, step_dt) if bodies_second is not None else first
+            step_leapfrog(hydro, step_dt, clock.time, first, second)
+        else:
+            if bodies is not None:
+                b, ix, iy = bodies(clock)
+                hydro.set_bodies(b, ix, iy, 0.0)
+            hydro.step_euler(step_dt, clock.time)
         clock.dts.append(step_dt)
         clock.time += step_dt
         clock.n_hydro_iter += 1

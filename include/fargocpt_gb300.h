@@ -94,6 +94,7 @@ enum { FGPU_LIMITER_VANLEER = 0, FGPU_LIMITER_MC = 1 };
 enum { FGPU_BETA_REF_ZERO = 0, FGPU_BETA_REF_REFERENCE = 1,
        FGPU_BETA_REF_DISKMODEL = 2, FGPU_BETA_REF_FLOOR = 3 };
 enum { FGPU_PRECISION_FP64 = 0, FGPU_PRECISION_FP32_MIXED = 1 };
+enum { FGPU_INTEGRATOR_EULER = 0, FGPU_INTEGRATOR_LEAPFROG = 1 };
 
 /*
  * Flat parameter block: the subset of FargoCPT's parameters:: namespace and
@@ -119,7 +120,9 @@ typedef struct fgpu_params {
     int bc_vrad_inner, bc_vrad_outer;
     int bc_vaz_inner, bc_vaz_outer;
     int precision;          /* FGPU_PRECISION_* */
-    int reserved_i[7];
+    int integrator;         /* FGPU_INTEGRATOR_* (Interpret.cpp:174-185); LeapFrog
+                               scales three CFL limits by 0.6 (cfl.cpp:254-317) */
+    int reserved_i[6];
 
     double gamma;           /* AdiabaticIndex */
     double mu;              /* mean molecular weight */
@@ -250,6 +253,22 @@ int fgpu_phase_times(fgpu_engine *eng, double *ms, int capacity, int *count,
 		     int *steps);
 const char *fgpu_phase_name(int k);
 
+/* The phases of the step, for hosts that compose their own integrator
+ * (step_LeapFrog, src/simulation.cpp:276-459, kicks with dt/2 around one
+ * transport over dt):
+ *   fgpu_gas_kick       potential, update_with_sourceterms, artificial
+ *                       viscosity, recalculate_viscosity, stress tensor,
+ *                       update_velocities_with_viscosity, SubStep3 (the gas
+ *                       kick, :312-331 and :352-384), with the bodies of the
+ *                       last fgpu_set_bodies; t is the time the kick sees;
+ *   fgpu_transport      Transport (TransportEuler.cpp) over dt;
+ *   fgpu_compute_pressure  compute_pressure (SourceEuler.cpp:1345-1376).
+ * fgpu_step_euler is gas_kick(dt, t), the non-final boundary condition,
+ * transport(dt), the final boundary condition and the derived quantities. */
+int fgpu_gas_kick(fgpu_engine *eng, double dt, double t);
+int fgpu_transport(fgpu_engine *eng, double dt);
+int fgpu_compute_pressure(fgpu_engine *eng);
+
 /* Disk-on-body force and gas mass without any device allocation.  No
  * counterpart in the reference: it serves callers that keep sigma and the
  * scale height in their own device buffers and may not allocate device
@@ -326,7 +345,8 @@ typedef struct {
 } fgpu_clock;
 
 /* params[k], radii[k]: disk k as for fgpu_create; every disk must select
- * FGPU_PRECISION_FP32_MIXED; the longest ring must fit the azimuthal
+ * FGPU_PRECISION_FP32_MIXED and the Euler integrator (the batched step is
+ * step_Euler); the longest ring must fit the azimuthal
  * transport's shared memory (naz <= 6144).  1 <= n <= 1024. */
 int fgpu_batch_create(int n, const fgpu_params *params,
 		      const double *const *radii, fgpu_batch **out);

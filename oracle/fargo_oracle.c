@@ -349,7 +349,7 @@ static void compute_scale_height(or_state *s)
 }
 
 /* compute_pressure, src/SourceEuler.cpp:1345-1376 */
-static void compute_pressure(or_state *s)
+void or_compute_pressure(or_state *s)
 {
     const size_t n = (size_t)s->nr * s->nz;
     double *P = F(s, FGPU_PRESSURE), *E = F(s, FGPU_ENERGY),
@@ -504,9 +504,9 @@ int or_recalculate_derived(or_state *s, double t)
 	compute_temperature(s);
 	compute_sound_speed(s);
 	compute_scale_height(s);
-	compute_pressure(s);
+	or_compute_pressure(s);
     } else {
-	compute_pressure(s);
+	or_compute_pressure(s);
     }
     update_viscosity(s);
     return FGPU_OK;
@@ -1204,7 +1204,10 @@ void or_transport(or_state *s, double dt)
 /* step, init, CFL, forces                                             */
 /* ------------------------------------------------------------------ */
 
-int or_step_euler(or_state *s, double dt, double t)
+/* The gas kick of step_Euler (src/simulation.cpp:170-203) and of each half
+   of step_LeapFrog (:312-331, :352-384): potential, source terms, artificial
+   viscosity, viscosity, viscous stress and velocity update, SubStep3. */
+void or_gas_kick(or_state *s, double dt, double t)
 {
     or_calculate_potential(s);
     or_update_with_sourceterms(s, dt);
@@ -1213,6 +1216,11 @@ int or_step_euler(or_state *s, double dt, double t)
     or_viscous_stress_tensor(s);
     or_update_velocities_with_viscosity(s, dt);
     if (adiabatic(s)) or_substep3(s, t, dt);
+}
+
+int or_step_euler(or_state *s, double dt, double t)
+{
+    or_gas_kick(s, dt, t);
     or_apply_boundary_condition(s, t, 0.0, 0);
     or_transport(s, dt);
     or_apply_boundary_condition(s, t + dt, dt, 1);
@@ -1227,10 +1235,10 @@ int or_init_euler(or_state *s, double t)
 	compute_temperature(s);
 	compute_sound_speed(s);
 	compute_scale_height(s);
-	compute_pressure(s);
+	or_compute_pressure(s);
     } else {
 	compute_sound_speed(s);
-	compute_pressure(s);
+	or_compute_pressure(s);
 	compute_temperature(s);
 	compute_scale_height(s);
     }
@@ -1256,7 +1264,9 @@ int or_init_euler(or_state *s, double t)
     return FGPU_OK;
 }
 
-/* cfl::condition_cfl, src/cfl.cpp:185-382 (Euler integrator) */
+/* cfl::condition_cfl, src/cfl.cpp:185-382; the LeapFrog integrator allows
+   the source-term limits (artificial viscosity, viscosity, heating/cooling)
+   a 0.6 factor (:254-317) */
 double or_condition_cfl(or_state *s)
 {
     const int nr = s->nr, nz = s->nz;
@@ -1264,6 +1274,7 @@ double or_condition_cfl(or_state *s)
 	   *cs = F(s, FGPU_SOUNDSPEED), *nu = F(s, FGPU_VISCOSITY),
 	   *Qp = F(s, FGPU_QPLUS), *Qm = F(s, FGPU_QMINUS), *E = F(s, FGPU_ENERGY);
     const fgpu_params *p = &s->p;
+    const double lf = p->integrator == FGPU_INTEGRATOR_LEAPFROG ? 0.6 : 1.0;
     double *vm = s->vmean;
 #pragma omp parallel for
     for (int i = 0; i < nr; ++i) {
@@ -1296,7 +1307,7 @@ double or_condition_cfl(or_state *s)
 		dvR = dvR > 0.0 ? 0.0 : -dvR;
 		dvA = dvA > 0.0 ? 0.0 : -dvA;
 		const double a = dvR / dxR, b = dvA / dxA;
-		invdt4 = 4.0 * pow(p->art_visc_factor, 2) * (a > b ? a : b) * 1.0;
+		invdt4 = 4.0 * pow(p->art_visc_factor, 2) * (a > b ? a : b) * lf;
 	    } else {
 		const double eps_rr = (AT(vr, i + 1, j) - AT(vr, i, j)) * s->InvDiffRsup[i];
 		const double eps_pp =
@@ -1304,13 +1315,13 @@ double or_condition_cfl(or_state *s)
 				     0.5 * (AT(vr, i + 1, j) + AT(vr, i, j)));
 		const double d = eps_rr + eps_pp;
 		const double mdiv = -(d < 0.0 ? d : 0.0);
-		invdt4 = 4.0 * pow(p->art_visc_factor, 2) * mdiv * 1.0;
+		invdt4 = 4.0 * pow(p->art_visc_factor, 2) * mdiv * lf;
 	    }
-	    const double invdt5 = 4.0 * AT(nu, i, j) / pow(cell, 2) * 1.0;
+	    const double invdt5 = 4.0 * AT(nu, i, j) / pow(cell, 2) * lf;
 	    double invdt6 = 0.0;
 	    if (adiabatic(s)) {
 		const double inv_limit = 1.0 / p->heating_cooling_cfl_limit;
-		invdt6 = inv_limit * fabs((AT(Qp, i, j) - AT(Qm, i, j)) / AT(E, i, j)) * 1.0;
+		invdt6 = inv_limit * fabs((AT(Qp, i, j) - AT(Qm, i, j)) / AT(E, i, j)) * lf;
 	    }
 	    const double dt_cell =
 		p->cfl / sqrt(pow(invdt1, 2) + pow(invdt2, 2) + pow(invdt3, 2) +

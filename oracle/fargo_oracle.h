@@ -38,6 +38,8 @@ int or_recalculate_derived(or_state *s, double t);
 double or_condition_cfl(or_state *s);
 int or_apply_boundary_condition(or_state *s, double t, double dt, int final);
 int or_step_euler(or_state *s, double dt, double t);
+void or_gas_kick(or_state *s, double dt, double t);
+void or_compute_pressure(or_state *s);
 int or_disk_on_planet_accel(or_state *s, int k, double accel[2]);
 double or_total_mass(or_state *s);
 

@@ -59,6 +59,9 @@ def _load():
         getattr(lib, name).argtypes = [vp, C.c_double]
     lib.or_recalculate_viscosity.argtypes = [vp, C.c_double]
     lib.or_substep3.argtypes = [vp, C.c_double, C.c_double]
+    lib.or_gas_kick.argtypes = [vp, C.c_double, C.c_double]
+    lib.or_transport.argtypes = [vp, C.c_double]
+    lib.or_compute_pressure.argtypes = [vp]
     _lib = lib
     return lib
 
@@ -125,6 +128,16 @@ class OracleState:
 
     def step_euler(self, dt, t):
         self.lib.or_step_euler(self.h, dt, t)
+
+    # the phases step_LeapFrog composes (simulation.cpp:276-459)
+    def gas_kick(self, dt, t):
+        self.lib.or_gas_kick(self.h, dt, t)
+
+    def transport(self, dt):
+        self.lib.or_transport(self.h, dt)
+
+    def compute_pressure(self):
+        self.lib.or_compute_pressure(self.h)
 
     def disk_on_planet_accel(self, k):
         out = (C.c_double * 2)()

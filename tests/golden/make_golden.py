@@ -108,6 +108,35 @@ CASES = {
                   DampingEnergyInner="Mean", DampingEnergyOuter="Reference",
                   MonitorTimestep=0.05, Nsnapshots=3),
         nrad=16, naz=40, rmin=0.3, rmax=3.0, planet=None, keep=[1, 2, 3]),
+    # LeapFrog (gas kick-drift-kick, simulation.cpp:276-459), locally
+    # isothermal, CFL-limited, star only
+    "iso_star_cfl_leapfrog": dict(
+        keys=dict(SigmaSlope=0.5, AspectRatio=0.05, FlaringIndex=0.0,
+                  EquationOfState="Isothermal", ViscousAlpha=1e-3,
+                  ArtificialViscosity="SN", Transport="FARGO",
+                  InnerBoundary="zerogradient", OuterBoundary="zerogradient",
+                  Damping="yes", DampingInnerLimit=1.1, DampingOuterLimit=0.9,
+                  DampingSurfaceDensityInner="Reference",
+                  DampingSurfaceDensityOuter="Reference",
+                  DampingVRadialInner="Reference", DampingVRadialOuter="Reference",
+                  DampingVAzimuthalInner="Reference", DampingVAzimuthalOuter="Reference",
+                  MonitorTimestep=0.5, Nsnapshots=4, Integrator="LeapFrog"),
+        nrad=16, naz=40, rmin=0.4, rmax=2.5, planet=None, keep=[1, 2, 3, 4]),
+    # LeapFrog, adiabatic with beta cooling and SN, FARGO, star only
+    "adi_star_cfl_leapfrog": dict(
+        keys=dict(SigmaSlope=1.0, AspectRatio=0.05, FlaringIndex=0.25,
+                  EquationOfState="Ideal", AdiabaticIndex=1.4, ViscousAlpha=1e-3,
+                  ArtificialViscosity="SN", ArtificialViscosityFactor=1.41421356,
+                  CoolingBetaLocal="yes", CoolingBeta=10, Transport="FARGO",
+                  InnerBoundary="zerogradient", OuterBoundary="outflow",
+                  Damping="yes", DampingInnerLimit=1.1, DampingOuterLimit=0.9,
+                  DampingSurfaceDensityInner="Reference",
+                  DampingSurfaceDensityOuter="Reference",
+                  DampingVRadialInner="Reference", DampingVRadialOuter="Reference",
+                  DampingVAzimuthalInner="Reference", DampingVAzimuthalOuter="Reference",
+                  DampingEnergyInner="Reference", DampingEnergyOuter="Reference",
+                  MonitorTimestep=0.4, Nsnapshots=4, Integrator="LeapFrog"),
+        nrad=16, naz=40, rmin=0.3, rmax=3.0, planet=None, keep=[1, 2, 3, 4]),
 }
 
 
@@ -172,6 +201,7 @@ def engine_params(case, consts, temp_unit):
         bc_vrad_inner=BC[vi], bc_vrad_outer=BC[vo],
         bc_vaz_inner=BC["keplerian"], bc_vaz_outer=BC["keplerian"],
         precision=0,
+        integrator=1 if str(k.get("Integrator", "Euler")).lower().startswith("l") else 0,
         gamma=float(k.get("AdiabaticIndex", 1.4)), mu=float(k["mu"]),
         aspect_ratio=float(k["AspectRatio"]), flaring_index=float(k["FlaringIndex"]),
         viscous_alpha=float(k["ViscousAlpha"]), constant_viscosity=0.0,
@@ -290,8 +320,12 @@ def make_case(name, case, seed):
 
 
 def main():
+    """python make_golden.py [case ...]: all cases, or the named ones."""
     build_reference()
+    only = set(sys.argv[1:])
     for i, (name, case) in enumerate(CASES.items()):
+        if only and name not in only:
+            continue
         make_case(name, case, seed=1000 + i)
 
 

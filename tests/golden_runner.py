@@ -17,7 +17,7 @@ from fargocpt_gb300.simulation import RunClock, advance, indirect_term_euler, st
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = ["iso_planet_fixed_dt", "adi_planet_fixed_dt", "iso_star_cfl",
-         "adi_star_cfl_mc_std"]
+         "adi_star_cfl_mc_std", "iso_star_cfl_leapfrog", "adi_star_cfl_leapfrog"]
 EVOLVED = ["SIGMA", "V_RADIAL", "V_AZIMUTHAL", "ENERGY"]
 
 
@@ -92,7 +92,8 @@ def replay(make_backend, name, params_override=None):
     t_final = meta["nsnapshots"] * 1 * meta["monitor_timestep"]
     advance(hyd, clock, cfl_max_var=cmv, monitor_timestep=meta["monitor_timestep"],
             t_final=t_final, bodies=lambda c: body_state(c.n_monitor),
-            on_monitor=on_monitor)
+            on_monitor=on_monitor,
+            integrator="leapfrog" if int(pd.get("integrator", 0)) == 1 else "euler")
     return snaps, times, torques, clock.dts, arrays
 
 

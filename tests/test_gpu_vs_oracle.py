@@ -70,3 +70,43 @@ def test_mc_limiter_standard_transport():
     (o, _), (g, _) = run_both(params, d, steps=8)
     for f in EVOLVED:
         assert rel_linf(g.get_field(f), o.get_field(f)) <= TOL, f
+
+
+@pytest.mark.parametrize("adiabatic", [False, True])
+def test_leapfrog_with_moving_planet(adiabatic):
+    """step_LeapFrog's gas part (simulation.cpp:276-459) composed from the
+    phase functions: the planet drifted to the half step for the first kick,
+    the indirect term renewed for the second, the LeapFrog CFL factor."""
+    from fargocpt_gb300.engine import Engine, grid_radii
+    from fargocpt_gb300.simulation import indirect_term_euler, step_leapfrog
+    from oracle.oracle_py import OracleState
+
+    params, d = make_params(32, 96, adiabatic=adiabatic, integrator=1)
+    radii = grid_radii(d["radial_spacing"], d["rmin"], d["rmax"], d["nrad"])
+    st = initial_state(d, radii, seed=5)
+
+    def bodies(t):
+        x, y = math.cos(0.2 + t), math.sin(0.2 + t)
+        return [(0.0, 0.0, 1.0, 0.0, 0.0), (x, y, 1e-3, 0.0, 1.0)]
+
+    hyd = []
+    for cls in (OracleState, Engine):
+        h = cls(params, radii)
+        load(h, st, bodies(0.0))
+        h.apply_boundary_condition(0.0, 0.0, False)
+        hyd.append(h)
+    t = 0.0
+    for _ in range(10):
+        dts = [h.condition_cfl() for h in hyd]
+        np.testing.assert_allclose(dts[1], dts[0], rtol=1e-12)
+        dt = dts[0]
+        b = bodies(t + dt / 2)
+        ix, iy = indirect_term_euler(b)
+        first = (b, ix, iy)
+        second = (b, 0.9 * ix, 1.1 * iy)
+        for h in hyd:
+            step_leapfrog(h, dt, t, first, second)
+        t += dt
+    for f in EVOLVED:
+        err = rel_linf(hyd[1].get_field(f), hyd[0].get_field(f))
+        assert err <= TOL, f"{f}: {err:.3e}"

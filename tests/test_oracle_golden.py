@@ -38,3 +38,8 @@ def test_step_counts_follow_cfl():
     assert len(dts) == 22
     _, _, _, dts, _ = replay(OracleState, "adi_star_cfl_mc_std")
     assert len(dts) == 12
+    # LeapFrog: the reference's own run logs report 22 and 32 hydro steps
+    _, _, _, dts, _ = replay(OracleState, "iso_star_cfl_leapfrog")
+    assert len(dts) == 22
+    _, _, _, dts, _ = replay(OracleState, "adi_star_cfl_leapfrog")
+    assert len(dts) == 32
