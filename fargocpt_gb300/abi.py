@@ -152,6 +152,7 @@ EXPORTED_SYMBOLS = [
     "fgpu_disk_on_planet_accel", "fgpu_total_mass", "fgpu_check_finite",
     "fgpu_synchronize", "fgpu_set_phase_timing", "fgpu_phase_times", "fgpu_phase_name",
     "fgpu_disk_force_static", "fgpu_gas_kick", "fgpu_transport", "fgpu_compute_pressure",
+    "fgpu_snapshot_begin", "fgpu_snapshot_wait", "fgpu_host_alloc", "fgpu_host_free",
     "fgpu_batch_create", "fgpu_batch_destroy", "fgpu_batch_last_error", "fgpu_batch_size",
     "fgpu_batch_disk", "fgpu_batch_get_tiles", "fgpu_batch_set_tiles", "fgpu_batch_autotune",
     "fgpu_batch_step", "fgpu_batch_set_clock", "fgpu_batch_get_clock", "fgpu_batch_run",
@@ -186,6 +187,10 @@ def _declare(lib: C.CDLL) -> C.CDLL:
         "fgpu_phase_name": ([C.c_int], C.c_char_p),
         "fgpu_disk_force_static": ([vp, vp, vp, C.c_int, C.c_int, C.c_double, C.c_double,
                                     P(FgpuBody), vp, vp], C.c_int),
+        "fgpu_snapshot_begin": ([vp, C.c_int, P(C.c_int), P(dp)], C.c_int),
+        "fgpu_snapshot_wait": ([vp], C.c_int),
+        "fgpu_host_alloc": ([C.c_size_t, P(vp)], C.c_int),
+        "fgpu_host_free": ([vp], C.c_int),
         "fgpu_gas_kick": ([vp, C.c_double, C.c_double], C.c_int),
         "fgpu_transport": ([vp, C.c_double], C.c_int),
         "fgpu_compute_pressure": ([vp], C.c_int),

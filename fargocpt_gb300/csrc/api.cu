@@ -59,6 +59,13 @@ struct fgpu_engine {
     std::vector<cudaEvent_t> ev_free;
     int ev_cursor = 0;
 
+    // asynchronous snapshots: device staging, a copy stream and its events
+    double *snap_stage = nullptr;
+    size_t snap_capacity = 0;  // doubles
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t snap_staged = nullptr, snap_copied = nullptr;
+    bool snap_pending = false;
+
     fgpu32::Engine32 *e32 = nullptr;  // FP32-mixed form, when selected
     bool owns_stream = true;          // false for the disks of a batch
     bool batch_owned = false;         // disks of a batch are freed by the batch
@@ -516,6 +523,13 @@ extern "C" int fgpu_destroy(fgpu_engine *eng)
     cudaFree(eng->damp_rings); cudaFree(eng->partial); cudaFree(eng->red_out);
     cudaFree(eng->d_dtmin); cudaFree(eng->d_bad);
     if (eng->h_pinned) cudaFreeHost(eng->h_pinned);
+    if (eng->copy_stream) {
+        cudaStreamSynchronize(eng->copy_stream);
+        cudaStreamDestroy(eng->copy_stream);
+    }
+    if (eng->snap_staged) cudaEventDestroy(eng->snap_staged);
+    if (eng->snap_copied) cudaEventDestroy(eng->snap_copied);
+    cudaFree(eng->snap_stage);
     if (eng->stream && eng->owns_stream) cudaStreamDestroy(eng->stream);
     delete eng;
     return FGPU_OK;
@@ -615,6 +629,88 @@ extern "C" int fgpu_download_field(fgpu_engine *eng, int field, double *host, in
     CK(cudaMemcpyAsync(host, eng->field[field], sizeof(double) * (size_t)rows * cols,
                        cudaMemcpyDeviceToHost, eng->stream));
     CK(cudaStreamSynchronize(eng->stream));
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_host_alloc(size_t bytes, void **ptr)
+{
+    if (!ptr || bytes == 0) return FGPU_ERR_BAD_ARG;
+    *ptr = nullptr;
+    if (cudaMallocHost(ptr, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        *ptr = nullptr;
+        return FGPU_ERR_OOM;
+    }
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_host_free(void *ptr)
+{
+    if (!ptr) return FGPU_ERR_BAD_ARG;
+    return cudaFreeHost(ptr) == cudaSuccess ? FGPU_OK : FGPU_ERR_CUDA;
+}
+
+extern "C" int fgpu_snapshot_wait(fgpu_engine *eng)
+{
+    if (!eng) return FGPU_ERR_BAD_ARG;
+    if (!eng->snap_pending) return FGPU_OK;
+    eng->snap_pending = false;
+    CK(cudaEventSynchronize(eng->snap_copied));
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_snapshot_begin(fgpu_engine *eng, int n, const int *fields,
+                                   double *const *host)
+{
+    if (!eng || n < 1 || n > FGPU_FIELD_COUNT || !fields || !host) return FGPU_ERR_BAD_ARG;
+    for (int k = 0; k < n; ++k) {
+        if (fields[k] < 0 || fields[k] >= FGPU_FIELD_COUNT || !host[k]) return FGPU_ERR_BAD_ARG;
+    }
+    int rc = fgpu_snapshot_wait(eng);  // one snapshot in flight at a time
+    if (rc) return rc;
+    if (!eng->copy_stream) {
+        CK(cudaStreamCreateWithFlags(&eng->copy_stream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&eng->snap_staged, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&eng->snap_copied, cudaEventDisableTiming));
+    }
+    const size_t need = (size_t)n * eng->vcells;
+    if (need > eng->snap_capacity) {
+        cudaFree(eng->snap_stage);
+        eng->snap_stage = nullptr;
+        eng->snap_capacity = 0;
+        if (cudaMalloc(&eng->snap_stage, need * sizeof(double)) != cudaSuccess) {
+            cudaGetLastError();
+            eng->err = "snapshot: out of device memory for the staging buffers";
+            return FGPU_ERR_OOM;
+        }
+        eng->snap_capacity = need;
+    }
+    // the staging copies are ordered with the steps on the engine's stream
+    for (int k = 0; k < n; ++k) {
+        const int rows = field_rows(eng, fields[k]);
+        double *dst = eng->snap_stage + (size_t)k * eng->vcells;
+        if (eng->e32) {
+            rc = eng->e32->to_fp64(fields[k], dst, rows);
+            if (rc) {
+                eng->err = eng->e32->err;
+                return rc;
+            }
+        } else {
+            CK(cudaMemcpyAsync(dst, eng->field[fields[k]], sizeof(double) * rows * eng->nz,
+                               cudaMemcpyDeviceToDevice, eng->stream));
+        }
+    }
+    CK(cudaEventRecord(eng->snap_staged, eng->stream));
+    // the copies to the host drain on the copy stream while the steps go on
+    CK(cudaStreamWaitEvent(eng->copy_stream, eng->snap_staged, 0));
+    for (int k = 0; k < n; ++k) {
+        const int rows = field_rows(eng, fields[k]);
+        CK(cudaMemcpyAsync(host[k], eng->snap_stage + (size_t)k * eng->vcells,
+                           sizeof(double) * rows * eng->nz, cudaMemcpyDeviceToHost,
+                           eng->copy_stream));
+    }
+    CK(cudaEventRecord(eng->snap_copied, eng->copy_stream));
+    eng->snap_pending = true;
     return FGPU_OK;
 }
 

@@ -196,12 +196,13 @@ __global__ void b_transport_radial(const DiskF *__restrict__ D, const StepF *__r
 // strided over the block; PER * blockDim.x covers the longest ring of the
 // batch; the transported quantities are staged in dynamic shared memory,
 // azimuthal_smem_floats(naz_max, nq_max, true) floats
-// (two blocks per SM up to 4 cells per thread: 64 registers without spills)
-template <int PER>
-__global__ void __launch_bounds__(512, PER <= 4 ? 2 : 1)
-    b_transport_azimuthal(const DiskF *__restrict__ D,
-                                                             const StepF *__restrict__ S,
-                                                             const int *__restrict__ start, int nd)
+// (two blocks of up to 384 threads per SM up to 4 cells per thread, 85
+// registers).  One instantiation per number of transported quantities (4
+// isothermal, 5 with the energy); disks of the other kind are skipped.
+template <int PER, int NQ>
+__global__ void __launch_bounds__(PER <= 4 ? 384 : 512, PER <= 4 ? 2 : 1)
+    b_transport_azimuthal(const DiskF *__restrict__ D, const StepF *__restrict__ S,
+                          const int *__restrict__ start, int nd)
 {
     extern __shared__ __align__(16) float smf[];
     __shared__ float redf[33];
@@ -211,10 +212,11 @@ __global__ void __launch_bounds__(512, PER <= 4 ? 2 : 1)
         const int d = disk_of(start, nd, item);
         if (!S[d].run) continue;
         const DiskF &k = D[d];
+        if (k.nq != NQ) continue;
         const int i = item - __ldg(start + d);
-        azimuthal_ring<PER, true>(k.g, k.t, S[d].dt, k.ph.limiter_mc, k.ph.fast_transport, k.nq, k.dv_b,
-                            k.mom[0], k.mom[1], k.mom[2], k.mom[3], k.energy_t, k.sigma_t,
-                            k.sigma_lo_t, i, smf, redf, redl);
+        azimuthal_ring<PER, NQ, true>(k.g, k.t, S[d].dt, k.ph.limiter_mc, k.ph.fast_transport,
+                                      k.dv_b, k.mom[0], k.mom[1], k.mom[2], k.mom[3], k.energy_t,
+                                      k.sigma_t, k.sigma_lo_t, i, smf, redf, redl);
     }
 }
 
@@ -365,20 +367,22 @@ static int per_for(int nz_max, int threads)
 }
 
 typedef void (*AzFn)(const DiskF *, const StepF *, const int *, int);
-static AzFn az_fn(int per)
+template <int NQ>
+static AzFn az_fn_nq(int per)
 {
     switch (per) {
-    case 1: return b_transport_azimuthal<1>;
-    case 2: return b_transport_azimuthal<2>;
-    case 3: return b_transport_azimuthal<3>;
-    case 4: return b_transport_azimuthal<4>;
-    case 6: return b_transport_azimuthal<6>;
-    case 8: return b_transport_azimuthal<8>;
-    case 12: return b_transport_azimuthal<12>;
-    case 16: return b_transport_azimuthal<16>;
+    case 1: return b_transport_azimuthal<1, NQ>;
+    case 2: return b_transport_azimuthal<2, NQ>;
+    case 3: return b_transport_azimuthal<3, NQ>;
+    case 4: return b_transport_azimuthal<4, NQ>;
+    case 6: return b_transport_azimuthal<6, NQ>;
+    case 8: return b_transport_azimuthal<8, NQ>;
+    case 12: return b_transport_azimuthal<12, NQ>;
+    case 16: return b_transport_azimuthal<16, NQ>;
     default: return nullptr;
     }
 }
+static AzFn az_fn(int per, int nq) { return nq == 5 ? az_fn_nq<5>(per) : az_fn_nq<4>(per); }
 
 static const void *kernel_fn(int k, int per)
 {
@@ -391,7 +395,7 @@ static const void *kernel_fn(int k, int per)
     case FGPU_BK_VISCOUS: return (const void *)b_viscous;
     case FGPU_BK_GHOST: return (const void *)b_ghost;
     case FGPU_BK_TRANSPORT_RADIAL: return (const void *)b_transport_radial;
-    case FGPU_BK_TRANSPORT_AZIMUTHAL: return (const void *)az_fn(per);
+    case FGPU_BK_TRANSPORT_AZIMUTHAL: return (const void *)az_fn(per, 5);
     case FGPU_BK_FINISH: return (const void *)b_finish;
     case FGPU_BK_DAMPING: return (const void *)b_damping;
     case FGPU_BK_DERIVED_CFL: return (const void *)b_derived_cfl;
@@ -410,7 +414,7 @@ struct fgpu_batch {
     std::vector<Engine32 *> disks;
     std::vector<int> nr, nz;
     int nz_max = 0, nsm = 0;
-    bool any_art = false;
+    bool any_art = false, any_iso = false, any_adi = false;
     std::string err;
 
     DiskF *d_disks = nullptr;
@@ -517,6 +521,13 @@ static int apply_tiles(fgpu_batch *b, const fgpu_tiles &t)
     for (int k = 0; k < FGPU_BK_COUNT; ++k) {
         const void *fn = kernel_fn(k, b->az_per);
         const size_t smem = k == FGPU_BK_TRANSPORT_AZIMUTHAL ? b->az_smem : 0;
+        cudaFuncAttributes attr;
+        CKB(cudaFuncGetAttributes(&attr, fn));
+        if (t.k[k].threads > attr.maxThreadsPerBlock) {
+            b->err = "kernel " + std::to_string(k) + " takes at most " +
+                     std::to_string(attr.maxThreadsPerBlock) + " threads per block";
+            return FGPU_ERR_UNSUPPORTED;
+        }
         int per_sm = 0;
         CKB(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, t.k[k].threads, smem));
         if (per_sm < 1) {
@@ -566,7 +577,8 @@ static void launch_kernel(fgpu_batch *b, int k, int ghost_b = 0)
         b_transport_radial<<<g, th, 0, s>>>(D, S, b->table(k), nd, r);
         break;
     case FGPU_BK_TRANSPORT_AZIMUTHAL:
-        az_fn(b->az_per)<<<g, th, b->az_smem, s>>>(D, S, b->table(k), nd);
+        if (b->any_iso) az_fn(b->az_per, 4)<<<g, th, b->az_smem, s>>>(D, S, b->table(k), nd);
+        if (b->any_adi) az_fn(b->az_per, 5)<<<g, th, b->az_smem, s>>>(D, S, b->table(k), nd);
         break;
     case FGPU_BK_FINISH: b_finish<<<g, th, 0, s>>>(D, S, b->table(k), nd, r); break;
     case FGPU_BK_DAMPING:
@@ -675,6 +687,8 @@ extern "C" int fgpu_batch_create(int n, const fgpu_params *params, const double 
         b->nz_max = std::max(b->nz_max, e->azimuthal());
         desc[k] = e->describe();
         b->any_art = b->any_art || desc[k].ph.adiabatic || desc[k].ph.art_visc_sn;
+        b->any_iso = b->any_iso || desc[k].nq == 4;
+        b->any_adi = b->any_adi || desc[k].nq == 5;
         int nrings = 0;
         const int *rings = e->damping_rings(&nrings);
         for (int q = 0; q < nrings; ++q) damp.push_back(make_int2(k, rings[q]));
@@ -697,9 +711,12 @@ extern "C" int fgpu_batch_create(int n, const fgpu_params *params, const double 
             return fail(FGPU_ERR_CUDA);                                  \
         }                                                                \
     } while (0)
-    for (int per : kPerChoices)
-        CKC(cudaFuncSetAttribute((const void *)az_fn(per),
+    for (int per : kPerChoices) {
+        CKC(cudaFuncSetAttribute((const void *)az_fn(per, 4),
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->az_smem));
+        CKC(cudaFuncSetAttribute((const void *)az_fn(per, 5),
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->az_smem));
+    }
     CKC(cudaMalloc(&b->d_disks, sizeof(DiskF) * n));
     CKC(cudaMemcpy(b->d_disks, desc.data(), sizeof(DiskF) * n, cudaMemcpyHostToDevice));
     CKC(cudaMalloc(&b->d_steps, sizeof(StepF) * n));
@@ -1097,8 +1114,10 @@ extern "C" int fgpu_batch_autotune(fgpu_batch *b, int reps, fgpu_tiles *best)
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    b->err.clear();
+    if (rc == FGPU_OK) b->err.clear();
+    const std::string keep = b->err;
     int rc2 = apply_tiles(b, cur);
+    if (rc != FGPU_OK) b->err = keep;
     if (rc == FGPU_OK) rc = rc2;
     // put the state (evolved and derived fields, CFL minima) back
     int rc3 = take_snapshot(b, snap, true);

@@ -633,17 +633,19 @@ __device__ __forceinline__ void radial_col(const GeoF &g, const TablesF &t, floa
 // 630-664): FP32 advection, FP64 ring mean and shift phase.  The residual
 // angular momentum is advected like any specific quantity (J_K is constant on
 // a ring, so its part cancels exactly).  One block per ring; thread tid owns
-// cells tid + n * blockDim.x, n < PER, which must cover the ring.
+// cells tid + n * blockDim.x, n < PER, which must cover the ring.  Each
+// quantity takes three barriers: specific values, slopes, fluxes (a separate
+// flux array lets the update read them while the next quantity starts).
 // ---------------------------------------------------------------------------
-template <int PER>
-__device__ __forceinline__ void ring_pass_f(float *S, float *SS, float *W, float *D,
-                                            float *const *qrow, int nq, const float *v,
+template <int PER, int NQ>
+__device__ __forceinline__ void ring_pass_f(float *S, float *SS, float *W, float *D, float *F,
+                                            float *const *qrow, const float *v,
                                             float *slo, float dt, float dxtheta,
                                             float half_invdx, float dxrad, float invsurf, int nz,
                                             int mc, bool uniform, float vconst)
 {
     const int tid = threadIdx.x, bs = blockDim.x;
-    float invs[PER], f[PER];
+    float invs[PER];
 #pragma unroll
     for (int n = 0; n < PER; ++n) {
         const int j = tid + n * bs;
@@ -665,7 +667,8 @@ __device__ __forceinline__ void ring_pass_f(float *S, float *SS, float *W, float
         }
     }
     __syncthreads();
-    for (int q = 0; q < nq; ++q) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
         float *Q = qrow[q];
 #pragma unroll
         for (int n = 0; n < PER; ++n) {
@@ -691,59 +694,51 @@ __device__ __forceinline__ void ring_pass_f(float *S, float *SS, float *W, float
                 const float ksi = vv * dt;
                 const float qs = ksi > 0.f ? W[jm] + (dxtheta - ksi) * D[jm]
                                            : W[j] - (dxtheta + ksi) * D[j];
-                f[n] = dxrad * qs * SS[j] * vv;
+                F[j] = dxrad * qs * SS[j] * vv;
             }
         }
         __syncthreads();
 #pragma unroll
         for (int n = 0; n < PER; ++n) {
             const int j = tid + n * bs;
-            if (j < nz) W[j] = f[n];
+            if (j < nz) Q[j] += (F[j] - F[j == nz - 1 ? 0 : j + 1]) * invsurf;
         }
-        __syncthreads();
-#pragma unroll
-        for (int n = 0; n < PER; ++n) {
-            const int j = tid + n * bs;
-            if (j < nz) Q[j] += (W[j] - W[j == nz - 1 ? 0 : j + 1]) * invsurf;
-        }
-        __syncthreads();
     }
+    __syncthreads();
 #pragma unroll
     for (int n = 0; n < PER; ++n) {
         const int j = tid + n * bs;
-        if (j < nz) W[j] = dxrad * SS[j] * (uniform ? vconst : v[n]);
+        if (j < nz) F[j] = dxrad * SS[j] * (uniform ? vconst : v[n]);
     }
     __syncthreads();
 #pragma unroll
     for (int n = 0; n < PER; ++n) {
         const int j = tid + n * bs;
         if (j < nz) {
-            f[n] = S[j];
-            comp_add(f[n], slo[n], (W[j] - W[j == nz - 1 ? 0 : j + 1]) * invsurf);
+            float sn = S[j];
+            comp_add(sn, slo[n], (F[j] - F[j == nz - 1 ? 0 : j + 1]) * invsurf);
+            S[j] = sn;
         }
     }
     __syncthreads();
-#pragma unroll
-    for (int n = 0; n < PER; ++n) {
-        const int j = tid + n * bs;
-        if (j < nz) S[j] = f[n];
-    }
-    __syncthreads();
-}
-
-// Shared memory of azimuthal_ring: 4 ring-long work arrays, plus the nq
-// quantity rows when STAGE (then every row is read from HBM once, up front,
-// and the passes and the shift work in shared memory).
-__host__ __device__ constexpr size_t azimuthal_smem_floats(int nz, int nq, bool stage)
-{
-    return (size_t)(stage ? 4 + nq : 4) * (size_t)nz;
 }
 
 // smf: azimuthal_smem_floats(nz, nq, STAGE) floats of shared memory; redf: 33
 // floats, redl: 33 long longs (shared memory)
-template <int PER, bool STAGE>
+// Shared memory of azimuthal_ring: 5 ring-long work arrays (sigma, its star
+// value, the specific quantity, its slope, the flux), plus the nq quantity
+// rows when STAGE (then every row is read from HBM once, up front, and the
+// passes and the shift work in shared memory).
+__host__ __device__ constexpr size_t azimuthal_smem_floats(int nz, int nq, bool stage)
+{
+    return (size_t)(stage ? 5 + nq : 5) * (size_t)nz;
+}
+
+// smf: azimuthal_smem_floats(nz, nq, STAGE) floats of shared memory; redf: 33
+// floats, redl: 33 long longs (shared memory)
+template <int PER, int NQ, bool STAGE>
 __device__ __forceinline__ void azimuthal_ring(const GeoF &g, const TablesF &t, double dt, int mc,
-                                               int fast, int nq, const float *__restrict__ dv,
+                                               int fast, const float *__restrict__ dv,
                                                float *m0, float *m1, float *m2, float *m3,
                                                float *E, float *S, float *S_lo, int i, float *smf,
                                                float *redf, long long *redl)
@@ -751,11 +746,11 @@ __device__ __forceinline__ void azimuthal_ring(const GeoF &g, const TablesF &t, 
     const int nz = g.nz;
     const int tid = threadIdx.x, bs = blockDim.x;
     const size_t row = (size_t)i * nz;
-    float *Sr = smf, *SS = smf + nz, *W = smf + 2 * nz, *D = smf + 3 * nz;
+    float *Sr = smf, *SS = smf + nz, *W = smf + 2 * nz, *D = smf + 3 * nz, *Fx = smf + 4 * nz;
     float *grow[5] = {m0 + row, m1 + row, m2 + row, m3 + row, E + row};
     float *qrow[5];
 #pragma unroll
-    for (int q = 0; q < 5; ++q) qrow[q] = STAGE ? smf + (size_t)(4 + q) * nz : grow[q];
+    for (int q = 0; q < 5; ++q) qrow[q] = STAGE ? smf + (size_t)(5 + q) * nz : grow[q];
 
     float vown[PER], slo[PER];
     float amax = 0.f;
@@ -768,7 +763,8 @@ __device__ __forceinline__ void azimuthal_ring(const GeoF &g, const TablesF &t, 
             Sr[j] = S[row + j];
             slo[n] = S_lo[row + j];
             if (STAGE) {
-                for (int q = 0; q < nq; ++q) qrow[q][j] = grow[q][j];
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) qrow[q][j] = grow[q][j];
             }
         }
     }
@@ -800,11 +796,11 @@ __device__ __forceinline__ void azimuthal_ring(const GeoF &g, const TablesF &t, 
     const float half_invdx = 0.5f / dxtheta;
     const float dxrad = (t.Rsup[i] - t.Rinf[i]) * (float)dt;
     const float invsurf = t.InvSurf[i];
-    ring_pass_f<PER>(Sr, SS, W, D, qrow, nq, vown, slo, (float)dt, dxtheta, half_invdx, dxrad,
-                     invsurf, nz, mc, false, 0.f);
+    ring_pass_f<PER, NQ>(Sr, SS, W, D, Fx, qrow, vown, slo, (float)dt, dxtheta, half_invdx,
+                         dxrad, invsurf, nz, mc, false, 0.f);
     if (fast) {
-        ring_pass_f<PER>(Sr, SS, W, D, qrow, nq, vown, slo, (float)dt, dxtheta, half_invdx, dxrad,
-                         invsurf, nz, mc, true, vt);
+        ring_pass_f<PER, NQ>(Sr, SS, W, D, Fx, qrow, vown, slo, (float)dt, dxtheta, half_invdx,
+                             dxrad, invsurf, nz, mc, true, vt);
     }
     // the integer shift (AdvectSHIFT, :238-268): cell j takes cell j - nshift
     const int ns = nshift % nz;
@@ -818,9 +814,10 @@ __device__ __forceinline__ void azimuthal_ring(const GeoF &g, const TablesF &t, 
     }
     if (STAGE) {
         // all rows are in shared memory: shift straight out of it
-        for (int q = 0; q <= nq; ++q) {
-            const float *from = q < nq ? qrow[q] : Sr;
-            float *to = q < nq ? grow[q] : S + row;
+#pragma unroll
+        for (int q = 0; q <= NQ; ++q) {
+            const float *from = q < NQ ? qrow[q] : Sr;
+            float *to = q < NQ ? grow[q] : S + row;
 #pragma unroll
             for (int n = 0; n < PER; ++n) {
                 const int j = tid + n * bs;
@@ -828,9 +825,10 @@ __device__ __forceinline__ void azimuthal_ring(const GeoF &g, const TablesF &t, 
             }
         }
     } else {
-        for (int q = 0; q <= nq; ++q) {
-            float *Q = q < nq ? grow[q] : S + row;
-            const float *from = q < nq ? grow[q] : Sr;
+#pragma unroll
+        for (int q = 0; q <= NQ; ++q) {
+            float *Q = q < NQ ? grow[q] : S + row;
+            const float *from = q < NQ ? grow[q] : Sr;
 #pragma unroll
             for (int n = 0; n < PER; ++n) {
                 const int j = tid + n * bs;

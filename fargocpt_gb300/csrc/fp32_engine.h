@@ -129,6 +129,7 @@ class Engine32 {
     void destroy();
     int upload(int field, const double *host, int rows);
     int download(int field, double *host, int rows);
+    int to_fp64(int field, double *dst, int rows);
     void set_bodies(int n, const fgpu_body *b, double ix, double iy);
     int init_euler(double t);
     int derived_cfl(int mode);

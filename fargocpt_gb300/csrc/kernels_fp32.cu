@@ -126,9 +126,9 @@ __global__ void f_transport_radial(GeoF g, TablesF t, float dt, int mc, int chun
                    S_lo_out, blockIdx.y * chunk, j);
 }
 
-template <int PER, bool STAGE>
+template <int PER, int NQ, bool STAGE>
 __global__ void __launch_bounds__(512) f_transport_azimuthal(GeoF g, TablesF t, double dt, int mc,
-                                                             int fast, int nq,
+                                                             int fast,
                                                              const float *__restrict__ dv,
                                                              float *m0, float *m1, float *m2,
                                                              float *m3, float *E, float *S,
@@ -137,8 +137,8 @@ __global__ void __launch_bounds__(512) f_transport_azimuthal(GeoF g, TablesF t, 
     extern __shared__ __align__(16) float smf[];
     __shared__ float redf[33];
     __shared__ long long redl[33];
-    azimuthal_ring<PER, STAGE>(g, t, dt, mc, fast, nq, dv, m0, m1, m2, m3, E, S, S_lo,
-                               blockIdx.x, smf, redf, redl);
+    azimuthal_ring<PER, NQ, STAGE>(g, t, dt, mc, fast, dv, m0, m1, m2, m3, E, S, S_lo,
+                                   blockIdx.x, smf, redf, redl);
 }
 
 __global__ void f_pressure(GeoF g, TablesF t, PhysF ph, const float *__restrict__ S,
@@ -532,10 +532,19 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
         err = "ring too long for the FP32 azimuthal kernel";
         return FGPU_ERR_UNSUPPORTED;
     }
-    const void *az_kernels[6] = {
-        (const void *)f_transport_azimuthal<4, false>, (const void *)f_transport_azimuthal<8, false>,
-        (const void *)f_transport_azimuthal<16, false>, (const void *)f_transport_azimuthal<4, true>,
-        (const void *)f_transport_azimuthal<8, true>, (const void *)f_transport_azimuthal<16, true>};
+    const void *az_kernels[12] = {
+        (const void *)f_transport_azimuthal<4, 4, false>,
+        (const void *)f_transport_azimuthal<8, 4, false>,
+        (const void *)f_transport_azimuthal<16, 4, false>,
+        (const void *)f_transport_azimuthal<4, 4, true>,
+        (const void *)f_transport_azimuthal<8, 4, true>,
+        (const void *)f_transport_azimuthal<16, 4, true>,
+        (const void *)f_transport_azimuthal<4, 5, false>,
+        (const void *)f_transport_azimuthal<8, 5, false>,
+        (const void *)f_transport_azimuthal<16, 5, false>,
+        (const void *)f_transport_azimuthal<4, 5, true>,
+        (const void *)f_transport_azimuthal<8, 5, true>,
+        (const void *)f_transport_azimuthal<16, 5, true>};
     for (const void *fn : az_kernels) {
         if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)az_smem) !=
             cudaSuccess) {
@@ -626,14 +635,23 @@ int Engine32::upload(int f, const double *host, int rows)
     return FGPU_OK;
 }
 
-int Engine32::download(int f, double *host, int rows)
+// FargoCPT's FP64 values of field f into the device buffer dst, in stream order
+int Engine32::to_fp64(int f, double *dst, int rows)
 {
     const size_t n = (size_t)rows * nz;
     if (f == FGPU_SIGMA)
-        f_join_f64<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(fld[f], sigma_lo, stage, n);
+        f_join_f64<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(fld[f], sigma_lo, dst, n);
     else
-        f_to_f64<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(fld[f], stage, n, nz, offset_of(f));
+        f_to_f64<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(fld[f], dst, n, nz, offset_of(f));
     CKF(cudaGetLastError());
+    return FGPU_OK;
+}
+
+int Engine32::download(int f, double *host, int rows)
+{
+    const size_t n = (size_t)rows * nz;
+    int rc = to_fp64(f, stage, rows);
+    if (rc) return rc;
     CKF(cudaMemcpyAsync(host, stage, n * sizeof(double), cudaMemcpyDeviceToHost, stream));
     CKF(cudaStreamSynchronize(stream));
     return FGPU_OK;
@@ -798,20 +816,26 @@ int Engine32::transport(double dt)
     }
     mark(7);
     {
-        const int nq = adi ? 5 : 4;
-#define AZ32(P, ST)                                                                              \
-    f_transport_azimuthal<P, ST><<<nr, az_block, az_smem, stream>>>(                             \
-        geo, tabs, dt, phys.limiter_mc, phys.fast_transport, nq, s.dv, mom[0], mom[1], mom[2],  \
+#define AZ32(P, NQ, ST)                                                                          \
+    f_transport_azimuthal<P, NQ, ST><<<nr, az_block, az_smem, stream>>>(                         \
+        geo, tabs, dt, phys.limiter_mc, phys.fast_transport, s.dv, mom[0], mom[1], mom[2],      \
         mom[3], alt_e, alt_sigma, alt_sigma_lo)
-        if (az_stage) {
-            if (per == 4) AZ32(4, true);
-            else if (per == 8) AZ32(8, true);
-            else AZ32(16, true);
+#define AZ32_NQ(NQ)                                      \
+    if (az_stage) {                                      \
+        if (per == 4) AZ32(4, NQ, true);                 \
+        else if (per == 8) AZ32(8, NQ, true);            \
+        else AZ32(16, NQ, true);                         \
+    } else {                                             \
+        if (per == 4) AZ32(4, NQ, false);                \
+        else if (per == 8) AZ32(8, NQ, false);           \
+        else AZ32(16, NQ, false);                        \
+    }
+        if (adi) {
+            AZ32_NQ(5)
         } else {
-            if (per == 4) AZ32(4, false);
-            else if (per == 8) AZ32(8, false);
-            else AZ32(16, false);
+            AZ32_NQ(4)
         }
+#undef AZ32_NQ
 #undef AZ32
     }
     mark(8);

@@ -253,6 +253,21 @@ int fgpu_phase_times(fgpu_engine *eng, double *ms, int capacity, int *count,
 		     int *steps);
 const char *fgpu_phase_name(int k);
 
+/* Asynchronous snapshots (the payload of FargoCPT's write2D,
+ * src/polargrid.cpp:135-180: every row of the grid, row-major FP64, the
+ * FP32-mixed form converted back to FargoCPT's values).  fgpu_snapshot_begin
+ * copies fields[0 .. n-1] into device staging buffers in order with the
+ * steps, then copies them to host[k] (rows x naz doubles each) on a second
+ * stream, so the steps that follow run while the copy drains; host[k] must
+ * stay valid until fgpu_snapshot_wait returns.  One snapshot is in flight at
+ * a time (begin waits for the previous one).  Page-locked buffers from
+ * fgpu_host_alloc copy at full speed.  No counterpart in the reference, whose
+ * output stops the run while it writes (src/output.cpp:249-304). */
+int fgpu_snapshot_begin(fgpu_engine *eng, int n, const int *fields, double *const *host);
+int fgpu_snapshot_wait(fgpu_engine *eng);
+int fgpu_host_alloc(size_t bytes, void **ptr);
+int fgpu_host_free(void *ptr);
+
 /* The phases of the step, for hosts that compose their own integrator
  * (step_LeapFrog, src/simulation.cpp:276-459, kicks with dt/2 around one
  * transport over dt):
@@ -347,7 +362,7 @@ typedef struct {
 /* params[k], radii[k]: disk k as for fgpu_create; every disk must select
  * FGPU_PRECISION_FP32_MIXED and the Euler integrator (the batched step is
  * step_Euler); the longest ring must fit the azimuthal
- * transport's shared memory (naz <= 6144).  1 <= n <= 1024. */
+ * transport's shared memory (naz <= 5632).  1 <= n <= 1024. */
 int fgpu_batch_create(int n, const fgpu_params *params,
 		      const double *const *radii, fgpu_batch **out);
 int fgpu_batch_destroy(fgpu_batch *b);
