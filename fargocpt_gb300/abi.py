@@ -57,7 +57,8 @@ class FgpuParams(C.Structure):
         ("bc_energy_inner", C.c_int), ("bc_energy_outer", C.c_int),
         ("bc_vrad_inner", C.c_int), ("bc_vrad_outer", C.c_int),
         ("bc_vaz_inner", C.c_int), ("bc_vaz_outer", C.c_int),
-        ("precision", C.c_int), ("integrator", C.c_int), ("reserved_i", C.c_int * 6),
+        ("precision", C.c_int), ("integrator", C.c_int),
+        ("stabilize_viscosity", C.c_int), ("reserved_i", C.c_int * 5),
         ("gamma", C.c_double), ("mu", C.c_double), ("aspect_ratio", C.c_double),
         ("flaring_index", C.c_double), ("viscous_alpha", C.c_double),
         ("constant_viscosity", C.c_double), ("art_visc_factor", C.c_double),

@@ -61,6 +61,9 @@ struct fgpu_engine {
 
     // asynchronous snapshots: device staging, a copy stream and its events
     double *snap_stage = nullptr;
+    // StabilizeViscosity correction factors (VISCOSITY_CORRECTION_FACTOR_PHI/R),
+    // zero until the first stress evaluation like the reference's grids
+    double *corr_phi = nullptr, *corr_r = nullptr;
     size_t snap_capacity = 0;  // doubles
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t snap_staged = nullptr, snap_copied = nullptr;
@@ -189,8 +192,12 @@ static int validate(const fgpu_params *p, std::string &why)
     if (p->nrad < 6 || p->naz < 8) { why = "nrad >= 6 and naz >= 8 required"; return FGPU_ERR_BAD_ARG; }
     if (p->naz > 8192) { why = "naz > 8192 not supported by the azimuthal kernel (16 cells x 512 threads per ring)"; return FGPU_ERR_UNSUPPORTED; }
     if (p->eos != FGPU_EOS_ISOTHERMAL && p->eos != FGPU_EOS_IDEAL) { why = "eos"; return FGPU_ERR_BAD_ARG; }
-    if (p->art_visc == FGPU_ARTVISC_TW) { why = "Tscharnuter-Winkler artificial viscosity is not on the GPU path"; return FGPU_ERR_UNSUPPORTED; }
-    if (p->art_visc != FGPU_ARTVISC_NONE && p->art_visc != FGPU_ARTVISC_SN) { why = "art_visc"; return FGPU_ERR_BAD_ARG; }
+    if (p->art_visc != FGPU_ARTVISC_NONE && p->art_visc != FGPU_ARTVISC_SN && p->art_visc != FGPU_ARTVISC_TW) { why = "art_visc"; return FGPU_ERR_BAD_ARG; }
+    if (p->stabilize_viscosity < 0 || p->stabilize_viscosity > 2) { why = "stabilize_viscosity must be 0, 1 or 2"; return FGPU_ERR_BAD_ARG; }
+    if (p->precision == FGPU_PRECISION_FP32_MIXED && (p->art_visc == FGPU_ARTVISC_TW || p->stabilize_viscosity)) {
+        why = "Tscharnuter-Winkler artificial viscosity and StabilizeViscosity are FP64 only";
+        return FGPU_ERR_UNSUPPORTED;
+    }
     if (p->precision != FGPU_PRECISION_FP64 && p->precision != FGPU_PRECISION_FP32_MIXED) { why = "precision"; return FGPU_ERR_BAD_ARG; }
     if (p->integrator != FGPU_INTEGRATOR_EULER && p->integrator != FGPU_INTEGRATOR_LEAPFROG) { why = "integrator"; return FGPU_ERR_BAD_ARG; }
     if (p->radial_spacing != FGPU_SPACING_LOGARITHMIC && p->radial_spacing != FGPU_SPACING_ARITHMETIC) { why = "radial_spacing"; return FGPU_ERR_BAD_ARG; }
@@ -219,7 +226,8 @@ static int setup_tables(fgpu_engine *eng, const double *radii)
     eng->geo = Geo{nr, nz, dphi, invdphi};
     enum { RINF, RSUP, RMED, SURF, INVRMED, INVSURF, INVDIFFRMED, INVDIFFRSUP, INVDIFFRSUPRB,
            INVRINF, RINFSQ, TWOOVER, OMEGAK, INVOMEGAK, CSISO, INVDXSRC, INVDXTHETA, EMODEL,
-           HFACADI, INVCELL, INVCELL2, TWOOVERRMEDSUM, NTAB };
+           HFACADI, INVCELL, INVCELL2, TWOOVERRMEDSUM, LSQTW, TWOOVERDRMED2, DIFFRMED,
+           RA3IDRMED, F43, CRPP1, CRPP2, CRRR1, CRRR2, CRRP, CRSCALE, NTAB };
     std::vector<double> h((size_t)NTAB * R, 0.0);
     auto T = [&](int k) { return h.data() + (size_t)k * R; };
     for (int n = 0; n <= nr; ++n) {
@@ -257,6 +265,30 @@ static int setup_tables(fgpu_engine *eng, const double *radii)
     for (int n = 0; n < nr; ++n) {
         T(TWOOVER)[n] = 2.0 / (std::pow(T(RINF)[n + 1], 2) - std::pow(T(RINF)[n], 2));
     }
+    for (int n = 0; n <= nr; ++n) {
+        // Tscharnuter-Winkler length scale, artificial_viscosity.cpp:60-73
+        if (n < nr) {
+            const double Dr = T(RINF)[n + 1] - T(RINF)[n], rDphi = T(RMED)[n] * dphi;
+            const double dx = nz <= 16 ? std::min(Dr, rDphi) : std::max(Dr, rDphi);
+            T(LSQTW)[n] = std::pow(p.art_visc_factor, 2) * std::pow(dx, 2);
+        }
+        // StabilizeViscosity ring factors, viscosity.cpp:280-331 (Ra = Rinf)
+        const double ra = T(RINF)[n];
+        T(RA3IDRMED)[n] = std::pow(ra, 3) * T(INVDIFFRMED)[n];
+        T(F43)[n] = 4.0 / 3.0 / T(RMED)[n] * invdphi * invdphi;
+        T(CRRP)[n] = 1.0 / (dphi * dphi * ra);
+        if (n >= 1) {
+            T(TWOOVERDRMED2)[n] = 2.0 / (std::pow(T(RMED)[n], 2) - std::pow(T(RMED)[n - 1], 2));
+            T(DIFFRMED)[n] = T(RMED)[n] - T(RMED)[n - 1];
+            T(CRPP1)[n] = 2.0 * (0.5 * T(INVRMED)[n] + 1.0 / 3.0 * ra * T(INVDIFFRSUPRB)[n]);
+            T(CRPP2)[n] = 2.0 * (0.5 * T(INVRMED)[n - 1] - 1.0 / 3.0 * ra * T(INVDIFFRSUPRB)[n - 1]);
+            T(CRRR1)[n] = T(RMED)[n] * 2.0 *
+                          (-T(INVDIFFRSUP)[n] + 1.0 / 3.0 * ra * T(INVDIFFRSUPRB)[n]);
+            T(CRRR2)[n] = -1.0 * T(RMED)[n - 1] * 2.0 *
+                          (T(INVDIFFRSUP)[n - 1] - 1.0 / 3.0 * ra * T(INVDIFFRSUPRB)[n - 1]);
+            T(CRSCALE)[n] = p.radial_viscosity_factor / (0.5 * (T(RMED)[n] + T(RMED)[n - 1]));
+        }
+    }
     std::vector<double> cs(nz), sn(nz);
     for (int j = 0; j < nz; ++j) {
         cs[j] = std::cos(dphi * (double)j);  // SideEuler.cpp:56-61
@@ -277,6 +309,9 @@ static int setup_tables(fgpu_engine *eng, const double *radii)
     t.InvOmegaK = D(INVOMEGAK); t.CsIso = D(CSISO); t.InvDxSrc = D(INVDXSRC);
     t.InvDxTheta = D(INVDXTHETA); t.EModel = D(EMODEL); t.HFacAdi = D(HFACADI);
     t.InvCell = D(INVCELL); t.InvCell2 = D(INVCELL2); t.TwoOverRmedSum = D(TWOOVERRMEDSUM);
+    t.LSqTW = D(LSQTW); t.TwoOverDRmed2 = D(TWOOVERDRMED2); t.DiffRmed = D(DIFFRMED);
+    t.Ra3IDRmed = D(RA3IDRMED); t.F43 = D(F43); t.CrPp1 = D(CRPP1); t.CrPp2 = D(CRPP2);
+    t.CrRr1 = D(CRRR1); t.CrRr2 = D(CRRR2); t.CrRp = D(CRRP); t.CrScale = D(CRSCALE);
     t.cosj = tc; t.sinj = tc + nz;
 
     // boundary hooks
@@ -343,6 +378,8 @@ static int setup_tables(fgpu_engine *eng, const double *radii)
     Phys &ph = eng->ph;
     ph.adiabatic = p.eos == FGPU_EOS_IDEAL;
     ph.art_visc_sn = p.art_visc == FGPU_ARTVISC_SN;
+    ph.art_visc_tw = p.art_visc == FGPU_ARTVISC_TW;
+    ph.stabilize = p.stabilize_viscosity;
     ph.dissipation = p.art_visc_dissipation;
     ph.limiter_mc = p.flux_limiter == FGPU_LIMITER_MC;
     ph.fast_transport = p.fast_transport;
@@ -461,6 +498,15 @@ static int create_engine(const fgpu_params *params, const double *radii, cudaStr
         }
         cudaMemset(*alts[k], 0, n * sizeof(double));
     }
+    if (params->stabilize_viscosity) {
+        if (cudaMalloc(&eng->corr_phi, eng->cells * sizeof(double)) != cudaSuccess ||
+            cudaMalloc(&eng->corr_r, eng->cells * sizeof(double)) != cudaSuccess) {
+            eng->err = "out of device memory (viscosity correction factors)";
+            return fail(FGPU_ERR_OOM);
+        }
+        cudaMemset(eng->corr_phi, 0, eng->cells * sizeof(double));
+        cudaMemset(eng->corr_r, 0, eng->cells * sizeof(double));
+    }
     for (int k = 0; k < 4; ++k) {
         if (cudaMalloc(&eng->mom[k], eng->cells * sizeof(double)) != cudaSuccess) {
             eng->err = "out of device memory (momenta)";
@@ -522,6 +568,7 @@ extern "C" int fgpu_destroy(fgpu_engine *eng)
     cudaFree(eng->ring_ws); cudaFree(eng->tables_mem); cudaFree(eng->damp_mem);
     cudaFree(eng->damp_rings); cudaFree(eng->partial); cudaFree(eng->red_out);
     cudaFree(eng->d_dtmin); cudaFree(eng->d_bad);
+    cudaFree(eng->corr_phi); cudaFree(eng->corr_r);
     if (eng->h_pinned) cudaFreeHost(eng->h_pinned);
     if (eng->copy_stream) {
         cudaStreamSynchronize(eng->copy_stream);
@@ -582,6 +629,7 @@ static State state_of(fgpu_engine *eng)
     s.pot = f[FGPU_POTENTIAL]; s.divv = f[FGPU_DIV_V]; s.trr = f[FGPU_TAU_R_R];
     s.tpp = f[FGPU_TAU_PHI_PHI]; s.trp = f[FGPU_TAU_R_PHI]; s.qr = f[FGPU_Q_R];
     s.qphi = f[FGPU_Q_PHI];
+    s.corr_phi = eng->corr_phi; s.corr_r = eng->corr_r;
     return s;
 }
 
@@ -768,6 +816,7 @@ extern "C" int fgpu_init_euler(fgpu_engine *eng, double t)
     if (eng->ph.adiabatic) {
         // compute_heating_cooling_for_CFL, SourceEuler.cpp:1410-1450
         launch_stress(L, s.sigma, s.vr, s.vaz, s.nu, s.divv, s.trr, s.tpp, s.trp);
+        if (eng->ph.stabilize) launch_visc_corr(L, s);
         launch_viscous(L, 0.0, beta_inv_at(eng->p, t), 2, s);
     }
     eng->cfl_valid = false;
@@ -842,7 +891,7 @@ static void gas_kick(fgpu_engine *eng, double dt, double t)
     mark(eng, 1);
     State s = state_of(eng);
     // compression heating + artificial viscosity (simulation.cpp:190-194)
-    if (adi || eng->ph.art_visc_sn) {
+    if (adi || eng->ph.art_visc_sn || eng->ph.art_visc_tw) {
         launch_artvisc_q(L, dt, s.sigma, s.vr, s.vaz, s.energy, s.qr, s.qphi);
         mark(eng, 2);
         launch_artvisc_v(L, dt, s.sigma, s.energy, s.qr, s.qphi, s.vr, s.vaz, s.cs, s.H, s.nu);
@@ -853,6 +902,7 @@ static void gas_kick(fgpu_engine *eng, double dt, double t)
     }
     // viscous stress and velocity update, SubStep3 (simulation.cpp:196-203)
     launch_stress(L, s.sigma, s.vr, s.vaz, s.nu, s.divv, s.trr, s.tpp, s.trp);
+    if (eng->ph.stabilize) launch_visc_corr(L, s);
     mark(eng, 4);
     launch_viscous(L, dt, beta_inv_at(eng->p, t), adi ? 7 : 1, s);
     mark(eng, 5);

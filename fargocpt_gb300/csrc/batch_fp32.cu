@@ -165,7 +165,10 @@ __global__ void b_ghost(const DiskF *__restrict__ D, const StepF *__restrict__ S
     }
 }
 
-// radial transport tiles: blockDim.x columns x one chunk of rings
+// radial transport tiles: blockDim.x columns x one chunk of rings; one
+// instantiation per number of transported quantities, disks of the other
+// kind skipped
+template <int NQ>
 __global__ void b_transport_radial(const DiskF *__restrict__ D, const StepF *__restrict__ S,
                                    const int *__restrict__ start, int nd, int chunk)
 {
@@ -174,6 +177,7 @@ __global__ void b_transport_radial(const DiskF *__restrict__ D, const StepF *__r
         const int d = disk_of(start, nd, tile);
         if (!S[d].run) continue;
         const DiskF &k = D[d];
+        if (k.nq != NQ) continue;
         const int nz = k.g.nz;
         const int ncol = (nz + blockDim.x - 1) / blockDim.x;
         const int local = tile - __ldg(start + d);
@@ -181,14 +185,9 @@ __global__ void b_transport_radial(const DiskF *__restrict__ D, const StepF *__r
         if (j >= nz) continue;
         const int i0 = (local / ncol) * chunk;
         const StateF &s = k.s;
-        if (k.nq == 5)
-            radial_col<5>(k.g, k.t, S[d].fdt, k.ph.limiter_mc, chunk, s.sigma, k.vr_b, k.dv_b,
-                          s.energy, k.mom[0], k.mom[1], k.mom[2], k.mom[3], k.energy_t, k.sigma_t,
-                          s.sigma_lo, k.sigma_lo_t, i0, j);
-        else
-            radial_col<4>(k.g, k.t, S[d].fdt, k.ph.limiter_mc, chunk, s.sigma, k.vr_b, k.dv_b,
-                          s.energy, k.mom[0], k.mom[1], k.mom[2], k.mom[3], k.energy_t, k.sigma_t,
-                          s.sigma_lo, k.sigma_lo_t, i0, j);
+        radial_col<NQ>(k.g, k.t, S[d].fdt, k.ph.limiter_mc, chunk, s.sigma, k.vr_b, k.dv_b,
+                       s.energy, k.mom[0], k.mom[1], k.mom[2], k.mom[3], k.energy_t, k.sigma_t,
+                       s.sigma_lo, k.sigma_lo_t, i0, j);
     }
 }
 
@@ -239,7 +238,7 @@ __global__ void b_derived_cfl(const DiskF *__restrict__ D, const StepF *__restri
                               const int *__restrict__ start, int nd, int mode, int all)
 {
     __shared__ float red[33];
-    __shared__ long long redl[33];
+    __shared__ longlong2 red2[33];
     const int total = __ldg(start + nd);
     for (int item = blockIdx.x; item < total; item += gridDim.x) {
         const int d = disk_of(start, nd, item);
@@ -247,7 +246,7 @@ __global__ void b_derived_cfl(const DiskF *__restrict__ D, const StepF *__restri
         const DiskF &k = D[d];
         const int i = item - __ldg(start + d);
         derived_cfl_ring(k.g, k.t, k.ph, mode, k.s.sigma, k.s.energy, k.s.vr, k.s.dv, k.qplus,
-                         k.qminus, k.cs, k.H, k.P, k.T, k.nu, k.dtmin, i, red, redl);
+                         k.qminus, k.cs, k.H, k.P, k.T, k.nu, k.dtmin, i, red, red2);
     }
 }
 
@@ -394,7 +393,7 @@ static const void *kernel_fn(int k, int per)
     case FGPU_BK_STRESS: return (const void *)b_stress;
     case FGPU_BK_VISCOUS: return (const void *)b_viscous;
     case FGPU_BK_GHOST: return (const void *)b_ghost;
-    case FGPU_BK_TRANSPORT_RADIAL: return (const void *)b_transport_radial;
+    case FGPU_BK_TRANSPORT_RADIAL: return (const void *)b_transport_radial<5>;
     case FGPU_BK_TRANSPORT_AZIMUTHAL: return (const void *)az_fn(per, 5);
     case FGPU_BK_FINISH: return (const void *)b_finish;
     case FGPU_BK_DAMPING: return (const void *)b_damping;
@@ -574,7 +573,8 @@ static void launch_kernel(fgpu_batch *b, int k, int ghost_b = 0)
     case FGPU_BK_VISCOUS: b_viscous<<<g, th, 0, s>>>(D, S, b->table(k), nd, r); break;
     case FGPU_BK_GHOST: b_ghost<<<g, th, 0, s>>>(D, S, b->table(k), nd, ghost_b); break;
     case FGPU_BK_TRANSPORT_RADIAL:
-        b_transport_radial<<<g, th, 0, s>>>(D, S, b->table(k), nd, r);
+        if (b->any_iso) b_transport_radial<4><<<g, th, 0, s>>>(D, S, b->table(k), nd, r);
+        if (b->any_adi) b_transport_radial<5><<<g, th, 0, s>>>(D, S, b->table(k), nd, r);
         break;
     case FGPU_BK_TRANSPORT_AZIMUTHAL:
         if (b->any_iso) az_fn(b->az_per, 4)<<<g, th, b->az_smem, s>>>(D, S, b->table(k), nd);

@@ -131,6 +131,49 @@ __device__ __forceinline__ double exact_sum_result(long long part, int k, long l
     return ldexp((double)s, -k);
 }
 
+__device__ __forceinline__ float2 warp_max_f2(float2 v)
+{
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x = fmaxf(v.x, __shfl_down_sync(0xffffffffu, v.x, o));
+        v.y = fmaxf(v.y, __shfl_down_sync(0xffffffffu, v.y, o));
+    }
+    return v;
+}
+__device__ __forceinline__ longlong2 warp_sum_ll2(longlong2 v)
+{
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+    }
+    return v;
+}
+
+// Means of two rows at once (the CFL's ring i and ring i + 1), each with its
+// own scale, in two block reductions.  red2: 33 float2, redl2: 33 longlong2.
+__device__ __forceinline__ float2 exact_row_means2(const float *a, const float *b, int n,
+                                                   float2 *red2, longlong2 *redl2)
+{
+    float2 m = make_float2(0.f, 0.f);
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        m.x = fmaxf(m.x, fabsf(a[j]));
+        m.y = fmaxf(m.y, fabsf(b[j]));
+    }
+    m = block_reduce<float2, warp_max_f2>(m, red2, make_float2(0.f, 0.f));
+    int ea = 0, eb = 0;
+    frexpf(m.x, &ea);
+    frexpf(m.y, &eb);
+    const int ln = 32 - __clz(n);
+    const int ka = 62 - ea - ln, kb = 62 - eb - ln;
+    longlong2 part = make_longlong2(0, 0);
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        part.x += to_fixed(a[j], ka);
+        part.y += to_fixed(b[j], kb);
+    }
+    part = block_reduce<longlong2, warp_sum_ll2>(part, redl2, make_longlong2(0, 0));
+    return make_float2((float)(ldexp((double)part.x, -ka) / (double)n),
+                       (float)(ldexp((double)part.y, -kb) / (double)n));
+}
+
 // Mean of row[0 .. n-1] (global memory, cells strided over the block).
 __device__ __forceinline__ float exact_row_mean(const float *row, int n, float *redf,
                                                 long long *redl)
@@ -958,16 +1001,19 @@ __device__ __forceinline__ void derived_cfl_ring(
     const float *__restrict__ E, const float *__restrict__ vr, const float *__restrict__ dv,
     const float *__restrict__ qplus, const float *__restrict__ qminus, float *__restrict__ cs,
     float *__restrict__ H, float *__restrict__ P, float *__restrict__ T, float *__restrict__ nu,
-    unsigned int *__restrict__ dt_min, int i, float *red, long long *redl)
+    unsigned int *__restrict__ dt_min, int i, float *red, longlong2 *red2)
 {
     const int nz = g.nz, nr = g.nr;
     const size_t row = (size_t)i * nz;
     const bool do_cfl = (mode & 4) != 0;
     float md0 = 0.f, md1 = 0.f;
     if (do_cfl && i < nr - 1) {
-        // ring means of dv, independent of the block's shape
-        md0 = exact_row_mean(dv + row, nz, red, redl);
-        md1 = exact_row_mean(dv + row + nz, nz, red, redl);
+        // ring means of dv, independent of the block's shape; red2 (33
+        // longlong2) serves both pair reductions one after the other
+        const float2 m = exact_row_means2(dv + row, dv + row + nz, nz,
+                                          reinterpret_cast<float2 *>(red2), red2);
+        md0 = m.x;
+        md1 = m.y;
     }
     float local = 3.0e38f;
     if (do_cfl && i < nr - 1 && i >= 0 && (i == 0 || i < nr - 1)) {

@@ -30,6 +30,16 @@ struct Tables {
     const double *InvCell;     // 1 / min(Rsup - Rinf, Rmed dphi)  (cfl.cpp:223-225)
     const double *InvCell2;    // InvCell^2
     const double *TwoOverRmedSum; // 2 / (Rmed[i] + Rmed[i-1])  (viscosity.cpp:407)
+    // Tscharnuter-Winkler artificial viscosity (artificial_viscosity.cpp:35-140)
+    const double *LSqTW;       // pow(C, 2) * pow(max(Ra[i+1] - Ra[i], Rmed dphi), 2)
+    const double *TwoOverDRmed2; // 2 / (pow(Rmed[i], 2) - pow(Rmed[i-1], 2))
+    const double *DiffRmed;    // Rmed[i] - Rmed[i-1]
+    // StabilizeViscosity correction factors (viscosity.cpp:256-348)
+    const double *Ra3IDRmed;   // pow(Ra[i], 3) * InvDiffRmed[i]
+    const double *F43;         // FourThirdInvRbInvdphiSq (init.cpp:213-214)
+    const double *CrPp1, *CrPp2, *CrRr1, *CrRr2; // ring factors of c_r's four terms
+    const double *CrRp;        // 1 / (dphi dphi Ra[i])
+    const double *CrScale;     // RadialViscosityFactor / (0.5 (Rmed[i] + Rmed[i-1]))
     const double *cosj, *sinj; // cos / sin (dphi j)
 };
 
@@ -44,6 +54,8 @@ struct Phys {
     int adiabatic, art_visc_sn, dissipation, limiter_mc, fast_transport;
     int heating_viscous, cooling_beta, beta_ref;
     int leapfrog;         // LeapFrog integrator: three CFL limits x 0.6
+    int art_visc_tw;      // Tscharnuter-Winkler artificial viscosity
+    int stabilize;        // StabilizeViscosity 0 / 1 / 2
     double gamma, gm1, g_gm1, sqrt_gamma, mu, alpha, constant_viscosity;
     double C2;            // pow(ArtificialViscosityFactor, 2)
     double rvf, hvf, cfl, inv_hc_limit, sigma_min, sigma_floor10;
@@ -92,6 +104,7 @@ struct State {
     double *sigma0, *vr0, *vaz0, *energy0;    // reference values
     double *cs, *H, *P, *T, *nu, *qplus, *qminus, *pot;
     double *divv, *trr, *tpp, *trp, *qr, *qphi;
+    double *corr_phi, *corr_r;                // StabilizeViscosity factors (or null)
 };
 
 }  // namespace fgpu

@@ -27,6 +27,7 @@ void launch_artvisc_v(const Launch &L, double dt, const double *S, const double 
 void launch_stress(const Launch &L, const double *S, const double *vr, const double *vaz,
                    const double *nu, double *divv, double *trr, double *tpp, double *trp);
 void launch_viscous(const Launch &L, double dt, double beta_inv, int mode, const State &s);
+void launch_visc_corr(const Launch &L, const State &s);
 void launch_ghost(const Launch &L, const BcSpec &bc, double omf, const State &s);
 void launch_transport_radial(const Launch &L, double dt, double omf, int chunk, const double *S,
                              const double *vr, const double *vaz, const double *E,

@@ -178,9 +178,9 @@ __global__ void f_derived_cfl(GeoF g, TablesF t, PhysF ph, int mode, const float
                               float *__restrict__ nu, unsigned int *__restrict__ dt_min)
 {
     __shared__ float red[33];
-    __shared__ long long redl[33];
+    __shared__ longlong2 red2[33];
     derived_cfl_ring(g, t, ph, mode, S, E, vr, dv, qplus, qminus, cs, H, P, T, nu, dt_min,
-                     blockIdx.x, red, redl);
+                     blockIdx.x, red, red2);
 }
 
 // disk force on a body and gas mass: FP64 separations and accumulation

@@ -166,9 +166,9 @@ __global__ void k_source(Geo g, Tables t, double dt, double omega_frame,
 
 // ---------------------------------------------------------------------------
 // compression_heating (SourceEuler.cpp:459-493) and the first half of
-// update_with_artificial_viscosity_SN (artificial_viscosity.cpp:148-207):
-// q_r, q_phi and the energy update, then the temperature floor
-// (artificial_viscosity.cpp:19-21).
+// update_with_artificial_viscosity_SN (artificial_viscosity.cpp:148-207) or
+// _TW (:35-91): q_r, q_phi (TW: the diagonal tensor elements) and the energy
+// update, then the temperature floor (artificial_viscosity.cpp:19-21).
 // ---------------------------------------------------------------------------
 __global__ void k_artvisc_q(Geo g, Tables t, Phys ph, double dt, const double *__restrict__ S,
                             const double *__restrict__ vr, const double *__restrict__ vaz,
@@ -204,6 +204,23 @@ __global__ void k_artvisc_q(Geo g, Tables t, Phys ph, double dt, const double *_
             e = e - dt * qr * dv_r * t.InvDiffRsup[i] - dt * qp * dv_p * t.InvDxTheta[i];
         }
     }
+    if (ph.art_visc_tw) {
+        // update_with_artificial_viscosity_TW, artificial_viscosity.cpp:52-91
+        const double sig = S[c];
+        const double eps_rr = (vr1 - vr0) * t.InvDiffRsup[i];
+        const double eps_pp = t.InvRmed[i] * ((va1 - va0) * g.invdphi + 0.5 * (vr1 + vr0));
+        const double sum = eps_rr + eps_pp;
+        const double div_V = sum < 0.0 ? sum : 0.0;
+        const double lsig = t.LSqTW[i] * sig;
+        Qr[c] = lsig * -div_V * (eps_rr - 1.0 / 3.0 * div_V);
+        Qp[c] = lsig * -div_V * (eps_pp - 1.0 / 3.0 * div_V);
+        if (ph.adiabatic && ph.dissipation && i >= 1 && i < nr - 1) {
+            const double d = eps_rr - eps_pp;
+            const double qplus = -t.LSqTW[i] * div_V * sig * (1.0 / 3.0) *
+                                 (eps_rr * eps_rr + eps_pp * eps_pp + d * d);
+            e += qplus * dt;
+        }
+    }
     if (ph.adiabatic) {
         if (ph.dissipation) e = temperature_floor(e, S[c], ph);
         E[c] = e;
@@ -211,8 +228,8 @@ __global__ void k_artvisc_q(Geo g, Tables t, Phys ph, double dt, const double *_
 }
 
 // ---------------------------------------------------------------------------
-// Second half of update_with_artificial_viscosity_SN (velocity updates,
-// artificial_viscosity.cpp:209-248) and recalculate_viscosity
+// Second half of update_with_artificial_viscosity_SN / _TW (velocity updates,
+// artificial_viscosity.cpp:209-248 / :93-139) and recalculate_viscosity
 // (SourceEuler.cpp:205-223: c_s, H, nu for the ideal EOS).
 // ---------------------------------------------------------------------------
 __global__ void k_artvisc_v(Geo g, Tables t, Phys ph, double dt, const double *__restrict__ S,
@@ -235,6 +252,20 @@ __global__ void k_artvisc_v(Geo g, Tables t, Phys ph, double dt, const double *_
             const int jp = jprev(j, nz);
             vaz[c] = vaz[c] - dt * 2.0 * fast_rcp(S[c] + S[CELL(i, jp)]) *
                                   (Qp[c] - Qp[CELL(i, jp)]) * t.InvDxTheta[i];
+        }
+    }
+    if (ph.art_visc_tw) {
+        // artificial_viscosity.cpp:93-139 (conservative volume-integral form)
+        if (i >= 1 && i < nr - 1) {
+            const int jp = jprev(j, nz);
+            const double sigma_phi_avg = 0.5 * (S[c] + S[CELL(i, jp)]);
+            vaz[c] += fast_div(dt, sigma_phi_avg) * t.InvDxSrc[i] * (Qp[c] - Qp[CELL(i, jp)]);
+        }
+        if (i >= 2 && i < nr - 1) {
+            const double sigma_r_avg = 0.5 * (S[c] + S[CELL(i - 1, j)]);
+            vr[c] += ph.rvf * fast_div(dt, sigma_r_avg) * t.TwoOverDRmed2[i] *
+                     ((Qr[c] * t.Rmed[i] - Qr[CELL(i - 1, j)] * t.Rmed[i - 1]) -
+                      0.5 * (Qp[c] + Qp[CELL(i - 1, j)]) * t.DiffRmed[i]);
         }
     }
     if (ph.adiabatic) {
@@ -284,6 +315,61 @@ __global__ void k_stress(Geo g, Tables t, const double *__restrict__ S, const do
 }
 
 // ---------------------------------------------------------------------------
+// StabilizeViscosity's pseudo-implicit correction factors, the last loop of
+// compute_viscous_stress_tensor (viscosity.cpp:256-348), rows 1 .. nr - 1.
+// nu * Sigma at the cell centres and the four-cell averages at the r-phi
+// corners are recomputed from nu and Sigma (the reference stores them in
+// VISCOSITY_SIGMA / VISCOSITY_SIGMA_RP; row nr of the latter is never written
+// and stays zero).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double nusig_rp(const double *nu, const double *S, int nz, int i, int j)
+{
+    const int jp = jprev(j, nz);
+    const double n = 0.25 * (nu[CELL(i, j)] + nu[CELL(i - 1, j)] + nu[CELL(i, jp)] +
+                             nu[CELL(i - 1, jp)]);
+    const double sg = 0.25 * (S[CELL(i, j)] + S[CELL(i - 1, j)] + S[CELL(i, jp)] +
+                              S[CELL(i - 1, jp)]);
+    return n * sg;
+}
+
+__global__ void k_visc_corr(Geo g, Tables t, const double *__restrict__ S,
+                            const double *__restrict__ nu, double *__restrict__ corr_phi,
+                            double *__restrict__ corr_r)
+{
+    const int nz = g.nz, nr = g.nr;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y + 1;  // 1 .. nr - 1
+    if (j >= nz || i >= nr) return;
+    const size_t c = CELL(i, j);
+    const int jp = jprev(j, nz), jn = jnext(j, nz);
+    const double rp = nusig_rp(nu, S, nz, i, j);
+    const double rp_ip = i + 1 < nr ? nusig_rp(nu, S, nz, i + 1, j) : 0.0;
+    const double rp_jp = nusig_rp(nu, S, nz, i, jn);
+    const double ns = nu[c] * S[c];
+    const double ns_jm = nu[CELL(i, jp)] * S[CELL(i, jp)];
+    const double ns_im = nu[CELL(i - 1, j)] * S[CELL(i - 1, j)];
+    // v_phi factor
+    const double cphi_rp = -t.InvRmed[i] * t.TwoOverDRa2[i] *
+                           (rp_ip * t.Ra3IDRmed[i + 1] + rp * t.Ra3IDRmed[i]);
+    const double cphi_pp = -t.F43[i] * (ns + ns_jm);
+    const double sigma_avg_phi = 0.5 * (S[c] + S[CELL(i, jp)]);
+    corr_phi[c] = fast_div(cphi_rp + cphi_pp, sigma_avg_phi * t.Rmed[i]);
+    // v_r factor
+    const double sigma_avg_r = 0.5 * (S[c] + S[CELL(i - 1, j)]);
+    const double cr_rp = -(rp_jp + rp) * t.CrRp[i];
+    const double cr_pp = -0.5 * (ns * t.CrPp1[i] + ns_im * t.CrPp2[i]);
+    const double cr_rr = t.InvDiffRmed[i] * (ns * t.CrRr1[i] + ns_im * t.CrRr2[i]);
+    corr_r[c] = fast_div(t.CrScale[i] * (cr_rr + cr_rp + cr_pp), sigma_avg_r);
+}
+
+// pseudo-implicit limiter of a viscous velocity change, viscosity.cpp:395-399
+__device__ __forceinline__ double stabilized(double dv, double dt, double c)
+{
+    const double a = 1.0 + dt * c;
+    return dv * (1.0 / ((a > 0.0 ? a : 0.0) - dt * c));
+}
+
+// ---------------------------------------------------------------------------
 // update_velocities_with_viscosity (viscosity.cpp:355-421) fused with SubStep3
 // (SourceEuler.cpp:859-954: beta cooling, viscous heating, energy update,
 // temperature floor).  mode bit 1: velocities, bit 2: heating/cooling rates,
@@ -296,7 +382,8 @@ __global__ void k_viscous(Geo g, Tables t, Phys ph, double dt, double beta_inv, 
                           const double *__restrict__ H, const double *__restrict__ S0,
                           const double *__restrict__ E0, double *__restrict__ vr,
                           double *__restrict__ vaz, double *__restrict__ E,
-                          double *__restrict__ qplus, double *__restrict__ qminus)
+                          double *__restrict__ qplus, double *__restrict__ qminus,
+                          const double *__restrict__ corr_phi, const double *__restrict__ corr_r)
 {
     const int nz = g.nz, nr = g.nr;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -307,18 +394,20 @@ __global__ void k_viscous(Geo g, Tables t, Phys ph, double dt, double beta_inv, 
     if (mode & 1) {
         if (i >= 1 && i < nr - 1) {
             const double sigma_avg = 0.5 * (S[c] + S[CELL(i, jp)]);
-            const double dVp = fast_div(dt * t.InvRmed[i], sigma_avg) *
-                               (t.TwoOverDRa2[i] * (t.RinfSq[i + 1] * trp[CELL(i + 1, j)] -
-                                                    t.RinfSq[i] * trp[c]) +
-                                (tpp[c] - tpp[CELL(i, jp)]) * g.invdphi);
+            double dVp = fast_div(dt * t.InvRmed[i], sigma_avg) *
+                         (t.TwoOverDRa2[i] * (t.RinfSq[i + 1] * trp[CELL(i + 1, j)] -
+                                              t.RinfSq[i] * trp[c]) +
+                          (tpp[c] - tpp[CELL(i, jp)]) * g.invdphi);
+            if (ph.stabilize == 1) dVp = stabilized(dVp, dt, corr_phi[c]);
             vaz[c] += dVp;
         }
         if (i >= 2 && i < nr - 1) {
             const double sigma_avg = 0.5 * (S[c] + S[CELL(i - 1, j)]);
-            const double dVr =
+            double dVr =
                 fast_div(dt, sigma_avg) * ph.rvf * t.TwoOverRmedSum[i] *
                 ((t.Rmed[i] * trr[c] - t.Rmed[i - 1] * trr[CELL(i - 1, j)]) * t.InvDiffRmed[i] +
                  (trp[CELL(i, jn)] - trp[c]) * g.invdphi - 0.5 * (tpp[c] + tpp[CELL(i - 1, j)]));
+            if (ph.stabilize == 1) dVr = stabilized(dVr, dt, corr_r[c]);
             vr[c] += dVr;
         }
     }
@@ -972,6 +1061,8 @@ __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const 
                               const double *__restrict__ qminus, double *__restrict__ cs,
                               double *__restrict__ H, double *__restrict__ P,
                               double *__restrict__ T, double *__restrict__ nu,
+                              const double *__restrict__ corr_phi,
+                              const double *__restrict__ corr_r,
                               unsigned long long *__restrict__ dt_min)
 {
     __shared__ double red[33];
@@ -1067,9 +1158,18 @@ __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const 
                 invdt5 *= 0.6;
                 invdt6 *= 0.6;
             }
-            const double dt_cell =
+            double dt_cell =
                 fast_div(ph.cfl, sqrt(invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 +
                                       invdt4 * invdt4 + invdt5 * invdt5 + invdt6 * invdt6));
+            if (ph.stabilize == 2) {
+                // viscous stability limit, cfl.cpp:332-351
+                const double cphi = corr_phi[c], cr = corr_r[c];
+                const double cc = cr < cphi ? cr : cphi;
+                if (cc != 0.0) {
+                    const double dt_stable = -fast_div(ph.cfl, cc);
+                    if (dt_stable < dt_cell) dt_cell = dt_stable;
+                }
+            }
             // positive doubles order like their bit patterns
             if (dbits(dt_cell) < dbits(local)) local = dt_cell;
         }
@@ -1196,7 +1296,13 @@ void launch_viscous(const Launch &L, double dt, double beta_inv, int mode, const
 {
     k_viscous<<<grid2d(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(
         L.g, L.t, L.ph, dt, beta_inv, mode, s.sigma, s.trr, s.tpp, s.trp, s.divv, s.nu, s.H,
-        s.sigma0, s.energy0, s.vr, s.vaz, s.energy, s.qplus, s.qminus);
+        s.sigma0, s.energy0, s.vr, s.vaz, s.energy, s.qplus, s.qminus, s.corr_phi, s.corr_r);
+}
+
+void launch_visc_corr(const Launch &L, const State &s)
+{
+    k_visc_corr<<<grid2d(L.g.nz, L.g.nr - 1, L.bx), L.bx, 0, L.stream>>>(L.g, L.t, s.sigma, s.nu,
+                                                                          s.corr_phi, s.corr_r);
 }
 
 void launch_ghost(const Launch &L, const BcSpec &bc, double omf, const State &s)
@@ -1305,7 +1411,8 @@ void launch_derived_cfl(const Launch &L, int mode, const State &s, unsigned long
 {
     k_derived_cfl<<<L.g.nr, 256, 0, L.stream>>>(L.g, L.t, L.ph, mode, L.ph.art_visc_sn, s.sigma,
                                                 s.energy, s.vr, s.vaz, s.qplus, s.qminus, s.cs,
-                                                s.H, s.P, s.T, s.nu, dt_min);
+                                                s.H, s.P, s.T, s.nu, s.corr_phi, s.corr_r,
+                                                dt_min);
 }
 
 void launch_disk_force(const Launch &L, double px, double py, double pa, double rsm,

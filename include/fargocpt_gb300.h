@@ -122,7 +122,11 @@ typedef struct fgpu_params {
     int precision;          /* FGPU_PRECISION_* */
     int integrator;         /* FGPU_INTEGRATOR_* (Interpret.cpp:174-185); LeapFrog
                                scales three CFL limits by 0.6 (cfl.cpp:254-317) */
-    int reserved_i[6];
+    int stabilize_viscosity; /* StabilizeViscosity (Interpret.cpp:669-681): 0 off,
+                               1 pseudo-implicit viscous update, 2 viscous dt limit
+                               (viscosity.cpp:256-348, 395-417; cfl.cpp:332-351);
+                               FP64 only */
+    int reserved_i[5];
 
     double gamma;           /* AdiabaticIndex */
     double mu;              /* mean molecular weight */

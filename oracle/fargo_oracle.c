@@ -48,6 +48,12 @@ struct or_state {
 
     double *sigma1d;
 
+    /* StabilizeViscosity (viscosity.cpp:256-348): nu*Sigma at cell centres
+       and at the r-phi corners, and the correction factors; cleared at
+       creation like every t_polargrid (polargrid.cpp:51-64) */
+    double *visc_sigma, *visc_sigma_rp, *corr_phi, *corr_r;
+    double *FourThirdInvRbInvdphiSq;
+
     int nb;
     fgpu_body b[MAX_BODIES];
     double ix, iy, omega_frame;
@@ -250,6 +256,15 @@ int or_create(const fgpu_params *p, const double *radii, or_state **out)
     s->nshift = calloc((size_t)nr, sizeof(int));
     s->nosplit = calloc((size_t)nr, sizeof(int));
     s->sigma1d = calloc((size_t)nr, sizeof(double));
+    s->visc_sigma = calloc(cells, sizeof(double));
+    s->visc_sigma_rp = calloc(vcells, sizeof(double));
+    s->corr_phi = calloc(cells, sizeof(double));
+    s->corr_r = calloc(cells, sizeof(double));
+    /* init.cpp:213-214 */
+    s->FourThirdInvRbInvdphiSq = calloc((size_t)R, sizeof(double));
+    for (int n = 0; n <= nr; ++n) {
+	s->FourThirdInvRbInvdphiSq[n] = 4.0 / 3.0 / s->Rmed[n] * s->invdphi * s->invdphi;
+    }
     setup_damping(s);
     *out = s;
     return FGPU_OK;
@@ -263,7 +278,9 @@ void or_destroy(or_state *s)
 		      s->InvDiffRsupRb, s->TwoDiffRaSq, s->InvRinf, s->cosj,
 		      s->sinj, s->rmp, s->rmm, s->amp, s->amm, s->vres,
 		      s->vmean, s->work, s->qrstar, s->densstar, s->tempshift,
-		      s->dq, s->density_int, s->sigma1d};
+		      s->dq, s->density_int, s->sigma1d, s->visc_sigma,
+		      s->visc_sigma_rp, s->corr_phi, s->corr_r,
+		      s->FourThirdInvRbInvdphiSq};
     for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i) free(ptrs[i]);
     for (int f = 0; f < FGPU_FIELD_COUNT; ++f) free(s->f[f]);
     free(s->nshift);
@@ -605,6 +622,67 @@ void or_update_with_sourceterms(or_state *s, double dt)
     }
 }
 
+/* update_with_artificial_viscosity_TW, artificial_viscosity.cpp:35-140:
+   tensor artificial viscosity of Tscharnuter & Winkler with only the
+   diagonal elements, its dissipation, then the velocity updates */
+static void artificial_viscosity_tw(or_state *s, double dt)
+{
+    const int nr = s->nr, nz = s->nz;
+    double *E = F(s, FGPU_ENERGY), *S = F(s, FGPU_SIGMA), *vr = F(s, FGPU_V_RADIAL),
+	   *vaz = F(s, FGPU_V_AZIMUTHAL), *Qrr = F(s, FGPU_Q_R), *Qpp = F(s, FGPU_Q_PHI);
+    const int dissipate = adiabatic(s) && s->p.art_visc_dissipation;
+#pragma omp parallel for
+    for (int i = 0; i < nr; ++i) {
+	for (int j = 0; j < nz; ++j) {
+	    const int jn = j == nz - 1 ? 0 : j + 1;
+	    const double eps_rr = (AT(vr, i + 1, j) - AT(vr, i, j)) * s->InvDiffRsup[i];
+	    const double eps_pp =
+		s->InvRmed[i] * ((AT(vaz, i, jn) - AT(vaz, i, j)) * s->invdphi +
+				 0.5 * (AT(vr, i + 1, j) + AT(vr, i, j)));
+	    const double sum = eps_rr + eps_pp;
+	    const double div_V = sum < 0.0 ? sum : 0.0;
+	    const double Dr = s->Rinf[i + 1] - s->Rinf[i];
+	    const double rDphi = s->Rmed[i] * s->dphi;
+	    double dx_sq;
+	    if (nz <= 16) {
+		dx_sq = pow(Dr < rDphi ? Dr : rDphi, 2);
+	    } else {
+		dx_sq = pow(Dr > rDphi ? Dr : rDphi, 2);
+	    }
+	    const double l_sq = pow(s->p.art_visc_factor, 2) * dx_sq;
+	    AT(Qrr, i, j) = l_sq * AT(S, i, j) * -div_V * (eps_rr - 1.0 / 3.0 * div_V);
+	    AT(Qpp, i, j) = l_sq * AT(S, i, j) * -div_V * (eps_pp - 1.0 / 3.0 * div_V);
+	    if (dissipate && i > 0 && i < nr - 1) {
+		const double Qplus = -l_sq * div_V * AT(S, i, j) * 1.0 / 3.0 *
+				     (pow(eps_rr, 2) + pow(eps_pp, 2) + pow((eps_rr - eps_pp), 2));
+		AT(E, i, j) += Qplus * dt;
+	    }
+	}
+    }
+#pragma omp parallel for
+    for (int i = 1; i < nr - 1; ++i) {
+	for (int j = 0; j < nz; ++j) {
+	    const int jp = j == 0 ? nz - 1 : j - 1;
+	    const double sigma_phi_avg = 0.5 * (AT(S, i, j) + AT(S, i, jp));
+	    const double dVp = 2.0 * dt / ((s->Rsup[i] + s->Rinf[i]) * sigma_phi_avg) *
+			       (AT(Qpp, i, j) - AT(Qpp, i, jp)) * s->invdphi;
+	    AT(vaz, i, j) += dVp;
+	}
+    }
+#pragma omp parallel for
+    for (int i = 2; i < nr - 1; ++i) {
+	for (int j = 0; j < nz; ++j) {
+	    const double sigma_r_avg = 0.5 * (AT(S, i, j) + AT(S, i - 1, j));
+	    const double dVr =
+		s->p.radial_viscosity_factor * dt / sigma_r_avg * 2.0 /
+		(pow(s->Rmed[i], 2) - pow(s->Rmed[i - 1], 2)) *
+		((AT(Qrr, i, j) * s->Rmed[i] - AT(Qrr, i - 1, j) * s->Rmed[i - 1]) -
+		 0.5 * (AT(Qpp, i, j) + AT(Qpp, i - 1, j)) * (s->Rmed[i] - s->Rmed[i - 1]));
+	    AT(vr, i, j) += dVr;
+	}
+    }
+}
+
 /* ------------------------------------------------------------------ */
 /* art_visc::update_with_artificial_viscosity(_SN),                     */
 /* src/viscosity/artificial_viscosity.cpp:11-28, 148-250                */
@@ -660,6 +738,9 @@ void or_artificial_viscosity(or_state *s, double dt)
 	    }
 	}
     }
+    if (s->p.art_visc == FGPU_ARTVISC_TW) {
+	artificial_viscosity_tw(s, dt);
+    }
     if (adiabatic(s) && s->p.art_visc_dissipation) {
 	assure_temperature_range(s);
     }
@@ -674,6 +755,55 @@ void or_recalculate_viscosity(or_state *s, double t)
 	compute_scale_height(s);
     }
     update_viscosity(s);
+}
+
+/* The pseudo-implicit correction factors of StabilizeViscosity,
+   viscosity.cpp:256-348: c_phi at v_phi and c_r at v_r positions, rows
+   1 .. Nrad-1 */
+static void viscosity_correction_factors(or_state *s)
+{
+    const int nr = s->nr, nz = s->nz;
+    const double *S = F(s, FGPU_SIGMA);
+    const double *NS = s->visc_sigma, *NSrp = s->visc_sigma_rp;
+    const double *Ra = s->Rinf;
+#pragma omp parallel for
+    for (int i = 1; i < nr; ++i) {
+	for (int j = 0; j < nz; ++j) {
+	    const int jp = j == 0 ? nz - 1 : j - 1;
+	    const int jn = j == nz - 1 ? 0 : j + 1;
+	    const double NuSig_rp = AT(NSrp, i, j);
+	    const double NuSig_rp_ip = AT(NSrp, i + 1, j);
+	    const double NuSig_rp_jp = AT(NSrp, i, jn);
+	    const double NuSigma = AT(NS, i, j);
+	    const double NuSigma_jm = AT(NS, i, jp);
+	    const double NuSigma_im = AT(NS, i - 1, j);
+
+	    const double a3 = NuSig_rp * pow(Ra[i], 3) * s->InvDiffRmed[i];
+	    const double a3p = NuSig_rp_ip * pow(Ra[i + 1], 3) * s->InvDiffRmed[i + 1];
+	    const double cphi_rp = -s->InvRmed[i] * s->TwoDiffRaSq[i] * (a3p + a3);
+	    const double cphi_pp = -s->FourThirdInvRbInvdphiSq[i] * (NuSigma + NuSigma_jm);
+	    const double sigma_avg_phi = 0.5 * (AT(S, i, j) + AT(S, i, jp));
+	    AT(s->corr_phi, i, j) = (cphi_rp + cphi_pp) / (sigma_avg_phi * s->Rmed[i]);
+
+	    const double sigma_avg_r = 0.5 * (AT(S, i, j) + AT(S, i - 1, j));
+	    const double cr_rp = -(NuSig_rp_jp + NuSig_rp) / (s->dphi * s->dphi * Ra[i]);
+	    const double cr_pp_1 = 2.0 * NuSigma *
+				   (0.5 * s->InvRmed[i] + 1.0 / 3.0 * Ra[i] * s->InvDiffRsupRb[i]);
+	    const double cr_pp_2 =
+		2.0 * NuSigma_im *
+		(0.5 * s->InvRmed[i - 1] - 1.0 / 3.0 * Ra[i] * s->InvDiffRsupRb[i - 1]);
+	    const double cr_rr_1 = s->Rmed[i] * 2.0 * NuSigma *
+				   (-s->InvDiffRsup[i] + 1.0 / 3.0 * Ra[i] * s->InvDiffRsupRb[i]);
+	    const double cr_rr_2 =
+		-1.0 * s->Rmed[i - 1] * 2.0 * NuSigma_im *
+		(s->InvDiffRsup[i - 1] - 1.0 / 3.0 * Ra[i] * s->InvDiffRsupRb[i - 1]);
+	    const double cr_pp = -0.5 * (cr_pp_1 + cr_pp_2);
+	    const double cr_rr = s->InvDiffRmed[i] * (cr_rr_1 + cr_rr_2);
+	    const double Rmed_mid = 0.5 * (s->Rmed[i] + s->Rmed[i - 1]);
+	    AT(s->corr_r, i, j) = s->p.radial_viscosity_factor * (cr_rr + cr_rp + cr_pp) /
+				  (sigma_avg_r * Rmed_mid);
+	}
+    }
 }
 
 /* viscosity::compute_viscous_stress_tensor, src/viscosity/viscosity.cpp:139-254 */
@@ -706,6 +836,7 @@ void or_viscous_stress_tensor(or_state *s)
 		0.5 * (AT(vr, i + 1, j) + AT(vr, i, j)) * s->InvRmed[i];
 	    const double n = AT(nu, i, j), sg = AT(S, i, j);
 	    AT(Tpp, i, j) = 2.0 * n * sg * (dpp - 1.0 / 3.0 * AT(dv, i, j));
+	    AT(s->visc_sigma, i, j) = n * sg;
 	}
     }
 #pragma omp parallel for
@@ -722,7 +853,11 @@ void or_viscous_stress_tensor(or_state *s)
 	    const double sg = 0.25 * (AT(S, i, j) + AT(S, i - 1, j) + AT(S, i, jp) +
 				      AT(S, i - 1, jp));
 	    AT(Trp, i, j) = n * sg * drp;
+	    AT(s->visc_sigma_rp, i, j) = n * sg;
 	}
+    }
+    if (s->p.stabilize_viscosity) {
+	viscosity_correction_factors(s);
     }
 }
 
@@ -738,12 +873,17 @@ void or_update_velocities_with_viscosity(or_state *s, double dt)
 	for (int j = 0; j < nz; ++j) {
 	    const int jp = j == 0 ? nz - 1 : j - 1;
 	    const double sigma_avg = 0.5 * (AT(S, i, j) + AT(S, i, jp));
-	    const double dVp =
+	    double dVp =
 		dt * s->InvRmed[i] / (sigma_avg) *
 		((2.0 / (pow(s->Rinf[i + 1], 2) - pow(s->Rinf[i], 2))) *
 		     (pow(s->Rinf[i + 1], 2) * AT(Trp, i + 1, j) -
 		      pow(s->Rinf[i], 2) * AT(Trp, i, j)) +
 		 (AT(Tpp, i, j) - AT(Tpp, i, jp)) * s->invdphi);
+	    if (s->p.stabilize_viscosity == 1) {
+		const double cphi = AT(s->corr_phi, i, j);
+		const double a = 1.0 + dt * cphi;
+		dVp *= 1.0 / ((a > 0.0 ? a : 0.0) - dt * cphi);
+	    }
 	    AT(vaz, i, j) += dVp;
 	}
     }
@@ -752,13 +892,18 @@ void or_update_velocities_with_viscosity(or_state *s, double dt)
 	for (int j = 0; j < nz; ++j) {
 	    const int jn = j == nz - 1 ? 0 : j + 1;
 	    const double sigma_avg = 0.5 * (AT(S, i, j) + AT(S, i - 1, j));
-	    const double dVr =
+	    double dVr =
 		dt / (sigma_avg)*s->p.radial_viscosity_factor * 2.0 /
 		(s->Rmed[i] + s->Rmed[i - 1]) *
 		((s->Rmed[i] * AT(Trr, i, j) - s->Rmed[i - 1] * AT(Trr, i - 1, j)) *
 		     s->InvDiffRmed[i] +
 		 (AT(Trp, i, jn) - AT(Trp, i, j)) * s->invdphi -
 		 0.5 * (AT(Tpp, i, j) + AT(Tpp, i - 1, j)));
+	    if (s->p.stabilize_viscosity == 1) {
+		const double cr = AT(s->corr_r, i, j);
+		const double a = 1.0 + dt * cr;
+		dVr *= 1.0 / ((a > 0.0 ? a : 0.0) - dt * cr);
+	    }
 	    AT(vr, i, j) += dVr;
 	}
     }
@@ -1323,9 +1468,18 @@ double or_condition_cfl(or_state *s)
 		const double inv_limit = 1.0 / p->heating_cooling_cfl_limit;
 		invdt6 = inv_limit * fabs((AT(Qp, i, j) - AT(Qm, i, j)) / AT(E, i, j)) * lf;
 	    }
-	    const double dt_cell =
+	    double dt_cell =
 		p->cfl / sqrt(pow(invdt1, 2) + pow(invdt2, 2) + pow(invdt3, 2) +
 			      pow(invdt4, 2) + pow(invdt5, 2) + pow(invdt6, 2));
+	    if (p->stabilize_viscosity == 2) {
+		/* cfl.cpp:332-351 */
+		const double cphi = AT(s->corr_phi, i, j), cr = AT(s->corr_r, i, j);
+		const double c = cphi < cr ? cphi : cr;
+		if (c != 0.0) {
+		    const double dt_stable = -p->cfl / c;
+		    if (dt_stable < dt_cell) dt_cell = dt_stable;
+		}
+	    }
 	    if (dt_cell < dt_core) dt_core = dt_cell;
 	}
     }

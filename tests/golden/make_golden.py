@@ -137,6 +137,55 @@ CASES = {
                   DampingEnergyInner="Reference", DampingEnergyOuter="Reference",
                   MonitorTimestep=0.4, Nsnapshots=4, Integrator="LeapFrog"),
         nrad=16, naz=40, rmin=0.3, rmax=3.0, planet=None, keep=[1, 2, 3, 4]),
+    # Tscharnuter-Winkler artificial viscosity, adiabatic, planet, fixed dt
+    "adi_planet_tw": dict(
+        keys=dict(SigmaSlope=1.0, AspectRatio=0.05, FlaringIndex=0.25,
+                  EquationOfState="Ideal", AdiabaticIndex=1.4, ViscousAlpha=3e-2,
+                  ArtificialViscosity="TW", ArtificialViscosityFactor=1.41421356,
+                  CoolingBetaLocal="yes", CoolingBeta=10,
+                  Transport="FARGO",
+                  InnerBoundary="zerogradient", OuterBoundary="outflow",
+                  Damping="yes", DampingInnerLimit=1.15, DampingOuterLimit=0.85,
+                  DampingTimeFactor=0.5,
+                  DampingSurfaceDensityInner="Reference",
+                  DampingSurfaceDensityOuter="Reference",
+                  DampingVRadialInner="Reference", DampingVRadialOuter="Reference",
+                  DampingVAzimuthalInner="Reference",
+                  DampingVAzimuthalOuter="Reference",
+                  DampingEnergyInner="Reference", DampingEnergyOuter="Reference",
+                  MonitorTimestep=0.002, Nsnapshots=20),
+        nrad=20, naz=48, rmin=0.3, rmax=3.0, planet=1e-3, keep=[1, 2, 5, 10, 20]),
+    # TW with the pseudo-implicit viscous update (StabilizeViscosity 1):
+    # viscosity-dominated CFL at CFL 1.3, so that dt |c| exceeds 1 in cells
+    # and the correction acts; adiabatic, star only
+    "adi_star_cfl_tw_stab1": dict(
+        keys=dict(SigmaSlope=1.0, AspectRatio=0.05, FlaringIndex=0.25,
+                  EquationOfState="Ideal", AdiabaticIndex=1.4, ConstantViscosity=1e-2,
+                  ArtificialViscosity="TW", StabilizeViscosity=1, CFL=1.3,
+                  CoolingBetaLocal="yes", CoolingBeta=10, Transport="FARGO",
+                  InnerBoundary="zerogradient", OuterBoundary="zerogradient",
+                  Damping="yes", DampingInnerLimit=1.1, DampingOuterLimit=0.9,
+                  DampingSurfaceDensityInner="Reference",
+                  DampingSurfaceDensityOuter="Reference",
+                  DampingVRadialInner="Reference", DampingVRadialOuter="Reference",
+                  DampingVAzimuthalInner="Reference", DampingVAzimuthalOuter="Reference",
+                  DampingEnergyInner="Reference", DampingEnergyOuter="Reference",
+                  MonitorTimestep=0.3, Nsnapshots=3),
+        nrad=16, naz=40, rmin=0.4, rmax=2.5, planet=None, keep=[1, 2, 3]),
+    # TW with the viscous stability dt limit (StabilizeViscosity 2), locally
+    # isothermal, a viscosity-dominated CFL so that the limit binds
+    "iso_star_cfl_tw_stab2": dict(
+        keys=dict(SigmaSlope=0.5, AspectRatio=0.05, FlaringIndex=0.0,
+                  EquationOfState="Isothermal", ConstantViscosity=1e-2,
+                  ArtificialViscosity="TW", StabilizeViscosity=2, Transport="FARGO",
+                  InnerBoundary="zerogradient", OuterBoundary="zerogradient",
+                  Damping="yes", DampingInnerLimit=1.1, DampingOuterLimit=0.9,
+                  DampingSurfaceDensityInner="Reference",
+                  DampingSurfaceDensityOuter="Reference",
+                  DampingVRadialInner="Reference", DampingVRadialOuter="Reference",
+                  DampingVAzimuthalInner="Reference", DampingVAzimuthalOuter="Reference",
+                  MonitorTimestep=0.05, Nsnapshots=4),
+        nrad=16, naz=40, rmin=0.4, rmax=2.5, planet=None, keep=[1, 2, 3, 4]),
 }
 
 
@@ -186,7 +235,8 @@ def engine_params(case, consts, temp_unit):
 
     return dict(
         nrad=case["nrad"], naz=case["naz"], eos=1 if adi else 0,
-        art_visc=1 if k.get("ArtificialViscosity", "SN").upper() == "SN" else 0,
+        art_visc={"s": 1, "t": 2, "n": 0}[str(k.get("ArtificialViscosity", "SN")).lower()[0]],
+        stabilize_viscosity=int(k.get("StabilizeViscosity", 0)),
         art_visc_dissipation=1, flux_limiter=1 if k.get("FluxLimiter", "") == "mc" else 0,
         fast_transport=1 if k["Transport"].lower().startswith("f") else 0,
         heating_viscous=1, cooling_beta=1 if k.get("CoolingBetaLocal") == "yes" else 0,
@@ -204,7 +254,8 @@ def engine_params(case, consts, temp_unit):
         integrator=1 if str(k.get("Integrator", "Euler")).lower().startswith("l") else 0,
         gamma=float(k.get("AdiabaticIndex", 1.4)), mu=float(k["mu"]),
         aspect_ratio=float(k["AspectRatio"]), flaring_index=float(k["FlaringIndex"]),
-        viscous_alpha=float(k["ViscousAlpha"]), constant_viscosity=0.0,
+        viscous_alpha=float(k.get("ViscousAlpha", 0.0)),
+        constant_viscosity=float(k.get("ConstantViscosity", 0.0)),
         art_visc_factor=float(k.get("ArtificialViscosityFactor", 1.41)),
         radial_viscosity_factor=1.0, heating_viscous_factor=1.0,
         cfl=float(k["CFL"]), cfl_max_var=1.1, heating_cooling_cfl_limit=10.0,

@@ -17,7 +17,8 @@ from fargocpt_gb300.simulation import RunClock, advance, indirect_term_euler, st
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = ["iso_planet_fixed_dt", "adi_planet_fixed_dt", "iso_star_cfl",
-         "adi_star_cfl_mc_std", "iso_star_cfl_leapfrog", "adi_star_cfl_leapfrog"]
+         "adi_star_cfl_mc_std", "iso_star_cfl_leapfrog", "adi_star_cfl_leapfrog",
+         "adi_planet_tw", "adi_star_cfl_tw_stab1", "iso_star_cfl_tw_stab2"]
 EVOLVED = ["SIGMA", "V_RADIAL", "V_AZIMUTHAL", "ENERGY"]
 
 

@@ -14,7 +14,7 @@ import math
 import numpy as np
 import pytest
 
-from golden_runner import CASES, EVOLVED, replay, rel_linf
+from golden_runner import CASES, EVOLVED, load_case, replay, rel_linf
 
 pytestmark = pytest.mark.gpu
 
@@ -28,7 +28,13 @@ def rel_l1(a, b):
     return float(np.sum(np.abs(a - b)) / np.sum(np.abs(b)))
 
 
-@pytest.mark.parametrize("name", CASES)
+def _fp32_case(name):
+    # TW artificial viscosity and StabilizeViscosity run in the FP64 form only
+    params = load_case(name)[0]["params"]
+    return params.get("art_visc") != 2 and not params.get("stabilize_viscosity")
+
+
+@pytest.mark.parametrize("name", [c for c in CASES if _fp32_case(c)])
 def test_fp32_mixed_against_reference_snapshots(name):
     snaps, times, torques, dts, arrays = replay(_engine(), name, {"precision": 1})
     assert snaps

@@ -110,3 +110,20 @@ def test_leapfrog_with_moving_planet(adiabatic):
     for f in EVOLVED:
         err = rel_linf(hyd[1].get_field(f), hyd[0].get_field(f))
         assert err <= TOL, f"{f}: {err:.3e}"
+
+
+@pytest.mark.parametrize("adiabatic,stabilize", [(True, 0), (True, 1), (False, 2)])
+def test_tw_artificial_viscosity_and_stabilize(adiabatic, stabilize):
+    """Tscharnuter-Winkler artificial viscosity (artificial_viscosity.cpp:35-140)
+    and StabilizeViscosity (viscosity.cpp:256-348, 395-417; cfl.cpp:332-351)
+    with a constant viscosity that dominates the CFL, at CFL 1.3 so that the
+    pseudo-implicit correction acts (dt |c| > 1 in cells) and the viscous dt
+    limit binds."""
+    params, d = make_params(48, 128, adiabatic=adiabatic, art_visc=2,
+                            stabilize_viscosity=stabilize, viscous_alpha=0.0,
+                            constant_viscosity=3e-3, cfl=1.3 if stabilize == 1 else 0.5)
+    (o, dto), (g, dtg) = run_both(params, d, steps=10)
+    np.testing.assert_allclose(dtg, dto, rtol=1e-12)
+    for f in EVOLVED:
+        err = rel_linf(g.get_field(f), o.get_field(f))
+        assert err <= TOL, f"{f}: {err:.3e}"
