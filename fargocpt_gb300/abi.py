@@ -35,7 +35,9 @@ FIELDS = {
 }
 VECTOR_FIELDS = {"V_RADIAL", "V_RADIAL0", "TAU_R_PHI"}
 
-BC = {"none": 0, "zerogradient": 1, "outflow": 2, "reference": 3, "keplerian": 4}
+BC = {"none": 0, "zerogradient": 1, "outflow": 2, "reference": 3, "keplerian": 4,
+      "diskmodel": 5, "reflecting": 6, "viscous": 7, "keplerian_radial": 8, "zeroshear": 9,
+      "balanced": 10}
 DAMP = {"none": 0, "reference": 1, "zero": 2, "mean": 3}
 EOS_ISOTHERMAL, EOS_IDEAL = 0, 1
 SPACING_ARITHMETIC, SPACING_LOGARITHMIC = 0, 1
@@ -58,7 +60,8 @@ class FgpuParams(C.Structure):
         ("bc_vrad_inner", C.c_int), ("bc_vrad_outer", C.c_int),
         ("bc_vaz_inner", C.c_int), ("bc_vaz_outer", C.c_int),
         ("precision", C.c_int), ("integrator", C.c_int),
-        ("stabilize_viscosity", C.c_int), ("reserved_i", C.c_int * 5),
+        ("stabilize_viscosity", C.c_int), ("profile_cutoff_outer", C.c_int),
+        ("viscous_accretion", C.c_int), ("reserved_i", C.c_int * 3),
         ("gamma", C.c_double), ("mu", C.c_double), ("aspect_ratio", C.c_double),
         ("flaring_index", C.c_double), ("viscous_alpha", C.c_double),
         ("constant_viscosity", C.c_double), ("art_visc_factor", C.c_double),
@@ -78,13 +81,27 @@ class FgpuParams(C.Structure):
         ("vaz_outer_keplerian_factor", C.c_double),
         ("rmin", C.c_double), ("rmax", C.c_double),
         ("radial_spacing", C.c_int), ("reserved_j", C.c_int),
-        ("reserved_d", C.c_double * 8),
+        ("accretion_radius_fraction", C.c_double), ("sigma_slope", C.c_double),
+        ("viscous_outflow_speed", C.c_double), ("vrad_inner_keplerian_factor", C.c_double),
+        ("vrad_outer_keplerian_factor", C.c_double), ("binary_quadrupole_moment", C.c_double),
+        ("reserved_d", C.c_double * 2),
     ]
 
 
 class FgpuBody(C.Structure):
     _fields_ = [("x", C.c_double), ("y", C.c_double), ("mass", C.c_double),
                 ("r_sm", C.c_double), ("a", C.c_double)]
+
+
+ACCRETION = {"kley": 0, "viscous": 1, "sinkhole": 2}
+
+
+class FgpuAccretor(C.Structure):
+    """fgpu_accretor: one accreting planet (accretion.cpp:84-480)."""
+    _fields_ = [("type", C.c_int), ("reserved", C.c_int), ("x", C.c_double),
+                ("y", C.c_double), ("r", C.c_double), ("phi", C.c_double),
+                ("roche_radius", C.c_double), ("efficiency", C.c_double),
+                ("orbital_period", C.c_double)]
 
 
 def params_from_dict(d: dict) -> FgpuParams:
@@ -150,7 +167,8 @@ EXPORTED_SYMBOLS = [
     "fgpu_get_stream", "fgpu_upload_field", "fgpu_download_field",
     "fgpu_set_bodies", "fgpu_init_euler", "fgpu_recalculate_derived",
     "fgpu_condition_cfl", "fgpu_apply_boundary_condition", "fgpu_step_euler",
-    "fgpu_disk_on_planet_accel", "fgpu_total_mass", "fgpu_check_finite",
+    "fgpu_disk_on_planet_accel", "fgpu_total_mass", "fgpu_accrete_onto_planet",
+    "fgpu_check_finite",
     "fgpu_synchronize", "fgpu_set_phase_timing", "fgpu_phase_times", "fgpu_phase_name",
     "fgpu_disk_force_static", "fgpu_gas_kick", "fgpu_transport", "fgpu_compute_pressure",
     "fgpu_snapshot_begin", "fgpu_snapshot_wait", "fgpu_host_alloc", "fgpu_host_free",
@@ -181,6 +199,7 @@ def _declare(lib: C.CDLL) -> C.CDLL:
         "fgpu_step_euler": ([vp, C.c_double, C.c_double], C.c_int),
         "fgpu_disk_on_planet_accel": ([vp, C.c_int, dp], C.c_int),
         "fgpu_total_mass": ([vp, dp], C.c_int),
+        "fgpu_accrete_onto_planet": ([vp, C.POINTER(FgpuAccretor), C.c_double, dp], C.c_int),
         "fgpu_check_finite": ([vp, P(C.c_int), P(C.c_int), P(C.c_int)], C.c_int),
         "fgpu_synchronize": ([vp], C.c_int),
         "fgpu_set_phase_timing": ([vp, C.c_int], C.c_int),

@@ -187,6 +187,8 @@ static double omega_kepler(const fgpu_params &p, double r)
     return std::sqrt(p.G * p.hydro_center_mass / (r * r * r));  // Theo.cpp:246-249
 }
 
+static bool hook_allowed(int field, int kind, bool outer);
+
 static int validate(const fgpu_params *p, std::string &why)
 {
     if (p->nrad < 6 || p->naz < 8) { why = "nrad >= 6 and naz >= 8 required"; return FGPU_ERR_BAD_ARG; }
@@ -204,7 +206,14 @@ static int validate(const fgpu_params *p, std::string &why)
     const int bcs[8] = {p->bc_sigma_inner, p->bc_sigma_outer, p->bc_energy_inner, p->bc_energy_outer,
                         p->bc_vrad_inner, p->bc_vrad_outer, p->bc_vaz_inner, p->bc_vaz_outer};
     for (int k = 0; k < 8; ++k) {
-        if (bcs[k] < FGPU_BC_NONE || bcs[k] > FGPU_BC_KEPLERIAN) { why = "boundary kind"; return FGPU_ERR_BAD_ARG; }
+        if (bcs[k] < FGPU_BC_NONE || bcs[k] > FGPU_BC_BALANCED) { why = "boundary kind"; return FGPU_ERR_BAD_ARG; }
+        if (!hook_allowed(k / 2, bcs[k], k % 2 == 1)) {
+            why = bcs[k] == FGPU_BC_VISCOUS
+                      ? "the viscous v_radial hook exists at the inner edge only (the reference's "
+                        "outer version reads past the viscosity grid)"
+                      : "boundary kind not available for this field";
+            return bcs[k] == FGPU_BC_VISCOUS ? FGPU_ERR_UNSUPPORTED : FGPU_ERR_BAD_ARG;
+        }
     }
     for (int q = 0; q < 4; ++q) {
         if (p->damping_inner[q] < 0 || p->damping_inner[q] > FGPU_DAMP_MEAN ||
@@ -214,6 +223,102 @@ static int validate(const fgpu_params *p, std::string &why)
     }
     if (!(p->cfl > 0) || !(p->G > 0) || !(p->hydro_center_mass > 0)) { why = "cfl, G, mass must be > 0"; return FGPU_ERR_BAD_ARG; }
     return FGPU_OK;
+}
+
+// compute_v_kepler, Theo.cpp:207-211
+static double v_kepler(const fgpu_params &p, double r)
+{
+    return std::sqrt(p.G * p.hydro_center_mass / r);
+}
+
+// The constants of every boundary hook (see BcSpec), with the reference's
+// expressions: keplerian_azimuthal.cpp:27-31, diskmodel.cpp:18-31,
+// viscous.cpp:33-35, keplerian_radial.cpp:31-33 and 55-57, zero_shear.cpp:28-32,
+// balanced.cpp:20-66 with support_azi_* (Theo.cpp:131-157).
+namespace fgpu32 {
+void boundary_values(const fgpu_params &p, const double *Rmed, const double *Rinf, int nr,
+                     double vin[4][2], double vout[4][2])
+{
+    for (int f = 0; f < 4; ++f) vin[f][0] = vin[f][1] = vout[f][0] = vout[f][1] = 0.0;
+    const double sigexp = -p.sigma_slope;
+    auto calc_sig = [&](double R) { return p.sigma0 * std::pow(R, sigexp); };
+    auto calc_eng = [&](double R) {
+        return 1.0 / (p.gamma - 1.0) * p.sigma0 * std::pow(p.aspect_ratio, 2) *
+               std::pow(R, sigexp - 1.0 + 2.0 * p.flaring_index);
+    };
+    auto balanced = [&](double R) {
+        const double vk_2 = std::pow(v_kepler(p, R), 2);
+        double support = 0.0;
+        if (!p.profile_cutoff_outer) {
+            const double F = p.flaring_index, S = p.sigma_slope;
+            const double h = p.aspect_ratio * std::pow(R, F);
+            support += (2.0 * F - 1.0 - S) * std::pow(h, 2);
+            const double eps = p.thickness_smoothing;
+            support += (1.0 + (F + 1.0) * std::pow(h * eps, 2)) /
+                       std::pow(std::sqrt(1 + std::pow(h * eps, 2)), 3);
+        }
+        if (p.binary_quadrupole_moment > 0.0) {
+            support += 3.0 * p.binary_quadrupole_moment / std::pow(R, 2);
+        }
+        return std::sqrt(vk_2 * support);
+    };
+    const int kinds_in[4] = {p.bc_sigma_inner, p.bc_energy_inner, p.bc_vrad_inner, p.bc_vaz_inner};
+    const int kinds_out[4] = {p.bc_sigma_outer, p.bc_energy_outer, p.bc_vrad_outer,
+                              p.bc_vaz_outer};
+    for (int f = 0; f < 4; ++f) {
+        for (int side = 0; side < 2; ++side) {
+            const int kind = side ? kinds_out[f] : kinds_in[f];
+            double *v = side ? vout[f] : vin[f];
+            const bool vec = f == 2;
+            const int edge = side ? (vec ? nr : nr - 1) : 0;
+            const int next = side ? edge - 1 : 1;
+            switch (kind) {
+            case FGPU_BC_KEPLERIAN:
+                v[0] = (side ? p.vaz_outer_keplerian_factor : p.vaz_inner_keplerian_factor) *
+                       v_kepler(p, Rmed[edge]);
+                break;
+            case FGPU_BC_DISKMODEL:
+                v[0] = f == 0 ? calc_sig(Rmed[edge]) : calc_eng(Rmed[edge]);
+                break;
+            case FGPU_BC_VISCOUS:
+                v[0] = -1.5 * p.viscous_outflow_speed / Rinf[0];
+                v[1] = -1.5 * p.viscous_outflow_speed / Rinf[1];
+                break;
+            case FGPU_BC_KEPLERIAN_RADIAL: {
+                const double c = side ? p.vrad_outer_keplerian_factor : p.vrad_inner_keplerian_factor;
+                v[0] = c * v_kepler(p, Rmed[edge]);
+                v[1] = c * v_kepler(p, Rmed[next]);
+                break;
+            }
+            case FGPU_BC_ZEROSHEAR:
+                v[0] = Rmed[edge];
+                v[1] = Rmed[next];
+                break;
+            case FGPU_BC_BALANCED:
+                v[0] = balanced(Rmed[edge]);
+                break;
+            default:
+                break;
+            }
+        }
+    }
+}
+
+}  // namespace fgpu32
+using fgpu32::boundary_values;
+
+// Which hooks exist for which field (boundary_conditions/config.cpp:95-340).
+static bool hook_allowed(int field, int kind, bool outer)
+{
+    switch (kind) {
+    case FGPU_BC_NONE: case FGPU_BC_ZEROGRADIENT: case FGPU_BC_REFERENCE: return true;
+    case FGPU_BC_DISKMODEL: return field == 0 || field == 1;
+    case FGPU_BC_OUTFLOW: case FGPU_BC_REFLECTING: case FGPU_BC_KEPLERIAN_RADIAL:
+        return field == 2;
+    case FGPU_BC_VISCOUS: return field == 2 && !outer;
+    case FGPU_BC_KEPLERIAN: case FGPU_BC_ZEROSHEAR: case FGPU_BC_BALANCED: return field == 3;
+    default: return false;
+    }
 }
 
 static int setup_tables(fgpu_engine *eng, const double *radii)
@@ -320,9 +425,7 @@ static int setup_tables(fgpu_engine *eng, const double *radii)
     bc.energy_in = p.bc_energy_inner; bc.energy_out = p.bc_energy_outer;
     bc.vr_in = p.bc_vrad_inner; bc.vr_out = p.bc_vrad_outer;
     bc.vaz_in = p.bc_vaz_inner; bc.vaz_out = p.bc_vaz_outer;
-    bc.vk_in = std::sqrt(p.G * p.hydro_center_mass / T(RMED)[0]);        // Theo.cpp:207-211
-    bc.vk_out = std::sqrt(p.G * p.hydro_center_mass / T(RMED)[nr - 1]);
-    bc.kep_in = p.vaz_inner_keplerian_factor; bc.kep_out = p.vaz_outer_keplerian_factor;
+    boundary_values(p, T(RMED), T(RINF), nr, bc.val_in, bc.val_out);
 
     // damping (damping.cpp:311-752)
     std::vector<double> Rmed(T(RMED), T(RMED) + R);
@@ -852,6 +955,18 @@ extern "C" int fgpu_condition_cfl(fgpu_engine *eng, double *dt_out)
     return FGPU_OK;
 }
 
+// parameters::VISCOUS_ACCRETION (Interpret.cpp:704-707): with the viscous
+// v_radial hook or viscous accretion, c_s, H and nu of the transported state
+// before the final boundary call (simulation.cpp:232-242, 432-441); only the
+// ideal EOS changes them.
+static void viscous_recompute(fgpu_engine *eng, const Launch &L)
+{
+    const fgpu_params &p = eng->p;
+    if (eng->ph.adiabatic && (p.viscous_accretion || p.bc_vrad_inner == FGPU_BC_VISCOUS)) {
+        launch_derived_cfl(L, 1, state_of(eng), nullptr);
+    }
+}
+
 static void ghost(fgpu_engine *eng, const Launch &L)
 {
     launch_ghost(L, eng->bc, eng->bodies.omega_frame, state_of(eng));
@@ -863,6 +978,7 @@ extern "C" int fgpu_apply_boundary_condition(fgpu_engine *eng, double t, double 
     if (!eng) return FGPU_ERR_BAD_ARG;
     ROUTE32(eng->e32->boundary(dt, final != 0));
     Launch L = launch_of(eng);
+    if (final) viscous_recompute(eng, L);
     if (final && eng->p.damping) {
         launch_damping(L, eng->dm, dt, eng->damp_rings, eng->n_damp_rings, state_of(eng));
     }
@@ -939,6 +1055,7 @@ extern "C" int fgpu_step_euler(fgpu_engine *eng, double dt, double t)
     ghost(eng, L);
     mark(eng, 6);
     transport(eng, dt);
+    viscous_recompute(eng, L);
     State s = state_of(eng);
     // apply_boundary_condition(final = true) (simulation.cpp:244)
     if (eng->p.damping) {
@@ -1030,6 +1147,81 @@ extern "C" int fgpu_total_mass(fgpu_engine *eng, double *mass)
                        eng->stream));
     CK(cudaStreamSynchronize(eng->stream));
     *mass = eng->h_pinned[4];
+    return FGPU_OK;
+}
+
+// accretion::AccreteOntoPlanets for one planet (accretion.cpp:84-480): the
+// constants of the planet's kind and its region (hill_radial_index /
+// hill_azimuthal_index, :21-58, with get_rinf_id and get_med_azimuthal_id of
+// find_cell_id.cpp under NDEBUG) on the host, the cells on the device.
+extern "C" int fgpu_accrete_onto_planet(fgpu_engine *eng, const fgpu_accretor *a, double dt,
+                                        double out[3])
+{
+    if (!eng || !a || !out || !(dt >= 0.0)) return FGPU_ERR_BAD_ARG;
+    if (eng->e32) {
+        eng->err = "accretion runs in the FP64 form only";
+        return FGPU_ERR_UNSUPPORTED;
+    }
+    if (a->type != FGPU_ACCRETION_KLEY && a->type != FGPU_ACCRETION_VISCOUS &&
+        a->type != FGPU_ACCRETION_SINKHOLE) {
+        eng->err = "accretion type";
+        return FGPU_ERR_BAD_ARG;
+    }
+    if (!(a->orbital_period > 0.0) && a->type != FGPU_ACCRETION_VISCOUS) {
+        eng->err = "accretion needs the planet's orbital period";
+        return FGPU_ERR_BAD_ARG;
+    }
+    const fgpu_params &p = eng->p;
+    const int nr = eng->nr, ns = eng->nz;
+    AccretionSpec sp{};
+    sp.type = a->type;
+    sp.x = a->x;
+    sp.y = a->y;
+    sp.rhill = a->roche_radius;
+    sp.density_floor = p.sigma_floor * p.sigma0;
+    sp.omf = eng->bodies.omega_frame;
+    const double frac = p.accretion_radius_fraction;
+    if (a->type == FGPU_ACCRETION_KLEY) {
+        const double facc = dt * a->efficiency / a->orbital_period * std::log(2);
+        sp.facc1 = 1.0 / 3.0 * facc;
+        sp.facc2 = 2.0 / 3.0 * facc;
+        sp.frac1 = frac;
+        sp.frac2 = 0.5 * frac;
+    } else if (a->type == FGPU_ACCRETION_SINKHOLE) {
+        sp.facc1 = dt * a->efficiency / a->orbital_period * std::log(2.0);
+        sp.frac1 = frac;
+    } else {
+        sp.facc1 = dt * 3.0 * M_PI * a->efficiency;
+        sp.frac1 = frac;
+        sp.dist_max = a->roche_radius * frac;
+        sp.f_const = 3.0 / M_PI / std::pow(sp.dist_max, 2);
+    }
+    const double R = a->r;
+    const double search = a->roche_radius * sp.frac1 + 2.0 * R / ns;
+    std::vector<double> Rmed;  // unused by the rinf search
+    sp.i0 = (R - search < p.rmin) ? 0 : clamp_id(cell_id(eng, Rmed, R - search, true), false, nr);
+    sp.i1 = clamp_id(cell_id(eng, Rmed, R + search, true) + 1, false, nr);
+    const double max_angle = R == 0.0 ? 2.0 * M_PI : std::min(2.0 * M_PI, 2.0 * search / R);
+    const double cell = 2.0 * M_PI / (double)ns, inv = (double)ns / 2.0 / M_PI;
+    const int j_min = (int)std::floor((a->phi - max_angle - 0.5 * cell) * inv);
+    int j_max = (int)std::floor((a->phi + max_angle - 0.5 * cell) * inv) + 1;
+    j_max = j_min + std::min(j_max - j_min, ns - 1);
+    sp.j0 = j_min;
+    sp.ncols = j_max - j_min + 1;
+    if (sp.i1 < sp.i0 || sp.ncols < 1) {
+        out[0] = out[1] = out[2] = 0.0;
+        return FGPU_OK;
+    }
+    double **f = eng->field;
+    launch_accrete(launch_of(eng), sp, f[FGPU_SIGMA], f[FGPU_ENERGY], f[FGPU_V_RADIAL],
+                   f[FGPU_V_AZIMUTHAL], f[FGPU_VISCOSITY], eng->red_out);
+    int rc = check_launch(eng);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(eng->h_pinned, eng->red_out, 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                       eng->stream));
+    CK(cudaStreamSynchronize(eng->stream));
+    for (int k = 0; k < 3; ++k) out[k] = eng->h_pinned[k];
+    eng->cfl_valid = false;
     return FGPU_OK;
 }
 

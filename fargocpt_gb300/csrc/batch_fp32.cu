@@ -648,6 +648,11 @@ extern "C" int fgpu_batch_create(int n, const fgpu_params *params, const double 
         if (params[k].precision != FGPU_PRECISION_FP32_MIXED ||
             params[k].integrator != FGPU_INTEGRATOR_EULER)
             return FGPU_ERR_UNSUPPORTED;
+        // the recompute of c_s, H, nu before the final hooks is not part of
+        // the batched step
+        if (params[k].eos == FGPU_EOS_IDEAL &&
+            (params[k].viscous_accretion || params[k].bc_vrad_inner == FGPU_BC_VISCOUS))
+            return FGPU_ERR_UNSUPPORTED;
     }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {

@@ -291,7 +291,9 @@ __device__ __forceinline__ void artvisc_q_cell(const GeoF &g, const TablesF &t, 
     if (ph.adiabatic) {
         e = E[c];
         if (i < nr - 1) {
-            const float div_v = (vr1 * t.Rinf[i + 1] - vr0 * t.Rinf[i]) * t.InvDiffRsupRb[i] +
+            // (vr1 Rinf[i+1] - vr0 Rinf[i]) / ((Rsup - Rinf) Rmed), regrouped
+            // exactly (Rinf[i+1] = Rsup[i]) so that no product cancels
+            const float div_v = (vr1 - vr0) * t.RsupIDRR[i] + vr0 * t.InvRmed[i] +
                                 dvp * g.invdphi * t.InvRmed[i];
             e = e * __expf(-ph.gm1 * dt * div_v);
         }
@@ -359,7 +361,7 @@ __device__ __forceinline__ void stress_cell(const GeoF &g, const TablesF &t,
     const float vr0 = vr[c], vr1 = vr[CELL(i + 1, j)];
     const float dvp = dv[CELL(i, jn)] - dv[c];
     const float n = nu[c], sg = S[c];
-    const float d = (vr1 * t.Rinf[i + 1] - vr0 * t.Rinf[i]) * t.InvDiffRsupRb[i] +
+    const float d = (vr1 - vr0) * t.RsupIDRR[i] + vr0 * t.InvRmed[i] +
                     dvp * g.invdphi * t.InvRmed[i];
     divv[c] = d;
     const float drr = (vr1 - vr0) * t.InvDiffRsup[i];
@@ -458,9 +460,12 @@ __device__ __forceinline__ void viscous_cell(
 // ghost rings (boundary_conditions.cpp:65-114); v_phi hooks work on the
 // residual, with the reference-profile offsets per ring
 __device__ __forceinline__ void ghost_f(float *x, const float *x0, int kind, int outer, int vec,
-                                        int nr, int nz, int j, float kep_value, float zg_offset)
+                                        int nr, int nz, int j, float kep_value, float zg_offset,
+                                        const float *val, const float *nu)
 {
     const int irad = vec ? nr : nr - 1;
+    const int edge = outer ? irad : 0;
+    const int next = outer ? irad - 1 : 1;
     switch (kind) {
     case 1:
         if (!outer) {
@@ -491,16 +496,32 @@ __device__ __forceinline__ void ghost_f(float *x, const float *x0, int kind, int
         }
         break;
     case 3:
-        if (!outer) {
-            x[CELL(0, j)] = x0[CELL(0, j)];
-            if (vec) x[CELL(1, j)] = x0[CELL(1, j)];
-        } else {
-            x[CELL(irad, j)] = x0[CELL(irad, j)];
-            if (vec) x[CELL(irad - 1, j)] = x0[CELL(irad - 1, j)];
-        }
+        x[CELL(edge, j)] = x0[CELL(edge, j)];
+        if (vec) x[CELL(next, j)] = x0[CELL(next, j)];
         break;
     case 4:
-        x[CELL(outer ? irad : 0, j)] = kep_value;
+        x[CELL(edge, j)] = kep_value;
+        break;
+    case 5:   // disk model
+    case 10:  // balanced (residual)
+        x[CELL(edge, j)] = val[0];
+        break;
+    case 6:  // reflecting
+        x[CELL(edge, j)] = -x[CELL(outer ? irad - 2 : 2, j)];
+        x[CELL(next, j)] = 0.f;
+        break;
+    case 7: {  // viscous outflow (inner edge)
+        const float Nu = 0.5f * (nu[CELL(0, j)] + nu[CELL(1, j)]);
+        x[CELL(1, j)] = val[1] * Nu;
+        x[CELL(0, j)] = val[0] * Nu;
+        break;
+    }
+    case 8:  // Keplerian radial
+        x[CELL(edge, j)] = val[0];
+        x[CELL(next, j)] = val[1];
+        break;
+    case 9:  // zero shear on the residual: ratio * dv_active + offset
+        x[CELL(edge, j)] = fmaf(val[0], x[CELL(next, j)], val[1]);
         break;
     default:
         break;
@@ -510,19 +531,23 @@ __device__ __forceinline__ void ghost_f(float *x, const float *x0, int kind, int
 __device__ __forceinline__ void ghost_col(const GeoF &g, const BcF &bc, const StateF &s, int j)
 {
     const int nz = g.nz, nr = g.nr;
-    ghost_f(s.sigma, s.sigma0, bc.sigma_in, 0, 0, nr, nz, j, 0.f, 0.f);
-    ghost_f(s.sigma, s.sigma0, bc.sigma_out, 1, 0, nr, nz, j, 0.f, 0.f);
-    // low part of sigma: copied by zero-gradient, cleared by reference hooks
+    ghost_f(s.sigma, s.sigma0, bc.sigma_in, 0, 0, nr, nz, j, 0.f, 0.f, bc.val_in[0], bc.nu);
+    ghost_f(s.sigma, s.sigma0, bc.sigma_out, 1, 0, nr, nz, j, 0.f, 0.f, bc.val_out[0], bc.nu);
+    // low part of sigma: copied by zero-gradient, cleared by reference hooks,
+    // the disk model's own low part
     if (bc.sigma_in == 1) s.sigma_lo[CELL(0, j)] = s.sigma_lo[CELL(1, j)];
     else if (bc.sigma_in == 3) s.sigma_lo[CELL(0, j)] = 0.f;
+    else if (bc.sigma_in == 5) s.sigma_lo[CELL(0, j)] = bc.val_in[0][1];
     if (bc.sigma_out == 1) s.sigma_lo[CELL(nr - 1, j)] = s.sigma_lo[CELL(nr - 2, j)];
     else if (bc.sigma_out == 3) s.sigma_lo[CELL(nr - 1, j)] = 0.f;
-    ghost_f(s.energy, s.energy0, bc.energy_in, 0, 0, nr, nz, j, 0.f, 0.f);
-    ghost_f(s.energy, s.energy0, bc.energy_out, 1, 0, nr, nz, j, 0.f, 0.f);
-    ghost_f(s.vr, s.vr0, bc.vr_in, 0, 1, nr, nz, j, 0.f, 0.f);
-    ghost_f(s.vr, s.vr0, bc.vr_out, 1, 1, nr, nz, j, 0.f, 0.f);
-    ghost_f(s.dv, s.dv0, bc.vaz_in, 0, 0, nr, nz, j, bc.kep_in, bc.zg_in);
-    ghost_f(s.dv, s.dv0, bc.vaz_out, 1, 0, nr, nz, j, bc.kep_out, bc.zg_out);
+    else if (bc.sigma_out == 5) s.sigma_lo[CELL(nr - 1, j)] = bc.val_out[0][1];
+    ghost_f(s.energy, s.energy0, bc.energy_in, 0, 0, nr, nz, j, 0.f, 0.f, bc.val_in[1], bc.nu);
+    ghost_f(s.energy, s.energy0, bc.energy_out, 1, 0, nr, nz, j, 0.f, 0.f, bc.val_out[1], bc.nu);
+    ghost_f(s.vr, s.vr0, bc.vr_in, 0, 1, nr, nz, j, 0.f, 0.f, bc.val_in[2], bc.nu);
+    ghost_f(s.vr, s.vr0, bc.vr_out, 1, 1, nr, nz, j, 0.f, 0.f, bc.val_out[2], bc.nu);
+    ghost_f(s.dv, s.dv0, bc.vaz_in, 0, 0, nr, nz, j, bc.kep_in, bc.zg_in, bc.val_in[3], bc.nu);
+    ghost_f(s.dv, s.dv0, bc.vaz_out, 1, 0, nr, nz, j, bc.kep_out, bc.zg_out, bc.val_out[3],
+            bc.nu);
 }
 
 // ---------------------------------------------------------------------------
@@ -766,8 +791,96 @@ __device__ __forceinline__ void ring_pass_f(float *S, float *SS, float *W, float
     __syncthreads();
 }
 
-// smf: azimuthal_smem_floats(nz, nq, STAGE) floats of shared memory; redf: 33
-// floats, redl: 33 long longs (shared memory)
+// The uniform pass of FARGO (QuantitiesAdvection with the ring's residual
+// shift velocity, TransportEuler.cpp:292-304) in difference form.  The whole
+// ring has one upwind direction, so with u the upwind cell of face j
+// (j - 1 for a positive shift, j otherwise) and a the interpolation distance
+// (dx - ksi, or -(dx + ksi)), face j's star value is X_u + a D_u and cell j
+// changes by dxrad v invsurf (q*_j S*_j - q*_{j+1} S*_{j+1})
+//   = dxrad v invsurf (q*_j dS*_j + S*_{j+1} dq*_j),
+//   dS*_j = (S_u - S_{u+1}) + a (D_u - D_{u+1}),  dq*_j likewise.
+// This is the flux form's arithmetic regrouped: forming the neighbour
+// differences first keeps FP32's rounding at the size of the changes, where
+// the flux form rounds at the size of the fluxes, up to half of the ring's
+// content per step, and repeats the same rounding pattern every step.
+// dS* and S*_{j+1} go to the SS and F arrays (unused by this pass).
+template <int PER, int NQ>
+__device__ __forceinline__ void ring_pass_uniform_f(float *S, float *SS, float *W, float *D,
+                                                    float *F, float *const *qrow, float *slo,
+                                                    float dt, float dxtheta, float half_invdx,
+                                                    float dxrad, float invsurf, int nz, int mc,
+                                                    float vconst)
+{
+    const int tid = threadIdx.x, bs = blockDim.x;
+    const float ksi = vconst * dt;
+    const bool pos = ksi > 0.f;
+    const float a = pos ? dxtheta - ksi : -(dxtheta + ksi);
+    const float c = dxrad * vconst * invsurf;
+    float invs[PER];
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = tid + n * bs;
+        if (j < nz) {
+            const int jp = j == nz - 1 ? 0 : j + 1, jm = j == 0 ? nz - 1 : j - 1;
+            D[j] = lim_f(S[jp] - S[j], S[j] - S[jm], mc) * half_invdx;
+            invs[n] = __frcp_rn(S[j]);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = tid + n * bs;
+        if (j < nz) {
+            const int jp = j == nz - 1 ? 0 : j + 1, jm = j == 0 ? nz - 1 : j - 1;
+            const int u = pos ? jm : j, u1 = pos ? j : jp;
+            SS[j] = (S[u] - S[u1]) + a * (D[u] - D[u1]);
+            F[j] = S[u1] + a * D[u1];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+        float *Q = qrow[q];
+#pragma unroll
+        for (int n = 0; n < PER; ++n) {
+            const int j = tid + n * bs;
+            if (j < nz) W[j] = Q[j] * invs[n];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int n = 0; n < PER; ++n) {
+            const int j = tid + n * bs;
+            if (j < nz) {
+                const int jp = j == nz - 1 ? 0 : j + 1, jm = j == 0 ? nz - 1 : j - 1;
+                D[j] = lim_f(W[jp] - W[j], W[j] - W[jm], mc) * half_invdx;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int n = 0; n < PER; ++n) {
+            const int j = tid + n * bs;
+            if (j < nz) {
+                const int jp = j == nz - 1 ? 0 : j + 1, jm = j == 0 ? nz - 1 : j - 1;
+                const int u = pos ? jm : j, u1 = pos ? j : jp;
+                const float qs = W[u] + a * D[u];
+                const float dqs = (W[u] - W[u1]) + a * (D[u] - D[u1]);
+                Q[j] += c * (qs * SS[j] + F[j] * dqs);
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = tid + n * bs;
+        if (j < nz) {
+            float sn = S[j];
+            comp_add(sn, slo[n], c * SS[j]);
+            S[j] = sn;
+        }
+    }
+    __syncthreads();
+}
+
 // Shared memory of azimuthal_ring: 5 ring-long work arrays (sigma, its star
 // value, the specific quantity, its slope, the flux), plus the nq quantity
 // rows when STAGE (then every row is read from HBM once, up front, and the
@@ -837,13 +950,13 @@ __device__ __forceinline__ void azimuthal_ring(const GeoF &g, const TablesF &t, 
     }
     const float dxtheta = g.dphi * t.Rmed[i];
     const float half_invdx = 0.5f / dxtheta;
-    const float dxrad = (t.Rsup[i] - t.Rinf[i]) * (float)dt;
+    const float dxrad = t.DRsup[i] * (float)dt;
     const float invsurf = t.InvSurf[i];
     ring_pass_f<PER, NQ>(Sr, SS, W, D, Fx, qrow, vown, slo, (float)dt, dxtheta, half_invdx,
                          dxrad, invsurf, nz, mc, false, 0.f);
     if (fast) {
-        ring_pass_f<PER, NQ>(Sr, SS, W, D, Fx, qrow, vown, slo, (float)dt, dxtheta, half_invdx,
-                             dxrad, invsurf, nz, mc, true, vt);
+        ring_pass_uniform_f<PER, NQ>(Sr, SS, W, D, Fx, qrow, slo, (float)dt, dxtheta, half_invdx,
+                                     dxrad, invsurf, nz, mc, vt);
     }
     // the integer shift (AdvectSHIFT, :238-268): cell j takes cell j - nshift
     const int ns = nshift % nz;

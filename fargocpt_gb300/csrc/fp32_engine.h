@@ -35,6 +35,10 @@ struct TablesF {
     const float *DJ;        // J_K(i-1) - J_K(i), J_K = r v_K
     const float *JSlope;    // (J_K(i+1) - J_K(i)) / (Rmed(i+1) - Rmed(i))
     const float *DRmed;     // Rmed(i) - Rmed(i-1)
+    const float *DRsup;     // Rsup(i) - Rinf(i), formed in FP64 (an FP32 difference of
+                            // the radii loses ~1e-4 of it on fine grids)
+    const float *RsupIDRR;  // Rsup(i) / ((Rsup(i) - Rinf(i)) Rmed(i)): div v without
+                            // the cancelling v_r Rinf products
     const float *OmRefDiff; // v_K(i)/R(i) - v_K(i+1)/R(i+1)
     const float *Vref;      // v_K(Rmed)
     const double *Rmed_d, *InvRmed_d, *Vref_d, *Surf_d, *PhiK_d, *cos_d, *sin_d;
@@ -62,6 +66,12 @@ struct BcF {
     int sigma_in, sigma_out, energy_in, energy_out, vr_in, vr_out, vaz_in, vaz_out;
     float kep_in, kep_out;  // Keplerian-hook value of the residual
     float zg_in, zg_out;    // zero-gradient offset of the residual between rings
+    // per field (0 sigma, 1 energy, 2 v_r, 3 v_phi residual) and side: the
+    // disk-model value (sigma: high and low part), the viscous-outflow factors,
+    // the Keplerian-radial values, the zero-shear ratio and offset of the
+    // residual, the balanced residual
+    float val_in[4][2], val_out[4][2];
+    const float *nu;        // viscosity (viscous-outflow hook)
 };
 
 struct DampQF {
@@ -73,6 +83,10 @@ struct DampQF {
 struct DampingF {
     DampQF q[4];
 };
+
+// Host constants of every boundary hook in FP64 (api.cu), shared by both forms.
+void boundary_values(const fgpu_params &p, const double *Rmed, const double *Rinf, int nr,
+                     double vin[4][2], double vout[4][2]);
 
 struct StateF {
     float *sigma, *vr, *dv, *energy, *sigma0, *vr0, *dv0, *energy0;
@@ -198,6 +212,7 @@ class Engine32 {
     int per = 4, az_block = 128;
     size_t az_smem = 0;
     bool az_stage = false;
+    bool visc_recompute = false;  // c_s, H, nu before the final hooks (adiabatic)
     bool cfl_valid = false;
 };
 

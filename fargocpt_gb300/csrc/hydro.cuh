@@ -75,11 +75,15 @@ struct Bodies {
     double omega_frame;
 };
 
-// Ghost-ring hooks of one step (FGPU_BC_* per field and side).
+// Ghost-ring hooks of one step (FGPU_BC_* per field and side).  val_in /
+// val_out hold each hook's host-computed constants per field (0 sigma,
+// 1 energy, 2 v_radial, 3 v_azimuthal): Keplerian c v_K; disk-model values;
+// the viscous-outflow factors -1.5 s / Rinf[k]; Keplerian-radial values of the
+// two ghost rings; zero-shear radii (edge ring, active ring); the balanced
+// velocity before the frame correction.
 struct BcSpec {
     int sigma_in, sigma_out, energy_in, energy_out, vr_in, vr_out, vaz_in, vaz_out;
-    double vk_in, vk_out;       // compute_v_kepler(Rmed[0]) , (Rmed[nr-1])
-    double kep_in, kep_out;     // keplerian factors
+    double val_in[4][2], val_out[4][2];
 };
 
 // Damping set-up of one quantity (boundary_conditions/damping.cpp:311-752).
@@ -96,6 +100,20 @@ struct DampQ {
 
 struct Damping {
     DampQ q[4];                 // v_radial, v_azimuthal, sigma, energy
+};
+
+// One planet's accretion region and constants (accretion.cpp:84-480); the
+// region's rings and azimuthal indices are found on the host exactly as
+// hill_radial_index / hill_azimuthal_index do.
+struct AccretionSpec {
+    int type;                   // FGPU_ACCRETION_*
+    int i0, i1;                 // rings i0 .. i1
+    int j0, ncols;              // azimuthal indices j0 .. j0 + ncols - 1 (wrapped)
+    double x, y, rhill;
+    double frac1, frac2;        // zone radii in Hill radii (frac2: Kley's inner zone)
+    double facc1, facc2;        // removal fractions per call
+    double f_const, dist_max;   // viscous accretion profile
+    double density_floor, omf;
 };
 
 // Pointers of the evolved state and the work arrays of one step.

@@ -48,5 +48,7 @@ void launch_pressure(const Launch &L, const double *S, const double *E, double *
 void launch_disk_force(const Launch &L, double px, double py, double pa, double rsm,
                        const double *S, const double *H, double *partial, double *out);
 void launch_check_finite(const Launch &L, const double *x, size_t n, unsigned long long *bad);
+void launch_accrete(const Launch &L, const AccretionSpec &a, double *S, double *E,
+                    const double *vr, const double *vaz, const double *nu, double *out);
 
 }  // namespace fgpu

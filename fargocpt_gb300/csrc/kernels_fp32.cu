@@ -313,11 +313,13 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
     enum { RINF, RSUP, RMED, SURF, INVRMED, INVSURF, INVDIFFRMED, INVDIFFRSUP, INVDIFFRSUPRB,
            INVRINF, RINFSQ, TWOOVER, OMEGAK, INVOMEGAK, CSISO, INVDXSRC, INVDXTHETA, EMODEL,
            HFACADI, INVCELL, INVCELL2, TWOOVERRMEDSUM, KBAL, AFACE, SHEAR, DJ, JSLOPE, DRMED,
-           OMREFDIFF, VREF, NT };
+           OMREFDIFF, VREF, DRSUP, RSUPIDRR, NT };
     std::vector<float> hf((size_t)NT * R, 0.f);
     auto F = [&](int k) { return hf.data() + (size_t)k * R; };
     for (int n = 0; n <= nr; ++n) {
         const double rm = Rmed[n], dxr = Rsup[n] - Rinf[n], dxa = rm * dphi;
+        F(DRSUP)[n] = (float)dxr;
+        F(RSUPIDRR)[n] = (float)(Rsup[n] / (dxr * rm));
         const double om = std::sqrt(G * M / (rm * rm * rm));
         const double cell = std::min(dxr, dxa);
         F(RINF)[n] = (float)Rinf[n];
@@ -387,7 +389,7 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
     t.InvDxTheta = Df(INVDXTHETA); t.EModel = Df(EMODEL); t.HFacAdi = Df(HFACADI);
     t.InvCell = Df(INVCELL); t.InvCell2 = Df(INVCELL2); t.TwoOverRmedSum = Df(TWOOVERRMEDSUM);
     t.Kbal = Df(KBAL); t.Aface = Df(AFACE); t.Shear = Df(SHEAR); t.DJ = Df(DJ);
-    t.JSlope = Df(JSLOPE); t.DRmed = Df(DRMED); t.OmRefDiff = Df(OMREFDIFF); t.Vref = Df(VREF);
+    t.JSlope = Df(JSLOPE); t.DRmed = Df(DRMED); t.DRsup = Df(DRSUP); t.RsupIDRR = Df(RSUPIDRR); t.OmRefDiff = Df(OMREFDIFF); t.Vref = Df(VREF);
     t.Rmed_d = tab_d; t.InvRmed_d = tab_d + R; t.Vref_d = tab_d + 2 * R; t.Surf_d = tab_d + 3 * R;
     t.PhiK_d = tab_d + 4 * R; t.cos_d = tab_d + 5 * R; t.sin_d = tab_d + 5 * R + nz;
 
@@ -463,6 +465,37 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
                          Vref[nr - 1]);
     bc.zg_in = (float)(Vref[1] - Vref[0]);
     bc.zg_out = (float)(Vref[nr - 2] - Vref[nr - 1]);
+    bc.nu = fld[FGPU_VISCOSITY];
+    visc_recompute = p.eos == FGPU_EOS_IDEAL &&
+                     (p.viscous_accretion || p.bc_vrad_inner == FGPU_BC_VISCOUS);
+    {
+        // the remaining hooks' constants, in the residual form where v_phi is
+        // concerned (the FP32 form runs without a rotating frame)
+        double vin[4][2], vout[4][2];
+        boundary_values(p, Rmed.data(), Rinf.data(), nr, vin, vout);
+        const int kin[4] = {p.bc_sigma_inner, p.bc_energy_inner, p.bc_vrad_inner, p.bc_vaz_inner};
+        const int kout[4] = {p.bc_sigma_outer, p.bc_energy_outer, p.bc_vrad_outer,
+                             p.bc_vaz_outer};
+        for (int f = 0; f < 4; ++f) {
+            for (int side = 0; side < 2; ++side) {
+                const double *v = side ? vout[f] : vin[f];
+                float *o = side ? bc.val_out[f] : bc.val_in[f];
+                const int kind = side ? kout[f] : kin[f];
+                const int edge = side ? nr - 1 : 0, next = side ? nr - 2 : 1;
+                o[0] = (float)v[0];
+                o[1] = (float)v[1];
+                if (f == 0 && kind == FGPU_BC_DISKMODEL) {
+                    o[1] = (float)(v[0] - (double)o[0]);
+                } else if (f == 3 && kind == FGPU_BC_ZEROSHEAR) {
+                    const double ratio = v[0] / v[1];
+                    o[0] = (float)ratio;
+                    o[1] = (float)(ratio * Vref[next] - Vref[edge]);
+                } else if (f == 3 && kind == FGPU_BC_BALANCED) {
+                    o[0] = (float)(v[0] - Vref[edge]);
+                }
+            }
+        }
+    }
 
     // damping
     const int dq_field[4] = {FGPU_V_RADIAL, FGPU_V_AZIMUTHAL, FGPU_SIGMA, FGPU_ENERGY};
@@ -733,6 +766,12 @@ int Engine32::cfl(double *dt_out)
 
 int Engine32::boundary(double dt, bool final)
 {
+    if (final && visc_recompute) {
+        // c_s, H, nu of the transported state before the final hooks
+        // (simulation.cpp:232-242, 432-441)
+        int rc = derived_cfl(1);
+        if (rc) return rc;
+    }
     if (final && p.damping && n_rings)
         f_damping<<<n_rings, 256, 0, stream>>>(geo, dm, (float)dt, damp_rings, state());
     f_ghost<<<(nz + 127) / 128, 128, 0, stream>>>(geo, bc, state());
@@ -871,6 +910,10 @@ int Engine32::step(double dt, double t)
     mark(6);
     rc = transport(dt);
     if (rc) return rc;
+    if (visc_recompute) {
+        rc = derived_cfl(1);
+        if (rc) return rc;
+    }
     StateF s = state();
     if (p.damping && n_rings)
         f_damping<<<n_rings, 256, 0, stream>>>(geo, dm, (float)dt, damp_rings, s);

@@ -472,9 +472,12 @@ __global__ void k_viscous(Geo g, Tables t, Phys ph, double dt, double beta_inv, 
 // Ghost-ring hooks of apply_boundary_condition (boundary_conditions.cpp:65-114)
 // ---------------------------------------------------------------------------
 __device__ void ghost_hook(double *x, const double *x0, int kind, int outer, int vec, int nr,
-                           int nz, int j, double vk, double kep, double rmed_edge, double omf)
+                           int nz, int j, const double *val, const double *nu,
+                           double rmed_edge, double omf)
 {
     const int irad = vec ? nr : nr - 1;  // get_max_radial()
+    const int edge = outer ? irad : 0;
+    const int next = outer ? irad - 1 : 1;
     switch (kind) {
     case 1:  // zero_gradient.cpp:14-90
         if (!outer) {
@@ -513,19 +516,33 @@ __device__ void ghost_hook(double *x, const double *x0, int kind, int outer, int
         }
         break;
     case 3:  // reference.cpp:17-88
-        if (!outer) {
-            x[CELL(0, j)] = x0[CELL(0, j)];
-            if (vec) x[CELL(1, j)] = x0[CELL(1, j)];
-        } else {
-            x[CELL(irad, j)] = x0[CELL(irad, j)];
-            if (vec) x[CELL(irad - 1, j)] = x0[CELL(irad - 1, j)];
-        }
+        x[CELL(edge, j)] = x0[CELL(edge, j)];
+        if (vec) x[CELL(next, j)] = x0[CELL(next, j)];
         break;
-    case 4: {  // keplerian_azimuthal.cpp:18-59
-        const int i = outer ? irad : 0;
-        x[CELL(i, j)] = kep * vk - rmed_edge * omf;
+    case 4:   // keplerian_azimuthal.cpp:18-59: c v_K - r Omega_F
+    case 10:  // balanced.cpp:20-66: sqrt(v^2) - Rb Omega_F
+        x[CELL(edge, j)] = val[0] - rmed_edge * omf;
+        break;
+    case 5:  // diskmodel.cpp:33-77
+        x[CELL(edge, j)] = val[0];
+        break;
+    case 6:  // reflecting.cpp:15-40
+        x[CELL(edge, j)] = -x[CELL(outer ? irad - 2 : 2, j)];
+        x[CELL(next, j)] = 0.0;
+        break;
+    case 7: {  // viscous.cpp:15-40 (inner edge)
+        const double Nu = 0.5 * (nu[CELL(0, j)] + nu[CELL(1, j)]);
+        x[CELL(1, j)] = val[1] * Nu;
+        x[CELL(0, j)] = val[0] * Nu;
         break;
     }
+    case 8:  // keplerian_radial.cpp:17-62
+        x[CELL(edge, j)] = val[0];
+        x[CELL(next, j)] = val[1];
+        break;
+    case 9:  // zero_shear.cpp:19-53: r_edge (v_active / r_active)
+        x[CELL(edge, j)] = val[0] * (x[CELL(next, j)] / val[1]);
+        break;
     default:
         break;
     }
@@ -536,14 +553,14 @@ __global__ void k_ghost(Geo g, Tables t, BcSpec bc, double omf, State s)
     const int nz = g.nz, nr = g.nr;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= nz) return;
-    ghost_hook(s.sigma, s.sigma0, bc.sigma_in, 0, 0, nr, nz, j, 0, 0, 0, 0);
-    ghost_hook(s.sigma, s.sigma0, bc.sigma_out, 1, 0, nr, nz, j, 0, 0, 0, 0);
-    ghost_hook(s.energy, s.energy0, bc.energy_in, 0, 0, nr, nz, j, 0, 0, 0, 0);
-    ghost_hook(s.energy, s.energy0, bc.energy_out, 1, 0, nr, nz, j, 0, 0, 0, 0);
-    ghost_hook(s.vr, s.vr0, bc.vr_in, 0, 1, nr, nz, j, 0, 0, 0, 0);
-    ghost_hook(s.vr, s.vr0, bc.vr_out, 1, 1, nr, nz, j, 0, 0, 0, 0);
-    ghost_hook(s.vaz, s.vaz0, bc.vaz_in, 0, 0, nr, nz, j, bc.vk_in, bc.kep_in, t.Rmed[0], omf);
-    ghost_hook(s.vaz, s.vaz0, bc.vaz_out, 1, 0, nr, nz, j, bc.vk_out, bc.kep_out, t.Rmed[nr - 1],
+    ghost_hook(s.sigma, s.sigma0, bc.sigma_in, 0, 0, nr, nz, j, bc.val_in[0], s.nu, 0, 0);
+    ghost_hook(s.sigma, s.sigma0, bc.sigma_out, 1, 0, nr, nz, j, bc.val_out[0], s.nu, 0, 0);
+    ghost_hook(s.energy, s.energy0, bc.energy_in, 0, 0, nr, nz, j, bc.val_in[1], s.nu, 0, 0);
+    ghost_hook(s.energy, s.energy0, bc.energy_out, 1, 0, nr, nz, j, bc.val_out[1], s.nu, 0, 0);
+    ghost_hook(s.vr, s.vr0, bc.vr_in, 0, 1, nr, nz, j, bc.val_in[2], s.nu, 0, 0);
+    ghost_hook(s.vr, s.vr0, bc.vr_out, 1, 1, nr, nz, j, bc.val_out[2], s.nu, 0, 0);
+    ghost_hook(s.vaz, s.vaz0, bc.vaz_in, 0, 0, nr, nz, j, bc.val_in[3], s.nu, t.Rmed[0], omf);
+    ghost_hook(s.vaz, s.vaz0, bc.vaz_out, 1, 0, nr, nz, j, bc.val_out[3], s.nu, t.Rmed[nr - 1],
                omf);
 }
 
@@ -1183,6 +1200,75 @@ __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const 
 }
 
 // ---------------------------------------------------------------------------
+// Accretion onto one planet (accretion.cpp:84-480): Kley's two zones, the
+// sink hole or the viscous profile over the planet's region, one block; the
+// mass and momentum taken from the active rings are block sums written to
+// out[0 .. 2].  Cells are independent, so the in-place updates do not race.
+// ---------------------------------------------------------------------------
+__global__ void k_accrete(Geo g, Tables t, Phys ph, AccretionSpec a, double *__restrict__ S,
+                          double *__restrict__ E, const double *__restrict__ vr,
+                          const double *__restrict__ vaz, const double *__restrict__ nu,
+                          double *__restrict__ out)
+{
+    __shared__ double red[33];
+    const int nz = g.nz, nr = g.nr;
+    const int rows = a.i1 - a.i0 + 1;
+    const long long cells = (long long)rows * a.ncols;
+    double dM = 0.0, dPx = 0.0, dPy = 0.0;
+    for (long long k = threadIdx.x; k < cells; k += blockDim.x) {
+        const int i = a.i0 + (int)(k / a.ncols);
+        int jf = a.j0 + (int)(k % a.ncols);
+        jf %= nz;
+        if (jf < 0) jf += nz;
+        const size_t l = CELL(i, jf);
+        const double xc = t.Rmed[i] * t.cosj[jf];
+        const double yc = t.Rmed[i] * t.sinj[jf];
+        const double dx = a.x - xc, dy = a.y - yc;
+        const double distance = sqrt(dx * dx + dy * dy);
+        const double vtcell = 0.5 * (vaz[l] + vaz[CELL(i, jnext(jf, nz))]) + t.Rmed[i] * a.omf;
+        const double vrcell = 0.5 * (vr[l] + vr[l + nz]);
+        const double vxcell = (vrcell * xc - vtcell * yc) / t.Rmed[i];
+        const double vycell = (vrcell * yc + vtcell * xc) / t.Rmed[i];
+        const double facc_max = 1 - a.density_floor / S[l];
+        const bool active = 1 < i && i < nr - 1;
+        if (distance < a.frac1 * a.rhill) {
+            double f = a.facc1;
+            if (a.type == 1 /* viscous */)
+                f = a.facc1 * nu[l] * (a.f_const * (1.0 - distance / a.dist_max));
+            const double fc = facc_max < f ? facc_max : f;
+            const double deltaM = fc * S[l] * t.Surf[i];
+            S[l] *= 1.0 - fc;
+            if (ph.adiabatic) E[l] *= 1.0 - fc;
+            if (active) {
+                dPx += deltaM * vxcell;
+                dPy += deltaM * vycell;
+                dM += deltaM;
+            }
+        }
+        if (a.type == 0 /* Kley */ && distance < a.frac2 * a.rhill) {
+            const double fc = facc_max < a.facc2 ? facc_max : a.facc2;
+            const double deltaM = fc * S[l] * t.Surf[i];
+            S[l] *= 1.0 - fc;
+            // the reference scales the energy by the uncapped factor here
+            if (ph.adiabatic) E[l] *= 1.0 - a.facc2;
+            if (active) {
+                dPx += deltaM * vxcell;
+                dPy += deltaM * vycell;
+                dM += deltaM;
+            }
+        }
+    }
+    dM = block_sum(dM, red);
+    dPx = block_sum(dPx, red);
+    dPy = block_sum(dPy, red);
+    if (threadIdx.x == 0) {
+        out[0] = dM;
+        out[1] = dPx;
+        out[2] = dPy;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // ComputeDiskOnPlanetAccel (src/Force.cpp:23-122) with CorrectDiskSelfgravity
 // (the ring mean of sigma subtracted, Pframeforce.cpp:175-190), and
 // gas_total_mass (quantities.cpp:51-74).  One CTA per active ring writes its
@@ -1297,6 +1383,12 @@ void launch_viscous(const Launch &L, double dt, double beta_inv, int mode, const
     k_viscous<<<grid2d(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(
         L.g, L.t, L.ph, dt, beta_inv, mode, s.sigma, s.trr, s.tpp, s.trp, s.divv, s.nu, s.H,
         s.sigma0, s.energy0, s.vr, s.vaz, s.energy, s.qplus, s.qminus, s.corr_phi, s.corr_r);
+}
+
+void launch_accrete(const Launch &L, const AccretionSpec &a, double *S, double *E,
+                    const double *vr, const double *vaz, const double *nu, double *out)
+{
+    k_accrete<<<1, 512, 0, L.stream>>>(L.g, L.t, L.ph, a, S, E, vr, vaz, nu, out);
 }
 
 void launch_visc_corr(const Launch &L, const State &s)

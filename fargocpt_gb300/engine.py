@@ -155,6 +155,14 @@ class Engine:
         self._check(self.lib.fgpu_total_mass(self.h, C.byref(out)), "fgpu_total_mass")
         return out.value
 
+    def accrete_onto_planet(self, accretor, dt):
+        """One planet's part of AccreteOntoPlanets; accretor is an
+        abi.FgpuAccretor.  Returns (mass, x momentum, y momentum) taken."""
+        out = (C.c_double * 3)()
+        self._check(self.lib.fgpu_accrete_onto_planet(self.h, C.byref(accretor), dt, out),
+                    "fgpu_accrete_onto_planet")
+        return out[0], out[1], out[2]
+
     def check_finite(self):
         f, i, j = C.c_int(), C.c_int(), C.c_int()
         rc = self.lib.fgpu_check_finite(self.h, C.byref(f), C.byref(i), C.byref(j))

@@ -74,7 +74,7 @@ def step_leapfrog(hydro, dt: float, t: float, first, second) -> None:
 def advance(hydro, clock: RunClock, *, cfl_max_var: float,
             monitor_timestep: float, t_final: float, max_steps: int = -1,
             bodies=None, on_monitor=None, integrator: str = "euler",
-            bodies_second=None) -> None:
+            bodies_second=None, accrete=None) -> None:
     """The loop of sim::run (simulation.cpp:505-558) with step_Euler or, for
     integrator "leapfrog", step_LeapFrog's gas part.
 
@@ -82,6 +82,8 @@ def advance(hydro, clock: RunClock, *, cfl_max_var: float,
     before every step (the N-body state of the host at the start of the step;
     for LeapFrog the state the first kick sees); bodies_second(clock, dt), for
     LeapFrog, gives the second kick's (defaults to the first's);
+    accrete(clock, dt), for Euler, runs AccreteOntoPlanets where step_Euler
+    does, first in the step (simulation.cpp:150-153);
     on_monitor(clock) after every step that lands on a monitor time.
     """
     while clock.time < t_final:
@@ -98,6 +100,8 @@ def advance(hydro, clock: RunClock, *, cfl_max_var: float,
             second = bodies_second(clock, step_dt) if bodies_second is not None else first
             step_leapfrog(hydro, step_dt, clock.time, first, second)
         else:
+            if accrete is not None:
+                accrete(clock, step_dt)
             if bodies is not None:
                 b, ix, iy = bodies(clock)
                 hydro.set_bodies(b, ix, iy, 0.0)
@@ -109,6 +113,42 @@ def advance(hydro, clock: RunClock, *, cfl_max_var: float,
             clock.n_monitor += 1
             if on_monitor is not None:
                 on_monitor(clock)
+
+
+def l1_point(central_mass: float, other_mass: float) -> float:
+    """init_l1 (Theo.cpp:251-277): the dimensionless distance of the L1 point
+    from the central mass, by Newton-Raphson."""
+    q = central_mass / (central_mass + other_mass)
+    x = math.pow(other_mass / (3.0 * central_mass), 1.0 / 3.0)
+    counter = 0
+    while True:
+        counter += 1
+        if counter > 10:
+            break
+        f = q / math.pow(1.0 - x, 2) - (1.0 - q) / math.pow(x, 2) - q + x
+        df = 2.0 * q / math.pow(1.0 - x, 3) + 2.0 * (1.0 - q) / math.pow(x, 3) + 1.0
+        x = x - f / df
+        if not math.fabs(f) > 1e-14:
+            break
+    return x
+
+
+def orbital_period(x, y, vx, vy, com_mass, mass, G) -> float:
+    """The period of t_planet::calculate_orbital_elements (planet.cpp:488-566)
+    for relative position and velocity (x, y, vx, vy) about com_mass; 0 where
+    the reference sets the elements to zero."""
+    m = com_mass + mass
+    h = x * vy - y * vx
+    d = math.sqrt(x * x + y * y)
+    if d == 0.0 or h == 0.0:
+        return 0.0
+    Ax = x * vy * vy - y * vx * vy - G * m * x / d
+    Ay = y * vx * vx - x * vx * vy - G * m * y / d
+    e = math.sqrt(Ax * Ax + Ay * Ay) / G / m
+    a = h * h / G / m / (1.0 - e * e)
+    if e > 1.0 or e < 0 or a < 0.0:
+        return 0.0
+    return 2.0 * math.pi * math.sqrt(math.pow(a, 3) / (m * G))
 
 
 def indirect_term_euler(bodies) -> tuple[float, float]:

@@ -72,7 +72,15 @@ typedef enum fgpu_bc {
     FGPU_BC_ZEROGRADIENT = 1,  /* zero_gradient.cpp:39-90 */
     FGPU_BC_OUTFLOW = 2,       /* outflow.cpp:16-57 (v_radial only) */
     FGPU_BC_REFERENCE = 3,     /* reference.cpp:17-88 */
-    FGPU_BC_KEPLERIAN = 4      /* keplerian_azimuthal.cpp:18-59 (v_azimuthal only) */
+    FGPU_BC_KEPLERIAN = 4,     /* keplerian_azimuthal.cpp:18-59 (v_azimuthal only) */
+    FGPU_BC_DISKMODEL = 5,     /* diskmodel.cpp:18-77 (sigma, energy) */
+    FGPU_BC_REFLECTING = 6,    /* reflecting.cpp:15-40 (v_radial) */
+    FGPU_BC_VISCOUS = 7,       /* viscous.cpp:15-40 (v_radial, inner edge only: the
+                                  outer version reads one ring past the viscosity
+                                  grid, viscous.cpp:46-66, and is refused) */
+    FGPU_BC_KEPLERIAN_RADIAL = 8, /* keplerian_radial.cpp:17-62 (v_radial) */
+    FGPU_BC_ZEROSHEAR = 9,     /* zero_shear.cpp:19-53 (v_azimuthal) */
+    FGPU_BC_BALANCED = 10      /* balanced.cpp:20-94 (v_azimuthal; no self-gravity) */
 } fgpu_bc;
 
 /* Damping kinds (src/boundary_conditions/boundary_conditions.h:93-99). */
@@ -126,7 +134,14 @@ typedef struct fgpu_params {
                                1 pseudo-implicit viscous update, 2 viscous dt limit
                                (viscosity.cpp:256-348, 395-417; cfl.cpp:332-351);
                                FP64 only */
-    int reserved_i[5];
+    int profile_cutoff_outer; /* ProfileCutoffOuter (parameters.cpp:730): balanced
+                                 boundary without pressure support */
+    int viscous_accretion;  /* a planet accretes with the viscous profile
+                               (planetary_system.cpp:255-257); with it, or with the
+                               viscous v_radial hook, c_s, H and nu are recomputed
+                               before the final boundary call (simulation.cpp:232-242,
+                               432-441; Interpret.cpp:704-707) */
+    int reserved_i[3];
 
     double gamma;           /* AdiabaticIndex */
     double mu;              /* mean molecular weight */
@@ -161,7 +176,18 @@ typedef struct fgpu_params {
     double rmin, rmax;      /* RMIN, RMAX */
     int radial_spacing;     /* FGPU_SPACING_* (used for damping ring search) */
     int reserved_j;
-    double reserved_d[8];
+    double accretion_radius_fraction; /* MassAccretionRadius (parameters.cpp:789-790,
+                                         FargoCPT's default 1.0) */
+    double sigma_slope;     /* SigmaSlope (Interpret.cpp:88): disk-model and balanced
+                               boundaries */
+    double viscous_outflow_speed; /* ViscousOutflowSpeed (config.cpp:498, default 1) */
+    double vrad_inner_keplerian_factor; /* InnerBoundaryVradKeplerianFactor (config.cpp:220,
+                                           default 0.1) */
+    double vrad_outer_keplerian_factor; /* OuterBoundaryVradKeplerianFactor (default 0.1) */
+    double binary_quadrupole_moment;    /* Theo.cpp:74 when
+                                           VazimuthalConsidersQuadropoleMoment is set,
+                                           else 0 (balanced boundary) */
+    double reserved_d[2];
 } fgpu_params;
 
 /* One N-body object as the gas sees it (src/Pframeforce.cpp:24-35). */
@@ -237,6 +263,33 @@ int fgpu_disk_on_planet_accel(fgpu_engine *eng, int k, double accel[2]);
 
 /* quantities::gas_total_mass (src/quantities.cpp:51-74) over the active rings. */
 int fgpu_total_mass(fgpu_engine *eng, double *mass);
+
+/* Accretion kinds of t_planet (src/nbody/planet.h:6-9). */
+enum { FGPU_ACCRETION_KLEY = 0, FGPU_ACCRETION_VISCOUS = 1, FGPU_ACCRETION_SINKHOLE = 2 };
+
+/* One accreting planet as accretion::AccreteOntoPlanets reads it
+ * (src/accretion.cpp:84-480); the host's t_planet supplies every value. */
+typedef struct fgpu_accretor {
+    int type;               /* FGPU_ACCRETION_* (t_planet::get_accretion_type) */
+    int reserved;
+    double x, y;            /* get_x(), get_y() */
+    double r, phi;          /* get_r(), get_phi() (planet.cpp:159-160) */
+    double roche_radius;    /* get_dimensionless_roche_radius() *
+                               get_distance_to_primary() */
+    double efficiency;      /* get_accretion_efficiency() */
+    double orbital_period;  /* get_orbital_period() */
+} fgpu_accretor;
+
+/* One planet's part of accretion::AccreteOntoPlanets (src/accretion.cpp:84-480,
+ * Kley's two zones, the sink hole, or the viscous profile): removes gas, and
+ * energy with it, from the cells around the planet, down to the density
+ * floor, and returns in out[0 .. 2] the mass and the x/y momentum taken from
+ * the active rings.  The host adds them to the planet (update_planet,
+ * accretion.cpp:60-82) and its accreted-mass monitor.  Call it for each
+ * accreting planet where step_Euler / step_LeapFrog call AccreteOntoPlanets
+ * (simulation.cpp:150-153, 301-304, 402-405).  FP64 form only. */
+int fgpu_accrete_onto_planet(fgpu_engine *eng, const fgpu_accretor *a, double dt,
+			     double out[3]);
 
 /* Scans the evolved fields for NaN/Inf; returns FGPU_ERR_NONFINITE and the
  * first bad (field, ring, azimuth) when one is found. */
@@ -365,8 +418,9 @@ typedef struct {
 
 /* params[k], radii[k]: disk k as for fgpu_create; every disk must select
  * FGPU_PRECISION_FP32_MIXED and the Euler integrator (the batched step is
- * step_Euler); the longest ring must fit the azimuthal
- * transport's shared memory (naz <= 5632).  1 <= n <= 1024. */
+ * step_Euler); adiabatic disks with the viscous v_radial hook or viscous
+ * accretion are refused (FGPU_ERR_UNSUPPORTED); the longest ring must fit the
+ * azimuthal transport's shared memory (naz <= 5632).  1 <= n <= 1024. */
 int fgpu_batch_create(int n, const fgpu_params *params,
 		      const double *const *radii, fgpu_batch **out);
 int fgpu_batch_destroy(fgpu_batch *b);

@@ -1063,6 +1063,79 @@ static void ghost_hook(or_state *s, int field, int kind, int outer)
 	    AT(x, i, j) = c * vK - r * s->omega_frame;
 	    break;
 	}
+	case FGPU_BC_DISKMODEL: {
+	    /* diskmodel.cpp:18-77 (calc_sig, calc_eng at Rmed of the ghost ring) */
+	    const double R = s->Rmed[outer ? irad : 0];
+	    const double sig0 = s->p.sigma0, sigexp = -s->p.sigma_slope;
+	    double v;
+	    if (field == FGPU_SIGMA) {
+		v = sig0 * pow(R, sigexp);
+	    } else {
+		v = 1.0 / (s->p.gamma - 1.0) * sig0 * pow(s->p.aspect_ratio, 2) *
+		    pow(R, sigexp - 1.0 + 2.0 * s->p.flaring_index);
+	    }
+	    AT(x, outer ? irad : 0, j) = v;
+	    break;
+	}
+	case FGPU_BC_REFLECTING:
+	    /* reflecting.cpp:15-40 */
+	    if (!outer) {
+		AT(x, 0, j) = -AT(x, 2, j);
+		AT(x, 1, j) = 0;
+	    } else {
+		AT(x, irad, j) = -AT(x, irad - 2, j);
+		AT(x, irad - 1, j) = 0;
+	    }
+	    break;
+	case FGPU_BC_VISCOUS:
+	    /* viscous_outflow_inner, viscous.cpp:15-40 */
+	    if (!outer) {
+		const double *visc = F(s, FGPU_VISCOSITY);
+		const double sp = s->p.viscous_outflow_speed;
+		const double Nu = 0.5 * (AT(visc, 0, j) + AT(visc, 1, j));
+		AT(x, 1, j) = -1.5 * sp / s->Rinf[1] * Nu;
+		AT(x, 0, j) = -1.5 * sp / s->Rinf[0] * Nu;
+	    }
+	    break;
+	case FGPU_BC_KEPLERIAN_RADIAL: {
+	    /* keplerian_radial.cpp:17-62 */
+	    const double c = outer ? s->p.vrad_outer_keplerian_factor
+				   : s->p.vrad_inner_keplerian_factor;
+	    const int k0 = outer ? irad : 0, k1 = outer ? irad - 1 : 1;
+	    AT(x, k0, j) = c * sqrt(s->p.G * s->p.hydro_center_mass / s->Rmed[k0]);
+	    AT(x, k1, j) = c * sqrt(s->p.G * s->p.hydro_center_mass / s->Rmed[k1]);
+	    break;
+	}
+	case FGPU_BC_ZEROSHEAR: {
+	    /* zero_shear.cpp:19-53 */
+	    const int e = outer ? irad : 0, a = outer ? irad - 1 : 1;
+	    const double Omega_active = AT(x, a, j) / s->Rmed[a];
+	    AT(x, e, j) = s->Rmed[e] * Omega_active;
+	    break;
+	}
+	case FGPU_BC_BALANCED: {
+	    /* balanced_boundary, balanced.cpp:20-66, support_azi_*
+	       Theo.cpp:131-157 (no self-gravity) */
+	    const int e = outer ? irad : 0;
+	    const double R = s->Rmed[e];
+	    const double vk = sqrt(s->p.G * s->p.hydro_center_mass / R);
+	    const double vk_2 = pow(vk, 2);
+	    double support = 0.0;
+	    if (!s->p.profile_cutoff_outer) {
+		const double F = s->p.flaring_index, S = s->p.sigma_slope;
+		const double h = s->p.aspect_ratio * pow(R, F);
+		support += (2.0 * F - 1.0 - S) * pow(h, 2);
+		const double eps = s->p.thickness_smoothing;
+		support += (1.0 + (F + 1.0) * pow(h * eps, 2)) / pow(sqrt(1 + pow(h * eps, 2)), 3);
+	    }
+	    if (s->p.binary_quadrupole_moment > 0.0) {
+		support += 3.0 * s->p.binary_quadrupole_moment / pow(R, 2);
+	    }
+	    double vaz_balanced = sqrt(vk_2 * support);
+	    vaz_balanced -= R * s->omega_frame;
+	    AT(x, e, j) = vaz_balanced;
+	    break;
+	}
 	}
     }
 }
@@ -1071,6 +1144,14 @@ int or_apply_boundary_condition(or_state *s, double t, double dt, int final)
 {
     (void)t;
     const fgpu_params *p = &s->p;
+    if (final && (p->viscous_accretion || p->bc_vrad_inner == FGPU_BC_VISCOUS)) {
+	/* parameters::VISCOUS_ACCRETION (Interpret.cpp:704-707): c_s, H, nu of
+	   the transported state before the final boundary call
+	   (simulation.cpp:232-242, 432-441) */
+	compute_sound_speed(s);
+	compute_scale_height(s);
+	update_viscosity(s);
+    }
     if (final && p->damping) {
 	for (int q = 0; q < 4; ++q) {
 	    damp_one(s, q, 0, dt);
@@ -1544,4 +1625,124 @@ double or_total_mass(or_state *s)
 	for (int j = 0; j < nz; ++j) m += s->Surf[i] * AT(S, i, j);
     }
     return m;
+}
+
+/* ------------------------------------------------------------------ */
+/* accretion::AccreteOntoPlanets for one planet, src/accretion.cpp:21-480 */
+/* ------------------------------------------------------------------ */
+static int med_azimuthal_id(const or_state *s, double phi)
+{
+    /* get_med_azimuthal_id, find_cell_id.cpp:322-345 (init_cell_finder_*:
+       phi_cell_size = 2 pi / Naz, inv_phi_cell_size = Naz / 2 / pi) */
+    const double cell = 2.0 * M_PI / (double)s->nz;
+    const double inv = (double)s->nz / 2.0 / M_PI;
+    return (int)floor((phi - 0.5 * cell) * inv);
+}
+
+int or_accrete_onto_planet(or_state *s, const fgpu_accretor *a, double dt, double out[3])
+{
+    const int nr = s->nr, ns = s->nz;
+    double *dens = F(s, FGPU_SIGMA), *energy = F(s, FGPU_ENERGY);
+    const double *vrad = F(s, FGPU_V_RADIAL), *vazi = F(s, FGPU_V_AZIMUTHAL);
+    const double *nuf = F(s, FGPU_VISCOSITY);
+    const double density_floor = s->p.sigma_floor * s->p.sigma0;
+    const double RHill = a->roche_radius;
+    const double Rplanet = a->r;
+    double frac1, frac2 = 0.0, facc1, facc2 = 0.0, f_const = 0.0, dist_max = 0.0;
+    const double frac = s->p.accretion_radius_fraction;
+    if (a->type == FGPU_ACCRETION_KLEY) {
+	/* AccreteOntoSinglePlanet, :84-221 */
+	const double facc = dt * a->efficiency / a->orbital_period * log(2);
+	facc1 = 1.0 / 3.0 * facc;
+	facc2 = 2.0 / 3.0 * facc;
+	frac1 = frac;
+	frac2 = 0.5 * frac;
+    } else if (a->type == FGPU_ACCRETION_SINKHOLE) {
+	/* SinkHoleSinglePlanet, :223-333 */
+	facc1 = dt * a->efficiency / a->orbital_period * log(2.0);
+	frac1 = frac;
+    } else if (a->type == FGPU_ACCRETION_VISCOUS) {
+	/* AccreteOntoSinglePlanetViscous, :335-480 */
+	facc1 = dt * 3.0 * M_PI * a->efficiency;
+	frac1 = frac;
+	dist_max = RHill * frac;
+	f_const = 3.0 / M_PI / pow(dist_max, 2);
+    } else {
+	return FGPU_ERR_BAD_ARG;
+    }
+    const double search_radius = RHill * frac1 + 2.0 * Rplanet / ns;
+    /* hill_radial_index, :21-38 */
+    int i_min;
+    if (Rplanet - search_radius < s->p.rmin) {
+	i_min = 0;
+    } else {
+	i_min = clamp_id(cell_id_rinf(s, Rplanet - search_radius), 0, nr);
+    }
+    const int i_max = clamp_id(cell_id_rinf(s, Rplanet + search_radius) + 1, 0, nr);
+    /* hill_azimuthal_index, :40-58 */
+    double max_angle;
+    if (Rplanet == 0.0) {
+	max_angle = 2.0 * M_PI;
+    } else {
+	const double m = 2.0 * search_radius / Rplanet;
+	max_angle = m < 2.0 * M_PI ? m : 2.0 * M_PI;
+    }
+    const int j_min = med_azimuthal_id(s, a->phi - max_angle);
+    int j_max = med_azimuthal_id(s, a->phi + max_angle) + 1;
+    j_max = j_min + (j_max - j_min < ns - 1 ? j_max - j_min : ns - 1);
+
+    double dM = 0.0, dPx = 0.0, dPy = 0.0;
+    for (int i = i_min; i <= i_max; i++) {
+	for (int j = j_min; j <= j_max; j++) {
+	    int jf = j;
+	    while (jf < 0) jf += ns;
+	    while (jf >= ns) jf -= ns;
+	    const int l = jf + i * ns;
+	    const int lip = l + ns;
+	    const int ljp = jf == ns - 1 ? i * ns : l + 1;
+	    const double xc = s->Rmed[i] * s->cosj[jf];
+	    const double yc = s->Rmed[i] * s->sinj[jf];
+	    const double dx = a->x - xc;
+	    const double dy = a->y - yc;
+	    const double distance = sqrt(dx * dx + dy * dy);
+	    const double vtcell = 0.5 * (vazi[l] + vazi[ljp]) + s->Rmed[i] * s->omega_frame;
+	    const double vrcell = 0.5 * (vrad[l] + vrad[lip]);
+	    const double vxcell = (vrcell * xc - vtcell * yc) / s->Rmed[i];
+	    const double vycell = (vrcell * yc + vtcell * xc) / s->Rmed[i];
+	    const double facc_max = 1 - density_floor / dens[l];
+	    const int active = 1 < i && i < nr - 1;
+	    if (distance < frac1 * RHill) {
+		double f = facc1;
+		if (a->type == FGPU_ACCRETION_VISCOUS) {
+		    const double spread = f_const * (1.0 - distance / dist_max);
+		    f = facc1 * nuf[l] * spread;
+		}
+		const double fc = facc_max < f ? facc_max : f;
+		const double deltaM = fc * dens[l] * s->Surf[i];
+		dens[l] *= 1.0 - fc;
+		if (adiabatic(s)) energy[l] *= 1.0 - fc;
+		if (active) {
+		    dPx += deltaM * vxcell;
+		    dPy += deltaM * vycell;
+		    dM += deltaM;
+		}
+	    }
+	    if (a->type == FGPU_ACCRETION_KLEY && distance < frac2 * RHill) {
+		const double fc = facc_max < facc2 ? facc_max : facc2;
+		const double deltaM = fc * dens[l] * s->Surf[i];
+		dens[l] *= 1.0 - fc;
+		/* the reference scales the energy by the uncapped factor here */
+		if (adiabatic(s)) energy[l] *= 1.0 - facc2;
+		if (active) {
+		    dPx += deltaM * vxcell;
+		    dPy += deltaM * vycell;
+		    dM += deltaM;
+		}
+	    }
+	}
+    }
+    out[0] = dM;
+    out[1] = dPx;
+    out[2] = dPy;
+    return FGPU_OK;
 }

@@ -42,6 +42,7 @@ void or_gas_kick(or_state *s, double dt, double t);
 void or_compute_pressure(or_state *s);
 int or_disk_on_planet_accel(or_state *s, int k, double accel[2]);
 double or_total_mass(or_state *s);
+int or_accrete_onto_planet(or_state *s, const fgpu_accretor *a, double dt, double out[3]);
 
 /* Sub-steps, exported so tests can check the GPU kernels one phase at a time. */
 void or_calculate_potential(or_state *s);

@@ -13,7 +13,7 @@ import subprocess
 
 import numpy as np
 
-from fargocpt_gb300.abi import FIELDS, VECTOR_FIELDS, FgpuBody, FgpuParams
+from fargocpt_gb300.abi import FIELDS, VECTOR_FIELDS, FgpuAccretor, FgpuBody, FgpuParams
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
@@ -52,6 +52,7 @@ def _load():
     lib.or_disk_on_planet_accel.argtypes = [vp, C.c_int, dp]
     lib.or_total_mass.argtypes = [vp]
     lib.or_total_mass.restype = C.c_double
+    lib.or_accrete_onto_planet.argtypes = [vp, C.POINTER(FgpuAccretor), C.c_double, dp]
     for name in ("or_calculate_potential", "or_viscous_stress_tensor"):
         getattr(lib, name).argtypes = [vp]
     for name in ("or_update_with_sourceterms", "or_artificial_viscosity",
@@ -148,6 +149,13 @@ class OracleState:
 
     def total_mass(self):
         return self.lib.or_total_mass(self.h)
+
+    def accrete_onto_planet(self, accretor, dt):
+        out = (C.c_double * 3)()
+        rc = self.lib.or_accrete_onto_planet(self.h, C.byref(accretor), dt, out)
+        if rc != 0:
+            raise ValueError(rc)
+        return out[0], out[1], out[2]
 
     # phase-by-phase access for kernel tests
     def phase(self, name, *args):

@@ -34,7 +34,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 
-from fargocpt_gb300.abi import BC, DAMP, BETA_REF  # noqa: E402
+from fargocpt_gb300.abi import ACCRETION, BC, DAMP, BETA_REF  # noqa: E402
 
 REF_SRC = os.environ.get("FARGO_REFERENCE_SRC", "/root/reference/src")
 REF_EXE = os.path.join(REPO, "oracle", "_ref", "parity", "fargocpt")
@@ -172,6 +172,94 @@ CASES = {
                   DampingEnergyInner="Reference", DampingEnergyOuter="Reference",
                   MonitorTimestep=0.3, Nsnapshots=3),
         nrad=16, naz=40, rmin=0.4, rmax=2.5, planet=None, keep=[1, 2, 3]),
+    # Accretion onto the planet (accretion.cpp:84-480), Kley's two zones,
+    # locally isothermal, fixed dt; the planet's mass stays fixed
+    # (DiskFeedback no), the accreted mass is in the monitor's accretion rate
+    "iso_planet_accretion_kley": dict(
+        keys=dict(SigmaSlope=0.5, AspectRatio=0.05, FlaringIndex=0.0,
+                  EquationOfState="Isothermal", ViscousAlpha=1e-3,
+                  ArtificialViscosity="SN", Transport="FARGO",
+                  InnerBoundary="outflow", OuterBoundary="reference",
+                  Damping="yes", DampingInnerLimit=1.1, DampingOuterLimit=0.9,
+                  DampingSurfaceDensityInner="Reference",
+                  DampingSurfaceDensityOuter="Reference",
+                  DampingVRadialInner="Reference", DampingVRadialOuter="Reference",
+                  DampingVAzimuthalInner="Reference",
+                  DampingVAzimuthalOuter="Reference",
+                  MassAccretionRadius=2.0, MonitorTimestep=0.002, Nsnapshots=20),
+        nrad=24, naz=64, rmin=0.4, rmax=2.5, planet=3e-3,
+        planet_keys={"accretion efficiency": 10, "accretion method": "kley"},
+        keep=[1, 2, 5, 10, 20]),
+    # sink-hole accretion, adiabatic
+    "adi_planet_accretion_sinkhole": dict(
+        keys=dict(SigmaSlope=1.0, AspectRatio=0.05, FlaringIndex=0.25,
+                  EquationOfState="Ideal", AdiabaticIndex=1.4, ViscousAlpha=1e-3,
+                  ArtificialViscosity="SN", ArtificialViscosityFactor=1.41421356,
+                  CoolingBetaLocal="yes", CoolingBeta=10, Transport="FARGO",
+                  InnerBoundary="zerogradient", OuterBoundary="outflow",
+                  Damping="yes", DampingInnerLimit=1.15, DampingOuterLimit=0.85,
+                  DampingTimeFactor=0.5,
+                  DampingSurfaceDensityInner="Reference",
+                  DampingSurfaceDensityOuter="Reference",
+                  DampingVRadialInner="Reference", DampingVRadialOuter="Reference",
+                  DampingVAzimuthalInner="Reference",
+                  DampingVAzimuthalOuter="Reference",
+                  DampingEnergyInner="Reference", DampingEnergyOuter="Reference",
+                  MassAccretionRadius=1.5, MonitorTimestep=0.002, Nsnapshots=20),
+        nrad=24, naz=64, rmin=0.3, rmax=3.0, planet=3e-3,
+        planet_keys={"accretion efficiency": 5, "accretion method": "sinkhole"},
+        keep=[1, 2, 5, 10, 20]),
+    # viscous accretion profile (M_dot = 3 pi nu Sigma), locally isothermal
+    "iso_planet_accretion_viscous": dict(
+        keys=dict(SigmaSlope=0.5, AspectRatio=0.05, FlaringIndex=0.0,
+                  EquationOfState="Isothermal", ViscousAlpha=1e-2,
+                  ArtificialViscosity="SN", Transport="FARGO",
+                  InnerBoundary="outflow", OuterBoundary="reference",
+                  Damping="yes", DampingInnerLimit=1.1, DampingOuterLimit=0.9,
+                  DampingSurfaceDensityInner="Reference",
+                  DampingSurfaceDensityOuter="Reference",
+                  DampingVRadialInner="Reference", DampingVRadialOuter="Reference",
+                  DampingVAzimuthalInner="Reference",
+                  DampingVAzimuthalOuter="Reference",
+                  MassAccretionRadius=2.0, MonitorTimestep=0.002, Nsnapshots=20),
+        nrad=24, naz=64, rmin=0.4, rmax=2.5, planet=3e-3,
+        planet_keys={"accretion efficiency": 300, "accretion method": "viscous"},
+        keep=[1, 2, 5, 10, 20]),
+    # per-field boundary hooks: disk model, reflecting, zero shear, Keplerian
+    # radial, balanced; locally isothermal, planet, fixed dt, no damping
+    "iso_planet_bc_individual": dict(
+        keys=dict(SigmaSlope=0.5, AspectRatio=0.05, FlaringIndex=0.0,
+                  EquationOfState="Isothermal", ViscousAlpha=1e-3,
+                  ArtificialViscosity="SN", Transport="FARGO",
+                  InnerBoundary="individual", OuterBoundary="individual",
+                  InnerBoundarySigma="diskmodel", InnerBoundaryEnergy="zerogradient",
+                  InnerBoundaryVrad="reflecting", InnerBoundaryVazi="zeroshear",
+                  OuterBoundarySigma="zerogradient", OuterBoundaryEnergy="zerogradient",
+                  OuterBoundaryVrad="keplerian", OuterBoundaryVradKeplerianFactor=0.05,
+                  OuterBoundaryVazi="balanced",
+                  Damping="no", DampingInnerLimit=1.1, DampingOuterLimit=0.9,
+                  MonitorTimestep=0.002, Nsnapshots=20),
+        nrad=20, naz=48, rmin=0.4, rmax=2.5, planet=1e-3, keep=[1, 2, 5, 10, 20]),
+    # viscous outflow at the inner edge, balanced inner, zero-shear outer,
+    # disk-model sigma and energy; adiabatic, CFL-limited, damping on
+    "adi_star_cfl_bc_individual": dict(
+        keys=dict(SigmaSlope=1.0, AspectRatio=0.05, FlaringIndex=0.25,
+                  EquationOfState="Ideal", AdiabaticIndex=1.4, ViscousAlpha=1e-2,
+                  ArtificialViscosity="SN", CoolingBetaLocal="yes", CoolingBeta=10,
+                  Transport="FARGO",
+                  InnerBoundary="individual", OuterBoundary="individual",
+                  InnerBoundarySigma="reference", InnerBoundaryEnergy="diskmodel",
+                  InnerBoundaryVrad="viscous", InnerBoundaryVazi="balanced",
+                  OuterBoundarySigma="diskmodel", OuterBoundaryEnergy="diskmodel",
+                  OuterBoundaryVrad="reflecting", OuterBoundaryVazi="zeroshear",
+                  ViscousOutflowSpeed=2.0,
+                  Damping="yes", DampingInnerLimit=1.1, DampingOuterLimit=0.9,
+                  DampingSurfaceDensityInner="Reference",
+                  DampingSurfaceDensityOuter="Reference",
+                  DampingVRadialInner="Reference", DampingVRadialOuter="Reference",
+                  DampingEnergyInner="Reference", DampingEnergyOuter="Reference",
+                  MonitorTimestep=0.4, Nsnapshots=4),
+        nrad=16, naz=40, rmin=0.3, rmax=3.0, planet=None, keep=[1, 2, 3, 4]),
     # TW with the viscous stability dt limit (StabilizeViscosity 2), locally
     # isothermal, a viscosity-dominated CFL so that the limit binds
     "iso_star_cfl_tw_stab2": dict(
@@ -226,8 +314,28 @@ def engine_params(case, consts, temp_unit):
                 "outflow": ("zerogradient", "zerogradient", "outflow"),
                 "reference": ("reference", "reference", "reference")}[name]
 
-    si, ei, vi = composite(inner)
-    so, eo, vo = composite(outer)
+    def side_names(side, comp):
+        # per-field names after the composite and the individual keys
+        # (config.cpp:75-96, 345-440); the inner energy hook reads and
+        # overwrites the outer name (config.cpp:147)
+        names = dict(zip(("sigma", "energy", "vrad"),
+                         composite(comp) if comp != "individual" else ("", "", "")))
+        for key, fld in (("Sigma", "sigma"), ("Vrad", "vrad")):
+            if f"{side}Boundary{key}" in k:
+                names[fld] = str(k[f"{side}Boundary{key}"]).lower()
+        names["vazi"] = str(k.get(f"{side}BoundaryVazi", "keplerian")).lower()
+        return names
+
+    nin, nout = side_names("Inner", inner), side_names("Outer", outer)
+    energy_outer_name = nout["energy"]
+    if "InnerBoundaryEnergy" in k:
+        energy_outer_name = str(k["InnerBoundaryEnergy"]).lower()
+    ei = energy_outer_name
+    eo = str(k.get("OuterBoundaryEnergy", energy_outer_name)).lower()
+    si, vi, so, vo = nin["sigma"], nin["vrad"], nout["sigma"], nout["vrad"]
+
+    def vrad_kind(name):
+        return BC["keplerian_radial"] if name == "keplerian" else BC[name]
 
     def damp(key):
         v = str(k.get(key, "None")).lower()[0]
@@ -246,11 +354,15 @@ def engine_params(case, consts, temp_unit):
         damping_outer=[damp("DampingVRadialOuter"), damp("DampingVAzimuthalOuter"),
                        damp("DampingSurfaceDensityOuter"), damp("DampingEnergyOuter")],
         bc_sigma_inner=BC[si], bc_sigma_outer=BC[so],
-        # energy_inner reads the outer composite's name (config.cpp:146)
-        bc_energy_inner=BC[eo], bc_energy_outer=BC[eo],
-        bc_vrad_inner=BC[vi], bc_vrad_outer=BC[vo],
-        bc_vaz_inner=BC["keplerian"], bc_vaz_outer=BC["keplerian"],
+        bc_energy_inner=BC[ei], bc_energy_outer=BC[eo],
+        bc_vrad_inner=vrad_kind(vi), bc_vrad_outer=vrad_kind(vo),
+        bc_vaz_inner=BC[nin["vazi"]], bc_vaz_outer=BC[nout["vazi"]],
+        sigma_slope=float(k["SigmaSlope"]),
+        viscous_outflow_speed=float(k.get("ViscousOutflowSpeed", 1.0)),
+        vrad_inner_keplerian_factor=float(k.get("InnerBoundaryVradKeplerianFactor", 0.1)),
+        vrad_outer_keplerian_factor=float(k.get("OuterBoundaryVradKeplerianFactor", 0.1)),
         precision=0,
+        accretion_radius_fraction=float(k.get("MassAccretionRadius", 1.0)),
         integrator=1 if str(k.get("Integrator", "Euler")).lower().startswith("l") else 0,
         gamma=float(k.get("AdiabaticIndex", 1.4)), mu=float(k["mu"]),
         aspect_ratio=float(k["AspectRatio"]), flaring_index=float(k["FlaringIndex"]),
@@ -296,6 +408,8 @@ def write_setup(case, path, seed):
     if case["planet"] is not None:
         lines.append(f"- name: planet\n  semi-major axis: 1.0\n  mass: {case['planet']}\n"
                      "  eccentricity: 0.0")
+        for key, v in case.get("planet_keys", {}).items():
+            lines.append(f"  {key}: {v}")
     text = "\n".join(lines) + "\n"
     with open(os.path.join(path, "setup.yml"), "w") as f:
         f.write(text)
@@ -320,8 +434,10 @@ def read_nbody(out, k):
         rows.append([float(x) for x in line.split()])
     a = np.array(rows)
     # columns (nbody/planet.cpp:361-372): snapshot, monitor, x, y, vx, vy,
-    # mass, time, omega_frame, ..., torque (18)
-    return dict(x=a[:, 2], y=a[:, 3], mass=a[:, 6], time=a[:, 7], torque=a[:, 18])
+    # mass, time, omega_frame, ..., torque (18), accretion torque (19),
+    # indirect torque (20), accretion rate (21)
+    return dict(x=a[:, 2], y=a[:, 3], vx=a[:, 4], vy=a[:, 5], mass=a[:, 6], time=a[:, 7],
+                torque=a[:, 18], accretion_rate=a[:, 21])
 
 
 def make_case(name, case, seed):
@@ -359,6 +475,10 @@ def make_case(name, case, seed):
                     monitor_timestep=float(case["keys"]["MonitorTimestep"]),
                     nsnapshots=int(case["keys"]["Nsnapshots"]), nbodies=nb,
                     seed=seed, reference_log_tail=r.stdout.splitlines()[-1])
+        if case.get("planet_keys"):
+            pk = case["planet_keys"]
+            meta["accretion"] = dict(type=ACCRETION[pk["accretion method"]],
+                                     efficiency=float(pk["accretion efficiency"]))
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **arrays)
         with open(os.path.join(HERE, f"{name}.json"), "w") as f:
             json.dump(meta, f, indent=1, sort_keys=True)

@@ -12,13 +12,17 @@ import os
 
 import numpy as np
 
-from fargocpt_gb300.abi import params_from_dict
-from fargocpt_gb300.simulation import RunClock, advance, indirect_term_euler, start
+from fargocpt_gb300.abi import FgpuAccretor, params_from_dict
+from fargocpt_gb300.simulation import (RunClock, advance, indirect_term_euler, l1_point,
+                                       orbital_period, start)
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = ["iso_planet_fixed_dt", "adi_planet_fixed_dt", "iso_star_cfl",
          "adi_star_cfl_mc_std", "iso_star_cfl_leapfrog", "adi_star_cfl_leapfrog",
-         "adi_planet_tw", "adi_star_cfl_tw_stab1", "iso_star_cfl_tw_stab2"]
+         "adi_planet_tw", "adi_star_cfl_tw_stab1", "iso_star_cfl_tw_stab2",
+         "iso_planet_accretion_kley", "adi_planet_accretion_sinkhole",
+         "iso_planet_accretion_viscous", "iso_planet_bc_individual",
+         "adi_star_cfl_bc_individual"]
 EVOLVED = ["SIGMA", "V_RADIAL", "V_AZIMUTHAL", "ENERGY"]
 
 
@@ -39,8 +43,32 @@ def bodies_at(arrays, nb, row):
     return out
 
 
-def replay(make_backend, name, params_override=None):
-    """Runs the case; returns (snapshots, times, torques, dts)."""
+def accretor_at(arrays, meta, row):
+    """The planet (body 1) as AccreteOntoPlanets sees it at the start of the
+    step after monitor row `row`: position, Roche radius (init_l1 times the
+    distance to the star, planetary_system.cpp:940-1004) and orbital period
+    (calculate_orbital_elements about the star, planetary_system.cpp:773-793)."""
+    b = {k: float(arrays[f"body1_{k}"][row]) for k in ("x", "y", "vx", "vy", "mass")}
+    s = {k: float(arrays[f"body0_{k}"][row]) for k in ("x", "y", "vx", "vy", "mass")}
+    G = float(meta["params"]["G"])
+    # get_center_of_mass(1) / get_center_of_mass_velocity(1) of the star alone
+    cx, cy = (0.0 + s["x"] * s["mass"]) / s["mass"], (0.0 + s["y"] * s["mass"]) / s["mass"]
+    cvx = (0.0 + s["vx"] * s["mass"]) / s["mass"]
+    cvy = (0.0 + s["vy"] * s["mass"]) / s["mass"]
+    period = orbital_period(b["x"] - cx, b["y"] - cy, b["vx"] - cvx, b["vy"] - cvy,
+                            0.0 + s["mass"], b["mass"], G)
+    dist = math.sqrt(math.pow(b["x"] - s["x"], 2) + math.pow(b["y"] - s["y"], 2))
+    acc = meta["accretion"]
+    return FgpuAccretor(type=int(acc["type"]), x=b["x"], y=b["y"],
+                        r=math.hypot(b["x"], b["y"]), phi=math.atan2(b["y"], b["x"]),
+                        roche_radius=l1_point(s["mass"], b["mass"]) * dist,
+                        efficiency=float(acc["efficiency"]), orbital_period=period)
+
+
+def replay(make_backend, name, params_override=None, accreted=None):
+    """Runs the case; returns (snapshots, times, torques, dts).  With
+    accreted (a dict), the mass each monitor interval accreted is added to
+    accreted[monitor]."""
     meta, arrays = load_case(name)
     pd = dict(meta["params"])
     if params_override:
@@ -90,11 +118,19 @@ def replay(make_backend, name, params_override=None):
         if c.n_monitor in keep:
             snaps[c.n_monitor] = {f: hyd.get_field(f) for f in EVOLVED}
 
+    accrete = None
+    if "accretion" in meta:
+        def accrete(c, dt):
+            dm, _, _ = hyd.accrete_onto_planet(accretor_at(arrays, meta, c.n_monitor), dt)
+            if accreted is not None:
+                accreted[c.n_monitor + 1] = accreted.get(c.n_monitor + 1, 0.0) + dm
+
     t_final = meta["nsnapshots"] * 1 * meta["monitor_timestep"]
     advance(hyd, clock, cfl_max_var=cmv, monitor_timestep=meta["monitor_timestep"],
             t_final=t_final, bodies=lambda c: body_state(c.n_monitor),
             on_monitor=on_monitor,
-            integrator="leapfrog" if int(pd.get("integrator", 0)) == 1 else "euler")
+            integrator="leapfrog" if int(pd.get("integrator", 0)) == 1 else "euler",
+            accrete=accrete)
     return snaps, times, torques, clock.dts, arrays
 
 

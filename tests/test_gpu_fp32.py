@@ -29,9 +29,12 @@ def rel_l1(a, b):
 
 
 def _fp32_case(name):
-    # TW artificial viscosity and StabilizeViscosity run in the FP64 form only
-    params = load_case(name)[0]["params"]
-    return params.get("art_visc") != 2 and not params.get("stabilize_viscosity")
+    # TW artificial viscosity, StabilizeViscosity and accretion run in the
+    # FP64 form only
+    meta = load_case(name)[0]
+    params = meta["params"]
+    return (params.get("art_visc") != 2 and not params.get("stabilize_viscosity")
+            and "accretion" not in meta)
 
 
 @pytest.mark.parametrize("name", [c for c in CASES if _fp32_case(c)])

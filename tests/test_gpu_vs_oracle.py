@@ -127,3 +127,38 @@ def test_tw_artificial_viscosity_and_stabilize(adiabatic, stabilize):
     for f in EVOLVED:
         err = rel_linf(g.get_field(f), o.get_field(f))
         assert err <= TOL, f"{f}: {err:.3e}"
+
+
+@pytest.mark.parametrize("kind", ["kley", "sinkhole", "viscous"])
+def test_accretion_onto_planet(kind):
+    """AccreteOntoPlanets (accretion.cpp:84-480) on a 64 x 192 adiabatic disk:
+    the removed mass and momentum (relative 1e-12) and the fields after
+    accretion plus a step."""
+    from fargocpt_gb300.abi import ACCRETION, FgpuAccretor
+    from fargocpt_gb300.engine import Engine, grid_radii
+    from oracle.oracle_py import OracleState
+
+    params, d = make_params(64, 192, adiabatic=True, accretion_radius_fraction=1.5)
+    radii = grid_radii(d["radial_spacing"], d["rmin"], d["rmax"], d["nrad"])
+    st = initial_state(d, radii, seed=7)
+    x, y = 1.05 * math.cos(0.3), 1.05 * math.sin(0.3)
+    bodies = [(0.0, 0.0, 1.0, 0.0, 0.0), (x, y, 3e-3, 0.0, 1.05)]
+    acc = FgpuAccretor(type=ACCRETION[kind], x=x, y=y, r=math.hypot(x, y),
+                       phi=math.atan2(y, x), roche_radius=0.1 * 1.05,
+                       efficiency={"kley": 10.0, "sinkhole": 5.0, "viscous": 300.0}[kind],
+                       orbital_period=2 * math.pi * 1.05 ** 1.5)
+    res = []
+    for cls in (OracleState, Engine):
+        h = cls(params, radii)
+        load(h, st, bodies)
+        h.apply_boundary_condition(0.0, 0.0, False)
+        dt = h.condition_cfl()
+        sums = h.accrete_onto_planet(acc, dt)
+        h.step_euler(dt, 0.0)
+        res.append((h, sums))
+    (o, so), (g, sg) = res
+    assert so[0] > 0
+    np.testing.assert_allclose(sg, so, rtol=1e-12, atol=1e-14 * abs(so[0]))
+    for f in EVOLVED:
+        err = rel_linf(g.get_field(f), o.get_field(f))
+        assert err <= TOL, f"{f}: {err:.3e}"

@@ -43,3 +43,22 @@ def test_step_counts_follow_cfl():
     assert len(dts) == 22
     _, _, _, dts, _ = replay(OracleState, "adi_star_cfl_leapfrog")
     assert len(dts) == 32
+
+
+@pytest.mark.parametrize("name", [c for c in CASES if "accretion" in c])
+def test_oracle_accreted_mass_matches_reference_monitor(name):
+    # The reference writes accreted mass / monitor interval as the planet's
+    # accretion rate (nbody/planet.cpp:357-369).
+    accreted = {}
+    snaps, _, _, _, arrays = replay(OracleState, name, accreted=accreted)
+    rate = arrays["body1_accretion_rate"]
+    from golden_runner import load_case
+    dt_mon = load_case(name)[0]["monitor_timestep"]
+    assert len(accreted) == len(rate) - 1
+    for n, m in accreted.items():
+        assert m > 0
+        assert abs(m / dt_mon - rate[n]) <= 1e-12 * rate[n], (n, m / dt_mon, rate[n])
+    # and the accretion is visible in the fields
+    plain, _, _, _, _ = replay(OracleState, name, {"accretion_radius_fraction": 0.0})
+    last = max(snaps)
+    assert rel_linf(plain[last]["SIGMA"], snaps[last]["SIGMA"]) > 1e-4
