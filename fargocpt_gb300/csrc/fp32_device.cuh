@@ -803,19 +803,15 @@ __device__ __forceinline__ void ring_pass_f(float *S, float *SS, float *W, float
 // differences first keeps FP32's rounding at the size of the changes, where
 // the flux form rounds at the size of the fluxes, up to half of the ring's
 // content per step, and repeats the same rounding pattern every step.
-// dS* and S*_{j+1} go to the SS and F arrays (unused by this pass).
+// dS* and S*_{j+1} go to the SS and F arrays (unused by this pass); c is
+// dxrad v invsurf and a the interpolation distance.
 template <int PER, int NQ>
 __device__ __forceinline__ void ring_pass_uniform_f(float *S, float *SS, float *W, float *D,
                                                     float *F, float *const *qrow, float *slo,
-                                                    float dt, float dxtheta, float half_invdx,
-                                                    float dxrad, float invsurf, int nz, int mc,
-                                                    float vconst)
+                                                    bool pos, float a, float c, float half_invdx,
+                                                    int nz, int mc)
 {
     const int tid = threadIdx.x, bs = blockDim.x;
-    const float ksi = vconst * dt;
-    const bool pos = ksi > 0.f;
-    const float a = pos ? dxtheta - ksi : -(dxtheta + ksi);
-    const float c = dxrad * vconst * invsurf;
     float invs[PER];
 #pragma unroll
     for (int n = 0; n < PER; ++n) {
@@ -955,8 +951,11 @@ __device__ __forceinline__ void azimuthal_ring(const GeoF &g, const TablesF &t, 
     ring_pass_f<PER, NQ>(Sr, SS, W, D, Fx, qrow, vown, slo, (float)dt, dxtheta, half_invdx,
                          dxrad, invsurf, nz, mc, false, 0.f);
     if (fast) {
-        ring_pass_uniform_f<PER, NQ>(Sr, SS, W, D, Fx, qrow, slo, (float)dt, dxtheta, half_invdx,
-                                     dxrad, invsurf, nz, mc, vt);
+        const float ksi = vt * (float)dt;
+        const bool pos = ksi > 0.f;
+        ring_pass_uniform_f<PER, NQ>(Sr, SS, W, D, Fx, qrow, slo, pos,
+                                     pos ? dxtheta - ksi : -(dxtheta + ksi),
+                                     dxrad * vt * invsurf, half_invdx, nz, mc);
     }
     // the integer shift (AdvectSHIFT, :238-268): cell j takes cell j - nshift
     const int ns = nshift % nz;

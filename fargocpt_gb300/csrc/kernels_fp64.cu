@@ -59,6 +59,19 @@ __device__ __forceinline__ double fast_rcp(double b)
 }
 __device__ __forceinline__ double fast_div(double a, double b) { return a * fast_rcp(b); }
 
+// The same with one Newton-Raphson iteration: the hardware seed is within
+// 2^-20 of 1/b (measured on GB300 over 61 binades), so one iteration leaves
+// a relative error below 2^-40.  Used for the van Leer slope only, where that
+// error scales a slope correction that is itself a small part of the
+// interface value.
+__device__ __forceinline__ double fast_rcp1(double b)
+{
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(b));
+    const double e = fma(-b, r, 1.0);
+    return fma(r, e, r);
+}
+
 // van_leer_lim / MC_lim, src/TransportEuler.cpp:306-337
 __device__ __forceinline__ double flux_limiter(double a, double b, int mc)
 {
@@ -68,7 +81,7 @@ __device__ __forceinline__ double flux_limiter(double a, double b, int mc)
         if (same_sign_nonzero(c, d)) return abs_less(c, d) ? c : d;
         return 0.0;
     }
-    if (same_sign_nonzero(a, b)) return fast_div(2.0 * a * b, a + b);
+    if (same_sign_nonzero(a, b)) return 2.0 * a * b * fast_rcp1(a + b);
     return 0.0;
 }
 
@@ -673,18 +686,22 @@ __global__ void k_transport_radial(Geo g, Tables t, double dt, double omf, int m
                 double sstar;
                 const bool up = positive(v);
                 // DensityStar, then QRStar of every specific quantity
+                // base sigma* v, the factor every quantity's flux shares
                 if (up) {
                     const double f = (t.Rmed[k] - t.Rmed[k - 1] - vdt) * 0.5;
                     sstar = wa[NQ] + f * da[NQ];
+                    const double bsv = base * sstar * v;
 #pragma unroll
-                    for (int q = 0; q < NQ; ++q) flux[q] = base * (wa[q] + f * da[q]) * sstar * v;
+                    for (int q = 0; q < NQ; ++q) flux[q] = (wa[q] + f * da[q]) * bsv;
+                    flux[NQ] = bsv;
                 } else {
                     const double f = (t.Rmed[k + 1] - t.Rmed[k] + vdt) * 0.5;
                     sstar = wb[NQ] - f * db[NQ];
+                    const double bsv = base * sstar * v;
 #pragma unroll
-                    for (int q = 0; q < NQ; ++q) flux[q] = base * (wb[q] - f * db[q]) * sstar * v;
+                    for (int q = 0; q < NQ; ++q) flux[q] = (wb[q] - f * db[q]) * bsv;
+                    flux[NQ] = bsv;
                 }
-                flux[NQ] = base * sstar * v;
             }
             if (k > i0) {
                 // VanLeerRadial update of ring k-1 (:586-591)
@@ -784,9 +801,10 @@ __device__ double block_min(double v, double *red)
 // (TransportEuler.cpp:270-288): ring mean, ComputeConstantResidual (:207-236),
 // QuantitiesAdvection with the residual then the uniform velocity (:292-304,
 // ComputeStarTheta :416-466, VanLeerTheta :630-664) and AdvectSHIFT
-// (:238-268).  One CTA owns one ring; the ring's sigma, sigma*, velocity,
-// specific quantity and slopes live in shared memory (or in a per-ring global
-// workspace when the ring is too long for shared memory).
+// (:238-268).  One CTA owns one ring; the ring's sigma, specific quantity
+// and slopes live in shared memory (3 x naz doubles, up to 9386 cells; a
+// per-ring global workspace stands in beyond that).  The face factor
+// dxrad S* v / Surf that every quantity's flux shares is formed once per face.
 // ---------------------------------------------------------------------------
 // Each thread owns the cells j = threadIdx.x + n * blockDim.x, n < PER.
 
@@ -796,10 +814,10 @@ __device__ double block_min(double v, double *red)
 // sigma on entry and its advected value on exit.  v[n] is the owned cells'
 // velocity (ignored when uniform).
 template <int PER>
-__device__ void ring_advection_pass(double *S, double *SS, double *W, double *D,
-                                    double *const *qrow, int nq, const double *v, double dt,
-                                    double dxtheta, double half_invdx, double dxrad,
-                                    double invsurf, int nz, int mc, bool uniform, double vconst)
+__device__ void ring_advection_pass(double *S, double *W, double *D, double *const *qrow,
+                                    int nq, const double *v, double dt, double dxtheta,
+                                    double half_invdx, double dxrad_invsurf, int nz, int mc,
+                                    bool uniform, double vconst)
 {
     const int tid = threadIdx.x, bs = blockDim.x;
     double invs[PER], f[PER];
@@ -815,6 +833,9 @@ __device__ void ring_advection_pass(double *S, double *SS, double *W, double *D,
         }
     }
     __syncthreads();
+    // per face: the star density and dxrad S* v / Surf, the factor every
+    // quantity's flux shares
+    double cf[PER];
 #pragma unroll
     for (int n = 0; n < PER; ++n) {
         const int j = tid + n * bs;
@@ -822,7 +843,9 @@ __device__ void ring_advection_pass(double *S, double *SS, double *W, double *D,
             const int jm = j == 0 ? nz - 1 : j - 1;
             const double vv = uniform ? vconst : v[n];
             const double ksi = vv * dt;
-            SS[j] = positive(vv) ? S[jm] + (dxtheta - ksi) * D[jm] : S[j] - (dxtheta + ksi) * D[j];
+            const double ss =
+                positive(vv) ? S[jm] + (dxtheta - ksi) * D[jm] : S[j] - (dxtheta + ksi) * D[j];
+            cf[n] = dxrad_invsurf * ss * vv;
         }
     }
     __syncthreads();
@@ -853,7 +876,7 @@ __device__ void ring_advection_pass(double *S, double *SS, double *W, double *D,
                 const double ksi = vv * dt;
                 const double qs = positive(vv) ? W[jm] + (dxtheta - ksi) * D[jm]
                                                : W[j] - (dxtheta + ksi) * D[j];
-                f[n] = dxrad * qs * SS[j] * vv;
+                f[n] = qs * cf[n];
             }
         }
         __syncthreads();
@@ -868,7 +891,7 @@ __device__ void ring_advection_pass(double *S, double *SS, double *W, double *D,
             const int j = tid + n * bs;
             if (j < nz) {
                 const int jp = j == nz - 1 ? 0 : j + 1;
-                Q[j] += (W[j] - W[jp]) * invsurf;
+                Q[j] += W[j] - W[jp];
             }
         }
         __syncthreads();
@@ -877,7 +900,7 @@ __device__ void ring_advection_pass(double *S, double *SS, double *W, double *D,
 #pragma unroll
     for (int n = 0; n < PER; ++n) {
         const int j = tid + n * bs;
-        if (j < nz) W[j] = dxrad * SS[j] * (uniform ? vconst : v[n]);
+        if (j < nz) W[j] = cf[n];
     }
     __syncthreads();
 #pragma unroll
@@ -885,7 +908,7 @@ __device__ void ring_advection_pass(double *S, double *SS, double *W, double *D,
         const int j = tid + n * bs;
         if (j < nz) {
             const int jp = j == nz - 1 ? 0 : j + 1;
-            f[n] = S[j] + (W[j] - W[jp]) * invsurf;
+            f[n] = S[j] + (W[j] - W[jp]);
         }
     }
     __syncthreads();
@@ -910,8 +933,8 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(Geo g, Tables t, do
     const int i = blockIdx.x;
     const int tid = threadIdx.x, bs = blockDim.x;
     const size_t row = (size_t)i * nz;
-    double *base = ring_ws ? ring_ws + (size_t)i * 4 * nz : smem;
-    double *Sr = base, *SS = base + nz, *W = base + 2 * nz, *D = base + 3 * nz;
+    double *base = ring_ws ? ring_ws + (size_t)i * 3 * nz : smem;
+    double *Sr = base, *W = base + nz, *D = base + 2 * nz;
 
     // compute_average_azimuthal_velocity, :174-189
     double vown[PER];
@@ -948,11 +971,11 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(Geo g, Tables t, do
     const double half_invdx = 0.5 * (1.0 / dxtheta);
     const double dxrad = (t.Rsup[i] - t.Rinf[i]) * dt;
     const double invsurf = t.InvSurf[i];
-    ring_advection_pass<PER>(Sr, SS, W, D, qrow, nq, vown, dt, dxtheta, half_invdx, dxrad,
-                             invsurf, nz, mc, false, 0.0);
+    ring_advection_pass<PER>(Sr, W, D, qrow, nq, vown, dt, dxtheta, half_invdx,
+                             dxrad * invsurf, nz, mc, false, 0.0);
     if (fast) {
-        ring_advection_pass<PER>(Sr, SS, W, D, qrow, nq, vown, dt, dxtheta, half_invdx, dxrad,
-                                 invsurf, nz, mc, true, vt);
+        ring_advection_pass<PER>(Sr, W, D, qrow, nq, vown, dt, dxtheta, half_invdx,
+                                 dxrad * invsurf, nz, mc, true, vt);
     }
     // AdvectSHIFT of every quantity, sigma last
     for (int q = 0; q <= nq; ++q) {
@@ -1072,6 +1095,78 @@ __global__ void k_damping(Geo g, Damping dm, double dt, const int *__restrict__ 
 // mode bit 1: derived quantities (bit 2: include T, c_s, H for init),
 // bit 4: CFL.
 // ---------------------------------------------------------------------------
+// The CFL time step of one cell in FP32, to screen the cells whose FP64 dt
+// can be the ring's minimum.  The differences that cancel (v_phi - mean,
+// the velocity jumps, Q+ - Q-) are taken in FP64 by the caller; the values
+// reach FP32 by truncating their FP64 bits to 20 mantissa bits on the integer
+// pipe (no FP64 instruction), so every term, and the result, is within
+// 2^-19 of its FP64 value.
+struct CflRing32 {
+    float inv_cell, inv_cell2, inv_drsup, inv_dxtheta, inv_rmed, invdphi, four_C2, inv_hc, cfl;
+};
+
+__device__ __forceinline__ float dtrunc_f(double x)
+{
+    const int hi = __double2hiint(x);
+    const int em = ((hi >> 20) & 0x7ff) - 1023 + 127;
+    if (em <= 0) return 0.f;
+    if (em >= 255) return __int_as_float((hi & 0x80000000) | 0x7f800000);
+    return __int_as_float((hi & 0x80000000) | (em << 23) | ((hi & 0xfffff) << 3));
+}
+
+__device__ __forceinline__ float cfl_cell32(const CflRing32 &t, const Phys &ph, int sn,
+                                            double c_s, double n, double vr0, double vr1,
+                                            double va, double va1, double vm0, double qp,
+                                            double qm, double e, double cphi, double cr)
+{
+    const float vres = dtrunc_f(ph.fast_transport ? va - vm0 : va);
+    const float i1 = dtrunc_f(c_s) * t.inv_cell;
+    const float i2 = dtrunc_f(vr0) * t.inv_drsup;
+    const float i3 = vres * t.inv_dxtheta;
+    float i4;
+    if (sn) {
+        const float dvR = dtrunc_f(vr0 - vr1), dvA = dtrunc_f(va - va1);
+        i4 = t.four_C2 * fmaxf(fmaxf(dvR, 0.f) * t.inv_drsup, fmaxf(dvA, 0.f) * t.inv_dxtheta);
+    } else {
+        const float eps_rr = dtrunc_f(vr1 - vr0) * t.inv_drsup;
+        const float eps_pp =
+            t.inv_rmed * (dtrunc_f(va1 - va) * t.invdphi + 0.5f * (dtrunc_f(vr1) + dtrunc_f(vr0)));
+        i4 = t.four_C2 * fmaxf(-(eps_rr + eps_pp), 0.f);
+    }
+    float i5 = 4.f * dtrunc_f(n) * t.inv_cell2;
+    float i6 = 0.f;
+    if (ph.adiabatic) i6 = t.inv_hc * fabsf(dtrunc_f(qp - qm) / dtrunc_f(e));
+    if (ph.leapfrog) {
+        i4 *= 0.6f;
+        i5 *= 0.6f;
+        i6 *= 0.6f;
+    }
+    const float sum = i1 * i1 + i2 * i2 + i3 * i3 + i4 * i4 + i5 * i5 + i6 * i6;
+    float d = t.cfl / sqrtf(sum);
+    if (ph.stabilize == 2) {
+        const float fc = fminf(dtrunc_f(cphi), dtrunc_f(cr));
+        if (fc != 0.f) d = fminf(d, -t.cfl / fc);
+    }
+    return d;
+}
+
+__device__ __forceinline__ float block_min_f(float v, float *red)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_down_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        float x = lane < nw ? red[lane] : 3.0e38f;
+        for (int o = 16; o > 0; o >>= 1) x = fminf(x, __shfl_down_sync(0xffffffffu, x, o));
+        if (lane == 0) red[32] = x;
+    }
+    __syncthreads();
+    return red[32];
+}
+
 __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const double *__restrict__ S,
                               const double *__restrict__ E, const double *__restrict__ vr,
                               const double *__restrict__ vaz, const double *__restrict__ qplus,
@@ -1083,8 +1178,20 @@ __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const 
                               unsigned long long *__restrict__ dt_min)
 {
     __shared__ double red[33];
+    __shared__ float redf[33];
     const int nz = g.nz, nr = g.nr;
     const int i = blockIdx.x;
+    float local32 = 3.0e38f;
+    CflRing32 t32;
+    t32.inv_cell = (float)t.InvCell[i];
+    t32.inv_cell2 = (float)t.InvCell2[i];
+    t32.inv_drsup = (float)t.InvDiffRsup[i];
+    t32.inv_dxtheta = (float)t.InvDxTheta[i];
+    t32.inv_rmed = (float)t.InvRmed[i];
+    t32.invdphi = (float)g.invdphi;
+    t32.four_C2 = (float)ph.four_C2;
+    t32.inv_hc = (float)ph.inv_hc_limit;
+    t32.cfl = (float)ph.cfl;
     const size_t row = (size_t)i * nz;
     const bool do_cfl = (mode & 4) != 0;
     double vm0 = 0.0, vm1 = 0.0;
@@ -1142,6 +1249,34 @@ __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const 
             n = nu[c];
         }
         if (cfl_ring) {
+            const float d32 = cfl_cell32(t32, ph, sn, c_s, n, vr[c], vr[c + nz], vaz[c],
+                                         vaz[row + (j == nz - 1 ? 0 : j + 1)], vm0,
+                                         ph.adiabatic ? qplus[c] : 0.0,
+                                         ph.adiabatic ? qminus[c] : 0.0,
+                                         ph.adiabatic ? E[c] : 1.0,
+                                         ph.stabilize == 2 ? corr_phi[c] : 0.0,
+                                         ph.stabilize == 2 ? corr_r[c] : 0.0);
+            local32 = fminf(local32, d32);
+        }
+    }
+    if (cfl_ring) {
+        // the FP64 dt of the cells the FP32 screen puts within 2^-15 of the
+        // ring's FP32 minimum; that set holds the FP64 minimum, since the
+        // screen's error is below 2^-19
+        const float ringmin = block_min_f(local32, redf);
+        const float thr = ringmin * (1.0f + 0x1p-15f);
+        for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+            const size_t c = row + j;
+            const double c_s = ((mode & 1) && !ph.adiabatic) ? t.CsIso[i] : cs[c];
+            const double n = nu[c];
+            const float d32 = cfl_cell32(t32, ph, sn, c_s, n, vr[c], vr[c + nz], vaz[c],
+                                         vaz[row + (j == nz - 1 ? 0 : j + 1)], vm0,
+                                         ph.adiabatic ? qplus[c] : 0.0,
+                                         ph.adiabatic ? qminus[c] : 0.0,
+                                         ph.adiabatic ? E[c] : 1.0,
+                                         ph.stabilize == 2 ? corr_phi[c] : 0.0,
+                                         ph.stabilize == 2 ? corr_r[c] : 0.0);
+            if (!(d32 <= thr)) continue;
             const double va = vaz[c];
             const double vres = ph.fast_transport ? va - vm0 : va;
             const double invdt1 = c_s * t.InvCell[i];
@@ -1420,7 +1555,7 @@ void launch_transport_radial(const Launch &L, double dt, double omf, int chunk, 
     }
 }
 
-size_t azimuthal_smem_bytes(int nz) { return (size_t)4 * nz * sizeof(double); }
+size_t azimuthal_smem_bytes(int nz) { return (size_t)3 * nz * sizeof(double); }
 
 // Cells per thread of the azimuthal kernel: blocks stay at <= 512 threads so
 // that the per-thread cell arrays fit 128 registers.

@@ -1,8 +1,8 @@
 """GPU FP64 path against the oracle on synthetic disks larger than the
 reference fixtures: noisy power-law disks, a planet, CFL-limited steps.
 Bar: relative L-infinity <= 1e-10 per evolved field after the run, same CFL
-dt sequence to 1e-12.  Also covers the shared-memory (> 48 KB) and the global
-ring-workspace variants of the azimuthal transport kernel."""
+dt sequence to 1e-12.  Also covers the azimuthal transport kernel with the
+ring in more than 48 KB of shared memory and at 16 cells per thread."""
 import math
 
 import numpy as np
@@ -56,8 +56,8 @@ def test_gpu_vs_oracle_cfl_steps(adiabatic, nrad, naz):
 
 @pytest.mark.parametrize("naz", [1536, 7680])
 def test_azimuthal_kernel_variants(naz):
-    # naz = 1536 runs the ring in > 48 KB of shared memory, 7680 in the
-    # global per-ring workspace
+    # naz = 1536 runs the ring in > 48 KB of shared memory, 7680 in 180 KB
+    # (one block per SM, 16 cells per thread)
     params, d = make_params(8, naz, adiabatic=True)
     (o, dto), (g, dtg) = run_both(params, d, steps=3, planet=False)
     np.testing.assert_allclose(dtg, dto, rtol=1e-12)
