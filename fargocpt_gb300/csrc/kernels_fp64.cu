@@ -61,9 +61,12 @@ __device__ __forceinline__ double fast_div(double a, double b) { return a * fast
 
 // The same with one Newton-Raphson iteration: the hardware seed is within
 // 2^-20 of 1/b (measured on GB300 over 61 binades), so one iteration leaves
-// a relative error below 2^-40.  Used for the van Leer slope only, where that
-// error scales a slope correction that is itself a small part of the
-// interface value.
+// a relative error below 2^-40 (always low).  Used where the quotient only
+// forms an increment or a derived quantity (slopes, source and viscous
+// terms, heating and cooling, the sound speed, the radial specific energy);
+// the velocities rebuilt from momenta, the azimuthal specific quantities and
+// the CFL step keep the two-iteration form, whose one-sided error would
+// otherwise accumulate in the state or shift the time step.
 __device__ __forceinline__ double fast_rcp1(double b)
 {
     double r;
@@ -71,6 +74,8 @@ __device__ __forceinline__ double fast_rcp1(double b)
     const double e = fma(-b, r, 1.0);
     return fma(r, e, r);
 }
+
+__device__ __forceinline__ double fast_div1(double a, double b) { return a * fast_rcp1(b); }
 
 // van_leer_lim / MC_lim, src/TransportEuler.cpp:306-337
 __device__ __forceinline__ double flux_limiter(double a, double b, int mc)
@@ -149,7 +154,7 @@ __global__ void k_source(Geo g, Tables t, double dt, double omega_frame,
     // v_radial rows One_no_ghost_vr (2) .. MaxMo_no_ghost_vr (nr - 1)
     double vr = vr_in[CELL(i, j)];
     if (i >= 2 && i < nr - 1) {
-        double gradp = 2.0 * fast_rcp(S[CELL(i, j)] + S[CELL(i - 1, j)]);
+        double gradp = 2.0 * fast_rcp1(S[CELL(i, j)] + S[CELL(i - 1, j)]);
         gradp *= (P[CELL(i, j)] - P[CELL(i - 1, j)]);
         gradp *= t.InvDiffRmed[i];
         const double gradphi = (pot[CELL(i, j)] - pot[CELL(i - 1, j)]) * t.InvDiffRmed[i];
@@ -168,7 +173,7 @@ __global__ void k_source(Geo g, Tables t, double dt, double omega_frame,
         if (i >= 1 && i < nr - 1) {
             const int jp = jprev(j, nz);
             const double invdx = t.InvDxSrc[i];
-            const double gradp = 2.0 * fast_rcp(S[CELL(i, j)] + S[CELL(i, jp)]) *
+            const double gradp = 2.0 * fast_rcp1(S[CELL(i, j)] + S[CELL(i, jp)]) *
                                  (P[CELL(i, j)] - P[CELL(i, jp)]) * invdx;
             const double gradphi = (pot[CELL(i, j)] - pot[CELL(i, jp)]) * invdx;
             va = va + dt * (-gradp - gradphi);
@@ -258,12 +263,12 @@ __global__ void k_artvisc_v(Geo g, Tables t, Phys ph, double dt, const double *_
     const size_t c = CELL(i, j);
     if (ph.art_visc_sn) {
         if (i >= 2 && i < nr - 1) {
-            vr[c] = vr[c] - dt * 2.0 * fast_rcp(S[c] + S[CELL(i - 1, j)]) *
+            vr[c] = vr[c] - dt * 2.0 * fast_rcp1(S[c] + S[CELL(i - 1, j)]) *
                                 (Qr[c] - Qr[CELL(i - 1, j)]) * t.InvDiffRmed[i];
         }
         if (i >= 1 && i < nr - 1) {
             const int jp = jprev(j, nz);
-            vaz[c] = vaz[c] - dt * 2.0 * fast_rcp(S[c] + S[CELL(i, jp)]) *
+            vaz[c] = vaz[c] - dt * 2.0 * fast_rcp1(S[c] + S[CELL(i, jp)]) *
                                   (Qp[c] - Qp[CELL(i, jp)]) * t.InvDxTheta[i];
         }
     }
@@ -272,18 +277,18 @@ __global__ void k_artvisc_v(Geo g, Tables t, Phys ph, double dt, const double *_
         if (i >= 1 && i < nr - 1) {
             const int jp = jprev(j, nz);
             const double sigma_phi_avg = 0.5 * (S[c] + S[CELL(i, jp)]);
-            vaz[c] += fast_div(dt, sigma_phi_avg) * t.InvDxSrc[i] * (Qp[c] - Qp[CELL(i, jp)]);
+            vaz[c] += fast_div1(dt, sigma_phi_avg) * t.InvDxSrc[i] * (Qp[c] - Qp[CELL(i, jp)]);
         }
         if (i >= 2 && i < nr - 1) {
             const double sigma_r_avg = 0.5 * (S[c] + S[CELL(i - 1, j)]);
-            vr[c] += ph.rvf * fast_div(dt, sigma_r_avg) * t.TwoOverDRmed2[i] *
+            vr[c] += ph.rvf * fast_div1(dt, sigma_r_avg) * t.TwoOverDRmed2[i] *
                      ((Qr[c] * t.Rmed[i] - Qr[CELL(i - 1, j)] * t.Rmed[i - 1]) -
                       0.5 * (Qp[c] + Qp[CELL(i - 1, j)]) * t.DiffRmed[i]);
         }
     }
     if (ph.adiabatic) {
         // compute_sound_speed_normal / compute_scale_height_old / update_viscosity
-        const double c_s = sqrt(ph.g_gm1 * fast_div(E[c], S[c]));
+        const double c_s = sqrt(ph.g_gm1 * fast_div1(E[c], S[c]));
         const double h = c_s * t.HFacAdi[i];
         cs[c] = c_s;
         H[c] = h;
@@ -407,7 +412,7 @@ __global__ void k_viscous(Geo g, Tables t, Phys ph, double dt, double beta_inv, 
     if (mode & 1) {
         if (i >= 1 && i < nr - 1) {
             const double sigma_avg = 0.5 * (S[c] + S[CELL(i, jp)]);
-            double dVp = fast_div(dt * t.InvRmed[i], sigma_avg) *
+            double dVp = fast_div1(dt * t.InvRmed[i], sigma_avg) *
                          (t.TwoOverDRa2[i] * (t.RinfSq[i + 1] * trp[CELL(i + 1, j)] -
                                               t.RinfSq[i] * trp[c]) +
                           (tpp[c] - tpp[CELL(i, jp)]) * g.invdphi);
@@ -417,7 +422,7 @@ __global__ void k_viscous(Geo g, Tables t, Phys ph, double dt, double beta_inv, 
         if (i >= 2 && i < nr - 1) {
             const double sigma_avg = 0.5 * (S[c] + S[CELL(i - 1, j)]);
             double dVr =
-                fast_div(dt, sigma_avg) * ph.rvf * t.TwoOverRmedSum[i] *
+                fast_div1(dt, sigma_avg) * ph.rvf * t.TwoOverRmedSum[i] *
                 ((t.Rmed[i] * trr[c] - t.Rmed[i - 1] * trr[CELL(i - 1, j)]) * t.InvDiffRmed[i] +
                  (trp[CELL(i, jn)] - trp[c]) * g.invdphi - 0.5 * (tpp[c] + tpp[CELL(i - 1, j)]));
             if (ph.stabilize == 1) dVr = stabilized(dVr, dt, corr_r[c]);
@@ -434,7 +439,7 @@ __global__ void k_viscous(Geo g, Tables t, Phys ph, double dt, double beta_inv, 
             // thermal_relaxation, SourceEuler.cpp:632-690
             double delta_E = e;
             if (ph.beta_ref == 1) {
-                delta_E -= fast_div(E0[c], S0[c]) * sig;
+                delta_E -= fast_div1(E0[c], S0[c]) * sig;
             } else if (ph.beta_ref == 2) {
                 delta_E -= t.EModel[i] * sig;
             } else if (ph.beta_ref == 3) {
@@ -449,7 +454,7 @@ __global__ void k_viscous(Geo g, Tables t, Phys ph, double dt, double beta_inv, 
                 const double tau_r_phi = 0.25 * (trp[c] + trp[CELL(i + 1, j)] + trp[CELL(i, jn)] +
                                                  trp[CELL(i + 1, jn)]);
                 const double t_rr = trr[c], t_pp = tpp[c], d = divv[c];
-                double q = fast_rcp(2.0 * n * sig) *
+                double q = fast_rcp1(2.0 * n * sig) *
                            (t_rr * t_rr + 2 * (tau_r_phi * tau_r_phi) + t_pp * t_pp);
                 q += (2.0 / 9.0) * n * sig * (d * d);
                 q *= ph.hvf;
@@ -457,11 +462,11 @@ __global__ void k_viscous(Geo g, Tables t, Phys ph, double dt, double beta_inv, 
             }
         }
         // radiative alpha factor, SourceEuler.cpp:905-912
-        const double x = ph.mu_gm1_over_R * fast_rcp(sig);
+        const double x = ph.mu_gm1_over_R * fast_rcp1(sig);
         const double x2 = x * x;
         const double inv_pow4 = x2 * x2;
         const double alpha = 1.0 + H[c] * ph.cool_const * inv_pow4 * (e * e * e);
-        const double inv_alpha = fast_rcp(alpha);
+        const double inv_alpha = fast_rcp1(alpha);
         qp *= inv_alpha;
         qm *= inv_alpha;
     }
@@ -602,7 +607,7 @@ __device__ __forceinline__ void rad_ring(int i, int j, int nz, const double *S, 
     w[1] = vr[CELL(i, j)];
     w[2] = (vaz[CELL(i, jnext(j, nz))] + r * omf) * r;
     w[3] = (vaz[CELL(i, j)] + r * omf) * r;
-    if (NQ == 5) w[4] = fast_div(E[CELL(i, j)], sg);
+    if (NQ == 5) w[4] = fast_div1(E[CELL(i, j)], sg);
     w[NQ] = sg;
     sig = sg;
 }
@@ -801,9 +806,9 @@ __device__ double block_min(double v, double *red)
 // (TransportEuler.cpp:270-288): ring mean, ComputeConstantResidual (:207-236),
 // QuantitiesAdvection with the residual then the uniform velocity (:292-304,
 // ComputeStarTheta :416-466, VanLeerTheta :630-664) and AdvectSHIFT
-// (:238-268).  One CTA owns one ring; the ring's sigma, specific quantity
-// and slopes live in shared memory (3 x naz doubles, up to 9386 cells; a
-// per-ring global workspace stands in beyond that).  The face factor
+// (:238-268).  One CTA owns one ring; the ring's sigma, specific quantity,
+// slopes and fluxes live in shared memory (4 x naz doubles, up to 7040 cells;
+// a per-ring global workspace stands in beyond that).  The face factor
 // dxrad S* v / Surf that every quantity's flux shares is formed once per face.
 // ---------------------------------------------------------------------------
 // Each thread owns the cells j = threadIdx.x + n * blockDim.x, n < PER.
@@ -814,13 +819,24 @@ __device__ double block_min(double v, double *red)
 // sigma on entry and its advected value on exit.  v[n] is the owned cells'
 // velocity (ignored when uniform).
 template <int PER>
-__device__ void ring_advection_pass(double *S, double *W, double *D, double *const *qrow,
-                                    int nq, const double *v, double dt, double dxtheta,
-                                    double half_invdx, double dxrad_invsurf, int nz, int mc,
-                                    bool uniform, double vconst)
+__device__ void ring_advection_pass(double *S, double *W, double *D, double *F,
+                                    double *const *qrow, int nq, const double *v, double dt,
+                                    double dxtheta, double half_invdx, double dxrad_invsurf,
+                                    int nz, int mc, bool uniform, double vconst)
 {
     const int tid = threadIdx.x, bs = blockDim.x;
-    double invs[PER], f[PER];
+    // the upwind cell and interpolation distance are kept per cell up to 8
+    // cells per thread and recomputed beyond (registers)
+    constexpr bool KEEP = PER <= 8;
+    double invs[PER], cf[PER], am[KEEP ? PER : 1];
+    int up[KEEP ? PER : 1];
+    auto upwind = [&](int n, int j, int &u, double &a) {
+        const double vv = uniform ? vconst : v[n];
+        const double ksi = vv * dt;
+        const bool pos = positive(vv);
+        u = pos ? (j == 0 ? nz - 1 : j - 1) : j;
+        a = pos ? dxtheta - ksi : -(dxtheta + ksi);
+    };
     // DensityStar
 #pragma unroll
     for (int n = 0; n < PER; ++n) {
@@ -833,22 +849,26 @@ __device__ void ring_advection_pass(double *S, double *W, double *D, double *con
         }
     }
     __syncthreads();
-    // per face: the star density and dxrad S* v / Surf, the factor every
+    // per face j: the upwind cell, the signed interpolation distance
+    // (dx - ksi, or -(dx + ksi)) and dxrad S* v / Surf, the factor every
     // quantity's flux shares
-    double cf[PER];
 #pragma unroll
     for (int n = 0; n < PER; ++n) {
         const int j = tid + n * bs;
         if (j < nz) {
-            const int jm = j == 0 ? nz - 1 : j - 1;
-            const double vv = uniform ? vconst : v[n];
-            const double ksi = vv * dt;
-            const double ss =
-                positive(vv) ? S[jm] + (dxtheta - ksi) * D[jm] : S[j] - (dxtheta + ksi) * D[j];
-            cf[n] = dxrad_invsurf * ss * vv;
+            int u;
+            double a;
+            upwind(n, j, u, a);
+            if (KEEP) {
+                up[n] = u;
+                am[n] = a;
+            }
+            cf[n] = dxrad_invsurf * (S[u] + a * D[u]) * (uniform ? vconst : v[n]);
         }
     }
     __syncthreads();
+    // three barriers per quantity: specific values, slopes, fluxes (the
+    // update reads F while the next quantity fills W and D)
     for (int q = 0; q < nq; ++q) {
         double *Q = qrow[q];
 #pragma unroll
@@ -871,45 +891,38 @@ __device__ void ring_advection_pass(double *S, double *W, double *D, double *con
         for (int n = 0; n < PER; ++n) {
             const int j = tid + n * bs;
             if (j < nz) {
-                const int jm = j == 0 ? nz - 1 : j - 1;
-                const double vv = uniform ? vconst : v[n];
-                const double ksi = vv * dt;
-                const double qs = positive(vv) ? W[jm] + (dxtheta - ksi) * D[jm]
-                                               : W[j] - (dxtheta + ksi) * D[j];
-                f[n] = qs * cf[n];
+                int u;
+                double a;
+                if (KEEP) {
+                    u = up[n];
+                    a = am[n];
+                } else {
+                    upwind(n, j, u, a);
+                }
+                F[j] = (W[u] + a * D[u]) * cf[n];
             }
         }
         __syncthreads();
 #pragma unroll
         for (int n = 0; n < PER; ++n) {
             const int j = tid + n * bs;
-            if (j < nz) W[j] = f[n];
+            if (j < nz) Q[j] += F[j] - F[j == nz - 1 ? 0 : j + 1];
         }
-        __syncthreads();
-#pragma unroll
-        for (int n = 0; n < PER; ++n) {
-            const int j = tid + n * bs;
-            if (j < nz) {
-                const int jp = j == nz - 1 ? 0 : j + 1;
-                Q[j] += W[j] - W[jp];
-            }
-        }
-        __syncthreads();
     }
-    // sigma: its specific quantity is exactly 1, so QRStar == 1
-#pragma unroll
-    for (int n = 0; n < PER; ++n) {
-        const int j = tid + n * bs;
-        if (j < nz) W[j] = cf[n];
-    }
+    // sigma: its specific quantity is exactly 1, so QRStar == 1 (the barrier
+    // lets the last quantity's update finish reading F)
     __syncthreads();
 #pragma unroll
     for (int n = 0; n < PER; ++n) {
         const int j = tid + n * bs;
-        if (j < nz) {
-            const int jp = j == nz - 1 ? 0 : j + 1;
-            f[n] = S[j] + (W[j] - W[jp]);
-        }
+        if (j < nz) F[j] = cf[n];
+    }
+    __syncthreads();
+    double f[PER];
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = tid + n * bs;
+        if (j < nz) f[n] = S[j] + (F[j] - F[j == nz - 1 ? 0 : j + 1]);
     }
     __syncthreads();
 #pragma unroll
@@ -933,8 +946,8 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(Geo g, Tables t, do
     const int i = blockIdx.x;
     const int tid = threadIdx.x, bs = blockDim.x;
     const size_t row = (size_t)i * nz;
-    double *base = ring_ws ? ring_ws + (size_t)i * 3 * nz : smem;
-    double *Sr = base, *W = base + nz, *D = base + 2 * nz;
+    double *base = ring_ws ? ring_ws + (size_t)i * 4 * nz : smem;
+    double *Sr = base, *W = base + nz, *D = base + 2 * nz, *F = base + 3 * nz;
 
     // compute_average_azimuthal_velocity, :174-189
     double vown[PER];
@@ -971,10 +984,10 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(Geo g, Tables t, do
     const double half_invdx = 0.5 * (1.0 / dxtheta);
     const double dxrad = (t.Rsup[i] - t.Rinf[i]) * dt;
     const double invsurf = t.InvSurf[i];
-    ring_advection_pass<PER>(Sr, W, D, qrow, nq, vown, dt, dxtheta, half_invdx,
+    ring_advection_pass<PER>(Sr, W, D, F, qrow, nq, vown, dt, dxtheta, half_invdx,
                              dxrad * invsurf, nz, mc, false, 0.0);
     if (fast) {
-        ring_advection_pass<PER>(Sr, W, D, qrow, nq, vown, dt, dxtheta, half_invdx,
+        ring_advection_pass<PER>(Sr, W, D, F, qrow, nq, vown, dt, dxtheta, half_invdx,
                                  dxrad * invsurf, nz, mc, true, vt);
     }
     // AdvectSHIFT of every quantity, sigma last
@@ -1224,7 +1237,7 @@ __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const 
             const double sg = S[c];
             if (ph.adiabatic) {
                 const double e = E[c];
-                const double es = fast_div(e, sg);
+                const double es = fast_div1(e, sg);
                 T[c] = ph.c_v_inv * es;
                 c_s = sqrt(ph.g_gm1 * es);
                 const double h = c_s * t.HFacAdi[i];
@@ -1555,7 +1568,7 @@ void launch_transport_radial(const Launch &L, double dt, double omf, int chunk, 
     }
 }
 
-size_t azimuthal_smem_bytes(int nz) { return (size_t)3 * nz * sizeof(double); }
+size_t azimuthal_smem_bytes(int nz) { return (size_t)4 * nz * sizeof(double); }
 
 // Cells per thread of the azimuthal kernel: blocks stay at <= 512 threads so
 // that the per-thread cell arrays fit 128 registers.
