@@ -49,8 +49,8 @@ STEP_BYTES_PER_CELL = {"adiabatic": 64, "isothermal": 48}   # one read + write o
 # commands in profiles/transport_kernels_c2_fp64.md and
 # profiles/transport_azimuthal_c2_fp32.md)
 NCU_DRAM_BYTES_C2 = {
-    ("fp64", "transport_azimuthal"): 44.128e6 + 0.389e6,
-    ("fp64", "transport_radial"): 25.255e6 + 0.525e6,
+    ("fp64", "transport_azimuthal"): 44.127e6 + 0.422e6,
+    ("fp64", "transport_radial"): 25.252e6 + 0.738e6,
     ("fp32", "transport_azimuthal"): 25.256e6 + 1.903e6,
 }
 KERNELS_IN_TIMED_STEP = 13   # the adiabatic step's kernels between the step's events
@@ -458,9 +458,9 @@ def main():
     value = world * cells * args.steps / (vals[0] * 1e-3)
     e2e = world * cells * args.steps / vals[1]
     rl, rls = roofline(r64, args.steps, 1.0, "fp64", args.config)
-    # the FP64 kernels are bound by the FP64 pipe (75-81% busy, DRAM at 1%
+    # the FP64 kernels are bound by the FP64 pipe (72-80% busy, DRAM at 1%
     # of peak in profiles/transport_kernels_c2_fp64.md)
-    rl["fp64_pipe_busy_pct_ncu"] = {"transport_azimuthal": 75.0, "transport_radial": 80.6}
+    rl["fp64_pipe_busy_pct_ncu"] = {"transport_azimuthal": 72.5, "transport_radial": 79.7}
     fp32 = None
     if r32 is not None:
         value32 = world * cells * args.steps / (vals[2] * 1e-3)

@@ -90,6 +90,23 @@ __device__ __forceinline__ double flux_limiter(double a, double b, int mc)
     return 0.0;
 }
 
+// exp(x) by its Taylor series through x^7 for |x| <= 1/64 (the remainder,
+// below x^8 / 8! <= 1e-19, is under half an ulp of the result), exp() beyond:
+// compression heating's exponent is a fraction of the cell's CFL number, so
+// the series covers the disk and exp() the shocks.
+__device__ __forceinline__ double exp_small(double x)
+{
+    if (fabs(x) > 0.015625) return exp(x);
+    double p = 1.0 / 5040.0;
+    p = fma(p, x, 1.0 / 720.0);
+    p = fma(p, x, 1.0 / 120.0);
+    p = fma(p, x, 1.0 / 24.0);
+    p = fma(p, x, 1.0 / 6.0);
+    p = fma(p, x, 0.5);
+    p = fma(p, x, 1.0);
+    return fma(p, x, 1.0);
+}
+
 // assure_temperature_range, src/SourceEuler.cpp:136-202: the bounds are
 // Tmin/max * sigma / mu * R / (gamma - 1); the constant factor is folded on
 // the host.
@@ -207,7 +224,7 @@ __global__ void k_artvisc_q(Geo g, Tables t, Phys ph, double dt, const double *_
         if (i < nr - 1) {
             const double div_v = (vr1 * t.Rinf[i + 1] - vr0 * t.Rinf[i]) * t.InvDiffRsupRb[i] +
                                  (va1 - va0) * g.invdphi * t.InvRmed[i];
-            e = e * exp(-ph.gm1 * dt * div_v);
+            e = e * exp_small(-ph.gm1 * dt * div_v);
         }
     }
     if (ph.art_visc_sn) {
@@ -605,8 +622,13 @@ __device__ __forceinline__ void rad_ring(int i, int j, int nz, const double *S, 
     const double r = t.Rmed[i];
     w[0] = vr[CELL(i + 1, j)];
     w[1] = vr[CELL(i, j)];
-    w[2] = (vaz[CELL(i, jnext(j, nz))] + r * omf) * r;
-    w[3] = (vaz[CELL(i, j)] + r * omf) * r;
+    if (omf != 0.0) {
+        w[2] = (vaz[CELL(i, jnext(j, nz))] + r * omf) * r;
+        w[3] = (vaz[CELL(i, j)] + r * omf) * r;
+    } else {
+        w[2] = vaz[CELL(i, jnext(j, nz))] * r;
+        w[3] = vaz[CELL(i, j)] * r;
+    }
     if (NQ == 5) w[4] = fast_div1(E[CELL(i, j)], sg);
     w[NQ] = sg;
     sig = sg;
