@@ -36,7 +36,7 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
 # Compulsory HBM bytes per cell of each kernel of the FP64 adiabatic step
-# (unique fields read + written, 8 B each); see the design doc.
+# (unique fields read + written, 8 B each; halved for FP32).
 KERNEL_BYTES_PER_CELL = {
     "potential": 16, "source": 56, "artvisc_q": 56, "artvisc_v": 88, "stress": 64,
     "viscous_substep3": 120, "ghost_pre": 0, "transport_radial": 80,
@@ -45,9 +45,8 @@ KERNEL_BYTES_PER_CELL = {
 }
 STEP_BYTES_PER_CELL = {"adiabatic": 64, "isothermal": 48}   # one read + write of the state
 # dram__bytes_read.sum + dram__bytes_write.sum per launch from one ncu capture
-# of the dominant kernels on the 512 x 1536 adiabatic disk (summaries and
-# commands in profiles/transport_kernels_c2_fp64.md and
-# profiles/transport_azimuthal_c2_fp32.md)
+# of the dominant kernels on the 512 x 1536 adiabatic disk (--set full of the
+# FP64 transports and of the FP32 azimuthal transport)
 NCU_DRAM_BYTES_C2 = {
     ("fp64", "transport_azimuthal"): 44.127e6 + 0.422e6,
     ("fp64", "transport_radial"): 25.252e6 + 0.738e6,
@@ -374,9 +373,19 @@ def roofline(res, steps, bytes_scale, form, cfg_name):
     sbpc = STEP_BYTES_PER_CELL[kind] * bytes_scale
     step_achieved = sbpc * cells * steps / (res["total_ms"] * 1e-3) / 1e9
     traffic = NCU_DRAM_BYTES_C2.get((form, dom)) if cfg_name == "c2" else None
+    # every kernel's algorithmic HBM rate against the peak
+    per_kernel = {}
+    for k, tot in phases.items():
+        ms = tot / max(1, nsteps)
+        b = KERNEL_BYTES_PER_CELL.get(k, 0) * bytes_scale
+        if ms > 0 and b > 0:
+            gbs = b * cells / (ms * 1e-3) / 1e9
+            per_kernel[k] = {"ms": ms, "bytes_per_cell": b, "achieved_gbs": gbs,
+                             "frac": gbs / peak}
     return ({"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
              "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
-             "traffic_unit": "B per launch", "bytes_per_cell": bpc, "ms_per_launch": dom_ms},
+             "traffic_unit": "B per launch", "bytes_per_cell": bpc, "ms_per_launch": dom_ms,
+             "per_kernel": per_kernel},
             {"achieved": step_achieved, "peak": peak, "unit": "GB/s",
              "frac": step_achieved / peak, "bytes_per_cell": sbpc})
 
@@ -459,7 +468,7 @@ def main():
     e2e = world * cells * args.steps / vals[1]
     rl, rls = roofline(r64, args.steps, 1.0, "fp64", args.config)
     # the FP64 kernels are bound by the FP64 pipe (72-80% busy, DRAM at 1%
-    # of peak in profiles/transport_kernels_c2_fp64.md)
+    # of peak in the same captures)
     rl["fp64_pipe_busy_pct_ncu"] = {"transport_azimuthal": 72.5, "transport_radial": 79.7}
     fp32 = None
     if r32 is not None:

@@ -706,14 +706,18 @@ __device__ __forceinline__ void radial_col(const GeoF &g, const TablesF &t, floa
 // flux array lets the update read them while the next quantity starts).
 // ---------------------------------------------------------------------------
 template <int PER, int NQ>
-__device__ __forceinline__ void ring_pass_f(float *S, float *SS, float *W, float *D, float *F,
-                                            float *const *qrow, const float *v,
-                                            float *slo, float dt, float dxtheta,
-                                            float half_invdx, float dxrad, float invsurf, int nz,
-                                            int mc, bool uniform, float vconst)
+__device__ __forceinline__ void ring_pass_f(float *S, float *W, float *D, float *F, float *X,
+                                            float *const *qrow, const float *v, float *slo,
+                                            float dt, float dxtheta, float half_invdx,
+                                            float dxrad_invsurf, int nz, int mc)
 {
     const int tid = threadIdx.x, bs = blockDim.x;
-    float invs[PER];
+    // per face: 1 / sigma of the cell and dxrad S* v / Surf, the factor every
+    // quantity's flux shares; kept in the X array up to 4 cells per thread
+    // (short rings, shared memory to spare) and in registers beyond
+    constexpr bool XS = PER <= 4;
+    float invs[PER], cfr[XS ? 1 : PER];
+    auto cf = [&](int n, int j) -> float & { return XS ? X[j] : cfr[n]; };
 #pragma unroll
     for (int n = 0; n < PER; ++n) {
         const int j = tid + n * bs;
@@ -729,9 +733,11 @@ __device__ __forceinline__ void ring_pass_f(float *S, float *SS, float *W, float
         const int j = tid + n * bs;
         if (j < nz) {
             const int jm = j == 0 ? nz - 1 : j - 1;
-            const float vv = uniform ? vconst : v[n];
+            const float vv = v[n];
             const float ksi = vv * dt;
-            SS[j] = ksi > 0.f ? S[jm] + (dxtheta - ksi) * D[jm] : S[j] - (dxtheta + ksi) * D[j];
+            const float ss =
+                ksi > 0.f ? S[jm] + (dxtheta - ksi) * D[jm] : S[j] - (dxtheta + ksi) * D[j];
+            cf(n, j) = dxrad_invsurf * ss * vv;
         }
     }
     __syncthreads();
@@ -758,25 +764,24 @@ __device__ __forceinline__ void ring_pass_f(float *S, float *SS, float *W, float
             const int j = tid + n * bs;
             if (j < nz) {
                 const int jm = j == 0 ? nz - 1 : j - 1;
-                const float vv = uniform ? vconst : v[n];
-                const float ksi = vv * dt;
+                const float ksi = v[n] * dt;
                 const float qs = ksi > 0.f ? W[jm] + (dxtheta - ksi) * D[jm]
                                            : W[j] - (dxtheta + ksi) * D[j];
-                F[j] = dxrad * qs * SS[j] * vv;
+                F[j] = qs * cf(n, j);
             }
         }
         __syncthreads();
 #pragma unroll
         for (int n = 0; n < PER; ++n) {
             const int j = tid + n * bs;
-            if (j < nz) Q[j] += (F[j] - F[j == nz - 1 ? 0 : j + 1]) * invsurf;
+            if (j < nz) Q[j] += F[j] - F[j == nz - 1 ? 0 : j + 1];
         }
     }
     __syncthreads();
 #pragma unroll
     for (int n = 0; n < PER; ++n) {
         const int j = tid + n * bs;
-        if (j < nz) F[j] = dxrad * SS[j] * (uniform ? vconst : v[n]);
+        if (j < nz) F[j] = cf(n, j);
     }
     __syncthreads();
 #pragma unroll
@@ -784,7 +789,7 @@ __device__ __forceinline__ void ring_pass_f(float *S, float *SS, float *W, float
         const int j = tid + n * bs;
         if (j < nz) {
             float sn = S[j];
-            comp_add(sn, slo[n], (F[j] - F[j == nz - 1 ? 0 : j + 1]) * invsurf);
+            comp_add(sn, slo[n], F[j] - F[j == nz - 1 ? 0 : j + 1]);
             S[j] = sn;
         }
     }
@@ -803,16 +808,18 @@ __device__ __forceinline__ void ring_pass_f(float *S, float *SS, float *W, float
 // differences first keeps FP32's rounding at the size of the changes, where
 // the flux form rounds at the size of the fluxes, up to half of the ring's
 // content per step, and repeats the same rounding pattern every step.
-// dS* and S*_{j+1} go to the SS and F arrays (unused by this pass); c is
-// dxrad v invsurf and a the interpolation distance.
+// dS* goes to the X array (up to 4 cells per thread) or registers, S*_{j+1}
+// to the F array; c is dxrad v invsurf and a the interpolation distance.
 template <int PER, int NQ>
-__device__ __forceinline__ void ring_pass_uniform_f(float *S, float *SS, float *W, float *D,
-                                                    float *F, float *const *qrow, float *slo,
+__device__ __forceinline__ void ring_pass_uniform_f(float *S, float *W, float *D, float *F,
+                                                    float *X, float *const *qrow, float *slo,
                                                     bool pos, float a, float c, float half_invdx,
                                                     int nz, int mc)
 {
     const int tid = threadIdx.x, bs = blockDim.x;
-    float invs[PER];
+    constexpr bool XS = PER <= 4;
+    float invs[PER], dssr[XS ? 1 : PER];
+    auto dss = [&](int n, int j) -> float & { return XS ? X[j] : dssr[n]; };
 #pragma unroll
     for (int n = 0; n < PER; ++n) {
         const int j = tid + n * bs;
@@ -829,7 +836,7 @@ __device__ __forceinline__ void ring_pass_uniform_f(float *S, float *SS, float *
         if (j < nz) {
             const int jp = j == nz - 1 ? 0 : j + 1, jm = j == 0 ? nz - 1 : j - 1;
             const int u = pos ? jm : j, u1 = pos ? j : jp;
-            SS[j] = (S[u] - S[u1]) + a * (D[u] - D[u1]);
+            dss(n, j) = (S[u] - S[u1]) + a * (D[u] - D[u1]);
             F[j] = S[u1] + a * D[u1];
         }
     }
@@ -860,7 +867,7 @@ __device__ __forceinline__ void ring_pass_uniform_f(float *S, float *SS, float *
                 const int u = pos ? jm : j, u1 = pos ? j : jp;
                 const float qs = W[u] + a * D[u];
                 const float dqs = (W[u] - W[u1]) + a * (D[u] - D[u1]);
-                Q[j] += c * (qs * SS[j] + F[j] * dqs);
+                Q[j] += c * (qs * dss(n, j) + F[j] * dqs);
             }
         }
         __syncthreads();
@@ -870,20 +877,23 @@ __device__ __forceinline__ void ring_pass_uniform_f(float *S, float *SS, float *
         const int j = tid + n * bs;
         if (j < nz) {
             float sn = S[j];
-            comp_add(sn, slo[n], c * SS[j]);
+            comp_add(sn, slo[n], c * dss(n, j));
             S[j] = sn;
         }
     }
     __syncthreads();
 }
 
-// Shared memory of azimuthal_ring: 5 ring-long work arrays (sigma, its star
-// value, the specific quantity, its slope, the flux), plus the nq quantity
-// rows when STAGE (then every row is read from HBM once, up front, and the
-// passes and the shift work in shared memory).
+// Shared memory of azimuthal_ring: ring-long work arrays for sigma, the
+// specific quantity, its slope and the flux, a fifth for the per-face factors
+// on rings up to 2048 cells (where at most 4 cells per thread leave no
+// registers for them), plus the nq quantity rows when STAGE (then every row
+// is read from HBM once, up front, and the passes and the shift work in
+// shared memory).
+__host__ __device__ constexpr int azimuthal_work_rows(int nz) { return nz <= 2048 ? 5 : 4; }
 __host__ __device__ constexpr size_t azimuthal_smem_floats(int nz, int nq, bool stage)
 {
-    return (size_t)(stage ? 5 + nq : 5) * (size_t)nz;
+    return (size_t)(azimuthal_work_rows(nz) + (stage ? nq : 0)) * (size_t)nz;
 }
 
 // smf: azimuthal_smem_floats(nz, nq, STAGE) floats of shared memory; redf: 33
@@ -898,11 +908,14 @@ __device__ __forceinline__ void azimuthal_ring(const GeoF &g, const TablesF &t, 
     const int nz = g.nz;
     const int tid = threadIdx.x, bs = blockDim.x;
     const size_t row = (size_t)i * nz;
-    float *Sr = smf, *SS = smf + nz, *W = smf + 2 * nz, *D = smf + 3 * nz, *Fx = smf + 4 * nz;
+    float *Sr = smf, *W = smf + nz, *D = smf + 2 * nz, *Fx = smf + 3 * nz;
+    // the per-face array exists when PER <= 4, which needs nz <= 4 x 512
+    float *X = smf + 4 * nz;
+    const int wr = azimuthal_work_rows(nz);
     float *grow[5] = {m0 + row, m1 + row, m2 + row, m3 + row, E + row};
     float *qrow[5];
 #pragma unroll
-    for (int q = 0; q < 5; ++q) qrow[q] = STAGE ? smf + (size_t)(5 + q) * nz : grow[q];
+    for (int q = 0; q < 5; ++q) qrow[q] = STAGE ? smf + (size_t)(wr + q) * nz : grow[q];
 
     float vown[PER], slo[PER];
     float amax = 0.f;
@@ -948,12 +961,12 @@ __device__ __forceinline__ void azimuthal_ring(const GeoF &g, const TablesF &t, 
     const float half_invdx = 0.5f / dxtheta;
     const float dxrad = t.DRsup[i] * (float)dt;
     const float invsurf = t.InvSurf[i];
-    ring_pass_f<PER, NQ>(Sr, SS, W, D, Fx, qrow, vown, slo, (float)dt, dxtheta, half_invdx,
-                         dxrad, invsurf, nz, mc, false, 0.f);
+    ring_pass_f<PER, NQ>(Sr, W, D, Fx, X, qrow, vown, slo, (float)dt, dxtheta, half_invdx,
+                         dxrad * invsurf, nz, mc);
     if (fast) {
         const float ksi = vt * (float)dt;
         const bool pos = ksi > 0.f;
-        ring_pass_uniform_f<PER, NQ>(Sr, SS, W, D, Fx, qrow, slo, pos,
+        ring_pass_uniform_f<PER, NQ>(Sr, W, D, Fx, X, qrow, slo, pos,
                                      pos ? dxtheta - ksi : -(dxtheta + ksi),
                                      dxrad * vt * invsurf, half_invdx, nz, mc);
     }

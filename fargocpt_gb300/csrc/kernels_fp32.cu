@@ -554,7 +554,7 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
         CKF(cudaMemcpy(damp_rings, rings.data(), sizeof(int) * rings.size(), cudaMemcpyHostToDevice));
     }
     // azimuthal kernel configuration
-    per = nz <= 2048 ? 4 : (nz <= 4096 ? 8 : 16);
+    per = nz <= 2048 ? 4 : (nz <= 4096 ? 8 : (nz <= 6144 ? 12 : 16));
     az_block = std::max(128, std::min(512, ((nz + per - 1) / per + 31) / 32 * 32));
     // cells strided over the block; the transported quantities staged in
     // shared memory when they fit in its 227 KB
@@ -565,18 +565,22 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
         err = "ring too long for the FP32 azimuthal kernel";
         return FGPU_ERR_UNSUPPORTED;
     }
-    const void *az_kernels[12] = {
+    const void *az_kernels[16] = {
         (const void *)f_transport_azimuthal<4, 4, false>,
         (const void *)f_transport_azimuthal<8, 4, false>,
+        (const void *)f_transport_azimuthal<12, 4, false>,
         (const void *)f_transport_azimuthal<16, 4, false>,
         (const void *)f_transport_azimuthal<4, 4, true>,
         (const void *)f_transport_azimuthal<8, 4, true>,
+        (const void *)f_transport_azimuthal<12, 4, true>,
         (const void *)f_transport_azimuthal<16, 4, true>,
         (const void *)f_transport_azimuthal<4, 5, false>,
         (const void *)f_transport_azimuthal<8, 5, false>,
+        (const void *)f_transport_azimuthal<12, 5, false>,
         (const void *)f_transport_azimuthal<16, 5, false>,
         (const void *)f_transport_azimuthal<4, 5, true>,
         (const void *)f_transport_azimuthal<8, 5, true>,
+        (const void *)f_transport_azimuthal<12, 5, true>,
         (const void *)f_transport_azimuthal<16, 5, true>};
     for (const void *fn : az_kernels) {
         if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)az_smem) !=
@@ -863,10 +867,12 @@ int Engine32::transport(double dt)
     if (az_stage) {                                      \
         if (per == 4) AZ32(4, NQ, true);                 \
         else if (per == 8) AZ32(8, NQ, true);            \
+        else if (per == 12) AZ32(12, NQ, true);          \
         else AZ32(16, NQ, true);                         \
     } else {                                             \
         if (per == 4) AZ32(4, NQ, false);                \
         else if (per == 8) AZ32(8, NQ, false);           \
+        else if (per == 12) AZ32(12, NQ, false);         \
         else AZ32(16, NQ, false);                        \
     }
         if (adi) {

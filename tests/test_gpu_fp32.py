@@ -107,3 +107,32 @@ def test_fp32_round_trip_keeps_residual_precision():
     vk = np.sqrt(1.0 / rmed)[:, None]
     res = v - vk
     assert np.max(np.abs(back - v)) <= 1e-7 * np.max(np.abs(res))
+
+
+@pytest.mark.parametrize("naz", [6144, 7680])
+def test_fp32_long_rings_against_fp64_form(naz):
+    """Long rings: 12 cells per thread with the rows staged in shared memory
+    (6144) and 16 cells per thread without staging (7680), adiabatic, against
+    the FP64 form after a few CFL steps."""
+    from fargocpt_gb300.engine import Engine, grid_radii
+    from gpu_cases import initial_state, load, make_params
+
+    p64, d = make_params(8, naz, adiabatic=True)
+    p32, _ = make_params(8, naz, adiabatic=True, precision=1)
+    radii = grid_radii(d["radial_spacing"], d["rmin"], d["rmax"], d["nrad"])
+    st = initial_state(d, radii, seed=9)
+    bodies = [(0.0, 0.0, 1.0, 0.0, 0.0)]
+    engs = [Engine(p64, radii), Engine(p32, radii)]
+    for e in engs:
+        load(e, st, bodies)
+        e.apply_boundary_condition(0.0, 0.0, False)
+    t = 0.0
+    for _ in range(4):
+        dt = engs[0].condition_cfl()
+        for e in engs:
+            e.step_euler(dt, t)
+        t += dt
+    s64, s32 = engs[0].get_field("SIGMA"), engs[1].get_field("SIGMA")
+    assert rel_linf(s32, s64) <= 1e-6
+    e64, e32 = engs[0].get_field("ENERGY"), engs[1].get_field("ENERGY")
+    assert rel_linf(e32, e64) <= 1e-5
