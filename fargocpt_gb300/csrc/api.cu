@@ -196,10 +196,6 @@ static int validate(const fgpu_params *p, std::string &why)
     if (p->eos != FGPU_EOS_ISOTHERMAL && p->eos != FGPU_EOS_IDEAL) { why = "eos"; return FGPU_ERR_BAD_ARG; }
     if (p->art_visc != FGPU_ARTVISC_NONE && p->art_visc != FGPU_ARTVISC_SN && p->art_visc != FGPU_ARTVISC_TW) { why = "art_visc"; return FGPU_ERR_BAD_ARG; }
     if (p->stabilize_viscosity < 0 || p->stabilize_viscosity > 2) { why = "stabilize_viscosity must be 0, 1 or 2"; return FGPU_ERR_BAD_ARG; }
-    if (p->precision == FGPU_PRECISION_FP32_MIXED && (p->art_visc == FGPU_ARTVISC_TW || p->stabilize_viscosity)) {
-        why = "Tscharnuter-Winkler artificial viscosity and StabilizeViscosity are FP64 only";
-        return FGPU_ERR_UNSUPPORTED;
-    }
     if (p->precision != FGPU_PRECISION_FP64 && p->precision != FGPU_PRECISION_FP32_MIXED) { why = "precision"; return FGPU_ERR_BAD_ARG; }
     if (p->integrator != FGPU_INTEGRATOR_EULER && p->integrator != FGPU_INTEGRATOR_LEAPFROG) { why = "integrator"; return FGPU_ERR_BAD_ARG; }
     if (p->radial_spacing != FGPU_SPACING_LOGARITHMIC && p->radial_spacing != FGPU_SPACING_ARITHMETIC) { why = "radial_spacing"; return FGPU_ERR_BAD_ARG; }
@@ -1158,10 +1154,6 @@ extern "C" int fgpu_accrete_onto_planet(fgpu_engine *eng, const fgpu_accretor *a
                                         double out[3])
 {
     if (!eng || !a || !out || !(dt >= 0.0)) return FGPU_ERR_BAD_ARG;
-    if (eng->e32) {
-        eng->err = "accretion runs in the FP64 form only";
-        return FGPU_ERR_UNSUPPORTED;
-    }
     if (a->type != FGPU_ACCRETION_KLEY && a->type != FGPU_ACCRETION_VISCOUS &&
         a->type != FGPU_ACCRETION_SINKHOLE) {
         eng->err = "accretion type";
@@ -1211,6 +1203,12 @@ extern "C" int fgpu_accrete_onto_planet(fgpu_engine *eng, const fgpu_accretor *a
     if (sp.i1 < sp.i0 || sp.ncols < 1) {
         out[0] = out[1] = out[2] = 0.0;
         return FGPU_OK;
+    }
+    if (eng->e32) {
+        const fgpu32::AccrF af{sp.type, sp.i0, sp.i1, sp.j0, sp.ncols, sp.x, sp.y, sp.rhill,
+                               sp.frac1, sp.frac2, sp.facc1, sp.facc2, sp.f_const, sp.dist_max,
+                               sp.density_floor, sp.omf};
+        ROUTE32(eng->e32->accrete(af, out));
     }
     double **f = eng->field;
     launch_accrete(launch_of(eng), sp, f[FGPU_SIGMA], f[FGPU_ENERGY], f[FGPU_V_RADIAL],

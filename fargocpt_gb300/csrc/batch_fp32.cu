@@ -101,7 +101,7 @@ __global__ void b_artvisc_q(const DiskF *__restrict__ D, const StepF *__restrict
                             const int *__restrict__ start, int nd, int rpb)
 {
     for_cells(D, S, start, nd, rpb, 0, [&](const DiskF &k, const StepF &st, int i, int j) {
-        if (!(k.ph.adiabatic || k.ph.art_visc_sn)) return;
+        if (!(k.ph.adiabatic || k.ph.art_visc_sn || k.ph.art_visc_tw)) return;
         artvisc_q_cell(k.g, k.t, k.ph, st.fdt, k.s.sigma, k.vr_b, k.dv_b, k.s.energy, k.Qr, k.Qp,
                        i, j);
     });
@@ -111,7 +111,7 @@ __global__ void b_artvisc_v(const DiskF *__restrict__ D, const StepF *__restrict
                             const int *__restrict__ start, int nd, int rpb)
 {
     for_cells(D, S, start, nd, rpb, 0, [&](const DiskF &k, const StepF &st, int i, int j) {
-        if (!(k.ph.adiabatic || k.ph.art_visc_sn)) return;
+        if (!(k.ph.adiabatic || k.ph.art_visc_sn || k.ph.art_visc_tw)) return;
         artvisc_v_cell(k.g, k.t, k.ph, st.fdt, k.s.sigma, k.s.energy, k.Qr, k.Qp, k.vr_b, k.dv_b,
                        k.cs, k.H, k.nu, i, j);
     });
@@ -131,7 +131,7 @@ __global__ void b_viscous(const DiskF *__restrict__ D, const StepF *__restrict__
     for_cells(D, S, start, nd, rpb, 0, [&](const DiskF &k, const StepF &st, int i, int j) {
         viscous_cell(k.g, k.t, k.ph, st.fdt, st.beta_inv, k.ph.adiabatic ? 7 : 1, k.s.sigma, k.trr,
                      k.tpp, k.trp, k.divv, k.nu, k.H, k.s.sigma0, k.s.energy0, k.vr_b, k.dv_b,
-                     k.s.energy, k.qplus, k.qminus, i, j);
+                     k.s.energy, k.qplus, k.qminus, nullptr, nullptr, i, j);
     });
 }
 
@@ -246,7 +246,8 @@ __global__ void b_derived_cfl(const DiskF *__restrict__ D, const StepF *__restri
         const DiskF &k = D[d];
         const int i = item - __ldg(start + d);
         derived_cfl_ring(k.g, k.t, k.ph, mode, k.s.sigma, k.s.energy, k.s.vr, k.s.dv, k.qplus,
-                         k.qminus, k.cs, k.H, k.P, k.T, k.nu, k.dtmin, i, red, red2);
+                         k.qminus, k.cs, k.H, k.P, k.T, k.nu, k.dtmin, i, red, red2, nullptr,
+                         nullptr);
     }
 }
 
@@ -648,8 +649,9 @@ extern "C" int fgpu_batch_create(int n, const fgpu_params *params, const double 
         if (params[k].precision != FGPU_PRECISION_FP32_MIXED ||
             params[k].integrator != FGPU_INTEGRATOR_EULER)
             return FGPU_ERR_UNSUPPORTED;
-        // the recompute of c_s, H, nu before the final hooks is not part of
-        // the batched step
+        // StabilizeViscosity and the recompute of c_s, H, nu before the final
+        // hooks are not part of the batched step
+        if (params[k].stabilize_viscosity) return FGPU_ERR_UNSUPPORTED;
         if (params[k].eos == FGPU_EOS_IDEAL &&
             (params[k].viscous_accretion || params[k].bc_vrad_inner == FGPU_BC_VISCOUS))
             return FGPU_ERR_UNSUPPORTED;
@@ -691,7 +693,8 @@ extern "C" int fgpu_batch_create(int n, const fgpu_params *params, const double 
         b->nz.push_back(e->azimuthal());
         b->nz_max = std::max(b->nz_max, e->azimuthal());
         desc[k] = e->describe();
-        b->any_art = b->any_art || desc[k].ph.adiabatic || desc[k].ph.art_visc_sn;
+        b->any_art = b->any_art || desc[k].ph.adiabatic || desc[k].ph.art_visc_sn ||
+                     desc[k].ph.art_visc_tw;
         b->any_iso = b->any_iso || desc[k].nq == 4;
         b->any_adi = b->any_adi || desc[k].nq == 5;
         int nrings = 0;

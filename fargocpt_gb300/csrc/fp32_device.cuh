@@ -309,6 +309,21 @@ __device__ __forceinline__ void artvisc_q_cell(const GeoF &g, const TablesF &t, 
             e = e - dt * qr * dv_r * t.InvDiffRsup[i] - dt * qp * dvp * t.InvDxTheta[i];
         }
     }
+    if (ph.art_visc_tw) {
+        // update_with_artificial_viscosity_TW, artificial_viscosity.cpp:52-91
+        // (velocity differences within a ring are the same for the residual)
+        const float sig = S[c];
+        const float eps_rr = (vr1 - vr0) * t.InvDiffRsup[i];
+        const float eps_pp = t.InvRmed[i] * (dvp * g.invdphi + 0.5f * (vr1 + vr0));
+        const float div_V = fminf(eps_rr + eps_pp, 0.f);
+        const float lsig = t.LSqTW[i] * sig;
+        Qr[c] = lsig * -div_V * (eps_rr - (1.f / 3.f) * div_V);
+        Qp[c] = lsig * -div_V * (eps_pp - (1.f / 3.f) * div_V);
+        if (ph.adiabatic && ph.dissipation && i >= 1 && i < nr - 1) {
+            const float d = eps_rr - eps_pp;
+            e += -lsig * div_V * (1.f / 3.f) * (eps_rr * eps_rr + eps_pp * eps_pp + d * d) * dt;
+        }
+    }
     if (ph.adiabatic) {
         if (ph.dissipation) e = tfloor(e, S[c], ph);
         E[c] = e;
@@ -335,6 +350,20 @@ __device__ __forceinline__ void artvisc_v_cell(const GeoF &g, const TablesF &t, 
             const int jp = jprev(j, nz);
             dv[c] -= dt * 2.f * __fdividef(Qp[c] - Qp[CELL(i, jp)], S[c] + S[CELL(i, jp)]) *
                      t.InvDxTheta[i];
+        }
+    }
+    if (ph.art_visc_tw) {
+        // artificial_viscosity.cpp:93-139
+        if (i >= 1 && i < nr - 1) {
+            const int jp = jprev(j, nz);
+            dv[c] += __fdividef(dt, 0.5f * (S[c] + S[CELL(i, jp)])) * t.InvDxSrc[i] *
+                     (Qp[c] - Qp[CELL(i, jp)]);
+        }
+        if (i >= 2 && i < nr - 1) {
+            const size_t cm = CELL(i - 1, j);
+            vr[c] += ph.rvf * __fdividef(dt, 0.5f * (S[c] + S[cm])) * t.TwoOverDRmed2[i] *
+                     ((Qr[c] * t.Rmed[i] - Qr[cm] * t.Rmed[i - 1]) -
+                      0.5f * (Qp[c] + Qp[cm]) * t.DRmed[i]);
         }
     }
     if (ph.adiabatic) {
@@ -381,6 +410,44 @@ __device__ __forceinline__ void stress_cell(const GeoF &g, const TablesF &t,
     }
 }
 
+// StabilizeViscosity's correction factors (viscosity.cpp:256-348), rows
+// 1 .. nr - 1, from nu and sigma (nu sigma at the centres, the four-cell
+// averages at the r-phi corners; row nr of the latter is zero)
+__device__ __forceinline__ float nusig_rp_f(const float *nu, const float *S, int nz, int i, int j)
+{
+    const int jp = jprev(j, nz);
+    const float n = 0.25f * (nu[CELL(i, j)] + nu[CELL(i - 1, j)] + nu[CELL(i, jp)] +
+                             nu[CELL(i - 1, jp)]);
+    const float s = 0.25f * (S[CELL(i, j)] + S[CELL(i - 1, j)] + S[CELL(i, jp)] +
+                             S[CELL(i - 1, jp)]);
+    return n * s;
+}
+
+__device__ __forceinline__ void visc_corr_cell(const GeoF &g, const TablesF &t,
+                                               const float *__restrict__ S,
+                                               const float *__restrict__ nu,
+                                               float *__restrict__ corr_phi,
+                                               float *__restrict__ corr_r, int i, int j)
+{
+    const int nz = g.nz, nr = g.nr;
+    const size_t c = CELL(i, j);
+    const int jp = jprev(j, nz), jn = jnext(j, nz);
+    const float rp = nusig_rp_f(nu, S, nz, i, j);
+    const float rp_ip = i + 1 < nr ? nusig_rp_f(nu, S, nz, i + 1, j) : 0.f;
+    const float rp_jp = nusig_rp_f(nu, S, nz, i, jn);
+    const float ns = nu[c] * S[c];
+    const float ns_jm = nu[CELL(i, jp)] * S[CELL(i, jp)];
+    const float ns_im = nu[CELL(i - 1, j)] * S[CELL(i - 1, j)];
+    const float cphi_rp = -t.InvRmed[i] * t.TwoOverDRa2[i] *
+                          (rp_ip * t.Ra3IDRmed[i + 1] + rp * t.Ra3IDRmed[i]);
+    const float cphi_pp = -t.F43[i] * (ns + ns_jm);
+    corr_phi[c] = (cphi_rp + cphi_pp) / (0.5f * (S[c] + S[CELL(i, jp)]) * t.Rmed[i]);
+    const float cr_rp = -(rp_jp + rp) * t.CrRp[i];
+    const float cr_pp = -0.5f * (ns * t.CrPp1[i] + ns_im * t.CrPp2[i]);
+    const float cr_rr = t.InvDiffRmed[i] * (ns * t.CrRr1[i] + ns_im * t.CrRr2[i]);
+    corr_r[c] = t.CrScale[i] * (cr_rr + cr_rp + cr_pp) / (0.5f * (S[c] + S[CELL(i - 1, j)]));
+}
+
 // viscous velocity update + SubStep3.  mode bits: 1 velocities
 // (viscosity.cpp:355-421), 2 heating/cooling rates, 4 energy update
 // (SourceEuler.cpp:859-954)
@@ -390,24 +457,41 @@ __device__ __forceinline__ void viscous_cell(
     const float *__restrict__ trp, const float *__restrict__ divv, const float *__restrict__ nu,
     const float *__restrict__ H, const float *__restrict__ S0, const float *__restrict__ E0,
     float *__restrict__ vr, float *__restrict__ dv, float *__restrict__ E,
-    float *__restrict__ qplus, float *__restrict__ qminus, int i, int j)
+    float *__restrict__ qplus, float *__restrict__ qminus, const float *__restrict__ corr_phi,
+    const float *__restrict__ corr_r, int i, int j)
 {
     const int nz = g.nz, nr = g.nr;
     const size_t c = CELL(i, j);
     const int jp = jprev(j, nz), jn = jnext(j, nz);
+    // pseudo-implicit limiter of StabilizeViscosity 1, viscosity.cpp:395-399
+    auto stabilized = [&](float d, float cc) {
+        const float a = 1.f + dt * cc;
+        return d * (1.f / (fmaxf(a, 0.f) - dt * cc));
+    };
     if (mode & 1) {
         if (i >= 1 && i < nr - 1) {
             const float sa = 0.5f * (S[c] + S[CELL(i, jp)]);
-            dv[c] += __fdividef(dt * t.InvRmed[i], sa) *
-                     (t.TwoOverDRa2[i] * (t.RinfSq[i + 1] * trp[CELL(i + 1, j)] -
-                                          t.RinfSq[i] * trp[c]) +
-                      (tpp[c] - tpp[CELL(i, jp)]) * g.invdphi);
+            const float fac = __fdividef(dt * t.InvRmed[i], sa);
+            const float rhs = t.TwoOverDRa2[i] * (t.RinfSq[i + 1] * trp[CELL(i + 1, j)] -
+                                                  t.RinfSq[i] * trp[c]) +
+                              (tpp[c] - tpp[CELL(i, jp)]) * g.invdphi;
+            // the fused form is spelled out so that every kernel built from
+            // this body rounds the update the same way
+            if (ph.stabilize == 1)
+                dv[c] += stabilized(fac * rhs, corr_phi[c]);
+            else
+                dv[c] = fmaf(fac, rhs, dv[c]);
         }
         if (i >= 2 && i < nr - 1) {
             const float sa = 0.5f * (S[c] + S[CELL(i - 1, j)]);
-            vr[c] += __fdividef(dt, sa) * ph.rvf * t.TwoOverRmedSum[i] *
-                     ((t.Rmed[i] * trr[c] - t.Rmed[i - 1] * trr[CELL(i - 1, j)]) * t.InvDiffRmed[i] +
-                      (trp[CELL(i, jn)] - trp[c]) * g.invdphi - 0.5f * (tpp[c] + tpp[CELL(i - 1, j)]));
+            const float fac = __fdividef(dt, sa) * ph.rvf * t.TwoOverRmedSum[i];
+            const float rhs =
+                (t.Rmed[i] * trr[c] - t.Rmed[i - 1] * trr[CELL(i - 1, j)]) * t.InvDiffRmed[i] +
+                (trp[CELL(i, jn)] - trp[c]) * g.invdphi - 0.5f * (tpp[c] + tpp[CELL(i - 1, j)]);
+            if (ph.stabilize == 1)
+                vr[c] += stabilized(fac * rhs, corr_r[c]);
+            else
+                vr[c] = fmaf(fac, rhs, vr[c]);
         }
     }
     if (!(mode & 6) || !ph.adiabatic) return;
@@ -1126,7 +1210,8 @@ __device__ __forceinline__ void derived_cfl_ring(
     const float *__restrict__ E, const float *__restrict__ vr, const float *__restrict__ dv,
     const float *__restrict__ qplus, const float *__restrict__ qminus, float *__restrict__ cs,
     float *__restrict__ H, float *__restrict__ P, float *__restrict__ T, float *__restrict__ nu,
-    unsigned int *__restrict__ dt_min, int i, float *red, longlong2 *red2)
+    unsigned int *__restrict__ dt_min, int i, float *red, longlong2 *red2,
+    const float *__restrict__ corr_phi, const float *__restrict__ corr_r)
 {
     const int nz = g.nz, nr = g.nr;
     const size_t row = (size_t)i * nz;
@@ -1208,7 +1293,13 @@ __device__ __forceinline__ void derived_cfl_ring(
             }
             const float s2 = invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 +
                              invdt4 * invdt4 + invdt5 * invdt5 + invdt6 * invdt6;
-            local = fminf(local, ph.cfl * rsqrtf(s2));
+            float dt_cell = ph.cfl * rsqrtf(s2);
+            if (ph.stabilize == 2) {
+                // viscous stability limit, cfl.cpp:332-351
+                const float cc = fminf(corr_phi[c], corr_r[c]);
+                if (cc != 0.f) dt_cell = fminf(dt_cell, -ph.cfl / cc);
+            }
+            local = fminf(local, dt_cell);
         }
     }
     if (do_cfl) {

@@ -35,6 +35,10 @@ struct TablesF {
     const float *DJ;        // J_K(i-1) - J_K(i), J_K = r v_K
     const float *JSlope;    // (J_K(i+1) - J_K(i)) / (Rmed(i+1) - Rmed(i))
     const float *DRmed;     // Rmed(i) - Rmed(i-1)
+    const float *LSqTW;     // TW length scale squared, pow(C, 2) pow(max(dr, r dphi), 2)
+    const float *TwoOverDRmed2; // 2 / (Rmed(i)^2 - Rmed(i-1)^2)
+    // StabilizeViscosity correction-factor ring terms (viscosity.cpp:280-331)
+    const float *Ra3IDRmed, *F43, *CrPp1, *CrPp2, *CrRr1, *CrRr2, *CrRp, *CrScale;
     const float *DRsup;     // Rsup(i) - Rinf(i), formed in FP64 (an FP32 difference of
                             // the radii loses ~1e-4 of it on fine grids)
     const float *RsupIDRR;  // Rsup(i) / ((Rsup(i) - Rinf(i)) Rmed(i)): div v without
@@ -46,6 +50,8 @@ struct TablesF {
 
 struct PhysF {
     int adiabatic, art_visc_sn, dissipation, limiter_mc, fast_transport;
+    int art_visc_tw;  // Tscharnuter-Winkler artificial viscosity
+    int stabilize;    // StabilizeViscosity 0 / 1 / 2
     int heating_viscous, cooling_beta, beta_ref;
     int leapfrog;  // LeapFrog integrator: three CFL limits x 0.6
     float gm1, g_gm1, mu, alpha, constant_viscosity, C2, four_C2, rvf, hvf, cfl, inv_hc_limit;
@@ -82,6 +88,13 @@ struct DampQF {
 };
 struct DampingF {
     DampQF q[4];
+};
+
+// One planet's accretion region and constants (accretion.cpp:84-480), as the
+// host finds them (see fgpu_accrete_onto_planet).
+struct AccrF {
+    int type, i0, i1, j0, ncols;
+    double x, y, rhill, frac1, frac2, facc1, facc2, f_const, dist_max, density_floor, omf;
 };
 
 // Host constants of every boundary hook in FP64 (api.cu), shared by both forms.
@@ -157,6 +170,7 @@ class Engine32 {
     // the step's buffers are the ones the batched kernels were given
     bool canonical() const { return fld[FGPU_V_RADIAL] == vr_a && fld[FGPU_V_AZIMUTHAL] == dv_a; }
     int disk_force(double px, double py, double pa, double rsm, double out[5]);
+    int accrete(const AccrF &a, double out[3]);
     int check_finite(int *field, int *nr_out, int *naz_out);
     // the device description used by the batched kernels
     DiskF describe();
@@ -213,6 +227,8 @@ class Engine32 {
     size_t az_smem = 0;
     bool az_stage = false;
     bool visc_recompute = false;  // c_s, H, nu before the final hooks (adiabatic)
+    float *corr_phi = nullptr, *corr_r = nullptr;  // StabilizeViscosity factors
+    void visc_corr(const StateF &s);
     bool cfl_valid = false;
 };
 

@@ -96,12 +96,24 @@ __global__ void f_viscous(GeoF g, TablesF t, PhysF ph, float dt, float beta_inv,
                           const float *__restrict__ H, const float *__restrict__ S0,
                           const float *__restrict__ E0, float *__restrict__ vr,
                           float *__restrict__ dv, float *__restrict__ E, float *__restrict__ qplus,
-                          float *__restrict__ qminus)
+                          float *__restrict__ qminus, const float *__restrict__ corr_phi,
+                          const float *__restrict__ corr_r)
 {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= g.nz) return;
     viscous_cell(g, t, ph, dt, beta_inv, mode, S, trr, tpp, trp, divv, nu, H, S0, E0, vr, dv, E,
-                 qplus, qminus, blockIdx.y, j);
+                 qplus, qminus, corr_phi, corr_r, blockIdx.y, j);
+}
+
+// StabilizeViscosity's correction factors, rows 1 .. nr - 1
+__global__ void f_visc_corr(GeoF g, TablesF t, const float *__restrict__ S,
+                            const float *__restrict__ nu, float *__restrict__ corr_phi,
+                            float *__restrict__ corr_r)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y + 1;
+    if (j >= g.nz || i >= g.nr) return;
+    visc_corr_cell(g, t, S, nu, corr_phi, corr_r, i, j);
 }
 
 __global__ void f_ghost(GeoF g, BcF bc, StateF s)
@@ -175,12 +187,14 @@ __global__ void f_derived_cfl(GeoF g, TablesF t, PhysF ph, int mode, const float
                               const float *__restrict__ dv, const float *__restrict__ qplus,
                               const float *__restrict__ qminus, float *__restrict__ cs,
                               float *__restrict__ H, float *__restrict__ P, float *__restrict__ T,
-                              float *__restrict__ nu, unsigned int *__restrict__ dt_min)
+                              float *__restrict__ nu, unsigned int *__restrict__ dt_min,
+                              const float *__restrict__ corr_phi,
+                              const float *__restrict__ corr_r)
 {
     __shared__ float red[33];
     __shared__ longlong2 red2[33];
     derived_cfl_ring(g, t, ph, mode, S, E, vr, dv, qplus, qminus, cs, H, P, T, nu, dt_min,
-                     blockIdx.x, red, red2);
+                     blockIdx.x, red, red2, corr_phi, corr_r);
 }
 
 // disk force on a body and gas mass: FP64 separations and accumulation
@@ -313,13 +327,25 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
     enum { RINF, RSUP, RMED, SURF, INVRMED, INVSURF, INVDIFFRMED, INVDIFFRSUP, INVDIFFRSUPRB,
            INVRINF, RINFSQ, TWOOVER, OMEGAK, INVOMEGAK, CSISO, INVDXSRC, INVDXTHETA, EMODEL,
            HFACADI, INVCELL, INVCELL2, TWOOVERRMEDSUM, KBAL, AFACE, SHEAR, DJ, JSLOPE, DRMED,
-           OMREFDIFF, VREF, DRSUP, RSUPIDRR, NT };
+           OMREFDIFF, VREF, DRSUP, RSUPIDRR, LSQTW, TWOOVERDRMED2, RA3IDRMED, F43, CRPP1,
+           CRPP2, CRRR1, CRRR2, CRRP, CRSCALE, NT };
     std::vector<float> hf((size_t)NT * R, 0.f);
     auto F = [&](int k) { return hf.data() + (size_t)k * R; };
     for (int n = 0; n <= nr; ++n) {
         const double rm = Rmed[n], dxr = Rsup[n] - Rinf[n], dxa = rm * dphi;
         F(DRSUP)[n] = (float)dxr;
         F(RSUPIDRR)[n] = (float)(Rsup[n] / (dxr * rm));
+        F(F43)[n] = (float)(4.0 / 3.0 / rm * (1.0 / dphi) * (1.0 / dphi));
+        F(CRRP)[n] = (float)(1.0 / (dphi * dphi * Rinf[n]));
+        if (n >= 1) {
+            F(RA3IDRMED)[n] = (float)(std::pow(Rinf[n], 3) / (rm - Rmed[n - 1]));
+        }
+        if (n < nr) {
+            // artificial_viscosity.cpp:60-73
+            const double Dr = Rinf[n + 1] - Rinf[n];
+            const double dxtw = nz <= 16 ? std::min(Dr, dxa) : std::max(Dr, dxa);
+            F(LSQTW)[n] = (float)(std::pow(p.art_visc_factor, 2) * std::pow(dxtw, 2));
+        }
         const double om = std::sqrt(G * M / (rm * rm * rm));
         const double cell = std::min(dxr, dxa);
         F(RINF)[n] = (float)Rinf[n];
@@ -354,6 +380,19 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
         F(INVDIFFRMED)[n] = (float)idr;
         F(TWOOVERRMEDSUM)[n] = (float)(2.0 / (Rmed[n] + Rmed[n - 1]));
         F(DRMED)[n] = (float)(Rmed[n] - Rmed[n - 1]);
+        F(TWOOVERDRMED2)[n] = (float)(2.0 / (std::pow(Rmed[n], 2) - std::pow(Rmed[n - 1], 2)));
+        {
+            // StabilizeViscosity ring terms, viscosity.cpp:280-331 (Ra = Rinf)
+            const double ra = Rinf[n], idr_sup = 1.0 / (Rsup[n] - Rinf[n]);
+            const double idr_sup_m = 1.0 / (Rsup[n - 1] - Rinf[n - 1]);
+            const double irb = 1.0 / ((Rsup[n] - Rinf[n]) * Rmed[n]);
+            const double irb_m = 1.0 / ((Rsup[n - 1] - Rinf[n - 1]) * Rmed[n - 1]);
+            F(CRPP1)[n] = (float)(2.0 * (0.5 / Rmed[n] + 1.0 / 3.0 * ra * irb));
+            F(CRPP2)[n] = (float)(2.0 * (0.5 / Rmed[n - 1] - 1.0 / 3.0 * ra * irb_m));
+            F(CRRR1)[n] = (float)(Rmed[n] * 2.0 * (-idr_sup + 1.0 / 3.0 * ra * irb));
+            F(CRRR2)[n] = (float)(-1.0 * Rmed[n - 1] * 2.0 * (idr_sup_m - 1.0 / 3.0 * ra * irb_m));
+            F(CRSCALE)[n] = (float)(p.radial_viscosity_factor / (0.5 * (Rmed[n] + Rmed[n - 1])));
+        }
         F(DJ)[n] = (float)(Jref[n - 1] - Jref[n]);
         F(SHEAR)[n] = (float)((Vref[n] / Rmed[n] - Vref[n - 1] / Rmed[n - 1]) * idr);
         const double A = 0.5 * (Vref[n] + Vref[n - 1]);
@@ -389,7 +428,10 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
     t.InvDxTheta = Df(INVDXTHETA); t.EModel = Df(EMODEL); t.HFacAdi = Df(HFACADI);
     t.InvCell = Df(INVCELL); t.InvCell2 = Df(INVCELL2); t.TwoOverRmedSum = Df(TWOOVERRMEDSUM);
     t.Kbal = Df(KBAL); t.Aface = Df(AFACE); t.Shear = Df(SHEAR); t.DJ = Df(DJ);
-    t.JSlope = Df(JSLOPE); t.DRmed = Df(DRMED); t.DRsup = Df(DRSUP); t.RsupIDRR = Df(RSUPIDRR); t.OmRefDiff = Df(OMREFDIFF); t.Vref = Df(VREF);
+    t.JSlope = Df(JSLOPE); t.DRmed = Df(DRMED); t.DRsup = Df(DRSUP); t.RsupIDRR = Df(RSUPIDRR);
+    t.LSqTW = Df(LSQTW); t.TwoOverDRmed2 = Df(TWOOVERDRMED2);
+    t.Ra3IDRmed = Df(RA3IDRMED); t.F43 = Df(F43); t.CrPp1 = Df(CRPP1); t.CrPp2 = Df(CRPP2);
+    t.CrRr1 = Df(CRRR1); t.CrRr2 = Df(CRRR2); t.CrRp = Df(CRRP); t.CrScale = Df(CRSCALE); t.OmRefDiff = Df(OMREFDIFF); t.Vref = Df(VREF);
     t.Rmed_d = tab_d; t.InvRmed_d = tab_d + R; t.Vref_d = tab_d + 2 * R; t.Surf_d = tab_d + 3 * R;
     t.PhiK_d = tab_d + 4 * R; t.cos_d = tab_d + 5 * R; t.sin_d = tab_d + 5 * R + nz;
 
@@ -397,6 +439,8 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
     PhysF &ph = phys;
     ph.adiabatic = p.eos == FGPU_EOS_IDEAL;
     ph.art_visc_sn = p.art_visc == FGPU_ARTVISC_SN;
+    ph.art_visc_tw = p.art_visc == FGPU_ARTVISC_TW;
+    ph.stabilize = p.stabilize_viscosity;
     ph.dissipation = p.art_visc_dissipation;
     ph.limiter_mc = p.flux_limiter == FGPU_LIMITER_MC;
     ph.fast_transport = p.fast_transport;
@@ -454,6 +498,13 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
     CKF(cudaMalloc(&d_bad, sizeof(unsigned long long)));
     CKF(cudaMallocHost(&h_pinned, sizeof(double) * 16));
     CKF(cudaMalloc(&stage, sizeof(double) * vcells));
+    if (p.stabilize_viscosity) {
+        // zero until the first stress evaluation, like the reference's grids
+        CKF(cudaMalloc(&corr_phi, cells * sizeof(float)));
+        CKF(cudaMalloc(&corr_r, cells * sizeof(float)));
+        CKF(cudaMemset(corr_phi, 0, cells * sizeof(float)));
+        CKF(cudaMemset(corr_r, 0, cells * sizeof(float)));
+    }
 
     // boundary hooks on the residual v_phi
     bc.sigma_in = p.bc_sigma_inner; bc.sigma_out = p.bc_sigma_outer;
@@ -601,6 +652,7 @@ void Engine32::destroy()
     cudaFree(sigma_lo); cudaFree(alt_sigma_lo);
     for (int k = 0; k < 4; ++k) cudaFree(mom[k]);
     cudaFree(partial); cudaFree(red_out); cudaFree(d_dtmin); cudaFree(d_bad); cudaFree(stage);
+    cudaFree(corr_phi); cudaFree(corr_r);
     cudaFree(tab_f); cudaFree(tab_d); cudaFree(damp_mem); cudaFree(damp_aux); cudaFree(damp_rings);
     if (h_pinned) cudaFreeHost(h_pinned);
 }
@@ -720,10 +772,18 @@ int Engine32::derived_cfl(int mode)
     f_derived_cfl<<<nr, 256, 0, stream>>>(geo, tabs, phys, mode, s.sigma, s.energy, s.vr, s.dv,
                                           fld[FGPU_QPLUS], fld[FGPU_QMINUS], fld[FGPU_SOUNDSPEED],
                                           fld[FGPU_SCALE_HEIGHT], fld[FGPU_PRESSURE],
-                                          fld[FGPU_TEMPERATURE], fld[FGPU_VISCOSITY], d_dtmin);
+                                          fld[FGPU_TEMPERATURE], fld[FGPU_VISCOSITY], d_dtmin,
+                                          corr_phi, corr_r);
     CKF(cudaGetLastError());
     if (mode & 4) cfl_valid = true;
     return FGPU_OK;
+}
+
+// StabilizeViscosity's correction factors from the current nu and sigma
+void Engine32::visc_corr(const StateF &s)
+{
+    f_visc_corr<<<dim3((nz + 127) / 128, nr - 1), 128, 0, stream>>>(
+        geo, tabs, s.sigma, fld[FGPU_VISCOSITY], corr_phi, corr_r);
 }
 
 int Engine32::init_euler(double t)
@@ -736,11 +796,12 @@ int Engine32::init_euler(double t)
                                                     fld[FGPU_VISCOSITY], fld[FGPU_DIV_V],
                                                     fld[FGPU_TAU_R_R], fld[FGPU_TAU_PHI_PHI],
                                                     fld[FGPU_TAU_R_PHI]);
+        if (phys.stabilize) visc_corr(s);
         f_viscous<<<grid2(nz, nr), 128, 0, stream>>>(
             geo, tabs, phys, 0.f, (float)beta_inv(t), 2, s.sigma, fld[FGPU_TAU_R_R],
             fld[FGPU_TAU_PHI_PHI], fld[FGPU_TAU_R_PHI], fld[FGPU_DIV_V], fld[FGPU_VISCOSITY],
             fld[FGPU_SCALE_HEIGHT], s.sigma0, s.energy0, s.vr, s.dv, s.energy, fld[FGPU_QPLUS],
-            fld[FGPU_QMINUS]);
+            fld[FGPU_QMINUS], corr_phi, corr_r);
         CKF(cudaGetLastError());
     }
     cfl_valid = false;
@@ -805,7 +866,7 @@ int Engine32::kick(double dt, double t)
     std::swap(fld[FGPU_V_AZIMUTHAL], alt_dv);
     mark(1);
     StateF s = state();
-    if (adi || phys.art_visc_sn) {
+    if (adi || phys.art_visc_sn || phys.art_visc_tw) {
         f_artvisc_q<<<grid2(nz, nr), 128, 0, stream>>>(geo, tabs, phys, fdt, s.sigma, s.vr, s.dv,
                                                        s.energy, fld[FGPU_Q_R], fld[FGPU_Q_PHI]);
         mark(2);
@@ -821,12 +882,13 @@ int Engine32::kick(double dt, double t)
                                                 fld[FGPU_VISCOSITY], fld[FGPU_DIV_V],
                                                 fld[FGPU_TAU_R_R], fld[FGPU_TAU_PHI_PHI],
                                                 fld[FGPU_TAU_R_PHI]);
+    if (phys.stabilize) visc_corr(s);
     mark(4);
     f_viscous<<<grid2(nz, nr), 128, 0, stream>>>(
         geo, tabs, phys, fdt, (float)beta_inv(t), adi ? 7 : 1, s.sigma, fld[FGPU_TAU_R_R],
         fld[FGPU_TAU_PHI_PHI], fld[FGPU_TAU_R_PHI], fld[FGPU_DIV_V], fld[FGPU_VISCOSITY],
         fld[FGPU_SCALE_HEIGHT], s.sigma0, s.energy0, s.vr, s.dv, s.energy, fld[FGPU_QPLUS],
-        fld[FGPU_QMINUS]);
+        fld[FGPU_QMINUS], corr_phi, corr_r);
     mark(5);
     CKF(cudaGetLastError());
     cfl_valid = false;
@@ -943,6 +1005,96 @@ int Engine32::disk_force(double px, double py, double pa, double rsm, double out
     CKF(cudaMemcpyAsync(h_pinned, red_out, sizeof(double) * 5, cudaMemcpyDeviceToHost, stream));
     CKF(cudaStreamSynchronize(stream));
     for (int k = 0; k < 5; ++k) out[k] = h_pinned[k];
+    return FGPU_OK;
+}
+
+// Accretion onto one planet (accretion.cpp:84-480) on the FP32 state: the
+// compensated sigma pair and the cell geometry in FP64, the removed mass and
+// momentum summed in FP64 (one block; cells are independent).
+__global__ void f_accrete(GeoF g, TablesF t, PhysF ph, AccrF a, float *__restrict__ S,
+                          float *__restrict__ S_lo, float *__restrict__ E,
+                          const float *__restrict__ vr, const float *__restrict__ dv,
+                          const float *__restrict__ nu, double *__restrict__ out)
+{
+    __shared__ double red[33];
+    const int nz = g.nz, nr = g.nr;
+    const long long cells = (long long)(a.i1 - a.i0 + 1) * a.ncols;
+    double dM = 0.0, dPx = 0.0, dPy = 0.0;
+    for (long long k = threadIdx.x; k < cells; k += blockDim.x) {
+        const int i = a.i0 + (int)(k / a.ncols);
+        int jf = (a.j0 + (int)(k % a.ncols)) % nz;
+        if (jf < 0) jf += nz;
+        const size_t l = CELL(i, jf);
+        const double rm = t.Rmed_d[i];
+        const double xc = rm * t.cos_d[jf], yc = rm * t.sin_d[jf];
+        const double dx = a.x - xc, dy = a.y - yc;
+        const double distance = sqrt(dx * dx + dy * dy);
+        const double vtcell = t.Vref_d[i] + 0.5 * ((double)dv[l] + (double)dv[CELL(i, jnext(jf, nz))]) +
+                              rm * a.omf;
+        const double vrcell = 0.5 * ((double)vr[l] + (double)vr[l + nz]);
+        const double vxcell = (vrcell * xc - vtcell * yc) / rm;
+        const double vycell = (vrcell * yc + vtcell * xc) / rm;
+        double sig = (double)S[l] + (double)S_lo[l];
+        const double sig0 = sig;
+        double e = ph.adiabatic ? (double)E[l] : 0.0;
+        const double facc_max = 1 - a.density_floor / sig0;
+        const bool active = 1 < i && i < nr - 1;
+        bool changed = false;
+        if (distance < a.frac1 * a.rhill) {
+            double f = a.facc1;
+            if (a.type == 1 /* viscous */)
+                f = a.facc1 * (double)nu[l] * (a.f_const * (1.0 - distance / a.dist_max));
+            const double fc = facc_max < f ? facc_max : f;
+            const double deltaM = fc * sig * t.Surf_d[i];
+            sig *= 1.0 - fc;
+            e *= 1.0 - fc;
+            changed = true;
+            if (active) {
+                dPx += deltaM * vxcell;
+                dPy += deltaM * vycell;
+                dM += deltaM;
+            }
+        }
+        if (a.type == 0 /* Kley */ && distance < a.frac2 * a.rhill) {
+            const double fc = facc_max < a.facc2 ? facc_max : a.facc2;
+            const double deltaM = fc * sig * t.Surf_d[i];
+            sig *= 1.0 - fc;
+            // the reference scales the energy by the uncapped factor here
+            e *= 1.0 - a.facc2;
+            changed = true;
+            if (active) {
+                dPx += deltaM * vxcell;
+                dPy += deltaM * vycell;
+                dM += deltaM;
+            }
+        }
+        if (changed) {
+            const float hi = (float)sig;
+            S[l] = hi;
+            S_lo[l] = (float)(sig - (double)hi);
+            if (ph.adiabatic) E[l] = (float)e;
+        }
+    }
+    dM = bsum_d(dM, red);
+    dPx = bsum_d(dPx, red);
+    dPy = bsum_d(dPy, red);
+    if (threadIdx.x == 0) {
+        out[0] = dM;
+        out[1] = dPx;
+        out[2] = dPy;
+    }
+}
+
+int Engine32::accrete(const AccrF &a, double out[3])
+{
+    StateF s = state();
+    f_accrete<<<1, 512, 0, stream>>>(geo, tabs, phys, a, s.sigma, s.sigma_lo, s.energy, s.vr,
+                                     s.dv, fld[FGPU_VISCOSITY], red_out);
+    CKF(cudaGetLastError());
+    CKF(cudaMemcpyAsync(h_pinned, red_out, sizeof(double) * 3, cudaMemcpyDeviceToHost, stream));
+    CKF(cudaStreamSynchronize(stream));
+    for (int k = 0; k < 3; ++k) out[k] = h_pinned[k];
+    cfl_valid = false;
     return FGPU_OK;
 }
 

@@ -133,7 +133,7 @@ typedef struct fgpu_params {
     int stabilize_viscosity; /* StabilizeViscosity (Interpret.cpp:669-681): 0 off,
                                1 pseudo-implicit viscous update, 2 viscous dt limit
                                (viscosity.cpp:256-348, 395-417; cfl.cpp:332-351);
-                               FP64 only */
+                               not in the batched form */
     int profile_cutoff_outer; /* ProfileCutoffOuter (parameters.cpp:730): balanced
                                  boundary without pressure support */
     int viscous_accretion;  /* a planet accretes with the viscous profile
@@ -287,7 +287,8 @@ typedef struct fgpu_accretor {
  * the active rings.  The host adds them to the planet (update_planet,
  * accretion.cpp:60-82) and its accreted-mass monitor.  Call it for each
  * accreting planet where step_Euler / step_LeapFrog call AccreteOntoPlanets
- * (simulation.cpp:150-153, 301-304, 402-405).  FP64 form only. */
+ * (simulation.cpp:150-153, 301-304, 402-405).  In the FP32-mixed form the
+ * removal acts on the compensated sigma pair and the sums are formed in FP64. */
 int fgpu_accrete_onto_planet(fgpu_engine *eng, const fgpu_accretor *a, double dt,
 			     double out[3]);
 
@@ -418,9 +419,10 @@ typedef struct {
 
 /* params[k], radii[k]: disk k as for fgpu_create; every disk must select
  * FGPU_PRECISION_FP32_MIXED and the Euler integrator (the batched step is
- * step_Euler); adiabatic disks with the viscous v_radial hook or viscous
- * accretion are refused (FGPU_ERR_UNSUPPORTED); the longest ring must fit the
- * azimuthal transport's shared memory (naz <= 5632).  1 <= n <= 1024. */
+ * step_Euler); StabilizeViscosity, and adiabatic disks with the viscous
+ * v_radial hook or viscous accretion, are refused (FGPU_ERR_UNSUPPORTED); the
+ * longest ring must fit the azimuthal transport's shared memory (naz <= 6257
+ * with the energy equation, 7040 without).  1 <= n <= 1024. */
 int fgpu_batch_create(int n, const fgpu_params *params,
 		      const double *const *radii, fgpu_batch **out);
 int fgpu_batch_destroy(fgpu_batch *b);

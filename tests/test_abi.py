@@ -59,11 +59,6 @@ def test_unsupported_options_are_reported(lib):
     from gpu_cases import make_params
     out = np.zeros(40)
     h = C.c_void_p()
-    # TW artificial viscosity and StabilizeViscosity are FP64 only
-    p, _ = make_params(16, 32, art_visc=abi.ARTVISC_TW, precision=1)
-    assert lib.fgpu_create(C.byref(p), out.ctypes.data_as(C.POINTER(C.c_double)), C.byref(h)) == -4
-    p, _ = make_params(16, 32, stabilize_viscosity=1, precision=1)
-    assert lib.fgpu_create(C.byref(p), out.ctypes.data_as(C.POINTER(C.c_double)), C.byref(h)) == -4
     p, _ = make_params(16, 32, stabilize_viscosity=3)
     assert lib.fgpu_create(C.byref(p), out.ctypes.data_as(C.POINTER(C.c_double)), C.byref(h)) == -1
     p, _ = make_params(16, 9000)
