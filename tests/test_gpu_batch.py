@@ -97,6 +97,49 @@ def test_host_clock_matches_single_disks_bit_for_bit():
     batch.close()
 
 
+def test_accretion_on_a_batch_disk_matches_single_disk():
+    # AccreteOntoPlanets (accretion.cpp:84-480) called on a disk of a batch
+    # between batch steps acts like the same call on a single-disk engine.
+    import math
+
+    from fargocpt_gb300.abi import ACCRETION, FgpuAccretor
+    from fargocpt_gb300.batch import Batch
+    from fargocpt_gb300.engine import Engine
+    from fargocpt_gb300.setups import log_radii
+
+    disks = []
+    for k, (nr, nz, adi) in enumerate([(24, 72, False), (16, 48, True)]):
+        p, d = make_params(nr, nz, adi, precision=1, viscous_alpha=1e-3,
+                           accretion_radius_fraction=1.5)
+        radii = log_radii(nr, 0.4, 2.5)
+        disks.append((p, radii, initial_state(d, radii, seed=30 + k)))
+    singles = [Engine(p, r) for p, r, _ in disks]
+    batch = Batch([p for p, *_ in disks], [r for _, r, _ in disks])
+    b0 = _bodies(0.0)
+    for e, (_, _, st), be in zip(singles, disks, batch.disks):
+        _load(e, st, b0)
+        _load(be, st, b0)
+    x, y = b0[1][0], b0[1][1]
+    t = np.zeros(len(disks))
+    for n in range(4):
+        dts = np.array([e.condition_cfl() for e in singles])
+        for k, (e, be) in enumerate(zip(singles, batch.disks)):
+            assert be.condition_cfl() == dts[k]
+            acc = FgpuAccretor(type=ACCRETION["kley"], x=x, y=y, r=math.hypot(x, y),
+                               phi=math.atan2(y, x), roche_radius=(1e-3 / 3) ** (1 / 3),
+                               efficiency=10.0, orbital_period=2 * math.pi)
+            ss, sb = e.accrete_onto_planet(acc, dts[k]), be.accrete_onto_planet(acc, dts[k])
+            assert ss[0] > 0 and ss == sb, (n, k, ss, sb)
+            e.step_euler(float(dts[k]), float(t[k]))
+        batch.step(dts, t)
+        t += dts
+    for k, (e, be) in enumerate(zip(singles, batch.disks)):
+        for f in EVOLVED:
+            a, b = be.get_field(f), e.get_field(f)
+            assert np.array_equal(a, b), f"disk {k} {f}: {np.max(np.abs(a - b))}"
+    batch.close()
+
+
 def _sweep(n, seed):
     from fargocpt_gb300 import setups
     return setups.sweep(n_disks=n, seed=seed, nr_choices=(16, 24, 32, 48))
