@@ -61,7 +61,10 @@ class FgpuParams(C.Structure):
         ("bc_vaz_inner", C.c_int), ("bc_vaz_outer", C.c_int),
         ("precision", C.c_int), ("integrator", C.c_int),
         ("stabilize_viscosity", C.c_int), ("profile_cutoff_outer", C.c_int),
-        ("viscous_accretion", C.c_int), ("reserved_i", C.c_int * 3),
+        ("viscous_accretion", C.c_int), ("composite_inner", C.c_int),
+        ("composite_outer", C.c_int), ("initialize_pure_keplerian", C.c_int),
+        ("initialize_vradial_zero", C.c_int), ("profile_cutoff_inner", C.c_int),
+        ("reserved_i", C.c_int * 1),
         ("gamma", C.c_double), ("mu", C.c_double), ("aspect_ratio", C.c_double),
         ("flaring_index", C.c_double), ("viscous_alpha", C.c_double),
         ("constant_viscosity", C.c_double), ("art_visc_factor", C.c_double),
@@ -84,6 +87,9 @@ class FgpuParams(C.Structure):
         ("accretion_radius_fraction", C.c_double), ("sigma_slope", C.c_double),
         ("viscous_outflow_speed", C.c_double), ("vrad_inner_keplerian_factor", C.c_double),
         ("vrad_outer_keplerian_factor", C.c_double), ("binary_quadrupole_moment", C.c_double),
+        ("profile_cutoff_point_outer", C.c_double), ("profile_cutoff_width_outer", C.c_double),
+        ("profile_cutoff_point_inner", C.c_double), ("profile_cutoff_width_inner", C.c_double),
+        ("temperature_cgs_to_code", C.c_double),
         ("reserved_d", C.c_double * 2),
     ]
 
@@ -94,6 +100,14 @@ class FgpuBody(C.Structure):
 
 
 ACCRETION = {"kley": 0, "viscous": 1, "sinkhole": 2}
+COMPOSITE = {"individual": 0, "centerofmass": 1}
+
+
+class FgpuFrameCenter(C.Structure):
+    """fgpu_frame_center: centre of mass, its velocity and the mass of a set
+    of bodies (nbody/planetary_system.cpp:580-650)."""
+    _fields_ = [("x", C.c_double), ("y", C.c_double), ("vx", C.c_double),
+                ("vy", C.c_double), ("mass", C.c_double)]
 
 
 class FgpuAccretor(C.Structure):
@@ -168,7 +182,7 @@ EXPORTED_SYMBOLS = [
     "fgpu_set_bodies", "fgpu_init_euler", "fgpu_recalculate_derived",
     "fgpu_condition_cfl", "fgpu_apply_boundary_condition", "fgpu_step_euler",
     "fgpu_disk_on_planet_accel", "fgpu_total_mass", "fgpu_accrete_onto_planet",
-    "fgpu_check_finite",
+    "fgpu_check_finite", "fgpu_init_center_of_mass_boundary", "fgpu_set_frame_centers",
     "fgpu_synchronize", "fgpu_set_phase_timing", "fgpu_phase_times", "fgpu_phase_name",
     "fgpu_disk_force_static", "fgpu_gas_kick", "fgpu_transport", "fgpu_compute_pressure",
     "fgpu_snapshot_begin", "fgpu_snapshot_wait", "fgpu_host_alloc", "fgpu_host_free",
@@ -201,6 +215,9 @@ def _declare(lib: C.CDLL) -> C.CDLL:
         "fgpu_total_mass": ([vp, dp], C.c_int),
         "fgpu_accrete_onto_planet": ([vp, C.POINTER(FgpuAccretor), C.c_double, dp], C.c_int),
         "fgpu_check_finite": ([vp, P(C.c_int), P(C.c_int), P(C.c_int)], C.c_int),
+        "fgpu_init_center_of_mass_boundary": ([vp, C.c_double, C.c_double, C.c_int,
+                                               C.c_double], C.c_int),
+        "fgpu_set_frame_centers": ([vp, P(FgpuFrameCenter), P(FgpuFrameCenter)], C.c_int),
         "fgpu_synchronize": ([vp], C.c_int),
         "fgpu_set_phase_timing": ([vp, C.c_int], C.c_int),
         "fgpu_phase_times": ([vp, dp, C.c_int, P(C.c_int), P(C.c_int)], C.c_int),

@@ -17,6 +17,8 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <mutex>
+#include <unordered_map>
 #include <vector>
 
 using namespace fgpu;
@@ -68,6 +70,13 @@ struct fgpu_engine {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t snap_staged = nullptr, snap_copied = nullptr;
     bool snap_pending = false;
+
+    // centre-of-mass composite boundary: constants, tables on the device
+    // (com_mem), and the centres of the current and the post-N-body state
+    ComSpec com{};
+    bool com_any = false, com_ready = false;
+    ComCenter com_now[2]{}, com_after[2]{};
+    double *com_mem = nullptr;
 
     fgpu32::Engine32 *e32 = nullptr;  // FP32-mixed form, when selected
     bool owns_stream = true;          // false for the disks of a batch
@@ -153,9 +162,8 @@ extern "C" int fgpu_get_stream(const fgpu_engine *eng, void **stream)
 // ------------------------------------------------------------------------
 // damping ring search (find_cell_id.cpp:222-452 with NDEBUG clamping)
 // ------------------------------------------------------------------------
-static int cell_id(const fgpu_engine *e, const std::vector<double> &Rmed, double r, bool rinf)
+static int cell_id_p(const fgpu_params &p, int nr, const double *Rmed, double r, bool rinf)
 {
-    const fgpu_params &p = e->p;
     int id;
     if (p.radial_spacing == FGPU_SPACING_LOGARITHMIC) {
         const double g = std::pow(p.rmax / p.rmin, 1.0 / ((double)p.nrad - 2.0));
@@ -169,12 +177,36 @@ static int cell_id(const fgpu_engine *e, const std::vector<double> &Rmed, double
     } else {
         const double g = ((double)p.nrad - 2.0) / (p.rmax - p.rmin);
         id = (int)std::floor((r - p.rmin) * g) + 1;
-        if (!rinf && id >= 0 && id <= e->nr && Rmed[id] > r) id--;
+        if (!rinf && id >= 0 && id <= nr && Rmed[id] > r) id--;
     }
     if (id < 0) id = 0;
-    if (id > e->nr - 1) id = e->nr - 1;
+    if (id > nr - 1) id = nr - 1;
     return id;
 }
+
+static int cell_id(const fgpu_engine *e, const std::vector<double> &Rmed, double r, bool rinf)
+{
+    return cell_id_p(e->p, e->nr, Rmed.data(), r, rinf);
+}
+
+// Dynamic shared-memory limits belong to the kernel, process-wide: an engine
+// may only raise a limit, or a later engine with shorter rings would shrink
+// it under the launches of an earlier one.
+cudaError_t raise_smem_limit(const void *fn, size_t bytes)
+{
+    static std::mutex mu;
+    static std::unordered_map<const void *, size_t> limit;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t &cur = limit[fn];
+    if (bytes <= cur) return cudaSuccess;
+    const cudaError_t e =
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) cur = bytes;
+    return e;
+}
+
+// nodes of each viscous-speed lookup table (viscous_radial_speed.cpp:256)
+constexpr int kComTableNodes = 1000;
 
 static int clamp_id(int id, bool vec, int nr)
 {
@@ -218,6 +250,20 @@ static int validate(const fgpu_params *p, std::string &why)
         }
     }
     if (!(p->cfl > 0) || !(p->G > 0) || !(p->hydro_center_mass > 0)) { why = "cfl, G, mass must be > 0"; return FGPU_ERR_BAD_ARG; }
+    const int comp[2] = {p->composite_inner, p->composite_outer};
+    for (int side = 0; side < 2; ++side) {
+        if (comp[side] != FGPU_COMPOSITE_INDIVIDUAL && comp[side] != FGPU_COMPOSITE_CENTER_OF_MASS) {
+            why = "composite boundary kind"; return FGPU_ERR_BAD_ARG;
+        }
+        if (comp[side] != FGPU_COMPOSITE_CENTER_OF_MASS) continue;
+        // boundary_conditions/config.cpp:512-528
+        for (int q = 0; q < 4; ++q) {
+            if ((side ? p->damping_outer[q] : p->damping_inner[q]) != FGPU_DAMP_NONE) {
+                why = "damping is enabled twice: per field and through the center-of-mass boundary";
+                return FGPU_ERR_BAD_ARG;
+            }
+        }
+    }
     return FGPU_OK;
 }
 
@@ -296,6 +342,163 @@ void boundary_values(const fgpu_params &p, const double *Rmed, const double *Rin
             default:
                 break;
             }
+        }
+    }
+}
+
+// viscous_speed::init_vr_table_boundary (viscosity/viscous_radial_speed.cpp:
+// 269-347) with the model functions it evaluates (get_sigma, get_nu2, get_w,
+// derive, get_vr_with_numerical_viscous_speed and the outer grid correction,
+// viscous_radial_speed.cpp:14-254; Theo.cpp:131-200).  radii holds nr + 2
+// interface radii (Radii[0 .. nr + 1]).  Each table gets n + 1 nodes: the
+// reference interpolates from node i to node i + 1 and has n, so that a radius
+// in its last bin reads past the table; the extra node is that next node of
+// the same formula.
+void viscous_speed_tables(const fgpu_params &p, const double *radii, const double *Rmed, int nr,
+                          double mass_all, double mass_center, bool binary_on_primary,
+                          double com_max_dist, int n, double min_r[2], double dlog[2],
+                          double *r_tab, double *vr_tab)
+{
+    const bool adi = p.eos == FGPU_EOS_IDEAL;
+    auto cut_out = [&](double x) {
+        return 1.0 / (1.0 + std::exp((x - p.profile_cutoff_point_outer) / p.profile_cutoff_width_outer));
+    };
+    auto cut_in = [&](double x) {
+        return 1.0 / (1.0 + std::exp((p.profile_cutoff_point_inner - x) / p.profile_cutoff_width_inner));
+    };
+    auto get_sigma = [&](double R) {
+        double d = p.sigma0 * std::pow(R, -p.sigma_slope);
+        const double floor = p.sigma_floor * p.sigma0;
+        if (p.profile_cutoff_outer) d *= cut_out(R);
+        if (p.profile_cutoff_inner) d *= cut_in(R);
+        return std::max(d, floor);
+    };
+    auto get_nu2 = [&](double R, double M, double Sigma) {
+        const double v_k = std::sqrt(p.G * M / R);
+        const double h = p.aspect_ratio * std::pow(R, p.flaring_index);
+        double cutoff = 1.0;
+        if (p.profile_cutoff_outer) cutoff *= cut_out(R);
+        if (p.profile_cutoff_inner) cutoff *= cut_in(R);
+        double cs_adb, H;
+        if (adi) {
+            const double gamma = p.gamma;
+            double energy = cutoff * 1.0 / (gamma - 1.0) * Sigma * std::pow(h * v_k, 2);
+            const double energy_floor = p.minimum_temperature * Sigma / p.mu * p.R_gas / (gamma - 1.0);
+            const double energy_ceil = p.maximum_temperature * Sigma / p.mu * p.R_gas / (gamma - 1.0);
+            energy = std::max(energy, energy_floor);
+            energy = std::min(energy, energy_ceil);
+            cs_adb = std::sqrt(gamma * (gamma - 1.0) * energy / Sigma);
+            const double cs_iso = std::sqrt((gamma - 1.0) * energy / Sigma);
+            H = cs_iso / (v_k / R);
+        } else {
+            cs_adb = h * v_k;
+            H = h * R;
+        }
+        return p.viscous_alpha * cs_adb * H;
+    };
+    // the smoothed, pressure-supported angular velocity; the quadrupole term
+    // is zero unless VazimuthalConsidersQuadropoleMoment is set
+    auto get_w = [&](double R, double M) {
+        const double F = p.flaring_index, S = p.sigma_slope;
+        const double h = p.aspect_ratio * std::pow(R, F);
+        const double eps = p.thickness_smoothing;
+        const double smooth = (1.0 + (F + 1.0) * std::pow(h * eps, 2)) /
+                              std::pow(std::sqrt(1 + std::pow(h * eps, 2)), 3);
+        const double press = (2.0 * F - 1.0 - S) * std::pow(h, 2);
+        const double quad = p.binary_quadrupole_moment > 0.0
+                                ? 3.0 * p.binary_quadrupole_moment / std::pow(R, 2) : 0.0;
+        const double vk_2 = p.G * M / R;
+        return std::sqrt(vk_2 * (quad + smooth + press)) / R;
+    };
+    auto derive = [](double x, auto &&f) {
+        const double h = 8.0e-4 * x;
+        const double f1 = -1.0 * f(x + 2.0 * h);
+        const double f2 = 8.0 * f(x + h);
+        const double f3 = -8.0 * f(x - h);
+        const double f4 = 1.0 * f(x - 2.0 * h);
+        return (f1 + f2 + f3 + f4) / (12.0 * h);
+    };
+    auto vr_numerical = [&](double r, double M) {
+        auto w = [&](double x) { return get_w(x, M); };
+        auto nu_S_r3_dwdr = [&](double x) {
+            const double dw_dr = derive(x, w);
+            const double Sigma = get_sigma(x);
+            return get_nu2(x, M, Sigma) * Sigma * std::pow(x, 3) * dw_dr;
+        };
+        auto r2_w = [&](double x) { return std::pow(x, 2) * get_w(x, M); };
+        const double num = 1.0 / r * derive(r, nu_S_r3_dwdr);
+        const double den = get_sigma(r) * derive(r, r2_w);
+        return num / den;
+    };
+    // GlobalRmed (init.cpp:176-179) up to index nr
+    std::vector<double> grmed(nr + 1);
+    for (int k = 0; k <= nr; ++k) {
+        grmed[k] = 2.0 / 3.0 * (std::pow(radii[k + 1], 3) - std::pow(radii[k], 3));
+        grmed[k] = grmed[k] / (std::pow(radii[k + 1], 2) - std::pow(radii[k], 2));
+    }
+    auto outer_correction = [&](double r, double M) {
+        const int id = cell_id_p(p, nr, Rmed, r, false);
+        const int k = std::max(2, std::min(std::max(id, 0), nr));
+        const double rinf = radii[k];
+        const double rmed_p = grmed[k + 1], rmed = grmed[k], rmed_m = grmed[k - 1],
+                     rmed_m2 = grmed[k - 2];
+        const double w_p = get_w(rmed_p, M), w = get_w(rmed, M), w_m = get_w(rmed_m, M),
+                     w_m2 = get_w(rmed_m2, M);
+        const double dw_dr = (0.5 * (w_p + w) - 0.5 * (w + w_m)) / (radii[k + 1] - radii[k]);
+        const double dw_dr_m = (0.5 * (w + w_m) - 0.5 * (w_m + w_m2)) / (radii[k] - radii[k - 1]);
+        const double Sigma = get_sigma(rmed);
+        const double nu = get_nu2(rmed, M, Sigma);
+        const double Sigma_m = get_sigma(rmed_m);
+        const double nu_m = get_nu2(rmed_m, M, Sigma_m);
+        const double a = nu * Sigma * std::pow(rmed, 3) * dw_dr;
+        const double a_m = nu_m * Sigma_m * std::pow(rmed_m, 3) * dw_dr_m;
+        const double num = 1.0 / rinf * (a - a_m) / (rmed - rmed_m);
+        const double r2w = std::pow(rmed, 2) * get_w(rmed, M);
+        const double r2w_m = std::pow(rmed_m, 2) * get_w(rmed_m, M);
+        const double den = Sigma_m * ((r2w - r2w_m) / (rmed - rmed_m));
+        return (num / den) / vr_numerical(rinf, M);
+    };
+    const double *Rinf = radii, *Rsup = radii + 1;
+    // outer edge
+    {
+        const double safety = Rsup[nr - 1] - Rinf[nr - 1];
+        double lo, hi;
+        if (binary_on_primary) {
+            lo = Rinf[nr - 1] * p.damping_outer_limit - com_max_dist - safety;
+            hi = Rsup[nr - 1] + com_max_dist + safety;
+        } else {
+            lo = Rinf[nr - 1] * p.damping_outer_limit - safety;
+            hi = Rsup[nr - 1] + safety;
+        }
+        lo = std::max(p.rmin, lo);
+        min_r[1] = lo;
+        dlog[1] = std::log10(hi / lo) / (double)n;
+        for (int i = 0; i <= n; ++i) {
+            const double r = lo * std::pow(10.0, (dlog[1] * (double)i));
+            r_tab[(n + 1) + i] = r;
+            vr_tab[(n + 1) + i] = vr_numerical(r, mass_all) * outer_correction(r, mass_all);
+        }
+    }
+    // inner edge
+    {
+        const int lim = clamp_id(cell_id_p(p, nr, Rmed, p.rmin * p.damping_inner_limit, false),
+                                 false, nr) + 1;
+        const double safety = Rsup[lim] - Rinf[lim];
+        double lo, hi;
+        if (binary_on_primary) {
+            lo = Rinf[1] - com_max_dist - safety;
+            lo = std::max(lo, Rsup[0] - Rinf[0]);
+            hi = Rsup[1] * p.damping_inner_limit + com_max_dist + safety;
+        } else {
+            lo = Rinf[1] - safety;
+            hi = Rsup[1] * p.damping_inner_limit + safety;
+        }
+        min_r[0] = lo;
+        dlog[0] = std::log10(hi / lo) / (double)n;
+        for (int i = 0; i <= n; ++i) {
+            const double r = lo * std::pow(10.0, (dlog[0] * (double)i));
+            r_tab[i] = r;
+            vr_tab[i] = vr_numerical(r, mass_center);
         }
     }
 }
@@ -471,6 +674,76 @@ static int setup_tables(fgpu_engine *eng, const double *radii)
     if (!rings.empty()) {
         CK(cudaMalloc(&eng->damp_rings, sizeof(int) * rings.size()));
         CK(cudaMemcpy(eng->damp_rings, rings.data(), sizeof(int) * rings.size(), cudaMemcpyHostToDevice));
+    }
+
+    // centre-of-mass composite boundary: constants, half-cell trig tables and
+    // the damping rings of center_of_mass.cpp:339-720
+    eng->com_any = p.composite_inner == FGPU_COMPOSITE_CENTER_OF_MASS ||
+                   p.composite_outer == FGPU_COMPOSITE_CENTER_OF_MASS;
+    if (eng->com_any) {
+        ComSpec &c = eng->com;
+        c.active[0] = p.composite_inner == FGPU_COMPOSITE_CENTER_OF_MASS;
+        c.active[1] = p.composite_outer == FGPU_COMPOSITE_CENTER_OF_MASS;
+        c.pure_keplerian = p.initialize_pure_keplerian;
+        c.vr_zero = p.initialize_vradial_zero;
+        c.adiabatic = p.eos == FGPU_EOS_IDEAL;
+        c.G = p.G; c.h0 = p.aspect_ratio; c.F = p.flaring_index; c.S = p.sigma_slope;
+        c.eps = p.thickness_smoothing; c.Q = p.binary_quadrupole_moment;
+        c.sigma0 = p.sigma0; c.gamma_m1 = p.gamma - 1.0;
+        c.alpha = p.viscous_alpha; c.nu_const = p.constant_viscosity;
+        c.sqrt_gamma = c.adiabatic ? std::sqrt(p.gamma) : 1.0;
+        c.energy_floor = p.minimum_temperature * p.temperature_cgs_to_code / p.mu * p.R_gas /
+                         (p.gamma - 1.0);
+        c.n = kComTableNodes;
+        const size_t N1 = (size_t)kComTableNodes + 1;
+        // cos_h, sin_h, fac_vr[2], fac_az[2], r_tab[2], vr_tab[2]
+        const size_t count = 2 * (size_t)nz + 4 * (size_t)(nr + 1) + 4 * N1;
+        CK(cudaMalloc(&eng->com_mem, sizeof(double) * count));
+        std::vector<double> hc(count, 0.0);
+        double *ch = hc.data(), *sh = ch + nz;
+        for (int j = 0; j < nz; ++j) {
+            const double phi = ((double)j - 0.5) * dphi;  // center_of_mass.cpp:60
+            ch[j] = std::cos(phi);
+            sh[j] = std::sin(phi);
+        }
+        double *fv[2] = {sh + nz, sh + nz + (nr + 1)};
+        double *fa[2] = {sh + nz + 2 * (nr + 1), sh + nz + 3 * (nr + 1)};
+        const double rin = p.rmin * p.damping_inner_limit, rout = p.rmax * p.damping_outer_limit;
+        for (int n = 0; n <= nr; ++n) {
+            fv[0][n] = std::pow((T(RINF)[n] - rin) / (p.rmin - rin), 2);
+            fv[1][n] = std::pow((T(RINF)[n] - rout) / (p.rmax - rout), 2);
+            // the inner v_phi and energy damping use the outer zone's profile
+            // (center_of_mass.cpp:628-631, 689-692)
+            fa[0][n] = std::pow((T(RMED)[n] - rout) / (p.rmax - rout), 2);
+            fa[1][n] = fa[0][n];
+        }
+        CK(cudaMemcpy(eng->com_mem, hc.data(), sizeof(double) * count, cudaMemcpyHostToDevice));
+        double *dm = eng->com_mem;
+        c.cos_h = dm; c.sin_h = dm + nz;
+        c.Rinf = eng->tabs.Rinf; c.Rsup = eng->tabs.Rsup; c.Rmed = eng->tabs.Rmed;
+        c.cos_j = eng->tabs.cosj; c.sin_j = eng->tabs.sinj;
+        for (int k = 0; k < 2; ++k) {
+            c.fac_vr[k] = dm + 2 * nz + k * (nr + 1);
+            c.fac_az[k] = dm + 2 * nz + (2 + k) * (nr + 1);
+            c.r_tab[k] = dm + 2 * nz + 4 * (nr + 1) + k * N1;
+            c.vr_tab[k] = dm + 2 * nz + 4 * (nr + 1) + (2 + k) * N1;
+        }
+        // inner: damping_diskmodel_center_of_mass_inner (center_of_mass.cpp:552-720)
+        const bool din = p.damping && c.active[0] && p.damping_inner_limit > 1.0 &&
+                         T(RMED)[0] < rin;
+        c.vr_lo[0] = 2;  // One_no_ghost_vr
+        c.vr_hi[0] = din ? clamp_id(cell_id(eng, Rmed, rin, true), true, nr) + 1 : 0;
+        c.az_lo[0] = 1;  // Zero_no_ghost
+        c.az_hi[0] = din ? clamp_id(cell_id(eng, Rmed, rin, false), false, nr) + 1 : 0;
+        c.tau[0] = p.damping_time_factor * 2.0 * M_PI / omega_kepler(p, p.rmin);
+        // outer: damping_diskmodel_center_of_mass_outer (:339-549)
+        const bool dout = p.damping && c.active[1] && p.damping_outer_limit < 1.0 &&
+                          T(RINF)[nr] > rout;
+        c.vr_lo[1] = clamp_id(cell_id(eng, Rmed, rout, true), true, nr) + 1;
+        c.vr_hi[1] = dout ? nr - 1 : 0;  // MaxMo_no_ghost_vr
+        c.az_lo[1] = clamp_id(cell_id(eng, Rmed, rout, false), false, nr) + 1;
+        c.az_hi[1] = dout ? nr - 1 : 0;  // Max_no_ghost
+        c.tau[1] = p.damping_time_factor * 2.0 * M_PI / omega_kepler(p, p.damping_time_radius_outer);
     }
 
     // physics constants
@@ -666,6 +939,7 @@ extern "C" int fgpu_destroy(fgpu_engine *eng)
     for (int k = 0; k < 4; ++k) cudaFree(eng->mom[k]);
     cudaFree(eng->ring_ws); cudaFree(eng->tables_mem); cudaFree(eng->damp_mem);
     cudaFree(eng->damp_rings); cudaFree(eng->partial); cudaFree(eng->red_out);
+    cudaFree(eng->com_mem);
     cudaFree(eng->d_dtmin); cudaFree(eng->d_bad);
     cudaFree(eng->corr_phi); cudaFree(eng->corr_r);
     if (eng->h_pinned) cudaFreeHost(eng->h_pinned);
@@ -968,17 +1242,111 @@ static void ghost(fgpu_engine *eng, const Launch &L)
     launch_ghost(L, eng->bc, eng->bodies.omega_frame, state_of(eng));
 }
 
+// The centre-of-mass composite: its damping runs after the regular damping
+// in the final boundary call, its ghost rings after the per-field hooks
+// (boundary_conditions.cpp:46-110).
+static ComSpec com_spec(const fgpu_engine *eng, const ComCenter *c)
+{
+    ComSpec cs = eng->com;
+    cs.c[0] = c[0];
+    cs.c[1] = c[1];
+    cs.omf = eng->bodies.omega_frame;
+    return cs;
+}
+
+static void com_boundary(fgpu_engine *eng, const Launch &L, const ComCenter *c)
+{
+    if (eng->com_any) launch_com_boundary(L, com_spec(eng, c), state_of(eng));
+}
+
+static void com_damping(fgpu_engine *eng, const Launch &L, double dt, const ComCenter *c)
+{
+    if (eng->com_any && eng->p.damping) launch_com_damping(L, com_spec(eng, c), dt, state_of(eng));
+}
+
+static int com_unready(fgpu_engine *eng)
+{
+    if (eng->com_any && !eng->com_ready) {
+        eng->err = "a centerofmass composite boundary needs fgpu_init_center_of_mass_boundary first";
+        return FGPU_ERR_BAD_ARG;
+    }
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_init_center_of_mass_boundary(fgpu_engine *eng, double mass_all,
+                                                 double mass_center, int binary_on_primary,
+                                                 double com_max_dist)
+{
+    if (!eng) return FGPU_ERR_BAD_ARG;
+    if (!eng->com_any) {
+        eng->err = "no composite boundary is centerofmass";
+        return FGPU_ERR_BAD_ARG;
+    }
+    if (!(mass_all > 0.0) || !(mass_center > 0.0) || !(com_max_dist >= 0.0)) {
+        eng->err = "masses must be > 0 and com_max_dist >= 0";
+        return FGPU_ERR_BAD_ARG;
+    }
+    const int nr = eng->nr, n = kComTableNodes;
+    const double *radii = eng->host_radii.data();
+    std::vector<double> Rmed(nr + 2, 0.0);
+    for (int k = 0; k <= nr; ++k) {
+        double rm = 2.0 / 3.0 * (std::pow(radii[k + 1], 3) - std::pow(radii[k], 3));
+        Rmed[k] = rm / (std::pow(radii[k + 1], 2) - std::pow(radii[k], 2));
+    }
+    std::vector<double> tabs(4 * (size_t)(n + 1));
+    double *rt = tabs.data(), *vt = rt + 2 * (n + 1);
+    ComSpec &c = eng->com;
+    fgpu32::viscous_speed_tables(eng->p, radii, Rmed.data(), nr, mass_all, mass_center,
+                                 binary_on_primary != 0, com_max_dist, n, c.min_r, c.dlog, rt,
+                                 vt);
+    for (int k = 0; k < 2; ++k) {
+        if (!std::isfinite(c.min_r[k]) || !std::isfinite(c.dlog[k]) || !(c.dlog[k] > 0.0)) {
+            eng->err = "viscous-speed table range is empty";
+            return FGPU_ERR_BAD_ARG;
+        }
+    }
+    // the four tables lie back to back in com_mem: r_tab[0], r_tab[1], vr_tab[0], vr_tab[1]
+    CK(cudaMemcpyAsync(const_cast<double *>(c.r_tab[0]), tabs.data(), sizeof(double) * tabs.size(),
+                       cudaMemcpyHostToDevice, eng->stream));
+    CK(cudaStreamSynchronize(eng->stream));
+    eng->com_ready = true;
+    if (eng->e32) {
+        eng->e32->com = eng->com;
+        eng->e32->com_any = true;
+    }
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_set_frame_centers(fgpu_engine *eng, const fgpu_frame_center now[2],
+                                      const fgpu_frame_center *after)
+{
+    if (!eng || !now) return FGPU_ERR_BAD_ARG;
+    const fgpu_frame_center *a = after ? after : now;
+    for (int k = 0; k < 2; ++k) {
+        eng->com_now[k] = ComCenter{now[k].x, now[k].y, now[k].vx, now[k].vy, now[k].mass};
+        eng->com_after[k] = ComCenter{a[k].x, a[k].y, a[k].vx, a[k].vy, a[k].mass};
+        if (eng->e32) {
+            eng->e32->com_now[k] = eng->com_now[k];
+            eng->e32->com_after[k] = eng->com_after[k];
+        }
+    }
+    return FGPU_OK;
+}
+
 extern "C" int fgpu_apply_boundary_condition(fgpu_engine *eng, double t, double dt, int final)
 {
     (void)t;
     if (!eng) return FGPU_ERR_BAD_ARG;
+    if (int rc = com_unready(eng)) return rc;
     ROUTE32(eng->e32->boundary(dt, final != 0));
     Launch L = launch_of(eng);
     if (final) viscous_recompute(eng, L);
     if (final && eng->p.damping) {
         launch_damping(L, eng->dm, dt, eng->damp_rings, eng->n_damp_rings, state_of(eng));
+        com_damping(eng, L, dt, eng->com_now);
     }
     ghost(eng, L);
+    com_boundary(eng, L, eng->com_now);
     eng->cfl_valid = false;
     return check_launch(eng);
 }
@@ -1043,12 +1411,14 @@ static void transport(fgpu_engine *eng, double dt)
 extern "C" int fgpu_step_euler(fgpu_engine *eng, double dt, double t)
 {
     if (!eng || !(dt > 0.0)) return FGPU_ERR_BAD_ARG;
+    if (int rc = com_unready(eng)) return rc;
     ROUTE32(eng->e32->step(dt, t));
     Launch L = launch_of(eng);
     mark(eng, -1);
     gas_kick(eng, dt, t);
     // apply_boundary_condition(final = false) (simulation.cpp:213)
     ghost(eng, L);
+    com_boundary(eng, L, eng->com_now);
     mark(eng, 6);
     transport(eng, dt);
     viscous_recompute(eng, L);
@@ -1056,9 +1426,11 @@ extern "C" int fgpu_step_euler(fgpu_engine *eng, double dt, double t)
     // apply_boundary_condition(final = true) (simulation.cpp:244)
     if (eng->p.damping) {
         launch_damping(L, eng->dm, dt, eng->damp_rings, eng->n_damp_rings, s);
+        com_damping(eng, L, dt, eng->com_after);
     }
     mark(eng, 10);
     ghost(eng, L);
+    com_boundary(eng, L, eng->com_after);
     mark(eng, 11);
     // recalculate_derived_disk_quantities (simulation.cpp:265) + the next CFL
     CK(cudaMemsetAsync(eng->d_dtmin, 0x7f, sizeof(unsigned long long), eng->stream));

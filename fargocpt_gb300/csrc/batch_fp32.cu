@@ -649,9 +649,13 @@ extern "C" int fgpu_batch_create(int n, const fgpu_params *params, const double 
         if (params[k].precision != FGPU_PRECISION_FP32_MIXED ||
             params[k].integrator != FGPU_INTEGRATOR_EULER)
             return FGPU_ERR_UNSUPPORTED;
-        // StabilizeViscosity and the recompute of c_s, H, nu before the final
-        // hooks are not part of the batched step
+        // StabilizeViscosity, the centre-of-mass composite boundary and the
+        // recompute of c_s, H, nu before the final hooks are not part of the
+        // batched step
         if (params[k].stabilize_viscosity) return FGPU_ERR_UNSUPPORTED;
+        if (params[k].composite_inner != FGPU_COMPOSITE_INDIVIDUAL ||
+            params[k].composite_outer != FGPU_COMPOSITE_INDIVIDUAL)
+            return FGPU_ERR_UNSUPPORTED;
         if (params[k].eos == FGPU_EOS_IDEAL &&
             (params[k].viscous_accretion || params[k].bc_vrad_inner == FGPU_BC_VISCOUS))
             return FGPU_ERR_UNSUPPORTED;
@@ -720,10 +724,8 @@ extern "C" int fgpu_batch_create(int n, const fgpu_params *params, const double 
         }                                                                \
     } while (0)
     for (int per : kPerChoices) {
-        CKC(cudaFuncSetAttribute((const void *)az_fn(per, 4),
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->az_smem));
-        CKC(cudaFuncSetAttribute((const void *)az_fn(per, 5),
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->az_smem));
+        CKC(raise_smem_limit((const void *)az_fn(per, 4), b->az_smem));
+        CKC(raise_smem_limit((const void *)az_fn(per, 5), b->az_smem));
     }
     CKC(cudaMalloc(&b->d_disks, sizeof(DiskF) * n));
     CKC(cudaMemcpy(b->d_disks, desc.data(), sizeof(DiskF) * n, cudaMemcpyHostToDevice));

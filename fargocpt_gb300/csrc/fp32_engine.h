@@ -4,12 +4,16 @@
 #pragma once
 
 #include "../../include/fargocpt_gb300.h"
+#include "com_boundary.cuh"
 
 #include <cuda_runtime.h>
 #include <stddef.h>
 
 #include <string>
 #include <vector>
+
+// raises a kernel's dynamic shared-memory limit, never lowers it (api.cu)
+cudaError_t raise_smem_limit(const void *fn, size_t bytes);
 
 namespace fgpu32 {
 
@@ -171,6 +175,14 @@ class Engine32 {
     bool canonical() const { return fld[FGPU_V_RADIAL] == vr_a && fld[FGPU_V_AZIMUTHAL] == dv_a; }
     int disk_force(double px, double py, double pa, double rsm, double out[5]);
     int accrete(const AccrF &a, double out[3]);
+
+    // centre-of-mass composite boundary: the constants and tables (owned by
+    // the ABI handle) and the centres of the two boundary calls of a step
+    bool com_any = false;
+    ComSpec com{};
+    ComCenter com_now[2]{}, com_after[2]{};
+    void com_boundary(const ComCenter *c);
+    void com_damping(double dt, const ComCenter *c);
     int check_finite(int *field, int *nr_out, int *naz_out);
     // the device description used by the batched kernels
     DiskF describe();

@@ -8,6 +8,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "com_boundary.cuh"
+
 namespace fgpu {
 
 constexpr int kMaxBodies = 16;

@@ -5,6 +5,9 @@
 
 #include <stddef.h>
 
+// raises a kernel's dynamic shared-memory limit, never lowers it (api.cu)
+cudaError_t raise_smem_limit(const void *fn, size_t bytes);
+
 namespace fgpu {
 
 struct Launch {
@@ -29,6 +32,8 @@ void launch_stress(const Launch &L, const double *S, const double *vr, const dou
 void launch_viscous(const Launch &L, double dt, double beta_inv, int mode, const State &s);
 void launch_visc_corr(const Launch &L, const State &s);
 void launch_ghost(const Launch &L, const BcSpec &bc, double omf, const State &s);
+void launch_com_boundary(const Launch &L, const ComSpec &c, const State &s);
+void launch_com_damping(const Launch &L, const ComSpec &c, double dt, const State &s);
 void launch_transport_radial(const Launch &L, double dt, double omf, int chunk, const double *S,
                              const double *vr, const double *vaz, const double *E,
                              double *const mom[4], double *E_out, double *S_out);

@@ -292,6 +292,16 @@ __global__ void f_join_f64(const float *__restrict__ hi, const float *__restrict
 
 static bool is_vec(int f) { return f == FGPU_V_RADIAL || f == FGPU_V_RADIAL0 || f == FGPU_TAU_R_PHI; }
 
+// the launch just made failed: name it
+#define CKL(what)                                                           \
+    do {                                                                    \
+        cudaError_t e_ = cudaGetLastError();                                \
+        if (e_ != cudaSuccess) {                                            \
+            err = std::string("launch of ") + (what) + ": " + cudaGetErrorString(e_); \
+            return FGPU_ERR_CUDA;                                           \
+        }                                                                   \
+    } while (0)
+
 #define CKF(call)                                                           \
     do {                                                                    \
         cudaError_t e_ = (call);                                            \
@@ -634,8 +644,7 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
         (const void *)f_transport_azimuthal<12, 5, true>,
         (const void *)f_transport_azimuthal<16, 5, true>};
     for (const void *fn : az_kernels) {
-        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)az_smem) !=
-            cudaSuccess) {
+        if (raise_smem_limit(fn, az_smem) != cudaSuccess) {
             err = "cannot reserve shared memory for the FP32 azimuthal kernel";
             return FGPU_ERR_CUDA;
         }
@@ -829,6 +838,28 @@ int Engine32::cfl(double *dt_out)
     return FGPU_OK;
 }
 
+void Engine32::com_boundary(const ComCenter *c)
+{
+    if (!com_any) return;
+    ComSpec cs = com;
+    cs.c[0] = c[0];
+    cs.c[1] = c[1];
+    StateF s = state();
+    const ComFields32 f{s.sigma, s.sigma_lo, s.vr, s.dv, s.energy, tabs.Vref_d};
+    k_com_boundary<<<dim3((nz + 127) / 128, 2), 128, 0, stream>>>(cs, nz, nr, f);
+}
+
+void Engine32::com_damping(double dt, const ComCenter *c)
+{
+    if (!com_any || !p.damping) return;
+    ComSpec cs = com;
+    cs.c[0] = c[0];
+    cs.c[1] = c[1];
+    StateF s = state();
+    const ComFields32 f{s.sigma, s.sigma_lo, s.vr, s.dv, s.energy, tabs.Vref_d};
+    launch_com_damping_sides(cs, nz, dt, f, stream);
+}
+
 int Engine32::boundary(double dt, bool final)
 {
     if (final && visc_recompute) {
@@ -839,7 +870,9 @@ int Engine32::boundary(double dt, bool final)
     }
     if (final && p.damping && n_rings)
         f_damping<<<n_rings, 256, 0, stream>>>(geo, dm, (float)dt, damp_rings, state());
+    if (final) com_damping(dt, com_now);
     f_ghost<<<(nz + 127) / 128, 128, 0, stream>>>(geo, bc, state());
+    com_boundary(com_now);
     CKF(cudaGetLastError());
     cfl_valid = false;
     return FGPU_OK;
@@ -857,11 +890,13 @@ int Engine32::kick(double dt, double t)
     };
     f_potential<<<grid2(nz, nr), 128, 0, stream>>>(geo, tabs, phys, bodies, fld[FGPU_SCALE_HEIGHT],
                                                    fld[FGPU_POTENTIAL]);
+    CKL("potential");
     mark(0);
     f_source<<<grid2(nz, nr + 1), 128, 0, stream>>>(geo, tabs, fdt, fld[FGPU_SIGMA],
                                                     fld[FGPU_PRESSURE], fld[FGPU_POTENTIAL],
                                                     fld[FGPU_V_RADIAL], fld[FGPU_V_AZIMUTHAL],
                                                     alt_vr, alt_dv);
+    CKL("source");
     std::swap(fld[FGPU_V_RADIAL], alt_vr);
     std::swap(fld[FGPU_V_AZIMUTHAL], alt_dv);
     mark(1);
@@ -869,10 +904,12 @@ int Engine32::kick(double dt, double t)
     if (adi || phys.art_visc_sn || phys.art_visc_tw) {
         f_artvisc_q<<<grid2(nz, nr), 128, 0, stream>>>(geo, tabs, phys, fdt, s.sigma, s.vr, s.dv,
                                                        s.energy, fld[FGPU_Q_R], fld[FGPU_Q_PHI]);
+        CKL("artvisc_q");
         mark(2);
         f_artvisc_v<<<grid2(nz, nr), 128, 0, stream>>>(
             geo, tabs, phys, fdt, s.sigma, s.energy, fld[FGPU_Q_R], fld[FGPU_Q_PHI], s.vr, s.dv,
             fld[FGPU_SOUNDSPEED], fld[FGPU_SCALE_HEIGHT], fld[FGPU_VISCOSITY]);
+        CKL("artvisc_v");
         mark(3);
     } else {
         mark(2);
@@ -882,6 +919,7 @@ int Engine32::kick(double dt, double t)
                                                 fld[FGPU_VISCOSITY], fld[FGPU_DIV_V],
                                                 fld[FGPU_TAU_R_R], fld[FGPU_TAU_PHI_PHI],
                                                 fld[FGPU_TAU_R_PHI]);
+    CKL("stress");
     if (phys.stabilize) visc_corr(s);
     mark(4);
     f_viscous<<<grid2(nz, nr), 128, 0, stream>>>(
@@ -889,8 +927,8 @@ int Engine32::kick(double dt, double t)
         fld[FGPU_TAU_PHI_PHI], fld[FGPU_TAU_R_PHI], fld[FGPU_DIV_V], fld[FGPU_VISCOSITY],
         fld[FGPU_SCALE_HEIGHT], s.sigma0, s.energy0, s.vr, s.dv, s.energy, fld[FGPU_QPLUS],
         fld[FGPU_QMINUS], corr_phi, corr_r);
+    CKL("viscous");
     mark(5);
-    CKF(cudaGetLastError());
     cfl_valid = false;
     return FGPU_OK;
 }
@@ -919,6 +957,7 @@ int Engine32::transport(double dt)
                                                            mom[1], mom[2], mom[3], alt_e, alt_sigma,
                                                            sigma_lo, alt_sigma_lo);
     }
+    CKL("transport_radial");
     mark(7);
     {
 #define AZ32(P, NQ, ST)                                                                          \
@@ -945,15 +984,16 @@ int Engine32::transport(double dt)
 #undef AZ32_NQ
 #undef AZ32
     }
+    CKL("transport_azimuthal");
     mark(8);
     f_finish<<<grid2(nz, nr + 1), 128, 0, stream>>>(geo, tabs, phys, mom[0], mom[1], mom[2],
                                                     mom[3], alt_sigma, alt_e, s.vr, alt_vr,
                                                     alt_dv, s.sigma, s.energy, alt_sigma_lo,
                                                     sigma_lo);
+    CKL("finish");
     std::swap(fld[FGPU_V_RADIAL], alt_vr);
     std::swap(fld[FGPU_V_AZIMUTHAL], alt_dv);
     mark(9);
-    CKF(cudaGetLastError());
     cfl_valid = false;
     return FGPU_OK;
 }
@@ -975,6 +1015,9 @@ int Engine32::step(double dt, double t)
     int rc = kick(dt, t);
     if (rc) return rc;
     f_ghost<<<(nz + 127) / 128, 128, 0, stream>>>(geo, bc, state());
+    CKL("ghost");
+    com_boundary(com_now);
+    CKL("com_boundary");
     mark(6);
     rc = transport(dt);
     if (rc) return rc;
@@ -985,8 +1028,14 @@ int Engine32::step(double dt, double t)
     StateF s = state();
     if (p.damping && n_rings)
         f_damping<<<n_rings, 256, 0, stream>>>(geo, dm, (float)dt, damp_rings, s);
+    CKL("damping");
+    com_damping(dt, com_after);
+    CKL("com_damping");
     mark(10);
     f_ghost<<<(nz + 127) / 128, 128, 0, stream>>>(geo, bc, s);
+    CKL("ghost");
+    com_boundary(com_after);
+    CKL("com_boundary");
     mark(11);
     rc = derived_cfl(1 | 4);
     if (rc) return rc;

@@ -1567,6 +1567,19 @@ void launch_visc_corr(const Launch &L, const State &s)
                                                                           s.corr_phi, s.corr_r);
 }
 
+// The centre-of-mass composite (com_boundary.cuh) on the FP64 fields.
+void launch_com_boundary(const Launch &L, const ComSpec &c, const State &s)
+{
+    const ComFields64 f{s.sigma, s.vr, s.vaz, s.energy};
+    k_com_boundary<<<dim3((L.g.nz + 127) / 128, 2), 128, 0, L.stream>>>(c, L.g.nz, L.g.nr, f);
+}
+
+void launch_com_damping(const Launch &L, const ComSpec &c, double dt, const State &s)
+{
+    const ComFields64 f{s.sigma, s.vr, s.vaz, s.energy};
+    launch_com_damping_sides(c, L.g.nz, dt, f, L.stream);
+}
+
 void launch_ghost(const Launch &L, const BcSpec &bc, double omf, const State &s)
 {
     k_ghost<<<(L.g.nz + 127) / 128, 128, 0, L.stream>>>(L.g, L.t, bc, omf, s);
@@ -1598,14 +1611,9 @@ int azimuthal_cells_per_thread(int nz) { return nz <= 2048 ? 4 : (nz <= 4096 ? 8
 
 cudaError_t prepare_azimuthal(size_t smem)
 {
-    cudaError_t e = cudaFuncSetAttribute(k_transport_azimuthal<4>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_transport_azimuthal<8>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_transport_azimuthal<16>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = raise_smem_limit((const void *)k_transport_azimuthal<4>, smem);
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_transport_azimuthal<8>, smem);
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_transport_azimuthal<16>, smem);
     return e;
 }
 

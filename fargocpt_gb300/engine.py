@@ -11,7 +11,7 @@ import ctypes as C
 
 import numpy as np
 
-from .abi import (FIELDS, STATUS_NAMES, VECTOR_FIELDS, FgpuBody, FgpuParams,
+from .abi import (FIELDS, STATUS_NAMES, VECTOR_FIELDS, FgpuBody, FgpuFrameCenter, FgpuParams,
                   load_library)
 
 
@@ -162,6 +162,21 @@ class Engine:
         self._check(self.lib.fgpu_accrete_onto_planet(self.h, C.byref(accretor), dt, out),
                     "fgpu_accrete_onto_planet")
         return out[0], out[1], out[2]
+
+    def init_center_of_mass_boundary(self, mass_all, mass_center, binary_on_primary,
+                                     com_max_dist):
+        """init_center_of_mass (center_of_mass.cpp:25-27): the viscous-speed
+        tables of a centerofmass composite boundary."""
+        self._check(self.lib.fgpu_init_center_of_mass_boundary(
+            self.h, mass_all, mass_center, int(binary_on_primary), com_max_dist),
+            "fgpu_init_center_of_mass_boundary")
+
+    def set_frame_centers(self, now, after=None):
+        """now / after: two (x, y, vx, vy, mass) centres, of the first
+        n_bodies_for_hydroframe_center bodies and of all bodies."""
+        n = (FgpuFrameCenter * 2)(*[FgpuFrameCenter(*c) for c in now])
+        a = (FgpuFrameCenter * 2)(*[FgpuFrameCenter(*c) for c in after]) if after else None
+        self._check(self.lib.fgpu_set_frame_centers(self.h, n, a), "fgpu_set_frame_centers")
 
     def check_finite(self):
         f, i, j = C.c_int(), C.c_int(), C.c_int()

@@ -74,7 +74,7 @@ def step_leapfrog(hydro, dt: float, t: float, first, second) -> None:
 def advance(hydro, clock: RunClock, *, cfl_max_var: float,
             monitor_timestep: float, t_final: float, max_steps: int = -1,
             bodies=None, on_monitor=None, integrator: str = "euler",
-            bodies_second=None, accrete=None) -> None:
+            bodies_second=None, accrete=None, frame_centers=None) -> None:
     """The loop of sim::run (simulation.cpp:505-558) with step_Euler or, for
     integrator "leapfrog", step_LeapFrog's gas part.
 
@@ -84,6 +84,8 @@ def advance(hydro, clock: RunClock, *, cfl_max_var: float,
     LeapFrog, gives the second kick's (defaults to the first's);
     accrete(clock, dt), for Euler, runs AccreteOntoPlanets where step_Euler
     does, first in the step (simulation.cpp:150-153);
+    frame_centers(clock, dt) -> (now, after), for Euler, gives the centres a
+    centre-of-mass boundary reads before transport and after the N-body step;
     on_monitor(clock) after every step that lands on a monitor time.
     """
     while clock.time < t_final:
@@ -105,6 +107,8 @@ def advance(hydro, clock: RunClock, *, cfl_max_var: float,
             if bodies is not None:
                 b, ix, iy = bodies(clock)
                 hydro.set_bodies(b, ix, iy, 0.0)
+            if frame_centers is not None:
+                hydro.set_frame_centers(*frame_centers(clock, step_dt))
             hydro.step_euler(step_dt, clock.time)
         clock.dts.append(step_dt)
         clock.time += step_dt
@@ -133,22 +137,65 @@ def l1_point(central_mass: float, other_mass: float) -> float:
     return x
 
 
-def orbital_period(x, y, vx, vy, com_mass, mass, G) -> float:
-    """The period of t_planet::calculate_orbital_elements (planet.cpp:488-566)
-    for relative position and velocity (x, y, vx, vy) about com_mass; 0 where
-    the reference sets the elements to zero."""
+def orbital_elements(x, y, vx, vy, com_mass, mass, G) -> tuple[float, float, float]:
+    """Semi-major axis, eccentricity and period of
+    t_planet::calculate_orbital_elements (planet.cpp:488-566) for relative
+    position and velocity (x, y, vx, vy) about com_mass; zeros where the
+    reference sets the elements to zero."""
     m = com_mass + mass
     h = x * vy - y * vx
     d = math.sqrt(x * x + y * y)
     if d == 0.0 or h == 0.0:
-        return 0.0
+        return 0.0, 0.0, 0.0
     Ax = x * vy * vy - y * vx * vy - G * m * x / d
     Ay = y * vx * vx - x * vx * vy - G * m * y / d
     e = math.sqrt(Ax * Ax + Ay * Ay) / G / m
     a = h * h / G / m / (1.0 - e * e)
     if e > 1.0 or e < 0 or a < 0.0:
-        return 0.0
-    return 2.0 * math.pi * math.sqrt(math.pow(a, 3) / (m * G))
+        return 0.0, 0.0, 0.0
+    return a, e, 2.0 * math.pi * math.sqrt(math.pow(a, 3) / (m * G))
+
+
+def orbital_period(x, y, vx, vy, com_mass, mass, G) -> float:
+    """The period of calculate_orbital_elements (0 where it zeroes them)."""
+    return orbital_elements(x, y, vx, vy, com_mass, mass, G)[2]
+
+
+def center_of_mass(bodies, n) -> tuple[float, float, float, float, float]:
+    """get_center_of_mass(n), get_center_of_mass_velocity(n) and get_mass(n)
+    (nbody/planetary_system.cpp:580-650) of the first n bodies, each an
+    (x, y, vx, vy, mass) tuple: the centre a centre-of-mass boundary reads."""
+    x = y = vx = vy = mass = 0.0
+    for b in bodies[:n]:
+        mass += b[4]
+        x += b[0] * b[4]
+        y += b[1] * b[4]
+        vx += b[2] * b[4]
+        vy += b[3] * b[4]
+    if mass > 0:
+        return (x / mass, y / mass, vx / mass, vy / mass, mass)
+    return (0.0, 0.0, 0.0, 0.0, mass)
+
+
+def com_boundary_setup(bodies, G, n_center=1) -> tuple[float, float, int, float]:
+    """The arguments of fgpu_init_center_of_mass_boundary for bodies given
+    as (x, y, vx, vy, mass) tuples, as init_vr_table_boundary reads them
+    (viscous_radial_speed.cpp:269-347): the mass of all bodies, of the
+    hydro-frame centre, whether a two-body system is centred on its first
+    body, and then a (1 + e) q of the second."""
+    n = len(bodies)
+    mass_all = center_of_mass(bodies, n)[4]
+    mass_center = center_of_mass(bodies, n_center)[4]
+    binary = n == 2 and n_center == 1
+    dist = 0.0
+    if binary:
+        c = center_of_mass(bodies, 1)
+        b = bodies[1]
+        a, e, _ = orbital_elements(b[0] - c[0], b[1] - c[1], b[2] - c[2], b[3] - c[3],
+                                   c[4], b[4], G)
+        q = b[4] / (b[4] + bodies[0][4])
+        dist = a * (1.0 + e) * q
+    return mass_all, mass_center, int(binary), dist
 
 
 def indirect_term_euler(bodies) -> tuple[float, float]:

@@ -103,6 +103,12 @@ enum { FGPU_BETA_REF_ZERO = 0, FGPU_BETA_REF_REFERENCE = 1,
        FGPU_BETA_REF_DISKMODEL = 2, FGPU_BETA_REF_FLOOR = 3 };
 enum { FGPU_PRECISION_FP64 = 0, FGPU_PRECISION_FP32_MIXED = 1 };
 enum { FGPU_INTEGRATOR_EULER = 0, FGPU_INTEGRATOR_LEAPFROG = 1 };
+/* composite boundaries (boundary_conditions/config.cpp:344-430): "individual"
+ * composites run the per-field hooks; "centerofmass" imposes the initial disk
+ * model about the centre of mass of the bodies on that edge's ghost ring and,
+ * with damping on, damps towards it (center_of_mass.cpp); the per-field hooks
+ * of that edge should then be FGPU_BC_NONE and its damping kinds none. */
+enum { FGPU_COMPOSITE_INDIVIDUAL = 0, FGPU_COMPOSITE_CENTER_OF_MASS = 1 };
 
 /*
  * Flat parameter block: the subset of FargoCPT's parameters:: namespace and
@@ -141,7 +147,13 @@ typedef struct fgpu_params {
                                viscous v_radial hook, c_s, H and nu are recomputed
                                before the final boundary call (simulation.cpp:232-242,
                                432-441; Interpret.cpp:704-707) */
-    int reserved_i[3];
+    int composite_inner;    /* FGPU_COMPOSITE_* (InnerBoundary, config.cpp:344-380) */
+    int composite_outer;    /* FGPU_COMPOSITE_* (OuterBoundary, config.cpp:384-430) */
+    int initialize_pure_keplerian; /* InitializePureKeplerian (parameters.cpp:568):
+                                      the centre-of-mass model disk is Keplerian */
+    int initialize_vradial_zero;   /* InitializeVradialZero (parameters.cpp:570) */
+    int profile_cutoff_inner;      /* ProfileCutoffInner (parameters.cpp:738) */
+    int reserved_i[1];
 
     double gamma;           /* AdiabaticIndex */
     double mu;              /* mean molecular weight */
@@ -186,7 +198,13 @@ typedef struct fgpu_params {
     double vrad_outer_keplerian_factor; /* OuterBoundaryVradKeplerianFactor (default 0.1) */
     double binary_quadrupole_moment;    /* Theo.cpp:74 when
                                            VazimuthalConsidersQuadropoleMoment is set,
-                                           else 0 (balanced boundary) */
+                                           else 0 (balanced and centre-of-mass
+                                           boundaries) */
+    double profile_cutoff_point_outer, profile_cutoff_width_outer; /* parameters.cpp:732-735 */
+    double profile_cutoff_point_inner, profile_cutoff_width_inner; /* parameters.cpp:740-743 */
+    double temperature_cgs_to_code; /* units::temperature.get_cgs_to_code_factor(): the
+                                       centre-of-mass boundary scales its temperature
+                                       floor by it once more (center_of_mass.cpp:196-200) */
     double reserved_d[2];
 } fgpu_params;
 
@@ -291,6 +309,34 @@ typedef struct fgpu_accretor {
  * removal acts on the compensated sigma pair and the sums are formed in FP64. */
 int fgpu_accrete_onto_planet(fgpu_engine *eng, const fgpu_accretor *a, double dt,
 			     double out[3]);
+
+/* The centre of a set of bodies as the centre-of-mass boundary reads it from
+ * the planetary system (nbody/planetary_system.cpp:580-650). */
+typedef struct fgpu_frame_center {
+    double x, y;            /* get_center_of_mass(n) */
+    double vx, vy;          /* get_center_of_mass_velocity(n) */
+    double mass;            /* get_mass(n) */
+} fgpu_frame_center;
+
+/* init_center_of_mass (center_of_mass.cpp:25-27): builds the viscous-speed
+ * lookup tables of viscous_speed::init_vr_table_boundary
+ * (viscosity/viscous_radial_speed.cpp:269-347) for both edges.  mass_all is
+ * get_mass() of all bodies, mass_center get_mass(n_bodies_for_hydroframe_center);
+ * binary_on_primary is 1 when the system has two bodies and the hydro frame is
+ * centred on the first, and com_max_dist is then a (1 + e) q of the second
+ * (q = m2 / (m1 + m2)).  Call it once after fgpu_create when a composite is
+ * FGPU_COMPOSITE_CENTER_OF_MASS. */
+int fgpu_init_center_of_mass_boundary(fgpu_engine *eng, double mass_all, double mass_center,
+				      int binary_on_primary, double com_max_dist);
+
+/* The centres each boundary call uses: c[0] of the first
+ * n_bodies_for_hydroframe_center bodies (inner edge), c[1] of all bodies
+ * (outer edge).  now[] serves fgpu_apply_boundary_condition and the boundary
+ * call before transport in fgpu_step_euler; after[] (NULL: now[]) serves the
+ * final call of fgpu_step_euler, which FargoCPT makes after the N-body step
+ * (simulation.cpp:219-244). */
+int fgpu_set_frame_centers(fgpu_engine *eng, const fgpu_frame_center now[2],
+			   const fgpu_frame_center *after);
 
 /* Scans the evolved fields for NaN/Inf; returns FGPU_ERR_NONFINITE and the
  * first bad (field, ring, azimuth) when one is found. */

@@ -58,6 +58,13 @@ struct or_state {
     fgpu_body b[MAX_BODIES];
     double ix, iy, omega_frame;
 
+    /* centre-of-mass composite boundary: viscous-speed tables (inner 0,
+       outer 1; N + 1 nodes) and the centres of the two boundary calls */
+    int com_ready;
+    double com_min_r[2], com_dlog[2];
+    double *com_r[2], *com_vr[2];
+    fgpu_frame_center com_now[2], com_after[2];
+
     /* damping ring limits (damping.cpp:311-427), per quantity */
     int damp_limit_inner[4];
     int damp_limit_outer[4];
@@ -283,6 +290,10 @@ void or_destroy(or_state *s)
 		      s->FourThirdInvRbInvdphiSq};
     for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i) free(ptrs[i]);
     for (int f = 0; f < FGPU_FIELD_COUNT; ++f) free(s->f[f]);
+    for (int k = 0; k < 2; ++k) {
+	free(s->com_r[k]);
+	free(s->com_vr[k]);
+    }
     free(s->nshift);
     free(s->nosplit);
     free(s);
@@ -1140,10 +1151,438 @@ static void ghost_hook(or_state *s, int field, int kind, int outer)
     }
 }
 
+/* ------------------------------------------------------------------ */
+/* centre-of-mass composite boundary: src/boundary_conditions/         */
+/* center_of_mass.cpp, the model of src/Theo.cpp:86-243 and the        */
+/* viscous-speed tables of src/viscosity/viscous_radial_speed.cpp      */
+/* ------------------------------------------------------------------ */
+
+#define OR_VR_TABLE_N 1000 /* viscous_radial_speed.cpp:256 */
+
+static double th_h(const or_state *s, double R)
+{
+    return s->p.aspect_ratio * pow(R, s->p.flaring_index);
+}
+
+/* support_azi_pressure / _smoothing_derivative / _quadrupole, Theo.cpp:131-157 */
+static double th_pressure(const or_state *s, double R)
+{
+    const double F = s->p.flaring_index, S = s->p.sigma_slope;
+    return (2.0 * F - 1.0 - S) * pow(th_h(s, R), 2);
+}
+
+static double th_smoothing(const or_state *s, double R)
+{
+    const double F = s->p.flaring_index, eps = s->p.thickness_smoothing;
+    const double h = th_h(s, R);
+    return (1.0 + (F + 1.0) * pow(h * eps, 2)) / pow(sqrt(1 + pow(h * eps, 2)), 3);
+}
+
+static double th_quadrupole(const or_state *s, double R)
+{
+    const double Q = s->p.binary_quadrupole_moment;
+    return Q > 0.0 ? 3.0 * Q / pow(R, 2) : 0.0;
+}
+
+/* initial_locally_isothermal_smoothed_v_az (Theo.cpp:166-181) and the
+   variant with the quadrupole moment (:183-200); the quadrupole moment is
+   zero unless VazimuthalConsidersQuadropoleMoment is set */
+static double th_vaz(const or_state *s, double R, double M, int quad)
+{
+    double support;
+    if (quad) {
+	support = th_quadrupole(s, R) + th_smoothing(s, R) + th_pressure(s, R);
+    } else {
+	const double sm = th_smoothing(s, R);
+	support = sm + th_pressure(s, R);
+    }
+    const double vk_2 = s->p.G * M / R;
+    return sqrt(vk_2 * support);
+}
+
+/* initial_viscous_radial_speed, Theo.cpp:220-243 */
+static double th_vr_steady(const or_state *s, double R, double M)
+{
+    const fgpu_params *p = &s->p;
+    if (p->viscous_alpha > 0) {
+	const double sqrt_gamma = adiabatic(s) ? sqrt(p->gamma) : 1.0;
+	const double v_k = sqrt(p->G * M / R);
+	const double h = p->aspect_ratio * pow(R, p->flaring_index);
+	const double cs = sqrt_gamma * h * v_k;
+	const double H = h * R;
+	const double nu = p->viscous_alpha * cs * H;
+	return -3.0 * nu / R * (-p->sigma_slope + 2.0 * p->flaring_index + 1.0);
+    }
+    return -3.0 * p->constant_viscosity / R * (-p->sigma_slope + .5);
+}
+
+/* initial_energy, Theo.cpp:86-99 */
+static double th_energy(const or_state *s, double R, double M)
+{
+    const fgpu_params *p = &s->p;
+    return 1.0 / (p->gamma - 1.0) * p->sigma0 * pow(p->aspect_ratio, 2) *
+	   pow(R, -p->sigma_slope - 1.0 + 2.0 * p->flaring_index) * p->G * M;
+}
+
+/* cutoff_outer / cutoff_inner, util.cpp:69-93 */
+static double cutoff_out(const or_state *s, double x)
+{
+    return 1.0 / (1.0 + exp((x - s->p.profile_cutoff_point_outer) /
+			    s->p.profile_cutoff_width_outer));
+}
+
+static double cutoff_in(const or_state *s, double x)
+{
+    return 1.0 / (1.0 + exp((s->p.profile_cutoff_point_inner - x) /
+			    s->p.profile_cutoff_width_inner));
+}
+
+/* get_sigma, viscous_radial_speed.cpp:92-115 */
+static double vs_sigma(const or_state *s, double R)
+{
+    const fgpu_params *p = &s->p;
+    double d = p->sigma0 * pow(R, -p->sigma_slope);
+    const double floor_ = p->sigma_floor * p->sigma0;
+    if (p->profile_cutoff_outer) d *= cutoff_out(s, R);
+    if (p->profile_cutoff_inner) d *= cutoff_in(s, R);
+    return d > floor_ ? d : floor_;
+}
+
+/* get_nu2, viscous_radial_speed.cpp:37-90 */
+static double vs_nu2(const or_state *s, double R, double M, double Sigma)
+{
+    const fgpu_params *p = &s->p;
+    const double v_k = sqrt(p->G * M / R);
+    const double h = p->aspect_ratio * pow(R, p->flaring_index);
+    double cutoff = 1.0;
+    if (p->profile_cutoff_outer) cutoff *= cutoff_out(s, R);
+    if (p->profile_cutoff_inner) cutoff *= cutoff_in(s, R);
+    double cs_adb, H;
+    if (adiabatic(s)) {
+	const double gamma = p->gamma;
+	double energy = cutoff * 1.0 / (gamma - 1.0) * Sigma * pow(h * v_k, 2);
+	const double efloor = p->minimum_temperature * Sigma / p->mu * p->R_gas / (gamma - 1.0);
+	const double eceil = p->maximum_temperature * Sigma / p->mu * p->R_gas / (gamma - 1.0);
+	energy = fmax(energy, efloor);
+	energy = fmin(energy, eceil);
+	cs_adb = sqrt(gamma * (gamma - 1.0) * energy / Sigma);
+	const double cs_iso = sqrt((gamma - 1.0) * energy / Sigma);
+	const double omega_k = v_k / R;
+	H = cs_iso / omega_k;
+    } else {
+	cs_adb = h * v_k;
+	H = h * R;
+    }
+    return p->viscous_alpha * cs_adb * H;
+}
+
+typedef double (*vs_fn)(const or_state *, double, double);
+
+/* derive, viscous_radial_speed.cpp:122-135 */
+static double vs_derive(const or_state *s, double x, double M, vs_fn f)
+{
+    const double h = 8.0e-4 * x;
+    const double f1 = -1.0 * f(s, x + 2.0 * h, M);
+    const double f2 = 8.0 * f(s, x + h, M);
+    const double f3 = -8.0 * f(s, x - h, M);
+    const double f4 = 1.0 * f(s, x - 2.0 * h, M);
+    return (f1 + f2 + f3 + f4) / (12.0 * h);
+}
+
+/* get_w with VazimuthalConsidersQuadropoleMoment folded into the moment */
+static double vs_w(const or_state *s, double r, double M)
+{
+    return th_vaz(s, r, M, 1) / r;
+}
+
+static double vs_r2_w(const or_state *s, double r, double M)
+{
+    return pow(r, 2) * vs_w(s, r, M);
+}
+
+static double vs_nu_S_r3_dwdr(const or_state *s, double r, double M)
+{
+    const double dw_dr = vs_derive(s, r, M, vs_w);
+    const double Sigma = vs_sigma(s, r);
+    const double nu = vs_nu2(s, r, M, Sigma);
+    return nu * Sigma * pow(r, 3) * dw_dr;
+}
+
+/* get_vr_with_numerical_viscous_speed, viscous_radial_speed.cpp:184-200 */
+static double vs_vr(const or_state *s, double r, double M)
+{
+    const double num = 1.0 / r * vs_derive(s, r, M, vs_nu_S_r3_dwdr);
+    const double den = vs_sigma(s, r) * vs_derive(s, r, M, vs_r2_w);
+    return num / den;
+}
+
+/* interface radius k (Radii[k]) and GlobalRmed[k] (init.cpp:176-179) */
+static double radii_at(const or_state *s, int k)
+{
+    return k <= s->nr ? s->Rinf[k] : s->Rsup[k - 1];
+}
+
+static double global_rmed(const or_state *s, int k)
+{
+    const double a = radii_at(s, k), b = radii_at(s, k + 1);
+    double r = 2.0 / 3.0 * (pow(b, 3) - pow(a, 3));
+    return r / (pow(b, 2) - pow(a, 2));
+}
+
+/* get_vr_outer_viscous_speed_correction_factor, viscous_radial_speed.cpp:207-254 */
+static double vs_outer_correction(const or_state *s, double r, double M)
+{
+    int k = clamp_id(cell_id_rmed(s, r), 1, s->nr);
+    if (k < 2) k = 2;
+    const double rinf = radii_at(s, k);
+    const double rmed_p = global_rmed(s, k + 1), rmed = global_rmed(s, k);
+    const double rmed_m = global_rmed(s, k - 1), rmed_m2 = global_rmed(s, k - 2);
+    const double w_p = vs_w(s, rmed_p, M), w = vs_w(s, rmed, M);
+    const double w_m = vs_w(s, rmed_m, M), w_m2 = vs_w(s, rmed_m2, M);
+    const double dw_dr = (0.5 * (w_p + w) - 0.5 * (w + w_m)) / (radii_at(s, k + 1) - radii_at(s, k));
+    const double dw_dr_m = (0.5 * (w + w_m) - 0.5 * (w_m + w_m2)) / (radii_at(s, k) - radii_at(s, k - 1));
+    const double Sigma = vs_sigma(s, rmed);
+    const double nu = vs_nu2(s, rmed, M, Sigma);
+    const double Sigma_m = vs_sigma(s, rmed_m);
+    const double nu_m = vs_nu2(s, rmed_m, M, Sigma_m);
+    const double a = nu * Sigma * pow(rmed, 3) * dw_dr;
+    const double a_m = nu_m * Sigma_m * pow(rmed_m, 3) * dw_dr_m;
+    const double dr = rmed - rmed_m;
+    const double num = 1.0 / rinf * (a - a_m) / dr;
+    const double r2w = pow(rmed, 2) * vs_w(s, rmed, M);
+    const double r2w_m = pow(rmed_m, 2) * vs_w(s, rmed_m, M);
+    const double dr2w_dr = (r2w - r2w_m) / (rmed - rmed_m);
+    const double den = Sigma_m * dr2w_dr;
+    const double vr = num / den;
+    return vr / vs_vr(s, rinf, M);
+}
+
+/* init_vr_table_boundary, viscous_radial_speed.cpp:269-347; the tables get
+   one node more than the reference's so that the last bin has a right node */
+int or_init_center_of_mass_boundary(or_state *s, double mass_all, double mass_center,
+				    int binary_on_primary, double com_max_dist)
+{
+    const fgpu_params *p = &s->p;
+    const int nr = s->nr, N = OR_VR_TABLE_N;
+    for (int k = 0; k < 2; ++k) {
+	free(s->com_r[k]);
+	free(s->com_vr[k]);
+	s->com_r[k] = calloc(N + 1, sizeof(double));
+	s->com_vr[k] = calloc(N + 1, sizeof(double));
+    }
+    {
+	const double safety = s->Rsup[nr - 1] - s->Rinf[nr - 1];
+	double lo, hi;
+	if (binary_on_primary) {
+	    lo = s->Rinf[nr - 1] * p->damping_outer_limit - com_max_dist - safety;
+	    hi = s->Rsup[nr - 1] + com_max_dist + safety;
+	} else {
+	    lo = s->Rinf[nr - 1] * p->damping_outer_limit - safety;
+	    hi = s->Rsup[nr - 1] + safety;
+	}
+	if (lo < p->rmin) lo = p->rmin;
+	s->com_min_r[1] = lo;
+	s->com_dlog[1] = log10(hi / lo) / (double)N;
+	for (int i = 0; i <= N; ++i) {
+	    const double r = lo * pow(10.0, (s->com_dlog[1] * (double)i));
+	    s->com_r[1][i] = r;
+	    s->com_vr[1][i] = vs_vr(s, r, mass_all) * vs_outer_correction(s, r, mass_all);
+	}
+    }
+    {
+	const int lim = clamp_id(cell_id_rmed(s, p->rmin * p->damping_inner_limit), 0, nr) + 1;
+	const double safety = s->Rsup[lim] - s->Rinf[lim];
+	double lo, hi;
+	if (binary_on_primary) {
+	    lo = s->Rinf[1] - com_max_dist - safety;
+	    if (lo < s->Rsup[0] - s->Rinf[0]) lo = s->Rsup[0] - s->Rinf[0];
+	    hi = s->Rsup[1] * p->damping_inner_limit + com_max_dist + safety;
+	} else {
+	    lo = s->Rinf[1] - safety;
+	    hi = s->Rsup[1] * p->damping_inner_limit + safety;
+	}
+	s->com_min_r[0] = lo;
+	s->com_dlog[0] = log10(hi / lo) / (double)N;
+	for (int i = 0; i <= N; ++i) {
+	    const double r = lo * pow(10.0, (s->com_dlog[0] * (double)i));
+	    s->com_r[0][i] = r;
+	    s->com_vr[0][i] = vs_vr(s, r, mass_center);
+	}
+    }
+    s->com_ready = 1;
+    return FGPU_OK;
+}
+
+int or_set_frame_centers(or_state *s, const fgpu_frame_center now[2],
+			 const fgpu_frame_center *after)
+{
+    for (int k = 0; k < 2; ++k) {
+	s->com_now[k] = now[k];
+	s->com_after[k] = after ? after[k] : now[k];
+    }
+    return FGPU_OK;
+}
+
+/* lookup_initial_vr_outer / _inner, viscous_radial_speed.cpp:350-407 */
+static double com_lookup(const or_state *s, int side, double r)
+{
+    const int N = OR_VR_TABLE_N;
+    const int i = (int)floor(log10(r / s->com_min_r[side]) / s->com_dlog[side]);
+    const double *rt = s->com_r[side], *vt = s->com_vr[side];
+    if (i > N - 1) return vt[N - 1];
+    if (i < 0) return vt[0];
+    const double x = (r - rt[i]) / (rt[i + 1] - rt[i]);
+    return (1.0 - x) * vt[i] + x * vt[i + 1];
+}
+
+/* the model velocity at (cx, cy) in the primary's frame; side 0 is the
+   inner edge (no quadrupole term), 1 the outer edge */
+static void com_velocity(const or_state *s, int side, int damping, const fgpu_frame_center *c,
+			 double cx, double cy, double *vx, double *vy)
+{
+    const double x_com = cx - c->x, y_com = cy - c->y;
+    const double r_com = sqrt(x_com * x_com + y_com * y_com);
+    double vazi0, vr0;
+    if (s->p.initialize_pure_keplerian) {
+	vazi0 = sqrt(s->p.G * c->mass / r_com); /* compute_v_kepler */
+	vr0 = (damping && s->p.initialize_vradial_zero) ? 0.0
+						       : th_vr_steady(s, r_com, c->mass);
+    } else {
+	vazi0 = th_vaz(s, r_com, c->mass, side == 1);
+	vr0 = com_lookup(s, side, r_com);
+    }
+    const double vx_com = (vr0 * x_com - vazi0 * y_com) / r_com;
+    const double vy_com = (vr0 * y_com + vazi0 * x_com) / r_com;
+    *vx = vx_com + c->vx;
+    *vy = vy_com + c->vy;
+}
+
+/* diskmodel_center_of_mass_boundary_inner / _outer, center_of_mass.cpp:38-336 */
+static void com_ghost(or_state *s, int side, const fgpu_frame_center *c)
+{
+    const fgpu_params *p = &s->p;
+    const int nz = s->nz;
+    const int i = side ? s->nr - 1 : 0;
+    double *sig = s->f[FGPU_SIGMA], *en = s->f[FGPU_ENERGY];
+    double *vr = s->f[FGPU_V_RADIAL], *vaz = s->f[FGPU_V_AZIMUTHAL];
+    for (int j = 0; j < nz; ++j) {
+	double vx, vy;
+	{
+	    const double phi = ((double)j - 0.5) * s->dphi;
+	    const double rmed = s->Rmed[i];
+	    const double cx = rmed * cos(phi), cy = rmed * sin(phi);
+	    com_velocity(s, side, 0, c, cx, cy, &vx, &vy);
+	    vaz[(size_t)i * nz + j] = (cx * vy - vx * cy) / rmed - s->omega_frame * rmed;
+	}
+	for (int k = 0; k < 2; ++k) {
+	    const double phi = (double)j * s->dphi;
+	    const double rr = k ? s->Rsup[i] : s->Rinf[i];
+	    const double cx = rr * cos(phi), cy = rr * sin(phi);
+	    com_velocity(s, side, 0, c, cx, cy, &vx, &vy);
+	    vr[(size_t)(i + k) * nz + j] = (cx * vx + cy * vy) / rr;
+	}
+	{
+	    const double cx = s->Rmed[i] * s->cosj[j], cy = s->Rmed[i] * s->sinj[j];
+	    const double x_com = cx - c->x, y_com = cy - c->y;
+	    const double r_com = sqrt(x_com * x_com + y_com * y_com);
+	    const double cell_sigma = p->sigma0 * pow(r_com, -p->sigma_slope);
+	    sig[(size_t)i * nz + j] = cell_sigma;
+	    const double cell_energy = th_energy(s, r_com, c->mass);
+	    const double tfloor = p->minimum_temperature * p->temperature_cgs_to_code;
+	    const double efloor = tfloor * cell_sigma / p->mu * p->R_gas / (p->gamma - 1.0);
+	    en[(size_t)i * nz + j] = fmax(cell_energy, efloor);
+	}
+    }
+}
+
+/* damping_diskmodel_center_of_mass_outer / _inner, center_of_mass.cpp:339-720 */
+static void com_damp(or_state *s, int side, const fgpu_frame_center *c, double dt)
+{
+    const fgpu_params *p = &s->p;
+    const int nr = s->nr, nz = s->nz;
+    double *vr = s->f[FGPU_V_RADIAL], *vaz = s->f[FGPU_V_AZIMUTHAL], *en = s->f[FGPU_ENERGY];
+    const double rin = p->rmin * p->damping_inner_limit, rout = p->rmax * p->damping_outer_limit;
+    int vr_lo, vr_hi, az_lo, az_hi;
+    double tau;
+    if (side) {
+	if (!(p->damping_outer_limit < 1.0 && s->Rinf[nr] > rout)) return;
+	vr_lo = clamp_id(cell_id_rinf(s, rout), 1, nr) + 1;
+	vr_hi = nr - 1; /* MaxMo_no_ghost_vr */
+	az_lo = clamp_id(cell_id_rmed(s, rout), 0, nr) + 1;
+	az_hi = nr - 1; /* Max_no_ghost */
+	tau = p->damping_time_factor * 2.0 * M_PI / omega_kepler(s, p->damping_time_radius_outer);
+    } else {
+	if (!(p->damping_inner_limit > 1.0 && s->Rmed[0] < rin)) return;
+	vr_lo = 2; /* One_no_ghost_vr */
+	vr_hi = clamp_id(cell_id_rinf(s, rin), 1, nr) + 1;
+	az_lo = 1; /* Zero_no_ghost */
+	az_hi = clamp_id(cell_id_rmed(s, rin), 0, nr) + 1;
+	tau = p->damping_time_factor * 2.0 * M_PI / omega_kepler(s, p->rmin);
+    }
+    for (int i = vr_lo; i < vr_hi; ++i) {
+	const double factor = side ? pow((s->Rinf[i] - rout) / (p->rmax - rout), 2)
+				   : pow((s->Rinf[i] - rin) / (p->rmin - rin), 2);
+	const double ef = exp(-dt * factor / tau);
+	for (int j = 0; j < nz; ++j) {
+	    const double phi = (double)j * s->dphi;
+	    const double rinf = s->Rinf[i];
+	    const double cx = rinf * cos(phi), cy = rinf * sin(phi);
+	    double vx, vy;
+	    com_velocity(s, side, 1, c, cx, cy, &vx, &vy);
+	    const double v0 = (cx * vx + cy * vy) / rinf;
+	    double *v = &vr[(size_t)i * nz + j];
+	    *v = (*v - v0) * ef + v0;
+	}
+    }
+    for (int i = az_lo; i < az_hi; ++i) {
+	/* both sides use the outer zone's profile here (center_of_mass.cpp:491-494,
+	   628-631) */
+	const double factor = pow((s->Rmed[i] - rout) / (p->rmax - rout), 2);
+	const double ef = exp(-dt * factor / tau);
+	for (int j = 0; j < nz; ++j) {
+	    const double phi = ((double)j - 0.5) * s->dphi;
+	    const double rmed = s->Rmed[i];
+	    const double cx = rmed * cos(phi), cy = rmed * sin(phi);
+	    double vx, vy;
+	    com_velocity(s, side, 1, c, cx, cy, &vx, &vy);
+	    const double v0 = (cx * vy - vx * cy) / rmed - s->omega_frame * rmed;
+	    double *v = &vaz[(size_t)i * nz + j];
+	    *v = (*v - v0) * ef + v0;
+	}
+    }
+    if (adiabatic(s)) {
+	for (int i = az_lo; i < az_hi; ++i) {
+	    const double factor = pow((s->Rmed[i] - rout) / (p->rmax - rout), 2);
+	    const double ef = exp(-dt * factor / tau);
+	    for (int j = 0; j < nz; ++j) {
+		const double cx = s->Rmed[i] * s->cosj[j], cy = s->Rmed[i] * s->sinj[j];
+		const double x_com = cx - c->x, y_com = cy - c->y;
+		const double r_com = sqrt(x_com * x_com + y_com * y_com);
+		const double e0 = th_energy(s, r_com, c->mass);
+		double *e = &en[(size_t)i * nz + j];
+		*e = (*e - e0) * ef + e0;
+	    }
+	}
+    }
+}
+
+static int com_active(const or_state *s, int side)
+{
+    return (side ? s->p.composite_outer : s->p.composite_inner) == FGPU_COMPOSITE_CENTER_OF_MASS;
+}
+
+static int apply_bc(or_state *s, double dt, int final, const fgpu_frame_center *c);
+
 int or_apply_boundary_condition(or_state *s, double t, double dt, int final)
 {
     (void)t;
+    return apply_bc(s, dt, final, s->com_now);
+}
+
+static int apply_bc(or_state *s, double dt, int final, const fgpu_frame_center *c)
+{
     const fgpu_params *p = &s->p;
+    if ((com_active(s, 0) || com_active(s, 1)) && !s->com_ready) return FGPU_ERR_BAD_ARG;
     if (final && (p->viscous_accretion || p->bc_vrad_inner == FGPU_BC_VISCOUS)) {
 	/* parameters::VISCOUS_ACCRETION (Interpret.cpp:704-707): c_s, H, nu of
 	   the transported state before the final boundary call
@@ -1157,6 +1596,9 @@ int or_apply_boundary_condition(or_state *s, double t, double dt, int final)
 	    damp_one(s, q, 0, dt);
 	    damp_one(s, q, 1, dt);
 	}
+	/* boundary_conditions.cpp:46-60 */
+	if (com_active(s, 0)) com_damp(s, 0, &c[0], dt);
+	if (com_active(s, 1)) com_damp(s, 1, &c[1], dt);
     }
     ghost_hook(s, FGPU_SIGMA, p->bc_sigma_inner, 0);
     ghost_hook(s, FGPU_SIGMA, p->bc_sigma_outer, 1);
@@ -1166,6 +1608,9 @@ int or_apply_boundary_condition(or_state *s, double t, double dt, int final)
     ghost_hook(s, FGPU_V_RADIAL, p->bc_vrad_outer, 1);
     ghost_hook(s, FGPU_V_AZIMUTHAL, p->bc_vaz_inner, 0);
     ghost_hook(s, FGPU_V_AZIMUTHAL, p->bc_vaz_outer, 1);
+    /* the composite after the per-field hooks, boundary_conditions.cpp:92-102 */
+    if (com_active(s, 0)) com_ghost(s, 0, &c[0]);
+    if (com_active(s, 1)) com_ghost(s, 1, &c[1]);
     return FGPU_OK;
 }
 
@@ -1446,10 +1891,12 @@ void or_gas_kick(or_state *s, double dt, double t)
 
 int or_step_euler(or_state *s, double dt, double t)
 {
+    if ((com_active(s, 0) || com_active(s, 1)) && !s->com_ready) return FGPU_ERR_BAD_ARG;
     or_gas_kick(s, dt, t);
-    or_apply_boundary_condition(s, t, 0.0, 0);
+    apply_bc(s, 0.0, 0, s->com_now);
     or_transport(s, dt);
-    or_apply_boundary_condition(s, t + dt, dt, 1);
+    /* the final call sees the bodies after the N-body step (simulation.cpp:219-244) */
+    apply_bc(s, dt, 1, s->com_after);
     or_recalculate_derived(s, t + dt);
     return FGPU_OK;
 }

@@ -43,6 +43,10 @@ void or_compute_pressure(or_state *s);
 int or_disk_on_planet_accel(or_state *s, int k, double accel[2]);
 double or_total_mass(or_state *s);
 int or_accrete_onto_planet(or_state *s, const fgpu_accretor *a, double dt, double out[3]);
+int or_init_center_of_mass_boundary(or_state *s, double mass_all, double mass_center,
+				    int binary_on_primary, double com_max_dist);
+int or_set_frame_centers(or_state *s, const fgpu_frame_center now[2],
+			 const fgpu_frame_center *after);
 
 /* Sub-steps, exported so tests can check the GPU kernels one phase at a time. */
 void or_calculate_potential(or_state *s);

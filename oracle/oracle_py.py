@@ -13,7 +13,8 @@ import subprocess
 
 import numpy as np
 
-from fargocpt_gb300.abi import FIELDS, VECTOR_FIELDS, FgpuAccretor, FgpuBody, FgpuParams
+from fargocpt_gb300.abi import (FIELDS, VECTOR_FIELDS, FgpuAccretor, FgpuBody,
+                                FgpuFrameCenter, FgpuParams)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
@@ -53,6 +54,10 @@ def _load():
     lib.or_total_mass.argtypes = [vp]
     lib.or_total_mass.restype = C.c_double
     lib.or_accrete_onto_planet.argtypes = [vp, C.POINTER(FgpuAccretor), C.c_double, dp]
+    lib.or_init_center_of_mass_boundary.argtypes = [vp, C.c_double, C.c_double, C.c_int,
+                                                    C.c_double]
+    lib.or_set_frame_centers.argtypes = [vp, C.POINTER(FgpuFrameCenter),
+                                         C.POINTER(FgpuFrameCenter)]
     for name in ("or_calculate_potential", "or_viscous_stress_tensor"):
         getattr(lib, name).argtypes = [vp]
     for name in ("or_update_with_sourceterms", "or_artificial_viscosity",
@@ -156,6 +161,18 @@ class OracleState:
         if rc != 0:
             raise ValueError(rc)
         return out[0], out[1], out[2]
+
+    def init_center_of_mass_boundary(self, mass_all, mass_center, binary_on_primary,
+                                     com_max_dist):
+        rc = self.lib.or_init_center_of_mass_boundary(self.h, mass_all, mass_center,
+                                                      int(binary_on_primary), com_max_dist)
+        if rc != 0:
+            raise ValueError(rc)
+
+    def set_frame_centers(self, now, after=None):
+        n = (FgpuFrameCenter * 2)(*[FgpuFrameCenter(*c) for c in now])
+        a = (FgpuFrameCenter * 2)(*[FgpuFrameCenter(*c) for c in after]) if after else None
+        self.lib.or_set_frame_centers(self.h, n, a)
 
     # phase-by-phase access for kernel tests
     def phase(self, name, *args):

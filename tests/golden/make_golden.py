@@ -34,7 +34,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 
-from fargocpt_gb300.abi import ACCRETION, BC, DAMP, BETA_REF  # noqa: E402
+from fargocpt_gb300.abi import ACCRETION, BC, COMPOSITE, DAMP, BETA_REF  # noqa: E402
 
 REF_SRC = os.environ.get("FARGO_REFERENCE_SRC", "/root/reference/src")
 REF_EXE = os.path.join(REPO, "oracle", "_ref", "parity", "fargocpt")
@@ -274,6 +274,42 @@ CASES = {
                   DampingVAzimuthalInner="Reference", DampingVAzimuthalOuter="Reference",
                   MonitorTimestep=0.05, Nsnapshots=4),
         nrad=16, naz=40, rmin=0.4, rmax=2.5, planet=None, keep=[1, 2, 3, 4]),
+    # centre-of-mass composite at both edges (center_of_mass.cpp) with its
+    # damping: locally isothermal, one planet (the star-planet pair takes the
+    # binary branch of the viscous-speed tables), fixed dt
+    "iso_planet_bc_com": dict(
+        keys=dict(SigmaSlope=0.5, AspectRatio=0.05, FlaringIndex=0.0,
+                  EquationOfState="Isothermal", ViscousAlpha=1e-3,
+                  ArtificialViscosity="SN", Transport="FARGO",
+                  InnerBoundary="centerofmass", OuterBoundary="centerofmass",
+                  Damping="yes", DampingInnerLimit=1.1, DampingOuterLimit=0.9,
+                  MonitorTimestep=0.002, Nsnapshots=20),
+        nrad=20, naz=48, rmin=0.4, rmax=2.5, planet=1e-3, keep=[1, 2, 5, 10, 20]),
+    # the same with the Keplerian model (InitializePureKeplerian): adiabatic,
+    # star only, CFL-limited, energy damping
+    "adi_star_cfl_bc_com_keplerian": dict(
+        keys=dict(SigmaSlope=1.0, AspectRatio=0.05, FlaringIndex=0.25,
+                  EquationOfState="Ideal", AdiabaticIndex=1.4, ViscousAlpha=1e-2,
+                  ArtificialViscosity="SN", CoolingBetaLocal="yes", CoolingBeta=10,
+                  Transport="FARGO", InitializePureKeplerian="yes",
+                  InnerBoundary="centerofmass", OuterBoundary="centerofmass",
+                  Damping="yes", DampingInnerLimit=1.2, DampingOuterLimit=0.85,
+                  MonitorTimestep=0.4, Nsnapshots=4),
+        nrad=16, naz=40, rmin=0.3, rmax=3.0, planet=None, keep=[1, 2, 3, 4]),
+    # the viscous-speed model at an adiabatic disk with a planet: the outer
+    # grid correction of the tables, energy at both ghost rings
+    "adi_planet_bc_com": dict(
+        keys=dict(SigmaSlope=1.0, AspectRatio=0.05, FlaringIndex=0.25,
+                  EquationOfState="Ideal", AdiabaticIndex=1.4, ViscousAlpha=3e-3,
+                  ArtificialViscosity="SN", CoolingBetaLocal="yes", CoolingBeta=10,
+                  Transport="FARGO",
+                  InnerBoundary="zerogradient", OuterBoundary="centerofmass",
+                  Damping="yes", DampingInnerLimit=1.15, DampingOuterLimit=0.85,
+                  DampingSurfaceDensityInner="Reference",
+                  DampingVRadialInner="Reference", DampingVAzimuthalInner="Reference",
+                  DampingEnergyInner="Reference",
+                  MonitorTimestep=0.002, Nsnapshots=20),
+        nrad=20, naz=48, rmin=0.3, rmax=3.0, planet=3e-3, keep=[1, 2, 5, 10, 20]),
 }
 
 
@@ -312,7 +348,8 @@ def engine_params(case, consts, temp_unit):
     def composite(name):   # boundary_conditions/config.cpp:344-430
         return {"zerogradient": ("zerogradient", "zerogradient", "zerogradient"),
                 "outflow": ("zerogradient", "zerogradient", "outflow"),
-                "reference": ("reference", "reference", "reference")}[name]
+                "reference": ("reference", "reference", "reference"),
+                "centerofmass": ("none", "none", "none")}[name]
 
     def side_names(side, comp):
         # per-field names after the composite and the individual keys
@@ -323,7 +360,8 @@ def engine_params(case, consts, temp_unit):
         for key, fld in (("Sigma", "sigma"), ("Vrad", "vrad")):
             if f"{side}Boundary{key}" in k:
                 names[fld] = str(k[f"{side}Boundary{key}"]).lower()
-        names["vazi"] = str(k.get(f"{side}BoundaryVazi", "keplerian")).lower()
+        default_vazi = "none" if comp == "centerofmass" else "keplerian"
+        names["vazi"] = str(k.get(f"{side}BoundaryVazi", default_vazi)).lower()
         return names
 
     nin, nout = side_names("Inner", inner), side_names("Outer", outer)
@@ -386,6 +424,12 @@ def engine_params(case, consts, temp_unit):
         damping_time_radius_outer=float(case["rmax"]),
         vaz_inner_keplerian_factor=1.0, vaz_outer_keplerian_factor=1.0,
         rmin=float(case["rmin"]), rmax=float(case["rmax"]), radial_spacing=1,
+        composite_inner=COMPOSITE.get(inner, 0), composite_outer=COMPOSITE.get(outer, 0),
+        initialize_pure_keplerian=int(str(k.get("InitializePureKeplerian", "no")) == "yes"),
+        initialize_vradial_zero=int(str(k.get("InitializeVradialZero", "no")) == "yes"),
+        profile_cutoff_point_outer=1.0e300, profile_cutoff_width_outer=1.0,
+        profile_cutoff_point_inner=0.0, profile_cutoff_width_inner=1.0,
+        temperature_cgs_to_code=1.0 / temp_unit,
     )
 
 

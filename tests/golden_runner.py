@@ -13,8 +13,8 @@ import os
 import numpy as np
 
 from fargocpt_gb300.abi import FgpuAccretor, params_from_dict
-from fargocpt_gb300.simulation import (RunClock, advance, indirect_term_euler, l1_point,
-                                       orbital_period, start)
+from fargocpt_gb300.simulation import (RunClock, advance, center_of_mass, com_boundary_setup,
+                                       indirect_term_euler, l1_point, orbital_period, start)
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = ["iso_planet_fixed_dt", "adi_planet_fixed_dt", "iso_star_cfl",
@@ -22,7 +22,8 @@ CASES = ["iso_planet_fixed_dt", "adi_planet_fixed_dt", "iso_star_cfl",
          "adi_planet_tw", "adi_star_cfl_tw_stab1", "iso_star_cfl_tw_stab2",
          "iso_planet_accretion_kley", "adi_planet_accretion_sinkhole",
          "iso_planet_accretion_viscous", "iso_planet_bc_individual",
-         "adi_star_cfl_bc_individual"]
+         "adi_star_cfl_bc_individual", "iso_planet_bc_com", "adi_star_cfl_bc_com_keplerian",
+         "adi_planet_bc_com"]
 EVOLVED = ["SIGMA", "V_RADIAL", "V_AZIMUTHAL", "ENERGY"]
 
 
@@ -41,6 +42,28 @@ def bodies_at(arrays, nb, row):
         m = float(arrays[f"body{k}_mass"][row])
         out.append((x, y, m, 0.0, math.sqrt(x * x + y * y)))
     return out
+
+
+def moving_bodies_at(arrays, nb, row):
+    """(x, y, vx, vy, mass) of every body at monitor row `row`."""
+    return [tuple(float(arrays[f"body{k}_{q}"][row]) for q in ("x", "y", "vx", "vy", "mass"))
+            for k in range(nb)]
+
+
+def frame_centers_at(arrays, nb, row, dt):
+    """The centres the two boundary calls of the step after monitor row `row`
+    read: before transport, the bodies of the row after
+    apply_indirect_term_on_Nbody (planetary_system.cpp:730-744,
+    simulation.cpp:165-166); after the N-body step, the next row."""
+    mb = moving_bodies_at(arrays, nb, row)
+    if nb > 1:
+        ix, iy = indirect_term_euler(bodies_at(arrays, nb, row))
+    else:
+        ix, iy = 0.0, 0.0
+    kicked = [(x, y, vx + dt * ix, vy + dt * iy, m) for (x, y, vx, vy, m) in mb]
+    nxt = moving_bodies_at(arrays, nb, min(row + 1, len(arrays["body0_x"]) - 1))
+    return ([center_of_mass(kicked, 1), center_of_mass(kicked, nb)],
+            [center_of_mass(nxt, 1), center_of_mass(nxt, nb)])
 
 
 def accretor_at(arrays, meta, row):
@@ -101,6 +124,16 @@ def replay(make_backend, name, params_override=None, accreted=None):
     hyd.set_field("V_RADIAL", arrays["s0_V_RADIAL"])
     hyd.set_field("V_AZIMUTHAL", arrays["s0_V_AZIMUTHAL"])
 
+    frame_centers = None
+    if int(pd.get("composite_inner", 0)) == 1 or int(pd.get("composite_outer", 0)) == 1:
+        mb = moving_bodies_at(arrays, nb, 0)
+        hyd.init_center_of_mass_boundary(*com_boundary_setup(mb, float(pd["G"])))
+        c0 = [center_of_mass(mb, 1), center_of_mass(mb, nb)]
+        hyd.set_frame_centers(c0)
+
+        def frame_centers(c, dt):
+            return frame_centers_at(arrays, nb, c.n_monitor, dt)
+
     clock = RunClock(time=0.0, last_dt=meta["first_dt"])
     cmv = float(pd["cfl_max_var"])
     start(hyd, clock, cmv)
@@ -130,7 +163,7 @@ def replay(make_backend, name, params_override=None, accreted=None):
             t_final=t_final, bodies=lambda c: body_state(c.n_monitor),
             on_monitor=on_monitor,
             integrator="leapfrog" if int(pd.get("integrator", 0)) == 1 else "euler",
-            accrete=accrete)
+            accrete=accrete, frame_centers=frame_centers)
     return snaps, times, torques, clock.dts, arrays
 
 

@@ -65,6 +65,27 @@ def test_unsupported_options_are_reported(lib):
     assert lib.fgpu_create(C.byref(p), out.ctypes.data_as(C.POINTER(C.c_double)), C.byref(h)) == -4
 
 
+def test_center_of_mass_composite_is_validated(lib):
+    from gpu_cases import make_params
+    radii = np.linspace(0.4, 2.5, 18)
+    rd = radii.ctypes.data_as(C.POINTER(C.c_double))
+    h = C.c_void_p()
+    p, _ = make_params(16, 32, composite_outer=2)
+    assert lib.fgpu_create(C.byref(p), rd, C.byref(h)) == -1
+    # per-field damping on a centre-of-mass edge dies in the reference
+    # (boundary_conditions/config.cpp:512-528)
+    p, _ = make_params(16, 32, composite_outer=1)
+    assert list(p.damping_outer) != [0, 0, 0, 0]
+    assert lib.fgpu_create(C.byref(p), rd, C.byref(h)) == -1
+    # the batched form has no centre-of-mass boundary
+    q, _ = make_params(16, 48, composite_inner=1, damping_inner=[0, 0, 0, 0], precision=1)
+    ps = (abi.FgpuParams * 1)(q)
+    rp = (C.POINTER(C.c_double) * 1)(rd)
+    assert lib.fgpu_batch_create(1, ps, rp, C.byref(h)) == -4
+    assert lib.fgpu_init_center_of_mass_boundary(None, 1.0, 1.0, 0, 0.0) == -1
+    assert lib.fgpu_set_frame_centers(None, None, None) == -1
+
+
 def test_no_device_is_an_error_not_a_fallback(lib):
     try:
         import torch

@@ -162,3 +162,69 @@ def test_accretion_onto_planet(kind):
     for f in EVOLVED:
         err = rel_linf(g.get_field(f), o.get_field(f))
         assert err <= TOL, f"{f}: {err:.3e}"
+
+
+@pytest.mark.parametrize("keplerian", [False, True])
+def test_center_of_mass_boundary(keplerian):
+    """The centre-of-mass composite (center_of_mass.cpp) at both edges with
+    its damping, on a 48 x 128 adiabatic disk in a rotating frame: a centre
+    that moves within and between steps, the binary branch of the
+    viscous-speed tables, the quadrupole term of the outer model; or the
+    Keplerian model with InitializeVradialZero."""
+    from fargocpt_gb300.engine import Engine, grid_radii
+    from oracle.oracle_py import OracleState
+
+    params, d = make_params(48, 128, adiabatic=True, composite_inner=1, composite_outer=1,
+                            damping_inner=[0, 0, 0, 0], damping_outer=[0, 0, 0, 0],
+                            damping_inner_limit=1.2, damping_outer_limit=0.85,
+                            binary_quadrupole_moment=2e-4,
+                            initialize_pure_keplerian=int(keplerian),
+                            initialize_vradial_zero=1, temperature_cgs_to_code=1e-3)
+    radii = grid_radii(d["radial_spacing"], d["rmin"], d["rmax"], d["nrad"])
+    st = initial_state(d, radii, seed=11)
+    bodies = [(0.0, 0.0, 1.0, 0.0, 0.0), (1.0, 0.05, 1e-3, 0.0, math.hypot(1.0, 0.05))]
+
+    def centres(n):
+        ph = 0.3 + 0.05 * n
+        q = 1e-3 / 1.001
+        return [(0.0, 0.0, 0.0, 0.0, 1.0),
+                (q * math.cos(ph), q * math.sin(ph), -q * math.sin(ph), q * math.cos(ph), 1.001)]
+
+    res = []
+    for cls in (OracleState, Engine):
+        b = cls(params, radii)
+        load(b, st, bodies)
+        b.set_bodies(bodies, 0.0, 0.0, 0.25)
+        b.init_center_of_mass_boundary(1.001, 1.0, 1, 1.0 * 1e-3 / 1.001)
+        b.set_frame_centers(centres(0))
+        b.apply_boundary_condition(0.0, 0.0, False)
+        t = 0.0
+        for n in range(8):
+            b.set_frame_centers(centres(n), centres(n + 1))
+            dt = b.condition_cfl()
+            b.step_euler(dt, t)
+            t += dt
+        res.append(b)
+    o, g = res
+    for f in EVOLVED:
+        err = rel_linf(g.get_field(f), o.get_field(f))
+        assert err <= TOL, f"{f}: {err:.3e}"
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_engines_with_different_rings_coexist(precision):
+    # A kernel's dynamic shared-memory limit is process-wide: an engine with
+    # short rings created after one with long rings (more than 48 KB of ring
+    # in shared memory) must not lower the limit the first one launches with.
+    from fargocpt_gb300.engine import Engine, grid_radii
+
+    engines = []
+    for naz in (1536, 64):
+        params, d = make_params(16, naz, precision=precision)
+        radii = grid_radii(d["radial_spacing"], d["rmin"], d["rmax"], d["nrad"])
+        e = Engine(params, radii)
+        load(e, initial_state(d, radii, seed=5), [(0.0, 0.0, 1.0, 0.0, 0.0)])
+        engines.append(e)
+    for e in engines:
+        e.step_euler(e.condition_cfl(), 0.0)
+        assert np.all(np.isfinite(e.get_field("SIGMA")))
