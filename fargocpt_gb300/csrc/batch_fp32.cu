@@ -269,6 +269,7 @@ __device__ void circular_bodies(const ClockF &c, float gm_ref, int star_is_centr
     b.x[0] = 0.0;
     b.y[0] = 0.0;
     b.a[0] = 0.0;
+    split_position(b, 0);
     b.gm[0] = (float)__dmul_rn(G, c.mstar);
     b.rsm[0] = 0.f;
     double ax = 0.0, ay = 0.0;
@@ -279,6 +280,7 @@ __device__ void circular_bodies(const ClockF &c, float gm_ref, int star_is_centr
         const double x = __dmul_rn(a, cos(ang)), y = __dmul_rn(a, sin(ang));
         b.x[p + 1] = x;
         b.y[p + 1] = y;
+        split_position(b, p + 1);
         b.a[p + 1] = a;
         b.gm[p + 1] = (float)__dmul_rn(G, m);
         b.rsm[p + 1] = 0.f;

@@ -194,8 +194,14 @@ __device__ __forceinline__ void potential_cell(const GeoF &g, const TablesF &t, 
                                                float *__restrict__ pot, int i, int j)
 {
     const int nz = g.nz;
-    const double xd = t.Rmed_d[i] * t.cos_d[j];
-    const double yd = t.Rmed_d[i] * t.sin_d[j];
+    // the cell centre as float pairs (x = xh + xl): the product's rounding
+    // error by FMA plus the cross terms of the split factors; the distance to
+    // a body then loses nothing to cancellation however close the body is
+    const float rh = t.Rmed[i], rl = t.RmedLo[i];
+    const float ch = t.cosHi[j], cl = t.cosLo[j], sh = t.sinHi[j], sl = t.sinLo[j];
+    const float xh = rh * ch, yh = rh * sh;
+    const float xl = fmaf(rh, ch, -xh) + fmaf(rh, cl, rl * ch);
+    const float yl = fmaf(rh, sh, -yh) + fmaf(rh, sl, rl * sh);
     const float eps = ph.eps_smooth * H[CELL(i, j)];
     const float s2 = eps * eps;
     float acc = 0.f;
@@ -207,9 +213,26 @@ __device__ __forceinline__ void potential_cell(const GeoF &g, const TablesF &t, 
             const float r = t.Rmed[i];
             const float d = sqrtf(r * r + s2);
             term = b.gm[0] * s2 / ((d + r) * r * d);
-        } else {
-            const double dx = xd - b.x[k], dy = yd - b.y[k];
+        } else if (k == 0) {
+            // central object off the origin: residual against -G M / r in FP64
+            const double xd = t.Rmed_d[i] * t.cos_d[j], yd = t.Rmed_d[i] * t.sin_d[j];
+            const double dx = xd - b.x[0], dy = yd - b.y[0];
             const float d2 = (float)(dx * dx + dy * dy) + s2;
+            const float inv_d = rsqrtf(d2);
+            float fk = 1.f;
+            if (b.rsm[0] > 0.f) {
+                const float dsm = d2 * inv_d;
+                if (dsm < b.rsm[0]) {
+                    const float q = dsm / b.rsm[0];
+                    fk = q * q * q * q - 2.f * q * q * q + 2.f * q;
+                }
+            }
+            term = (float)(-(double)b.gm[0] * fk / sqrt(dx * dx + dy * dy + (double)s2) +
+                           (double)b.gm_ref * t.InvRmed_d[i]);
+        } else {
+            const float dx = (xh - b.xh[k]) + (xl - b.xl[k]);
+            const float dy = (yh - b.yh[k]) + (yl - b.yl[k]);
+            const float d2 = fmaf(dx, dx, fmaf(dy, dy, s2));
             const float inv_d = rsqrtf(d2);
             float fk = 1.f;
             if (b.rsm[k] > 0.f) {
@@ -219,17 +242,11 @@ __device__ __forceinline__ void potential_cell(const GeoF &g, const TablesF &t, 
                     fk = q * q * q * q - 2.f * q * q * q + 2.f * q;
                 }
             }
-            if (k == 0) {
-                // central object off the origin: residual against -G M / r in FP64
-                term = (float)(-(double)b.gm[0] * fk / sqrt(dx * dx + dy * dy + (double)s2) +
-                               (double)b.gm_ref * t.InvRmed_d[i]);
-            } else {
-                term = -b.gm[k] * inv_d * fk;
-            }
+            term = -b.gm[k] * inv_d * fk;
         }
         acc += term;
     }
-    acc += -b.ix * (float)xd - b.iy * (float)yd;
+    acc = fmaf(-b.iy, yh + yl, fmaf(-b.ix, xh + xl, acc));
     pot[CELL(i, j)] = acc;
 }
 

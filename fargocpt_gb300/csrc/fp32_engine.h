@@ -50,6 +50,9 @@ struct TablesF {
     const float *OmRefDiff; // v_K(i)/R(i) - v_K(i+1)/R(i+1)
     const float *Vref;      // v_K(Rmed)
     const double *Rmed_d, *InvRmed_d, *Vref_d, *Surf_d, *PhiK_d, *cos_d, *sin_d;
+    // cell centres as float pairs: Rmed = Rmed + RmedLo, cos (j dphi) =
+    // cosHi + cosLo, sin likewise
+    const float *RmedLo, *cosHi, *cosLo, *sinHi, *sinLo;
 };
 
 struct PhysF {
@@ -68,9 +71,19 @@ struct BodiesF {
     int n;
     int star_at_origin;
     double x[kMaxBodies], y[kMaxBodies], a[kMaxBodies];
+    float xh[kMaxBodies], xl[kMaxBodies], yh[kMaxBodies], yl[kMaxBodies]; // x = xh + xl
     float gm[kMaxBodies], rsm[kMaxBodies];
     float gm_ref, ix, iy;
 };
+
+// the position of body k as an unevaluated pair of floats
+__host__ __device__ inline void split_position(BodiesF &b, int k)
+{
+    b.xh[k] = (float)b.x[k];
+    b.xl[k] = (float)(b.x[k] - (double)b.xh[k]);
+    b.yh[k] = (float)b.y[k];
+    b.yl[k] = (float)(b.y[k] - (double)b.yh[k]);
+}
 
 struct BcF {
     int sigma_in, sigma_out, energy_in, energy_out, vr_in, vr_out, vaz_in, vaz_out;
@@ -227,6 +240,7 @@ class Engine32 {
     float *mom[4] = {};
     float *tab_f = nullptr;
     double *tab_d = nullptr;
+    float *tab_c = nullptr;  // cosHi, cosLo, sinHi, sinLo
     float *damp_mem = nullptr, *damp_aux = nullptr;
     int *damp_rings = nullptr;
     int n_rings = 0;

@@ -199,47 +199,63 @@ __global__ void f_derived_cfl(GeoF g, TablesF t, PhysF ph, int mode, const float
 
 // disk force on a body and gas mass: FP64 separations and accumulation
 __global__ void f_disk_force(GeoF g, TablesF t, PhysF ph, double px, double py, double pa,
-                             double rsm, const float *__restrict__ S, const float *__restrict__ H,
+                             double rsm, const float *__restrict__ S,
+                             const float *__restrict__ S_lo, const float *__restrict__ H,
                              double *__restrict__ partial)
 {
     __shared__ double red[33];
     const int nz = g.nz;
     const int i = blockIdx.x + 1;
     const size_t row = (size_t)i * nz;
+    // sigma as its compensated pair; the ring sum gives the ring mean and,
+    // times the cell area, the ring's mass
     double ps = 0.0;
-    for (int j = threadIdx.x; j < nz; j += blockDim.x) ps += (double)S[row + j];
-    const double sigma1d = bsum_d(ps, red) / nz;
-    double ax = 0.0, ay = 0.0, mass = 0.0;
+    for (int j = threadIdx.x; j < nz; j += blockDim.x)
+        ps += (double)S[row + j] + (double)S_lo[row + j];
+    const double ring_sum = bsum_d(ps, red);
+    const double sigma1d = ring_sum / nz;
+    // cell centres and the planet as float pairs (see potential_cell): the
+    // distance loses nothing to cancellation near the planet
+    const float pxh = (float)px, pxl = (float)(px - (double)pxh);
+    const float pyh = (float)py, pyl = (float)(py - (double)pyh);
+    const float rh = t.Rmed[i], rl = t.RmedLo[i];
+    const float frsm = (float)rsm;
+    double ax = 0.0, ay = 0.0;
     for (int j = threadIdx.x; j < nz; j += blockDim.x) {
-        const double dx = t.Rmed_d[i] * t.cos_d[j] - px, dy = t.Rmed_d[i] * t.sin_d[j] - py;
+        const float ch = t.cosHi[j], cl = t.cosLo[j], sh = t.sinHi[j], sl = t.sinLo[j];
+        const float xh = rh * ch, yh = rh * sh;
+        const float xl = fmaf(rh, ch, -xh) + fmaf(rh, cl, rl * ch);
+        const float yl = fmaf(rh, sh, -yh) + fmaf(rh, sl, rl * sh);
+        const float dx = (xh - pxh) + (xl - pxl);
+        const float dy = (yh - pyh) + (yl - pyl);
         const float sm = ph.eps_smooth * H[row + j];
-        const float d2 = (float)(dx * dx + dy * dy) + sm * sm;
+        const float d2 = fmaf(dx, dx, fmaf(dy, dy, sm * sm));
         const float rinv = rsqrtf(d2);
         float fk = 1.f;
         if (rsm > 0.0) {
             const float dsm = d2 * rinv;
-            if (dsm < (float)rsm) {
-                const float q = dsm / (float)rsm;
+            if (dsm < frsm) {
+                const float q = dsm / frsm;
                 fk = -(3.f * q * q * q * q - 4.f * q * q * q);
             }
         }
-        const double cellmass = t.Surf_d[i] * ((double)S[row + j] - sigma1d);
-        const double w = cellmass * (double)(rinv * rinv * rinv * fk) * ph.G_d;
-        ax += w * dx;
-        ay += w * dy;
-        mass += t.Surf_d[i] * (double)S[row + j];
+        // the ring mean is subtracted in FP64 (CorrectDiskSelfgravity)
+        const float dsig = (float)(((double)S[row + j] + (double)S_lo[row + j]) - sigma1d);
+        const float w = dsig * (rinv * rinv * rinv * fk);
+        ax += (double)(w * dx);
+        ay += (double)(w * dy);
     }
     ax = bsum_d(ax, red);
     ay = bsum_d(ay, red);
-    mass = bsum_d(mass, red);
     if (threadIdx.x == 0) {
+        const double f = t.Surf_d[i] * ph.G_d;
         const bool inner = t.Rmed_d[i] < pa;
         double *p = partial + (size_t)blockIdx.x * 5;
-        p[0] = inner ? ax : 0.0;
-        p[1] = inner ? ay : 0.0;
-        p[2] = inner ? 0.0 : ax;
-        p[3] = inner ? 0.0 : ay;
-        p[4] = mass;
+        p[0] = inner ? f * ax : 0.0;
+        p[1] = inner ? f * ay : 0.0;
+        p[2] = inner ? 0.0 : f * ax;
+        p[3] = inner ? 0.0 : f * ay;
+        p[4] = t.Surf_d[i] * ring_sum;
     }
 }
 
@@ -338,7 +354,7 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
            INVRINF, RINFSQ, TWOOVER, OMEGAK, INVOMEGAK, CSISO, INVDXSRC, INVDXTHETA, EMODEL,
            HFACADI, INVCELL, INVCELL2, TWOOVERRMEDSUM, KBAL, AFACE, SHEAR, DJ, JSLOPE, DRMED,
            OMREFDIFF, VREF, DRSUP, RSUPIDRR, LSQTW, TWOOVERDRMED2, RA3IDRMED, F43, CRPP1,
-           CRPP2, CRRR1, CRRR2, CRRP, CRSCALE, NT };
+           CRPP2, CRRR1, CRRR2, CRRP, CRSCALE, RMEDLO, NT };
     std::vector<float> hf((size_t)NT * R, 0.f);
     auto F = [&](int k) { return hf.data() + (size_t)k * R; };
     for (int n = 0; n <= nr; ++n) {
@@ -361,6 +377,7 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
         F(RINF)[n] = (float)Rinf[n];
         F(RSUP)[n] = (float)Rsup[n];
         F(RMED)[n] = (float)rm;
+        F(RMEDLO)[n] = (float)(rm - (double)(float)rm);
         F(SURF)[n] = (float)Surf[n];
         F(INVRMED)[n] = (float)(1.0 / rm);
         F(INVSURF)[n] = (float)(1.0 / Surf[n]);
@@ -428,6 +445,16 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
     CKF(cudaMemcpy(tab_f, hf.data(), sizeof(float) * hf.size(), cudaMemcpyHostToDevice));
     CKF(cudaMalloc(&tab_d, sizeof(double) * hd.size()));
     CKF(cudaMemcpy(tab_d, hd.data(), sizeof(double) * hd.size(), cudaMemcpyHostToDevice));
+    std::vector<float> hc((size_t)4 * nz);
+    for (int j = 0; j < nz; ++j) {
+        const double c = hd[5 * R + j], sn = hd[5 * R + nz + j];
+        hc[j] = (float)c;
+        hc[nz + j] = (float)(c - (double)hc[j]);
+        hc[2 * nz + j] = (float)sn;
+        hc[3 * nz + j] = (float)(sn - (double)hc[2 * nz + j]);
+    }
+    CKF(cudaMalloc(&tab_c, sizeof(float) * hc.size()));
+    CKF(cudaMemcpy(tab_c, hc.data(), sizeof(float) * hc.size(), cudaMemcpyHostToDevice));
     auto Df = [&](int k) -> const float * { return tab_f + (size_t)k * R; };
     TablesF &t = tabs;
     t.Rinf = Df(RINF); t.Rsup = Df(RSUP); t.Rmed = Df(RMED); t.Surf = Df(SURF);
@@ -444,6 +471,8 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
     t.CrRr1 = Df(CRRR1); t.CrRr2 = Df(CRRR2); t.CrRp = Df(CRRP); t.CrScale = Df(CRSCALE); t.OmRefDiff = Df(OMREFDIFF); t.Vref = Df(VREF);
     t.Rmed_d = tab_d; t.InvRmed_d = tab_d + R; t.Vref_d = tab_d + 2 * R; t.Surf_d = tab_d + 3 * R;
     t.PhiK_d = tab_d + 4 * R; t.cos_d = tab_d + 5 * R; t.sin_d = tab_d + 5 * R + nz;
+    t.RmedLo = Df(RMEDLO);
+    t.cosHi = tab_c; t.cosLo = tab_c + nz; t.sinHi = tab_c + 2 * nz; t.sinLo = tab_c + 3 * nz;
 
     // physics
     PhysF &ph = phys;
@@ -662,7 +691,7 @@ void Engine32::destroy()
     for (int k = 0; k < 4; ++k) cudaFree(mom[k]);
     cudaFree(partial); cudaFree(red_out); cudaFree(d_dtmin); cudaFree(d_bad); cudaFree(stage);
     cudaFree(corr_phi); cudaFree(corr_r);
-    cudaFree(tab_f); cudaFree(tab_d); cudaFree(damp_mem); cudaFree(damp_aux); cudaFree(damp_rings);
+    cudaFree(tab_f); cudaFree(tab_d); cudaFree(tab_c); cudaFree(damp_mem); cudaFree(damp_aux); cudaFree(damp_rings);
     if (h_pinned) cudaFreeHost(h_pinned);
 }
 
@@ -763,6 +792,7 @@ void Engine32::set_bodies(int n, const fgpu_body *b, double ix, double iy)
     for (int k = 0; k < n; ++k) {
         bodies.x[k] = b[k].x;
         bodies.y[k] = b[k].y;
+        split_position(bodies, k);
         bodies.gm[k] = (float)(p.G * b[k].mass);
         bodies.rsm[k] = (float)b[k].r_sm;
         bodies.a[k] = b[k].a;
@@ -1047,7 +1077,7 @@ int Engine32::step(double dt, double t)
 int Engine32::disk_force(double px, double py, double pa, double rsm, double out[5])
 {
     const int rows = nr - 2;
-    f_disk_force<<<rows, 256, 0, stream>>>(geo, tabs, phys, px, py, pa, rsm, fld[FGPU_SIGMA],
+    f_disk_force<<<rows, 256, 0, stream>>>(geo, tabs, phys, px, py, pa, rsm, fld[FGPU_SIGMA], sigma_lo,
                                            fld[FGPU_SCALE_HEIGHT], partial);
     f_reduce_rows<<<1, 32 * 5, 0, stream>>>(partial, rows, red_out);
     CKF(cudaGetLastError());

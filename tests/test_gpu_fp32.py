@@ -142,3 +142,33 @@ def test_fp32_mixed_accreted_mass_matches_reference_monitor(name):
     assert len(accreted) == len(rate) - 1
     for n, m in accreted.items():
         assert abs(m / dt_mon - rate[n]) <= 1e-5 * rate[n], (n, m / dt_mon, rate[n])
+
+
+@pytest.mark.parametrize("where", [(1.0, 0.05), (1.002, 0.0021), (1.6, -0.9)])
+def test_fp32_disk_force_against_fp64_form(where):
+    """ComputeDiskOnPlanetAccel (Force.cpp:23-122) with the ring mean removed
+    (Pframeforce.cpp:175-190) on the same state in both forms: the FP32-mixed
+    form forms distances as float pairs and sums in FP64, within 1e-6 of the
+    FP64 acceleration (inner + outer parts) and 1e-12 of the mass, also with
+    the planet inside a cell and with Klahr smoothing."""
+    from fargocpt_gb300 import setups
+    from fargocpt_gb300.abi import params_from_dict
+    from fargocpt_gb300.engine import Engine
+
+    p64, d, radii, fields, _ = setups.build("c1")
+    d32 = dict(d)
+    d32["precision"] = 1
+    x, y = where
+    r = math.hypot(x, y)
+    bodies = [(0.0, 0.0, 1.0, 0.0, 0.0), (x, y, 1e-3, 0.4 * 0.07 * r, r)]
+    out = []
+    for e in (Engine(p64, radii), Engine(params_from_dict(d32), radii)):
+        for k, a in fields.items():
+            e.set_field(k, a)
+            e.set_field(k + "0", a)
+        e.set_bodies(bodies, 0.0, 0.0, 0.0)
+        e.init_euler(0.0)
+        out.append((np.array(e.disk_on_planet_accel(1)), e.total_mass()))
+    (a64, m64), (a32, m32) = out
+    assert np.linalg.norm(a32 - a64) <= 1e-6 * np.linalg.norm(a64)
+    assert abs(m32 - m64) <= 1e-12 * m64
