@@ -50,7 +50,7 @@ STEP_BYTES_PER_CELL = {"adiabatic": 64, "isothermal": 48}   # one read + write o
 NCU_DRAM_BYTES_C2 = {
     ("fp64", "transport_azimuthal"): 44.127e6 + 0.422e6,
     ("fp64", "transport_radial"): 25.252e6 + 0.738e6,
-    ("fp32", "transport_azimuthal"): 25.256e6 + 1.903e6,
+    ("fp32", "transport_azimuthal"): 25.286e6 + 0.0005e6,
 }
 KERNELS_IN_TIMED_STEP = 13   # the adiabatic step's kernels between the step's events
 

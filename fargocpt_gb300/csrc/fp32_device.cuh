@@ -41,6 +41,17 @@ __device__ __forceinline__ void comp_add(float &hi, float &lo, float inc)
     hi = s;
 }
 
+// hi + lo += x with the rounding error of hi + x kept in lo (TwoSum,
+// Knuth 1969: exact for any order of magnitudes)
+__device__ __forceinline__ void two_sum_add(float &hi, float &lo, float x)
+{
+    const float s = __fadd_rn(hi, x);
+    const float bb = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+    hi = s;
+    lo = __fadd_rn(lo, err);
+}
+
 __device__ __forceinline__ float tfloor(float e, float sigma, const PhysF &ph)
 {
     const float emin = sigma * ph.emin_fac;

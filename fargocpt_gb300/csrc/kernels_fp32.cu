@@ -197,7 +197,8 @@ __global__ void f_derived_cfl(GeoF g, TablesF t, PhysF ph, int mode, const float
                      blockIdx.x, red, red2, corr_phi, corr_r);
 }
 
-// disk force on a body and gas mass: FP64 separations and accumulation
+// disk force on a body and gas mass: separations as float pairs, sums as
+// compensated float pairs per thread and in FP64 across the block
 __global__ void f_disk_force(GeoF g, TablesF t, PhysF ph, double px, double py, double pa,
                              double rsm, const float *__restrict__ S,
                              const float *__restrict__ S_lo, const float *__restrict__ H,
@@ -208,19 +209,23 @@ __global__ void f_disk_force(GeoF g, TablesF t, PhysF ph, double px, double py, 
     const int i = blockIdx.x + 1;
     const size_t row = (size_t)i * nz;
     // sigma as its compensated pair; the ring sum gives the ring mean and,
-    // times the cell area, the ring's mass
-    double ps = 0.0;
-    for (int j = threadIdx.x; j < nz; j += blockDim.x)
-        ps += (double)S[row + j] + (double)S_lo[row + j];
-    const double ring_sum = bsum_d(ps, red);
+    // times the cell area, the ring's mass.  Each thread sums its cells as a
+    // compensated float pair (TwoSum, Knuth 1969), the block in FP64.
+    float sh_ = 0.f, sl_ = 0.f;
+    for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+        two_sum_add(sh_, sl_, S[row + j]);
+        sl_ += S_lo[row + j];
+    }
+    const double ring_sum = bsum_d((double)sh_ + (double)sl_, red);
     const double sigma1d = ring_sum / nz;
+    const float mh = (float)sigma1d, ml = (float)(sigma1d - (double)mh);
     // cell centres and the planet as float pairs (see potential_cell): the
     // distance loses nothing to cancellation near the planet
     const float pxh = (float)px, pxl = (float)(px - (double)pxh);
     const float pyh = (float)py, pyl = (float)(py - (double)pyh);
     const float rh = t.Rmed[i], rl = t.RmedLo[i];
     const float frsm = (float)rsm;
-    double ax = 0.0, ay = 0.0;
+    float axh = 0.f, axl = 0.f, ayh = 0.f, ayl = 0.f;
     for (int j = threadIdx.x; j < nz; j += blockDim.x) {
         const float ch = t.cosHi[j], cl = t.cosLo[j], sh = t.sinHi[j], sl = t.sinLo[j];
         const float xh = rh * ch, yh = rh * sh;
@@ -239,14 +244,14 @@ __global__ void f_disk_force(GeoF g, TablesF t, PhysF ph, double px, double py, 
                 fk = -(3.f * q * q * q * q - 4.f * q * q * q);
             }
         }
-        // the ring mean is subtracted in FP64 (CorrectDiskSelfgravity)
-        const float dsig = (float)(((double)S[row + j] + (double)S_lo[row + j]) - sigma1d);
+        // the ring mean removed (CorrectDiskSelfgravity) from the pair
+        const float dsig = (S[row + j] - mh) + (S_lo[row + j] - ml);
         const float w = dsig * (rinv * rinv * rinv * fk);
-        ax += (double)(w * dx);
-        ay += (double)(w * dy);
+        two_sum_add(axh, axl, w * dx);
+        two_sum_add(ayh, ayl, w * dy);
     }
-    ax = bsum_d(ax, red);
-    ay = bsum_d(ay, red);
+    const double ax = bsum_d((double)axh + (double)axl, red);
+    const double ay = bsum_d((double)ayh + (double)ayl, red);
     if (threadIdx.x == 0) {
         const double f = t.Surf_d[i] * ph.G_d;
         const bool inner = t.Rmed_d[i] < pa;
