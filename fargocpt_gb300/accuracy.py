@@ -19,6 +19,11 @@ upload does to them; its sigma is a compensated pair and stays exact), plus
 optional relative noise of the given size on sigma (--sigma-noise).  The
 difference it grows to is the flow's own amplification of FP32-sized
 perturbations.
+
+    python -m fargocpt_gb300.accuracy --config c1 --set fast_transport=0 --no-planet ...
+
+changes parameters of both forms (--set name=value, repeatable) or drops the
+planet, to see which physics carries the difference.
 """
 from __future__ import annotations
 
@@ -40,12 +45,24 @@ def rel_linf(a, b):
 
 
 def run(config="c3", orbits=10.0, outputs=10, seed=1234, log=sys.stderr, compare="fp32",
-        sigma_noise=0.0):
+        sigma_noise=0.0, overrides=None, planet=True):
     from . import setups
     from .abi import params_from_dict
     from .engine import Engine
 
     p64, d, radii, fields, nbody = setups.build(config, seed=seed)
+    if overrides:
+        d = dict(d)
+        d.update(overrides)
+        p64 = params_from_dict(d)
+    full_bodies = nbody.bodies
+
+    def bodies_at(t):
+        b = full_bodies(t)
+        return b if planet else b[:1]
+
+    def indirect(b):
+        return nbody.indirect(b) if len(b) > 1 else (0.0, 0.0)
     nr = d["nrad"]
     rinf, rsup = radii[:nr], radii[1:nr + 1]
     rmed = 2.0 / 3.0 * (rsup ** 3 - rinf ** 3) / (rsup ** 2 - rinf ** 2)
@@ -69,8 +86,8 @@ def run(config="c3", orbits=10.0, outputs=10, seed=1234, log=sys.stderr, compare
         for k, a in start.items():
             e.set_field(k, a)
             e.set_field(k + "0", fields[k])
-        b = nbody.bodies(0.0)
-        e.set_bodies(b, *nbody.indirect(b), 0.0)
+        b = bodies_at(0.0)
+        e.set_bodies(b, *indirect(b), 0.0)
         e.init_euler(0.0)
         e.apply_boundary_condition(0.0, 0.0, False)
     e64, e32 = engines
@@ -83,23 +100,24 @@ def run(config="c3", orbits=10.0, outputs=10, seed=1234, log=sys.stderr, compare
             dt = min(e64.condition_cfl(), t_out - t)
             if t_out - t - dt < 1e-12 * t_out:
                 dt = t_out - t
-            b = nbody.bodies(t)
-            ix, iy = nbody.indirect(b)
+            b = bodies_at(t)
+            ix, iy = indirect(b)
             for e in engines:
                 e.set_bodies(b, ix, iy, 0.0)
                 e.step_euler(dt, t)
             t += dt
             steps += 1
-        b = nbody.bodies(t)
-        ix, iy = nbody.indirect(b)
+        b = bodies_at(t)
+        ix, iy = indirect(b)
         rec = {"orbits": t / (2 * math.pi), "steps": steps}
-        for name, e in (("fp64", e64), ("fp32", e32)):
-            e.set_bodies(b, ix, iy, 0.0)
-            ax, ay = e.disk_on_planet_accel(1)
-            x, y, m = b[1][0], b[1][1], b[1][2]
-            rec[f"torque_{name}"] = (x * ay - y * ax) * m
-        rec["torque_rel_err"] = abs(rec["torque_fp32"] - rec["torque_fp64"]) / max(
-            abs(rec["torque_fp64"]), 1e-300)
+        if planet:
+            for name, e in (("fp64", e64), ("fp32", e32)):
+                e.set_bodies(b, ix, iy, 0.0)
+                ax, ay = e.disk_on_planet_accel(1)
+                x, y, m = b[1][0], b[1][1], b[1][2]
+                rec[f"torque_{name}"] = (x * ay - y * ax) * m
+            rec["torque_rel_err"] = abs(rec["torque_fp32"] - rec["torque_fp64"]) / max(
+                abs(rec["torque_fp64"]), 1e-300)
         for f in ("SIGMA", "V_RADIAL", "V_AZIMUTHAL", "ENERGY"):
             a, c = e64.get_field(f), e32.get_field(f)
             if f == "ENERGY" and d["eos"] == 0:
@@ -113,7 +131,8 @@ def run(config="c3", orbits=10.0, outputs=10, seed=1234, log=sys.stderr, compare
         history.append(rec)
         print(json.dumps(rec), file=log, flush=True)
     return {"config": config, "grid": [d["nrad"], d["naz"]], "orbits": orbits,
-            "compare": compare, "sigma_noise": sigma_noise,
+            "compare": compare, "sigma_noise": sigma_noise, "overrides": overrides or {},
+            "planet": planet,
             "steps": steps, "seconds": time.time() - t0, "history": history,
             "final": history[-1]}
 
@@ -126,10 +145,18 @@ def main():
     ap.add_argument("--out", default=None)
     ap.add_argument("--compare", default="fp32", choices=["fp32", "perturbed"])
     ap.add_argument("--sigma-noise", type=float, default=0.0)
+    ap.add_argument("--set", action="append", default=[], metavar="NAME=VALUE",
+                    help="override an fgpu_params field in both forms")
+    ap.add_argument("--no-planet", action="store_true")
     a = ap.parse_args()
+    overrides = {}
+    for item in a.set:
+        name, _, value = item.partition("=")
+        overrides[name] = float(value) if "." in value or "e" in value else int(value)
     from .build import build
     build()
-    res = run(a.config, a.orbits, a.outputs, compare=a.compare, sigma_noise=a.sigma_noise)
+    res = run(a.config, a.orbits, a.outputs, compare=a.compare, sigma_noise=a.sigma_noise,
+              overrides=overrides, planet=not a.no_planet)
     text = json.dumps(res, indent=1)
     if a.out:
         with open(a.out, "w") as f:
