@@ -1213,13 +1213,16 @@ __device__ __forceinline__ void damp_ring_f(float *X, float *X0, const DampQF &d
     __syncthreads();
 }
 
+// fields q0 .. q1 - 1 of ring i (0 v_r, 1 v_phi residual, 2 sigma, 3 energy:
+// independent of one another)
 __device__ __forceinline__ void damping_ring(const GeoF &g, const DampingF &dm, float dt,
-                                             const StateF &s, int i, float *red, long long *redl)
+                                             const StateF &s, int i, float *red, long long *redl,
+                                             int q0 = 0, int q1 = 4)
 {
     const int nz = g.nz, nr = g.nr;
     float *X[4] = {s.vr, s.dv, s.sigma, s.energy};
     float *X0[4] = {s.vr0, s.dv0, s.sigma0, s.energy0};
-    for (int q = 0; q < 4; ++q) {
+    for (int q = q0; q < q1; ++q) {
         const DampQF &d = dm.q[q];
         const int size = d.vector ? nr + 1 : nr;
         float *lo = q == 2 ? s.sigma_lo : nullptr;

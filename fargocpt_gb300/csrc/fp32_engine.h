@@ -241,6 +241,7 @@ class Engine32 {
     float *tab_f = nullptr;
     double *tab_d = nullptr;
     float *tab_c = nullptr;  // cosHi, cosLo, sinHi, sinLo
+    int nsm = 1;             // streaming multiprocessors of the device
     float *damp_mem = nullptr, *damp_aux = nullptr;
     int *damp_rings = nullptr;
     int n_rings = 0;

@@ -179,7 +179,8 @@ __global__ void f_damping(GeoF g, DampingF dm, float dt, const int *__restrict__
 {
     __shared__ float red[33];
     __shared__ long long redl[33];
-    damping_ring(g, dm, dt, s, rings[blockIdx.x], red, redl);
+    // one block per (ring, damped field)
+    damping_ring(g, dm, dt, s, rings[blockIdx.x], red, redl, blockIdx.y, blockIdx.y + 1);
 }
 
 __global__ void f_derived_cfl(GeoF g, TablesF t, PhysF ph, int mode, const float *__restrict__ S,
@@ -648,6 +649,13 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
         CKF(cudaMalloc(&damp_rings, sizeof(int) * rings.size()));
         CKF(cudaMemcpy(damp_rings, rings.data(), sizeof(int) * rings.size(), cudaMemcpyHostToDevice));
     }
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (nsm <= 0) nsm = 1;
+    }
+
     // azimuthal kernel configuration
     per = nz <= 2048 ? 4 : (nz <= 4096 ? 8 : (nz <= 6144 ? 12 : 16));
     az_block = std::max(128, std::min(512, ((nz + per - 1) / per + 31) / 32 * 32));
@@ -904,7 +912,7 @@ int Engine32::boundary(double dt, bool final)
         if (rc) return rc;
     }
     if (final && p.damping && n_rings)
-        f_damping<<<n_rings, 256, 0, stream>>>(geo, dm, (float)dt, damp_rings, state());
+        f_damping<<<dim3(n_rings, 4), 256, 0, stream>>>(geo, dm, (float)dt, damp_rings, state());
     if (final) com_damping(dt, com_now);
     f_ghost<<<(nz + 127) / 128, 128, 0, stream>>>(geo, bc, state());
     com_boundary(com_now);
@@ -979,8 +987,13 @@ int Engine32::transport(double dt)
     };
     StateF s = state();
     {
-        const int chunk = 16;
-        dim3 grid((nz + 63) / 64, (nr + chunk - 1) / chunk);
+        // rings per thread: the longest walk that still gives every SM
+        // sixteen blocks of columns (each thread's rings are a dependent
+        // chain of loads, so short grids need short walks to hide latency)
+        const int cols = (nz + 63) / 64;
+        int chunk = 16;
+        while (chunk > 4 && (long long)cols * ((nr + chunk - 1) / chunk) < 16LL * nsm) chunk /= 2;
+        dim3 grid(cols, (nr + chunk - 1) / chunk);
         if (adi)
             f_transport_radial<5><<<grid, 64, 0, stream>>>(geo, tabs, fdt, phys.limiter_mc, chunk,
                                                            s.sigma, s.vr, s.dv, s.energy, mom[0],
@@ -1062,7 +1075,7 @@ int Engine32::step(double dt, double t)
     }
     StateF s = state();
     if (p.damping && n_rings)
-        f_damping<<<n_rings, 256, 0, stream>>>(geo, dm, (float)dt, damp_rings, s);
+        f_damping<<<dim3(n_rings, 4), 256, 0, stream>>>(geo, dm, (float)dt, damp_rings, s);
     CKL("damping");
     com_damping(dt, com_after);
     CKL("com_damping");

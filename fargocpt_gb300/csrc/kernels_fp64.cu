@@ -1108,17 +1108,17 @@ __global__ void k_damping(Geo g, Damping dm, double dt, const int *__restrict__ 
     __shared__ double red[33];
     const int nz = g.nz, nr = g.nr;
     const int i = rings[blockIdx.x];
+    // the four damped fields are independent: one block per (ring, field)
+    const int q = blockIdx.y;
     double *X[4] = {s.vr, s.vaz, s.sigma, s.energy};
     double *X0[4] = {s.vr0, s.vaz0, s.sigma0, s.energy0};
-    for (int q = 0; q < 4; ++q) {
-        const DampQ &d = dm.q[q];
-        const int size = d.vector ? nr + 1 : nr;
-        if (d.kind_in != 0 && d.active_in && i <= d.limit_in) {
-            damp_ring(X[q], X0[q], d, i, nz, 0, dt, red);
-        }
-        if (d.kind_out != 0 && d.active_out && i >= d.limit_out && i < size) {
-            damp_ring(X[q], X0[q], d, i, nz, 1, dt, red);
-        }
+    const DampQ &d = dm.q[q];
+    const int size = d.vector ? nr + 1 : nr;
+    if (d.kind_in != 0 && d.active_in && i <= d.limit_in) {
+        damp_ring(X[q], X0[q], d, i, nz, 0, dt, red);
+    }
+    if (d.kind_out != 0 && d.active_out && i >= d.limit_out && i < size) {
+        damp_ring(X[q], X0[q], d, i, nz, 1, dt, red);
     }
 }
 
@@ -1651,7 +1651,7 @@ void launch_damping(const Launch &L, const Damping &dm, double dt, const int *ri
                     const State &s)
 {
     if (nrings <= 0) return;
-    k_damping<<<nrings, 256, 0, L.stream>>>(L.g, dm, dt, rings, s);
+    k_damping<<<dim3(nrings, 4), 256, 0, L.stream>>>(L.g, dm, dt, rings, s);
 }
 
 // compute_pressure (SourceEuler.cpp:1345-1376): P alone, from sigma and c_s
