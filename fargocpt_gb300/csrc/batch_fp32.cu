@@ -219,17 +219,19 @@ __global__ void __launch_bounds__(PER <= 4 ? 384 : 512, PER <= 4 ? 2 : 1)
     }
 }
 
-// damping rings: items = (disk, ring) of every disk with damping zones
+// damping rings: items = (disk, ring) of every disk with damping zones, each
+// taken four times, once per damped field (the fields are independent)
 __global__ void b_damping(const DiskF *__restrict__ D, const StepF *__restrict__ S,
                           const int2 *__restrict__ items, int n)
 {
     __shared__ float red[33];
     __shared__ long long redl[33];
-    for (int it = blockIdx.x; it < n; it += gridDim.x) {
-        const int2 w = items[it];
+    for (int it = blockIdx.x; it < 4 * n; it += gridDim.x) {
+        const int2 w = items[it >> 2];
         if (!S[w.x].run) continue;
         const DiskF &k = D[w.x];
-        damping_ring(k.g, k.dm, S[w.x].fdt, k.s, w.y, red, redl);
+        const int q = it & 3;
+        damping_ring(k.g, k.dm, S[w.x].fdt, k.s, w.y, red, redl, q, q + 1);
     }
 }
 
@@ -514,7 +516,7 @@ static int apply_tiles(fgpu_batch *b, const fgpu_tiles &t)
             return FGPU_ERR_UNSUPPORTED;
         }
         s[nd] = (int)acc;
-        totals[k] = k == FGPU_BK_DAMPING ? b->n_damp_items : acc;
+        totals[k] = k == FGPU_BK_DAMPING ? 4LL * b->n_damp_items : acc;
     }
     CKB(cudaMemcpyAsync(b->d_tables, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice,
                         b->stream));
