@@ -172,6 +172,16 @@ def cpu_baseline(cfg_name, seconds, threads=None):
             f"({d['nrad']}x{d['naz']}) in {el:.1f} s"}
 
 
+def max_over_ranks(vals, dist, torch, device):
+    """The slowest rank's times: every rank's list of timings reduced with MAX
+    (identity without a process group)."""
+    if dist is None:
+        return list(vals)
+    tt = torch.tensor(vals, device=device, dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return [float(x) for x in tt]
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -427,10 +437,7 @@ def main():
     vals = [r64["total_ms"] if r64 else 1.0, r64["e2e_s"] if r64 else 1.0,
             r32["total_ms"] if r32 else 1.0, r32["e2e_s"] if r32 else 1.0,
             rb["ms"] if rb else 1.0, rb["e2e_s"] if rb else 1.0]
-    if dist is not None:
-        tt = torch.tensor(vals, device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        vals = [float(x) for x in tt]
+    vals = max_over_ranks(vals, dist, torch, "cuda")
     if rank != 0:
         return
     batched = None
