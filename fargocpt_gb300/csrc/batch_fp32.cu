@@ -27,6 +27,7 @@
 #include "fp32_engine.h"
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -817,6 +818,8 @@ static int check_canonical(fgpu_batch *b)
 
 extern "C" int fgpu_batch_step(fgpu_batch *b, const double *dt, const double *t)
 {
+    nvtxRangePushA("fgpu_batch_step");
+    struct Pop { ~Pop() { nvtxRangePop(); } } nvtx_pop_;
     if (!b || !dt || !t) return FGPU_ERR_BAD_ARG;
     for (int k = 0; k < b->nd; ++k) {
         if (!(dt[k] >= 0.0) || !std::isfinite(dt[k])) {
@@ -947,6 +950,8 @@ static int build_graph(fgpu_batch *b, int steps)
 
 extern "C" int fgpu_batch_run(fgpu_batch *b, int max_steps, int steps_per_graph, int *n_active)
 {
+    nvtxRangePushA("fgpu_batch_run");
+    struct Pop { ~Pop() { nvtxRangePop(); } } nvtx_pop_;
     if (!b || max_steps < 0 || steps_per_graph < 1 || steps_per_graph > 4096)
         return FGPU_ERR_BAD_ARG;
     CKB(cudaStreamSynchronize(b->stream));
