@@ -228,3 +228,44 @@ def test_engines_with_different_rings_coexist(precision):
     for e in engines:
         e.step_euler(e.condition_cfl(), 0.0)
         assert np.all(np.isfinite(e.get_field("SIGMA")))
+
+
+@pytest.mark.parametrize("nrad,naz,adiabatic", [(6, 8, False), (6, 9, True), (7, 13, False),
+                                                (12, 24, True), (9, 127, True),
+                                                (8, 8192, False)])
+def test_edge_grids_against_oracle(nrad, naz, adiabatic):
+    """The smallest grids the engine takes (6 rings incl. ghosts, 8 cells per
+    ring), odd and prime ring lengths (ring ends that do not fill a warp or a
+    block), and the longest ring (8192 cells): FP64 within 1e-10 of the
+    oracle after five CFL-limited steps with the same dt sequence,
+    FP32-mixed finite and within 1e-4 in sigma."""
+    from fargocpt_gb300.engine import Engine, grid_radii
+    from oracle.oracle_py import OracleState
+
+    params, d = make_params(nrad, naz, adiabatic=adiabatic)
+    p32, _ = make_params(nrad, naz, adiabatic=adiabatic, precision=1)
+    radii = grid_radii(d["radial_spacing"], d["rmin"], d["rmax"], d["nrad"])
+    st = initial_state(d, radii, seed=21)
+    bodies = [(0.0, 0.0, 1.0, 0.0, 0.0), (1.0, 0.05, 1e-3, 0.0, math.hypot(1.0, 0.05))]
+    runs = []
+    for cls, p in ((OracleState, params), (Engine, params), (Engine, p32)):
+        b = cls(p, radii)
+        load(b, st, bodies)
+        b.apply_boundary_condition(0.0, 0.0, False)
+        t, dts = 0.0, []
+        for _ in range(5):
+            dt = b.condition_cfl()
+            b.step_euler(dt, t)
+            t += dt
+            dts.append(dt)
+        runs.append((b, dts))
+    (o, dto), (g, dtg), (f, _) = runs
+    np.testing.assert_allclose(dtg, dto, rtol=1e-12)
+    for fld in EVOLVED:
+        ref = o.get_field(fld)
+        if not np.any(ref):
+            continue
+        err = rel_linf(g.get_field(fld), ref)
+        assert err <= TOL, f"FP64 {fld}: {err:.3e}"
+        assert np.all(np.isfinite(f.get_field(fld)))
+    assert rel_linf(f.get_field("SIGMA"), o.get_field("SIGMA")) <= 1e-4
