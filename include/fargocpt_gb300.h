@@ -465,10 +465,11 @@ typedef struct {
 
 /* params[k], radii[k]: disk k as for fgpu_create; every disk must select
  * FGPU_PRECISION_FP32_MIXED and the Euler integrator (the batched step is
- * step_Euler); StabilizeViscosity, and adiabatic disks with the viscous
- * v_radial hook or viscous accretion, are refused (FGPU_ERR_UNSUPPORTED); the
- * longest ring must fit the azimuthal transport's shared memory (naz <= 6257
- * with the energy equation, 7040 without).  1 <= n <= 1024. */
+ * step_Euler); StabilizeViscosity, the centre-of-mass composite boundary,
+ * and adiabatic disks with the viscous v_radial hook or viscous accretion,
+ * are refused (FGPU_ERR_UNSUPPORTED); the longest ring must fit the
+ * azimuthal transport's shared memory (naz <= 6257 with the energy equation,
+ * 7040 without).  1 <= n <= 1024. */
 int fgpu_batch_create(int n, const fgpu_params *params,
 		      const double *const *radii, fgpu_batch **out);
 int fgpu_batch_destroy(fgpu_batch *b);
