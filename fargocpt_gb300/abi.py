@@ -183,6 +183,7 @@ EXPORTED_SYMBOLS = [
     "fgpu_condition_cfl", "fgpu_apply_boundary_condition", "fgpu_step_euler",
     "fgpu_disk_on_planet_accel", "fgpu_total_mass", "fgpu_accrete_onto_planet",
     "fgpu_check_finite", "fgpu_init_center_of_mass_boundary", "fgpu_set_frame_centers",
+    "fgpu_correct_v_azimuthal",
     "fgpu_synchronize", "fgpu_set_phase_timing", "fgpu_phase_times", "fgpu_phase_name",
     "fgpu_disk_force_static", "fgpu_gas_kick", "fgpu_transport", "fgpu_compute_pressure",
     "fgpu_snapshot_begin", "fgpu_snapshot_wait", "fgpu_host_alloc", "fgpu_host_free",
@@ -218,6 +219,7 @@ def _declare(lib: C.CDLL) -> C.CDLL:
         "fgpu_init_center_of_mass_boundary": ([vp, C.c_double, C.c_double, C.c_int,
                                                C.c_double], C.c_int),
         "fgpu_set_frame_centers": ([vp, P(FgpuFrameCenter), P(FgpuFrameCenter)], C.c_int),
+        "fgpu_correct_v_azimuthal": ([vp, C.c_double], C.c_int),
         "fgpu_synchronize": ([vp], C.c_int),
         "fgpu_set_phase_timing": ([vp, C.c_int], C.c_int),
         "fgpu_phase_times": ([vp, dp, C.c_int, P(C.c_int), P(C.c_int)], C.c_int),

@@ -1331,6 +1331,20 @@ extern "C" int fgpu_init_center_of_mass_boundary(fgpu_engine *eng, double mass_a
     return FGPU_OK;
 }
 
+extern "C" int fgpu_correct_v_azimuthal(fgpu_engine *eng, double domega)
+{
+    if (!eng || !std::isfinite(domega)) return FGPU_ERR_BAD_ARG;
+    if (domega == 0.0) return FGPU_OK;
+    if (eng->e32) {
+        eng->err = "the FP32-mixed form runs in the fixed (non-rotating) frame";
+        return FGPU_ERR_UNSUPPORTED;
+    }
+    NvtxCall nvtx_("fgpu_correct_v_azimuthal");
+    launch_correct_vaz(launch_of(eng), domega, eng->field[FGPU_V_AZIMUTHAL]);
+    eng->cfl_valid = false;
+    return check_launch(eng);
+}
+
 extern "C" int fgpu_set_frame_centers(fgpu_engine *eng, const fgpu_frame_center now[2],
                                       const fgpu_frame_center *after)
 {

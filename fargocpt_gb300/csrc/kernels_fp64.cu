@@ -1567,6 +1567,21 @@ void launch_visc_corr(const Launch &L, const State &s)
                                                                           s.corr_phi, s.corr_r);
 }
 
+// correct_v_azimuthal, SideEuler.cpp:79-95
+__global__ void k_correct_vaz(Geo g, Tables t, double domega, double *__restrict__ vaz)
+{
+    const int nz = g.nz;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;
+    if (j < nz) vaz[CELL(i, j)] -= domega * t.Rmed[i];
+}
+
+void launch_correct_vaz(const Launch &L, double domega, double *vaz)
+{
+    k_correct_vaz<<<dim3((L.g.nz + 127) / 128, L.g.nr), 128, 0, L.stream>>>(L.g, L.t, domega,
+                                                                         vaz);
+}
+
 // The centre-of-mass composite (com_boundary.cuh) on the FP64 fields.
 void launch_com_boundary(const Launch &L, const ComSpec &c, const State &s)
 {

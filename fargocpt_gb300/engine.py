@@ -178,6 +178,12 @@ class Engine:
         a = (FgpuFrameCenter * 2)(*[FgpuFrameCenter(*c) for c in after]) if after else None
         self._check(self.lib.fgpu_set_frame_centers(self.h, n, a), "fgpu_set_frame_centers")
 
+    def correct_v_azimuthal(self, domega):
+        """correct_v_azimuthal (SideEuler.cpp:79-95), for a corotating frame
+        whose OmegaFrame changed by domega."""
+        self._check(self.lib.fgpu_correct_v_azimuthal(self.h, domega),
+                    "fgpu_correct_v_azimuthal")
+
     def check_finite(self):
         f, i, j = C.c_int(), C.c_int(), C.c_int()
         rc = self.lib.fgpu_check_finite(self.h, C.byref(f), C.byref(i), C.byref(j))

@@ -74,7 +74,8 @@ def step_leapfrog(hydro, dt: float, t: float, first, second) -> None:
 def advance(hydro, clock: RunClock, *, cfl_max_var: float,
             monitor_timestep: float, t_final: float, max_steps: int = -1,
             bodies=None, on_monitor=None, integrator: str = "euler",
-            bodies_second=None, accrete=None, frame_centers=None) -> None:
+            bodies_second=None, accrete=None, frame_centers=None,
+            corotation=None) -> None:
     """The loop of sim::run (simulation.cpp:505-558) with step_Euler or, for
     integrator "leapfrog", step_LeapFrog's gas part.
 
@@ -86,6 +87,10 @@ def advance(hydro, clock: RunClock, *, cfl_max_var: float,
     does, first in the step (simulation.cpp:150-153);
     frame_centers(clock, dt) -> (now, after), for Euler, gives the centres a
     centre-of-mass boundary reads before transport and after the N-body step;
+    corotation(clock) -> dOmega, for Euler, is the change of a corotating
+    frame's OmegaFrame in the step (handle_corotation,
+    frame_of_reference.cpp:30-60), applied to v_phi before the gas step, the
+    new OmegaFrame being the fourth item bodies(clock) returns;
     on_monitor(clock) after every step that lands on a monitor time.
     """
     while clock.time < t_final:
@@ -104,9 +109,13 @@ def advance(hydro, clock: RunClock, *, cfl_max_var: float,
         else:
             if accrete is not None:
                 accrete(clock, step_dt)
+            if corotation is not None:
+                domega = corotation(clock)
+                if domega != 0.0:
+                    hydro.correct_v_azimuthal(domega)
             if bodies is not None:
-                b, ix, iy = bodies(clock)
-                hydro.set_bodies(b, ix, iy, 0.0)
+                b, ix, iy, *omega = bodies(clock)
+                hydro.set_bodies(b, ix, iy, omega[0] if omega else 0.0)
             if frame_centers is not None:
                 hydro.set_frame_centers(*frame_centers(clock, step_dt))
             hydro.step_euler(step_dt, clock.time)

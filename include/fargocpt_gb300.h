@@ -338,6 +338,14 @@ int fgpu_init_center_of_mass_boundary(fgpu_engine *eng, double mass_all, double 
 int fgpu_set_frame_centers(fgpu_engine *eng, const fgpu_frame_center now[2],
 			   const fgpu_frame_center *after);
 
+/* correct_v_azimuthal (src/SideEuler.cpp:79-95): v_phi -= dOmega * Rmed on
+ * every ring, ghost rings included.  refframe::handle_corotation
+ * (src/frame_of_reference.cpp:30-60) calls it when the corotating frame's
+ * OmegaFrame changes by dOmega, before the gas step; the engine then takes the
+ * new OmegaFrame through fgpu_set_bodies.  The FP32-mixed form runs in the
+ * fixed frame and accepts dOmega = 0 only. */
+int fgpu_correct_v_azimuthal(fgpu_engine *eng, double domega);
+
 /* Scans the evolved fields for NaN/Inf; returns FGPU_ERR_NONFINITE and the
  * first bad (field, ring, azimuth) when one is found. */
 int fgpu_check_finite(fgpu_engine *eng, int *field, int *nr, int *naz);

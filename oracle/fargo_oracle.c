@@ -1413,6 +1413,15 @@ int or_init_center_of_mass_boundary(or_state *s, double mass_all, double mass_ce
     return FGPU_OK;
 }
 
+/* correct_v_azimuthal, src/SideEuler.cpp:79-95 */
+int or_correct_v_azimuthal(or_state *s, double domega)
+{
+    double *vaz = s->f[FGPU_V_AZIMUTHAL];
+    for (int i = 0; i < s->nr; ++i)
+	for (int j = 0; j < s->nz; ++j) vaz[(size_t)i * s->nz + j] -= domega * s->Rmed[i];
+    return FGPU_OK;
+}
+
 int or_set_frame_centers(or_state *s, const fgpu_frame_center now[2],
 			 const fgpu_frame_center *after)
 {

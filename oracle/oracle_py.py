@@ -56,6 +56,7 @@ def _load():
     lib.or_accrete_onto_planet.argtypes = [vp, C.POINTER(FgpuAccretor), C.c_double, dp]
     lib.or_init_center_of_mass_boundary.argtypes = [vp, C.c_double, C.c_double, C.c_int,
                                                     C.c_double]
+    lib.or_correct_v_azimuthal.argtypes = [vp, C.c_double]
     lib.or_set_frame_centers.argtypes = [vp, C.POINTER(FgpuFrameCenter),
                                          C.POINTER(FgpuFrameCenter)]
     for name in ("or_calculate_potential", "or_viscous_stress_tensor"):
@@ -168,6 +169,9 @@ class OracleState:
                                                       int(binary_on_primary), com_max_dist)
         if rc != 0:
             raise ValueError(rc)
+
+    def correct_v_azimuthal(self, domega):
+        self.lib.or_correct_v_azimuthal(self.h, domega)
 
     def set_frame_centers(self, now, after=None):
         n = (FgpuFrameCenter * 2)(*[FgpuFrameCenter(*c) for c in now])

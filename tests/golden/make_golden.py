@@ -285,6 +285,21 @@ CASES = {
                   Damping="yes", DampingInnerLimit=1.1, DampingOuterLimit=0.9,
                   MonitorTimestep=0.002, Nsnapshots=20),
         nrad=20, naz=48, rmin=0.4, rmax=2.5, planet=1e-3, keep=[1, 2, 5, 10, 20]),
+    # corotating frame (refframe::handle_corotation): OmegaFrame follows the
+    # planet, v_phi corrected by its change every step; locally isothermal,
+    # fixed dt, damping, outflow / reference edges
+    "iso_planet_corotating": dict(
+        keys=dict(SigmaSlope=0.5, AspectRatio=0.05, FlaringIndex=0.0,
+                  EquationOfState="Isothermal", ViscousAlpha=1e-3,
+                  ArtificialViscosity="SN", Transport="FARGO", Frame="Corotating",
+                  InnerBoundary="outflow", OuterBoundary="reference",
+                  Damping="yes", DampingInnerLimit=1.1, DampingOuterLimit=0.9,
+                  DampingSurfaceDensityInner="Reference",
+                  DampingSurfaceDensityOuter="Reference",
+                  DampingVRadialInner="Reference", DampingVRadialOuter="Reference",
+                  DampingVAzimuthalInner="Reference", DampingVAzimuthalOuter="Reference",
+                  MonitorTimestep=0.002, Nsnapshots=20),
+        nrad=20, naz=48, rmin=0.4, rmax=2.5, planet=1e-3, keep=[1, 2, 5, 10, 20]),
     # the same with the Keplerian model (InitializePureKeplerian): adiabatic,
     # star only, CFL-limited, energy damping
     "adi_star_cfl_bc_com_keplerian": dict(
@@ -481,7 +496,7 @@ def read_nbody(out, k):
     # mass, time, omega_frame, ..., torque (18), accretion torque (19),
     # indirect torque (20), accretion rate (21)
     return dict(x=a[:, 2], y=a[:, 3], vx=a[:, 4], vy=a[:, 5], mass=a[:, 6], time=a[:, 7],
-                torque=a[:, 18], accretion_rate=a[:, 21])
+                omega_frame=a[:, 8], torque=a[:, 18], accretion_rate=a[:, 21])
 
 
 def make_case(name, case, seed):
@@ -519,6 +534,8 @@ def make_case(name, case, seed):
                     monitor_timestep=float(case["keys"]["MonitorTimestep"]),
                     nsnapshots=int(case["keys"]["Nsnapshots"]), nbodies=nb,
                     seed=seed, reference_log_tail=r.stdout.splitlines()[-1])
+        if str(case["keys"].get("Frame", COMMON["Frame"])).lower().startswith("c"):
+            meta["corotating"] = True
         if case.get("planet_keys"):
             pk = case["planet_keys"]
             meta["accretion"] = dict(type=ACCRETION[pk["accretion method"]],

@@ -23,7 +23,7 @@ CASES = ["iso_planet_fixed_dt", "adi_planet_fixed_dt", "iso_star_cfl",
          "iso_planet_accretion_kley", "adi_planet_accretion_sinkhole",
          "iso_planet_accretion_viscous", "iso_planet_bc_individual",
          "adi_star_cfl_bc_individual", "iso_planet_bc_com", "adi_star_cfl_bc_com_keplerian",
-         "adi_planet_bc_com"]
+         "adi_planet_bc_com", "iso_planet_corotating"]
 EVOLVED = ["SIGMA", "V_RADIAL", "V_AZIMUTHAL", "ENERGY"]
 
 
@@ -111,8 +111,12 @@ def replay(make_backend, name, params_override=None, accreted=None):
     for f in EVOLVED:
         hyd.set_field(f, arrays[f"s0_{f}"])
         hyd.set_field(f + "0", arrays[f"s0_{f}"])
+    # corotating frame: OmegaFrame of the monitor rows (the value the step
+    # that ends at a row used), v_phi corrected by its changes
+    corot = bool(meta.get("corotating"))
+    omega = arrays["body0_omega_frame"] if corot else None
     b, ix, iy = body_state(0)
-    hyd.set_bodies(b, ix, iy, 0.0)
+    hyd.set_bodies(b, ix, iy, float(omega[0]) if corot else 0.0)
     # init_euler runs before the velocities are initialised in FargoCPT
     # (init.cpp:326-332): the heating/cooling rates the first CFL reads are
     # computed with v = 0.
@@ -158,9 +162,18 @@ def replay(make_backend, name, params_override=None, accreted=None):
             if accreted is not None:
                 accreted[c.n_monitor + 1] = accreted.get(c.n_monitor + 1, 0.0) + dm
 
+    def step_bodies(c):
+        b, ix, iy = body_state(c.n_monitor)
+        return (b, ix, iy, float(omega[c.n_monitor + 1])) if corot else (b, ix, iy)
+
+    corotation = None
+    if corot:
+        def corotation(c):
+            return float(omega[c.n_monitor + 1]) - float(omega[c.n_monitor])
+
     t_final = meta["nsnapshots"] * 1 * meta["monitor_timestep"]
     advance(hyd, clock, cfl_max_var=cmv, monitor_timestep=meta["monitor_timestep"],
-            t_final=t_final, bodies=lambda c: body_state(c.n_monitor),
+            t_final=t_final, bodies=step_bodies, corotation=corotation,
             on_monitor=on_monitor,
             integrator="leapfrog" if int(pd.get("integrator", 0)) == 1 else "euler",
             accrete=accrete, frame_centers=frame_centers)

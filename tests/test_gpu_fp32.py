@@ -28,7 +28,13 @@ def rel_l1(a, b):
     return float(np.sum(np.abs(a - b)) / np.sum(np.abs(b)))
 
 
-@pytest.mark.parametrize("name", CASES)
+def _fixed_frame(name):
+    # the FP32-mixed form runs in the fixed frame
+    from golden_runner import load_case
+    return not load_case(name)[0].get("corotating")
+
+
+@pytest.mark.parametrize("name", [c for c in CASES if _fixed_frame(c)])
 def test_fp32_mixed_against_reference_snapshots(name):
     snaps, times, torques, dts, arrays = replay(_engine(), name, {"precision": 1})
     assert snaps
