@@ -1163,11 +1163,11 @@ extern "C" int fgpu_set_bodies(fgpu_engine *eng, int n, const fgpu_body *bodies,
     b.iy = iy;
     b.omega_frame = omega_frame;
     if (eng->e32) {
-        if (omega_frame != 0.0) {
-            eng->err = "the FP32-mixed form runs in the fixed (non-rotating) frame";
+        if (omega_frame != 0.0 && eng->batch_owned) {
+            eng->err = "the batched form runs in the fixed (non-rotating) frame";
             return FGPU_ERR_UNSUPPORTED;
         }
-        eng->e32->set_bodies(n, bodies, ix, iy);
+        eng->e32->set_bodies(n, bodies, ix, iy, omega_frame);
     }
     return FGPU_OK;
 }
@@ -1336,8 +1336,12 @@ extern "C" int fgpu_correct_v_azimuthal(fgpu_engine *eng, double domega)
     if (!eng || !std::isfinite(domega)) return FGPU_ERR_BAD_ARG;
     if (domega == 0.0) return FGPU_OK;
     if (eng->e32) {
-        eng->err = "the FP32-mixed form runs in the fixed (non-rotating) frame";
-        return FGPU_ERR_UNSUPPORTED;
+        if (eng->batch_owned) {
+            eng->err = "the batched form runs in the fixed (non-rotating) frame";
+            return FGPU_ERR_UNSUPPORTED;
+        }
+        eng->e32->correct_v_azimuthal(domega);
+        return FGPU_OK;
     }
     NvtxCall nvtx_("fgpu_correct_v_azimuthal");
     launch_correct_vaz(launch_of(eng), domega, eng->field[FGPU_V_AZIMUTHAL]);

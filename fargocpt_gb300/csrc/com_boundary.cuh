@@ -121,19 +121,20 @@ struct ComFields64 {
 };
 
 // FP32-mixed fields: sigma as a compensated pair, v_phi as the residual about
-// the ring's Keplerian speed
+// the ring's inertial Keplerian speed (frame v_phi = vref + dv - rmed omega)
 struct ComFields32 {
     float *sigma, *sigma_lo, *vr, *dv, *energy;
-    const double *vref;
+    const double *vref, *rmed;
+    double omega;
     __device__ double get_vr(int nz, int i, int j) const { return (double)vr[(size_t)i * nz + j]; }
     __device__ void set_vr(int nz, int i, int j, double v) const { vr[(size_t)i * nz + j] = (float)v; }
     __device__ double get_vaz(int nz, int i, int j) const
     {
-        return vref[i] + (double)dv[(size_t)i * nz + j];
+        return vref[i] - rmed[i] * omega + (double)dv[(size_t)i * nz + j];
     }
     __device__ void set_vaz(int nz, int i, int j, double v) const
     {
-        dv[(size_t)i * nz + j] = (float)(v - vref[i]);
+        dv[(size_t)i * nz + j] = (float)(v - (vref[i] - rmed[i] * omega));
     }
     __device__ double get_energy(int nz, int i, int j) const
     {

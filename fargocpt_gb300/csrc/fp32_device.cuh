@@ -281,8 +281,12 @@ __device__ __forceinline__ void source_cell(const GeoF &g, const TablesF &t, flo
                             t.InvDiffRmed[i];
         const float gradphi = (pot[CELL(i, j)] - pot[CELL(i - 1, j)]) * t.InvDiffRmed[i];
         const int jn = jnext(j, nz);
-        const float d = 0.25f * (dv_in[CELL(i, j)] + dv_in[CELL(i, jn)] + dv_in[CELL(i - 1, j)] +
-                                 dv_in[CELL(i - 1, jn)]);
+        float d = 0.25f * (dv_in[CELL(i, j)] + dv_in[CELL(i, jn)] + dv_in[CELL(i - 1, j)] +
+                           dv_in[CELL(i - 1, jn)]);
+        // in a rotating frame the reference's vt (frame velocities averaged,
+        // plus Rinf OmegaFrame; SourceEuler.cpp:355-364) is the inertial mean
+        // plus OmegaFrame (Rinf - the mean of the two Rmed)
+        if (g.omega_frame != 0.0) d += (float)g.omega_frame * t.RinfOff[i];
         // vt^2 / r - dPhi_K/dr = Kbal + (2 A d + d^2) / Rinf
         const float centri = t.Kbal[i] + (2.f * t.Aface[i] + d) * d * t.InvRinf[i];
         vr += dt * (-gradp - gradphi + centri);
@@ -1053,7 +1057,9 @@ __device__ __forceinline__ void azimuthal_ring(const GeoF &g, const TablesF &t, 
     for (int n = 0; n < PER; ++n)
         if (tid + n * bs < nz) part += to_fixed(vown[n], ks);
     const double mean_dv = exact_sum_result(part, ks, redl) / (double)nz;
-    const double vmean = t.Vref_d[i] + mean_dv;
+    // the ring's mean frame velocity (the residual is about the inertial
+    // Keplerian speed)
+    const double vmean = (t.Vref_d[i] - t.Rmed_d[i] * g.omega_frame) + mean_dv;
     const double Ntilde = vmean * t.InvRmed_d[i] * dt * g.invdphi_d;
     const double Nround = floor(Ntilde + 0.5);
     const int nshift = (int)Nround;
@@ -1297,7 +1303,9 @@ __device__ __forceinline__ void derived_cfl_ring(
         }
         if (cfl_ring) {
             const float d0 = dv[c];
-            const float vres = ph.fast_transport ? d0 - md0 : t.Vref[i] + d0;
+            const float vres = ph.fast_transport
+                                   ? d0 - md0
+                                   : (float)(t.Vref_d[i] - t.Rmed_d[i] * g.omega_frame) + d0;
             const float invdt1 = c_s * t.InvCell[i];
             const float invdt2 = vr[c] * t.InvDiffRsup[i];
             const float invdt3 = vres * t.InvDxTheta[i];

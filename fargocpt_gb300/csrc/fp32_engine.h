@@ -25,6 +25,9 @@ struct GeoF {
     int nr, nz;
     float dphi, invdphi;
     double dphi_d, invdphi_d;
+    // OmegaFrame: the stored v_phi residual is about the inertial Keplerian
+    // speed, so the frame enters only where frame velocities are asked for
+    double omega_frame;
 };
 
 // Per-ring tables in FP32, plus the FP64 values the FP64 islands need.
@@ -53,6 +56,10 @@ struct TablesF {
     // cell centres as float pairs: Rmed = Rmed + RmedLo, cos (j dphi) =
     // cosHi + cosLo, sin likewise
     const float *RmedLo, *cosHi, *cosLo, *sinHi, *sinLo;
+    // Rinf - (Rmed(i) + Rmed(i-1)) / 2: the reference's interface azimuthal
+    // speed, the mean of four frame velocities plus Rinf OmegaFrame, exceeds
+    // the mean inertial speed by OmegaFrame times it
+    const float *RinfOff;
 };
 
 struct PhysF {
@@ -174,7 +181,9 @@ class Engine32 {
     int upload(int field, const double *host, int rows);
     int download(int field, double *host, int rows);
     int to_fp64(int field, double *dst, int rows);
-    void set_bodies(int n, const fgpu_body *b, double ix, double iy);
+    void set_bodies(int n, const fgpu_body *b, double ix, double iy, double omega_frame = 0.0);
+    // correct_v_azimuthal: the frame velocities less dOmega * Rmed
+    void correct_v_azimuthal(double domega) { pend_dv -= domega; }
     int init_euler(double t);
     int derived_cfl(int mode);
     int cfl(double *dt_out);
@@ -222,6 +231,13 @@ class Engine32 {
     double beta_inv(double t) const;
     const double *offset_of(int f) const;
     StateF state();
+    // applies the pending frame shifts of v_phi and its reference values
+    int sync_frame();
+    double pend_dv = 0.0, pend_dv0 = 0.0;  // shifts, per unit radius
+    double *vaz_offset = nullptr;          // per ring: Vref - Rmed OmegaFrame
+    std::vector<double> host_rmed, host_vref;
+    double zg_in_base = 0.0, zg_out_base = 0.0;
+    float *zero_vphi_tab = nullptr;        // damping target of v_phi -> 0 (frame)
 
     fgpu_params p{};
     cudaStream_t stream = nullptr;

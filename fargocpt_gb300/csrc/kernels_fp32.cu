@@ -360,7 +360,7 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
            INVRINF, RINFSQ, TWOOVER, OMEGAK, INVOMEGAK, CSISO, INVDXSRC, INVDXTHETA, EMODEL,
            HFACADI, INVCELL, INVCELL2, TWOOVERRMEDSUM, KBAL, AFACE, SHEAR, DJ, JSLOPE, DRMED,
            OMREFDIFF, VREF, DRSUP, RSUPIDRR, LSQTW, TWOOVERDRMED2, RA3IDRMED, F43, CRPP1,
-           CRPP2, CRRR1, CRRR2, CRRP, CRSCALE, RMEDLO, NT };
+           CRPP2, CRRR1, CRRR2, CRRP, CRSCALE, RMEDLO, RINFOFF, NT };
     std::vector<float> hf((size_t)NT * R, 0.f);
     auto F = [&](int k) { return hf.data() + (size_t)k * R; };
     for (int n = 0; n <= nr; ++n) {
@@ -384,6 +384,7 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
         F(RSUP)[n] = (float)Rsup[n];
         F(RMED)[n] = (float)rm;
         F(RMEDLO)[n] = (float)(rm - (double)(float)rm);
+        if (n >= 1) F(RINFOFF)[n] = (float)(Rinf[n] - 0.5 * (Rmed[n] + Rmed[n - 1]));
         F(SURF)[n] = (float)Surf[n];
         F(INVRMED)[n] = (float)(1.0 / rm);
         F(INVSURF)[n] = (float)(1.0 / Surf[n]);
@@ -478,6 +479,7 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
     t.Rmed_d = tab_d; t.InvRmed_d = tab_d + R; t.Vref_d = tab_d + 2 * R; t.Surf_d = tab_d + 3 * R;
     t.PhiK_d = tab_d + 4 * R; t.cos_d = tab_d + 5 * R; t.sin_d = tab_d + 5 * R + nz;
     t.RmedLo = Df(RMEDLO);
+    t.RinfOff = Df(RINFOFF);
     t.cosHi = tab_c; t.cosLo = tab_c + nz; t.sinHi = tab_c + 2 * nz; t.sinLo = tab_c + 3 * nz;
 
     // physics
@@ -559,8 +561,12 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
     bc.kep_in = (float)(p.vaz_inner_keplerian_factor * std::sqrt(G * M / Rmed[0]) - Vref[0]);
     bc.kep_out = (float)(p.vaz_outer_keplerian_factor * std::sqrt(G * M / Rmed[nr - 1]) -
                          Vref[nr - 1]);
-    bc.zg_in = (float)(Vref[1] - Vref[0]);
-    bc.zg_out = (float)(Vref[nr - 2] - Vref[nr - 1]);
+    zg_in_base = Vref[1] - Vref[0];
+    zg_out_base = Vref[nr - 2] - Vref[nr - 1];
+    bc.zg_in = (float)zg_in_base;
+    bc.zg_out = (float)zg_out_base;
+    CKF(cudaMalloc(&vaz_offset, sizeof(double) * nr));
+    CKF(cudaMemcpy(vaz_offset, Vref.data(), sizeof(double) * nr, cudaMemcpyHostToDevice));
     bc.nu = fld[FGPU_VISCOSITY];
     visc_recompute = p.eos == FGPU_EOS_IDEAL &&
                      (p.viscous_accretion || p.bc_vrad_inner == FGPU_BC_VISCOUS);
@@ -607,10 +613,13 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
                                   (p.rmax - p.rmax * p.damping_outer_limit), 2);
         }
     }
-    for (int n = 0; n <= nr; ++n) dzero[n] = (float)(-Vref[n]);  // v_phi -> 0
+    for (int n = 0; n <= nr; ++n) dzero[n] = (float)(-Vref[n]);  // v_phi -> 0 (fixed frame)
+    host_rmed.assign(Rmed.begin(), Rmed.begin() + nr + 1);
+    host_vref.assign(Vref.begin(), Vref.begin() + nr + 1);
     CKF(cudaMalloc(&damp_mem, sizeof(float) * (dfac.size() + dzero.size() + 2)));
     CKF(cudaMemcpy(damp_mem, dfac.data(), sizeof(float) * dfac.size(), cudaMemcpyHostToDevice));
     float *zero_vphi = damp_mem + dfac.size();
+    zero_vphi_tab = zero_vphi;
     CKF(cudaMemcpy(zero_vphi, dzero.data(), sizeof(float) * dzero.size(), cudaMemcpyHostToDevice));
     // a zero table for the other quantities and the sigma floor of "zero" damping
     std::vector<float> zf((size_t)(nr + 1), 0.f), sf((size_t)(nr + 1), (float)(p.sigma_floor * p.sigma0));
@@ -704,7 +713,7 @@ void Engine32::destroy()
     for (int k = 0; k < 4; ++k) cudaFree(mom[k]);
     cudaFree(partial); cudaFree(red_out); cudaFree(d_dtmin); cudaFree(d_bad); cudaFree(stage);
     cudaFree(corr_phi); cudaFree(corr_r);
-    cudaFree(tab_f); cudaFree(tab_d); cudaFree(tab_c); cudaFree(damp_mem); cudaFree(damp_aux); cudaFree(damp_rings);
+    cudaFree(tab_f); cudaFree(tab_d); cudaFree(tab_c); cudaFree(vaz_offset); cudaFree(damp_mem); cudaFree(damp_aux); cudaFree(damp_rings);
     if (h_pinned) cudaFreeHost(h_pinned);
 }
 
@@ -756,13 +765,14 @@ DiskF Engine32::describe()
 // rows of a field and the ring offset between stored and FargoCPT values
 const double *Engine32::offset_of(int f) const
 {
-    if (f == FGPU_V_AZIMUTHAL || f == FGPU_V_AZIMUTHAL0) return tabs.Vref_d;
+    if (f == FGPU_V_AZIMUTHAL || f == FGPU_V_AZIMUTHAL0) return vaz_offset;
     if (f == FGPU_POTENTIAL) return tabs.PhiK_d;
     return nullptr;
 }
 
 int Engine32::upload(int f, const double *host, int rows)
 {
+    if (int rc_ = sync_frame()) return rc_;
     const size_t n = (size_t)rows * nz;
     CKF(cudaMemcpyAsync(stage, host, n * sizeof(double), cudaMemcpyHostToDevice, stream));
     if (f == FGPU_SIGMA)
@@ -778,6 +788,7 @@ int Engine32::upload(int f, const double *host, int rows)
 // FargoCPT's FP64 values of field f into the device buffer dst, in stream order
 int Engine32::to_fp64(int f, double *dst, int rows)
 {
+    if (int rc_ = sync_frame()) return rc_;
     const size_t n = (size_t)rows * nz;
     if (f == FGPU_SIGMA)
         f_join_f64<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(fld[f], sigma_lo, dst, n);
@@ -789,6 +800,7 @@ int Engine32::to_fp64(int f, double *dst, int rows)
 
 int Engine32::download(int f, double *host, int rows)
 {
+    if (int rc_ = sync_frame()) return rc_;
     const size_t n = (size_t)rows * nz;
     int rc = to_fp64(f, stage, rows);
     if (rc) return rc;
@@ -797,8 +809,50 @@ int Engine32::download(int f, double *host, int rows)
     return FGPU_OK;
 }
 
-void Engine32::set_bodies(int n, const fgpu_body *b, double ix, double iy)
+// v_phi += Rmed s on every ring (the frame velocities kept when OmegaFrame
+// changes, or shifted by correct_v_azimuthal)
+__global__ void f_shift_vaz(GeoF g, const double *__restrict__ rmed, double s_dv, double s_dv0,
+                            float *__restrict__ dv, float *__restrict__ dv0)
 {
+    const int nz = g.nz;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;
+    if (j >= nz) return;
+    if (s_dv != 0.0) dv[CELL(i, j)] += (float)(rmed[i] * s_dv);
+    if (s_dv0 != 0.0) dv0[CELL(i, j)] += (float)(rmed[i] * s_dv0);
+}
+
+int Engine32::sync_frame()
+{
+    if (pend_dv == 0.0 && pend_dv0 == 0.0) return FGPU_OK;
+    f_shift_vaz<<<dim3((nz + 127) / 128, nr), 128, 0, stream>>>(
+        geo, tabs.Rmed_d, pend_dv, pend_dv0, fld[FGPU_V_AZIMUTHAL], fld[FGPU_V_AZIMUTHAL0]);
+    pend_dv = pend_dv0 = 0.0;
+    CKF(cudaGetLastError());
+    return FGPU_OK;
+}
+
+void Engine32::set_bodies(int n, const fgpu_body *b, double ix, double iy, double omega_frame)
+{
+    if (omega_frame != geo.omega_frame) {
+        // FargoCPT keeps the frame velocities when OmegaFrame changes: the
+        // residuals about the inertial Keplerian speed move by Rmed dOmega
+        const double d = omega_frame - geo.omega_frame;
+        pend_dv += d;
+        pend_dv0 += d;
+        geo.omega_frame = omega_frame;
+        bc.zg_in = (float)(zg_in_base - omega_frame * (host_rmed[1] - host_rmed[0]));
+        bc.zg_out = (float)(zg_out_base - omega_frame * (host_rmed[nr - 2] - host_rmed[nr - 1]));
+        std::vector<double> off(nr);
+        std::vector<float> z(nr + 1);
+        for (int k = 0; k < nr; ++k) off[k] = host_vref[k] - host_rmed[k] * omega_frame;
+        for (int k = 0; k <= nr; ++k) z[k] = (float)(host_rmed[k] * omega_frame - host_vref[k]);
+        cudaMemcpyAsync(vaz_offset, off.data(), sizeof(double) * nr, cudaMemcpyHostToDevice,
+                        stream);
+        cudaMemcpyAsync(zero_vphi_tab, z.data(), sizeof(float) * (nr + 1),
+                        cudaMemcpyHostToDevice, stream);
+        cudaStreamSynchronize(stream);
+    }
     bodies.n = n;
     bodies.star_at_origin = n > 0 && b[0].x == 0.0 && b[0].y == 0.0 &&
                             b[0].mass == p.hydro_center_mass && b[0].r_sm == 0.0;
@@ -819,6 +873,7 @@ static dim3 grid2(int nz, int rows) { return dim3((nz + 127) / 128, rows); }
 
 int Engine32::derived_cfl(int mode)
 {
+    if (int rc_ = sync_frame()) return rc_;
     StateF s = state();
     if (mode & 4) CKF(cudaMemsetAsync(d_dtmin, 0x7f, sizeof(unsigned int), stream));
     f_derived_cfl<<<nr, 256, 0, stream>>>(geo, tabs, phys, mode, s.sigma, s.energy, s.vr, s.dv,
@@ -840,6 +895,7 @@ void Engine32::visc_corr(const StateF &s)
 
 int Engine32::init_euler(double t)
 {
+    if (int rc_ = sync_frame()) return rc_;
     int rc = derived_cfl(1 | 2);
     if (rc) return rc;
     if (phys.adiabatic) {
@@ -887,8 +943,10 @@ void Engine32::com_boundary(const ComCenter *c)
     ComSpec cs = com;
     cs.c[0] = c[0];
     cs.c[1] = c[1];
+    cs.omf = geo.omega_frame;
     StateF s = state();
-    const ComFields32 f{s.sigma, s.sigma_lo, s.vr, s.dv, s.energy, tabs.Vref_d};
+    const ComFields32 f{s.sigma, s.sigma_lo, s.vr, s.dv, s.energy, tabs.Vref_d, tabs.Rmed_d,
+                        geo.omega_frame};
     k_com_boundary<<<dim3((nz + 127) / 128, 2), 128, 0, stream>>>(cs, nz, nr, f);
 }
 
@@ -898,13 +956,16 @@ void Engine32::com_damping(double dt, const ComCenter *c)
     ComSpec cs = com;
     cs.c[0] = c[0];
     cs.c[1] = c[1];
+    cs.omf = geo.omega_frame;
     StateF s = state();
-    const ComFields32 f{s.sigma, s.sigma_lo, s.vr, s.dv, s.energy, tabs.Vref_d};
+    const ComFields32 f{s.sigma, s.sigma_lo, s.vr, s.dv, s.energy, tabs.Vref_d, tabs.Rmed_d,
+                        geo.omega_frame};
     launch_com_damping_sides(cs, nz, dt, f, stream);
 }
 
 int Engine32::boundary(double dt, bool final)
 {
+    if (int rc_ = sync_frame()) return rc_;
     if (final && visc_recompute) {
         // c_s, H, nu of the transported state before the final hooks
         // (simulation.cpp:232-242, 432-441)
@@ -926,6 +987,7 @@ int Engine32::boundary(double dt, bool final)
 // updated velocities in the step's buffers.
 int Engine32::kick(double dt, double t)
 {
+    if (int rc_ = sync_frame()) return rc_;
     const float fdt = (float)dt;
     const bool adi = phys.adiabatic;
     auto mark = [&](int k) {
@@ -980,6 +1042,7 @@ int Engine32::kick(double dt, double t)
 // velocities from momenta and floors.
 int Engine32::transport(double dt)
 {
+    if (int rc_ = sync_frame()) return rc_;
     const float fdt = (float)dt;
     const bool adi = phys.adiabatic;
     auto mark = [&](int k) {
@@ -1126,8 +1189,9 @@ __global__ void f_accrete(GeoF g, TablesF t, PhysF ph, AccrF a, float *__restric
         const double xc = rm * t.cos_d[jf], yc = rm * t.sin_d[jf];
         const double dx = a.x - xc, dy = a.y - yc;
         const double distance = sqrt(dx * dx + dy * dy);
-        const double vtcell = t.Vref_d[i] + 0.5 * ((double)dv[l] + (double)dv[CELL(i, jnext(jf, nz))]) +
-                              rm * a.omf;
+        // the stored residual is about the inertial Keplerian speed, so this
+        // is the inertial v_phi the reference forms as v_phi + Rmed OmegaFrame
+        const double vtcell = t.Vref_d[i] + 0.5 * ((double)dv[l] + (double)dv[CELL(i, jnext(jf, nz))]);
         const double vrcell = 0.5 * ((double)vr[l] + (double)vr[l + nz]);
         const double vxcell = (vrcell * xc - vtcell * yc) / rm;
         const double vycell = (vrcell * yc + vtcell * xc) / rm;
@@ -1184,6 +1248,7 @@ __global__ void f_accrete(GeoF g, TablesF t, PhysF ph, AccrF a, float *__restric
 
 int Engine32::accrete(const AccrF &a, double out[3])
 {
+    if (int rc_ = sync_frame()) return rc_;
     StateF s = state();
     f_accrete<<<1, 512, 0, stream>>>(geo, tabs, phys, a, s.sigma, s.sigma_lo, s.energy, s.vr,
                                      s.dv, fld[FGPU_VISCOSITY], red_out);

@@ -342,8 +342,8 @@ int fgpu_set_frame_centers(fgpu_engine *eng, const fgpu_frame_center now[2],
  * every ring, ghost rings included.  refframe::handle_corotation
  * (src/frame_of_reference.cpp:30-60) calls it when the corotating frame's
  * OmegaFrame changes by dOmega, before the gas step; the engine then takes the
- * new OmegaFrame through fgpu_set_bodies.  The FP32-mixed form runs in the
- * fixed frame and accepts dOmega = 0 only. */
+ * new OmegaFrame through fgpu_set_bodies.  Not for the disks of a batch
+ * (fixed frame). */
 int fgpu_correct_v_azimuthal(fgpu_engine *eng, double domega);
 
 /* Scans the evolved fields for NaN/Inf; returns FGPU_ERR_NONFINITE and the

@@ -28,13 +28,7 @@ def rel_l1(a, b):
     return float(np.sum(np.abs(a - b)) / np.sum(np.abs(b)))
 
 
-def _fixed_frame(name):
-    # the FP32-mixed form runs in the fixed frame
-    from golden_runner import load_case
-    return not load_case(name)[0].get("corotating")
-
-
-@pytest.mark.parametrize("name", [c for c in CASES if _fixed_frame(c)])
+@pytest.mark.parametrize("name", CASES)
 def test_fp32_mixed_against_reference_snapshots(name):
     snaps, times, torques, dts, arrays = replay(_engine(), name, {"precision": 1})
     assert snaps
@@ -178,3 +172,37 @@ def test_fp32_disk_force_against_fp64_form(where):
     (a64, m64), (a32, m32) = out
     assert np.linalg.norm(a32 - a64) <= 1e-6 * np.linalg.norm(a64)
     assert abs(m32 - m64) <= 1e-12 * m64
+
+
+def test_fp32_rotating_frame_against_fp64_form():
+    """A rotating frame (OmegaFrame 0.25) with a change of OmegaFrame and the
+    v_phi correction of handle_corotation half way, on a 48 x 128 adiabatic
+    disk with a planet: the FP32-mixed form within 1e-5 of the FP64 form in
+    sigma and in the frame's v_phi."""
+    from fargocpt_gb300.engine import Engine, grid_radii
+    from gpu_cases import initial_state, load, make_params
+
+    p64, d = make_params(48, 128, adiabatic=True)
+    p32, _ = make_params(48, 128, adiabatic=True, precision=1)
+    radii = grid_radii(d["radial_spacing"], d["rmin"], d["rmax"], d["nrad"])
+    st = initial_state(d, radii, seed=13)
+    bodies = [(0.0, 0.0, 1.0, 0.0, 0.0), (1.0, 0.05, 1e-3, 0.0, math.hypot(1.0, 0.05))]
+    engs = [Engine(p64, radii), Engine(p32, radii)]
+    for e in engs:
+        load(e, st, bodies)
+        e.set_bodies(bodies, 0.0, 0.0, 0.25)
+        e.apply_boundary_condition(0.0, 0.0, False)
+    t, omega = 0.0, 0.25
+    for n in range(8):
+        if n == 4:
+            for e in engs:
+                e.correct_v_azimuthal(0.01)
+            omega += 0.01
+        dt = engs[0].condition_cfl()
+        for e in engs:
+            e.set_bodies(bodies, 0.0, 0.0, omega)
+            e.step_euler(dt, t)
+        t += dt
+    assert rel_linf(engs[1].get_field("SIGMA"), engs[0].get_field("SIGMA")) <= 1e-5
+    assert rel_linf(engs[1].get_field("V_AZIMUTHAL"), engs[0].get_field("V_AZIMUTHAL")) <= 1e-5
+
