@@ -103,6 +103,13 @@ ACCRETION = {"kley": 0, "viscous": 1, "sinkhole": 2}
 COMPOSITE = {"individual": 0, "centerofmass": 1}
 
 
+class FgpuCflCell(C.Structure):
+    """fgpu_cfl_cell: the cell that limits the CFL step (cfl.cpp:38-182)."""
+    _fields_ = [("ring", C.c_int), ("azimuth", C.c_int), ("shear_ring", C.c_int),
+                ("reserved", C.c_int), ("dt_cell", C.c_double), ("invdt", C.c_double * 6),
+                ("dt_shear", C.c_double)]
+
+
 class FgpuFrameCenter(C.Structure):
     """fgpu_frame_center: centre of mass, its velocity and the mass of a set
     of bodies (nbody/planetary_system.cpp:580-650)."""
@@ -183,7 +190,7 @@ EXPORTED_SYMBOLS = [
     "fgpu_condition_cfl", "fgpu_apply_boundary_condition", "fgpu_step_euler",
     "fgpu_disk_on_planet_accel", "fgpu_total_mass", "fgpu_accrete_onto_planet",
     "fgpu_check_finite", "fgpu_init_center_of_mass_boundary", "fgpu_set_frame_centers",
-    "fgpu_correct_v_azimuthal",
+    "fgpu_correct_v_azimuthal", "fgpu_cfl_limiting_cell",
     "fgpu_synchronize", "fgpu_set_phase_timing", "fgpu_phase_times", "fgpu_phase_name",
     "fgpu_disk_force_static", "fgpu_gas_kick", "fgpu_transport", "fgpu_compute_pressure",
     "fgpu_snapshot_begin", "fgpu_snapshot_wait", "fgpu_host_alloc", "fgpu_host_free",
@@ -220,6 +227,7 @@ def _declare(lib: C.CDLL) -> C.CDLL:
                                                C.c_double], C.c_int),
         "fgpu_set_frame_centers": ([vp, P(FgpuFrameCenter), P(FgpuFrameCenter)], C.c_int),
         "fgpu_correct_v_azimuthal": ([vp, C.c_double], C.c_int),
+        "fgpu_cfl_limiting_cell": ([vp, P(FgpuCflCell)], C.c_int),
         "fgpu_synchronize": ([vp], C.c_int),
         "fgpu_set_phase_timing": ([vp, C.c_int], C.c_int),
         "fgpu_phase_times": ([vp, dp, C.c_int, P(C.c_int), P(C.c_int)], C.c_int),

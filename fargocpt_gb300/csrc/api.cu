@@ -1331,6 +1331,46 @@ extern "C" int fgpu_init_center_of_mass_boundary(fgpu_engine *eng, double mass_a
     return FGPU_OK;
 }
 
+extern "C" int fgpu_cfl_limiting_cell(fgpu_engine *eng, fgpu_cfl_cell *out)
+{
+    if (!eng || !out) return FGPU_ERR_BAD_ARG;
+    if (eng->e32) {
+        eng->err = "the CFL report is a diagnostic of the FP64 form";
+        return FGPU_ERR_UNSUPPORTED;
+    }
+    double dt = 0.0;
+    if (int rc = fgpu_condition_cfl(eng, &dt)) return rc;  // derived quantities current
+    NvtxCall nvtx_("fgpu_cfl_limiting_cell");
+    const int rows = eng->nr - 1;
+    double *d = nullptr;
+    CK(cudaMalloc(&d, sizeof(double) * 10 * (size_t)rows));
+    launch_cfl_cells(launch_of(eng), state_of(eng), d);
+    std::vector<double> h(10 * (size_t)rows);
+    const cudaError_t e1 = cudaMemcpyAsync(h.data(), d, sizeof(double) * h.size(),
+                                           cudaMemcpyDeviceToHost, eng->stream);
+    const cudaError_t e2 = cudaStreamSynchronize(eng->stream);
+    cudaFree(d);
+    CK(e1);
+    CK(e2);
+    *out = fgpu_cfl_cell{};
+    out->ring = out->azimuth = out->shear_ring = -1;
+    out->dt_cell = out->dt_shear = 1.0e300;
+    for (int i = 0; i < rows; ++i) {
+        const double *o = h.data() + (size_t)10 * i;
+        if (o[1] >= 0.0 && o[0] < out->dt_cell) {
+            out->dt_cell = o[0];
+            out->ring = i;
+            out->azimuth = (int)o[1];
+            for (int k = 0; k < 6; ++k) out->invdt[k] = o[3 + k];
+        }
+        if (o[2] < out->dt_shear) {
+            out->dt_shear = o[2];
+            out->shear_ring = i;
+        }
+    }
+    return FGPU_OK;
+}
+
 extern "C" int fgpu_correct_v_azimuthal(fgpu_engine *eng, double domega)
 {
     if (!eng || !std::isfinite(domega)) return FGPU_ERR_BAD_ARG;

@@ -34,6 +34,7 @@ void launch_visc_corr(const Launch &L, const State &s);
 void launch_ghost(const Launch &L, const BcSpec &bc, double omf, const State &s);
 void launch_com_boundary(const Launch &L, const ComSpec &c, const State &s);
 void launch_correct_vaz(const Launch &L, double domega, double *vaz);
+void launch_cfl_cells(const Launch &L, const State &s, double *out);
 void launch_com_damping(const Launch &L, const ComSpec &c, double dt, const State &s);
 void launch_transport_radial(const Launch &L, double dt, double omf, int chunk, const double *S,
                              const double *vr, const double *vaz, const double *E,

@@ -1202,6 +1202,77 @@ __device__ __forceinline__ float block_min_f(float v, float *red)
     return red[32];
 }
 
+// The FP64 time step of cell (i, j) (cfl.cpp:185-382): the six inverse times
+// (sound speed, radial and azimuthal transport, artificial viscosity,
+// viscosity, heating and cooling; LeapFrog's 0.6 on the last three) into
+// inv[], CFL / sqrt of their squares, and StabilizeViscosity 2's limit.
+__device__ __forceinline__ double cfl_cell64(const Geo &g, const Tables &t, const Phys &ph,
+                                             int sn, int i, int j, double c_s, double n,
+                                             const double *__restrict__ vr,
+                                             const double *__restrict__ vaz, double vm0,
+                                             const double *__restrict__ qplus,
+                                             const double *__restrict__ qminus,
+                                             const double *__restrict__ E,
+                                             const double *__restrict__ corr_phi,
+                                             const double *__restrict__ corr_r, double inv[6])
+{
+    const int nz = g.nz;
+    const size_t row = (size_t)i * nz;
+    const size_t c = row + j;
+    const double va = vaz[c];
+    const double vres = ph.fast_transport ? va - vm0 : va;
+    const double invdt1 = c_s * t.InvCell[i];
+    const double invdt2 = vr[c] * t.InvDiffRsup[i];
+    const double invdt3 = vres * t.InvDxTheta[i];
+    const double vr1 = vr[c + nz];
+    const double va1 = vaz[row + (j == nz - 1 ? 0 : j + 1)];
+    double invdt4;
+    if (sn) {
+        double dvR = vr1 - vr[c];
+        double dvA = va1 - va;
+        dvR = dvR > 0.0 ? 0.0 : -dvR;
+        dvA = dvA > 0.0 ? 0.0 : -dvA;
+        const double a = dvR * t.InvDiffRsup[i], b = dvA * t.InvDxTheta[i];
+        invdt4 = ph.four_C2 * (dbits(a) > dbits(b) ? a : b);
+    } else {
+        const double eps_rr = (vr1 - vr[c]) * t.InvDiffRsup[i];
+        const double eps_pp = t.InvRmed[i] * ((va1 - va) * g.invdphi + 0.5 * (vr1 + vr[c]));
+        const double d = eps_rr + eps_pp;
+        const double mdiv = -(d < 0.0 ? d : 0.0);
+        invdt4 = ph.four_C2 * mdiv;
+    }
+    double invdt5 = 4.0 * n * t.InvCell2[i];
+    double invdt6 = 0.0;
+    if (ph.adiabatic) {
+        invdt6 = ph.inv_hc_limit * fabs(fast_div(qplus[c] - qminus[c], E[c]));
+    }
+    if (ph.leapfrog) {
+        // LeapFrog applies the source terms twice with dt/2 (cfl.cpp:254-317)
+        invdt4 *= 0.6;
+        invdt5 *= 0.6;
+        invdt6 *= 0.6;
+    }
+    double dt_cell =
+        fast_div(ph.cfl, sqrt(invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 +
+                              invdt4 * invdt4 + invdt5 * invdt5 + invdt6 * invdt6));
+    if (ph.stabilize == 2) {
+        // viscous stability limit, cfl.cpp:332-351
+        const double cphi = corr_phi[c], cr = corr_r[c];
+        const double cc = cr < cphi ? cr : cphi;
+        if (cc != 0.0) {
+            const double dt_stable = -fast_div(ph.cfl, cc);
+            if (dt_stable < dt_cell) dt_cell = dt_stable;
+        }
+    }
+    inv[0] = invdt1;
+    inv[1] = invdt2;
+    inv[2] = invdt3;
+    inv[3] = invdt4;
+    inv[4] = invdt5;
+    inv[5] = invdt6;
+    return dt_cell;
+}
+
 __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const double *__restrict__ S,
                               const double *__restrict__ E, const double *__restrict__ vr,
                               const double *__restrict__ vaz, const double *__restrict__ qplus,
@@ -1312,51 +1383,9 @@ __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const 
                                          ph.stabilize == 2 ? corr_phi[c] : 0.0,
                                          ph.stabilize == 2 ? corr_r[c] : 0.0);
             if (!(d32 <= thr)) continue;
-            const double va = vaz[c];
-            const double vres = ph.fast_transport ? va - vm0 : va;
-            const double invdt1 = c_s * t.InvCell[i];
-            const double invdt2 = vr[c] * t.InvDiffRsup[i];
-            const double invdt3 = vres * t.InvDxTheta[i];
-            const double vr1 = vr[c + nz];
-            const double va1 = vaz[row + (j == nz - 1 ? 0 : j + 1)];
-            double invdt4;
-            if (sn) {
-                double dvR = vr1 - vr[c];
-                double dvA = va1 - va;
-                dvR = dvR > 0.0 ? 0.0 : -dvR;
-                dvA = dvA > 0.0 ? 0.0 : -dvA;
-                const double a = dvR * t.InvDiffRsup[i], b = dvA * t.InvDxTheta[i];
-                invdt4 = ph.four_C2 * (dbits(a) > dbits(b) ? a : b);
-            } else {
-                const double eps_rr = (vr1 - vr[c]) * t.InvDiffRsup[i];
-                const double eps_pp = t.InvRmed[i] * ((va1 - va) * g.invdphi + 0.5 * (vr1 + vr[c]));
-                const double d = eps_rr + eps_pp;
-                const double mdiv = -(d < 0.0 ? d : 0.0);
-                invdt4 = ph.four_C2 * mdiv;
-            }
-            double invdt5 = 4.0 * n * t.InvCell2[i];
-            double invdt6 = 0.0;
-            if (ph.adiabatic) {
-                invdt6 = ph.inv_hc_limit * fabs(fast_div(qplus[c] - qminus[c], E[c]));
-            }
-            if (ph.leapfrog) {
-                // LeapFrog applies the source terms twice with dt/2 (cfl.cpp:254-317)
-                invdt4 *= 0.6;
-                invdt5 *= 0.6;
-                invdt6 *= 0.6;
-            }
-            double dt_cell =
-                fast_div(ph.cfl, sqrt(invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 +
-                                      invdt4 * invdt4 + invdt5 * invdt5 + invdt6 * invdt6));
-            if (ph.stabilize == 2) {
-                // viscous stability limit, cfl.cpp:332-351
-                const double cphi = corr_phi[c], cr = corr_r[c];
-                const double cc = cr < cphi ? cr : cphi;
-                if (cc != 0.0) {
-                    const double dt_stable = -fast_div(ph.cfl, cc);
-                    if (dt_stable < dt_cell) dt_cell = dt_stable;
-                }
-            }
+            double inv[6];
+            const double dt_cell = cfl_cell64(g, t, ph, sn, i, j, c_s, n, vr, vaz, vm0, qplus,
+                                              qminus, E, corr_phi, corr_r, inv);
             // positive doubles order like their bit patterns
             if (dbits(dt_cell) < dbits(local)) local = dt_cell;
         }
@@ -1690,6 +1719,79 @@ __global__ void k_pressure(Geo g, Tables t, Phys ph, const double *__restrict__ 
 void launch_pressure(const Launch &L, const double *S, const double *E, double *P)
 {
     k_pressure<<<dim3((L.g.nz + 127) / 128, L.g.nr), 128, 0, L.stream>>>(L.g, L.t, L.ph, S, E, P);
+}
+
+// The step's limiting cell, as cfl.cpp's timestep_debug_report (:38-182)
+// names it: per ring i (0 .. nr - 2) the shear limit and, on the CFL rings
+// (1 .. nr - 2), the smallest cell dt, its azimuth (the first on ties) and
+// its six inverse times, written as out[10 i .. 10 i + 9] =
+// {dt, azimuth, shear dt, invdt 1..6}.  Same arithmetic as k_derived_cfl.
+__global__ void k_cfl_cells(Geo g, Tables t, Phys ph, int sn, const double *__restrict__ vr,
+                            const double *__restrict__ vaz, const double *__restrict__ cs,
+                            const double *__restrict__ nu, const double *__restrict__ qplus,
+                            const double *__restrict__ qminus, const double *__restrict__ E,
+                            const double *__restrict__ corr_phi,
+                            const double *__restrict__ corr_r, double *__restrict__ out)
+{
+    __shared__ double red[33];
+    __shared__ int jmin;
+    const int nz = g.nz;
+    const int i = blockIdx.x;
+    const size_t row = (size_t)i * nz;
+    double p0 = 0.0, p1 = 0.0;
+    for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+        p0 += vaz[row + j];
+        p1 += vaz[row + nz + j];
+    }
+    const double vm0 = block_sum(p0, red) / (double)nz;
+    const double vm1 = block_sum(p1, red) / (double)nz;
+    const double denom = fabs(vm0 * t.InvRmed[i] - vm1 * t.InvRmed[i + 1]) + 1.0e-100;
+    const double shear = ph.cfl * g.dphi / denom;
+    const bool cfl_ring = i >= 1;
+    double local = 1.0e300;
+    double inv[6];
+    if (cfl_ring) {
+        for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+            const size_t c = row + j;
+            const double c_s = ph.adiabatic ? cs[c] : t.CsIso[i];
+            const double d = cfl_cell64(g, t, ph, sn, i, j, c_s, nu[c], vr, vaz, vm0, qplus,
+                                        qminus, E, corr_phi, corr_r, inv);
+            if (d < local) local = d;
+        }
+    }
+    if (threadIdx.x == 0) jmin = nz;
+    const double m = block_min(local, red);
+    if (cfl_ring) {
+        for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+            const size_t c = row + j;
+            const double c_s = ph.adiabatic ? cs[c] : t.CsIso[i];
+            const double d = cfl_cell64(g, t, ph, sn, i, j, c_s, nu[c], vr, vaz, vm0, qplus,
+                                        qminus, E, corr_phi, corr_r, inv);
+            if (d == m) atomicMin(&jmin, j);
+        }
+    }
+    __syncthreads();
+    double *o = out + (size_t)10 * i;
+    if (threadIdx.x == 0) {
+        o[0] = cfl_ring ? m : 1.0e300;
+        o[1] = cfl_ring ? (double)jmin : -1.0;
+        o[2] = shear;
+        for (int k = 0; k < 6; ++k) o[3 + k] = 0.0;
+        if (cfl_ring && jmin < nz) {
+            const size_t c = row + jmin;
+            const double c_s = ph.adiabatic ? cs[c] : t.CsIso[i];
+            cfl_cell64(g, t, ph, sn, i, jmin, c_s, nu[c], vr, vaz, vm0, qplus, qminus, E,
+                       corr_phi, corr_r, inv);
+            for (int k = 0; k < 6; ++k) o[3 + k] = inv[k];
+        }
+    }
+}
+
+void launch_cfl_cells(const Launch &L, const State &s, double *out)
+{
+    k_cfl_cells<<<L.g.nr - 1, 256, 0, L.stream>>>(L.g, L.t, L.ph, L.ph.art_visc_sn, s.vr, s.vaz,
+                                                  s.cs, s.nu, s.qplus, s.qminus, s.energy,
+                                                  s.corr_phi, s.corr_r, out);
 }
 
 void launch_derived_cfl(const Launch &L, int mode, const State &s, unsigned long long *dt_min)

@@ -11,7 +11,7 @@ import ctypes as C
 
 import numpy as np
 
-from .abi import (FIELDS, STATUS_NAMES, VECTOR_FIELDS, FgpuBody, FgpuFrameCenter, FgpuParams,
+from .abi import (FIELDS, STATUS_NAMES, VECTOR_FIELDS, FgpuBody, FgpuCflCell, FgpuFrameCenter, FgpuParams,
                   load_library)
 
 
@@ -177,6 +177,15 @@ class Engine:
         n = (FgpuFrameCenter * 2)(*[FgpuFrameCenter(*c) for c in now])
         a = (FgpuFrameCenter * 2)(*[FgpuFrameCenter(*c) for c in after]) if after else None
         self._check(self.lib.fgpu_set_frame_centers(self.h, n, a), "fgpu_set_frame_centers")
+
+    def cfl_limiting_cell(self):
+        """The cell that limits the CFL step (cfl.cpp:38-182): an
+        abi.FgpuCflCell with ring, azimuth, dt_cell, invdt[6], shear_ring,
+        dt_shear."""
+        out = FgpuCflCell()
+        self._check(self.lib.fgpu_cfl_limiting_cell(self.h, C.byref(out)),
+                    "fgpu_cfl_limiting_cell")
+        return out
 
     def correct_v_azimuthal(self, domega):
         """correct_v_azimuthal (SideEuler.cpp:79-95), for a corotating frame

@@ -346,6 +346,24 @@ int fgpu_set_frame_centers(fgpu_engine *eng, const fgpu_frame_center now[2],
  * (fixed frame). */
 int fgpu_correct_v_azimuthal(fgpu_engine *eng, double domega);
 
+/* The cell that limits the CFL time step, as FargoCPT's SIGUSR1 report
+ * (timestep_debug_report, src/cfl.cpp:38-182) names it: ring and azimuth of
+ * the smallest cell time step (the first in ring-major order on ties), that
+ * time step, its six inverse times (sound speed, radial and azimuthal
+ * transport, artificial viscosity, viscosity, heating/cooling; after
+ * LeapFrog's factor) and the smallest ring shear limit with its ring.  The
+ * step FargoCPT takes is the smaller of dt_cell and dt_shear (before
+ * CFLmaxVar).  FP64 form only; a diagnostic, it allocates. */
+typedef struct fgpu_cfl_cell {
+    int ring, azimuth;
+    int shear_ring, reserved;
+    double dt_cell;
+    double invdt[6];
+    double dt_shear;
+} fgpu_cfl_cell;
+
+int fgpu_cfl_limiting_cell(fgpu_engine *eng, fgpu_cfl_cell *out);
+
 /* Scans the evolved fields for NaN/Inf; returns FGPU_ERR_NONFINITE and the
  * first bad (field, ring, azimuth) when one is found. */
 int fgpu_check_finite(fgpu_engine *eng, int *field, int *nr, int *naz);

@@ -1949,14 +1949,74 @@ int or_init_euler(or_state *s, double t)
 /* cfl::condition_cfl, src/cfl.cpp:185-382; the LeapFrog integrator allows
    the source-term limits (artificial viscosity, viscosity, heating/cooling)
    a 0.6 factor (:254-317) */
+/* The time step of cell (i, j), cfl.cpp:185-382: the six inverse times
+   (LeapFrog's 0.6 on the last three) into inv[], CFL over the root of their
+   squares, and StabilizeViscosity 2's limit. */
+static double cfl_cell(const or_state *s, int i, int j, double vm_i, double inv[6])
+{
+    const int nz = s->nz;
+    const double *vr = F(s, FGPU_V_RADIAL), *vaz = F(s, FGPU_V_AZIMUTHAL),
+         *cs = F(s, FGPU_SOUNDSPEED), *nu = F(s, FGPU_VISCOSITY),
+         *Qp = F(s, FGPU_QPLUS), *Qm = F(s, FGPU_QMINUS), *E = F(s, FGPU_ENERGY);
+    const fgpu_params *p = &s->p;
+    const double lf = p->integrator == FGPU_INTEGRATOR_LEAPFROG ? 0.6 : 1.0;
+    const double dxR = s->Rsup[i] - s->Rinf[i];
+    const double dxA = s->Rmed[i] * s->dphi;
+    const double cell = dxR < dxA ? dxR : dxA;
+    const double vres = p->fast_transport ? AT(vaz, i, j) - vm_i : AT(vaz, i, j);
+    const double invdt1 = AT(cs, i, j) / cell;
+    const double invdt2 = AT(vr, i, j) / dxR;
+    const double invdt3 = vres / dxA;
+    const int jn = j == nz - 1 ? 0 : j + 1;
+    double invdt4;
+    if (p->art_visc == FGPU_ARTVISC_SN) {
+        double dvR = AT(vr, i + 1, j) - AT(vr, i, j);
+        double dvA = AT(vaz, i, jn) - AT(vaz, i, j);
+        dvR = dvR > 0.0 ? 0.0 : -dvR;
+        dvA = dvA > 0.0 ? 0.0 : -dvA;
+        const double a = dvR / dxR, b = dvA / dxA;
+        invdt4 = 4.0 * pow(p->art_visc_factor, 2) * (a > b ? a : b) * lf;
+    } else {
+        const double eps_rr = (AT(vr, i + 1, j) - AT(vr, i, j)) * s->InvDiffRsup[i];
+        const double eps_pp =
+            s->InvRmed[i] * ((AT(vaz, i, jn) - AT(vaz, i, j)) * s->invdphi +
+        		     0.5 * (AT(vr, i + 1, j) + AT(vr, i, j)));
+        const double d = eps_rr + eps_pp;
+        const double mdiv = -(d < 0.0 ? d : 0.0);
+        invdt4 = 4.0 * pow(p->art_visc_factor, 2) * mdiv * lf;
+    }
+    const double invdt5 = 4.0 * AT(nu, i, j) / pow(cell, 2) * lf;
+    double invdt6 = 0.0;
+    if (adiabatic(s)) {
+        const double inv_limit = 1.0 / p->heating_cooling_cfl_limit;
+        invdt6 = inv_limit * fabs((AT(Qp, i, j) - AT(Qm, i, j)) / AT(E, i, j)) * lf;
+    }
+    double dt_cell =
+        p->cfl / sqrt(pow(invdt1, 2) + pow(invdt2, 2) + pow(invdt3, 2) +
+        	      pow(invdt4, 2) + pow(invdt5, 2) + pow(invdt6, 2));
+    if (p->stabilize_viscosity == 2) {
+        /* cfl.cpp:332-351 */
+        const double cphi = AT(s->corr_phi, i, j), cr = AT(s->corr_r, i, j);
+        const double c = cphi < cr ? cphi : cr;
+        if (c != 0.0) {
+            const double dt_stable = -p->cfl / c;
+            if (dt_stable < dt_cell) dt_cell = dt_stable;
+        }
+    }
+    inv[0] = invdt1;
+    inv[1] = invdt2;
+    inv[2] = invdt3;
+    inv[3] = invdt4;
+    inv[4] = invdt5;
+    inv[5] = invdt6;
+    return dt_cell;
+}
+
 double or_condition_cfl(or_state *s)
 {
     const int nr = s->nr, nz = s->nz;
-    double *vr = F(s, FGPU_V_RADIAL), *vaz = F(s, FGPU_V_AZIMUTHAL),
-	   *cs = F(s, FGPU_SOUNDSPEED), *nu = F(s, FGPU_VISCOSITY),
-	   *Qp = F(s, FGPU_QPLUS), *Qm = F(s, FGPU_QMINUS), *E = F(s, FGPU_ENERGY);
+    double *vaz = F(s, FGPU_V_AZIMUTHAL);
     const fgpu_params *p = &s->p;
-    const double lf = p->integrator == FGPU_INTEGRATOR_LEAPFROG ? 0.6 : 1.0;
     double *vm = s->vmean;
 #pragma omp parallel for
     for (int i = 0; i < nr; ++i) {
@@ -1973,54 +2033,54 @@ double or_condition_cfl(or_state *s)
 	    fabs(vm[i] * s->InvRmed[i] - vm[i + 1] * s->InvRmed[i + 1]) + 1.0e-100;
 	const double shear_dt = p->cfl * s->dphi / denom;
 	if (shear_dt < dt_core) dt_core = shear_dt;
-	const double dxR = s->Rsup[i] - s->Rinf[i];
-	const double dxA = s->Rmed[i] * s->dphi;
-	const double cell = dxR < dxA ? dxR : dxA;
 	for (int j = 0; j < nz; ++j) {
-	    const double vres = p->fast_transport ? AT(vaz, i, j) - vm[i] : AT(vaz, i, j);
-	    const double invdt1 = AT(cs, i, j) / cell;
-	    const double invdt2 = AT(vr, i, j) / dxR;
-	    const double invdt3 = vres / dxA;
-	    const int jn = j == nz - 1 ? 0 : j + 1;
-	    double invdt4;
-	    if (p->art_visc == FGPU_ARTVISC_SN) {
-		double dvR = AT(vr, i + 1, j) - AT(vr, i, j);
-		double dvA = AT(vaz, i, jn) - AT(vaz, i, j);
-		dvR = dvR > 0.0 ? 0.0 : -dvR;
-		dvA = dvA > 0.0 ? 0.0 : -dvA;
-		const double a = dvR / dxR, b = dvA / dxA;
-		invdt4 = 4.0 * pow(p->art_visc_factor, 2) * (a > b ? a : b) * lf;
-	    } else {
-		const double eps_rr = (AT(vr, i + 1, j) - AT(vr, i, j)) * s->InvDiffRsup[i];
-		const double eps_pp =
-		    s->InvRmed[i] * ((AT(vaz, i, jn) - AT(vaz, i, j)) * s->invdphi +
-				     0.5 * (AT(vr, i + 1, j) + AT(vr, i, j)));
-		const double d = eps_rr + eps_pp;
-		const double mdiv = -(d < 0.0 ? d : 0.0);
-		invdt4 = 4.0 * pow(p->art_visc_factor, 2) * mdiv * lf;
-	    }
-	    const double invdt5 = 4.0 * AT(nu, i, j) / pow(cell, 2) * lf;
-	    double invdt6 = 0.0;
-	    if (adiabatic(s)) {
-		const double inv_limit = 1.0 / p->heating_cooling_cfl_limit;
-		invdt6 = inv_limit * fabs((AT(Qp, i, j) - AT(Qm, i, j)) / AT(E, i, j)) * lf;
-	    }
-	    double dt_cell =
-		p->cfl / sqrt(pow(invdt1, 2) + pow(invdt2, 2) + pow(invdt3, 2) +
-			      pow(invdt4, 2) + pow(invdt5, 2) + pow(invdt6, 2));
-	    if (p->stabilize_viscosity == 2) {
-		/* cfl.cpp:332-351 */
-		const double cphi = AT(s->corr_phi, i, j), cr = AT(s->corr_r, i, j);
-		const double c = cphi < cr ? cphi : cr;
-		if (c != 0.0) {
-		    const double dt_stable = -p->cfl / c;
-		    if (dt_stable < dt_cell) dt_cell = dt_stable;
-		}
-	    }
+	    double inv[6];
+	    const double dt_cell = cfl_cell(s, i, j, vm[i], inv);
 	    if (dt_cell < dt_core) dt_core = dt_cell;
 	}
     }
     return dt_core;
+}
+
+/* The limiting cell of the CFL step (timestep_debug_report, cfl.cpp:38-182):
+   the smallest cell time step on rings 1 .. nr - 2 (the first in ring-major
+   order on ties) with its inverse times, and the smallest ring shear limit
+   (rings 0 .. nr - 2). */
+int or_cfl_limiting_cell(or_state *s, fgpu_cfl_cell *out)
+{
+    const int nr = s->nr, nz = s->nz;
+    const double *vaz = F(s, FGPU_V_AZIMUTHAL);
+    const fgpu_params *p = &s->p;
+    double *vm = s->vmean;
+    for (int i = 0; i < nr; ++i) {
+	vm[i] = 0.0;
+	for (int j = 0; j < nz; ++j) vm[i] += AT(vaz, i, j);
+	vm[i] /= (double)nz;
+    }
+    memset(out, 0, sizeof(*out));
+    out->ring = out->azimuth = out->shear_ring = -1;
+    out->dt_cell = out->dt_shear = 1.0e300;
+    for (int i = 0; i < nr - 1; ++i) {
+	const double denom =
+	    fabs(vm[i] * s->InvRmed[i] - vm[i + 1] * s->InvRmed[i + 1]) + 1.0e-100;
+	const double shear_dt = p->cfl * s->dphi / denom;
+	if (shear_dt < out->dt_shear) {
+	    out->dt_shear = shear_dt;
+	    out->shear_ring = i;
+	}
+	if (i < 1) continue;
+	for (int j = 0; j < nz; ++j) {
+	    double inv[6];
+	    const double dt_cell = cfl_cell(s, i, j, vm[i], inv);
+	    if (dt_cell < out->dt_cell) {
+		out->dt_cell = dt_cell;
+		out->ring = i;
+		out->azimuth = j;
+		for (int k = 0; k < 6; ++k) out->invdt[k] = inv[k];
+	    }
+	}
+    }
+    return FGPU_OK;
 }
 
 /* ComputeDiskOnPlanetAccel, src/Force.cpp:23-122, with the default

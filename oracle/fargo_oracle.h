@@ -46,6 +46,7 @@ int or_accrete_onto_planet(or_state *s, const fgpu_accretor *a, double dt, doubl
 int or_init_center_of_mass_boundary(or_state *s, double mass_all, double mass_center,
 				    int binary_on_primary, double com_max_dist);
 int or_correct_v_azimuthal(or_state *s, double domega);
+int or_cfl_limiting_cell(or_state *s, fgpu_cfl_cell *out);
 int or_set_frame_centers(or_state *s, const fgpu_frame_center now[2],
 			 const fgpu_frame_center *after);
 

@@ -14,7 +14,7 @@ import subprocess
 import numpy as np
 
 from fargocpt_gb300.abi import (FIELDS, VECTOR_FIELDS, FgpuAccretor, FgpuBody,
-                                FgpuFrameCenter, FgpuParams)
+                                FgpuCflCell, FgpuFrameCenter, FgpuParams)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
@@ -57,6 +57,7 @@ def _load():
     lib.or_init_center_of_mass_boundary.argtypes = [vp, C.c_double, C.c_double, C.c_int,
                                                     C.c_double]
     lib.or_correct_v_azimuthal.argtypes = [vp, C.c_double]
+    lib.or_cfl_limiting_cell.argtypes = [vp, C.POINTER(FgpuCflCell)]
     lib.or_set_frame_centers.argtypes = [vp, C.POINTER(FgpuFrameCenter),
                                          C.POINTER(FgpuFrameCenter)]
     for name in ("or_calculate_potential", "or_viscous_stress_tensor"):
@@ -172,6 +173,11 @@ class OracleState:
 
     def correct_v_azimuthal(self, domega):
         self.lib.or_correct_v_azimuthal(self.h, domega)
+
+    def cfl_limiting_cell(self):
+        out = FgpuCflCell()
+        self.lib.or_cfl_limiting_cell(self.h, C.byref(out))
+        return out
 
     def set_frame_centers(self, now, after=None):
         n = (FgpuFrameCenter * 2)(*[FgpuFrameCenter(*c) for c in now])

@@ -269,3 +269,24 @@ def test_edge_grids_against_oracle(nrad, naz, adiabatic):
         assert err <= TOL, f"FP64 {fld}: {err:.3e}"
         assert np.all(np.isfinite(f.get_field(fld)))
     assert rel_linf(f.get_field("SIGMA"), o.get_field("SIGMA")) <= 1e-4
+
+
+@pytest.mark.parametrize("adiabatic", [False, True])
+def test_cfl_limiting_cell_matches_oracle(adiabatic):
+    """The CFL report (timestep_debug_report, cfl.cpp:38-182): the same
+    limiting cell as the oracle, its time step to 1e-12 and inverse times to
+    1e-11 of the largest, and
+    min(dt_cell, dt_shear) equal to the engine's CFL step."""
+    params, d = make_params(24, 64, adiabatic=adiabatic)
+    (o, _), (g, _) = run_both(params, d, steps=4)
+    co, cg = o.cfl_limiting_cell(), g.cfl_limiting_cell()
+    assert (cg.ring, cg.azimuth, cg.shear_ring) == (co.ring, co.azimuth, co.shear_ring)
+    assert 1 <= cg.ring < d["nrad"] - 1
+    assert abs(cg.dt_cell - co.dt_cell) <= 1e-12 * co.dt_cell
+    assert abs(cg.dt_shear - co.dt_shear) <= 1e-12 * co.dt_shear
+    # the terms enter as a root sum of squares; small ones (v_phi less its
+    # ring mean) carry the fields' 1e-13 differences relatively amplified
+    scale = max(abs(b) for b in co.invdt)
+    for a, b in zip(cg.invdt, co.invdt):
+        assert abs(a - b) <= 1e-11 * scale
+    assert min(cg.dt_cell, cg.dt_shear) == pytest.approx(g.condition_cfl(), rel=1e-14)
