@@ -286,7 +286,7 @@ __device__ __forceinline__ void source_cell(const GeoF &g, const TablesF &t, flo
         // in a rotating frame the reference's vt (frame velocities averaged,
         // plus Rinf OmegaFrame; SourceEuler.cpp:355-364) is the inertial mean
         // plus OmegaFrame (Rinf - the mean of the two Rmed)
-        if (g.omega_frame != 0.0) d += (float)g.omega_frame * t.RinfOff[i];
+        if (g.omega_f != 0.f) d += g.omega_f * t.RinfOff[i];
         // vt^2 / r - dPhi_K/dr = Kbal + (2 A d + d^2) / Rinf
         const float centri = t.Kbal[i] + (2.f * t.Aface[i] + d) * d * t.InvRinf[i];
         vr += dt * (-gradp - gradphi + centri);
@@ -1270,6 +1270,9 @@ __device__ __forceinline__ void derived_cfl_ring(
         local = ph.cfl * g.dphi / denom;
     }
     const bool cfl_ring = do_cfl && i >= 1 && i < nr - 1;
+    // standard transport: the ring's frame speed of the Keplerian reference
+    const float vref_frame =
+        ph.fast_transport ? 0.f : (float)(t.Vref_d[i] - t.Rmed_d[i] * g.omega_frame);
     for (int j = threadIdx.x; j < nz; j += blockDim.x) {
         const size_t c = row + j;
         float c_s, n;
@@ -1303,9 +1306,7 @@ __device__ __forceinline__ void derived_cfl_ring(
         }
         if (cfl_ring) {
             const float d0 = dv[c];
-            const float vres = ph.fast_transport
-                                   ? d0 - md0
-                                   : (float)(t.Vref_d[i] - t.Rmed_d[i] * g.omega_frame) + d0;
+            const float vres = ph.fast_transport ? d0 - md0 : vref_frame + d0;
             const float invdt1 = c_s * t.InvCell[i];
             const float invdt2 = vr[c] * t.InvDiffRsup[i];
             const float invdt3 = vres * t.InvDxTheta[i];

@@ -28,6 +28,7 @@ struct GeoF {
     // OmegaFrame: the stored v_phi residual is about the inertial Keplerian
     // speed, so the frame enters only where frame velocities are asked for
     double omega_frame;
+    float omega_f;  // the same in FP32
 };
 
 // Per-ring tables in FP32, plus the FP64 values the FP64 islands need.

@@ -841,6 +841,7 @@ void Engine32::set_bodies(int n, const fgpu_body *b, double ix, double iy, doubl
         pend_dv += d;
         pend_dv0 += d;
         geo.omega_frame = omega_frame;
+        geo.omega_f = (float)omega_frame;
         bc.zg_in = (float)(zg_in_base - omega_frame * (host_rmed[1] - host_rmed[0]));
         bc.zg_out = (float)(zg_out_base - omega_frame * (host_rmed[nr - 2] - host_rmed[nr - 1]));
         std::vector<double> off(nr);
