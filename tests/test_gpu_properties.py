@@ -79,3 +79,31 @@ def test_c2_size_stays_finite():
     e.apply_boundary_condition(0.0, 0.0, False)
     _advance(e, 50)
     assert e.check_finite() is None
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_injected_nonfinite_value_is_reported(precision):
+    """Failure detection without a GPU fault: a NaN planted on the host in an
+    uploaded field is reported by fgpu_check_finite with its field, ring and
+    azimuth (both forms); an infinite energy likewise; a clean state reports
+    nothing; a non-positive dt is refused before any launch."""
+    from fargocpt_gb300.abi import FIELDS
+    params, d = make_params(16, 48, adiabatic=True, precision=precision)
+    radii = _radii(d)
+    st = initial_state(d, radii, seed=4)
+    e = _engine(params, radii)
+    load(e, st, [(0.0, 0.0, 1.0, 0.0, 0.0)])
+    assert e.check_finite() is None
+    bad = st["SIGMA"].copy()
+    bad[5, 7] = np.nan
+    e.set_field("SIGMA", bad)
+    assert e.check_finite() == (FIELDS["SIGMA"], 5, 7)
+    e.set_field("SIGMA", st["SIGMA"])
+    hot = st["ENERGY"].copy()
+    hot[9, 40] = np.inf
+    e.set_field("ENERGY", hot)
+    assert e.check_finite() == (FIELDS["ENERGY"], 9, 40)
+    e.set_field("ENERGY", st["ENERGY"])
+    assert e.check_finite() is None
+    assert e.lib.fgpu_step_euler(e.h, 0.0, 0.0) == -1
+    assert e.lib.fgpu_step_euler(e.h, -1.0, 0.0) == -1
