@@ -848,11 +848,13 @@ void Engine32::set_bodies(int n, const fgpu_body *b, double ix, double iy, doubl
         std::vector<float> z(nr + 1);
         for (int k = 0; k < nr; ++k) off[k] = host_vref[k] - host_rmed[k] * omega_frame;
         for (int k = 0; k <= nr; ++k) z[k] = (float)(host_rmed[k] * omega_frame - host_vref[k]);
+        // stream-ordered after the kernels already queued that read the old
+        // tables; from pageable memory the call returns once the source is
+        // staged, so the local vectors may go
         cudaMemcpyAsync(vaz_offset, off.data(), sizeof(double) * nr, cudaMemcpyHostToDevice,
                         stream);
         cudaMemcpyAsync(zero_vphi_tab, z.data(), sizeof(float) * (nr + 1),
                         cudaMemcpyHostToDevice, stream);
-        cudaStreamSynchronize(stream);
     }
     bodies.n = n;
     bodies.star_at_origin = n > 0 && b[0].x == 0.0 && b[0].y == 0.0 &&
