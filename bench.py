@@ -1,16 +1,20 @@
-"""Benchmark of the GB300 hydro step: cell-updates/s on FargoCPT's adiabatic
-disk (512 x 1536, the configuration the metric is quoted on).
+"""Benchmark of the GB300 hydro step: cell-updates/s on the largest
+single-GPU disk of the benchmark set, FargoCPT's adiabatic 2048 x 6144 disk
+with three planets (r in [0.3, 5], beta cooling, SN artificial viscosity).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--config c2]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config c5]
     python bench.py --impl reference ...     # the CPU restatement, all host cores
 
 One step = one FargoCPT Euler hydro step (sim::step_Euler's gas part plus the
-CFL dt for the next step) over the whole disk.  value: device time of the
-steps (CUDA events on the engine's stream, L2 flushed before every timed step,
-fields resident in HBM).  e2e: wall time of the drop-in call sequence a C++
-driver makes every step through the C ABI (CFL read-back, N-body state in,
-step, disk force on the planet read back).  Multi-GPU runs are independent
-replicas (the path does not shard across GPUs here).
+CFL dt for the next step) over the whole disk, and the disk force on every
+body (ComputeDiskOnNbodyAccel, which step_Euler runs with DiskFeedback).
+value: device time of the steps (CUDA events on the engine's stream around
+the step and the force read-back, L2 flushed before every timed step, fields
+resident in HBM; every field of the 2048 x 6144 disk is 100 MB, so the step's
+working set is far larger than L2 too).  e2e: wall time of the drop-in call
+sequence a C++ driver makes every step through the C ABI (CFL read-back,
+N-body state in, step, disk forces read back).  Multi-GPU runs are
+independent replicas (the path does not shard across GPUs here).
 
 Beside the FP64 headline the line carries the FP32-mixed form on the same
 disk (``fp32_mixed``) and the batched form (``batched``): 64 independent
@@ -44,15 +48,15 @@ KERNEL_BYTES_PER_CELL = {
     "derived_cfl": 88,
 }
 STEP_BYTES_PER_CELL = {"adiabatic": 64, "isothermal": 48}   # one read + write of the state
-# dram__bytes_read.sum + dram__bytes_write.sum per launch from one ncu capture
-# of the dominant kernels on the 512 x 1536 adiabatic disk (--set full of the
-# FP64 transports and of the FP32 azimuthal transport)
-NCU_DRAM_BYTES_C2 = {
-    ("fp64", "transport_azimuthal"): 44.127e6 + 0.422e6,
-    ("fp64", "transport_radial"): 25.252e6 + 0.738e6,
-    ("fp32", "transport_azimuthal"): 25.286e6 + 0.0005e6,
+# dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant
+# kernels from one-kernel ncu captures (profiles/ names the capture of each)
+NCU_DRAM_BYTES = {
+    # 512 x 1536 adiabatic disk (--set full captures)
+    ("c2", "fp64", "transport_azimuthal"): 44.127e6 + 0.422e6,
+    ("c2", "fp64", "transport_radial"): 25.252e6 + 0.738e6,
+    ("c2", "fp32", "transport_azimuthal"): 25.286e6 + 0.0005e6,
 }
-KERNELS_IN_TIMED_STEP = 13   # the adiabatic step's kernels between the step's events
+STEP_KERNELS = 13   # the adiabatic step's kernels (the force adds two per body)
 
 
 def parse():
@@ -60,7 +64,7 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--config", default="c2")
+    ap.add_argument("--config", default="c5")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -161,7 +165,8 @@ def cpu_baseline(cfg_name, seconds, threads=None):
         ix, iy = nbody.indirect(b)
         o.set_bodies(b, ix, iy, 0.0)
         o.step_euler(dt, t)
-        o.disk_on_planet_accel(1)
+        for k in range(len(b)):   # ComputeDiskOnNbodyAccel, as the GPU step
+            o.disk_on_planet_accel(k)
         t += dt
         steps += 1
         el = time.perf_counter() - t0
@@ -210,7 +215,8 @@ def workload_config(name):
             f"{len(c['planets'])} planet(s), FARGO, SN art. visc, alpha=1e-3"
             + (", beta cooling 10" if c["adiabatic"] else "") + ", FP64",
             "nrad": c["nrad"], "naz": c["naz"], "precision": "fp64",
-            "l2": "flushed (256 MB write) before every timed step"}
+            "l2": "flushed (256 MB write) before every timed step; each FP64 field of the "
+                  f"disk is {c['nrad'] * c['naz'] * 8 / 1e6:.0f} MB"}
 
 
 def measure(args, precision, cfg_name, torch, dist, local):
@@ -242,9 +248,11 @@ def measure(args, precision, cfg_name, torch, dist, local):
                 flush.zero_()
                 timed_events[0].record(stream)
         eng.step_euler(dt, t)
+        # ComputeDiskOnNbodyAccel: every body, one read-back; the end event
+        # follows it, so the device time includes the force kernels
+        eng.disk_on_nbody_accel(len(b))
         if timed_events is not None:
             timed_events[1].record(stream)
-        eng.disk_on_planet_accel(1)
         state["t"] = t + dt
 
     for _ in range(args.warmup):
@@ -274,7 +282,8 @@ def measure(args, precision, cfg_name, torch, dist, local):
     phases, nsteps = eng.phase_times()
     eng.set_phase_timing(False)
     assert eng.check_finite() is None, "non-finite state after the benchmark"
-    return dict(total_ms=total_ms, e2e_s=e2e_s, phases=phases, nsteps=nsteps, cells=cells, d=d)
+    return dict(total_ms=total_ms, e2e_s=e2e_s, phases=phases, nsteps=nsteps, cells=cells, d=d,
+                nbodies=len(nbody.bodies(0.0)))
 
 
 def measure_batch(args, torch, dist):
@@ -382,7 +391,7 @@ def roofline(res, steps, bytes_scale, form, cfg_name):
     kind = "adiabatic" if d["eos"] == 1 else "isothermal"
     sbpc = STEP_BYTES_PER_CELL[kind] * bytes_scale
     step_achieved = sbpc * cells * steps / (res["total_ms"] * 1e-3) / 1e9
-    traffic = NCU_DRAM_BYTES_C2.get((form, dom)) if cfg_name == "c2" else None
+    traffic = NCU_DRAM_BYTES.get((cfg_name, form, dom))
     # every kernel's algorithmic HBM rate against the peak
     per_kernel = {}
     for k, tot in phases.items():
@@ -484,8 +493,9 @@ def main():
         rl32, rls32 = roofline(r32, args.steps, 0.5, "fp32", args.config)
         fp32 = {
             "value": value32, "unit": "cell-updates/s", "ms_per_step": vals[2] / args.steps,
-            "e2e": {"value": e2e32, "unit": "cell-updates/s", "h2d_bytes_per_step": 80,
-                    "d2h_bytes_per_step": 4 + 40},
+            "e2e": {"value": e2e32, "unit": "cell-updates/s",
+                    "h2d_bytes_per_step": 40 * r32["nbodies"],
+                    "d2h_bytes_per_step": 8 + 40 * r32["nbodies"]},
             "speedup_vs_fp64": value32 / value,
             "roofline": rl32, "roofline_step": rls32,
             "phase_ms_per_step": {k: v / max(1, r32["nsteps"])
@@ -499,14 +509,15 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(args.config),
         "e2e": {"value": e2e, "unit": "cell-updates/s",
-                "h2d_bytes_per_step": 2 * 40,   # fgpu_body x2, passed as kernel arguments
-                "d2h_bytes_per_step": 8 + 40},  # CFL dt + disk-force partial sums
+                # fgpu_body per body (kernel arguments); CFL dt + 5 force sums per body
+                "h2d_bytes_per_step": 40 * r64["nbodies"],
+                "d2h_bytes_per_step": 8 + 40 * r64["nbodies"]},
         "roofline": rl,
         "roofline_step": rls,
         "phase_ms_per_step": {k: v / max(1, r64["nsteps"]) for k, v in r64["phases"].items()},
         "fp32_mixed": fp32,
         "batched": batched,
-        "gpu_launches": args.steps * KERNELS_IN_TIMED_STEP,
+        "gpu_launches": args.steps * (STEP_KERNELS + 2 * r64["nbodies"]),
         "clocks": clocks,
     }
     if not args.no_cpu_baseline:

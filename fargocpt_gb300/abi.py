@@ -64,7 +64,7 @@ class FgpuParams(C.Structure):
         ("viscous_accretion", C.c_int), ("composite_inner", C.c_int),
         ("composite_outer", C.c_int), ("initialize_pure_keplerian", C.c_int),
         ("initialize_vradial_zero", C.c_int), ("profile_cutoff_inner", C.c_int),
-        ("reserved_i", C.c_int * 1),
+        ("keep_disk_mass_constant", C.c_int),
         ("gamma", C.c_double), ("mu", C.c_double), ("aspect_ratio", C.c_double),
         ("flaring_index", C.c_double), ("viscous_alpha", C.c_double),
         ("constant_viscosity", C.c_double), ("art_visc_factor", C.c_double),
@@ -83,7 +83,7 @@ class FgpuParams(C.Structure):
         ("vaz_inner_keplerian_factor", C.c_double),
         ("vaz_outer_keplerian_factor", C.c_double),
         ("rmin", C.c_double), ("rmax", C.c_double),
-        ("radial_spacing", C.c_int), ("reserved_j", C.c_int),
+        ("radial_spacing", C.c_int), ("correct_disk_selfgravity", C.c_int),
         ("accretion_radius_fraction", C.c_double), ("sigma_slope", C.c_double),
         ("viscous_outflow_speed", C.c_double), ("vrad_inner_keplerian_factor", C.c_double),
         ("vrad_outer_keplerian_factor", C.c_double), ("binary_quadrupole_moment", C.c_double),
@@ -125,9 +125,16 @@ class FgpuAccretor(C.Structure):
                 ("orbital_period", C.c_double)]
 
 
+# FargoCPT's defaults for keys a parameter dict may leave out
+# (CorrectDiskSelfgravity defaults to yes without self-gravity, parameters.cpp:699)
+PARAM_DEFAULTS = {"correct_disk_selfgravity": 1}
+
+
 def params_from_dict(d: dict) -> FgpuParams:
-    """Fills an FgpuParams from a flat dict of field name -> value."""
+    """Fills an FgpuParams from a flat dict of field name -> value; keys the
+    dict leaves out are zero, except those of PARAM_DEFAULTS."""
     p = FgpuParams()
+    d = {**PARAM_DEFAULTS, **d}
     for name, _ in FgpuParams._fields_:
         if name in d:
             v = d[name]
@@ -188,7 +195,9 @@ EXPORTED_SYMBOLS = [
     "fgpu_get_stream", "fgpu_upload_field", "fgpu_download_field",
     "fgpu_set_bodies", "fgpu_init_euler", "fgpu_recalculate_derived",
     "fgpu_condition_cfl", "fgpu_apply_boundary_condition", "fgpu_step_euler",
-    "fgpu_disk_on_planet_accel", "fgpu_total_mass", "fgpu_accrete_onto_planet",
+    "fgpu_disk_on_planet_accel", "fgpu_disk_on_nbody_accel", "fgpu_total_mass",
+    "fgpu_gas_total_mass",
+    "fgpu_gas_angular_momentum", "fgpu_set_disk_mass_target", "fgpu_accrete_onto_planet",
     "fgpu_check_finite", "fgpu_init_center_of_mass_boundary", "fgpu_set_frame_centers",
     "fgpu_correct_v_azimuthal", "fgpu_cfl_limiting_cell",
     "fgpu_synchronize", "fgpu_set_phase_timing", "fgpu_phase_times", "fgpu_phase_name",
@@ -220,7 +229,11 @@ def _declare(lib: C.CDLL) -> C.CDLL:
         "fgpu_apply_boundary_condition": ([vp, C.c_double, C.c_double, C.c_int], C.c_int),
         "fgpu_step_euler": ([vp, C.c_double, C.c_double], C.c_int),
         "fgpu_disk_on_planet_accel": ([vp, C.c_int, dp], C.c_int),
+        "fgpu_disk_on_nbody_accel": ([vp, dp], C.c_int),
         "fgpu_total_mass": ([vp, dp], C.c_int),
+        "fgpu_gas_total_mass": ([vp, C.c_double, dp], C.c_int),
+        "fgpu_gas_angular_momentum": ([vp, C.c_double, dp], C.c_int),
+        "fgpu_set_disk_mass_target": ([vp, C.c_double], C.c_int),
         "fgpu_accrete_onto_planet": ([vp, C.POINTER(FgpuAccretor), C.c_double, dp], C.c_int),
         "fgpu_check_finite": ([vp, P(C.c_int), P(C.c_int), P(C.c_int)], C.c_int),
         "fgpu_init_center_of_mass_boundary": ([vp, C.c_double, C.c_double, C.c_int,

@@ -79,6 +79,11 @@ struct fgpu_engine {
     ComCenter com_now[2]{}, com_after[2]{};
     double *com_mem = nullptr;
 
+    // KeepDiskMassConstant: the mass sigma is rescaled to after each final
+    // boundary call (sim::init's total_disk_mass_old)
+    double mass_target = 0.0;
+    bool mass_target_set = false;
+
     fgpu32::Engine32 *e32 = nullptr;  // FP32-mixed form, when selected
     bool owns_stream = true;          // false for the disks of a batch
     bool batch_owned = false;         // disks of a batch are freed by the batch
@@ -785,6 +790,7 @@ static int setup_tables(fgpu_engine *eng, const double *radii)
     ph.sigma_min = p.sigma_floor * p.sigma0;
     ph.sigma_floor10 = 10.0 * p.sigma0 * p.sigma_floor;
     ph.eps_smooth = p.thickness_smoothing;
+    ph.correct_sg = p.correct_disk_selfgravity != 0;
     ph.tmin = p.minimum_temperature;
     ph.tmax = p.maximum_temperature;
     ph.Rgas = p.R_gas;
@@ -896,10 +902,10 @@ static int create_engine(const fgpu_params *params, const double *radii, cudaStr
         }
     }
     if (cudaMalloc(&eng->partial, sizeof(double) * 5 * (size_t)eng->nr) != cudaSuccess ||
-        cudaMalloc(&eng->red_out, sizeof(double) * 8) != cudaSuccess ||
+        cudaMalloc(&eng->red_out, sizeof(double) * (8 + 5 * kMaxBodies)) != cudaSuccess ||
         cudaMalloc(&eng->d_dtmin, sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc(&eng->d_bad, sizeof(unsigned long long)) != cudaSuccess ||
-        cudaMallocHost(&eng->h_pinned, sizeof(double) * 16) != cudaSuccess) {
+        cudaMallocHost(&eng->h_pinned, sizeof(double) * (16 + 5 * kMaxBodies)) != cudaSuccess) {
         eng->err = "out of memory (reductions)";
         return fail(FGPU_ERR_OOM);
     }
@@ -1405,12 +1411,40 @@ extern "C" int fgpu_set_frame_centers(fgpu_engine *eng, const fgpu_frame_center 
     return FGPU_OK;
 }
 
+// KeepDiskMassConstant (simulation.cpp:246-251, 445-450): gas_total_mass at
+// RMAX on the device, then sigma *= target / mass over the whole grid.
+static void keep_mass(fgpu_engine *eng, const Launch &L)
+{
+    if (!eng->p.keep_disk_mass_constant) return;
+    launch_gas_quantities(L, eng->p.rmax, eng->bodies.omega_frame, eng->field[FGPU_SIGMA],
+                          eng->field[FGPU_V_AZIMUTHAL], eng->partial, eng->red_out + 5);
+    launch_scale_sigma(L, eng->field[FGPU_SIGMA], eng->mass_target, eng->red_out + 5);
+}
+
+static int mass_target_missing(fgpu_engine *eng)
+{
+    if (!eng->p.keep_disk_mass_constant || eng->mass_target_set) return FGPU_OK;
+    eng->err = "keep_disk_mass_constant needs fgpu_set_disk_mass_target first";
+    return FGPU_ERR_BAD_ARG;
+}
+
+extern "C" int fgpu_set_disk_mass_target(fgpu_engine *eng, double mass)
+{
+    if (!eng || !(mass > 0.0) || !std::isfinite(mass)) return FGPU_ERR_BAD_ARG;
+    eng->mass_target = mass;
+    eng->mass_target_set = true;
+    if (eng->e32) eng->e32->set_mass_target(mass);
+    return FGPU_OK;
+}
+
 extern "C" int fgpu_apply_boundary_condition(fgpu_engine *eng, double t, double dt, int final)
 {
     NvtxCall nvtx_("fgpu_apply_boundary_condition");
     (void)t;
     if (!eng) return FGPU_ERR_BAD_ARG;
     if (int rc = com_unready(eng)) return rc;
+    if (final)
+        if (int rc = mass_target_missing(eng)) return rc;
     ROUTE32(eng->e32->boundary(dt, final != 0));
     Launch L = launch_of(eng);
     if (final) viscous_recompute(eng, L);
@@ -1420,6 +1454,7 @@ extern "C" int fgpu_apply_boundary_condition(fgpu_engine *eng, double t, double 
     }
     ghost(eng, L);
     com_boundary(eng, L, eng->com_now);
+    if (final) keep_mass(eng, L);
     eng->cfl_valid = false;
     return check_launch(eng);
 }
@@ -1486,6 +1521,7 @@ extern "C" int fgpu_step_euler(fgpu_engine *eng, double dt, double t)
     NvtxCall nvtx_("fgpu_step_euler");
     if (!eng || !(dt > 0.0)) return FGPU_ERR_BAD_ARG;
     if (int rc = com_unready(eng)) return rc;
+    if (int rc = mass_target_missing(eng)) return rc;
     ROUTE32(eng->e32->step(dt, t));
     Launch L = launch_of(eng);
     mark(eng, -1);
@@ -1505,6 +1541,7 @@ extern "C" int fgpu_step_euler(fgpu_engine *eng, double dt, double t)
     mark(eng, 10);
     ghost(eng, L);
     com_boundary(eng, L, eng->com_after);
+    keep_mass(eng, L);
     mark(eng, 11);
     // recalculate_derived_disk_quantities (simulation.cpp:265) + the next CFL
     CK(cudaMemsetAsync(eng->d_dtmin, 0x7f, sizeof(unsigned long long), eng->stream));
@@ -1574,6 +1611,41 @@ extern "C" int fgpu_disk_on_planet_accel(fgpu_engine *eng, int k, double accel[2
     return FGPU_OK;
 }
 
+// ComputeDiskOnNbodyAccel (Pframeforce.cpp:194-220): the disk force on every
+// body of the last fgpu_set_bodies, all launches queued before one read-back.
+extern "C" int fgpu_disk_on_nbody_accel(fgpu_engine *eng, double *accel)
+{
+    NvtxCall nvtx_("fgpu_disk_on_nbody_accel");
+    if (!eng || !accel) return FGPU_ERR_BAD_ARG;
+    const Bodies &b = eng->bodies;
+    const int n = b.n;
+    if (n == 0) return FGPU_OK;
+    double *out = eng->red_out + 8;  // 5 doubles per body
+    if (eng->e32) {
+        int rc = eng->e32->disk_forces(n, b.x, b.y, b.a, b.rsm, eng->h_pinned + 16);
+        if (rc) {
+            eng->err = eng->e32->err;
+            return rc;
+        }
+    } else {
+        const Launch L = launch_of(eng);
+        for (int k = 0; k < n; ++k)
+            launch_disk_force(L, b.x[k], b.y[k], b.a[k], b.rsm[k], eng->field[FGPU_SIGMA],
+                              eng->field[FGPU_SCALE_HEIGHT], eng->partial, out + 5 * k);
+        int rc = check_launch(eng);
+        if (rc) return rc;
+        CK(cudaMemcpyAsync(eng->h_pinned + 16, out, sizeof(double) * 5 * n,
+                           cudaMemcpyDeviceToHost, eng->stream));
+        CK(cudaStreamSynchronize(eng->stream));
+    }
+    for (int k = 0; k < n; ++k) {
+        const double *o = eng->h_pinned + 16 + 5 * k;
+        accel[2 * k] = o[0] + o[2];
+        accel[2 * k + 1] = o[1] + o[3];
+    }
+    return FGPU_OK;
+}
+
 extern "C" int fgpu_total_mass(fgpu_engine *eng, double *mass)
 {
     if (!eng || !mass) return FGPU_ERR_BAD_ARG;
@@ -1593,6 +1665,48 @@ extern "C" int fgpu_total_mass(fgpu_engine *eng, double *mass)
     CK(cudaStreamSynchronize(eng->stream));
     *mass = eng->h_pinned[4];
     return FGPU_OK;
+}
+
+// gas_total_mass / gas_angular_momentum within a radius (quantities.cpp:51-74,
+// 242-276): out[0] mass, out[1] angular momentum.
+static int gas_quantities(fgpu_engine *eng, double radius, double out[2])
+{
+    if (eng->e32) {
+        int rc = eng->e32->gas_quantities(radius, out);
+        if (rc) eng->err = eng->e32->err;
+        return rc;
+    }
+    launch_gas_quantities(launch_of(eng), radius, eng->bodies.omega_frame,
+                          eng->field[FGPU_SIGMA], eng->field[FGPU_V_AZIMUTHAL], eng->partial,
+                          eng->red_out + 5);
+    int rc = check_launch(eng);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(eng->h_pinned, eng->red_out + 5, sizeof(double) * 2,
+                       cudaMemcpyDeviceToHost, eng->stream));
+    CK(cudaStreamSynchronize(eng->stream));
+    out[0] = eng->h_pinned[0];
+    out[1] = eng->h_pinned[1];
+    return FGPU_OK;
+}
+
+extern "C" int fgpu_gas_total_mass(fgpu_engine *eng, double radius, double *mass)
+{
+    NvtxCall nvtx_("fgpu_gas_total_mass");
+    if (!eng || !mass) return FGPU_ERR_BAD_ARG;
+    double o[2];
+    int rc = gas_quantities(eng, radius, o);
+    if (rc == FGPU_OK) *mass = o[0];
+    return rc;
+}
+
+extern "C" int fgpu_gas_angular_momentum(fgpu_engine *eng, double radius, double *momentum)
+{
+    NvtxCall nvtx_("fgpu_gas_angular_momentum");
+    if (!eng || !momentum) return FGPU_ERR_BAD_ARG;
+    double o[2];
+    int rc = gas_quantities(eng, radius, o);
+    if (rc == FGPU_OK) *momentum = o[1];
+    return rc;
 }
 
 // accretion::AccreteOntoPlanets for one planet (accretion.cpp:84-480): the

@@ -654,10 +654,11 @@ extern "C" int fgpu_batch_create(int n, const fgpu_params *params, const double 
         if (params[k].precision != FGPU_PRECISION_FP32_MIXED ||
             params[k].integrator != FGPU_INTEGRATOR_EULER)
             return FGPU_ERR_UNSUPPORTED;
-        // StabilizeViscosity, the centre-of-mass composite boundary and the
-        // recompute of c_s, H, nu before the final hooks are not part of the
-        // batched step
-        if (params[k].stabilize_viscosity) return FGPU_ERR_UNSUPPORTED;
+        // StabilizeViscosity, KeepDiskMassConstant, the centre-of-mass
+        // composite boundary and the recompute of c_s, H, nu before the final
+        // hooks are not part of the batched step
+        if (params[k].stabilize_viscosity || params[k].keep_disk_mass_constant)
+            return FGPU_ERR_UNSUPPORTED;
         if (params[k].composite_inner != FGPU_COMPOSITE_INDIVIDUAL ||
             params[k].composite_outer != FGPU_COMPOSITE_INDIVIDUAL)
             return FGPU_ERR_UNSUPPORTED;

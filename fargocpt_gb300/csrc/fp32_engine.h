@@ -69,6 +69,7 @@ struct PhysF {
     int stabilize;    // StabilizeViscosity 0 / 1 / 2
     int heating_viscous, cooling_beta, beta_ref;
     int leapfrog;  // LeapFrog integrator: three CFL limits x 0.6
+    int correct_sg;  // CorrectDiskSelfgravity: disk force from sigma less its ring mean
     float gm1, g_gm1, mu, alpha, constant_viscosity, C2, four_C2, rvf, hvf, cfl, inv_hc_limit;
     float sigma_min, sigma_floor10, eps_smooth, c_v_inv, mu_over_R, cool_const, mu_gm1_over_R;
     float emin_fac, emax_fac;
@@ -197,6 +198,12 @@ class Engine32 {
     // the step's buffers are the ones the batched kernels were given
     bool canonical() const { return fld[FGPU_V_RADIAL] == vr_a && fld[FGPU_V_AZIMUTHAL] == dv_a; }
     int disk_force(double px, double py, double pa, double rsm, double out[5]);
+    int disk_forces(int n, const double *x, const double *y, const double *a,
+                    const double *rsm, double *out);
+    // gas_total_mass and gas_angular_momentum within radius (out[0], out[1])
+    int gas_quantities(double radius, double out[2]);
+    // KeepDiskMassConstant's target mass
+    void set_mass_target(double m) { mass_target = m; }
     int accrete(const AccrF &a, double out[3]);
 
     // centre-of-mass composite boundary: the constants and tables (owned by
@@ -273,6 +280,8 @@ class Engine32 {
     bool visc_recompute = false;  // c_s, H, nu before the final hooks (adiabatic)
     float *corr_phi = nullptr, *corr_r = nullptr;  // StabilizeViscosity factors
     void visc_corr(const StateF &s);
+    int keep_mass();
+    double mass_target = 0.0;
     bool cfl_valid = false;
 };
 

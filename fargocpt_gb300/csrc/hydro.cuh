@@ -58,6 +58,7 @@ struct Phys {
     int leapfrog;         // LeapFrog integrator: three CFL limits x 0.6
     int art_visc_tw;      // Tscharnuter-Winkler artificial viscosity
     int stabilize;        // StabilizeViscosity 0 / 1 / 2
+    int correct_sg;       // CorrectDiskSelfgravity: disk force from sigma less its ring mean
     double gamma, gm1, g_gm1, sqrt_gamma, mu, alpha, constant_viscosity;
     double C2;            // pow(ArtificialViscosityFactor, 2)
     double rvf, hvf, cfl, inv_hc_limit, sigma_min, sigma_floor10;

@@ -54,6 +54,9 @@ void launch_derived_cfl(const Launch &L, int mode, const State &s, unsigned long
 void launch_pressure(const Launch &L, const double *S, const double *E, double *P);
 void launch_disk_force(const Launch &L, double px, double py, double pa, double rsm,
                        const double *S, const double *H, double *partial, double *out);
+void launch_gas_quantities(const Launch &L, double radius, double omf, const double *S,
+                           const double *vaz, double *partial, double *out);
+void launch_scale_sigma(const Launch &L, double *S, double target, const double *mass);
 void launch_check_finite(const Launch &L, const double *x, size_t n, unsigned long long *bad);
 void launch_accrete(const Launch &L, const AccretionSpec &a, double *S, double *E,
                     const double *vr, const double *vaz, const double *nu, double *out);

@@ -246,7 +246,8 @@ __global__ void f_disk_force(GeoF g, TablesF t, PhysF ph, double px, double py, 
             }
         }
         // the ring mean removed (CorrectDiskSelfgravity) from the pair
-        const float dsig = (S[row + j] - mh) + (S_lo[row + j] - ml);
+        const float dsig = ph.correct_sg ? (S[row + j] - mh) + (S_lo[row + j] - ml)
+                                         : S[row + j] + S_lo[row + j];
         const float w = dsig * (rinv * rinv * rinv * fk);
         two_sum_add(axh, axl, w * dx);
         two_sum_add(ayh, ayl, w * dy);
@@ -270,6 +271,56 @@ __global__ void f_reduce_rows(const double *__restrict__ partial, int rows, doub
 {
     const int w = threadIdx.x >> 5;
     if (w < 5) warp_compensated_rows(partial, rows, 5, w, out);
+}
+__global__ void f_reduce_rows2(const double *__restrict__ partial, int rows, double *__restrict__ out)
+{
+    const int w = threadIdx.x >> 5;
+    if (w < 2) warp_compensated_rows(partial, rows, 2, w, out);
+}
+
+// gas_total_mass and gas_angular_momentum (quantities.cpp:51-74, 242-276)
+// of each active ring with Rmed <= radius: sigma from its compensated pair
+// and the inertial azimuthal speed (the stored residual plus v_K(Rmed)), all
+// in FP64; one block per ring writes (mass, angular momentum).
+__global__ void f_gas_quantities(GeoF g, TablesF t, double radius, const float *__restrict__ S,
+                                 const float *__restrict__ S_lo, const float *__restrict__ dv,
+                                 double *__restrict__ partial)
+{
+    __shared__ double red[33];
+    const int nz = g.nz;
+    const int i = blockIdx.x + 1;
+    const size_t row = (size_t)i * nz;
+    const double vref = t.Vref_d[i];
+    double m = 0.0, l = 0.0;
+    for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+        const size_t c = row + j, cm = row + (j == 0 ? nz - 1 : j - 1);
+        const double sj = (double)S[c] + (double)S_lo[c];
+        const double sm = (double)S[cm] + (double)S_lo[cm];
+        m += sj;
+        l += 0.5 * (sj + sm) * ((double)dv[c] + vref);
+    }
+    m = bsum_d(m, red);
+    l = bsum_d(l, red);
+    if (threadIdx.x == 0) {
+        const bool in = t.Rmed_d[i] <= radius;
+        partial[(size_t)blockIdx.x * 2] = in ? t.Surf_d[i] * m : 0.0;
+        partial[(size_t)blockIdx.x * 2 + 1] = in ? t.Surf_d[i] * t.Rmed_d[i] * l : 0.0;
+    }
+}
+
+// KeepDiskMassConstant on the compensated pair: (hi + lo) * target / mass
+// in FP64, split again into the pair.
+__global__ void f_scale_sigma(float *__restrict__ S, float *__restrict__ S_lo, size_t n,
+                              double target, const double *__restrict__ mass)
+{
+    const double factor = target / mass[0];
+    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (size_t)gridDim.x * blockDim.x) {
+        const double v = ((double)S[k] + (double)S_lo[k]) * factor;
+        const float h = (float)v;
+        S[k] = h;
+        S_lo[k] = (float)(v - (double)h);
+    }
 }
 
 __global__ void f_check_finite(const float *__restrict__ x, size_t n, unsigned long long *bad)
@@ -509,6 +560,7 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
     ph.sigma_min = (float)(p.sigma_floor * p.sigma0);
     ph.sigma_floor10 = (float)(10.0 * p.sigma0 * p.sigma_floor);
     ph.eps_smooth = (float)p.thickness_smoothing;
+    ph.correct_sg = p.correct_disk_selfgravity != 0;
     ph.c_v_inv = (float)(p.mu / p.R_gas * (p.gamma - 1.0));
     ph.mu_over_R = (float)(p.mu / p.R_gas);
     ph.cool_const = (float)(8.0 * p.sigma_sb / p.c_light);
@@ -540,7 +592,7 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
     CKF(cudaMemset(alt_sigma_lo, 0, cells * sizeof(float)));
     for (int k = 0; k < 4; ++k) CKF(cudaMalloc(&mom[k], cells * sizeof(float)));
     CKF(cudaMalloc(&partial, sizeof(double) * 5 * (size_t)nr));
-    CKF(cudaMalloc(&red_out, sizeof(double) * 8));
+    CKF(cudaMalloc(&red_out, sizeof(double) * (8 + 5 * kMaxBodies)));
     CKF(cudaMalloc(&d_dtmin, sizeof(unsigned int)));
     CKF(cudaMalloc(&d_bad, sizeof(unsigned long long)));
     CKF(cudaMallocHost(&h_pinned, sizeof(double) * 16));
@@ -981,6 +1033,8 @@ int Engine32::boundary(double dt, bool final)
     f_ghost<<<(nz + 127) / 128, 128, 0, stream>>>(geo, bc, state());
     com_boundary(com_now);
     CKF(cudaGetLastError());
+    if (final)
+        if (int rc = keep_mass()) return rc;
     cfl_valid = false;
     return FGPU_OK;
 }
@@ -1150,11 +1204,65 @@ int Engine32::step(double dt, double t)
     CKL("ghost");
     com_boundary(com_after);
     CKL("com_boundary");
+    rc = keep_mass();
+    if (rc) return rc;
     mark(11);
     rc = derived_cfl(1 | 4);
     if (rc) return rc;
     mark(12);
     CKF(cudaGetLastError());
+    return FGPU_OK;
+}
+
+// the disk force on n bodies: every launch queued, one read-back into out
+// (5 doubles per body, host memory)
+int Engine32::disk_forces(int n, const double *x, const double *y, const double *a,
+                          const double *rsm, double *out)
+{
+    const int rows = nr - 2;
+    double *dev = red_out + 8;
+    for (int k = 0; k < n; ++k) {
+        f_disk_force<<<rows, 256, 0, stream>>>(geo, tabs, phys, x[k], y[k], a[k], rsm[k],
+                                               fld[FGPU_SIGMA], sigma_lo, fld[FGPU_SCALE_HEIGHT],
+                                               partial);
+        f_reduce_rows<<<1, 32 * 5, 0, stream>>>(partial, rows, dev + 5 * k);
+    }
+    CKF(cudaGetLastError());
+    CKF(cudaMemcpyAsync(out, dev, sizeof(double) * 5 * n, cudaMemcpyDeviceToHost, stream));
+    CKF(cudaStreamSynchronize(stream));
+    return FGPU_OK;
+}
+
+int Engine32::gas_quantities(double radius, double out[2])
+{
+    if (int rc_ = sync_frame()) return rc_;
+    const int rows = nr - 2;
+    f_gas_quantities<<<rows, 256, 0, stream>>>(geo, tabs, radius, fld[FGPU_SIGMA], sigma_lo,
+                                               fld[FGPU_V_AZIMUTHAL], partial);
+    f_reduce_rows2<<<1, 64, 0, stream>>>(partial, rows, red_out + 5);
+    CKF(cudaGetLastError());
+    CKF(cudaMemcpyAsync(h_pinned, red_out + 5, sizeof(double) * 2, cudaMemcpyDeviceToHost,
+                        stream));
+    CKF(cudaStreamSynchronize(stream));
+    out[0] = h_pinned[0];
+    out[1] = h_pinned[1];
+    return FGPU_OK;
+}
+
+// KeepDiskMassConstant after a final boundary call (simulation.cpp:246-251,
+// 445-450): the mass at RMAX on the device, then the rescale.
+int Engine32::keep_mass()
+{
+    if (!p.keep_disk_mass_constant) return FGPU_OK;
+    const int rows = nr - 2;
+    f_gas_quantities<<<rows, 256, 0, stream>>>(geo, tabs, p.rmax, fld[FGPU_SIGMA], sigma_lo,
+                                               fld[FGPU_V_AZIMUTHAL], partial);
+    f_reduce_rows2<<<1, 64, 0, stream>>>(partial, rows, red_out + 5);
+    const size_t n = cells;
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, 4096);
+    f_scale_sigma<<<blocks, 256, 0, stream>>>(fld[FGPU_SIGMA], sigma_lo, n, mass_target,
+                                              red_out + 5);
+    CKL("keep_mass");
     return FGPU_OK;
 }
 

@@ -12,6 +12,8 @@
 
 #include <math.h>
 
+#include <algorithm>
+
 namespace fgpu {
 
 #define CELL(i, j) ((size_t)(i) * (size_t)nz + (size_t)(j))
@@ -1468,9 +1470,9 @@ __global__ void k_accrete(Geo g, Tables t, Phys ph, AccretionSpec a, double *__r
 }
 
 // ---------------------------------------------------------------------------
-// ComputeDiskOnPlanetAccel (src/Force.cpp:23-122) with CorrectDiskSelfgravity
-// (the ring mean of sigma subtracted, Pframeforce.cpp:175-190), and
-// gas_total_mass (quantities.cpp:51-74).  One CTA per active ring writes its
+// ComputeDiskOnPlanetAccel (src/Force.cpp:23-122), with CorrectDiskSelfgravity
+// the ring mean of sigma subtracted (Force.cpp:64-66), and gas_total_mass
+// (quantities.cpp:51-74).  One CTA per active ring writes its
 // partial sums; k_reduce_rows adds them with compensation in a fixed order.
 // ---------------------------------------------------------------------------
 __global__ void k_disk_force(Geo g, Tables t, Phys ph, double px, double py, double pa,
@@ -1483,7 +1485,9 @@ __global__ void k_disk_force(Geo g, Tables t, Phys ph, double px, double py, dou
     const size_t row = (size_t)i * nz;
     double ps = 0.0;
     for (int j = threadIdx.x; j < nz; j += blockDim.x) ps += S[row + j];
-    const double sigma1d = block_sum(ps, red) / nz;
+    const double ring_sum = block_sum(ps, red);
+    // CorrectDiskSelfgravity (Force.cpp:64-66): the ring mean removed
+    const double sigma1d = ph.correct_sg ? ring_sum / nz : 0.0;
     double ax = 0.0, ay = 0.0, mass = 0.0;
     for (int j = threadIdx.x; j < nz; j += blockDim.x) {
         const double smooth = ph.eps_smooth * H[row + j];
@@ -1519,6 +1523,48 @@ __global__ void k_disk_force(Geo g, Tables t, Phys ph, double px, double py, dou
         p[3] = inner ? 0.0 : ay;
         p[4] = mass;
     }
+}
+
+// gas_total_mass (quantities.cpp:51-74) and gas_angular_momentum
+// (quantities.cpp:242-276) of each active ring with Rmed <= radius (zero
+// otherwise): one CTA per ring writes (mass, angular momentum).  The ring's
+// Surf and Rmed multiply its sums once; the angular momentum takes sigma at
+// the v_phi interface (cells j and j - 1) and the inertial speed.
+__global__ void k_gas_quantities(Geo g, Tables t, double radius, double omf,
+                                 const double *__restrict__ S, const double *__restrict__ vaz,
+                                 double *__restrict__ partial)
+{
+    __shared__ double red[33];
+    const int nz = g.nz;
+    const int i = blockIdx.x + 1;
+    const size_t row = (size_t)i * nz;
+    const double rmed = t.Rmed[i];
+    const double vframe = omf * rmed;
+    double m = 0.0, l = 0.0;
+    for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+        const double sj = S[row + j];
+        const double sm = S[row + (j == 0 ? nz - 1 : j - 1)];
+        m += sj;
+        l += 0.5 * (sj + sm) * (vaz[row + j] + vframe);
+    }
+    m = block_sum(m, red);
+    l = block_sum(l, red);
+    if (threadIdx.x == 0) {
+        const bool in = rmed <= radius;
+        partial[(size_t)blockIdx.x * 2] = in ? t.Surf[i] * m : 0.0;
+        partial[(size_t)blockIdx.x * 2 + 1] = in ? t.Surf[i] * rmed * l : 0.0;
+    }
+}
+
+// KeepDiskMassConstant (simulation.cpp:246-251): sigma *= target / mass over
+// every cell, the mass read on the device (no host round trip).
+__global__ void k_scale_sigma(double *__restrict__ S, size_t n, double target,
+                              const double *__restrict__ mass)
+{
+    const double factor = target / mass[0];
+    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (size_t)gridDim.x * blockDim.x)
+        S[k] *= factor;
 }
 
 // Kahan-compensated sum of `rows` records of `width` doubles, in order.
@@ -1800,6 +1846,21 @@ void launch_derived_cfl(const Launch &L, int mode, const State &s, unsigned long
                                                 s.energy, s.vr, s.vaz, s.qplus, s.qminus, s.cs,
                                                 s.H, s.P, s.T, s.nu, s.corr_phi, s.corr_r,
                                                 dt_min);
+}
+
+void launch_gas_quantities(const Launch &L, double radius, double omf, const double *S,
+                           const double *vaz, double *partial, double *out)
+{
+    const int rows = L.g.nr - 2;
+    k_gas_quantities<<<rows, 256, 0, L.stream>>>(L.g, L.t, radius, omf, S, vaz, partial);
+    k_reduce_rows<<<1, 32 * 2, 0, L.stream>>>(partial, rows, 2, out);
+}
+
+void launch_scale_sigma(const Launch &L, double *S, double target, const double *mass)
+{
+    const size_t n = (size_t)L.g.nr * L.g.nz;
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, 4096);
+    k_scale_sigma<<<blocks, 256, 0, L.stream>>>(S, n, target, mass);
 }
 
 void launch_disk_force(const Launch &L, double px, double py, double pa, double rsm,

@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <mutex>
 
 namespace {
 
@@ -29,9 +30,16 @@ constexpr int kWidth = 5;  // inner x, inner y, outer x, outer y, mass
 // call rewrites each row it later reads, so nothing has to be cleared first.
 static __device__ __align__(256) double g_ring_partials[kMaxRings * kWidth];
 
+// Device address of the array per device, from cudaGetSymbolAddress.  The
+// address is looked up again on every call that is not being captured into a
+// CUDA graph (a reset device or a new primary context may load the module at
+// another address); a call made while its stream captures uses the address
+// the last uncaptured call on that device found.  The mutex orders first
+// calls from several host threads.
 constexpr int kMaxDevices = 64;
-static double *g_scratch_addr[kMaxDevices];  // device address per device, from
-static bool g_scratch_ready[kMaxDevices];    // cudaGetSymbolAddress
+static double *g_scratch_addr[kMaxDevices];
+static bool g_scratch_ready[kMaxDevices];
+static std::mutex g_scratch_mutex;
 
 __device__ double warp_sum(double v)
 {
@@ -58,8 +66,9 @@ __device__ double block_sum(double v, double *red)
 
 // One block per active ring i = 1 .. nrad-2 (ComputeDiskOnPlanetAccel,
 // src/Force.cpp:23-122, with the ring-mean density subtracted as
-// CorrectDiskSelfgravity does, src/Pframeforce.cpp:175-190; gas_total_mass,
-// src/quantities.cpp:51-74).  The ring metric is formed from the radii.
+// CorrectDiskSelfgravity, FargoCPT's default without self-gravity, does at
+// src/Force.cpp:64-66; gas_total_mass, src/quantities.cpp:51-74).  The ring
+// metric is formed from the radii.
 __global__ void k_force_rows(const double *__restrict__ S, const double *__restrict__ H,
                              const double *__restrict__ radii, int naz, double G, double eps,
                              double px, double py, double pa, double rsm,
@@ -142,30 +151,54 @@ extern "C" int fgpu_disk_force_static(const double *sigma, const double *scale_h
                 nrad, kMaxRings + 2, kMaxRings);
         return FGPU_ERR_BAD_ARG;
     }
+    // An error the caller left pending on this thread is not this call's:
+    // report it without clearing it, so that the caller can still read it.
+    cudaError_t pending = cudaPeekAtLastError();
+    if (pending != cudaSuccess) {
+        fprintf(stderr, "fgpu_disk_force_static: an earlier CUDA error is pending: %s\n",
+                cudaGetErrorString(pending));
+        return FGPU_ERR_CUDA;
+    }
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
         cudaGetLastError();
         return FGPU_ERR_NO_DEVICE;
     }
-    // First call on this device: look up the device address of the static
-    // scratch (host code may not use the symbol itself as a pointer).  This
-    // must happen outside any stream capture, so make the first call on each
-    // device before capturing.
-    if (!g_scratch_ready[dev]) {
-        cudaError_t e = cudaGetSymbolAddress((void **)&g_scratch_addr[dev], g_ring_partials);
-        if (e != cudaSuccess) {
-            fprintf(stderr, "fgpu_disk_force_static: cudaGetSymbolAddress: %s\n",
-                    cudaGetErrorString(e));
-            return FGPU_ERR_CUDA;
-        }
-        g_scratch_ready[dev] = true;
-    }
-    double *rows = g_scratch_addr[dev];
     cudaStream_t s = (cudaStream_t)stream;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) {
+        cudaGetLastError();
+        cap = cudaStreamCaptureStatusActive;  // treat as capturing: no lookup
+    }
+    double *rows = nullptr;
+    {
+        // The device address of the static scratch (host code may not use
+        // the symbol itself as a pointer), looked up with this device
+        // current.  A capturing stream cannot make the lookup, so the first
+        // call on each device has to come before any stream capture.
+        std::lock_guard<std::mutex> lock(g_scratch_mutex);
+        if (cap == cudaStreamCaptureStatusNone) {
+            cudaError_t e = cudaGetSymbolAddress((void **)&g_scratch_addr[dev], g_ring_partials);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                g_scratch_ready[dev] = false;
+                fprintf(stderr, "fgpu_disk_force_static: cudaGetSymbolAddress: %s\n",
+                        cudaGetErrorString(e));
+                return FGPU_ERR_CUDA;
+            }
+            g_scratch_ready[dev] = true;
+        } else if (!g_scratch_ready[dev]) {
+            fprintf(stderr, "fgpu_disk_force_static: the first call on a device must not be "
+                            "made while its stream captures\n");
+            return FGPU_ERR_BAD_ARG;
+        }
+        rows = g_scratch_addr[dev];
+    }
     const int nrows = nrad - 2;
     k_force_rows<<<nrows, 256, 0, s>>>(sigma, scale_height, radii, naz, G, thickness_smoothing,
                                        body->x, body->y, body->a, body->r_sm, rows);
     k_sum_rows<<<1, 32, 0, s>>>(rows, nrows, out);
+    // nothing was pending before the launches, so an error now is theirs
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         fprintf(stderr, "fgpu_disk_force_static: launch: %s\n", cudaGetErrorString(e));

@@ -150,10 +150,36 @@ class Engine:
                     "fgpu_disk_on_planet_accel")
         return out[0], out[1]
 
+    def disk_on_nbody_accel(self, n):
+        """ComputeDiskOnNbodyAccel: [(ax, ay)] for the n bodies last set."""
+        out = (C.c_double * (2 * max(1, n)))()
+        self._check(self.lib.fgpu_disk_on_nbody_accel(self.h, out), "fgpu_disk_on_nbody_accel")
+        return [(out[2 * k], out[2 * k + 1]) for k in range(n)]
+
     def total_mass(self):
         out = C.c_double()
         self._check(self.lib.fgpu_total_mass(self.h, C.byref(out)), "fgpu_total_mass")
         return out.value
+
+    def gas_total_mass(self, radius):
+        """quantities::gas_total_mass (quantities.cpp:51-74): rings with Rmed <= radius."""
+        out = C.c_double()
+        self._check(self.lib.fgpu_gas_total_mass(self.h, radius, C.byref(out)),
+                    "fgpu_gas_total_mass")
+        return out.value
+
+    def gas_angular_momentum(self, radius):
+        """quantities::gas_angular_momentum (quantities.cpp:242-276)."""
+        out = C.c_double()
+        self._check(self.lib.fgpu_gas_angular_momentum(self.h, radius, C.byref(out)),
+                    "fgpu_gas_angular_momentum")
+        return out.value
+
+    def set_disk_mass_target(self, mass):
+        """KeepDiskMassConstant's target, sim::init's total_disk_mass_old
+        (simulation.cpp:476-480)."""
+        self._check(self.lib.fgpu_set_disk_mass_target(self.h, mass),
+                    "fgpu_set_disk_mass_target")
 
     def accrete_onto_planet(self, accretor, dt):
         """One planet's part of AccreteOntoPlanets; accretor is an

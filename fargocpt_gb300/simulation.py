@@ -41,13 +41,17 @@ def calculate_time_step(hydro, clock: RunClock, cfl_max_var: float) -> float:
     return rv
 
 
-def start(hydro, clock: RunClock, cfl_max_var: float) -> None:
+def start(hydro, clock: RunClock, cfl_max_var: float, keep_mass_rmax=None) -> None:
     """The calls main() and sim::init() make before the loop
     (main.cpp:117, simulation.cpp:462-480): one CFL evaluation, the initial
-    boundary condition, and a second CFL evaluation."""
+    boundary condition, a second CFL evaluation and, with
+    KeepDiskMassConstant (keep_mass_rmax = RMAX), the gas mass within RMAX as
+    the target of the rescale (total_disk_mass_old)."""
     calculate_time_step(hydro, clock, cfl_max_var)
     hydro.apply_boundary_condition(clock.time, 0.0, False)
     calculate_time_step(hydro, clock, cfl_max_var)
+    if keep_mass_rmax is not None:
+        hydro.set_disk_mass_target(hydro.gas_total_mass(keep_mass_rmax))
 
 
 def step_leapfrog(hydro, dt: float, t: float, first, second) -> None:

@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define FGPU_ABI_VERSION 1
+#define FGPU_ABI_VERSION 2
 
 typedef enum fgpu_status {
     FGPU_OK = 0,
@@ -153,7 +153,10 @@ typedef struct fgpu_params {
                                       the centre-of-mass model disk is Keplerian */
     int initialize_vradial_zero;   /* InitializeVradialZero (parameters.cpp:570) */
     int profile_cutoff_inner;      /* ProfileCutoffInner (parameters.cpp:738) */
-    int reserved_i[1];
+    int keep_disk_mass_constant;   /* KeepDiskMassConstant (parameters.cpp:660-661): after
+                                      every final boundary call sigma is rescaled to the
+                                      mass given to fgpu_set_disk_mass_target
+                                      (simulation.cpp:246-251, 445-450) */
 
     double gamma;           /* AdiabaticIndex */
     double mu;              /* mean molecular weight */
@@ -187,7 +190,9 @@ typedef struct fgpu_params {
     double vaz_outer_keplerian_factor;
     double rmin, rmax;      /* RMIN, RMAX */
     int radial_spacing;     /* FGPU_SPACING_* (used for damping ring search) */
-    int reserved_j;
+    int correct_disk_selfgravity; /* CorrectDiskSelfgravity (parameters.cpp:699; FargoCPT's
+                                     default 1 without self-gravity): the disk force on a
+                                     body uses sigma less its ring mean (Force.cpp:64-66) */
     double accretion_radius_fraction; /* MassAccretionRadius (parameters.cpp:789-790,
                                          FargoCPT's default 1.0) */
     double sigma_slope;     /* SigmaSlope (Interpret.cpp:88): disk-model and balanced
@@ -279,8 +284,29 @@ int fgpu_step_euler(fgpu_engine *eng, double dt, double t);
  * receive the x/y acceleration of the disk on the body. */
 int fgpu_disk_on_planet_accel(fgpu_engine *eng, int k, double accel[2]);
 
+/* ComputeDiskOnNbodyAccel (src/Pframeforce.cpp:194-220): the disk force on
+ * every body of the last fgpu_set_bodies (ComputeDiskOnPlanetAccel each,
+ * Force.cpp:23-122), accel[2k], accel[2k + 1] for body k; all bodies are
+ * computed before one read-back (one host synchronisation per call). */
+int fgpu_disk_on_nbody_accel(fgpu_engine *eng, double *accel);
+
 /* quantities::gas_total_mass (src/quantities.cpp:51-74) over the active rings. */
 int fgpu_total_mass(fgpu_engine *eng, double *mass);
+
+/* quantities::gas_total_mass (src/quantities.cpp:51-74) and
+ * quantities::gas_angular_momentum (src/quantities.cpp:242-276) over the
+ * active rings whose Rmed <= radius, as the monitor output asks for them
+ * (output.cpp:380-390).  Per-ring partial sums in FP64, added across rings
+ * with Kahan compensation in a fixed order (both forms). */
+int fgpu_gas_total_mass(fgpu_engine *eng, double radius, double *mass);
+int fgpu_gas_angular_momentum(fgpu_engine *eng, double radius, double *momentum);
+
+/* KeepDiskMassConstant: the mass sigma is rescaled to after each final
+ * boundary call, FargoCPT's total_disk_mass_old (gas_total_mass at RMAX in
+ * sim::init, simulation.cpp:476-480).  Needed before the first step when
+ * fgpu_params.keep_disk_mass_constant is set; a step or final boundary call
+ * without it returns FGPU_ERR_BAD_ARG. */
+int fgpu_set_disk_mass_target(fgpu_engine *eng, double mass);
 
 /* Accretion kinds of t_planet (src/nbody/planet.h:6-9). */
 enum { FGPU_ACCRETION_KLEY = 0, FGPU_ACCRETION_VISCOUS = 1, FGPU_ACCRETION_SINKHOLE = 2 };
@@ -423,9 +449,12 @@ int fgpu_compute_pressure(fgpu_engine *eng);
  * MAX1D), so nrad - 2 must not exceed 16384; larger grids get
  * FGPU_ERR_BAD_ARG.  sigma, scale_height: device, nrad x naz; radii: device,
  * nrad + 2 values; out: device, 5 doubles (inner x, inner y, outer x, outer y
- * acceleration, gas mass of the active rings).  The first call on a device
- * looks up the array's address; make it before any stream capture.  All calls
- * share the array: calls that overlap on the GPU race. */
+ * acceleration, gas mass of the active rings).  The force uses sigma less its
+ * ring mean, as FargoCPT's CorrectDiskSelfgravity (its default without
+ * self-gravity) does.  The first call on a device looks up the array's
+ * address; make it before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race.  A CUDA error left pending by the
+ * caller is reported as FGPU_ERR_CUDA and left pending. */
 int fgpu_disk_force_static(const double *sigma, const double *scale_height,
 			   const double *radii, int nrad, int naz, double G,
 			   double thickness_smoothing, const fgpu_body *body,

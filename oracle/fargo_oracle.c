@@ -54,6 +54,11 @@ struct or_state {
     double *visc_sigma, *visc_sigma_rp, *corr_phi, *corr_r;
     double *FourThirdInvRbInvdphiSq;
 
+    /* KeepDiskMassConstant: sim::init's total_disk_mass_old
+       (simulation.cpp:476-480), set by or_set_disk_mass_target */
+    double mass_target;
+    int mass_target_set;
+
     int nb;
     fgpu_body b[MAX_BODIES];
     double ix, iy, omega_frame;
@@ -1620,6 +1625,16 @@ static int apply_bc(or_state *s, double dt, int final, const fgpu_frame_center *
     /* the composite after the per-field hooks, boundary_conditions.cpp:92-102 */
     if (com_active(s, 0)) com_ghost(s, 0, &c[0]);
     if (com_active(s, 1)) com_ghost(s, 1, &c[1]);
+    if (final && p->keep_disk_mass_constant) {
+	/* KeepDiskMassConstant right after the final boundary call
+	   (simulation.cpp:246-251, 445-450): sigma *= old / new over the whole
+	   grid (t_polargrid::operator*=, polargrid.cpp:496-505) */
+	if (!s->mass_target_set) return FGPU_ERR_BAD_ARG;
+	const double factor = s->mass_target / or_gas_total_mass(s, p->rmax);
+	double *S = F(s, FGPU_SIGMA);
+	const size_t n = (size_t)s->nr * s->nz;
+	for (size_t k = 0; k < n; ++k) S[k] *= factor;
+    }
     return FGPU_OK;
 }
 
@@ -1905,7 +1920,8 @@ int or_step_euler(or_state *s, double dt, double t)
     apply_bc(s, 0.0, 0, s->com_now);
     or_transport(s, dt);
     /* the final call sees the bodies after the N-body step (simulation.cpp:219-244) */
-    apply_bc(s, dt, 1, s->com_after);
+    const int rc = apply_bc(s, dt, 1, s->com_after);
+    if (rc) return rc;
     or_recalculate_derived(s, t + dt);
     return FGPU_OK;
 }
@@ -2083,9 +2099,9 @@ int or_cfl_limiting_cell(or_state *s, fgpu_cfl_cell *out)
     return FGPU_OK;
 }
 
-/* ComputeDiskOnPlanetAccel, src/Force.cpp:23-122, with the default
-   CorrectDiskSelfgravity (ring-mean density subtracted,
-   Pframeforce.cpp:175-190). */
+/* ComputeDiskOnPlanetAccel, src/Force.cpp:23-122; with CorrectDiskSelfgravity
+   (FargoCPT's default without self-gravity) the ring-mean density is
+   subtracted (Force.cpp:64-66). */
 int or_disk_on_planet_accel(or_state *s, int k, double accel[2])
 {
     if (k < 0 || k >= s->nb) return FGPU_ERR_BAD_ARG;
@@ -2105,7 +2121,8 @@ int or_disk_on_planet_accel(or_state *s, int k, double accel[2])
 	    const double smooth = s->p.thickness_smoothing * AT(H, i, j);
 	    const double xc = s->Rmed[i] * s->cosj[j];
 	    const double yc = s->Rmed[i] * s->sinj[j];
-	    const double cell_sigma = AT(S, i, j) - s->sigma1d[i];
+	    double cell_sigma = AT(S, i, j);
+	    if (s->p.correct_disk_selfgravity) cell_sigma -= s->sigma1d[i];
 	    const double cellmass = s->Surf[i] * cell_sigma;
 	    const double dx = xc - x, dy = yc - y;
 	    const double d2 = pow(dx, 2) + pow(dy, 2);
@@ -2141,6 +2158,48 @@ double or_total_mass(or_state *s)
 	for (int j = 0; j < nz; ++j) m += s->Surf[i] * AT(S, i, j);
     }
     return m;
+}
+
+/* quantities::gas_total_mass, src/quantities.cpp:51-74: the active rings
+   with Rmed <= radius, ring-major (the order of a one-thread run) */
+double or_gas_total_mass(or_state *s, double radius)
+{
+    const int nr = s->nr, nz = s->nz;
+    const double *S = F(s, FGPU_SIGMA);
+    double m = 0.0;
+    for (int i = 1; i < nr - 1; ++i) {
+	for (int j = 0; j < nz; ++j) {
+	    if (s->Rmed[i] <= radius) m += s->Surf[i] * AT(S, i, j);
+	}
+    }
+    return m;
+}
+
+/* quantities::gas_angular_momentum, src/quantities.cpp:242-276: sigma
+   averaged onto the v_phi interface (j and j - 1, periodic), times Rmed and
+   the inertial azimuthal speed v_phi + OmegaFrame Rmed */
+double or_gas_angular_momentum(or_state *s, double radius)
+{
+    const int nr = s->nr, nz = s->nz;
+    const double *S = F(s, FGPU_SIGMA), *V = F(s, FGPU_V_AZIMUTHAL);
+    double L = 0.0;
+    for (int i = 1; i < nr - 1; ++i) {
+	for (int j = 0; j < nz; ++j) {
+	    if (s->Rmed[i] <= radius) {
+		const int jm = j == 0 ? nz - 1 : j - 1;
+		L += s->Surf[i] * 0.5 * (AT(S, i, j) + AT(S, i, jm)) * s->Rmed[i] *
+		     (AT(V, i, j) + s->omega_frame * s->Rmed[i]);
+	    }
+	}
+    }
+    return L;
+}
+
+int or_set_disk_mass_target(or_state *s, double mass)
+{
+    s->mass_target = mass;
+    s->mass_target_set = 1;
+    return FGPU_OK;
 }
 
 /* ------------------------------------------------------------------ */

@@ -42,6 +42,9 @@ void or_gas_kick(or_state *s, double dt, double t);
 void or_compute_pressure(or_state *s);
 int or_disk_on_planet_accel(or_state *s, int k, double accel[2]);
 double or_total_mass(or_state *s);
+double or_gas_total_mass(or_state *s, double radius);
+double or_gas_angular_momentum(or_state *s, double radius);
+int or_set_disk_mass_target(or_state *s, double mass);
 int or_accrete_onto_planet(or_state *s, const fgpu_accretor *a, double dt, double out[3]);
 int or_init_center_of_mass_boundary(or_state *s, double mass_all, double mass_center,
 				    int binary_on_primary, double com_max_dist);

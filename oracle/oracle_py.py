@@ -53,6 +53,10 @@ def _load():
     lib.or_disk_on_planet_accel.argtypes = [vp, C.c_int, dp]
     lib.or_total_mass.argtypes = [vp]
     lib.or_total_mass.restype = C.c_double
+    for name in ("or_gas_total_mass", "or_gas_angular_momentum"):
+        getattr(lib, name).argtypes = [vp, C.c_double]
+        getattr(lib, name).restype = C.c_double
+    lib.or_set_disk_mass_target.argtypes = [vp, C.c_double]
     lib.or_accrete_onto_planet.argtypes = [vp, C.POINTER(FgpuAccretor), C.c_double, dp]
     lib.or_init_center_of_mass_boundary.argtypes = [vp, C.c_double, C.c_double, C.c_int,
                                                     C.c_double]
@@ -156,6 +160,15 @@ class OracleState:
 
     def total_mass(self):
         return self.lib.or_total_mass(self.h)
+
+    def gas_total_mass(self, radius):
+        return self.lib.or_gas_total_mass(self.h, radius)
+
+    def gas_angular_momentum(self, radius):
+        return self.lib.or_gas_angular_momentum(self.h, radius)
+
+    def set_disk_mass_target(self, mass):
+        self.lib.or_set_disk_mass_target(self.h, mass)
 
     def accrete_onto_planet(self, accretor, dt):
         out = (C.c_double * 3)()

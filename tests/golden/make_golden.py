@@ -1,7 +1,9 @@
 """Generates the golden fixtures of tests/golden/ by running the FargoCPT
 reference itself.
 
-Needs the reference sources (default /root/reference/src) and builds them with
+Needs the reference sources (--ref=PATH or FARGO_REFERENCE_SRC: the
+reference's src/ directory; by default a checkout named "reference" beside
+the repository) and builds them with
 oracle/ref/Makefile (parity flags: -O2 -fno-fast-math -ffp-contract=off) into
 oracle/_ref/parity/fargocpt.  Each case writes a FargoCPT setup file plus a
 seeded initial surface density (loaded by the reference via
@@ -15,7 +17,7 @@ seeded initial surface density (loaded by the reference via
 The generating setups are recorded next to the fixtures (<case>.yml) and the
 engine parameters in <case>.json.  Run from the repository root:
 
-    python tests/golden/make_golden.py
+    FARGO_REFERENCE_SRC=<reference>/src python tests/golden/make_golden.py [case ...]
 """
 from __future__ import annotations
 
@@ -36,7 +38,10 @@ sys.path.insert(0, REPO)
 
 from fargocpt_gb300.abi import ACCRETION, BC, COMPOSITE, DAMP, BETA_REF  # noqa: E402
 
-REF_SRC = os.environ.get("FARGO_REFERENCE_SRC", "/root/reference/src")
+# the reference's src/ directory: --ref=PATH, FARGO_REFERENCE_SRC, or a
+# checkout named "reference" beside the repository
+REF_SRC = os.environ.get("FARGO_REFERENCE_SRC",
+                         os.path.join(os.path.dirname(REPO), "reference", "src"))
 REF_EXE = os.path.join(REPO, "oracle", "_ref", "parity", "fargocpt")
 
 COMMON = dict(
@@ -325,12 +330,57 @@ CASES = {
                   DampingEnergyInner="Reference",
                   MonitorTimestep=0.002, Nsnapshots=20),
         nrad=20, naz=48, rmin=0.3, rmax=3.0, planet=3e-3, keep=[1, 2, 5, 10, 20]),
+    # KeepDiskMassConstant (sigma rescaled after every final boundary call,
+    # simulation.cpp:246-251), CorrectDiskSelfgravity off (the disk force from
+    # sigma itself, Force.cpp:64-66), and the monitor quantities
+    # (Quantities.dat: mass and angular momentum within QuantitiesRadiusLimit,
+    # output.cpp:326-470) for gas_total_mass / gas_angular_momentum
+    "adi_planet_keep_mass_nocorr": dict(
+        keys=dict(SigmaSlope=1.0, AspectRatio=0.05, FlaringIndex=0.25,
+                  EquationOfState="Ideal", AdiabaticIndex=1.4, ViscousAlpha=1e-3,
+                  ArtificialViscosity="SN", ArtificialViscosityFactor=1.41421356,
+                  CoolingBetaLocal="yes", CoolingBeta=10,
+                  Transport="FARGO",
+                  InnerBoundary="outflow", OuterBoundary="outflow",
+                  Damping="yes", DampingInnerLimit=1.15, DampingOuterLimit=0.85,
+                  DampingTimeFactor=0.5,
+                  DampingSurfaceDensityInner="Reference",
+                  DampingSurfaceDensityOuter="Reference",
+                  DampingVRadialInner="Reference", DampingVRadialOuter="Reference",
+                  DampingVAzimuthalInner="Reference",
+                  DampingVAzimuthalOuter="Reference",
+                  DampingEnergyInner="Reference", DampingEnergyOuter="Reference",
+                  KeepDiskMassConstant="yes", CorrectDiskSelfgravity="no",
+                  WriteDiskQuantities="yes", QuantitiesRadiusLimit=1.5,
+                  MonitorTimestep=0.002, Nsnapshots=20),
+        nrad=20, naz=48, rmin=0.3, rmax=3.0, planet=1e-3, keep=[1, 2, 5, 10, 20]),
+    # The locally isothermal 128 x 384 disk with one planet of the benchmark
+    # set (FARGO, reference damping at both edges, CFL 0.5) over about a
+    # hundred CFL-limited steps; the planet moves on its circular orbit
+    # between the monitor outputs, so the replay takes its position from the
+    # orbit (circular_bodies) at every step.
+    "c1_cfl_100": dict(
+        keys=dict(SigmaSlope=0.5, AspectRatio=0.05, FlaringIndex=0.0,
+                  EquationOfState="Isothermal", ViscousAlpha=1e-3,
+                  ArtificialViscosity="SN", Transport="FARGO",
+                  InnerBoundary="reference", OuterBoundary="reference",
+                  Damping="yes", DampingInnerLimit=1.1, DampingOuterLimit=0.9,
+                  DampingTimeFactor=1.0,
+                  DampingSurfaceDensityInner="Reference",
+                  DampingSurfaceDensityOuter="Reference",
+                  DampingVRadialInner="Reference", DampingVRadialOuter="Reference",
+                  DampingVAzimuthalInner="Reference",
+                  DampingVAzimuthalOuter="Reference",
+                  MonitorTimestep=0.2, Nsnapshots=10),
+        nrad=128, naz=384, rmin=0.4, rmax=2.5, planet=1e-3, keep=[10],
+        circular_bodies=True),
 }
 
 
 def build_reference():
-    if not os.path.isdir(REF_SRC):
-        raise SystemExit(f"reference sources not found at {REF_SRC}")
+    if not REF_SRC or not os.path.isdir(REF_SRC):
+        raise SystemExit("set FARGO_REFERENCE_SRC (or --ref=PATH) to the reference's src/ "
+                         f"directory (got {REF_SRC!r})")
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle", "ref"),
                     "VARIANT=parity", f"REF={REF_SRC}", "-j8"], check=True)
 
@@ -445,6 +495,8 @@ def engine_params(case, consts, temp_unit):
         profile_cutoff_point_outer=1.0e300, profile_cutoff_width_outer=1.0,
         profile_cutoff_point_inner=0.0, profile_cutoff_width_inner=1.0,
         temperature_cgs_to_code=1.0 / temp_unit,
+        keep_disk_mass_constant=int(str(k.get("KeepDiskMassConstant", "no")) == "yes"),
+        correct_disk_selfgravity=int(str(k.get("CorrectDiskSelfgravity", "yes")) == "yes"),
     )
 
 
@@ -499,6 +551,21 @@ def read_nbody(out, k):
                 omega_frame=a[:, 8], torque=a[:, 18], accretion_rate=a[:, 21])
 
 
+def read_quantities(out):
+    """monitor/Quantities.dat (output.cpp:326-470): per monitor row the
+    monitor number, time, gas mass and angular momentum within
+    QuantitiesRadiusLimit."""
+    rows = []
+    for line in open(os.path.join(out, "monitor", "Quantities.dat")):
+        if line.startswith("#") or not line.strip():
+            continue
+        v = line.split()
+        rows.append([float(v[1]), float(v[2]), float(v[3]), float(v[5])])
+    a = np.array(rows)
+    return dict(monitor=a[:, 0].astype(np.int64), time=a[:, 1], mass=a[:, 2],
+                angular_momentum=a[:, 3])
+
+
 def make_case(name, case, seed):
     tmp = tempfile.mkdtemp(prefix=f"golden_{name}_")
     try:
@@ -530,12 +597,19 @@ def make_case(name, case, seed):
             for key, v in read_nbody(out, k).items():
                 arrays[f"body{k}_{key}"] = v
         arrays["keep"] = np.array(case["keep"])
+        if str(case["keys"].get("WriteDiskQuantities", "no")) == "yes":
+            for key, v in read_quantities(out).items():
+                arrays[f"quantities_{key}"] = v
         meta = dict(params=params, first_dt=float(COMMON["FirstDT"]),
                     monitor_timestep=float(case["keys"]["MonitorTimestep"]),
                     nsnapshots=int(case["keys"]["Nsnapshots"]), nbodies=nb,
                     seed=seed, reference_log_tail=r.stdout.splitlines()[-1])
         if str(case["keys"].get("Frame", COMMON["Frame"])).lower().startswith("c"):
             meta["corotating"] = True
+        if case.get("circular_bodies"):
+            meta["circular_bodies"] = True
+        if "QuantitiesRadiusLimit" in case["keys"]:
+            meta["quantities_radius"] = float(case["keys"]["QuantitiesRadiusLimit"])
         if case.get("planet_keys"):
             pk = case["planet_keys"]
             meta["accretion"] = dict(type=ACCRETION[pk["accretion method"]],
@@ -552,9 +626,16 @@ def make_case(name, case, seed):
 
 
 def main():
-    """python make_golden.py [case ...]: all cases, or the named ones."""
+    """python make_golden.py [--ref=PATH] [case ...]: all cases, or the named ones."""
+    global REF_SRC
+    args = []
+    for a in sys.argv[1:]:
+        if a.startswith("--ref="):
+            REF_SRC = a[len("--ref="):]
+        else:
+            args.append(a)
     build_reference()
-    only = set(sys.argv[1:])
+    only = set(args)
     for i, (name, case) in enumerate(CASES.items()):
         if only and name not in only:
             continue

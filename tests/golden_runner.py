@@ -23,7 +23,8 @@ CASES = ["iso_planet_fixed_dt", "adi_planet_fixed_dt", "iso_star_cfl",
          "iso_planet_accretion_kley", "adi_planet_accretion_sinkhole",
          "iso_planet_accretion_viscous", "iso_planet_bc_individual",
          "adi_star_cfl_bc_individual", "iso_planet_bc_com", "adi_star_cfl_bc_com_keplerian",
-         "adi_planet_bc_com", "iso_planet_corotating"]
+         "adi_planet_bc_com", "iso_planet_corotating", "adi_planet_keep_mass_nocorr",
+         "c1_cfl_100"]
 EVOLVED = ["SIGMA", "V_RADIAL", "V_AZIMUTHAL", "ENERGY"]
 
 
@@ -40,6 +41,22 @@ def bodies_at(arrays, nb, row):
         x = float(arrays[f"body{k}_x"][row])
         y = float(arrays[f"body{k}_y"][row])
         m = float(arrays[f"body{k}_mass"][row])
+        out.append((x, y, m, 0.0, math.sqrt(x * x + y * y)))
+    return out
+
+
+def circular_bodies_at(arrays, nb, G, t):
+    """The bodies at time t when every planet k >= 1 keeps the circular
+    orbit of its initial monitor row about the star at the origin."""
+    m0 = float(arrays["body0_mass"][0])
+    out = [(0.0, 0.0, m0, 0.0, 0.0)]
+    for k in range(1, nb):
+        x0, y0 = float(arrays[f"body{k}_x"][0]), float(arrays[f"body{k}_y"][0])
+        m = float(arrays[f"body{k}_mass"][0])
+        a = math.hypot(x0, y0)
+        om = math.sqrt(G * (m0 + m) / a ** 3)
+        ph = math.atan2(y0, x0) + om * t
+        x, y = a * math.cos(ph), a * math.sin(ph)
         out.append((x, y, m, 0.0, math.sqrt(x * x + y * y)))
     return out
 
@@ -88,10 +105,12 @@ def accretor_at(arrays, meta, row):
                         efficiency=float(acc["efficiency"]), orbital_period=period)
 
 
-def replay(make_backend, name, params_override=None, accreted=None):
+def replay(make_backend, name, params_override=None, accreted=None, quantities=None):
     """Runs the case; returns (snapshots, times, torques, dts).  With
     accreted (a dict), the mass each monitor interval accreted is added to
-    accreted[monitor]."""
+    accreted[monitor]; with quantities (a dict), the gas mass and angular
+    momentum within the case's quantities radius at each monitor are stored
+    in quantities[monitor]."""
     meta, arrays = load_case(name)
     pd = dict(meta["params"])
     if params_override:
@@ -140,7 +159,15 @@ def replay(make_backend, name, params_override=None, accreted=None):
 
     clock = RunClock(time=0.0, last_dt=meta["first_dt"])
     cmv = float(pd["cfl_max_var"])
-    start(hyd, clock, cmv)
+    start(hyd, clock, cmv,
+          keep_mass_rmax=float(pd["rmax"]) if int(pd.get("keep_disk_mass_constant", 0)) else None)
+    qradius = meta.get("quantities_radius")
+
+    def record_quantities(n):
+        if quantities is not None and qradius is not None:
+            quantities[n] = (hyd.gas_total_mass(qradius), hyd.gas_angular_momentum(qradius))
+
+    record_quantities(0)
     keep = set(int(k) for k in arrays["keep"])
     snaps, times, torques = {}, {}, {}
 
@@ -154,6 +181,7 @@ def replay(make_backend, name, params_override=None, accreted=None):
             torques[c.n_monitor] = (x * ay - y * ax) * m
         if c.n_monitor in keep:
             snaps[c.n_monitor] = {f: hyd.get_field(f) for f in EVOLVED}
+        record_quantities(c.n_monitor)
 
     accrete = None
     if "accretion" in meta:
@@ -163,6 +191,12 @@ def replay(make_backend, name, params_override=None, accreted=None):
                 accreted[c.n_monitor + 1] = accreted.get(c.n_monitor + 1, 0.0) + dm
 
     def step_bodies(c):
+        if meta.get("circular_bodies"):
+            # the planet between monitor outputs: its circular orbit about the
+            # star (REBOUND's two-body orbit agrees with it to ~1e-14 at the
+            # monitor rows the reference wrote)
+            b = circular_bodies_at(arrays, nb, float(pd["G"]), c.time)
+            return (b, *indirect_term_euler(b))
         b, ix, iy = body_state(c.n_monitor)
         return (b, ix, iy, float(omega[c.n_monitor + 1])) if corot else (b, ix, iy)
 

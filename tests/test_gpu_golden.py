@@ -39,5 +39,9 @@ def test_gpu_matches_reference_snapshots(name):
         assert abs(t - t_ref[n]) <= 1e-14 * max(1.0, abs(t_ref[n]))
     if torques:
         tq = arrays["body1_torque"]
+        # the orbit-positioned case: a sum with cancellation, held to the bar
+        # of the largest torque of the run
+        scale = np.max(np.abs(tq)) if meta.get("circular_bodies") else None
         for n, t in torques.items():
-            assert abs(t - tq[n]) <= TOL_TORQUE * abs(tq[n]), (n, t, tq[n])
+            ref = scale if scale is not None else abs(tq[n])
+            assert abs(t - tq[n]) <= TOL_TORQUE * ref, (n, t, tq[n])

@@ -1,5 +1,7 @@
-"""Size-independent properties of the GPU step at full benchmark sizes, where
-the oracle would be too slow to run step for step:
+"""Size-independent properties of the GPU step at full benchmark sizes (the
+step-for-step comparison with the oracle at these sizes is in
+test_gpu_baseline_configs.py; these properties hold without a second
+implementation):
 
 * azimuthal equivariance: with only the central star, rotating the initial
   disk by k cells rotates the result by k cells (to round-off: the ring
