@@ -1620,14 +1620,15 @@ extern "C" int fgpu_disk_on_nbody_accel(fgpu_engine *eng, double *accel)
     const Bodies &b = eng->bodies;
     const int n = b.n;
     if (n == 0) return FGPU_OK;
-    double *out = eng->red_out + 8;  // 5 doubles per body
+    double sums[5 * kMaxBodies];     // 5 doubles per body
     if (eng->e32) {
-        int rc = eng->e32->disk_forces(n, b.x, b.y, b.a, b.rsm, eng->h_pinned + 16);
+        int rc = eng->e32->disk_forces(n, b.x, b.y, b.a, b.rsm, sums);
         if (rc) {
             eng->err = eng->e32->err;
             return rc;
         }
     } else {
+        double *out = eng->red_out + 8;
         const Launch L = launch_of(eng);
         for (int k = 0; k < n; ++k)
             launch_disk_force(L, b.x[k], b.y[k], b.a[k], b.rsm[k], eng->field[FGPU_SIGMA],
@@ -1637,9 +1638,10 @@ extern "C" int fgpu_disk_on_nbody_accel(fgpu_engine *eng, double *accel)
         CK(cudaMemcpyAsync(eng->h_pinned + 16, out, sizeof(double) * 5 * n,
                            cudaMemcpyDeviceToHost, eng->stream));
         CK(cudaStreamSynchronize(eng->stream));
+        std::copy(eng->h_pinned + 16, eng->h_pinned + 16 + 5 * n, sums);
     }
     for (int k = 0; k < n; ++k) {
-        const double *o = eng->h_pinned + 16 + 5 * k;
+        const double *o = sums + 5 * k;
         accel[2 * k] = o[0] + o[2];
         accel[2 * k + 1] = o[1] + o[3];
     }

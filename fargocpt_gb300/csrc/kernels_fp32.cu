@@ -595,7 +595,7 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
     CKF(cudaMalloc(&red_out, sizeof(double) * (8 + 5 * kMaxBodies)));
     CKF(cudaMalloc(&d_dtmin, sizeof(unsigned int)));
     CKF(cudaMalloc(&d_bad, sizeof(unsigned long long)));
-    CKF(cudaMallocHost(&h_pinned, sizeof(double) * 16));
+    CKF(cudaMallocHost(&h_pinned, sizeof(double) * (16 + 5 * kMaxBodies)));
     CKF(cudaMalloc(&stage, sizeof(double) * vcells));
     if (p.stabilize_viscosity) {
         // zero until the first stress evaluation, like the reference's grids
@@ -1214,11 +1214,12 @@ int Engine32::step(double dt, double t)
     return FGPU_OK;
 }
 
-// the disk force on n bodies: every launch queued, one read-back into out
-// (5 doubles per body, host memory)
+// the disk force on n <= kMaxBodies bodies: every launch queued, one
+// read-back; out (host, 5 doubles per body) receives the sums
 int Engine32::disk_forces(int n, const double *x, const double *y, const double *a,
                           const double *rsm, double *out)
 {
+    if (n < 0 || n > kMaxBodies) return FGPU_ERR_BAD_ARG;
     const int rows = nr - 2;
     double *dev = red_out + 8;
     for (int k = 0; k < n; ++k) {
@@ -1228,8 +1229,10 @@ int Engine32::disk_forces(int n, const double *x, const double *y, const double 
         f_reduce_rows<<<1, 32 * 5, 0, stream>>>(partial, rows, dev + 5 * k);
     }
     CKF(cudaGetLastError());
-    CKF(cudaMemcpyAsync(out, dev, sizeof(double) * 5 * n, cudaMemcpyDeviceToHost, stream));
+    CKF(cudaMemcpyAsync(h_pinned + 16, dev, sizeof(double) * 5 * n, cudaMemcpyDeviceToHost,
+                        stream));
     CKF(cudaStreamSynchronize(stream));
+    std::copy(h_pinned + 16, h_pinned + 16 + 5 * n, out);
     return FGPU_OK;
 }
 

@@ -133,3 +133,26 @@ def test_disk_force_without_selfgravity_correction():
     e_on.set_bodies(PLANET, 0.0, 0.0, 0.0)
     a_on, a_off = np.array(e_on.disk_on_planet_accel(1)), np.array(g.disk_on_planet_accel(1))
     assert np.max(np.abs(a_on - a_off)) > 1e-3 * np.max(np.abs(a_off))
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_disk_on_nbody_accel_matches_per_body_calls(precision):
+    # ComputeDiskOnNbodyAccel (Pframeforce.cpp:194-220): every body in one
+    # call equals one ComputeDiskOnPlanetAccel call per body, bit for bit
+    from fargocpt_gb300 import setups
+    from fargocpt_gb300.abi import params_from_dict
+    from fargocpt_gb300.engine import Engine
+
+    _, d, radii, fields, nbody = setups.build("c1")
+    d = dict(d, precision=precision)
+    e = Engine(params_from_dict(d), radii)
+    for k, a in fields.items():
+        e.set_field(k, a)
+        e.set_field(k + "0", a)
+    bodies = nbody.bodies(0.3) + [(1.7, -0.4, 3e-4, 0.0, math.hypot(1.7, -0.4))]
+    e.set_bodies(bodies, 0.0, 0.0, 0.0)
+    e.init_euler(0.0)
+    all_at_once = e.disk_on_nbody_accel(len(bodies))
+    assert len(all_at_once) == len(bodies)
+    for k in range(len(bodies)):
+        assert all_at_once[k] == e.disk_on_planet_accel(k)
