@@ -51,6 +51,11 @@ STEP_BYTES_PER_CELL = {"adiabatic": 64, "isothermal": 48}   # one read + write o
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant
 # kernels from one-kernel ncu captures (profiles/ names the capture of each)
 NCU_DRAM_BYTES = {
+    # 2048 x 6144 three-planet adiabatic disk (profiles/traffic_c5_transports.md)
+    ("c5", "fp64", "transport_azimuthal"): 719267072 + 986360320,
+    ("c5", "fp64", "transport_radial"): 403436800 + 552501504,
+    ("c5", "fp32", "transport_azimuthal"): 403144448 + 288285952,
+    ("c5", "fp32", "transport_radial"): 260210688 + 302722816,
     # 512 x 1536 adiabatic disk (--set full captures)
     ("c2", "fp64", "transport_azimuthal"): 44.127e6 + 0.422e6,
     ("c2", "fp64", "transport_radial"): 25.252e6 + 0.738e6,
@@ -147,12 +152,14 @@ def load_disk(backend, fields, nbody):
 
 
 def cpu_baseline(cfg_name, seconds, threads=None):
-    """The oracle (CPU restatement of the reference's step) on this host's
+    """The oracle (CPU restatement of the reference's step), built with the
+    reference's shipped flags (-Ofast -march=native -fopenmp), on this host's
     cores over a bounded sample of the same workload."""
     from fargocpt_gb300 import setups
-    from oracle.oracle_py import OracleState, build_oracle, set_threads
+    from oracle.oracle_py import OracleState, build_oracle, set_threads, use_timing_build
 
     build_oracle()
+    use_timing_build()
     cores = set_threads(threads or os.cpu_count() or 1)
     params, d, radii, fields, nbody = setups.build(cfg_name)
     o = OracleState(params, radii)
@@ -173,7 +180,8 @@ def cpu_baseline(cfg_name, seconds, threads=None):
         if el >= seconds and steps >= 2:
             break
     return {"value": cells * steps / el, "unit": "cell-updates/s", "cores": cores,
-            "kind": "port", "sample": f"{steps} full steps of {cfg_name} "
+            "kind": "port", "build": "-Ofast -march=native -fopenmp (the reference's shipped "
+            "flags)", "sample": f"{steps} full steps of {cfg_name} "
             f"({d['nrad']}x{d['naz']}) in {el:.1f} s"}
 
 

@@ -18,6 +18,9 @@ from fargocpt_gb300.abi import (FIELDS, VECTOR_FIELDS, FgpuAccretor, FgpuBody,
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
+# the same source built with the reference's shipped flags (-Ofast
+# -march=native): only the CPU baseline's timing uses it, never a comparison
+LIB_TIMING = os.path.join(HERE, "liboracle_timing.so")
 
 
 def build_oracle() -> str:
@@ -26,15 +29,26 @@ def build_oracle() -> str:
 
 
 _lib = None
+_variant = "parity"
+
+
+def use_timing_build() -> None:
+    """Selects the shipped-flags build for this process (CPU baseline timing
+    only); call it before the first OracleState."""
+    global _variant, _lib
+    if _lib is not None and _variant != "timing":
+        raise RuntimeError("the parity build is already loaded in this process")
+    _variant = "timing"
 
 
 def _load():
     global _lib
     if _lib is not None:
         return _lib
-    if not os.path.exists(LIB):
+    path = LIB_TIMING if _variant == "timing" else LIB
+    if not os.path.exists(path):
         build_oracle()
-    lib = C.CDLL(LIB)
+    lib = C.CDLL(path)
     dp = C.POINTER(C.c_double)
     vp = C.c_void_p
     lib.or_create.argtypes = [C.POINTER(FgpuParams), dp, C.POINTER(vp)]

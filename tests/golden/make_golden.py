@@ -592,6 +592,10 @@ def make_case(name, case, seed):
         for n in case["keep"]:
             for k, v in read_snapshot(out, n, nrad, naz).items():
                 arrays[f"s{n}_{k}"] = v
+            # the snapshot's misc.bin as written (struct misc_entry,
+            # output.h:14-22, output.cpp:494-527), byte for byte
+            with open(os.path.join(out, "snapshots", str(n), "misc.bin"), "rb") as f:
+                arrays[f"s{n}_misc"] = np.frombuffer(f.read(), dtype=np.uint8)
         nb = 2 if case["planet"] is not None else 1
         for k in range(nb):
             for key, v in read_nbody(out, k).items():
@@ -639,7 +643,13 @@ def main():
     for i, (name, case) in enumerate(CASES.items()):
         if only and name not in only:
             continue
-        make_case(name, case, seed=1000 + i)
+        # a fixture keeps the seed it was first made with
+        seed = 1000 + i
+        meta_path = os.path.join(HERE, f"{name}.json")
+        if os.path.exists(meta_path):
+            with open(meta_path) as f:
+                seed = int(json.load(f).get("seed", seed))
+        make_case(name, case, seed=seed)
 
 
 if __name__ == "__main__":

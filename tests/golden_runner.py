@@ -105,12 +105,14 @@ def accretor_at(arrays, meta, row):
                         efficiency=float(acc["efficiency"]), orbital_period=period)
 
 
-def replay(make_backend, name, params_override=None, accreted=None, quantities=None):
+def replay(make_backend, name, params_override=None, accreted=None, quantities=None,
+           on_snapshot=None):
     """Runs the case; returns (snapshots, times, torques, dts).  With
     accreted (a dict), the mass each monitor interval accreted is added to
     accreted[monitor]; with quantities (a dict), the gas mass and angular
     momentum within the case's quantities radius at each monitor are stored
-    in quantities[monitor]."""
+    in quantities[monitor]; on_snapshot(backend, n, clock) is called at every
+    kept snapshot n (the run clock holds sim::time, last_dt, N_hydro_iter)."""
     meta, arrays = load_case(name)
     pd = dict(meta["params"])
     if params_override:
@@ -181,6 +183,8 @@ def replay(make_backend, name, params_override=None, accreted=None, quantities=N
             torques[c.n_monitor] = (x * ay - y * ax) * m
         if c.n_monitor in keep:
             snaps[c.n_monitor] = {f: hyd.get_field(f) for f in EVOLVED}
+            if on_snapshot is not None:
+                on_snapshot(hyd, c.n_monitor, c)
         record_quantities(c.n_monitor)
 
     accrete = None

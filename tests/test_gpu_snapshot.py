@@ -40,3 +40,66 @@ def test_snapshot_while_stepping(precision, tmp_path):
                           ref["V_RADIAL"])
     assert output.read_misc(str(tmp_path / "misc.bin"))["n_iter"] == 8
     snap.close()
+
+
+@pytest.mark.parametrize("name", ["adi_planet_fixed_dt", "c1_cfl_100"])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_snapshot_files_against_the_references(name, precision, tmp_path):
+    """A reference case replayed on the GPU and written through the
+    asynchronous snapshot path (staged on the device, copied on the second
+    stream, written by fargocpt_gb300.output) against the files the reference
+    wrote: every <name>.dat within the FP64 bar (relative L-infinity 1e-10;
+    FP32-mixed: sigma, v_phi, e 1e-5 and v_r 1e-3 of its maximum), same
+    size; misc.bin's snapshot and monitor numbers byte-equal, its time within
+    1e-12 relative, OmegaFrame and FrameAngle equal, and in the FP64 form the
+    hydro step count byte-equal and the last dt within 1e-12 (FP32-mixed:
+    1e-5) (polargrid.cpp:135-180, output.cpp:494-527)."""
+    import struct
+
+    from fargocpt_gb300 import output
+    from golden_runner import replay, rel_linf
+
+    dirs = {}
+
+    def on_snapshot(hyd, n, clock):
+        snap = output.Snapshotter(hyd)
+        snap.begin()
+        d = tmp_path / str(n)
+        snap.write(str(d), snapshot=n, monitor=n, time=clock.time, last_dt=clock.last_dt,
+                   n_iter=clock.n_hydro_iter)
+        snap.close()
+        dirs[n] = d
+
+    _, _, _, _, arrays = replay(_engine_cls(), name, {"precision": precision},
+                                on_snapshot=on_snapshot)
+    assert set(dirs) == set(int(k) for k in arrays["keep"])
+    for n, d in dirs.items():
+        for f in EVOLVED:
+            ref = arrays[f"s{n}_{f}"]
+            raw = (d / (output.GRID_NAMES[f] + ".dat")).read_bytes()
+            assert len(raw) == ref.size * 8
+            got = np.frombuffer(raw, dtype="<f8").reshape(ref.shape)
+            if not np.any(ref):
+                assert not np.any(got)
+                continue
+            tol = 1e-10 if precision == 0 else (1e-3 if f == "V_RADIAL" else 1e-5)
+            assert rel_linf(got, ref) <= tol, (name, n, f, rel_linf(got, ref))
+        mine = (d / "misc.bin").read_bytes()
+        theirs = arrays[f"s{n}_misc"].tobytes()
+        assert len(mine) == len(theirs) == 48
+        assert mine[:8] == theirs[:8]          # snapshot and monitor numbers
+        t_m, om_m, fa_m, dt_m = struct.unpack_from("<dddd", mine, 8)
+        t_r, om_r, fa_r, dt_r = struct.unpack_from("<dddd", theirs, 8)
+        assert abs(t_m - t_r) <= 1e-12 * abs(t_r)
+        assert (om_m, fa_m) == (om_r, fa_r)
+        if precision == 0:
+            assert mine[40:] == theirs[40:]    # the hydro step count
+            assert abs(dt_m - dt_r) <= 1e-12 * abs(dt_r)
+        else:
+            # the FP32-mixed CFL step is within FP32 rounding of FargoCPT's
+            assert abs(dt_m - dt_r) <= 1e-5 * abs(dt_r)
+
+
+def _engine_cls():
+    from fargocpt_gb300.engine import Engine
+    return Engine
