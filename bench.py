@@ -61,7 +61,7 @@ NCU_DRAM_BYTES = {
     ("c2", "fp64", "transport_radial"): 25.252e6 + 0.738e6,
     ("c2", "fp32", "transport_azimuthal"): 25.286e6 + 0.0005e6,
 }
-STEP_KERNELS = 13   # the adiabatic step's kernels (the force adds two per body)
+STEP_KERNELS = 13   # the adiabatic step's kernels (the force adds two per 4 bodies)
 
 
 def parse():
@@ -525,7 +525,7 @@ def main():
         "phase_ms_per_step": {k: v / max(1, r64["nsteps"]) for k, v in r64["phases"].items()},
         "fp32_mixed": fp32,
         "batched": batched,
-        "gpu_launches": args.steps * (STEP_KERNELS + 2 * r64["nbodies"]),
+        "gpu_launches": args.steps * (STEP_KERNELS + 2 * ((r64["nbodies"] + 3) // 4)),
         "clocks": clocks,
     }
     if not args.no_cpu_baseline:

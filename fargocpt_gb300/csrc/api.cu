@@ -901,7 +901,8 @@ static int create_engine(const fgpu_params *params, const double *radii, cudaStr
             return fail(FGPU_ERR_OOM);
         }
     }
-    if (cudaMalloc(&eng->partial, sizeof(double) * 5 * (size_t)eng->nr) != cudaSuccess ||
+    if (cudaMalloc(&eng->partial, sizeof(double) * 5 * kForceBodies * (size_t)eng->nr) !=
+            cudaSuccess ||
         cudaMalloc(&eng->red_out, sizeof(double) * (8 + 5 * kMaxBodies)) != cudaSuccess ||
         cudaMalloc(&eng->d_dtmin, sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc(&eng->d_bad, sizeof(unsigned long long)) != cudaSuccess ||
@@ -1599,8 +1600,9 @@ extern "C" int fgpu_disk_on_planet_accel(fgpu_engine *eng, int k, double accel[2
     }
     // inner/outer split at the body's distance from the origin (t_planet::get_r);
     // the cubic smoothing radius is the same r_sm the gas feels
-    launch_disk_force(launch_of(eng), b.x[k], b.y[k], b.a[k], b.rsm[k], eng->field[FGPU_SIGMA],
-                      eng->field[FGPU_SCALE_HEIGHT], eng->partial, eng->red_out);
+    launch_disk_force(launch_of(eng), 1, &b.x[k], &b.y[k], &b.a[k], &b.rsm[k],
+                      eng->field[FGPU_SIGMA], eng->field[FGPU_SCALE_HEIGHT], eng->partial,
+                      eng->red_out);
     int rc = check_launch(eng);
     if (rc) return rc;
     CK(cudaMemcpyAsync(eng->h_pinned, eng->red_out, sizeof(double) * 5, cudaMemcpyDeviceToHost,
@@ -1629,10 +1631,8 @@ extern "C" int fgpu_disk_on_nbody_accel(fgpu_engine *eng, double *accel)
         }
     } else {
         double *out = eng->red_out + 8;
-        const Launch L = launch_of(eng);
-        for (int k = 0; k < n; ++k)
-            launch_disk_force(L, b.x[k], b.y[k], b.a[k], b.rsm[k], eng->field[FGPU_SIGMA],
-                              eng->field[FGPU_SCALE_HEIGHT], eng->partial, out + 5 * k);
+        launch_disk_force(launch_of(eng), n, b.x, b.y, b.a, b.rsm, eng->field[FGPU_SIGMA],
+                          eng->field[FGPU_SCALE_HEIGHT], eng->partial, out);
         int rc = check_launch(eng);
         if (rc) return rc;
         CK(cudaMemcpyAsync(eng->h_pinned + 16, out, sizeof(double) * 5 * n,
@@ -1658,14 +1658,16 @@ extern "C" int fgpu_total_mass(fgpu_engine *eng, double *mass)
         *mass = o[4];
         return rc;
     }
-    launch_disk_force(launch_of(eng), 0.0, 0.0, 0.0, 0.0, eng->field[FGPU_SIGMA],
-                      eng->field[FGPU_SCALE_HEIGHT], eng->partial, eng->red_out);
+    // gas_total_mass over every active ring
+    launch_gas_quantities(launch_of(eng), INFINITY, eng->bodies.omega_frame,
+                          eng->field[FGPU_SIGMA], eng->field[FGPU_V_AZIMUTHAL], eng->partial,
+                          eng->red_out + 5);
     int rc = check_launch(eng);
     if (rc) return rc;
-    CK(cudaMemcpyAsync(eng->h_pinned, eng->red_out, sizeof(double) * 5, cudaMemcpyDeviceToHost,
+    CK(cudaMemcpyAsync(eng->h_pinned, eng->red_out + 5, sizeof(double), cudaMemcpyDeviceToHost,
                        eng->stream));
     CK(cudaStreamSynchronize(eng->stream));
-    *mass = eng->h_pinned[4];
+    *mass = eng->h_pinned[0];
     return FGPU_OK;
 }
 

@@ -52,8 +52,15 @@ void launch_damping(const Launch &L, const Damping &dm, double dt, const int *ri
                     const State &s);
 void launch_derived_cfl(const Launch &L, int mode, const State &s, unsigned long long *dt_min);
 void launch_pressure(const Launch &L, const double *S, const double *E, double *P);
-void launch_disk_force(const Launch &L, double px, double py, double pa, double rsm,
-                       const double *S, const double *H, double *partial, double *out);
+// bodies one disk-force pass handles
+constexpr int kForceBodies = 4;
+
+// the disk force on n bodies (ComputeDiskOnPlanetAccel each) and the gas
+// mass: out[5 b .. 5 b + 4] = inner x, inner y, outer x, outer y, mass;
+// partial holds 5 min(n, 4) doubles per active ring
+void launch_disk_force(const Launch &L, int n, const double *px, const double *py,
+                       const double *pa, const double *rsm, const double *S, const double *H,
+                       double *partial, double *out);
 void launch_gas_quantities(const Launch &L, double radius, double omf, const double *S,
                            const double *vaz, double *partial, double *out);
 void launch_scale_sigma(const Launch &L, double *S, double target, const double *mass);

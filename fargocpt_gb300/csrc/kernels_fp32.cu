@@ -198,12 +198,22 @@ __global__ void f_derived_cfl(GeoF g, TablesF t, PhysF ph, int mode, const float
                      blockIdx.x, red, red2, corr_phi, corr_r);
 }
 
-// disk force on a body and gas mass: separations as float pairs, sums as
-// compensated float pairs per thread and in FP64 across the block
-__global__ void f_disk_force(GeoF g, TablesF t, PhysF ph, double px, double py, double pa,
-                             double rsm, const float *__restrict__ S,
-                             const float *__restrict__ S_lo, const float *__restrict__ H,
-                             double *__restrict__ partial)
+// disk force on up to kForceBodies32 bodies in one pass over the ring, and the
+// gas mass: separations as float pairs, sums as compensated float pairs per
+// thread and in FP64 across the block.  partial[5 b .. 5 b + 4] of the ring's
+// row: inner x, inner y, outer x, outer y, mass (ComputeDiskOnPlanetAccel,
+// Force.cpp:23-122; the ring mean removed with CorrectDiskSelfgravity,
+// Force.cpp:64-66; gas_total_mass, quantities.cpp:51-74).
+constexpr int kForceBodies32 = 4;
+struct ForceBodies32 {
+    int n;
+    double x[kForceBodies32], y[kForceBodies32], a[kForceBodies32], rsm[kForceBodies32];
+};
+
+__global__ void f_disk_force_bodies(GeoF g, TablesF t, PhysF ph, ForceBodies32 fb,
+                                    const float *__restrict__ S,
+                                    const float *__restrict__ S_lo, const float *__restrict__ H,
+                                    double *__restrict__ partial, int width)
 {
     __shared__ double red[33];
     const int nz = g.nz;
@@ -218,52 +228,80 @@ __global__ void f_disk_force(GeoF g, TablesF t, PhysF ph, double px, double py, 
         sl_ += S_lo[row + j];
     }
     const double ring_sum = bsum_d((double)sh_ + (double)sl_, red);
-    const double sigma1d = ring_sum / nz;
+    const double sigma1d = ph.correct_sg ? ring_sum / nz : 0.0;
     const float mh = (float)sigma1d, ml = (float)(sigma1d - (double)mh);
-    // cell centres and the planet as float pairs (see potential_cell): the
-    // distance loses nothing to cancellation near the planet
-    const float pxh = (float)px, pxl = (float)(px - (double)pxh);
-    const float pyh = (float)py, pyl = (float)(py - (double)pyh);
+    // cell centres and the bodies as float pairs (see potential_cell): the
+    // distance loses nothing to cancellation near a body
+    float pxh[kForceBodies32], pxl[kForceBodies32], pyh[kForceBodies32], pyl[kForceBodies32];
+    float frsm[kForceBodies32];
+#pragma unroll
+    for (int b = 0; b < kForceBodies32; ++b) {
+        const double px = b < fb.n ? fb.x[b] : 0.0, py = b < fb.n ? fb.y[b] : 0.0;
+        pxh[b] = (float)px;
+        pxl[b] = (float)(px - (double)pxh[b]);
+        pyh[b] = (float)py;
+        pyl[b] = (float)(py - (double)pyh[b]);
+        frsm[b] = b < fb.n ? (float)fb.rsm[b] : 0.f;
+    }
     const float rh = t.Rmed[i], rl = t.RmedLo[i];
-    const float frsm = (float)rsm;
-    float axh = 0.f, axl = 0.f, ayh = 0.f, ayl = 0.f;
+    float axh[kForceBodies32], axl[kForceBodies32], ayh[kForceBodies32], ayl[kForceBodies32];
+#pragma unroll
+    for (int b = 0; b < kForceBodies32; ++b) axh[b] = axl[b] = ayh[b] = ayl[b] = 0.f;
     for (int j = threadIdx.x; j < nz; j += blockDim.x) {
         const float ch = t.cosHi[j], cl = t.cosLo[j], sh = t.sinHi[j], sl = t.sinLo[j];
         const float xh = rh * ch, yh = rh * sh;
         const float xl = fmaf(rh, ch, -xh) + fmaf(rh, cl, rl * ch);
         const float yl = fmaf(rh, sh, -yh) + fmaf(rh, sl, rl * sh);
-        const float dx = (xh - pxh) + (xl - pxl);
-        const float dy = (yh - pyh) + (yl - pyl);
         const float sm = ph.eps_smooth * H[row + j];
-        const float d2 = fmaf(dx, dx, fmaf(dy, dy, sm * sm));
-        const float rinv = rsqrtf(d2);
-        float fk = 1.f;
-        if (rsm > 0.0) {
-            const float dsm = d2 * rinv;
-            if (dsm < frsm) {
-                const float q = dsm / frsm;
-                fk = -(3.f * q * q * q * q - 4.f * q * q * q);
-            }
-        }
+        const float sm2 = sm * sm;
         // the ring mean removed (CorrectDiskSelfgravity) from the pair
         const float dsig = ph.correct_sg ? (S[row + j] - mh) + (S_lo[row + j] - ml)
                                          : S[row + j] + S_lo[row + j];
-        const float w = dsig * (rinv * rinv * rinv * fk);
-        two_sum_add(axh, axl, w * dx);
-        two_sum_add(ayh, ayl, w * dy);
+#pragma unroll
+        for (int b = 0; b < kForceBodies32; ++b) {
+            if (b < fb.n) {
+                const float dx = (xh - pxh[b]) + (xl - pxl[b]);
+                const float dy = (yh - pyh[b]) + (yl - pyl[b]);
+                const float d2 = fmaf(dx, dx, fmaf(dy, dy, sm2));
+                const float rinv = rsqrtf(d2);
+                float fk = 1.f;
+                if (frsm[b] > 0.f) {
+                    const float dsm = d2 * rinv;
+                    if (dsm < frsm[b]) {
+                        const float q = dsm / frsm[b];
+                        fk = -(3.f * q * q * q * q - 4.f * q * q * q);
+                    }
+                }
+                const float w = dsig * (rinv * rinv * rinv * fk);
+                two_sum_add(axh[b], axl[b], w * dx);
+                two_sum_add(ayh[b], ayl[b], w * dy);
+            }
+        }
     }
-    const double ax = bsum_d((double)axh + (double)axl, red);
-    const double ay = bsum_d((double)ayh + (double)ayl, red);
-    if (threadIdx.x == 0) {
-        const double f = t.Surf_d[i] * ph.G_d;
-        const bool inner = t.Rmed_d[i] < pa;
-        double *p = partial + (size_t)blockIdx.x * 5;
-        p[0] = inner ? f * ax : 0.0;
-        p[1] = inner ? f * ay : 0.0;
-        p[2] = inner ? 0.0 : f * ax;
-        p[3] = inner ? 0.0 : f * ay;
-        p[4] = t.Surf_d[i] * ring_sum;
+    const double f = t.Surf_d[i] * ph.G_d;
+    double *p = partial + (size_t)blockIdx.x * width;
+#pragma unroll
+    for (int b = 0; b < kForceBodies32; ++b) {
+        if (b < fb.n) {
+            const double ax = bsum_d((double)axh[b] + (double)axl[b], red);
+            const double ay = bsum_d((double)ayh[b] + (double)ayl[b], red);
+            if (threadIdx.x == 0) {
+                const bool inner = t.Rmed_d[i] < fb.a[b];
+                p[5 * b + 0] = inner ? f * ax : 0.0;
+                p[5 * b + 1] = inner ? f * ay : 0.0;
+                p[5 * b + 2] = inner ? 0.0 : f * ax;
+                p[5 * b + 3] = inner ? 0.0 : f * ay;
+                p[5 * b + 4] = t.Surf_d[i] * ring_sum;
+            }
+        }
     }
+}
+
+// the rows' components, one block (one warp) per component
+__global__ void f_reduce_cols(const double *__restrict__ partial, int rows, int width,
+                              double *__restrict__ out)
+{
+    warp_compensated_rows(partial, rows, width, blockIdx.x, out);
 }
 
 // one warp per component
@@ -591,7 +629,7 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
     CKF(cudaMalloc(&alt_sigma_lo, cells * sizeof(float)));
     CKF(cudaMemset(alt_sigma_lo, 0, cells * sizeof(float)));
     for (int k = 0; k < 4; ++k) CKF(cudaMalloc(&mom[k], cells * sizeof(float)));
-    CKF(cudaMalloc(&partial, sizeof(double) * 5 * (size_t)nr));
+    CKF(cudaMalloc(&partial, sizeof(double) * 5 * kForceBodies32 * (size_t)nr));
     CKF(cudaMalloc(&red_out, sizeof(double) * (8 + 5 * kMaxBodies)));
     CKF(cudaMalloc(&d_dtmin, sizeof(unsigned int)));
     CKF(cudaMalloc(&d_bad, sizeof(unsigned long long)));
@@ -1214,19 +1252,28 @@ int Engine32::step(double dt, double t)
     return FGPU_OK;
 }
 
-// the disk force on n <= kMaxBodies bodies: every launch queued, one
-// read-back; out (host, 5 doubles per body) receives the sums
+// the disk force on n <= kMaxBodies bodies, kForceBodies32 per pass over the
+// disk, one read-back; out (host, 5 doubles per body) receives the sums
 int Engine32::disk_forces(int n, const double *x, const double *y, const double *a,
                           const double *rsm, double *out)
 {
     if (n < 0 || n > kMaxBodies) return FGPU_ERR_BAD_ARG;
     const int rows = nr - 2;
     double *dev = red_out + 8;
-    for (int k = 0; k < n; ++k) {
-        f_disk_force<<<rows, 256, 0, stream>>>(geo, tabs, phys, x[k], y[k], a[k], rsm[k],
-                                               fld[FGPU_SIGMA], sigma_lo, fld[FGPU_SCALE_HEIGHT],
-                                               partial);
-        f_reduce_rows<<<1, 32 * 5, 0, stream>>>(partial, rows, dev + 5 * k);
+    for (int b0 = 0; b0 < n; b0 += kForceBodies32) {
+        ForceBodies32 fb{};
+        fb.n = std::min(kForceBodies32, n - b0);
+        for (int b = 0; b < fb.n; ++b) {
+            fb.x[b] = x[b0 + b];
+            fb.y[b] = y[b0 + b];
+            fb.a[b] = a[b0 + b];
+            fb.rsm[b] = rsm[b0 + b];
+        }
+        const int width = 5 * fb.n;
+        f_disk_force_bodies<<<rows, 256, 0, stream>>>(geo, tabs, phys, fb, fld[FGPU_SIGMA],
+                                                      sigma_lo, fld[FGPU_SCALE_HEIGHT], partial,
+                                                      width);
+        f_reduce_cols<<<width, 32, 0, stream>>>(partial, rows, width, dev + 5 * b0);
     }
     CKF(cudaGetLastError());
     CKF(cudaMemcpyAsync(h_pinned + 16, dev, sizeof(double) * 5 * n, cudaMemcpyDeviceToHost,
@@ -1271,15 +1318,7 @@ int Engine32::keep_mass()
 
 int Engine32::disk_force(double px, double py, double pa, double rsm, double out[5])
 {
-    const int rows = nr - 2;
-    f_disk_force<<<rows, 256, 0, stream>>>(geo, tabs, phys, px, py, pa, rsm, fld[FGPU_SIGMA], sigma_lo,
-                                           fld[FGPU_SCALE_HEIGHT], partial);
-    f_reduce_rows<<<1, 32 * 5, 0, stream>>>(partial, rows, red_out);
-    CKF(cudaGetLastError());
-    CKF(cudaMemcpyAsync(h_pinned, red_out, sizeof(double) * 5, cudaMemcpyDeviceToHost, stream));
-    CKF(cudaStreamSynchronize(stream));
-    for (int k = 0; k < 5; ++k) out[k] = h_pinned[k];
-    return FGPU_OK;
+    return disk_forces(1, &px, &py, &pa, &rsm, out);
 }
 
 // Accretion onto one planet (accretion.cpp:84-480) on the FP32 state: the

@@ -92,6 +92,17 @@ __device__ __forceinline__ double flux_limiter(double a, double b, int mc)
     return 0.0;
 }
 
+// The limited slope without its constant factor: van Leer's 2ab/(a+b) less
+// the 2, MC's value as is.  The azimuthal pass multiplies the factor (2 or
+// 1, and 1/(2 dx)) into each cell's interpolation distance once, instead of
+// into every quantity's slope.
+__device__ __forceinline__ double flux_limiter_unscaled(double a, double b, int mc)
+{
+    if (mc) return flux_limiter(a, b, 1);
+    if (same_sign_nonzero(a, b)) return a * b * fast_rcp1(a + b);
+    return 0.0;
+}
+
 // exp(x) by its Taylor series through x^7 for |x| <= 1/64 (the remainder,
 // below x^8 / 8! <= 1e-19, is under half an ulp of the result), exp() beyond:
 // compression heating's exponent is a fraction of the cell's CFL number, so
@@ -664,11 +675,13 @@ __global__ void k_transport_radial(Geo g, Tables t, double dt, double omf, int m
     double sa = 0.0, sb = 0.0;
 
     // slope of ring `ring` from its down/up differences (compute_star_radial,
-    // :357-367: zero on the first and last ring)
+    // :357-367: zero on the first and last ring), without van Leer's factor 2,
+    // which the interpolation distance below carries instead of its 1/2
     auto lim = [&](int ring, double up, double down) -> double {
         if (ring <= 0 || ring >= nr - 1) return 0.0;
-        return flux_limiter(up, down, mc);
+        return flux_limiter_unscaled(up, down, mc);
     };
+    auto half = [&](double x) { return mc ? x * 0.5 : x; };
 
     // prime rings k-1 = i0-1 and k = i0 (their slopes need rings i0-2 .. i0+1)
     {
@@ -717,14 +730,14 @@ __global__ void k_transport_radial(Geo g, Tables t, double dt, double omf, int m
                 // DensityStar, then QRStar of every specific quantity
                 // base sigma* v, the factor every quantity's flux shares
                 if (up) {
-                    const double f = (t.Rmed[k] - t.Rmed[k - 1] - vdt) * 0.5;
+                    const double f = half(t.Rmed[k] - t.Rmed[k - 1] - vdt);
                     sstar = wa[NQ] + f * da[NQ];
                     const double bsv = base * sstar * v;
 #pragma unroll
                     for (int q = 0; q < NQ; ++q) flux[q] = (wa[q] + f * da[q]) * bsv;
                     flux[NQ] = bsv;
                 } else {
-                    const double f = (t.Rmed[k + 1] - t.Rmed[k] + vdt) * 0.5;
+                    const double f = half(t.Rmed[k + 1] - t.Rmed[k] + vdt);
                     sstar = wb[NQ] - f * db[NQ];
                     const double bsv = base * sstar * v;
 #pragma unroll
@@ -844,7 +857,7 @@ __device__ double block_min(double v, double *red)
 // velocity (ignored when uniform).
 template <int PER>
 __device__ void ring_advection_pass(double *S, double *W, double *D, double *F,
-                                    double *const *qrow, int nq, const double *v, double dt,
+                                    double *const *qrow, int nq, double *v, double dt,
                                     double dxtheta, double half_invdx, double dxrad_invsurf,
                                     int nz, int mc, bool uniform, double vconst)
 {
@@ -854,12 +867,26 @@ __device__ void ring_advection_pass(double *S, double *W, double *D, double *F,
     constexpr bool KEEP = PER <= 8;
     double invs[PER], cf[PER], am[KEEP ? PER : 1];
     int up[KEEP ? PER : 1];
+    // D holds the slopes without their constant factor (van Leer's 2 and
+    // 1/(2 dx)); the interpolation distance carries it: with
+    // k = 2 / (2 dx) (van Leer) or 1 / (2 dx) (MC), the distance is
+    // k (dx - v dt) or -k (dx + v dt).  The velocities are scaled by k dt
+    // once (in place: the uniform pass does not read them), so a distance
+    // costs one addition where it is recomputed.
+    const double kfac = mc ? half_invdx : 2.0 * half_invdx;
+    const double kdt = kfac * dt;
+    const double dxk = dxtheta * kfac;
+    const double cvel = dxrad_invsurf / kdt;  // dxrad S* v / Surf = cvel S* (k dt v)
+    const double vkc = vconst * kdt;
+    if (!uniform) {
+#pragma unroll
+        for (int n = 0; n < PER; ++n) v[n] *= kdt;
+    }
     auto upwind = [&](int n, int j, int &u, double &a) {
-        const double vv = uniform ? vconst : v[n];
-        const double ksi = vv * dt;
-        const bool pos = positive(vv);
+        const double vk = uniform ? vkc : v[n];
+        const bool pos = positive(vk);
         u = pos ? (j == 0 ? nz - 1 : j - 1) : j;
-        a = pos ? dxtheta - ksi : -(dxtheta + ksi);
+        a = pos ? dxk - vk : -(dxk + vk);
     };
     // DensityStar
 #pragma unroll
@@ -868,7 +895,7 @@ __device__ void ring_advection_pass(double *S, double *W, double *D, double *F,
         if (j < nz) {
             const int jp = j == nz - 1 ? 0 : j + 1;
             const int jm = j == 0 ? nz - 1 : j - 1;
-            D[j] = flux_limiter(S[jp] - S[j], S[j] - S[jm], mc) * half_invdx;
+            D[j] = flux_limiter_unscaled(S[jp] - S[j], S[j] - S[jm], mc);
             invs[n] = fast_rcp(S[j]);
         }
     }
@@ -887,7 +914,7 @@ __device__ void ring_advection_pass(double *S, double *W, double *D, double *F,
                 up[n] = u;
                 am[n] = a;
             }
-            cf[n] = dxrad_invsurf * (S[u] + a * D[u]) * (uniform ? vconst : v[n]);
+            cf[n] = cvel * (S[u] + a * D[u]) * (uniform ? vkc : v[n]);
         }
     }
     __syncthreads();
@@ -907,7 +934,7 @@ __device__ void ring_advection_pass(double *S, double *W, double *D, double *F,
             if (j < nz) {
                 const int jp = j == nz - 1 ? 0 : j + 1;
                 const int jm = j == 0 ? nz - 1 : j - 1;
-                D[j] = flux_limiter(W[jp] - W[j], W[j] - W[jm], mc) * half_invdx;
+                D[j] = flux_limiter_unscaled(W[jp] - W[j], W[j] - W[jm], mc);
             }
         }
         __syncthreads();
@@ -1470,14 +1497,25 @@ __global__ void k_accrete(Geo g, Tables t, Phys ph, AccretionSpec a, double *__r
 }
 
 // ---------------------------------------------------------------------------
-// ComputeDiskOnPlanetAccel (src/Force.cpp:23-122), with CorrectDiskSelfgravity
-// the ring mean of sigma subtracted (Force.cpp:64-66), and gas_total_mass
-// (quantities.cpp:51-74).  One CTA per active ring writes its
-// partial sums; k_reduce_rows adds them with compensation in a fixed order.
+// ComputeDiskOnPlanetAccel (src/Force.cpp:23-122) for up to kForceBodies
+// bodies in one pass over the ring: with CorrectDiskSelfgravity the ring mean
+// of sigma is subtracted (Force.cpp:64-66), and the gas mass of the ring
+// (gas_total_mass, quantities.cpp:51-74) comes along.  One CTA per active
+// ring writes, for body b, partial[5 b .. 5 b + 4] = (inner x, inner y,
+// outer x, outer y, mass) of its ring (split at Rmed < a, the body's distance
+// from the origin); k_reduce_cols adds the rings with compensation in a
+// fixed order.  Per body and cell: the separation, its smoothed inverse cube
+// (one rsqrt), Klahr's cubic factor inside r_sm, and two FMAs into the
+// sums; G and the ring's Surf multiply the ring's sums once.
 // ---------------------------------------------------------------------------
-__global__ void k_disk_force(Geo g, Tables t, Phys ph, double px, double py, double pa,
-                             double rsm, const double *__restrict__ S,
-                             const double *__restrict__ H, double *__restrict__ partial)
+struct ForceBodies {
+    int n;  // bodies in this pass (1 .. kForceBodies)
+    double x[kForceBodies], y[kForceBodies], a[kForceBodies], rsm[kForceBodies];
+};
+
+__global__ void k_disk_force_bodies(Geo g, Tables t, Phys ph, ForceBodies fb,
+                                    const double *__restrict__ S, const double *__restrict__ H,
+                                    double *__restrict__ partial, int width)
 {
     __shared__ double red[33];
     const int nz = g.nz;
@@ -1486,42 +1524,52 @@ __global__ void k_disk_force(Geo g, Tables t, Phys ph, double px, double py, dou
     double ps = 0.0;
     for (int j = threadIdx.x; j < nz; j += blockDim.x) ps += S[row + j];
     const double ring_sum = block_sum(ps, red);
-    // CorrectDiskSelfgravity (Force.cpp:64-66): the ring mean removed
     const double sigma1d = ph.correct_sg ? ring_sum / nz : 0.0;
-    double ax = 0.0, ay = 0.0, mass = 0.0;
+    const double rmed = t.Rmed[i];
+    double ax[kForceBodies], ay[kForceBodies];
+#pragma unroll
+    for (int b = 0; b < kForceBodies; ++b) ax[b] = ay[b] = 0.0;
     for (int j = threadIdx.x; j < nz; j += blockDim.x) {
         const double smooth = ph.eps_smooth * H[row + j];
-        const double xc = t.Rmed[i] * t.cosj[j];
-        const double yc = t.Rmed[i] * t.sinj[j];
-        const double cellmass = t.Surf[i] * (S[row + j] - sigma1d);
-        const double dx = xc - px, dy = yc - py;
-        const double d2 = dx * dx + dy * dy;
-        const double dsm2 = d2 + smooth * smooth;
-        const double rinv = rsqrt(dsm2);
-        const double inv3 = rinv * rinv * rinv;
-        double fk = 1.0;
-        if (rsm > 0.0) {
-            const double dsm = dsm2 * rinv;
-            if (dsm < rsm) {
-                const double q = dsm / rsm;
-                fk = -(3.0 * (q * q * q * q) - 4.0 * (q * q * q));
+        const double s2 = smooth * smooth;
+        const double xc = rmed * t.cosj[j];
+        const double yc = rmed * t.sinj[j];
+        const double dsig = S[row + j] - sigma1d;
+#pragma unroll
+        for (int b = 0; b < kForceBodies; ++b) {
+            if (b < fb.n) {
+                const double dx = xc - fb.x[b], dy = yc - fb.y[b];
+                const double dsm2 = fma(dx, dx, fma(dy, dy, s2));
+                const double rinv = rsqrt(dsm2);
+                double w = dsig * (rinv * rinv * rinv);
+                if (fb.rsm[b] > 0.0) {
+                    const double dsm = dsm2 * rinv;
+                    if (dsm < fb.rsm[b]) {
+                        const double q = dsm / fb.rsm[b];
+                        w *= -(3.0 * (q * q * q * q) - 4.0 * (q * q * q));
+                    }
+                }
+                ax[b] = fma(w, dx, ax[b]);
+                ay[b] = fma(w, dy, ay[b]);
             }
         }
-        ax += ph.G * cellmass * dx * inv3 * fk;
-        ay += ph.G * cellmass * dy * inv3 * fk;
-        mass += t.Surf[i] * S[row + j];
     }
-    ax = block_sum(ax, red);
-    ay = block_sum(ay, red);
-    mass = block_sum(mass, red);
-    if (threadIdx.x == 0) {
-        const bool inner = t.Rmed[i] < pa;
-        double *p = partial + (size_t)blockIdx.x * 5;
-        p[0] = inner ? ax : 0.0;
-        p[1] = inner ? ay : 0.0;
-        p[2] = inner ? 0.0 : ax;
-        p[3] = inner ? 0.0 : ay;
-        p[4] = mass;
+    const double gs = ph.G * t.Surf[i];
+    double *p = partial + (size_t)blockIdx.x * width;
+#pragma unroll
+    for (int b = 0; b < kForceBodies; ++b) {
+        if (b < fb.n) {
+            const double sx = block_sum(ax[b], red) * gs;
+            const double sy = block_sum(ay[b], red) * gs;
+            if (threadIdx.x == 0) {
+                const bool inner = rmed < fb.a[b];
+                p[5 * b + 0] = inner ? sx : 0.0;
+                p[5 * b + 1] = inner ? sy : 0.0;
+                p[5 * b + 2] = inner ? 0.0 : sx;
+                p[5 * b + 3] = inner ? 0.0 : sy;
+                p[5 * b + 4] = t.Surf[i] * ring_sum;
+            }
+        }
     }
 }
 
@@ -1574,6 +1622,12 @@ __global__ void k_reduce_rows(const double *__restrict__ partial, int rows, int 
 {
     const int w = threadIdx.x >> 5;
     if (w < width) warp_compensated_rows(partial, rows, width, w, out);
+}
+// the same with one block (one warp) per component, for wide records
+__global__ void k_reduce_cols(const double *__restrict__ partial, int rows, int width,
+                              double *__restrict__ out)
+{
+    warp_compensated_rows(partial, rows, width, blockIdx.x, out);
 }
 
 // NaN/Inf scan of one field: records the first bad flat index (atomicMin).
@@ -1863,12 +1917,24 @@ void launch_scale_sigma(const Launch &L, double *S, double target, const double 
     k_scale_sigma<<<blocks, 256, 0, L.stream>>>(S, n, target, mass);
 }
 
-void launch_disk_force(const Launch &L, double px, double py, double pa, double rsm,
-                       const double *S, const double *H, double *partial, double *out)
+void launch_disk_force(const Launch &L, int n, const double *px, const double *py,
+                       const double *pa, const double *rsm, const double *S, const double *H,
+                       double *partial, double *out)
 {
     const int rows = L.g.nr - 2;
-    k_disk_force<<<rows, 256, 0, L.stream>>>(L.g, L.t, L.ph, px, py, pa, rsm, S, H, partial);
-    k_reduce_rows<<<1, 32 * 5, 0, L.stream>>>(partial, rows, 5, out);
+    for (int b0 = 0; b0 < n; b0 += kForceBodies) {
+        ForceBodies fb{};
+        fb.n = std::min(kForceBodies, n - b0);
+        for (int b = 0; b < fb.n; ++b) {
+            fb.x[b] = px[b0 + b];
+            fb.y[b] = py[b0 + b];
+            fb.a[b] = pa[b0 + b];
+            fb.rsm[b] = rsm[b0 + b];
+        }
+        const int width = 5 * fb.n;
+        k_disk_force_bodies<<<rows, 256, 0, L.stream>>>(L.g, L.t, L.ph, fb, S, H, partial, width);
+        k_reduce_cols<<<width, 32, 0, L.stream>>>(partial, rows, width, out + 5 * b0);
+    }
 }
 
 void launch_check_finite(const Launch &L, const double *x, size_t n, unsigned long long *bad)
