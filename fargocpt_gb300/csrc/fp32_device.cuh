@@ -41,6 +41,33 @@ __device__ __forceinline__ void comp_add(float &hi, float &lo, float inc)
     hi = s;
 }
 
+// The star values and fluxes of the azimuthal passes with the rounding of
+// every operation fixed (an explicit FMA where the value is interpolated),
+// so that the strided and the register-blocked ring kernels, whose code the
+// compiler would otherwise contract differently, give the same bits.
+//   upwind value on the positive side: W_jm + (dx - ksi) D_jm
+//   on the negative side:              W_j  - (dx + ksi) D_j
+__device__ __forceinline__ float star_pos(float w, float d, float dx, float ksi)
+{
+    return __fmaf_rn(__fsub_rn(dx, ksi), d, w);
+}
+__device__ __forceinline__ float star_neg(float w, float d, float dx, float ksi)
+{
+    return __fmaf_rn(-__fadd_rn(dx, ksi), d, w);
+}
+// X_u + a D_u and the neighbour difference (X_u - X_u1) + a (D_u - D_u1)
+__device__ __forceinline__ float star_at(float x, float d, float a) { return __fmaf_rn(a, d, x); }
+__device__ __forceinline__ float star_diff(float xu, float xu1, float du, float du1, float a)
+{
+    return __fmaf_rn(a, __fsub_rn(du, du1), __fsub_rn(xu, xu1));
+}
+// q += c (qs dS* + S*_{j+1} dq*) of the uniform pass
+__device__ __forceinline__ float uniform_update(float q, float c, float qs, float dss, float fs,
+                                                float dqs)
+{
+    return __fadd_rn(q, __fmul_rn(c, __fmaf_rn(qs, dss, __fmul_rn(fs, dqs))));
+}
+
 // hi + lo += x with the rounding error of hi + x kept in lo (TwoSum,
 // Knuth 1969: exact for any order of magnitudes)
 __device__ __forceinline__ void two_sum_add(float &hi, float &lo, float x)
@@ -850,10 +877,10 @@ __device__ __forceinline__ void ring_pass_f(float *S, float *W, float *D, float 
         if (j < nz) {
             const int jm = j == 0 ? nz - 1 : j - 1;
             const float vv = v[n];
-            const float ksi = vv * dt;
-            const float ss =
-                ksi > 0.f ? S[jm] + (dxtheta - ksi) * D[jm] : S[j] - (dxtheta + ksi) * D[j];
-            cf(n, j) = dxrad_invsurf * ss * vv;
+            const float ksi = __fmul_rn(vv, dt);
+            const float ss = ksi > 0.f ? star_pos(S[jm], D[jm], dxtheta, ksi)
+                                       : star_neg(S[j], D[j], dxtheta, ksi);
+            cf(n, j) = __fmul_rn(__fmul_rn(dxrad_invsurf, ss), vv);
         }
     }
     __syncthreads();
@@ -880,17 +907,17 @@ __device__ __forceinline__ void ring_pass_f(float *S, float *W, float *D, float 
             const int j = tid + n * bs;
             if (j < nz) {
                 const int jm = j == 0 ? nz - 1 : j - 1;
-                const float ksi = v[n] * dt;
-                const float qs = ksi > 0.f ? W[jm] + (dxtheta - ksi) * D[jm]
-                                           : W[j] - (dxtheta + ksi) * D[j];
-                F[j] = qs * cf(n, j);
+                const float ksi = __fmul_rn(v[n], dt);
+                const float qs = ksi > 0.f ? star_pos(W[jm], D[jm], dxtheta, ksi)
+                                           : star_neg(W[j], D[j], dxtheta, ksi);
+                F[j] = __fmul_rn(qs, cf(n, j));
             }
         }
         __syncthreads();
 #pragma unroll
         for (int n = 0; n < PER; ++n) {
             const int j = tid + n * bs;
-            if (j < nz) Q[j] += F[j] - F[j == nz - 1 ? 0 : j + 1];
+            if (j < nz) Q[j] = __fadd_rn(Q[j], __fsub_rn(F[j], F[j == nz - 1 ? 0 : j + 1]));
         }
     }
     __syncthreads();
@@ -952,8 +979,8 @@ __device__ __forceinline__ void ring_pass_uniform_f(float *S, float *W, float *D
         if (j < nz) {
             const int jp = j == nz - 1 ? 0 : j + 1, jm = j == 0 ? nz - 1 : j - 1;
             const int u = pos ? jm : j, u1 = pos ? j : jp;
-            dss(n, j) = (S[u] - S[u1]) + a * (D[u] - D[u1]);
-            F[j] = S[u1] + a * D[u1];
+            dss(n, j) = star_diff(S[u], S[u1], D[u], D[u1], a);
+            F[j] = star_at(S[u1], D[u1], a);
         }
     }
     __syncthreads();
@@ -981,9 +1008,9 @@ __device__ __forceinline__ void ring_pass_uniform_f(float *S, float *W, float *D
             if (j < nz) {
                 const int jp = j == nz - 1 ? 0 : j + 1, jm = j == 0 ? nz - 1 : j - 1;
                 const int u = pos ? jm : j, u1 = pos ? j : jp;
-                const float qs = W[u] + a * D[u];
-                const float dqs = (W[u] - W[u1]) + a * (D[u] - D[u1]);
-                Q[j] += c * (qs * dss(n, j) + F[j] * dqs);
+                const float qs = star_at(W[u], D[u], a);
+                const float dqs = star_diff(W[u], W[u1], D[u], D[u1], a);
+                Q[j] = uniform_update(Q[j], c, qs, dss(n, j), F[j], dqs);
             }
         }
         __syncthreads();
@@ -993,7 +1020,7 @@ __device__ __forceinline__ void ring_pass_uniform_f(float *S, float *W, float *D
         const int j = tid + n * bs;
         if (j < nz) {
             float sn = S[j];
-            comp_add(sn, slo[n], c * dss(n, j));
+            comp_add(sn, slo[n], __fmul_rn(c, dss(n, j)));
             S[j] = sn;
         }
     }
@@ -1141,6 +1168,260 @@ __device__ __forceinline__ void azimuthal_ring(const GeoF &g, const TablesF &t, 
         const int j = tid + n * bs;
         if (j < nz) S_lo[row + j] = W[src[n]];
     }
+    // the caller may reuse smf for the next ring
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// The same ring transport with the ring in registers: thread tid owns the
+// contiguous cells j0 = tid PER .. j0 + PER - 1 (nz = PER blockDim.x, PER a
+// multiple of 4), loads and stores them as 128-bit words, and computes every
+// stencil from registers.  The only cross-thread step per transported
+// quantity is one exchange of segment ends: each thread publishes its first
+// two and last two values, and after one barrier reads the two cells left of
+// its segment and the two right of it; with them it forms the slopes of
+// cells j0 - 1 .. j0 + PER and the fluxes of faces j0 .. j0 + PER itself, so
+// no slope or flux crosses threads.  The exchange area is double-buffered:
+// a thread writing buffer b for the next exchange has passed the barrier of
+// the exchange in between, which every thread reaches only after reading
+// buffer b, so no write overtakes a read.  Every cell's arithmetic is the
+// strided kernel's (ring_pass_f, ring_pass_uniform_f, the exact-sum ring mean,
+// the shift), expression for expression, so both give the same bits.
+//
+// Shared memory (rb_smem_floats): the NQ transported rows (each thread's
+// segment; their shifted copy-out reads across the ring), one spare row for
+// sigma and its low part at the shift, and 2 x 5 x blockDim.x floats for the
+// exchanges.
+// ---------------------------------------------------------------------------
+// threads per ring block of the register-blocked kernel: 16 cells per thread
+// need more registers than 128 (the budget at 512 threads)
+__host__ __device__ constexpr int rb_max_threads(int per) { return per >= 16 ? 384 : 512; }
+__host__ __device__ constexpr size_t rb_smem_floats(int nz, int nq, int threads)
+{
+    return (size_t)(nq + 1) * (size_t)nz + (size_t)10 * (size_t)threads;
+}
+
+template <int PER, int NQ>
+__device__ __forceinline__ void azimuthal_ring_rb(const GeoF &g, const TablesF &t, double dt,
+                                                  int mc, int fast, const float *__restrict__ dv,
+                                                  float *m0, float *m1, float *m2, float *m3,
+                                                  float *E, float *S, float *S_lo, int i,
+                                                  float *smf, float *redf, long long *redl)
+{
+    static_assert(PER % 4 == 0 && PER >= 4, "segments of whole 128-bit words");
+    const int nz = g.nz;  // == PER * blockDim.x
+    const int tid = threadIdx.x, bs = blockDim.x;
+    const size_t row = (size_t)i * nz;
+    const int j0 = tid * PER;
+    const int left = tid == 0 ? bs - 1 : tid - 1, right = tid == bs - 1 ? 0 : tid + 1;
+    float *qsm = smf;                               // NQ rows
+    float *spare = smf + (size_t)NQ * nz;           // one row
+    float *xs = spare + nz;                         // [2][5][bs]
+    float *grow[5] = {m0 + row, m1 + row, m2 + row, m3 + row, E + row};
+    int buf = 0;
+    // publishes a0, a1 (first two), a2, a3 (last two) and a4; returns the
+    // left neighbour's last two (l2, l3), the right neighbour's first two
+    // (r0, r1) and its a4 (r4)
+    auto exchange = [&](float a0, float a1, float a2, float a3, float a4, float &l2, float &l3,
+                        float &r0, float &r1, float &r4) {
+        float *x = xs + (size_t)buf * 5 * bs;
+        x[tid] = a0;
+        x[bs + tid] = a1;
+        x[2 * bs + tid] = a2;
+        x[3 * bs + tid] = a3;
+        x[4 * bs + tid] = a4;
+        __syncthreads();
+        l2 = x[2 * bs + left];
+        l3 = x[3 * bs + left];
+        r0 = x[right];
+        r1 = x[bs + right];
+        r4 = x[4 * bs + right];
+        buf ^= 1;
+    };
+    auto load_seg = [&](const float *src, float *dst) {
+#pragma unroll
+        for (int k = 0; k < PER / 4; ++k) {
+            const float4 w = reinterpret_cast<const float4 *>(src + j0)[k];
+            dst[4 * k] = w.x;
+            dst[4 * k + 1] = w.y;
+            dst[4 * k + 2] = w.z;
+            dst[4 * k + 3] = w.w;
+        }
+    };
+    auto store_seg = [&](float *dst, const float *src) {
+#pragma unroll
+        for (int k = 0; k < PER / 4; ++k)
+            reinterpret_cast<float4 *>(dst + j0)[k] =
+                make_float4(src[4 * k], src[4 * k + 1], src[4 * k + 2], src[4 * k + 3]);
+    };
+
+    // the transported rows into shared memory (coalesced), the own segment of
+    // v_phi and of the sigma pair into registers
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+        for (int j = tid; j < nz; j += bs) qsm[(size_t)q * nz + j] = grow[q][j];
+    float v[PER + 1], s[PER], slo[PER];
+    load_seg(dv + row, v);
+    load_seg(S + row, s);
+    load_seg(S_lo + row, slo);
+    float amax = 0.f;
+#pragma unroll
+    for (int n = 0; n < PER; ++n) amax = fmaxf(amax, fabsf(v[n]));
+    // ring mean of v_phi (exact integer sum: the same bits for any ownership)
+    // and the FARGO shift phase in FP64 (:174-236)
+    const int ks = exact_sum_scale(amax, nz, redf);
+    long long part = 0;
+#pragma unroll
+    for (int n = 0; n < PER; ++n) part += to_fixed(v[n], ks);
+    const double mean_dv = exact_sum_result(part, ks, redl) / (double)nz;
+    const double vmean = (t.Vref_d[i] - t.Rmed_d[i] * g.omega_frame) + mean_dv;
+    const double Ntilde = vmean * t.InvRmed_d[i] * dt * g.invdphi_d;
+    const double Nround = floor(Ntilde + 0.5);
+    const int nshift = (int)Nround;
+    const float vt = (float)((Ntilde - Nround) * t.Rmed_d[i] * (1.0 / dt) * g.dphi_d);
+    const float mdv = (float)mean_dv;
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        float vres = v[n] - mdv;
+        if (!fast) vres = vt + vres;
+        v[n] = vres;
+    }
+    const float dxtheta = g.dphi * t.Rmed[i];
+    const float half_invdx = 0.5f / dxtheta;
+    const float dxrad = t.DRsup[i] * (float)dt;
+    const float invsurf = t.InvSurf[i];
+    const float fdt = (float)dt;
+    const float dxrad_invsurf = dxrad * invsurf;
+    __syncthreads();  // the staged rows are complete
+
+    // values of cells j0 - 2 .. j0 + PER + 1 at index c + 2; slopes of cells
+    // j0 - 1 .. j0 + PER at index c + 1
+    float X[PER + 4], D[PER + 2], invs[PER];
+    auto slopes = [&]() {
+#pragma unroll
+        for (int c = -1; c <= PER; ++c)
+            D[c + 1] = lim_f(X[c + 3] - X[c + 2], X[c + 2] - X[c + 1], mc) * half_invdx;
+    };
+    auto sigma_ends = [&](float a4, float &r4) {
+        float l2, l3, r0, r1;
+        exchange(s[0], s[1], s[PER - 2], s[PER - 1], a4, l2, l3, r0, r1, r4);
+        X[0] = l2;
+        X[1] = l3;
+#pragma unroll
+        for (int n = 0; n < PER; ++n) X[n + 2] = s[n];
+        X[PER + 2] = r0;
+        X[PER + 3] = r1;
+    };
+    auto specific = [&](const float *q) {
+#pragma unroll
+        for (int n = 0; n < PER; ++n) X[n + 2] = q[n] * invs[n];
+        float l2, l3, r0, r1, r4;
+        exchange(X[2], X[3], X[PER], X[PER + 1], 0.f, l2, l3, r0, r1, r4);
+        X[0] = l2;
+        X[1] = l3;
+        X[PER + 2] = r0;
+        X[PER + 3] = r1;
+    };
+
+    // QuantitiesAdvection with the residual velocity (ring_pass_f)
+    {
+        float cf[PER + 1];
+        sigma_ends(v[0], v[PER]);  // face j0 + PER takes the right neighbour's velocity
+        slopes();
+#pragma unroll
+        for (int n = 0; n < PER; ++n) invs[n] = __frcp_rn(s[n]);
+#pragma unroll
+        for (int f = 0; f <= PER; ++f) {
+            const float vv = v[f];
+            const float ksi = __fmul_rn(vv, fdt);
+            const float ss = ksi > 0.f ? star_pos(X[f + 1], D[f], dxtheta, ksi)
+                                       : star_neg(X[f + 2], D[f + 1], dxtheta, ksi);
+            cf[f] = __fmul_rn(__fmul_rn(dxrad_invsurf, ss), vv);
+        }
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            float qv[PER];
+            load_seg(qsm + (size_t)q * nz, qv);
+            specific(qv);
+            slopes();
+            float F[PER + 1];
+#pragma unroll
+            for (int f = 0; f <= PER; ++f) {
+                const float ksi = __fmul_rn(v[f], fdt);
+                const float qs = ksi > 0.f ? star_pos(X[f + 1], D[f], dxtheta, ksi)
+                                           : star_neg(X[f + 2], D[f + 1], dxtheta, ksi);
+                F[f] = __fmul_rn(qs, cf[f]);
+            }
+#pragma unroll
+            for (int n = 0; n < PER; ++n) qv[n] = __fadd_rn(qv[n], __fsub_rn(F[n], F[n + 1]));
+            store_seg(qsm + (size_t)q * nz, qv);
+        }
+#pragma unroll
+        for (int n = 0; n < PER; ++n) comp_add(s[n], slo[n], cf[n] - cf[n + 1]);
+    }
+    // the uniform pass in difference form (ring_pass_uniform_f)
+    if (fast) {
+        const float ksi = vt * fdt;
+        const bool pos = ksi > 0.f;
+        const float a = pos ? dxtheta - ksi : -(dxtheta + ksi);
+        const float c = dxrad * vt * invsurf;
+        float dss[PER], Fs[PER];
+        float unused;
+        sigma_ends(0.f, unused);
+        slopes();
+#pragma unroll
+        for (int n = 0; n < PER; ++n) {
+            invs[n] = __frcp_rn(s[n]);
+            // cells u (upwind of face j) and u1 (of face j + 1): n - 1 and n
+            // for a positive shift, n and n + 1 otherwise (X index + 2, D
+            // index + 1); both candidates are read and one is selected, so
+            // the arrays stay in registers
+            const float xu = pos ? X[n + 1] : X[n + 2], xu1 = pos ? X[n + 2] : X[n + 3];
+            const float du = pos ? D[n] : D[n + 1], du1 = pos ? D[n + 1] : D[n + 2];
+            dss[n] = star_diff(xu, xu1, du, du1, a);
+            Fs[n] = star_at(xu1, du1, a);
+        }
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            float qv[PER];
+            load_seg(qsm + (size_t)q * nz, qv);
+            specific(qv);
+            slopes();
+#pragma unroll
+            for (int n = 0; n < PER; ++n) {
+                const float xu = pos ? X[n + 1] : X[n + 2], xu1 = pos ? X[n + 2] : X[n + 3];
+                const float du = pos ? D[n] : D[n + 1], du1 = pos ? D[n + 1] : D[n + 2];
+                const float qs = star_at(xu, du, a);
+                const float dqs = star_diff(xu, xu1, du, du1, a);
+                qv[n] = uniform_update(qv[n], c, qs, dss[n], Fs[n], dqs);
+            }
+            store_seg(qsm + (size_t)q * nz, qv);
+        }
+#pragma unroll
+        for (int n = 0; n < PER; ++n) comp_add(s[n], slo[n], __fmul_rn(c, dss[n]));
+    }
+
+    // the integer shift (AdvectSHIFT, :238-268): cell j takes cell j - nshift,
+    // copied out in the strided order so that both sides stay coalesced
+    const int ns = nshift % nz;
+    auto src_of = [&](int j) {
+        int ji = j - ns;
+        if (ji < 0) ji += nz;
+        else if (ji >= nz) ji -= nz;
+        return ji;
+    };
+    __syncthreads();  // every segment of the rows is final
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+        for (int j = tid; j < nz; j += bs) grow[q][j] = qsm[(size_t)q * nz + src_of(j)];
+    store_seg(spare, s);
+    __syncthreads();
+    for (int j = tid; j < nz; j += bs) S[row + j] = spare[src_of(j)];
+    __syncthreads();
+    // the low part of sigma moves with it
+    store_seg(spare, slo);
+    __syncthreads();
+    for (int j = tid; j < nz; j += bs) S_lo[row + j] = spare[src_of(j)];
     // the caller may reuse smf for the next ring
     __syncthreads();
 }

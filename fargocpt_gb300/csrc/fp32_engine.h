@@ -276,6 +276,8 @@ class Engine32 {
     double *h_pinned = nullptr;
     int per = 4, az_block = 128;
     size_t az_smem = 0;
+    int rb_per = 0;      // register-blocked azimuthal kernel: cells per thread (0: strided)
+    size_t rb_smem = 0;
     bool az_stage = false;
     bool visc_recompute = false;  // c_s, H, nu before the final hooks (adiabatic)
     float *corr_phi = nullptr, *corr_r = nullptr;  // StabilizeViscosity factors

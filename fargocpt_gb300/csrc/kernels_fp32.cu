@@ -32,6 +32,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -151,6 +152,22 @@ __global__ void __launch_bounds__(512) f_transport_azimuthal(GeoF g, TablesF t, 
     __shared__ long long redl[33];
     azimuthal_ring<PER, NQ, STAGE>(g, t, dt, mc, fast, dv, m0, m1, m2, m3, E, S, S_lo,
                                    blockIdx.x, smf, redf, redl);
+}
+
+// the register-blocked ring transport (azimuthal_ring_rb): nz = PER x blockDim.x
+template <int PER, int NQ>
+__global__ void __launch_bounds__(rb_max_threads(PER)) f_transport_azimuthal_rb(GeoF g, TablesF t, double dt,
+                                                                int mc, int fast,
+                                                                const float *__restrict__ dv,
+                                                                float *m0, float *m1, float *m2,
+                                                                float *m3, float *E, float *S,
+                                                                float *S_lo)
+{
+    extern __shared__ __align__(16) float smf[];
+    __shared__ float redf[33];
+    __shared__ long long redl[33];
+    azimuthal_ring_rb<PER, NQ>(g, t, dt, mc, fast, dv, m0, m1, m2, m3, E, S, S_lo, blockIdx.x,
+                               smf, redf, redl);
 }
 
 __global__ void f_pressure(GeoF g, TablesF t, PhysF ph, const float *__restrict__ S,
@@ -790,6 +807,51 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
             return FGPU_ERR_CUDA;
         }
     }
+    // the register-blocked kernel where the ring splits into whole 128-bit
+    // segments: the shortest segment of 4, 8, 12 or 16 cells whose thread
+    // count stays within the kernel's bound (384 for 16 cells, else 512;
+    // the most warps per ring measured fastest: 0.59 ms with 12 cells and
+    // 512 threads on a 6144-cell ring against 0.79 ms with 16 and 384), unless
+    // FARGO_GB300_AZIMUTHAL asks for "strided" or "blocked<PER>"
+    rb_per = 0;
+    {
+        const char *env = getenv("FARGO_GB300_AZIMUTHAL");
+        const std::string want = env ? env : "";
+        auto fits = [&](int pc, int lo) {
+            if (nz % pc != 0) return false;
+            const int th = nz / pc;
+            return th >= lo && th <= rb_max_threads(pc) &&
+                   rb_smem_floats(nz, nq, th) * sizeof(float) <= kMaxRingSmem;
+        };
+        if (want.rfind("blocked", 0) == 0) {
+            // an explicit request is honoured or refused, never replaced
+            const int pc = atoi(want.c_str() + 7);
+            if ((pc == 4 || pc == 8 || pc == 12 || pc == 16) && fits(pc, 1)) {
+                rb_per = pc;
+            } else {
+                err = "FARGO_GB300_AZIMUTHAL=" + want + " does not fit this ring";
+                return FGPU_ERR_UNSUPPORTED;
+            }
+        } else if (want != "strided") {
+            for (int pc : {4, 8, 12, 16}) {
+                if (!rb_per && fits(pc, 32)) rb_per = pc;
+            }
+        }
+    }
+    if (rb_per) {
+        rb_smem = rb_smem_floats(nz, nq, nz / rb_per) * sizeof(float);
+        const void *rb_kernels[8] = {
+            (const void *)f_transport_azimuthal_rb<4, 4>, (const void *)f_transport_azimuthal_rb<8, 4>,
+            (const void *)f_transport_azimuthal_rb<12, 4>, (const void *)f_transport_azimuthal_rb<16, 4>,
+            (const void *)f_transport_azimuthal_rb<4, 5>, (const void *)f_transport_azimuthal_rb<8, 5>,
+            (const void *)f_transport_azimuthal_rb<12, 5>, (const void *)f_transport_azimuthal_rb<16, 5>};
+        for (const void *fn : rb_kernels) {
+            if (raise_smem_limit(fn, rb_smem) != cudaSuccess) {
+                err = "cannot reserve shared memory for the FP32 azimuthal kernel";
+                return FGPU_ERR_CUDA;
+            }
+        }
+    }
 
     CKF(cudaDeviceSynchronize());
     return FGPU_OK;
@@ -1182,11 +1244,28 @@ int Engine32::transport(double dt)
         else if (per == 12) AZ32(12, NQ, false);         \
         else AZ32(16, NQ, false);                        \
     }
-        if (adi) {
+#define AZRB(P, NQ)                                                                              \
+    f_transport_azimuthal_rb<P, NQ><<<nr, nz / P, rb_smem, stream>>>(                            \
+        geo, tabs, dt, phys.limiter_mc, phys.fast_transport, s.dv, mom[0], mom[1], mom[2],      \
+        mom[3], alt_e, alt_sigma, alt_sigma_lo)
+#define AZRB_NQ(NQ)                         \
+    if (rb_per == 4) AZRB(4, NQ);           \
+    else if (rb_per == 8) AZRB(8, NQ);      \
+    else if (rb_per == 12) AZRB(12, NQ);    \
+    else AZRB(16, NQ);
+        if (rb_per) {
+            if (adi) {
+                AZRB_NQ(5)
+            } else {
+                AZRB_NQ(4)
+            }
+        } else if (adi) {
             AZ32_NQ(5)
         } else {
             AZ32_NQ(4)
         }
+#undef AZRB_NQ
+#undef AZRB
 #undef AZ32_NQ
 #undef AZ32
     }

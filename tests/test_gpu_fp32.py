@@ -206,3 +206,51 @@ def test_fp32_rotating_frame_against_fp64_form():
     assert rel_linf(engs[1].get_field("SIGMA"), engs[0].get_field("SIGMA")) <= 1e-5
     assert rel_linf(engs[1].get_field("V_AZIMUTHAL"), engs[0].get_field("V_AZIMUTHAL")) <= 1e-5
 
+
+
+@pytest.mark.parametrize("naz,per", [(384, 4), (384, 12), (768, 8), (1536, 16), (6144, 12),
+                                     (6144, 16)])
+@pytest.mark.parametrize("adiabatic,fargo,mc", [(False, 1, 0), (True, 1, 0), (True, 0, 1)])
+def test_register_blocked_ring_pass_matches_strided(naz, per, adiabatic, fargo, mc,
+                                                     monkeypatch):
+    """The register-blocked azimuthal pass (contiguous segments of `per`
+    cells, one exchange of segment ends per quantity) against the strided
+    pass: every cell's arithmetic is the same, so the fields after the steps
+    are bit-identical, with FARGO (residual and uniform passes and the integer
+    shift) and with standard transport and the MC limiter."""
+    from gpu_cases import initial_state, load, make_params
+
+    from fargocpt_gb300.engine import Engine, grid_radii
+
+    params, d = make_params(16, naz, adiabatic=adiabatic, precision=1, fast_transport=fargo,
+                            flux_limiter=mc)
+    radii = grid_radii(d["radial_spacing"], d["rmin"], d["rmax"], d["nrad"])
+    st = initial_state(d, radii, seed=21)
+    bodies = [(0.0, 0.0, 1.0, 0.0, 0.0), (1.0, 0.3, 1e-3, 0.0, math.hypot(1.0, 0.3))]
+    out = []
+    for variant in ("strided", f"blocked{per}"):
+        monkeypatch.setenv("FARGO_GB300_AZIMUTHAL", variant)
+        e = Engine(params, radii)
+        load(e, st, bodies)
+        e.apply_boundary_condition(0.0, 0.0, False)
+        t = 0.0
+        for _ in range(6):
+            dt = e.condition_cfl()
+            e.step_euler(dt, t)
+            t += dt
+        out.append({f: e.get_field(f) for f in EVOLVED})
+        e.close()
+    for f in EVOLVED:
+        assert np.array_equal(out[0][f], out[1][f]), f
+
+
+def test_register_blocked_request_that_does_not_fit_is_refused(monkeypatch):
+    from gpu_cases import make_params
+
+    from fargocpt_gb300.engine import Engine, EngineError, grid_radii
+
+    params, d = make_params(16, 392, precision=1)   # 392 cells: no 12-cell segments
+    radii = grid_radii(d["radial_spacing"], d["rmin"], d["rmax"], d["nrad"])
+    monkeypatch.setenv("FARGO_GB300_AZIMUTHAL", "blocked12")
+    with pytest.raises(EngineError, match="UNSUPPORTED"):
+        Engine(params, radii)
