@@ -1462,10 +1462,16 @@ __device__ __forceinline__ void finish_cell(
         vr_out[c] = 0.f;
     } else {
         const size_t cm = CELL(i - 1, j);
-        vr_out[c] = __fdividef(m0[cm] + m1[c], S_t[cm] + s);
+        vr_out[c] = __fdiv_rn(m0[cm] + m1[c], S_t[cm] + s);
     }
     const size_t cjm = CELL(i, jprev(j, nz));
-    dv_out[c] = __fdividef(m2[cjm] + m3[c], S_t[cjm] + s) * t.InvRmed[i];
+    // the residual angular momenta were formed as sigma (dv Rmed) with the
+    // FP32 Rmed of the ring: dividing by that same Rmed returns dv without
+    // bias, where multiplying by the FP32 1/Rmed would scale every ring's
+    // residual by Rmed 1/Rmed - 1 (up to ~6e-8) in every step, a drift that
+    // accumulates over tens of thousands of steps; the divisions are
+    // correctly rounded for the same reason
+    dv_out[c] = __fdiv_rn(m2[cjm] + m3[c], __fmul_rn(S_t[cjm] + s, t.Rmed[i]));
     const bool floored = s < ph.sigma_min;
     const float sf = floored ? ph.sigma_min : s;
     S_out[c] = sf;
