@@ -451,7 +451,8 @@ def engine_params(case, consts, temp_unit):
         art_visc_dissipation=1, flux_limiter=1 if k.get("FluxLimiter", "") == "mc" else 0,
         fast_transport=1 if k["Transport"].lower().startswith("f") else 0,
         heating_viscous=1, cooling_beta=1 if k.get("CoolingBetaLocal") == "yes" else 0,
-        cooling_beta_reference=BETA_REF["zero"], damping=1,
+        cooling_beta_reference=BETA_REF["zero"],
+        damping=int(str(k.get("Damping", "no")).lower() in ("yes", "true", "1")),
         damping_inner=[damp("DampingVRadialInner"), damp("DampingVAzimuthalInner"),
                        damp("DampingSurfaceDensityInner"), damp("DampingEnergyInner")],
         damping_outer=[damp("DampingVRadialOuter"), damp("DampingVAzimuthalOuter"),
@@ -495,6 +496,11 @@ def engine_params(case, consts, temp_unit):
         profile_cutoff_point_outer=1.0e300, profile_cutoff_width_outer=1.0,
         profile_cutoff_point_inner=0.0, profile_cutoff_width_inner=1.0,
         temperature_cgs_to_code=1.0 / temp_unit,
+        # parameters::VISCOUS_ACCRETION: a planet accreting with the viscous
+        # profile or the viscous v_radial hook (planetary_system.cpp:255-257,
+        # Interpret.cpp:704-707)
+        viscous_accretion=int(str(case.get("planet_keys", {}).get("accretion method", ""))
+                              == "viscous" or vi == "viscous" or vo == "viscous"),
         keep_disk_mass_constant=int(str(k.get("KeepDiskMassConstant", "no")) == "yes"),
         correct_disk_selfgravity=int(str(k.get("CorrectDiskSelfgravity", "yes")) == "yes"),
     )
