@@ -808,10 +808,13 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
         }
     }
     // the register-blocked kernel where the ring splits into whole 128-bit
-    // segments: the shortest segment of 4, 8, 12 or 16 cells whose thread
-    // count stays within the kernel's bound (384 for 16 cells, else 512;
-    // the most warps per ring measured fastest: 0.59 ms with 12 cells and
-    // 512 threads on a 6144-cell ring against 0.79 ms with 16 and 384), unless
+    // segments: 12 cells per thread where that leaves 128 .. 512 threads,
+    // else the shortest segment of 4, 8 or 16 cells that fits the kernel's
+    // thread bound (384 for 16 cells, else 512).  Measured FP32 steps:
+    // 6144-cell rings 2.34 ms with 12 cells (16: 2.54, strided 2.66),
+    // 3072: 0.569 ms (8: 0.597, 16: 0.601, strided 0.664), 1536: 0.269 ms
+    // (8: 0.275, 4: 0.283, strided 0.275), 384: 0.127 ms with 4 (8: 0.139,
+    // 12: 0.152, strided 0.137).  Unless
     // FARGO_GB300_AZIMUTHAL asks for "strided" or "blocked<PER>"
     rb_per = 0;
     {
@@ -833,7 +836,8 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
                 return FGPU_ERR_UNSUPPORTED;
             }
         } else if (want != "strided") {
-            for (int pc : {4, 8, 12, 16}) {
+            if (fits(12, 128)) rb_per = 12;
+            for (int pc : {4, 8, 16}) {
                 if (!rb_per && fits(pc, 32)) rb_per = pc;
             }
         }
