@@ -40,6 +40,7 @@ struct fgpu_engine {
     int radial_chunk = 16;
 
     double *tables_mem = nullptr;
+    float *pair_mem = nullptr;  // Rmed, cos, sin as float pairs
     Tables tabs{};
     double *damp_mem = nullptr;
     int *damp_rings = nullptr;
@@ -632,6 +633,25 @@ static int setup_tables(fgpu_engine *eng, const double *radii)
     t.Ra3IDRmed = D(RA3IDRMED); t.F43 = D(F43); t.CrPp1 = D(CRPP1); t.CrPp2 = D(CRPP2);
     t.CrRr1 = D(CRRR1); t.CrRr2 = D(CRRR2); t.CrRp = D(CRRP); t.CrScale = D(CRSCALE);
     t.cosj = tc; t.sinj = tc + nz;
+    {
+        // Rmed, cos and sin as float pairs hi + lo
+        std::vector<float> pr((size_t)2 * R + (size_t)4 * nz);
+        auto split = [](double v, float &h, float &l) {
+            h = (float)v;
+            l = (float)(v - (double)h);
+        };
+        for (int n = 0; n < R; ++n) split(T(RMED)[n], pr[(size_t)n], pr[(size_t)R + n]);
+        float *c = pr.data() + 2 * (size_t)R;
+        for (int j = 0; j < nz; ++j) {
+            split(cs[j], c[j], c[(size_t)nz + j]);
+            split(sn[j], c[2 * (size_t)nz + j], c[3 * (size_t)nz + j]);
+        }
+        CK(cudaMalloc(&eng->pair_mem, sizeof(float) * pr.size()));
+        CK(cudaMemcpy(eng->pair_mem, pr.data(), sizeof(float) * pr.size(), cudaMemcpyHostToDevice));
+        const float *q = eng->pair_mem;
+        t.RmedHi = q; t.RmedLo = q + R;
+        t.cosHi = q + 2 * R; t.cosLo = t.cosHi + nz; t.sinHi = t.cosLo + nz; t.sinLo = t.sinHi + nz;
+    }
 
     // boundary hooks
     BcSpec &bc = eng->bc;
@@ -956,6 +976,7 @@ extern "C" int fgpu_destroy(fgpu_engine *eng)
     for (int k = 0; k < 4; ++k) cudaFree(eng->mom[k]);
     cudaFree(eng->ring_ws); cudaFree(eng->tables_mem); cudaFree(eng->damp_mem);
     cudaFree(eng->damp_rings); cudaFree(eng->partial); cudaFree(eng->red_out);
+    cudaFree(eng->pair_mem);
     cudaFree(eng->com_mem);
     cudaFree(eng->d_dtmin); cudaFree(eng->d_bad);
     cudaFree(eng->corr_phi); cudaFree(eng->corr_r);
@@ -1169,6 +1190,15 @@ extern "C" int fgpu_set_bodies(fgpu_engine *eng, int n, const fgpu_body *bodies,
     b.ix = ix;
     b.iy = iy;
     b.omega_frame = omega_frame;
+    auto split = [](double v, float &h, float &l) {
+        h = (float)v;
+        l = (float)(v - (double)h);
+    };
+    for (int k = 0; k < n; ++k) {
+        split(b.x[k], b.xh[k], b.xl[k]);
+        split(b.y[k], b.yh[k], b.yl[k]);
+        split(-eng->p.G * b.m[k], b.gmh[k], b.gml[k]);
+    }
     if (eng->e32) {
         if (omega_frame != 0.0 && eng->batch_owned) {
             eng->err = "the batched form runs in the fixed (non-rotating) frame";

@@ -43,6 +43,8 @@ struct Tables {
     const double *CrRp;        // 1 / (dphi dphi Ra[i])
     const double *CrScale;     // RadialViscosityFactor / (0.5 (Rmed[i] + Rmed[i-1]))
     const double *cosj, *sinj; // cos / sin (dphi j)
+    // the same as float pairs hi + lo (for the pair-arithmetic kernels)
+    const float *RmedHi, *RmedLo, *cosHi, *cosLo, *sinHi, *sinLo;
 };
 
 struct Geo {
@@ -74,6 +76,9 @@ struct Phys {
 struct Bodies {
     int n;
     double x[kMaxBodies], y[kMaxBodies], m[kMaxBodies], rsm[kMaxBodies], a[kMaxBodies];
+    // positions and -G m as float pairs hi + lo, split on the host
+    float xh[kMaxBodies], xl[kMaxBodies], yh[kMaxBodies], yl[kMaxBodies];
+    float gmh[kMaxBodies], gml[kMaxBodies];
     double ix, iy;        // indirect term
     double omega_frame;
 };

@@ -7,6 +7,7 @@
 // rate is low, so every FP64 operation is done once and intermediates that
 // several neighbours reuse go through HBM/L2 instead of being recomputed.
 #include "hydro.cuh"
+#include "fp64_pair.cuh"
 #include "kernels.h"
 #include "reduce.cuh"
 
@@ -133,7 +134,16 @@ __device__ __forceinline__ double temperature_floor(double e, double sigma, cons
 }
 
 // ---------------------------------------------------------------------------
-// CalculateNbodyPotential, src/Pframeforce.cpp:21-86
+// CalculateNbodyPotential, src/Pframeforce.cpp:21-86.  The central object's
+// term -G M / sqrt(d^2 + eps^2) stays in FP64: the radial force is a small
+// difference of neighbouring potentials that gravity, pressure and the
+// centrifugal term nearly cancel, and v_r, itself small, inherits the error
+// of the dominant term amplified by both cancellations (with this term in
+// float pairs, 2^-46, v_r on the 512 x 1536 disk drifted to 1.1e-10 of its
+// largest value in 100 steps).  The other bodies' terms, at most ~1e-3 of it
+// away from a body, are formed in float-pair arithmetic (fp64_pair.cuh) and
+// summed as a pair: about 60 FP32 operations per body and cell instead of
+// about 15 FP64 ones, which GB300 issues 64 times slower.
 // ---------------------------------------------------------------------------
 __global__ void k_potential(Geo g, Tables t, Phys ph, Bodies b, const double *__restrict__ H,
                             double *__restrict__ pot)
@@ -142,18 +152,18 @@ __global__ void k_potential(Geo g, Tables t, Phys ph, Bodies b, const double *__
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.y;
     if (j >= nz) return;
+    const double smooth = ph.eps_smooth * H[CELL(i, j)];
     const double x = t.Rmed[i] * t.cosj[j];
     const double y = t.Rmed[i] * t.sinj[j];
-    const double smooth = ph.eps_smooth * H[CELL(i, j)];
     double acc = 0.0;
-    for (int k = 0; k < b.n; ++k) {
-        const double dx = x - b.x[k];
-        const double dy = y - b.y[k];
-        const double dist_2 = dx * dx + dy * dy;
-        const double d2 = dist_2 + smooth * smooth;
+    if (b.n > 0) {
+        // the central object in FP64, the reference's expressions
+        const double dx = x - b.x[0];
+        const double dy = y - b.y[0];
+        const double d2 = (dx * dx + dy * dy) + smooth * smooth;
         const double inv_d = rsqrt(d2);
         double fk = 1.0;
-        const double r_sm = b.rsm[k];
+        const double r_sm = b.rsm[0];
         if (r_sm > 0.0) {
             const double d_sm = d2 * inv_d;
             if (d_sm < r_sm) {
@@ -161,10 +171,33 @@ __global__ void k_potential(Geo g, Tables t, Phys ph, Bodies b, const double *__
                 fk = q * q * q * q - 2.0 * (q * q * q) + 2.0 * q;
             }
         }
-        acc += -ph.G * b.m[k] * inv_d * fk;
+        acc = -ph.G * b.m[0] * inv_d * fk;
     }
-    acc += -b.ix * x - b.iy * y;
-    pot[CELL(i, j)] = acc;
+    const f2 rm{t.RmedHi[i], t.RmedLo[i]};
+    const f2 xc = f2_mul(rm, f2{t.cosHi[j], t.cosLo[j]});
+    const f2 yc = f2_mul(rm, f2{t.sinHi[j], t.sinLo[j]});
+    const f2 s2 = f2_of(smooth * smooth);
+    float ah = 0.f, al = 0.f;
+    for (int k = 1; k < b.n; ++k) {
+        const f2 dx = f2_sub(xc, f2{b.xh[k], b.xl[k]});
+        const f2 dy = f2_sub(yc, f2{b.yh[k], b.yl[k]});
+        const f2 d2 = f2_add(f2_add(f2_mul(dx, dx), f2_mul(dy, dy)), s2);
+        const f2 inv_d = f2_rsqrt(d2);
+        f2 term = f2_mul(inv_d, f2{b.gmh[k], b.gml[k]});
+        const double r_sm = b.rsm[k];
+        if (r_sm > 0.0) {
+            // Klahr's cubic inside r_sm (Pframeforce.cpp:57-66): rare, in FP64
+            const double d_sm = f2_value(f2_mul(d2, inv_d));
+            if (d_sm < r_sm) {
+                const double q = d_sm / r_sm;
+                const double fk = q * q * q * q - 2.0 * (q * q * q) + 2.0 * q;
+                term = f2_of(f2_value(term) * fk);
+            }
+        }
+        f2_accumulate(ah, al, term);
+    }
+    acc += (double)ah + (double)al;
+    pot[CELL(i, j)] = acc + (-b.ix * x - b.iy * y);
 }
 
 // ---------------------------------------------------------------------------
@@ -1505,12 +1538,15 @@ __global__ void k_accrete(Geo g, Tables t, Phys ph, AccretionSpec a, double *__r
 // outer x, outer y, mass) of its ring (split at Rmed < a, the body's distance
 // from the origin); k_reduce_cols adds the rings with compensation in a
 // fixed order.  Per body and cell: the separation, its smoothed inverse cube
-// (one rsqrt), Klahr's cubic factor inside r_sm, and two FMAs into the
-// sums; G and the ring's Surf multiply the ring's sums once.
+// (one rsqrt), Klahr's cubic factor inside r_sm, and the two products into
+// the sums, all in float-pair arithmetic (fp64_pair.cuh, about 2^-46
+// relative; sums of pairs per thread, FP64 across the block); G and the
+// ring's Surf multiply the ring's sums once.
 // ---------------------------------------------------------------------------
 struct ForceBodies {
     int n;  // bodies in this pass (1 .. kForceBodies)
-    double x[kForceBodies], y[kForceBodies], a[kForceBodies], rsm[kForceBodies];
+    double a[kForceBodies], rsm[kForceBodies];
+    float xh[kForceBodies], xl[kForceBodies], yh[kForceBodies], yl[kForceBodies];
 };
 
 __global__ void k_disk_force_bodies(Geo g, Tables t, Phys ph, ForceBodies fb,
@@ -1526,31 +1562,35 @@ __global__ void k_disk_force_bodies(Geo g, Tables t, Phys ph, ForceBodies fb,
     const double ring_sum = block_sum(ps, red);
     const double sigma1d = ph.correct_sg ? ring_sum / nz : 0.0;
     const double rmed = t.Rmed[i];
-    double ax[kForceBodies], ay[kForceBodies];
+    const f2 rm{t.RmedHi[i], t.RmedLo[i]};
+    // per body and thread, the sums of the x and y terms as float pairs
+    float axh[kForceBodies], axl[kForceBodies], ayh[kForceBodies], ayl[kForceBodies];
 #pragma unroll
-    for (int b = 0; b < kForceBodies; ++b) ax[b] = ay[b] = 0.0;
+    for (int b = 0; b < kForceBodies; ++b) axh[b] = axl[b] = ayh[b] = ayl[b] = 0.f;
     for (int j = threadIdx.x; j < nz; j += blockDim.x) {
         const double smooth = ph.eps_smooth * H[row + j];
-        const double s2 = smooth * smooth;
-        const double xc = rmed * t.cosj[j];
-        const double yc = rmed * t.sinj[j];
-        const double dsig = S[row + j] - sigma1d;
+        const f2 s2 = f2_of(smooth * smooth);
+        const f2 xc = f2_mul(rm, f2{t.cosHi[j], t.cosLo[j]});
+        const f2 yc = f2_mul(rm, f2{t.sinHi[j], t.sinLo[j]});
+        const f2 dsig = f2_of(S[row + j] - sigma1d);
 #pragma unroll
         for (int b = 0; b < kForceBodies; ++b) {
             if (b < fb.n) {
-                const double dx = xc - fb.x[b], dy = yc - fb.y[b];
-                const double dsm2 = fma(dx, dx, fma(dy, dy, s2));
-                const double rinv = rsqrt(dsm2);
-                double w = dsig * (rinv * rinv * rinv);
+                const f2 dx = f2_sub(xc, f2{fb.xh[b], fb.xl[b]});
+                const f2 dy = f2_sub(yc, f2{fb.yh[b], fb.yl[b]});
+                const f2 dsm2 = f2_add(f2_add(f2_mul(dx, dx), f2_mul(dy, dy)), s2);
+                const f2 rinv = f2_rsqrt(dsm2);
+                f2 w = f2_mul(dsig, f2_mul(f2_mul(rinv, rinv), rinv));
                 if (fb.rsm[b] > 0.0) {
-                    const double dsm = dsm2 * rinv;
+                    // Klahr's factor inside r_sm (Force.cpp:88-100): rare, in FP64
+                    const double dsm = f2_value(f2_mul(dsm2, rinv));
                     if (dsm < fb.rsm[b]) {
                         const double q = dsm / fb.rsm[b];
-                        w *= -(3.0 * (q * q * q * q) - 4.0 * (q * q * q));
+                        w = f2_of(f2_value(w) * -(3.0 * (q * q * q * q) - 4.0 * (q * q * q)));
                     }
                 }
-                ax[b] = fma(w, dx, ax[b]);
-                ay[b] = fma(w, dy, ay[b]);
+                f2_accumulate(axh[b], axl[b], f2_mul(w, dx));
+                f2_accumulate(ayh[b], ayl[b], f2_mul(w, dy));
             }
         }
     }
@@ -1559,8 +1599,8 @@ __global__ void k_disk_force_bodies(Geo g, Tables t, Phys ph, ForceBodies fb,
 #pragma unroll
     for (int b = 0; b < kForceBodies; ++b) {
         if (b < fb.n) {
-            const double sx = block_sum(ax[b], red) * gs;
-            const double sy = block_sum(ay[b], red) * gs;
+            const double sx = block_sum((double)axh[b] + (double)axl[b], red) * gs;
+            const double sy = block_sum((double)ayh[b] + (double)ayl[b], red) * gs;
             if (threadIdx.x == 0) {
                 const bool inner = rmed < fb.a[b];
                 p[5 * b + 0] = inner ? sx : 0.0;
@@ -1926,8 +1966,10 @@ void launch_disk_force(const Launch &L, int n, const double *px, const double *p
         ForceBodies fb{};
         fb.n = std::min(kForceBodies, n - b0);
         for (int b = 0; b < fb.n; ++b) {
-            fb.x[b] = px[b0 + b];
-            fb.y[b] = py[b0 + b];
+            fb.xh[b] = (float)px[b0 + b];
+            fb.xl[b] = (float)(px[b0 + b] - (double)fb.xh[b]);
+            fb.yh[b] = (float)py[b0 + b];
+            fb.yl[b] = (float)(py[b0 + b] - (double)fb.yh[b]);
             fb.a[b] = pa[b0 + b];
             fb.rsm[b] = rsm[b0 + b];
         }
