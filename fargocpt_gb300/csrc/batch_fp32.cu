@@ -32,7 +32,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <string>
 #include <new>
 #include <string>
 #include <vector>
@@ -219,6 +221,43 @@ __global__ void __launch_bounds__(PER <= 4 ? 384 : 512, PER <= 4 ? 2 : 1)
                                       k.sigma_t, k.sigma_lo_t, i, smf, redf, redl);
     }
 }
+
+// the register-blocked ring transport (azimuthal_ring_rb) over the rings of
+// one group of disks with the same ring length nz = PER x blockDim.x and
+// quantity count; start holds only the group's disks' rings
+template <int PER, int NQ>
+__global__ void __launch_bounds__(rb_max_threads(PER))
+    b_transport_azimuthal_rb(const DiskF *__restrict__ D, const StepF *__restrict__ S,
+                             const int *__restrict__ start, int nd)
+{
+    extern __shared__ __align__(16) float smf[];
+    __shared__ float redf[33];
+    __shared__ long long redl[33];
+    const int total = __ldg(start + nd);
+    for (int item = blockIdx.x; item < total; item += gridDim.x) {
+        const int d = disk_of(start, nd, item);
+        if (!S[d].run) continue;
+        const DiskF &k = D[d];
+        const int i = item - __ldg(start + d);
+        azimuthal_ring_rb<PER, NQ>(k.g, k.t, S[d].dt, k.ph.limiter_mc, k.ph.fast_transport,
+                                   k.dv_b, k.mom[0], k.mom[1], k.mom[2], k.mom[3], k.energy_t,
+                                   k.sigma_t, k.sigma_lo_t, i, smf, redf, redl);
+    }
+}
+
+typedef void (*AzRbFn)(const DiskF *, const StepF *, const int *, int);
+template <int NQ>
+static AzRbFn az_rb_fn_nq(int per)
+{
+    switch (per) {
+    case 4: return b_transport_azimuthal_rb<4, NQ>;
+    case 8: return b_transport_azimuthal_rb<8, NQ>;
+    case 12: return b_transport_azimuthal_rb<12, NQ>;
+    case 16: return b_transport_azimuthal_rb<16, NQ>;
+    default: return nullptr;
+    }
+}
+static AzRbFn az_rb_fn(int per, int nq) { return nq == 5 ? az_rb_fn_nq<5>(per) : az_rb_fn_nq<4>(per); }
 
 // damping rings: items = (disk, ring) of every disk with damping zones, each
 // taken four times, once per damped field (the fields are independent)
@@ -436,6 +475,17 @@ struct fgpu_batch {
     int grid[FGPU_BK_COUNT] = {};
     int az_per = 0;
     size_t az_smem = 0;
+    // disks whose rings take the register-blocked pass, grouped by ring
+    // length and quantity count (one launch per group); the strided pass
+    // takes the rest
+    struct RbGroup {
+        int nz, nq, per, grid;
+        size_t smem;
+    };
+    std::vector<RbGroup> rb;
+    std::vector<char> rb_disk;
+    int *d_rb_tables = nullptr;  // rb.size() tables of nd + 1 tile starts
+    long long az_strided_rings = 0;
 
     cudaGraphExec_t graph = nullptr;
     int graph_steps = 0;
@@ -507,7 +557,9 @@ static int apply_tiles(fgpu_batch *b, const fgpu_tiles &t)
                 n = ncol;
             } else if (k == FGPU_BK_TRANSPORT_RADIAL) {
                 n = ((b->nr[d] + r - 1) / r) * ncol;
-            } else if (k == FGPU_BK_TRANSPORT_AZIMUTHAL || k == FGPU_BK_DERIVED_CFL) {
+            } else if (k == FGPU_BK_TRANSPORT_AZIMUTHAL) {
+                n = b->rb_disk[d] ? 0 : b->nr[d];
+            } else if (k == FGPU_BK_DERIVED_CFL) {
                 n = b->nr[d];
             }
             acc += n;
@@ -518,6 +570,7 @@ static int apply_tiles(fgpu_batch *b, const fgpu_tiles &t)
         }
         s[nd] = (int)acc;
         totals[k] = k == FGPU_BK_DAMPING ? 4LL * b->n_damp_items : acc;
+        if (k == FGPU_BK_TRANSPORT_AZIMUTHAL) b->az_strided_rings = acc;
     }
     CKB(cudaMemcpyAsync(b->d_tables, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice,
                         b->stream));
@@ -583,8 +636,15 @@ static void launch_kernel(fgpu_batch *b, int k, int ghost_b = 0)
         if (b->any_adi) b_transport_radial<5><<<g, th, 0, s>>>(D, S, b->table(k), nd, r);
         break;
     case FGPU_BK_TRANSPORT_AZIMUTHAL:
-        if (b->any_iso) az_fn(b->az_per, 4)<<<g, th, b->az_smem, s>>>(D, S, b->table(k), nd);
-        if (b->any_adi) az_fn(b->az_per, 5)<<<g, th, b->az_smem, s>>>(D, S, b->table(k), nd);
+        if (b->az_strided_rings > 0) {
+            if (b->any_iso) az_fn(b->az_per, 4)<<<g, th, b->az_smem, s>>>(D, S, b->table(k), nd);
+            if (b->any_adi) az_fn(b->az_per, 5)<<<g, th, b->az_smem, s>>>(D, S, b->table(k), nd);
+        }
+        for (size_t q = 0; q < b->rb.size(); ++q) {
+            const fgpu_batch::RbGroup &grp = b->rb[q];
+            az_rb_fn(grp.per, grp.nq)<<<grp.grid, grp.nz / grp.per, grp.smem, s>>>(
+                D, S, b->d_rb_tables + q * (size_t)(nd + 1), nd);
+        }
         break;
     case FGPU_BK_FINISH: b_finish<<<g, th, 0, s>>>(D, S, b->table(k), nd, r); break;
     case FGPU_BK_DAMPING:
@@ -635,6 +695,7 @@ static void release(fgpu_batch *b)
     cudaFree(b->d_aux);
     cudaFree(b->d_active);
     cudaFree(b->d_tables);
+    cudaFree(b->d_rb_tables);
     cudaFree(b->d_damp_items);
     if (b->h_steps) cudaFreeHost(b->h_steps);
     if (b->h_clocks) cudaFreeHost(b->h_clocks);
@@ -748,6 +809,53 @@ extern "C" int fgpu_batch_create(int n, const fgpu_params *params, const double 
     CKC(cudaMalloc(&b->d_active, sizeof(int)));
     CKC(cudaMallocHost(&b->h_active, sizeof(int)));
     CKC(cudaMalloc(&b->d_tables, sizeof(int) * FGPU_BK_COUNT * (n + 1)));
+    {
+        // register-blocked groups: disks with the same ring length and
+        // quantity count whose rings split into whole segments
+        // (rb_default_per); FARGO_GB300_AZIMUTHAL=strided keeps them all on
+        // the strided pass
+        const char *env = getenv("FARGO_GB300_AZIMUTHAL");
+        const bool strided_only = env && std::string(env) == "strided";
+        b->rb_disk.assign(n, 0);
+        for (int d = 0; d < n && !strided_only; ++d) {
+            const int nq = params[d].eos == FGPU_EOS_IDEAL ? 5 : 4;
+            const int per = rb_default_per(b->nz[d], nq, kMaxRingSmem);
+            if (!per) continue;
+            b->rb_disk[d] = 1;
+            bool found = false;
+            for (auto &g : b->rb) found = found || (g.nz == b->nz[d] && g.nq == nq);
+            if (!found)
+                b->rb.push_back({b->nz[d], nq, per, 1,
+                                 rb_smem_floats(b->nz[d], nq, b->nz[d] / per) * sizeof(float)});
+        }
+        if (!b->rb.empty()) {
+            std::vector<int> h((size_t)b->rb.size() * (n + 1), 0);
+            for (size_t q = 0; q < b->rb.size(); ++q) {
+                fgpu_batch::RbGroup &g = b->rb[q];
+                int *st = h.data() + q * (size_t)(n + 1);
+                long long acc = 0;
+                for (int d = 0; d < n; ++d) {
+                    st[d] = (int)acc;
+                    const int nq = params[d].eos == FGPU_EOS_IDEAL ? 5 : 4;
+                    if (b->rb_disk[d] && b->nz[d] == g.nz && nq == g.nq) acc += b->nr[d];
+                }
+                st[n] = (int)acc;
+                const void *fn = (const void *)az_rb_fn(g.per, g.nq);
+                CKC(raise_smem_limit(fn, g.smem));
+                int per_sm = 0;
+                CKC(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, g.nz / g.per,
+                                                                  g.smem));
+                if (per_sm < 1) {
+                    b->err = "the register-blocked ring pass cannot run on this device";
+                    return fail(FGPU_ERR_UNSUPPORTED);
+                }
+                g.grid = (int)std::max(1LL, std::min((long long)per_sm * b->nsm, acc));
+            }
+            CKC(cudaMalloc(&b->d_rb_tables, sizeof(int) * h.size()));
+            CKC(cudaMemcpy(b->d_rb_tables, h.data(), sizeof(int) * h.size(),
+                           cudaMemcpyHostToDevice));
+        }
+    }
     if (!damp.empty()) {
         CKC(cudaMalloc(&b->d_damp_items, sizeof(int2) * damp.size()));
         CKC(cudaMemcpy(b->d_damp_items, damp.data(), sizeof(int2) * damp.size(),

@@ -1200,6 +1200,29 @@ __host__ __device__ constexpr size_t rb_smem_floats(int nz, int nq, int threads)
 {
     return (size_t)(nq + 1) * (size_t)nz + (size_t)10 * (size_t)threads;
 }
+// whether a ring of nz cells splits into segments of per cells with between
+// min_threads and the kernel's bound of threads, within max_smem bytes
+__host__ __device__ inline bool rb_fits(int nz, int nq, int per, int min_threads, size_t max_smem)
+{
+    if (nz % per != 0) return false;
+    const int th = nz / per;
+    return th >= min_threads && th <= rb_max_threads(per) &&
+           rb_smem_floats(nz, nq, th) * sizeof(float) <= max_smem;
+}
+// The segment length the register-blocked pass takes for a ring of nz cells
+// (0: the strided pass): 12 cells per thread where that leaves at least 128
+// threads, else the shortest of 4, 8, 16 that leaves at least 32.  Measured
+// FP32 steps: 6144-cell rings 2.34 ms with 12 cells (16: 2.54, strided 2.66),
+// 3072: 0.569 ms (8: 0.597, 16: 0.601, strided 0.664), 1536: 0.269 ms
+// (8: 0.275, 4: 0.283, strided 0.275), 384: 0.127 ms with 4 (8: 0.139,
+// 12: 0.152, strided 0.137).
+__host__ inline int rb_default_per(int nz, int nq, size_t max_smem)
+{
+    if (rb_fits(nz, nq, 12, 128, max_smem)) return 12;
+    for (int per : {4, 8, 16})
+        if (rb_fits(nz, nq, per, 32, max_smem)) return per;
+    return 0;
+}
 
 template <int PER, int NQ>
 __device__ __forceinline__ void azimuthal_ring_rb(const GeoF &g, const TablesF &t, double dt,

@@ -808,38 +808,24 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
         }
     }
     // the register-blocked kernel where the ring splits into whole 128-bit
-    // segments: 12 cells per thread where that leaves 128 .. 512 threads,
-    // else the shortest segment of 4, 8 or 16 cells that fits the kernel's
-    // thread bound (384 for 16 cells, else 512).  Measured FP32 steps:
-    // 6144-cell rings 2.34 ms with 12 cells (16: 2.54, strided 2.66),
-    // 3072: 0.569 ms (8: 0.597, 16: 0.601, strided 0.664), 1536: 0.269 ms
-    // (8: 0.275, 4: 0.283, strided 0.275), 384: 0.127 ms with 4 (8: 0.139,
-    // 12: 0.152, strided 0.137).  Unless
-    // FARGO_GB300_AZIMUTHAL asks for "strided" or "blocked<PER>"
+    // segments (rb_default_per), unless FARGO_GB300_AZIMUTHAL asks for
+    // "strided" or "blocked<PER>" (an explicit request is honoured or
+    // refused, never replaced)
     rb_per = 0;
     {
         const char *env = getenv("FARGO_GB300_AZIMUTHAL");
         const std::string want = env ? env : "";
-        auto fits = [&](int pc, int lo) {
-            if (nz % pc != 0) return false;
-            const int th = nz / pc;
-            return th >= lo && th <= rb_max_threads(pc) &&
-                   rb_smem_floats(nz, nq, th) * sizeof(float) <= kMaxRingSmem;
-        };
         if (want.rfind("blocked", 0) == 0) {
-            // an explicit request is honoured or refused, never replaced
             const int pc = atoi(want.c_str() + 7);
-            if ((pc == 4 || pc == 8 || pc == 12 || pc == 16) && fits(pc, 1)) {
+            if ((pc == 4 || pc == 8 || pc == 12 || pc == 16) &&
+                rb_fits(nz, nq, pc, 1, kMaxRingSmem)) {
                 rb_per = pc;
             } else {
                 err = "FARGO_GB300_AZIMUTHAL=" + want + " does not fit this ring";
                 return FGPU_ERR_UNSUPPORTED;
             }
         } else if (want != "strided") {
-            if (fits(12, 128)) rb_per = 12;
-            for (int pc : {4, 8, 16}) {
-                if (!rb_per && fits(pc, 32)) rb_per = pc;
-            }
+            rb_per = rb_default_per(nz, nq, kMaxRingSmem);
         }
     }
     if (rb_per) {

@@ -277,3 +277,28 @@ def test_bad_tiles_are_rejected():
         batch.set_tiles(bad)
     assert batch.tiles() == t
     batch.close()
+
+
+def test_register_blocked_groups_match_strided_pass(monkeypatch):
+    """Disks whose rings split into whole segments take the register-blocked
+    ring pass in groups of equal ring length, the others the strided pass;
+    with FARGO_GB300_AZIMUTHAL=strided every disk takes the strided pass.
+    Both give the same bits."""
+    from fargocpt_gb300 import setups
+    from fargocpt_gb300.batch import Batch, start_disks
+    # rings of 96 and 144 cells (strided and blocked), 384 and 576 (blocked)
+    disks = setups.sweep(n_disks=6, seed=13, nr_choices=(32, 48, 128, 192))
+    out = []
+    for variant in ("strided", None):
+        if variant:
+            monkeypatch.setenv("FARGO_GB300_AZIMUTHAL", variant)
+        else:
+            monkeypatch.delenv("FARGO_GB300_AZIMUTHAL", raising=False)
+        batch = Batch([x[0] for x in disks], [x[2] for x in disks])
+        start_disks(batch, disks, t_end=1.0, monitor_dt=0.1)
+        batch.run(8, steps_per_graph=4)
+        out.append([{f: e.get_field(f) for f in EVOLVED} for e in batch.disks])
+        batch.close()
+    for k in range(len(disks)):
+        for f in EVOLVED:
+            assert np.array_equal(out[0][k][f], out[1][k][f]), (k, f)
