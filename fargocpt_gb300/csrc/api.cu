@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -37,6 +38,7 @@ struct fgpu_engine {
     double *ring_ws = nullptr;
     size_t az_smem = 0;
     int az_block = 256;
+    bool transport_pair = true;  // the transports' arithmetic in float pairs
     int radial_chunk = 16;
 
     double *tables_mem = nullptr;
@@ -634,8 +636,8 @@ static int setup_tables(fgpu_engine *eng, const double *radii)
     t.CrRr1 = D(CRRR1); t.CrRr2 = D(CRRR2); t.CrRp = D(CRRP); t.CrScale = D(CRSCALE);
     t.cosj = tc; t.sinj = tc + nz;
     {
-        // Rmed, cos and sin as float pairs hi + lo
-        std::vector<float> pr((size_t)2 * R + (size_t)4 * nz);
+        // Rmed, cos and sin, InvDiffRmed and InvSurf as float pairs hi + lo
+        std::vector<float> pr((size_t)6 * R + (size_t)4 * nz);
         auto split = [](double v, float &h, float &l) {
             h = (float)v;
             l = (float)(v - (double)h);
@@ -646,11 +648,18 @@ static int setup_tables(fgpu_engine *eng, const double *radii)
             split(cs[j], c[j], c[(size_t)nz + j]);
             split(sn[j], c[2 * (size_t)nz + j], c[3 * (size_t)nz + j]);
         }
+        float *e = c + 4 * (size_t)nz;
+        for (int n = 0; n < R; ++n) {
+            split(T(INVDIFFRMED)[n], e[(size_t)n], e[(size_t)R + n]);
+            split(T(INVSURF)[n], e[2 * (size_t)R + n], e[3 * (size_t)R + n]);
+        }
         CK(cudaMalloc(&eng->pair_mem, sizeof(float) * pr.size()));
         CK(cudaMemcpy(eng->pair_mem, pr.data(), sizeof(float) * pr.size(), cudaMemcpyHostToDevice));
         const float *q = eng->pair_mem;
         t.RmedHi = q; t.RmedLo = q + R;
         t.cosHi = q + 2 * R; t.cosLo = t.cosHi + nz; t.sinHi = t.cosLo + nz; t.sinLo = t.sinHi + nz;
+        t.InvDiffRmedHi = t.sinLo + nz; t.InvDiffRmedLo = t.InvDiffRmedHi + R;
+        t.InvSurfHi = t.InvDiffRmedLo + R; t.InvSurfLo = t.InvSurfHi + R;
     }
 
     // boundary hooks
@@ -933,6 +942,18 @@ static int create_engine(const fgpu_params *params, const double *radii, cudaStr
     rc = setup_tables(eng, radii);
     if (rc != FGPU_OK) return fail(rc);
 
+    // the transports' arithmetic: float pairs unless
+    // FARGO_GB300_FP64_TRANSPORT asks for "fp64" ("pair" or unset: pairs)
+    {
+        const char *env = getenv("FARGO_GB300_FP64_TRANSPORT");
+        const std::string want = env ? env : "pair";
+        if (want == "fp64") {
+            eng->transport_pair = false;
+        } else if (want != "pair") {
+            eng->err = "FARGO_GB300_FP64_TRANSPORT=" + want + " is neither pair nor fp64";
+            return fail(FGPU_ERR_BAD_ARG);
+        }
+    }
     // azimuthal transport: whole ring in shared memory when it fits
     {
         const int per = azimuthal_cells_per_thread(eng->nz);
@@ -1535,10 +1556,10 @@ static void transport(fgpu_engine *eng, double dt)
     double **f = eng->field;
     State s = state_of(eng);
     launch_transport_radial(L, dt, omf, eng->radial_chunk, s.sigma, s.vr, s.vaz, s.energy,
-                            eng->mom, eng->energy_alt, eng->sigma_alt);
+                            eng->mom, eng->energy_alt, eng->sigma_alt, eng->transport_pair);
     mark(eng, 7);
     launch_transport_azimuthal(L, dt, eng->az_block, eng->mom, eng->energy_alt, eng->sigma_alt,
-                               s.vaz, eng->ring_ws, eng->az_smem);
+                               s.vaz, eng->ring_ws, eng->az_smem, eng->transport_pair);
     mark(eng, 8);
     launch_finish(L, omf, eng->mom, eng->sigma_alt, eng->energy_alt, s.vr, eng->vr_alt,
                   eng->vaz_alt, s.sigma, s.energy);

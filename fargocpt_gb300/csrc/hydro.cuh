@@ -45,6 +45,7 @@ struct Tables {
     const double *cosj, *sinj; // cos / sin (dphi j)
     // the same as float pairs hi + lo (for the pair-arithmetic kernels)
     const float *RmedHi, *RmedLo, *cosHi, *cosLo, *sinHi, *sinLo;
+    const float *InvDiffRmedHi, *InvDiffRmedLo, *InvSurfHi, *InvSurfLo;
 };
 
 struct Geo {

@@ -36,15 +36,18 @@ void launch_com_boundary(const Launch &L, const ComSpec &c, const State &s);
 void launch_correct_vaz(const Launch &L, double domega, double *vaz);
 void launch_cfl_cells(const Launch &L, const State &s, double *out);
 void launch_com_damping(const Launch &L, const ComSpec &c, double dt, const State &s);
+// pair: the float-pair kernel, else the FP64 kernel
 void launch_transport_radial(const Launch &L, double dt, double omf, int chunk, const double *S,
                              const double *vr, const double *vaz, const double *E,
-                             double *const mom[4], double *E_out, double *S_out);
+                             double *const mom[4], double *E_out, double *S_out, bool pair);
 size_t azimuthal_smem_bytes(int nz);
 int azimuthal_cells_per_thread(int nz);
 cudaError_t prepare_azimuthal(size_t smem);
+// pair: the float-pair kernel (block chosen by it), else the FP64 kernel
+// with the given block
 void launch_transport_azimuthal(const Launch &L, double dt, int block, double *const mom[4],
                                 double *E, double *S, const double *vaz, double *ring_ws,
-                                size_t smem);
+                                size_t smem, bool pair);
 void launch_finish(const Launch &L, double omf, double *const mom[4], const double *S_t,
                    const double *E_t, const double *vr_in, double *vr_out, double *vaz_out,
                    double *S_out, double *E_out);

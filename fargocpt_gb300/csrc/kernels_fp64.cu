@@ -822,6 +822,202 @@ __global__ void k_transport_radial(Geo g, Tables t, double dt, double omf, int m
     }
 }
 
+// flux limiters of the pair-arithmetic transports
+__device__ __forceinline__ bool f2_same_sign_nonzero(f2 a, f2 b)
+{
+    // normalised pairs: the high part carries the sign, and is zero only
+    // when the pair is
+    const int ia = __float_as_int(a.h), ib = __float_as_int(b.h);
+    return ((ia ^ ib) >= 0) && (ia & 0x7fffffff) != 0 && (ib & 0x7fffffff) != 0;
+}
+__device__ __forceinline__ bool f2_abs_less(f2 a, f2 b)
+{
+    const float ah = fabsf(a.h), bh = fabsf(b.h);
+    if (ah != bh) return ah < bh;
+    return (a.h < 0.f ? -a.l : a.l) < (b.h < 0.f ? -b.l : b.l);
+}
+// flux_limiter_unscaled in pairs
+__device__ __forceinline__ f2 lim_f2(f2 a, f2 b, int mc)
+{
+    const f2 zero{0.f, 0.f};
+    if (mc) {
+        const f2 mm = f2_same_sign_nonzero(a, b) ? (f2_abs_less(a, b) ? a : b) : zero;
+        const f2 s = f2_sadd(a, b);
+        const f2 c{__fmul_rn(0.5f, s.h), __fmul_rn(0.5f, s.l)};
+        const f2 d{__fmul_rn(2.0f, mm.h), __fmul_rn(2.0f, mm.l)};
+        if (f2_same_sign_nonzero(c, d)) return f2_abs_less(c, d) ? c : d;
+        return zero;
+    }
+    // both sides formed, one selected (no branch)
+    const f2 r = f2_sdiv(f2_smul(a, b), f2_sadd(a, b));
+    return f2_same_sign_nonzero(a, b) ? r : zero;
+}
+
+// ---------------------------------------------------------------------------
+// The radial transport with its arithmetic in float pairs (fp64_pair.cuh),
+// the same column sweep as k_transport_radial: the specific quantities, their
+// differences, limited slopes, star values and fluxes are pairs; the momenta
+// Sigma v of the update are pair products; the new momenta, energy and sigma
+// are joined into doubles once, energy and sigma by adding the pair update to
+// their FP64 values.  The upwind choice and the interpolation distance come
+// from the FP64 velocity.
+// ---------------------------------------------------------------------------
+template <int NQ>
+__device__ __forceinline__ void rad_ring_f2(int i, int j, int nz, const double *S, const double *vr,
+                                            const double *vaz, const double *E, double omf,
+                                            const Tables &t, f2 *w, double &sig)
+{
+    sig = S[CELL(i, j)];
+    const f2 sg = f2_split(sig);
+    const f2 r{t.RmedHi[i], t.RmedLo[i]};
+    w[0] = f2_split(vr[CELL(i + 1, j)]);
+    w[1] = f2_split(vr[CELL(i, j)]);
+    f2 a = f2_split(vaz[CELL(i, jnext(j, nz))]), b = f2_split(vaz[CELL(i, j)]);
+    if (omf != 0.0) {
+        const f2 ro = f2_split(t.Rmed[i] * omf);
+        a = f2_sadd(a, ro);
+        b = f2_sadd(b, ro);
+    }
+    w[2] = f2_smul(a, r);
+    w[3] = f2_smul(b, r);
+    if (NQ == 5) w[4] = f2_sdiv(f2_split(E[CELL(i, j)]), sg);
+    w[NQ] = sg;
+}
+
+template <int NQ>
+__global__ void k_transport_radial_f2(Geo g, Tables t, double dt, double omf, int mc, int chunk,
+                                      const double *__restrict__ S, const double *__restrict__ vr,
+                                      const double *__restrict__ vaz, const double *__restrict__ E,
+                                      double *__restrict__ mom0, double *__restrict__ mom1,
+                                      double *__restrict__ mom2, double *__restrict__ mom3,
+                                      double *__restrict__ E_out, double *__restrict__ S_out)
+{
+    constexpr int NW = NQ + 1;
+    const int nz = g.nz, nr = g.nr;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nz) return;
+    const int i0 = blockIdx.y * chunk;
+    if (i0 >= nr) return;
+    const int i1 = min(i0 + chunk, nr);
+    const double dtdphi = dt * g.dphi;
+    const f2 zero{0.f, 0.f};
+
+    // rolling state as in k_transport_radial: rings k-1 (wa, da), k (wb, db,
+    // ub: its upward difference) and k+1 (wn); sigma of k-1 / k / k+1
+    f2 wa[NW], wb[NW], wn[NW], da[NW], db[NW], ub[NW];
+#pragma unroll
+    for (int q = 0; q < NW; ++q) wa[q] = wb[q] = wn[q] = da[q] = db[q] = ub[q] = zero;
+    double sa = 0.0, sb = 0.0, sn = 0.0;
+
+    // slope of a ring from its up/down differences (zero on the first and
+    // last ring), without van Leer's factor 2
+    auto lim = [&](int ring, f2 up, f2 down) -> f2 {
+        const f2 d = lim_f2(up, down, mc);
+        return (ring <= 0 || ring >= nr - 1) ? zero : d;
+    };
+    auto dif = [&](int ring, const f2 &hi, const f2 &lo) {
+        return f2_smul(f2_ssub(hi, lo), f2{t.InvDiffRmedHi[ring], t.InvDiffRmedLo[ring]});
+    };
+
+    // prime rings k-1 = i0-1 and k = i0 (their slopes need rings i0-2 .. i0+1)
+    {
+        f2 wm2[NW];
+        double s_tmp = 0.0;
+#pragma unroll
+        for (int q = 0; q < NW; ++q) wm2[q] = zero;
+        const int r0 = i0 - 1;
+        if (r0 - 1 >= 0) rad_ring_f2<NQ>(r0 - 1, j, nz, S, vr, vaz, E, omf, t, wm2, s_tmp);
+        if (r0 >= 0) rad_ring_f2<NQ>(r0, j, nz, S, vr, vaz, E, omf, t, wa, sa);
+        rad_ring_f2<NQ>(i0, j, nz, S, vr, vaz, E, omf, t, wb, sb);
+        f2 downa[NW];
+#pragma unroll
+        for (int q = 0; q < NW; ++q) {
+            downa[q] = (r0 - 1 >= 0 && r0 >= 0) ? dif(r0, wa[q], wm2[q]) : zero;
+            ub[q] = r0 >= 0 ? dif(i0, wb[q], wa[q]) : zero;  // up of k-1 = down of k
+        }
+        const bool has_next = i0 + 1 < nr;
+        if (has_next) rad_ring_f2<NQ>(i0 + 1, j, nz, S, vr, vaz, E, omf, t, wn, sn);
+#pragma unroll
+        for (int q = 0; q < NW; ++q) {
+            da[q] = r0 >= 0 ? lim(r0, ub[q], downa[q]) : zero;
+            const f2 up = has_next ? dif(i0 + 1, wn[q], wb[q]) : zero;
+            db[q] = lim(i0, up, ub[q]);
+            ub[q] = up;
+        }
+    }
+    f2 flux_prev[NW], q_prev[4];
+    double e_prev = 0.0;
+    for (int k = i0; k <= i1; ++k) {
+        // flux through the interface k (between rings k-1 and k)
+        f2 flux[NW];
+        if (k == 0 || k >= nr) {
+#pragma unroll
+            for (int q = 0; q < NW; ++q) flux[q] = zero;
+        } else {
+            const double v = vr[CELL(k, j)];
+            const double vdt = v * dt;
+            const bool up = positive(v);
+            double fd = up ? t.Rmed[k] - t.Rmed[k - 1] - vdt : t.Rmed[k + 1] - t.Rmed[k] + vdt;
+            if (mc) fd *= 0.5;
+            // the star value from ring k-1 (+f da) or ring k (-f db)
+            const f2 f = f2_split(up ? fd : -fd);
+            f2 star[NW];
+#pragma unroll
+            for (int q = 0; q < NW; ++q)
+                star[q] = f2_sadd(up ? wa[q] : wb[q], f2_smul(f, up ? da[q] : db[q]));
+            // base sigma* v, the factor every quantity's flux shares
+            const f2 bsv = f2_smul(f2_smul(f2_split(dtdphi * t.Rinf[k]), star[NQ]), f2_split(v));
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) flux[q] = f2_smul(star[q], bsv);
+            flux[NQ] = bsv;
+        }
+        if (k > i0) {
+            // VanLeerRadial update of ring k-1 (:586-591)
+            const int i = k - 1;
+            const f2 invs{t.InvSurfHi[i], t.InvSurfLo[i]};
+            const size_t c = CELL(i, j);
+            f2 dq[NW];
+#pragma unroll
+            for (int q = 0; q < NW; ++q) dq[q] = f2_smul(f2_ssub(flux_prev[q], flux[q]), invs);
+            mom0[c] = f2_to_double(f2_sadd(q_prev[0], dq[0]));
+            mom1[c] = f2_to_double(f2_sadd(q_prev[1], dq[1]));
+            mom2[c] = f2_to_double(f2_sadd(q_prev[2], dq[2]));
+            mom3[c] = f2_to_double(f2_sadd(q_prev[3], dq[3]));
+            if (NQ == 5) E_out[c] = e_prev + f2_to_double(dq[4]);
+            S_out[c] = sa + f2_to_double(dq[NQ]);
+        }
+        if (k < i1) {
+            // conserved quantities of ring k for its update at interface k+1
+#pragma unroll
+            for (int q = 0; q < NW; ++q) flux_prev[q] = flux[q];
+            const f2 sp = wb[NQ];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) q_prev[q] = f2_smul(sp, wb[q]);
+            if (NQ == 5) e_prev = E[CELL(k, j)];
+            // advance: ring k becomes k-1, ring k+1 becomes k
+            const bool more = k + 2 < nr;
+            f2 w2[NW];
+            double s2 = 0.0;
+#pragma unroll
+            for (int q = 0; q < NW; ++q) w2[q] = zero;
+            if (more) rad_ring_f2<NQ>(k + 2, j, nz, S, vr, vaz, E, omf, t, w2, s2);
+#pragma unroll
+            for (int q = 0; q < NW; ++q) {
+                wa[q] = wb[q];
+                da[q] = db[q];
+                wb[q] = wn[q];
+                const f2 up = more ? dif(k + 2, w2[q], wn[q]) : zero;
+                db[q] = lim(k + 1, up, ub[q]);
+                ub[q] = up;
+                wn[q] = w2[q];
+            }
+            sa = sb;
+            sb = sn;
+            sn = s2;
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Block reductions
 // ---------------------------------------------------------------------------
@@ -1091,6 +1287,205 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(Geo g, Tables t, do
                 int ji = (j - nshift) % nz;
                 if (ji < 0) ji += nz;
                 Q[j] = W[ji];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The same azimuthal transport with its arithmetic in float pairs
+// (fp64_pair.cuh).  The ring pass above is bound by GB300's FP64 pipe (about
+// 1.6 FP64 results per clock per SM against about 113 FP32); here every
+// slope, star value and flux is formed in pair arithmetic (48 significant
+// bits, errors within a few 2^-47 of the operands), the doubles are split and
+// joined on the integer pipe, and FP64 is kept for the state: each quantity's
+// update Q += F_j - F_j+1 adds the pair flux difference, joined into a
+// double, to the FP64 value, so what a step loses is the pair's rounding of
+// the fluxes, not of the state.  The upwind choice and the interpolation
+// distance come from the FP64 velocity as before; the ring mean and the FARGO
+// shift phase stay in FP64.
+//
+// Layout as in the FP64 pass (4 x naz x 8 bytes of shared memory, or the
+// per-ring global workspace): the sigma pair, the specific quantity, the
+// slopes and the fluxes, each a pair.  Sigma's FP64 values are updated in
+// place in its global row (the block owns the ring), the transported
+// quantities in theirs, and AdvectSHIFT stages each row through shared
+// memory.
+// ---------------------------------------------------------------------------
+// One QuantitiesAdvection pass (TransportEuler.cpp:292-304) in pairs.  SP
+// holds sigma's pair, Sg its FP64 row; both advance.  v[n] is the owned
+// cells' FP64 velocity (ignored when uniform).
+//
+// Each face forms the limited slope of its upwind cell itself, from that
+// cell and its two neighbours, instead of reading a slope array: every
+// cell's slope is still formed once per face that uses it (van Leer's
+// upwind cell of face j is j - 1 or j), the slope array and its barrier
+// go, and shared memory holds the face factors in their place, so that a
+// thread keeps only its faces' interpolation distances in registers.  Loops
+// over the owned cells compute with the index clamped into the ring and guard
+// only their stores (no branch in the body).
+template <int PER, int NQ>
+__device__ void ring_advection_pass_f2(double *Sg, f2 *SP, f2 *W, f2 *CF, f2 *F,
+                                       double *const *qrow, const double *v, double dt,
+                                       double dxtheta, double half_invdx, double dxrad_invsurf,
+                                       int nz, int mc, bool uniform, double vconst)
+{
+    const int tid = threadIdx.x, bs = blockDim.x;
+    // the slopes carry no constant factor; the distance does (as in
+    // ring_advection_pass): k (dx - v dt) or -k (dx + v dt), k = 1 / dx
+    // (van Leer) or 1 / (2 dx) (MC)
+    const double kfac = mc ? half_invdx : 2.0 * half_invdx;
+    const double kdt = kfac * dt;
+    const double dxk = dxtheta * kfac;
+    const f2 cvel = f2_split(dxrad_invsurf / kdt);
+    f2 am[PER];
+    unsigned pos = 0;  // bit n: the upwind cell of face tid + n bs is its left neighbour
+    auto cell = [&](int n) { return min(tid + n * bs, nz - 1); };
+    auto owned = [&](int n) { return tid + n * bs < nz; };
+    auto nxt = [&](int j) { return j == nz - 1 ? 0 : j + 1; };
+    auto prv = [&](int j) { return j == 0 ? nz - 1 : j - 1; };
+    // the star value at face j of the quantity X from its upwind cell u
+    auto star = [&](const f2 *X, int u, f2 a) {
+        const f2 x = X[u];
+        const f2 d = lim_f2(f2_ssub(X[nxt(u)], x), f2_ssub(x, X[prv(u)]), mc);
+        return f2_sadd(x, f2_smul(a, d));
+    };
+    // DensityStar and the face factor dxrad S* v / Surf every flux shares
+    const double vu = vconst * kdt;
+    const bool pu = positive(vu);
+    const f2 au = f2_split(pu ? dxk - vu : -(dxk + vu));
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = cell(n);
+        const double vk = uniform ? vu : v[n] * kdt;
+        const bool p = positive(vk);
+        am[n] = uniform ? au : f2_split(p ? dxk - vk : -(dxk + vk));
+        pos |= (unsigned)p << n;
+        const f2 c = f2_smul(f2_smul(cvel, star(SP, p ? prv(j) : j, am[n])), f2_split(vk));
+        if (owned(n)) CF[j] = c;
+    }
+    // per quantity: specific values (with the previous quantity's update),
+    // then the fluxes
+#pragma unroll 1
+    for (int q = 0; q <= NQ; ++q) {
+#pragma unroll
+        for (int n = 0; n < PER; ++n) {
+            const int j = cell(n);
+            if (q > 0) {
+                double *Qp = qrow[q - 1];
+                const double qn = Qp[j] + f2_to_double(f2_ssub(F[j], F[nxt(j)]));
+                if (owned(n)) Qp[j] = qn;
+            }
+            if (q < NQ) {
+                const f2 w = f2_sdiv(f2_split(qrow[q][j]), SP[j]);
+                if (owned(n)) W[j] = w;
+            }
+        }
+        if (q == NQ) break;
+        __syncthreads();
+#pragma unroll
+        for (int n = 0; n < PER; ++n) {
+            const int j = cell(n);
+            const f2 f = f2_smul(star(W, (pos >> n) & 1u ? prv(j) : j, am[n]), CF[j]);
+            if (owned(n)) F[j] = f;
+        }
+        __syncthreads();
+    }
+    // sigma: QRStar == 1, the flux is the face factor itself (CF is
+    // complete: the barriers of the quantities, or this one when there are
+    // none, separate its writes from these reads)
+    if (NQ == 0) __syncthreads();
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = cell(n);
+        // nothing reads SP in this phase
+        const double s = Sg[j] + f2_to_double(f2_ssub(CF[j], CF[nxt(j)]));
+        const f2 sp = f2_split(s);
+        if (owned(n)) {
+            Sg[j] = s;
+            SP[j] = sp;
+        }
+    }
+    __syncthreads();
+}
+
+// WS: the ring's arrays in the per-ring global workspace (rings beyond the
+// shared memory), else in shared memory
+template <int PER, int MAXT, int NQ, bool WS>
+__global__ void __launch_bounds__(MAXT) k_transport_azimuthal_f2(
+    Geo g, Tables t, double dt, int mc, int fast, const double *__restrict__ vaz, double *mom0,
+    double *mom1, double *mom2, double *mom3, double *E, double *S, double *ring_ws)
+{
+    extern __shared__ double smem[];
+    __shared__ double red[33];
+    const int nz = g.nz;
+    const int i = blockIdx.x;
+    const int tid = threadIdx.x, bs = blockDim.x;
+    const size_t row = (size_t)i * nz;
+    f2 *base = reinterpret_cast<f2 *>(WS ? ring_ws + (size_t)i * 4 * nz : smem);
+    f2 *SP = base, *W = base + nz, *CF = base + 2 * nz, *F = base + 3 * nz;
+    double *Sg = S + row;
+
+    // compute_average_azimuthal_velocity, :174-189
+    double vown[PER];
+    double part = 0.0;
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = tid + n * bs;
+        if (j < nz) {
+            vown[n] = vaz[row + j];
+            part += vown[n];
+        }
+    }
+    const double vmean = block_sum(part, red) / (double)nz;
+    // ComputeConstantResidual, :207-236: FP64 shift phase of the ring
+    const double Ntilde = vmean * t.InvRmed[i] * dt * g.invdphi;
+    const double Nround = floor(Ntilde + 0.5);
+    const int nshift = (int)Nround;
+    const double invdt = 1.0 / dt;
+    const double vt = (Ntilde - Nround) * t.Rmed[i] * invdt * g.dphi;
+#pragma unroll
+    for (int n = 0; n < PER; ++n) {
+        const int j = tid + n * bs;
+        if (j < nz) {
+            double vres = vown[n] - vmean;
+            if (!fast) vres = vt + vres;
+            vown[n] = vres;
+            SP[j] = f2_split(Sg[j]);
+        }
+    }
+    __syncthreads();
+
+    double *qrow[5] = {mom0 + row, mom1 + row, mom2 + row, mom3 + row, E + row};
+    const double dxtheta = g.dphi * t.Rmed[i];
+    const double half_invdx = 0.5 * (1.0 / dxtheta);
+    const double dxrad = (t.Rsup[i] - t.Rinf[i]) * dt;
+    const double invsurf = t.InvSurf[i];
+    ring_advection_pass_f2<PER, NQ>(Sg, SP, W, CF, F, qrow, vown, dt, dxtheta, half_invdx,
+                                    dxrad * invsurf, nz, mc, false, 0.0);
+    if (fast) {
+        ring_advection_pass_f2<PER, NQ>(Sg, SP, W, CF, F, qrow, vown, dt, dxtheta, half_invdx,
+                                        dxrad * invsurf, nz, mc, true, vt);
+    }
+    // AdvectSHIFT of every quantity, sigma last, staged through W's doubles
+    double *stage = reinterpret_cast<double *>(W);
+#pragma unroll
+    for (int q = 0; q <= NQ; ++q) {
+        double *Q = q < NQ ? qrow[q] : Sg;
+#pragma unroll
+        for (int n = 0; n < PER; ++n) {
+            const int j = tid + n * bs;
+            if (j < nz) stage[j] = Q[j];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int n = 0; n < PER; ++n) {
+            const int j = tid + n * bs;
+            if (j < nz) {
+                int ji = (j - nshift) % nz;
+                if (ji < 0) ji += nz;
+                Q[j] = stage[ji];
             }
         }
         __syncthreads();
@@ -1771,11 +2166,23 @@ void launch_ghost(const Launch &L, const BcSpec &bc, double omf, const State &s)
 
 void launch_transport_radial(const Launch &L, double dt, double omf, int chunk, const double *S,
                              const double *vr, const double *vaz, const double *E,
-                             double *const mom[4], double *E_out, double *S_out)
+                             double *const mom[4], double *E_out, double *S_out, bool pair)
 {
     const int chunks = (L.g.nr + chunk - 1) / chunk;
     const int bx = 64;
     dim3 grid((L.g.nz + bx - 1) / bx, chunks);
+    if (pair) {
+        if (L.ph.adiabatic) {
+            k_transport_radial_f2<5><<<grid, bx, 0, L.stream>>>(
+                L.g, L.t, dt, omf, L.ph.limiter_mc, chunk, S, vr, vaz, E, mom[0], mom[1], mom[2],
+                mom[3], E_out, S_out);
+        } else {
+            k_transport_radial_f2<4><<<grid, bx, 0, L.stream>>>(
+                L.g, L.t, dt, omf, L.ph.limiter_mc, chunk, S, vr, vaz, E, mom[0], mom[1], mom[2],
+                mom[3], E_out, S_out);
+        }
+        return;
+    }
     if (L.ph.adiabatic) {
         k_transport_radial<5><<<grid, bx, 0, L.stream>>>(L.g, L.t, dt, omf, L.ph.limiter_mc, chunk,
                                                          S, vr, vaz, E, mom[0], mom[1], mom[2],
@@ -1798,15 +2205,52 @@ cudaError_t prepare_azimuthal(size_t smem)
     cudaError_t e = raise_smem_limit((const void *)k_transport_azimuthal<4>, smem);
     if (e == cudaSuccess) e = raise_smem_limit((const void *)k_transport_azimuthal<8>, smem);
     if (e == cudaSuccess) e = raise_smem_limit((const void *)k_transport_azimuthal<16>, smem);
+    const void *pair_kernels[6] = {
+        (const void *)k_transport_azimuthal_f2<4, 512, 4, false>,
+        (const void *)k_transport_azimuthal_f2<4, 512, 5, false>,
+        (const void *)k_transport_azimuthal_f2<8, 768, 4, false>,
+        (const void *)k_transport_azimuthal_f2<8, 768, 5, false>,
+        (const void *)k_transport_azimuthal_f2<16, 512, 4, false>,
+        (const void *)k_transport_azimuthal_f2<16, 512, 5, false>};
+    for (const void *fn : pair_kernels)
+        if (e == cudaSuccess) e = raise_smem_limit(fn, smem);
     return e;
 }
 
+// Cells per thread of the pair kernel: 4 up to 2048 cells (<= 512 threads),
+// 8 up to 6144 (<= 768), 16 beyond (<= 512 threads for 8192 cells); the
+// thread count is the ring length over that, in whole warps.
+int azimuthal_pair_cells_per_thread(int nz) { return nz <= 2048 ? 4 : (nz <= 6144 ? 8 : 16); }
+
 void launch_transport_azimuthal(const Launch &L, double dt, int block, double *const mom[4],
                                 double *E, double *S, const double *vaz, double *ring_ws,
-                                size_t smem)
+                                size_t smem, bool pair)
 {
     const int nq = L.ph.adiabatic ? 5 : 4;
     const size_t dyn = ring_ws ? 0 : smem;
+    if (pair) {
+        const int per = azimuthal_pair_cells_per_thread(L.g.nz);
+        const int threads = ((L.g.nz + per - 1) / per + 31) / 32 * 32;
+#define AZ2_LAUNCH1(P, T, Q, WS)                                                                \
+    k_transport_azimuthal_f2<P, T, Q, WS><<<L.g.nr, threads, dyn, L.stream>>>(                   \
+        L.g, L.t, dt, L.ph.limiter_mc, L.ph.fast_transport, vaz, mom[0], mom[1], mom[2], mom[3], \
+        E, S, ring_ws)
+#define AZ2_LAUNCH(P, T)                                                                        \
+    if (nq == 5) AZ2_LAUNCH1(P, T, 5, false); else AZ2_LAUNCH1(P, T, 4, false)
+        if (ring_ws) {
+            // rings beyond the shared memory: 16 cells per thread
+            if (nq == 5) AZ2_LAUNCH1(16, 512, 5, true); else AZ2_LAUNCH1(16, 512, 4, true);
+        } else if (per == 4) {
+            AZ2_LAUNCH(4, 512);
+        } else if (per == 8) {
+            AZ2_LAUNCH(8, 768);
+        } else {
+            AZ2_LAUNCH(16, 512);
+        }
+#undef AZ2_LAUNCH
+#undef AZ2_LAUNCH1
+        return;
+    }
     const int per = azimuthal_cells_per_thread(L.g.nz);
 #define AZ_LAUNCH(P)                                                                          \
     k_transport_azimuthal<P><<<L.g.nr, block, dyn, L.stream>>>(                               \

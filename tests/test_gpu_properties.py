@@ -4,8 +4,11 @@ test_gpu_baseline_configs.py; these properties hold without a second
 implementation):
 
 * azimuthal equivariance: with only the central star, rotating the initial
-  disk by k cells rotates the result by k cells (to round-off: the ring
-  reductions change summation order);
+  disk by k cells rotates the result by k cells, within the FP64 bar of
+  1e-10 (the ring reductions change summation order with the rotation; v_r
+  near the inner damping zone, the most sensitive field, differs by 1.7e-11
+  of its largest value after one step, whichever arithmetic the transports
+  use);
 * axisymmetry: an axisymmetric disk without a planet stays axisymmetric;
 * finiteness after many steps of the C2-size adiabatic disk.
 """
@@ -52,7 +55,7 @@ def test_rotation_equivariance_c2_size():
         _advance(e, 5)
     for f in EVOLVED:
         a = np.roll(e1.get_field(f), k, axis=1)
-        assert rel_linf(e2.get_field(f), a) <= 1e-11, f
+        assert rel_linf(e2.get_field(f), a) <= 1e-10, f
 
 
 def test_axisymmetric_disk_stays_axisymmetric():
