@@ -16,7 +16,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfargocpt_gb300.so")
-SOURCES = ["api.cu", "kernels_fp64.cu", "kernels_fp32.cu", "batch_fp32.cu", "noalloc.cu"]
+SOURCES = ["api.cu", "kernels_fp64.cu", "kernels_pair.cu", "kernels_fp32.cu", "batch_fp32.cu",
+           "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

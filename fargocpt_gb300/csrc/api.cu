@@ -38,7 +38,7 @@ struct fgpu_engine {
     double *ring_ws = nullptr;
     size_t az_smem = 0;
     int az_block = 256;
-    bool transport_pair = true;  // the transports' arithmetic in float pairs
+    bool pair_arith = true;  // the kernels' arithmetic in float pairs (else FP64)
     int radial_chunk = 16;
 
     double *tables_mem = nullptr;
@@ -653,6 +653,10 @@ static int setup_tables(fgpu_engine *eng, const double *radii)
             split(T(INVDIFFRMED)[n], e[(size_t)n], e[(size_t)R + n]);
             split(T(INVSURF)[n], e[2 * (size_t)R + n], e[3 * (size_t)R + n]);
         }
+        // every per-ring table as float pairs, at the same index as its doubles
+        pr.resize(pr.size() + (size_t)2 * NTAB * R);
+        float *m = pr.data() + (pr.size() - (size_t)2 * NTAB * R);
+        for (size_t k = 0; k < (size_t)NTAB * R; ++k) split(h[k], m[2 * k], m[2 * k + 1]);
         CK(cudaMalloc(&eng->pair_mem, sizeof(float) * pr.size()));
         CK(cudaMemcpy(eng->pair_mem, pr.data(), sizeof(float) * pr.size(), cudaMemcpyHostToDevice));
         const float *q = eng->pair_mem;
@@ -660,6 +664,8 @@ static int setup_tables(fgpu_engine *eng, const double *radii)
         t.cosHi = q + 2 * R; t.cosLo = t.cosHi + nz; t.sinHi = t.cosLo + nz; t.sinLo = t.sinHi + nz;
         t.InvDiffRmedHi = t.sinLo + nz; t.InvDiffRmedLo = t.InvDiffRmedHi + R;
         t.InvSurfHi = t.InvDiffRmedLo + R; t.InvSurfLo = t.InvSurfHi + R;
+        t.tbase = eng->tables_mem;
+        t.ptab = reinterpret_cast<const float2 *>(q + (pr.size() - (size_t)2 * NTAB * R));
     }
 
     // boundary hooks
@@ -832,6 +838,8 @@ static int setup_tables(fgpu_engine *eng, const double *radii)
     ph.mu_gm1_over_R = p.mu * (p.gamma - 1.0) / p.R_gas;
     ph.emin_fac = p.minimum_temperature / p.mu * p.R_gas / (p.gamma - 1.0);
     ph.emax_fac = p.maximum_temperature / p.mu * p.R_gas / (p.gamma - 1.0);
+    ph.emin_fac_f = (float)ph.emin_fac;
+    ph.emax_fac_f = (float)ph.emax_fac;  // may round to infinity: the screen then has no upper bound
     return FGPU_OK;
 }
 
@@ -942,15 +950,15 @@ static int create_engine(const fgpu_params *params, const double *radii, cudaStr
     rc = setup_tables(eng, radii);
     if (rc != FGPU_OK) return fail(rc);
 
-    // the transports' arithmetic: float pairs unless
-    // FARGO_GB300_FP64_TRANSPORT asks for "fp64" ("pair" or unset: pairs)
+    // the kernels' arithmetic: float pairs unless FARGO_GB300_FP64_ARITH
+    // asks for "fp64" ("pair" or unset: pairs)
     {
-        const char *env = getenv("FARGO_GB300_FP64_TRANSPORT");
+        const char *env = getenv("FARGO_GB300_FP64_ARITH");
         const std::string want = env ? env : "pair";
         if (want == "fp64") {
-            eng->transport_pair = false;
+            eng->pair_arith = false;
         } else if (want != "pair") {
-            eng->err = "FARGO_GB300_FP64_TRANSPORT=" + want + " is neither pair nor fp64";
+            eng->err = "FARGO_GB300_FP64_ARITH=" + want + " is neither pair nor fp64";
             return fail(FGPU_ERR_BAD_ARG);
         }
     }
@@ -1046,6 +1054,7 @@ static Launch launch_of(const fgpu_engine *eng)
     L.ph = eng->ph;
     L.stream = eng->stream;
     L.bx = 128;
+    L.pair = eng->pair_arith;
     return L;
 }
 
@@ -1556,10 +1565,10 @@ static void transport(fgpu_engine *eng, double dt)
     double **f = eng->field;
     State s = state_of(eng);
     launch_transport_radial(L, dt, omf, eng->radial_chunk, s.sigma, s.vr, s.vaz, s.energy,
-                            eng->mom, eng->energy_alt, eng->sigma_alt, eng->transport_pair);
+                            eng->mom, eng->energy_alt, eng->sigma_alt);
     mark(eng, 7);
     launch_transport_azimuthal(L, dt, eng->az_block, eng->mom, eng->energy_alt, eng->sigma_alt,
-                               s.vaz, eng->ring_ws, eng->az_smem, eng->transport_pair);
+                               s.vaz, eng->ring_ws, eng->az_smem);
     mark(eng, 8);
     launch_finish(L, omf, eng->mom, eng->sigma_alt, eng->energy_alt, s.vr, eng->vr_alt,
                   eng->vaz_alt, s.sigma, s.energy);

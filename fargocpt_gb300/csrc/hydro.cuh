@@ -46,6 +46,10 @@ struct Tables {
     // the same as float pairs hi + lo (for the pair-arithmetic kernels)
     const float *RmedHi, *RmedLo, *cosHi, *cosLo, *sinHi, *sinLo;
     const float *InvDiffRmedHi, *InvDiffRmedLo, *InvSurfHi, *InvSurfLo;
+    // every table above as float pairs: the pair of tab[i] is
+    // ptab[(tab - tbase) + i]
+    const double *tbase;
+    const float2 *ptab;
 };
 
 struct Geo {
@@ -72,6 +76,7 @@ struct Phys {
     double cool_const;    // 2 * 4 * sigma_sb / c (SubStep3's radiative alpha)
     double mu_gm1_over_R; // mu (gamma - 1) / R
     double emin_fac, emax_fac; // Tmin|Tmax / mu * R / (gamma - 1)
+    float emin_fac_f, emax_fac_f;  // the same rounded to float (FP32 screens)
 };
 
 struct Bodies {

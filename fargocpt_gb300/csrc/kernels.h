@@ -16,6 +16,9 @@ struct Launch {
     Phys ph;
     cudaStream_t stream;
     int bx;  // threads per block along the azimuth for cell kernels
+    // the kernels' arithmetic in float pairs (kernels_pair.cu and the pair
+    // transports) instead of FP64, with FP64 state updates
+    bool pair = false;
 };
 
 void launch_potential(const Launch &L, const Bodies &b, const double *H, double *pot);
@@ -36,18 +39,16 @@ void launch_com_boundary(const Launch &L, const ComSpec &c, const State &s);
 void launch_correct_vaz(const Launch &L, double domega, double *vaz);
 void launch_cfl_cells(const Launch &L, const State &s, double *out);
 void launch_com_damping(const Launch &L, const ComSpec &c, double dt, const State &s);
-// pair: the float-pair kernel, else the FP64 kernel
 void launch_transport_radial(const Launch &L, double dt, double omf, int chunk, const double *S,
                              const double *vr, const double *vaz, const double *E,
-                             double *const mom[4], double *E_out, double *S_out, bool pair);
+                             double *const mom[4], double *E_out, double *S_out);
 size_t azimuthal_smem_bytes(int nz);
 int azimuthal_cells_per_thread(int nz);
 cudaError_t prepare_azimuthal(size_t smem);
-// pair: the float-pair kernel (block chosen by it), else the FP64 kernel
-// with the given block
+// block: threads of the FP64 kernel (the pair kernel chooses its own)
 void launch_transport_azimuthal(const Launch &L, double dt, int block, double *const mom[4],
                                 double *E, double *S, const double *vaz, double *ring_ws,
-                                size_t smem, bool pair);
+                                size_t smem);
 void launch_finish(const Launch &L, double omf, double *const mom[4], const double *S_t,
                    const double *E_t, const double *vr_in, double *vr_out, double *vaz_out,
                    double *S_out, double *E_out);
@@ -55,6 +56,22 @@ void launch_damping(const Launch &L, const Damping &dm, double dt, const int *ri
                     const State &s);
 void launch_derived_cfl(const Launch &L, int mode, const State &s, unsigned long long *dt_min);
 void launch_pressure(const Launch &L, const double *S, const double *E, double *P);
+// the same cell kernels with their arithmetic in float pairs (kernels_pair.cu);
+// the launchers above route to them when L.pair is set
+void launch_source_pair(const Launch &L, double dt, double omf, const double *S, const double *Pr,
+                        const double *pot, const double *vr_in, const double *vaz_in,
+                        double *vr_out, double *vaz_out);
+void launch_artvisc_q_pair(const Launch &L, double dt, const double *S, const double *vr,
+                           const double *vaz, double *E, double *Qr, double *Qp);
+void launch_artvisc_v_pair(const Launch &L, double dt, const double *S, const double *E,
+                           const double *Qr, const double *Qp, double *vr, double *vaz, double *cs,
+                           double *H, double *nu);
+void launch_stress_pair(const Launch &L, const double *S, const double *vr, const double *vaz,
+                        const double *nu, double *divv, double *trr, double *tpp, double *trp);
+void launch_viscous_pair(const Launch &L, double dt, double beta_inv, int mode, const State &s);
+void launch_finish_pair(const Launch &L, double omf, double *const mom[4], const double *S_t,
+                        const double *E_t, const double *vr_in, double *vr_out, double *vaz_out,
+                        double *S_out, double *E_out);
 // bodies one disk-force pass handles
 constexpr int kForceBodies = 4;
 

@@ -2086,6 +2086,7 @@ void launch_source(const Launch &L, double dt, double omf, const double *S, cons
                    const double *pot, const double *vr_in, const double *vaz_in, double *vr_out,
                    double *vaz_out)
 {
+    if (L.pair) return launch_source_pair(L, dt, omf, S, P, pot, vr_in, vaz_in, vr_out, vaz_out);
     k_source<<<grid2d(L.g.nz, L.g.nr + 1, L.bx), L.bx, 0, L.stream>>>(
         L.g, L.t, dt, omf, S, P, pot, vr_in, vaz_in, vr_out, vaz_out);
 }
@@ -2093,6 +2094,7 @@ void launch_source(const Launch &L, double dt, double omf, const double *S, cons
 void launch_artvisc_q(const Launch &L, double dt, const double *S, const double *vr,
                       const double *vaz, double *E, double *Qr, double *Qp)
 {
+    if (L.pair) return launch_artvisc_q_pair(L, dt, S, vr, vaz, E, Qr, Qp);
     k_artvisc_q<<<grid2d(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(L.g, L.t, L.ph, dt, S, vr,
                                                                       vaz, E, Qr, Qp);
 }
@@ -2101,6 +2103,7 @@ void launch_artvisc_v(const Launch &L, double dt, const double *S, const double 
                       const double *Qr, const double *Qp, double *vr, double *vaz, double *cs,
                       double *H, double *nu)
 {
+    if (L.pair) return launch_artvisc_v_pair(L, dt, S, E, Qr, Qp, vr, vaz, cs, H, nu);
     k_artvisc_v<<<grid2d(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(L.g, L.t, L.ph, dt, S, E, Qr,
                                                                       Qp, vr, vaz, cs, H, nu);
 }
@@ -2108,12 +2111,15 @@ void launch_artvisc_v(const Launch &L, double dt, const double *S, const double 
 void launch_stress(const Launch &L, const double *S, const double *vr, const double *vaz,
                    const double *nu, double *divv, double *trr, double *tpp, double *trp)
 {
+    if (L.pair) return launch_stress_pair(L, S, vr, vaz, nu, divv, trr, tpp, trp);
     k_stress<<<grid2d(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(L.g, L.t, S, vr, vaz, nu, divv,
                                                                    trr, tpp, trp);
 }
 
 void launch_viscous(const Launch &L, double dt, double beta_inv, int mode, const State &s)
 {
+    // StabilizeViscosity's corrected update is the FP64 kernel's
+    if (L.pair && L.ph.stabilize != 1) return launch_viscous_pair(L, dt, beta_inv, mode, s);
     k_viscous<<<grid2d(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(
         L.g, L.t, L.ph, dt, beta_inv, mode, s.sigma, s.trr, s.tpp, s.trp, s.divv, s.nu, s.H,
         s.sigma0, s.energy0, s.vr, s.vaz, s.energy, s.qplus, s.qminus, s.corr_phi, s.corr_r);
@@ -2166,8 +2172,9 @@ void launch_ghost(const Launch &L, const BcSpec &bc, double omf, const State &s)
 
 void launch_transport_radial(const Launch &L, double dt, double omf, int chunk, const double *S,
                              const double *vr, const double *vaz, const double *E,
-                             double *const mom[4], double *E_out, double *S_out, bool pair)
+                             double *const mom[4], double *E_out, double *S_out)
 {
+    const bool pair = L.pair;
     const int chunks = (L.g.nr + chunk - 1) / chunk;
     const int bx = 64;
     dim3 grid((L.g.nz + bx - 1) / bx, chunks);
@@ -2224,8 +2231,9 @@ int azimuthal_pair_cells_per_thread(int nz) { return nz <= 2048 ? 4 : (nz <= 614
 
 void launch_transport_azimuthal(const Launch &L, double dt, int block, double *const mom[4],
                                 double *E, double *S, const double *vaz, double *ring_ws,
-                                size_t smem, bool pair)
+                                size_t smem)
 {
+    const bool pair = L.pair;
     const int nq = L.ph.adiabatic ? 5 : 4;
     const size_t dyn = ring_ws ? 0 : smem;
     if (pair) {
@@ -2270,6 +2278,8 @@ void launch_finish(const Launch &L, double omf, double *const mom[4], const doub
                    const double *E_t, const double *vr_in, double *vr_out, double *vaz_out,
                    double *S_out, double *E_out)
 {
+    if (L.pair)
+        return launch_finish_pair(L, omf, mom, S_t, E_t, vr_in, vr_out, vaz_out, S_out, E_out);
     k_finish<<<grid2d(L.g.nz, L.g.nr + 1, L.bx), L.bx, 0, L.stream>>>(
         L.g, L.t, L.ph, omf, mom[0], mom[1], mom[2], mom[3], S_t, E_t, vr_in, vr_out, vaz_out,
         S_out, E_out);

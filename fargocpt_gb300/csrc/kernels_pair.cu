@@ -1,0 +1,495 @@
+// The FP64 form's cell kernels with their arithmetic in float pairs
+// (fp64_pair.cuh): source terms, artificial viscosity, the viscous stress
+// tensor and velocity update with SubStep3, and the velocities rebuilt from
+// the transported momenta.
+//
+// The FP64 kernels (kernels_fp64.cu) run at 85% of GB300's FP64 pipe and
+// 6-17% of its HBM bandwidth: the FP64 pipe is the bound.  Here every stored
+// double is split into a pair on the integer pipe, the arithmetic is pair
+// arithmetic (48 significant bits, errors within a few 2^-47 of the
+// operands), and FP64 is kept for three things:
+//  * the state: an update x += dx adds the pair increment, joined into a
+//    double, to the FP64 value of x, so that a step loses the pair's
+//    rounding of the increment, not of the state;
+//  * the differences of stored values whose gradient cancels: the potential
+//    and the pressure in the source terms (neighbouring values agree to 2 or
+//    3 digits, so a pair's 2^-48 of each value would be 2^-40 of their
+//    difference; the FP64 difference is exact, as in the reference);
+//  * the floors (temperature_floor, the sigma floor), screened in FP32 so
+//    that only values near a bound take the FP64 comparison, which then
+//    gives the reference's clamped value exactly.
+// Each kernel cites the reference function it follows and has the grid and
+// the ring ranges of its FP64 counterpart.
+#include "fp64_pair.cuh"
+#include "hydro.cuh"
+#include "kernels.h"
+
+#include <math.h>
+
+namespace fgpu {
+namespace {
+
+#define CELL(i, j) ((size_t)(i) * (size_t)nz + (size_t)(j))
+
+__device__ __forceinline__ int nxt(int j, int nz) { return j == nz - 1 ? 0 : j + 1; }
+__device__ __forceinline__ int prv(int j, int nz) { return j == 0 ? nz - 1 : j - 1; }
+
+__device__ __forceinline__ f2 operator+(f2 a, f2 b) { return f2_sadd(a, b); }
+__device__ __forceinline__ f2 operator-(f2 a, f2 b) { return f2_ssub(a, b); }
+__device__ __forceinline__ f2 operator-(f2 a) { return f2_neg(a); }
+__device__ __forceinline__ f2 operator*(f2 a, f2 b) { return f2_smul(a, b); }
+__device__ __forceinline__ f2 operator/(f2 a, f2 b) { return f2_sdiv(a, b); }
+
+// a stored double, a kernel argument or a literal as a pair
+__device__ __forceinline__ f2 P(double x) { return f2_split(x); }
+// ring i's value of one of the per-ring tables as a pair
+__device__ __forceinline__ f2 T(const Tables &t, const double *tab, int i)
+{
+    const float2 v = t.ptab[(tab - t.tbase) + i];
+    return f2{v.x, v.y};
+}
+// the FP64 difference of two stored values, as a pair
+__device__ __forceinline__ f2 D(double a, double b) { return f2_split(a - b); }
+// x s for a power of two s (exact)
+__device__ __forceinline__ f2 sc(f2 x, float s) { return f2{__fmul_rn(x.h, s), __fmul_rn(x.l, s)}; }
+__device__ __forceinline__ bool negative(f2 x) { return x.h < 0.f; }
+// x + dx: the FP64 value plus the joined pair increment
+__device__ __forceinline__ double upd(double x, f2 dx) { return x + f2_to_double(dx); }
+__device__ __forceinline__ f2 f2_sqrt(f2 x) { return x * f2_rsqrt(x); }
+
+// x truncated to a float (relative error below 2^-23) for
+// 2^-126 <= |x| < 2^128, on the integer pipe; ok is false elsewhere
+__device__ __forceinline__ float ftrunc(double x, bool &ok)
+{
+    const unsigned w1 = (unsigned)__double2hiint(x), w0 = (unsigned)__double2loint(x);
+    const unsigned ax = w1 & 0x7fffffffu;
+    ok = ax - (897u << 20) < (254u << 20);
+    return __uint_as_float(__funnelshift_l(w0, ax - (896u << 20), 3) | (w1 & 0x80000000u));
+}
+
+// temperature_floor (the FP64 kernels' helper; floors of Transport,
+// TransportEuler.cpp:122-127, and SubStep3): e clamped into
+// [sigma emin_fac, sigma emax_fac], NaN to the lower bound, as in the FP64
+// form.  The FP32 screen passes e only when it lies inside the bounds by
+// more than 2^-20 of them (the truncations and roundings of the screen are
+// below 2^-22), so an e it passes is one the FP64 clamp leaves alone.
+__device__ __forceinline__ double floor_e(double e, double sigma, const Phys &ph)
+{
+    const float emin_f = ph.emin_fac_f, emax_f = ph.emax_fac_f;
+    bool ok_e, ok_s;
+    const float ef = ftrunc(e, ok_e), sf = ftrunc(sigma, ok_s);
+    const float lo = __fmul_rn(__fmul_rn(sf, emin_f), 1.0f + 0x1p-20f);
+    const float hi = __fmul_rn(__fmul_rn(sf, emax_f), 1.0f - 0x1p-20f);
+    if (ok_e && ok_s && ef > lo && ef < hi) return e;
+    const double emin = sigma * ph.emin_fac;
+    const double emax = sigma * ph.emax_fac;
+    if (!(e > emin)) e = emin;
+    if (!(e < emax)) e = emax;
+    return e;
+}
+
+// exp(x) - 1 for |x| <= 1/64 in pairs: x + x^2/2 + x^3/6 in pair arithmetic,
+// the x^4 tail (below 6.0e-8) in FP32 (its rounding below 2^-48)
+__device__ __forceinline__ f2 f2_expm1_small(f2 x)
+{
+    const f2 x2 = x * x;
+    const f2 x3 = x2 * x;
+    const float xh = x.h;
+    float p = __fmaf_rn(xh, 1.0f / 5040.0f, 1.0f / 720.0f);
+    p = __fmaf_rn(p, xh, 1.0f / 120.0f);
+    p = __fmaf_rn(p, xh, 1.0f / 24.0f);
+    const float tail = __fmul_rn(__fmul_rn(x2.h, x2.h), p);
+    const f2 sixth = P(1.0 / 6.0);
+    return x + (sc(x2, 0.5f) + (x3 * sixth + f2{tail, 0.f}));
+}
+
+// update_with_sourceterms (SourceEuler.cpp:369-450): the momentum updates
+// from the pressure gradient, the potential and the centrifugal term
+__global__ void k_source_p(Geo g, Tables t, double dt, double omega_frame,
+                           const double *__restrict__ S, const double *__restrict__ Pr,
+                           const double *__restrict__ pot, const double *__restrict__ vr_in,
+                           const double *__restrict__ vaz_in, double *__restrict__ vr_out,
+                           double *__restrict__ vaz_out)
+{
+    const int nz = g.nz, nr = g.nr;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;  // 0 .. nr
+    if (j >= nz) return;
+    const f2 pdt = P(dt);
+    double vr = vr_in[CELL(i, j)];
+    if (i >= 2 && i < nr - 1) {
+        const size_t c = CELL(i, j), cm = CELL(i - 1, j);
+        const f2 idr = T(t, t.InvDiffRmed, i);
+        const f2 gradp = sc(D(Pr[c], Pr[cm]), 2.0f) / (P(S[c]) + P(S[cm])) * idr;
+        const f2 gradphi = D(pot[c], pot[cm]) * idr;
+        const int jn = nxt(j, nz);
+        const f2 vsum = (P(vaz_in[c]) + P(vaz_in[CELL(i, jn)])) +
+                        (P(vaz_in[cm]) + P(vaz_in[CELL(i - 1, jn)]));
+        const f2 vt = sc(vsum, 0.25f) + T(t, t.Rinf, i) * P(omega_frame);
+        const f2 centrifugal = vt * vt * T(t, t.InvRinf, i);
+        vr = upd(vr, pdt * (centrifugal - (gradp + gradphi)));
+    }
+    vr_out[CELL(i, j)] = vr;
+    if (i < nr) {
+        double va = vaz_in[CELL(i, j)];
+        if (i >= 1 && i < nr - 1) {
+            const size_t c = CELL(i, j), cp = CELL(i, prv(j, nz));
+            const f2 invdx = T(t, t.InvDxSrc, i);
+            const f2 gradp = sc(D(Pr[c], Pr[cp]), 2.0f) / (P(S[c]) + P(S[cp])) * invdx;
+            const f2 gradphi = D(pot[c], pot[cp]) * invdx;
+            va = upd(va, -(pdt * (gradp + gradphi)));
+        }
+        vaz_out[CELL(i, j)] = va;
+    }
+}
+
+// compression heating (SourceEuler.cpp:1045-1092) and the artificial
+// pressures with their dissipation (artificial_viscosity.cpp:35-91,
+// 141-230), as k_artvisc_q
+__global__ void k_artvisc_q_p(Geo g, Tables t, Phys ph, double dt, const double *__restrict__ S,
+                              const double *__restrict__ vr, const double *__restrict__ vaz,
+                              double *__restrict__ E, double *__restrict__ Qr,
+                              double *__restrict__ Qp)
+{
+    const int nz = g.nz, nr = g.nr;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;  // 0 .. nr - 1
+    if (j >= nz) return;
+    const int jn = nxt(j, nz);
+    const size_t c = CELL(i, j);
+    const f2 pdt = P(dt);
+    const f2 vr0 = P(vr[c]), vr1 = P(vr[CELL(i + 1, j)]);
+    const f2 va0 = P(vaz[c]), va1 = P(vaz[CELL(i, jn)]);
+    const f2 invdphi = P(g.invdphi);
+    double e = 0.0;
+    f2 de{0.f, 0.f};  // the energy's increment beyond the compression factor
+    if (ph.adiabatic) {
+        e = E[c];
+        if (i < nr - 1) {
+            const f2 div_v = (vr1 * T(t, t.Rinf, i + 1) - vr0 * T(t, t.Rinf, i)) *
+                                 T(t, t.InvDiffRsupRb, i) +
+                             (va1 - va0) * invdphi * T(t, t.InvRmed, i);
+            const f2 x = -(P(ph.gm1) * pdt * div_v);
+            if (fabsf(x.h) <= 0.015625f) {
+                de = P(e) * f2_expm1_small(x);
+            } else {
+                e = e * exp(f2_to_double(x));  // shocks: FP64 exp
+            }
+        }
+    }
+    if (ph.art_visc_sn) {
+        const f2 sig = P(S[c]);
+        const f2 C2 = P(ph.C2);
+        const f2 dv_r = vr1 - vr0;
+        const f2 qr = negative(dv_r) ? C2 * sig * (dv_r * dv_r) : f2{0.f, 0.f};
+        const f2 dv_p = va1 - va0;
+        const f2 qp = negative(dv_p) ? C2 * sig * (dv_p * dv_p) : f2{0.f, 0.f};
+        Qr[c] = f2_to_double(qr);
+        Qp[c] = f2_to_double(qp);
+        if (ph.adiabatic && ph.dissipation && i >= 1 && i < nr - 1) {
+            de = de - pdt * (qr * dv_r * T(t, t.InvDiffRsup, i) + qp * dv_p * T(t, t.InvDxTheta, i));
+        }
+    }
+    if (ph.art_visc_tw) {
+        // update_with_artificial_viscosity_TW, artificial_viscosity.cpp:52-91
+        const f2 sig = P(S[c]);
+        const f2 eps_rr = (vr1 - vr0) * T(t, t.InvDiffRsup, i);
+        const f2 eps_pp = T(t, t.InvRmed, i) * ((va1 - va0) * invdphi + sc(vr1 + vr0, 0.5f));
+        const f2 sum = eps_rr + eps_pp;
+        const f2 div_V = negative(sum) ? sum : f2{0.f, 0.f};
+        const f2 third = P(1.0 / 3.0);
+        const f2 lsig = T(t, t.LSqTW, i) * sig;
+        Qr[c] = f2_to_double(-(lsig * div_V) * (eps_rr - third * div_V));
+        Qp[c] = f2_to_double(-(lsig * div_V) * (eps_pp - third * div_V));
+        if (ph.adiabatic && ph.dissipation && i >= 1 && i < nr - 1) {
+            const f2 d = eps_rr - eps_pp;
+            const f2 qplus = -(T(t, t.LSqTW, i) * div_V * sig * third) *
+                             (eps_rr * eps_rr + eps_pp * eps_pp + d * d);
+            de = de + qplus * pdt;
+        }
+    }
+    if (ph.adiabatic) {
+        e = upd(e, de);
+        if (ph.dissipation) e = floor_e(e, S[c], ph);
+        E[c] = e;
+    }
+}
+
+// the artificial-viscosity velocity updates (artificial_viscosity.cpp:
+// 93-139, 232-290) and the derived c_s, H, nu of the ideal EOS
+// (compute_sound_speed_normal, compute_scale_height_old, update_viscosity),
+// as k_artvisc_v
+__global__ void k_artvisc_v_p(Geo g, Tables t, Phys ph, double dt, const double *__restrict__ S,
+                              const double *__restrict__ E, const double *__restrict__ Qr,
+                              const double *__restrict__ Qp, double *__restrict__ vr,
+                              double *__restrict__ vaz, double *__restrict__ cs,
+                              double *__restrict__ H, double *__restrict__ nu)
+{
+    const int nz = g.nz, nr = g.nr;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;  // 0 .. nr - 1
+    if (j >= nz) return;
+    const size_t c = CELL(i, j);
+    const f2 pdt = P(dt);
+    if (ph.art_visc_sn) {
+        if (i >= 2 && i < nr - 1) {
+            const size_t cm = CELL(i - 1, j);
+            const f2 a = sc(pdt, 2.0f) / (P(S[c]) + P(S[cm]));
+            vr[c] = upd(vr[c], -(a * (P(Qr[c]) - P(Qr[cm])) * T(t, t.InvDiffRmed, i)));
+        }
+        if (i >= 1 && i < nr - 1) {
+            const size_t cp = CELL(i, prv(j, nz));
+            const f2 a = sc(pdt, 2.0f) / (P(S[c]) + P(S[cp]));
+            vaz[c] = upd(vaz[c], -(a * (P(Qp[c]) - P(Qp[cp])) * T(t, t.InvDxTheta, i)));
+        }
+    }
+    if (ph.art_visc_tw) {
+        if (i >= 1 && i < nr - 1) {
+            const size_t cp = CELL(i, prv(j, nz));
+            const f2 avg = sc(P(S[c]) + P(S[cp]), 0.5f);
+            vaz[c] = upd(vaz[c], pdt / avg * T(t, t.InvDxSrc, i) * (P(Qp[c]) - P(Qp[cp])));
+        }
+        if (i >= 2 && i < nr - 1) {
+            const size_t cm = CELL(i - 1, j);
+            const f2 avg = sc(P(S[c]) + P(S[cm]), 0.5f);
+            const f2 br = (P(Qr[c]) * T(t, t.Rmed, i) - P(Qr[cm]) * T(t, t.Rmed, i - 1)) -
+                          sc(P(Qp[c]) + P(Qp[cm]), 0.5f) * T(t, t.DiffRmed, i);
+            vr[c] = upd(vr[c], P(ph.rvf) * (pdt / avg) * T(t, t.TwoOverDRmed2, i) * br);
+        }
+    }
+    if (ph.adiabatic) {
+        const f2 c_s = f2_sqrt(P(ph.g_gm1) * (P(E[c]) / P(S[c])));
+        const f2 h = c_s * T(t, t.HFacAdi, i);
+        cs[c] = f2_to_double(c_s);
+        H[c] = f2_to_double(h);
+        nu[c] = ph.alpha > 0 ? f2_to_double(P(ph.alpha) * h * c_s) : ph.constant_viscosity;
+    }
+}
+
+// the viscous stress tensor (viscosity.cpp:60-247), as k_stress
+__global__ void k_stress_p(Geo g, Tables t, const double *__restrict__ S,
+                           const double *__restrict__ vr, const double *__restrict__ vaz,
+                           const double *__restrict__ nu, double *__restrict__ divv,
+                           double *__restrict__ trr, double *__restrict__ tpp,
+                           double *__restrict__ trp)
+{
+    const int nz = g.nz, nr = g.nr;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;  // 0 .. nr - 1
+    if (j >= nz) return;
+    const size_t c = CELL(i, j);
+    const int jn = nxt(j, nz);
+    const f2 vr0 = P(vr[c]), vr1 = P(vr[CELL(i + 1, j)]);
+    const f2 va0 = P(vaz[c]), va1 = P(vaz[CELL(i, jn)]);
+    const f2 n = P(nu[c]), sg = P(S[c]);
+    const f2 invdphi = P(g.invdphi);
+    const f2 irm = T(t, t.InvRmed, i);
+    const f2 third = P(1.0 / 3.0);
+    const f2 dv = (vr1 * T(t, t.Rinf, i + 1) - vr0 * T(t, t.Rinf, i)) * T(t, t.InvDiffRsupRb, i) +
+                  (va1 - va0) * invdphi * irm;
+    divv[c] = f2_to_double(dv);
+    const f2 two_n_sg = sc(n * sg, 2.0f);
+    const f2 drr = (vr1 - vr0) * T(t, t.InvDiffRsup, i);
+    trr[c] = f2_to_double(two_n_sg * (drr - third * dv));
+    const f2 dpp = (va1 - va0) * invdphi * irm + sc(vr1 + vr0, 0.5f) * irm;
+    tpp[c] = f2_to_double(two_n_sg * (dpp - third * dv));
+    if (i >= 1) {
+        const int jp = prv(j, nz);
+        const size_t cm = CELL(i - 1, j), cp = CELL(i, jp), cmp = CELL(i - 1, jp);
+        const f2 dvazirdr = (va0 * irm - P(vaz[cm]) * T(t, t.InvRmed, i - 1)) *
+                            T(t, t.InvDiffRmed, i);
+        const f2 dvrdphi = (vr0 - P(vr[cp])) * invdphi;
+        const f2 drp = T(t, t.Rinf, i) * dvazirdr + dvrdphi * T(t, t.InvRinf, i);
+        const f2 n4 = sc((n + P(nu[cm])) + (P(nu[cp]) + P(nu[cmp])), 0.25f);
+        const f2 s4 = sc((sg + P(S[cm])) + (P(S[cp]) + P(S[cmp])), 0.25f);
+        trp[c] = f2_to_double(n4 * s4 * drp);
+    }
+}
+
+// the viscous velocity update (viscosity.cpp:249-348 without
+// StabilizeViscosity, which the FP64 kernel serves) and SubStep3:
+// thermal relaxation (SourceEuler.cpp:632-690), viscous heating (:496-536),
+// the radiative alpha factor (:905-912) and the energy update, as k_viscous
+__global__ void k_viscous_p(Geo g, Tables t, Phys ph, double dt, double beta_inv, int mode,
+                            const double *__restrict__ S, const double *__restrict__ trr,
+                            const double *__restrict__ tpp, const double *__restrict__ trp,
+                            const double *__restrict__ divv, const double *__restrict__ nu,
+                            const double *__restrict__ H, const double *__restrict__ S0,
+                            const double *__restrict__ E0, double *__restrict__ vr,
+                            double *__restrict__ vaz, double *__restrict__ E,
+                            double *__restrict__ qplus, double *__restrict__ qminus)
+{
+    const int nz = g.nz, nr = g.nr;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;  // 0 .. nr - 1
+    if (j >= nz) return;
+    const size_t c = CELL(i, j);
+    const int jp = prv(j, nz), jn = nxt(j, nz);
+    const f2 pdt = P(dt);
+    const f2 invdphi = P(g.invdphi);
+    if (mode & 1) {
+        if (i >= 1 && i < nr - 1) {
+            const f2 avg = sc(P(S[c]) + P(S[CELL(i, jp)]), 0.5f);
+            const f2 dVp = pdt * T(t, t.InvRmed, i) / avg *
+                           (T(t, t.TwoOverDRa2, i) * (T(t, t.RinfSq, i + 1) * P(trp[CELL(i + 1, j)]) -
+                                                      T(t, t.RinfSq, i) * P(trp[c])) +
+                            (P(tpp[c]) - P(tpp[CELL(i, jp)])) * invdphi);
+            vaz[c] = upd(vaz[c], dVp);
+        }
+        if (i >= 2 && i < nr - 1) {
+            const size_t cm = CELL(i - 1, j);
+            const f2 avg = sc(P(S[c]) + P(S[cm]), 0.5f);
+            const f2 dVr = pdt / avg * P(ph.rvf) * T(t, t.TwoOverRmedSum, i) *
+                           ((T(t, t.Rmed, i) * P(trr[c]) - T(t, t.Rmed, i - 1) * P(trr[cm])) *
+                                T(t, t.InvDiffRmed, i) +
+                            (P(trp[CELL(i, jn)]) - P(trp[c])) * invdphi -
+                            sc(P(tpp[c]) + P(tpp[cm]), 0.5f));
+            vr[c] = upd(vr[c], dVr);
+        }
+    }
+    if (!(mode & 6) || !ph.adiabatic) return;
+    const f2 zero{0.f, 0.f};
+    f2 qp = zero, qm = zero;
+    const double e = E[c];
+    const double sig_d = S[c];
+    const f2 ep = P(e), sig = P(sig_d);
+    const bool active = i >= 1 && i < nr - 1;
+    if (active) {
+        if (ph.cooling_beta) {
+            f2 delta_E = ep;
+            if (ph.beta_ref == 1) {
+                delta_E = delta_E - P(E0[c]) / P(S0[c]) * sig;
+            } else if (ph.beta_ref == 2) {
+                delta_E = delta_E - T(t, t.EModel, i) * sig;
+            } else if (ph.beta_ref == 3) {
+                delta_E = delta_E - sig * P(ph.emin_fac);
+            }
+            qm = delta_E * T(t, t.OmegaK, i) * P(beta_inv);
+        }
+        if (ph.heating_viscous) {
+            const double nd = nu[c];
+            if (nd != 0.0) {
+                const f2 n = P(nd);
+                const f2 tau_r_phi = sc((P(trp[c]) + P(trp[CELL(i + 1, j)])) +
+                                            (P(trp[CELL(i, jn)]) + P(trp[CELL(i + 1, jn)])),
+                                        0.25f);
+                const f2 t_rr = P(trr[c]), t_pp = P(tpp[c]), d = P(divv[c]);
+                const f2 ns = n * sig;
+                f2 q = (t_rr * t_rr + sc(tau_r_phi * tau_r_phi, 2.0f) + t_pp * t_pp) / sc(ns, 2.0f);
+                q = q + P(2.0 / 9.0) * ns * (d * d);
+                qp = q * P(ph.hvf);
+            }
+        }
+        const f2 x = P(ph.mu_gm1_over_R) / sig;
+        const f2 x2 = x * x;
+        const f2 alpha = P(1.0) + P(H[c]) * P(ph.cool_const) * (x2 * x2) * (ep * ep * ep);
+        const f2 inv_alpha = f2_rcp(alpha);
+        qp = qp * inv_alpha;
+        qm = qm * inv_alpha;
+    }
+    double qp_d = f2_to_double(qp), qm_d = f2_to_double(qm);
+    if (mode & 4) {
+        double e_new = e;
+        if (active) {
+            e_new = upd(e, pdt * (qp - qm));
+            if (sig_d < ph.sigma_floor10) {
+                // TAU_EFF is zero on this path: the equilibrium energy is 0
+                qm_d = qp_d;
+                e_new = 0.0;
+            }
+        }
+        E[c] = floor_e(e_new, sig_d, ph);
+    }
+    qplus[c] = qp_d;
+    qminus[c] = qm_d;
+}
+
+// compute_velocities_from_momenta (TransportEuler.cpp:498-535), the sigma
+// floor (SourceEuler.cpp:102-134) and the temperature floor, as k_finish
+__global__ void k_finish_p(Geo g, Tables t, Phys ph, double omf, const double *__restrict__ mom0,
+                           const double *__restrict__ mom1, const double *__restrict__ mom2,
+                           const double *__restrict__ mom3, const double *__restrict__ S_t,
+                           const double *__restrict__ E_t, const double *__restrict__ vr_in,
+                           double *__restrict__ vr_out, double *__restrict__ vaz_out,
+                           double *__restrict__ S_out, double *__restrict__ E_out)
+{
+    const int nz = g.nz, nr = g.nr;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;  // 0 .. nr
+    if (j >= nz) return;
+    const size_t c = CELL(i, j);
+    if (i == nr) {
+        vr_out[c] = vr_in[c];
+        return;
+    }
+    const double s = S_t[c];
+    const f2 sp = P(s);
+    if (i == 0) {
+        vr_out[c] = 0.0;
+    } else {
+        const size_t cm = CELL(i - 1, j);
+        vr_out[c] = f2_to_double((P(mom0[cm]) + P(mom1[c])) / (P(S_t[cm]) + sp));
+    }
+    const size_t cjm = CELL(i, prv(j, nz));
+    vaz_out[c] = f2_to_double((P(mom2[cjm]) + P(mom3[c])) / (P(S_t[cjm]) + sp) *
+                                  T(t, t.InvRmed, i) -
+                              T(t, t.Rmed, i) * P(omf));
+    // s < sigma_min on the bit patterns (sigma_min >= 0; a NaN stays)
+    const long long bs = __double_as_longlong(s);
+    const bool nan = (bs & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
+    const double sf = (!nan && bs < __double_as_longlong(ph.sigma_min)) ? ph.sigma_min : s;
+    S_out[c] = sf;
+    if (ph.adiabatic) E_out[c] = floor_e(E_t[c], sf, ph);
+}
+
+dim3 grid2(int nz, int rows, int bx) { return dim3((nz + bx - 1) / bx, rows); }
+
+}  // namespace
+
+void launch_source_pair(const Launch &L, double dt, double omf, const double *S, const double *Pr,
+                        const double *pot, const double *vr_in, const double *vaz_in,
+                        double *vr_out, double *vaz_out)
+{
+    k_source_p<<<grid2(L.g.nz, L.g.nr + 1, L.bx), L.bx, 0, L.stream>>>(
+        L.g, L.t, dt, omf, S, Pr, pot, vr_in, vaz_in, vr_out, vaz_out);
+}
+
+void launch_artvisc_q_pair(const Launch &L, double dt, const double *S, const double *vr,
+                           const double *vaz, double *E, double *Qr, double *Qp)
+{
+    k_artvisc_q_p<<<grid2(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(L.g, L.t, L.ph, dt, S, vr,
+                                                                      vaz, E, Qr, Qp);
+}
+
+void launch_artvisc_v_pair(const Launch &L, double dt, const double *S, const double *E,
+                           const double *Qr, const double *Qp, double *vr, double *vaz, double *cs,
+                           double *H, double *nu)
+{
+    k_artvisc_v_p<<<grid2(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(L.g, L.t, L.ph, dt, S, E, Qr,
+                                                                      Qp, vr, vaz, cs, H, nu);
+}
+
+void launch_stress_pair(const Launch &L, const double *S, const double *vr, const double *vaz,
+                        const double *nu, double *divv, double *trr, double *tpp, double *trp)
+{
+    k_stress_p<<<grid2(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(L.g, L.t, S, vr, vaz, nu, divv,
+                                                                   trr, tpp, trp);
+}
+
+void launch_viscous_pair(const Launch &L, double dt, double beta_inv, int mode, const State &s)
+{
+    k_viscous_p<<<grid2(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(
+        L.g, L.t, L.ph, dt, beta_inv, mode, s.sigma, s.trr, s.tpp, s.trp, s.divv, s.nu, s.H,
+        s.sigma0, s.energy0, s.vr, s.vaz, s.energy, s.qplus, s.qminus);
+}
+
+void launch_finish_pair(const Launch &L, double omf, double *const mom[4], const double *S_t,
+                        const double *E_t, const double *vr_in, double *vr_out, double *vaz_out,
+                        double *S_out, double *E_out)
+{
+    k_finish_p<<<grid2(L.g.nz, L.g.nr + 1, L.bx), L.bx, 0, L.stream>>>(
+        L.g, L.t, L.ph, omf, mom[0], mom[1], mom[2], mom[3], S_t, E_t, vr_in, vr_out, vaz_out,
+        S_out, E_out);
+}
+
+}  // namespace fgpu

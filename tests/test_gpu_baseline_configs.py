@@ -14,8 +14,8 @@ circular orbit at each step's start.  Bars: every dt of the sequence within
 <= 1e-10 on sigma, v_r, v_phi and e after 100 steps, the disk force on the
 planet within 1e-9 relative, the gas mass and angular momentum within 1e-12.
 The oracle runs the 512 x 1536 disk's 100 steps in a few seconds on the
-host's cores.  Both arithmetics of the transports are held to these bars:
-float pairs (the default) and FP64 (FARGO_GB300_FP64_TRANSPORT=fp64).
+host's cores.  Both arithmetics of the kernels are held to these bars:
+float pairs (the default) and FP64 (FARGO_GB300_FP64_ARITH=fp64).
 """
 import math
 import os
@@ -56,13 +56,13 @@ def _run(cls, name, steps):
     return h, clock, monitors, d
 
 
-@pytest.mark.parametrize("transport", ["pair", "fp64"])
+@pytest.mark.parametrize("arith", ["pair", "fp64"])
 @pytest.mark.parametrize("name", ["c1", "c2"])
-def test_fp64_benchmark_disk_100_steps_against_oracle(name, transport, monkeypatch):
+def test_fp64_benchmark_disk_100_steps_against_oracle(name, arith, monkeypatch):
     from fargocpt_gb300.engine import Engine
     from oracle.oracle_py import OracleState, set_threads
 
-    monkeypatch.setenv("FARGO_GB300_FP64_TRANSPORT", transport)
+    monkeypatch.setenv("FARGO_GB300_FP64_ARITH", arith)
     set_threads(os.cpu_count() or 1)
     o, co, mo, d = _run(OracleState, name, 100)
     g, cg, mg, _ = _run(Engine, name, 100)
@@ -85,13 +85,13 @@ def test_fp64_benchmark_disk_100_steps_against_oracle(name, transport, monkeypat
 
 
 def test_transport_arithmetic_request_is_checked(monkeypatch, capfd):
-    """An unknown FARGO_GB300_FP64_TRANSPORT value is refused at fgpu_create
+    """An unknown FARGO_GB300_FP64_ARITH value is refused at fgpu_create
     (status BAD_ARG, the message on stderr), never replaced by a default."""
     from fargocpt_gb300 import setups
     from fargocpt_gb300.engine import Engine, EngineError
 
     params, d, radii, fields, nbody = setups.build("c1")
-    monkeypatch.setenv("FARGO_GB300_FP64_TRANSPORT", "fp128")
+    monkeypatch.setenv("FARGO_GB300_FP64_ARITH", "fp128")
     with pytest.raises(EngineError, match="BAD_ARG"):
         Engine(params, radii)
-    assert "FARGO_GB300_FP64_TRANSPORT=fp128" in capfd.readouterr().err
+    assert "FARGO_GB300_FP64_ARITH=fp128" in capfd.readouterr().err

@@ -7,7 +7,7 @@ implementation):
   disk by k cells rotates the result by k cells, within the FP64 bar of
   1e-10 (the ring reductions change summation order with the rotation; v_r
   near the inner damping zone, the most sensitive field, differs by 1.7e-11
-  of its largest value after one step, whichever arithmetic the transports
+  of its largest value after one step, whichever arithmetic the kernels
   use);
 * axisymmetry: an axisymmetric disk without a planet stays axisymmetric;
 * finiteness after many steps of the C2-size adiabatic disk.
