@@ -100,40 +100,41 @@ __device__ __forceinline__ void f2_accumulate(float &hi, float &lo, f2 x)
 // doubles with bit operations and one integer-to-float conversion.
 // ---------------------------------------------------------------------------
 
-// x as a normalised pair, |x - (h + l)| <= 2^-48 |x|: h is x truncated to
+// x as a pair, |x - (h + l)| <= 2^-48 |x|, |l| < ulp(h): h is x truncated to
 // 24 significant bits (the sign, the rebased exponent and the top 23
 // mantissa bits, shifted into place), l the remaining 29 mantissa bits
-// converted to float and scaled by 2^(e - 1075).  Both are normal floats for
-// biased exponents e in [949, 1150] (2^-74 <= |x| < 2^128).  Below that range
-// x becomes zero (an absolute error under 2^-74); at or above it, and for
-// infinities and NaN, a NaN of x's sign, so that a state out of the pairs'
-// range shows as non-finite.  Branch-free: the callers' loops over a thread's
-// cells stay one instruction stream.
+// converted to float and scaled by 2^(e - 1075).  (The pair is not
+// renormalised: the pair operations take |l| < ulp(h) with error bounds at
+// most twice those for |l| <= ulp(h) / 2, and the sign of h is the sign of
+// x.)  Both are normal floats for biased exponents e in [949, 1150]
+// (2^-74 <= |x| < 2^128).  Below that range x becomes zero (an absolute
+// error under 2^-74); at or above it, and for infinities and NaN, a NaN of
+// x's sign, so that a state out of the pairs' range shows as non-finite.
+// Branch-free: the callers' loops over a thread's cells stay one
+// instruction stream.
 __device__ __forceinline__ f2 f2_split(double x)
 {
     const unsigned w1 = (unsigned)__double2hiint(x), w0 = (unsigned)__double2loint(x);
     const unsigned ax = w1 & 0x7fffffffu, sign = w1 & 0x80000000u;
     const unsigned hb = __funnelshift_l(w0, ax - (896u << 20), 3);
     const float scale = __uint_as_float((hb & 0x7f800000u) - (52u << 23));
-    const float l = __fmul_rn(__uint2float_rn(w0 & 0x1fffffffu), scale);
-    const f2 p = fast_two_sum(__uint_as_float(hb | sign), __uint_as_float(__float_as_uint(l) | sign));
-    const bool tiny = ax < (949u << 20), huge = ax >= (1151u << 20);
-    const float nan = __uint_as_float(0x7fc00000u | sign);
-    return f2{tiny ? 0.0f : (huge ? nan : p.h), tiny ? 0.0f : (huge ? nan : p.l)};
+    const unsigned lb = __float_as_uint(__fmul_rn(__uint2float_rn(w0 & 0x1fffffffu), scale));
+    const bool in = ax - (949u << 20) < (202u << 20);
+    const unsigned out = ax < (949u << 20) ? 0u : (0x7fc00000u | sign);
+    return f2{__uint_as_float(in ? (hb | sign) : out), __uint_as_float(in ? (lb | sign) : out)};
 }
 
 // a float as a double, exactly: the exponent rebased, the mantissa shifted;
-// zero and subnormal floats (below 2^-126) give a signed zero, infinities an
-// infinity, NaN a NaN.  Branch-free.
+// zero and subnormal floats (below 2^-126) give a signed zero, infinities and
+// NaN a NaN.  Branch-free.
 __device__ __forceinline__ double f_to_d(float f)
 {
     const unsigned b = __float_as_uint(f);
     const unsigned ef = (b >> 23) & 0xffu, sign = b & 0x80000000u;
-    const unsigned hi = sign | (((b & 0x7fffffffu) >> 3) + (896u << 20));
-    const unsigned special = sign | ((b & 0x7fffffu) ? 0x7ff80000u : 0x7ff00000u);
-    const unsigned w1 = ef == 0u ? sign : (ef == 255u ? special : hi);
-    const unsigned w0 = (ef == 0u || ef == 255u) ? 0u : (b << 29);
-    return __hiloint2double((int)w1, (int)w0);
+    const bool normal = ef - 1u < 254u;
+    const unsigned w1 = normal ? (sign | (((b & 0x7fffffffu) >> 3) + (896u << 20)))
+                               : (sign | (ef ? 0x7ff80000u : 0u));
+    return __hiloint2double((int)w1, (int)(normal ? b << 29 : 0u));
 }
 
 // h + l as a double (one FP64 addition of the two exact conversions)
@@ -160,6 +161,15 @@ __device__ __forceinline__ f2 f2_smul(f2 x, f2 y)
     const f2 c = two_prod(x.h, y.h);
     return fast_two_sum(c.h, __fadd_rn(c.l, __fmaf_rn(x.l, y.h, __fmul_rn(x.h, y.l))));
 }
+// x + a d in one: the product's error-free high part, the sum's TwoSum, one
+// renormalisation
+__device__ __forceinline__ f2 f2_sfma(f2 x, f2 a, f2 d)
+{
+    const f2 p = two_prod(a.h, d.h);
+    const float pl = __fmaf_rn(a.l, d.h, __fmaf_rn(a.h, d.l, p.l));
+    const f2 s = two_sum(x.h, p.h);
+    return fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(x.l, pl)));
+}
 
 __device__ __forceinline__ float rcp_approx(float x)
 {
@@ -176,6 +186,9 @@ __device__ __forceinline__ f2 f2_rcp(f2 d)
     const float e = __fsub_rn(__fsub_rn(1.0f, p.h), p.l);
     return fast_two_sum(r, __fmul_rn(r, e));
 }
+
+// sqrt(x) for x > 0: x rsqrt(x)
+__device__ __forceinline__ f2 f2_sqrt(f2 x) { return f2_smul(x, f2_rsqrt(x)); }
 
 // p / s for a normal s: q = p.h rcp(s.h), then q + (p - q s) rcp(s.h)
 __device__ __forceinline__ f2 f2_sdiv(f2 p, f2 s)

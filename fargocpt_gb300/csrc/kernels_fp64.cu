@@ -964,7 +964,7 @@ __global__ void k_transport_radial_f2(Geo g, Tables t, double dt, double omf, in
             f2 star[NW];
 #pragma unroll
             for (int q = 0; q < NW; ++q)
-                star[q] = f2_sadd(up ? wa[q] : wb[q], f2_smul(f, up ? da[q] : db[q]));
+                star[q] = f2_sfma(up ? wa[q] : wb[q], f, up ? da[q] : db[q]);
             // base sigma* v, the factor every quantity's flux shares
             const f2 bsv = f2_smul(f2_smul(f2_split(dtdphi * t.Rinf[k]), star[NQ]), f2_split(v));
 #pragma unroll
@@ -1322,10 +1322,15 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(Geo g, Tables t, do
 // cell's slope is still formed once per face that uses it (van Leer's
 // upwind cell of face j is j - 1 or j), the slope array and its barrier
 // go, and shared memory holds the face factors in their place, so that a
-// thread keeps only its faces' interpolation distances in registers.  Loops
-// over the owned cells compute with the index clamped into the ring and guard
-// only their stores (no branch in the body).
-template <int PER, int NQ>
+// thread keeps only its faces' interpolation distances in registers.
+//
+// The four ring arrays carry the periodic neighbours as halo cells: index -2
+// and -1 hold cells nz - 2 and nz - 1, index nz holds cell 0, written by the
+// owners of those cells with the cell itself, so that no index wraps.
+// EXACT (nz == PER blockDim.x): every thread owns PER cells; otherwise the
+// loops compute with the index clamped into the ring and guard only their
+// stores.  Either way the loop bodies have no branch.
+template <int PER, int NQ, bool EXACT>
 __device__ void ring_advection_pass_f2(double *Sg, f2 *SP, f2 *W, f2 *CF, f2 *F,
                                        double *const *qrow, const double *v, double dt,
                                        double dxtheta, double half_invdx, double dxrad_invsurf,
@@ -1341,15 +1346,20 @@ __device__ void ring_advection_pass_f2(double *Sg, f2 *SP, f2 *W, f2 *CF, f2 *F,
     const f2 cvel = f2_split(dxrad_invsurf / kdt);
     f2 am[PER];
     unsigned pos = 0;  // bit n: the upwind cell of face tid + n bs is its left neighbour
-    auto cell = [&](int n) { return min(tid + n * bs, nz - 1); };
-    auto owned = [&](int n) { return tid + n * bs < nz; };
-    auto nxt = [&](int j) { return j == nz - 1 ? 0 : j + 1; };
-    auto prv = [&](int j) { return j == 0 ? nz - 1 : j - 1; };
-    // the star value at face j of the quantity X from its upwind cell u
+    auto cell = [&](int n) { return EXACT ? tid + n * bs : min(tid + n * bs, nz - 1); };
+    auto owned = [&](int n) { return EXACT || tid + n * bs < nz; };
+    // X[j] and its halo copy (cells nz - 2, nz - 1 at -2, -1; cell 0 at nz)
+    auto put = [&](f2 *X, int j, f2 x) {
+        X[j] = x;
+        if (j >= nz - 2) X[j - nz] = x;
+        if (j == 0) X[nz] = x;
+    };
+    // the star value at a face of the quantity X from its upwind cell u
+    // (u in -1 .. nz - 1)
     auto star = [&](const f2 *X, int u, f2 a) {
         const f2 x = X[u];
-        const f2 d = lim_f2(f2_ssub(X[nxt(u)], x), f2_ssub(x, X[prv(u)]), mc);
-        return f2_sadd(x, f2_smul(a, d));
+        const f2 d = lim_f2(f2_ssub(X[u + 1], x), f2_ssub(x, X[u - 1]), mc);
+        return f2_sfma(x, a, d);
     };
     // DensityStar and the face factor dxrad S* v / Surf every flux shares
     const double vu = vconst * kdt;
@@ -1362,8 +1372,8 @@ __device__ void ring_advection_pass_f2(double *Sg, f2 *SP, f2 *W, f2 *CF, f2 *F,
         const bool p = positive(vk);
         am[n] = uniform ? au : f2_split(p ? dxk - vk : -(dxk + vk));
         pos |= (unsigned)p << n;
-        const f2 c = f2_smul(f2_smul(cvel, star(SP, p ? prv(j) : j, am[n])), f2_split(vk));
-        if (owned(n)) CF[j] = c;
+        const f2 c = f2_smul(f2_smul(cvel, star(SP, p ? j - 1 : j, am[n])), f2_split(vk));
+        if (owned(n)) put(CF, j, c);
     }
     // per quantity: specific values (with the previous quantity's update),
     // then the fluxes
@@ -1374,12 +1384,12 @@ __device__ void ring_advection_pass_f2(double *Sg, f2 *SP, f2 *W, f2 *CF, f2 *F,
             const int j = cell(n);
             if (q > 0) {
                 double *Qp = qrow[q - 1];
-                const double qn = Qp[j] + f2_to_double(f2_ssub(F[j], F[nxt(j)]));
+                const double qn = Qp[j] + f2_to_double(f2_ssub(F[j], F[j + 1]));
                 if (owned(n)) Qp[j] = qn;
             }
             if (q < NQ) {
                 const f2 w = f2_sdiv(f2_split(qrow[q][j]), SP[j]);
-                if (owned(n)) W[j] = w;
+                if (owned(n)) put(W, j, w);
             }
         }
         if (q == NQ) break;
@@ -1387,8 +1397,8 @@ __device__ void ring_advection_pass_f2(double *Sg, f2 *SP, f2 *W, f2 *CF, f2 *F,
 #pragma unroll
         for (int n = 0; n < PER; ++n) {
             const int j = cell(n);
-            const f2 f = f2_smul(star(W, (pos >> n) & 1u ? prv(j) : j, am[n]), CF[j]);
-            if (owned(n)) F[j] = f;
+            const f2 f = f2_smul(star(W, (pos >> n) & 1u ? j - 1 : j, am[n]), CF[j]);
+            if (owned(n)) put(F, j, f);
         }
         __syncthreads();
     }
@@ -1400,19 +1410,23 @@ __device__ void ring_advection_pass_f2(double *Sg, f2 *SP, f2 *W, f2 *CF, f2 *F,
     for (int n = 0; n < PER; ++n) {
         const int j = cell(n);
         // nothing reads SP in this phase
-        const double s = Sg[j] + f2_to_double(f2_ssub(CF[j], CF[nxt(j)]));
+        const double s = Sg[j] + f2_to_double(f2_ssub(CF[j], CF[j + 1]));
         const f2 sp = f2_split(s);
         if (owned(n)) {
             Sg[j] = s;
-            SP[j] = sp;
+            put(SP, j, sp);
         }
     }
     __syncthreads();
 }
 
+// Shared memory of the pair kernel per ring: four arrays of nz + 4 pairs
+// (two halo cells on either side)
+__host__ __device__ constexpr size_t pair_ring_f2s(int nz) { return (size_t)4 * (nz + 4); }
+
 // WS: the ring's arrays in the per-ring global workspace (rings beyond the
 // shared memory), else in shared memory
-template <int PER, int MAXT, int NQ, bool WS>
+template <int PER, int MAXT, int NQ, bool WS, bool EXACT>
 __global__ void __launch_bounds__(MAXT) k_transport_azimuthal_f2(
     Geo g, Tables t, double dt, int mc, int fast, const double *__restrict__ vaz, double *mom0,
     double *mom1, double *mom2, double *mom3, double *E, double *S, double *ring_ws)
@@ -1423,9 +1437,11 @@ __global__ void __launch_bounds__(MAXT) k_transport_azimuthal_f2(
     const int i = blockIdx.x;
     const int tid = threadIdx.x, bs = blockDim.x;
     const size_t row = (size_t)i * nz;
-    f2 *base = reinterpret_cast<f2 *>(WS ? ring_ws + (size_t)i * 4 * nz : smem);
-    f2 *SP = base, *W = base + nz, *CF = base + 2 * nz, *F = base + 3 * nz;
+    f2 *base = WS ? reinterpret_cast<f2 *>(ring_ws) + (size_t)i * pair_ring_f2s(nz)
+                  : reinterpret_cast<f2 *>(smem);
+    f2 *SP = base + 2, *W = SP + (nz + 4), *CF = W + (nz + 4), *F = CF + (nz + 4);
     double *Sg = S + row;
+    auto owned = [&](int n) { return EXACT || tid + n * bs < nz; };
 
     // compute_average_azimuthal_velocity, :174-189
     double vown[PER];
@@ -1433,7 +1449,7 @@ __global__ void __launch_bounds__(MAXT) k_transport_azimuthal_f2(
 #pragma unroll
     for (int n = 0; n < PER; ++n) {
         const int j = tid + n * bs;
-        if (j < nz) {
+        if (owned(n)) {
             vown[n] = vaz[row + j];
             part += vown[n];
         }
@@ -1448,11 +1464,14 @@ __global__ void __launch_bounds__(MAXT) k_transport_azimuthal_f2(
 #pragma unroll
     for (int n = 0; n < PER; ++n) {
         const int j = tid + n * bs;
-        if (j < nz) {
+        if (owned(n)) {
             double vres = vown[n] - vmean;
             if (!fast) vres = vt + vres;
             vown[n] = vres;
-            SP[j] = f2_split(Sg[j]);
+            const f2 sp = f2_split(Sg[j]);
+            SP[j] = sp;
+            if (j >= nz - 2) SP[j - nz] = sp;
+            if (j == 0) SP[nz] = sp;
         }
     }
     __syncthreads();
@@ -1462,11 +1481,11 @@ __global__ void __launch_bounds__(MAXT) k_transport_azimuthal_f2(
     const double half_invdx = 0.5 * (1.0 / dxtheta);
     const double dxrad = (t.Rsup[i] - t.Rinf[i]) * dt;
     const double invsurf = t.InvSurf[i];
-    ring_advection_pass_f2<PER, NQ>(Sg, SP, W, CF, F, qrow, vown, dt, dxtheta, half_invdx,
-                                    dxrad * invsurf, nz, mc, false, 0.0);
+    ring_advection_pass_f2<PER, NQ, EXACT>(Sg, SP, W, CF, F, qrow, vown, dt, dxtheta, half_invdx,
+                                           dxrad * invsurf, nz, mc, false, 0.0);
     if (fast) {
-        ring_advection_pass_f2<PER, NQ>(Sg, SP, W, CF, F, qrow, vown, dt, dxtheta, half_invdx,
-                                        dxrad * invsurf, nz, mc, true, vt);
+        ring_advection_pass_f2<PER, NQ, EXACT>(Sg, SP, W, CF, F, qrow, vown, dt, dxtheta,
+                                               half_invdx, dxrad * invsurf, nz, mc, true, vt);
     }
     // AdvectSHIFT of every quantity, sigma last, staged through W's doubles
     double *stage = reinterpret_cast<double *>(W);
@@ -1476,13 +1495,13 @@ __global__ void __launch_bounds__(MAXT) k_transport_azimuthal_f2(
 #pragma unroll
         for (int n = 0; n < PER; ++n) {
             const int j = tid + n * bs;
-            if (j < nz) stage[j] = Q[j];
+            if (owned(n)) stage[j] = Q[j];
         }
         __syncthreads();
 #pragma unroll
         for (int n = 0; n < PER; ++n) {
             const int j = tid + n * bs;
-            if (j < nz) {
+            if (owned(n)) {
                 int ji = (j - nshift) % nz;
                 if (ji < 0) ji += nz;
                 Q[j] = stage[ji];
@@ -1730,6 +1749,10 @@ __device__ __forceinline__ double cfl_cell64(const Geo &g, const Tables &t, cons
     return dt_cell;
 }
 
+// PAIR: the ideal-EOS derived quantities (T, c_s, H, nu) in float-pair
+// arithmetic (P = (gamma - 1) e stays one FP64 product: the source terms
+// difference it)
+template <bool PAIR>
 __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const double *__restrict__ S,
                               const double *__restrict__ E, const double *__restrict__ vr,
                               const double *__restrict__ vaz, const double *__restrict__ qplus,
@@ -1785,7 +1808,20 @@ __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const 
         double c_s, n;
         if (mode & 1) {
             const double sg = S[c];
-            if (ph.adiabatic) {
+            if (ph.adiabatic && PAIR) {
+                const double e = E[c];
+                const f2 es = f2_sdiv(f2_split(e), f2_split(sg));
+                T[c] = f2_to_double(f2_smul(f2_split(ph.c_v_inv), es));
+                const f2 cp = f2_sqrt(f2_smul(f2_split(ph.g_gm1), es));
+                const float2 hf = t.ptab[(t.HFacAdi - t.tbase) + i];
+                const f2 hp = f2_smul(cp, f2{hf.x, hf.y});
+                c_s = f2_to_double(cp);
+                cs[c] = c_s;
+                H[c] = f2_to_double(hp);
+                P[c] = ph.gm1 * e;
+                n = ph.alpha > 0 ? f2_to_double(f2_smul(f2_smul(f2_split(ph.alpha), hp), cp))
+                                 : ph.constant_viscosity;
+            } else if (ph.adiabatic) {
                 const double e = E[c];
                 const double es = fast_div1(e, sg);
                 T[c] = ph.c_v_inv * es;
@@ -2201,7 +2237,8 @@ void launch_transport_radial(const Launch &L, double dt, double omf, int chunk, 
     }
 }
 
-size_t azimuthal_smem_bytes(int nz) { return (size_t)4 * nz * sizeof(double); }
+// the larger of the two kernels' rings: the pair kernel's halo cells
+size_t azimuthal_smem_bytes(int nz) { return pair_ring_f2s(nz) * sizeof(f2); }
 
 // Cells per thread of the azimuthal kernel: blocks stay at <= 512 threads so
 // that the per-thread cell arrays fit 128 registers.
@@ -2212,13 +2249,13 @@ cudaError_t prepare_azimuthal(size_t smem)
     cudaError_t e = raise_smem_limit((const void *)k_transport_azimuthal<4>, smem);
     if (e == cudaSuccess) e = raise_smem_limit((const void *)k_transport_azimuthal<8>, smem);
     if (e == cudaSuccess) e = raise_smem_limit((const void *)k_transport_azimuthal<16>, smem);
-    const void *pair_kernels[6] = {
-        (const void *)k_transport_azimuthal_f2<4, 512, 4, false>,
-        (const void *)k_transport_azimuthal_f2<4, 512, 5, false>,
-        (const void *)k_transport_azimuthal_f2<8, 768, 4, false>,
-        (const void *)k_transport_azimuthal_f2<8, 768, 5, false>,
-        (const void *)k_transport_azimuthal_f2<16, 512, 4, false>,
-        (const void *)k_transport_azimuthal_f2<16, 512, 5, false>};
+#define AZ2_FN(P, T, Q, X) (const void *)k_transport_azimuthal_f2<P, T, Q, false, X>
+    const void *pair_kernels[12] = {
+        AZ2_FN(4, 512, 4, false), AZ2_FN(4, 512, 5, false), AZ2_FN(8, 768, 4, false),
+        AZ2_FN(8, 768, 5, false), AZ2_FN(16, 512, 4, false), AZ2_FN(16, 512, 5, false),
+        AZ2_FN(4, 512, 4, true), AZ2_FN(4, 512, 5, true), AZ2_FN(8, 768, 4, true),
+        AZ2_FN(8, 768, 5, true), AZ2_FN(16, 512, 4, true), AZ2_FN(16, 512, 5, true)};
+#undef AZ2_FN
     for (const void *fn : pair_kernels)
         if (e == cudaSuccess) e = raise_smem_limit(fn, smem);
     return e;
@@ -2239,15 +2276,19 @@ void launch_transport_azimuthal(const Launch &L, double dt, int block, double *c
     if (pair) {
         const int per = azimuthal_pair_cells_per_thread(L.g.nz);
         const int threads = ((L.g.nz + per - 1) / per + 31) / 32 * 32;
-#define AZ2_LAUNCH1(P, T, Q, WS)                                                                \
-    k_transport_azimuthal_f2<P, T, Q, WS><<<L.g.nr, threads, dyn, L.stream>>>(                   \
+        const bool exact = L.g.nz == per * threads;
+#define AZ2_LAUNCH1(P, T, Q, WS, X)                                                             \
+    k_transport_azimuthal_f2<P, T, Q, WS, X><<<L.g.nr, threads, dyn, L.stream>>>(                \
         L.g, L.t, dt, L.ph.limiter_mc, L.ph.fast_transport, vaz, mom[0], mom[1], mom[2], mom[3], \
         E, S, ring_ws)
+#define AZ2_LAUNCH2(P, T, Q)                                                                    \
+    if (exact) AZ2_LAUNCH1(P, T, Q, false, true); else AZ2_LAUNCH1(P, T, Q, false, false)
 #define AZ2_LAUNCH(P, T)                                                                        \
-    if (nq == 5) AZ2_LAUNCH1(P, T, 5, false); else AZ2_LAUNCH1(P, T, 4, false)
+    if (nq == 5) { AZ2_LAUNCH2(P, T, 5); } else { AZ2_LAUNCH2(P, T, 4); }
         if (ring_ws) {
             // rings beyond the shared memory: 16 cells per thread
-            if (nq == 5) AZ2_LAUNCH1(16, 512, 5, true); else AZ2_LAUNCH1(16, 512, 4, true);
+            if (nq == 5) AZ2_LAUNCH1(16, 512, 5, true, false);
+            else AZ2_LAUNCH1(16, 512, 4, true, false);
         } else if (per == 4) {
             AZ2_LAUNCH(4, 512);
         } else if (per == 8) {
@@ -2257,6 +2298,7 @@ void launch_transport_azimuthal(const Launch &L, double dt, int block, double *c
         }
 #undef AZ2_LAUNCH
 #undef AZ2_LAUNCH1
+#undef AZ2_LAUNCH2
         return;
     }
     const int per = azimuthal_cells_per_thread(L.g.nz);
@@ -2390,10 +2432,10 @@ void launch_cfl_cells(const Launch &L, const State &s, double *out)
 
 void launch_derived_cfl(const Launch &L, int mode, const State &s, unsigned long long *dt_min)
 {
-    k_derived_cfl<<<L.g.nr, 256, 0, L.stream>>>(L.g, L.t, L.ph, mode, L.ph.art_visc_sn, s.sigma,
-                                                s.energy, s.vr, s.vaz, s.qplus, s.qminus, s.cs,
-                                                s.H, s.P, s.T, s.nu, s.corr_phi, s.corr_r,
-                                                dt_min);
+    auto k = L.pair ? k_derived_cfl<true> : k_derived_cfl<false>;
+    k<<<L.g.nr, 256, 0, L.stream>>>(L.g, L.t, L.ph, mode, L.ph.art_visc_sn, s.sigma, s.energy,
+                                    s.vr, s.vaz, s.qplus, s.qminus, s.cs, s.H, s.P, s.T, s.nu,
+                                    s.corr_phi, s.corr_r, dt_min);
 }
 
 void launch_gas_quantities(const Launch &L, double radius, double omf, const double *S,

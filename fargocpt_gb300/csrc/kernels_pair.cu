@@ -55,7 +55,6 @@ __device__ __forceinline__ f2 sc(f2 x, float s) { return f2{__fmul_rn(x.h, s), _
 __device__ __forceinline__ bool negative(f2 x) { return x.h < 0.f; }
 // x + dx: the FP64 value plus the joined pair increment
 __device__ __forceinline__ double upd(double x, f2 dx) { return x + f2_to_double(dx); }
-__device__ __forceinline__ f2 f2_sqrt(f2 x) { return x * f2_rsqrt(x); }
 
 // x truncated to a float (relative error below 2^-23) for
 // 2^-126 <= |x| < 2^128, on the integer pipe; ok is false elsewhere
