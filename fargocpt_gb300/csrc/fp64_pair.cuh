@@ -1,9 +1,9 @@
-// FP64-accurate arithmetic from pairs of FP32 values, for the FP64 kernels
-// whose cost is all arithmetic (the potential and the disk force): a value is
-// the unevaluated sum hi + lo of two floats with |lo| <= ulp(hi) / 2, about
-// 48 significant bits.  GB300 issues FP32 operations at 64 times its FP64
-// rate, so a pair operation of 5 to 20 FP32 operations is several times
-// cheaper than one FP64 operation.
+// FP64-accurate arithmetic from pairs of FP32 values for the FP64 form's
+// kernels: a value is the unevaluated sum hi + lo of two floats with |lo|
+// at most about ulp(hi) / 2, about 48 significant bits.  GB300 issues FP32
+// operations at about 70 times its FP64 rate (measured: 113 against 1.6
+// results per clock per SM), so a pair operation of 5 to 20 FP32 operations
+// is several times cheaper than one FP64 operation.
 //
 // The building blocks are the error-free transformations TwoSum (Knuth 1969),
 // Fast2Sum (Dekker 1971) and TwoProduct by fused multiply-add, combined as in
@@ -22,13 +22,6 @@ namespace fgpu {
 struct f2 {
     float h, l;
 };
-
-__device__ __forceinline__ f2 f2_of(double x)
-{
-    const float h = __double2float_rn(x);
-    return f2{h, __double2float_rn(x - (double)h)};
-}
-__device__ __forceinline__ double f2_value(f2 a) { return (double)a.h + (double)a.l; }
 
 // a + b exactly as s + e, for |a| >= |b| or a = 0
 __device__ __forceinline__ f2 fast_two_sum(float a, float b)

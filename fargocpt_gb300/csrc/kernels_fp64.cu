@@ -145,6 +145,24 @@ __device__ __forceinline__ double temperature_floor(double e, double sigma, cons
 // summed as a pair: about 60 FP32 operations per body and cell instead of
 // about 15 FP64 ones, which GB300 issues 64 times slower.
 // ---------------------------------------------------------------------------
+// 1 / sqrt(d) for a normal d > 0 to FP64 accuracy: the float-pair estimate
+// (within a few 2^-46), then one FP64 Newton step, which squares that error
+// and leaves the roundings of the step (about one unit in the last place)
+__device__ __forceinline__ double rsqrt_fp64(double d)
+{
+    const double r = f2_to_double(f2_rsqrt(f2_split(d)));
+    const double e = fma(-d, r * r, 1.0);
+    return fma(0.5 * r, e, r);
+}
+
+// Klahr's smoothing applies inside r_sm: a float screen (the pair's high part
+// against r_sm with a 2^-20 margin) passes the cells certainly outside it;
+// the others compare in FP64
+__device__ __forceinline__ bool maybe_inside(f2 dsm, float rsm_f)
+{
+    return dsm.h < __fmul_rn(rsm_f, 1.0f + 0x1p-20f);
+}
+
 __global__ void k_potential(Geo g, Tables t, Phys ph, Bodies b, const double *__restrict__ H,
                             double *__restrict__ pot)
 {
@@ -153,6 +171,7 @@ __global__ void k_potential(Geo g, Tables t, Phys ph, Bodies b, const double *__
     const int i = blockIdx.y;
     if (j >= nz) return;
     const double smooth = ph.eps_smooth * H[CELL(i, j)];
+    const double s2d = smooth * smooth;
     const double x = t.Rmed[i] * t.cosj[j];
     const double y = t.Rmed[i] * t.sinj[j];
     double acc = 0.0;
@@ -160,8 +179,8 @@ __global__ void k_potential(Geo g, Tables t, Phys ph, Bodies b, const double *__
         // the central object in FP64, the reference's expressions
         const double dx = x - b.x[0];
         const double dy = y - b.y[0];
-        const double d2 = (dx * dx + dy * dy) + smooth * smooth;
-        const double inv_d = rsqrt(d2);
+        const double d2 = (dx * dx + dy * dy) + s2d;
+        const double inv_d = rsqrt_fp64(d2);
         double fk = 1.0;
         const double r_sm = b.rsm[0];
         if (r_sm > 0.0) {
@@ -176,7 +195,7 @@ __global__ void k_potential(Geo g, Tables t, Phys ph, Bodies b, const double *__
     const f2 rm{t.RmedHi[i], t.RmedLo[i]};
     const f2 xc = f2_mul(rm, f2{t.cosHi[j], t.cosLo[j]});
     const f2 yc = f2_mul(rm, f2{t.sinHi[j], t.sinLo[j]});
-    const f2 s2 = f2_of(smooth * smooth);
+    const f2 s2 = f2_split(s2d);
     float ah = 0.f, al = 0.f;
     for (int k = 1; k < b.n; ++k) {
         const f2 dx = f2_sub(xc, f2{b.xh[k], b.xl[k]});
@@ -187,16 +206,19 @@ __global__ void k_potential(Geo g, Tables t, Phys ph, Bodies b, const double *__
         const double r_sm = b.rsm[k];
         if (r_sm > 0.0) {
             // Klahr's cubic inside r_sm (Pframeforce.cpp:57-66): rare, in FP64
-            const double d_sm = f2_value(f2_mul(d2, inv_d));
-            if (d_sm < r_sm) {
-                const double q = d_sm / r_sm;
-                const double fk = q * q * q * q - 2.0 * (q * q * q) + 2.0 * q;
-                term = f2_of(f2_value(term) * fk);
+            const f2 dsm = f2_mul(d2, inv_d);
+            if (maybe_inside(dsm, f2_split(r_sm).h)) {
+                const double d_sm = f2_to_double(dsm);
+                if (d_sm < r_sm) {
+                    const double q = d_sm / r_sm;
+                    const double fk = q * q * q * q - 2.0 * (q * q * q) + 2.0 * q;
+                    term = f2_split(f2_to_double(term) * fk);
+                }
             }
         }
         f2_accumulate(ah, al, term);
     }
-    acc += (double)ah + (double)al;
+    acc += f2_to_double(f2{ah, al});
     pot[CELL(i, j)] = acc + (-b.ix * x - b.iy * y);
 }
 
@@ -1998,12 +2020,17 @@ __global__ void k_disk_force_bodies(Geo g, Tables t, Phys ph, ForceBodies fb,
     float axh[kForceBodies], axl[kForceBodies], ayh[kForceBodies], ayl[kForceBodies];
 #pragma unroll
     for (int b = 0; b < kForceBodies; ++b) axh[b] = axl[b] = ayh[b] = ayl[b] = 0.f;
+    const f2 eps = f2_split(ph.eps_smooth);
+    float rsm_f[kForceBodies];
+#pragma unroll
+    for (int b = 0; b < kForceBodies; ++b) rsm_f[b] = b < fb.n ? f2_split(fb.rsm[b]).h : 0.f;
     for (int j = threadIdx.x; j < nz; j += blockDim.x) {
-        const double smooth = ph.eps_smooth * H[row + j];
-        const f2 s2 = f2_of(smooth * smooth);
+        const f2 smooth = f2_smul(eps, f2_split(H[row + j]));
+        const f2 s2 = f2_smul(smooth, smooth);
         const f2 xc = f2_mul(rm, f2{t.cosHi[j], t.cosLo[j]});
         const f2 yc = f2_mul(rm, f2{t.sinHi[j], t.sinLo[j]});
-        const f2 dsig = f2_of(S[row + j] - sigma1d);
+        // sigma less the ring mean: the FP64 difference (they agree closely)
+        const f2 dsig = f2_split(S[row + j] - sigma1d);
 #pragma unroll
         for (int b = 0; b < kForceBodies; ++b) {
             if (b < fb.n) {
@@ -2014,10 +2041,14 @@ __global__ void k_disk_force_bodies(Geo g, Tables t, Phys ph, ForceBodies fb,
                 f2 w = f2_mul(dsig, f2_mul(f2_mul(rinv, rinv), rinv));
                 if (fb.rsm[b] > 0.0) {
                     // Klahr's factor inside r_sm (Force.cpp:88-100): rare, in FP64
-                    const double dsm = f2_value(f2_mul(dsm2, rinv));
-                    if (dsm < fb.rsm[b]) {
-                        const double q = dsm / fb.rsm[b];
-                        w = f2_of(f2_value(w) * -(3.0 * (q * q * q * q) - 4.0 * (q * q * q)));
+                    const f2 dsm_p = f2_mul(dsm2, rinv);
+                    if (maybe_inside(dsm_p, rsm_f[b])) {
+                        const double dsm = f2_to_double(dsm_p);
+                        if (dsm < fb.rsm[b]) {
+                            const double q = dsm / fb.rsm[b];
+                            w = f2_split(f2_to_double(w) *
+                                         -(3.0 * (q * q * q * q) - 4.0 * (q * q * q)));
+                        }
                     }
                 }
                 f2_accumulate(axh[b], axl[b], f2_mul(w, dx));
