@@ -1787,6 +1787,7 @@ __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const 
 {
     __shared__ double red[33];
     __shared__ float redf[33];
+    extern __shared__ float d32s[];  // the ring's FP32 cell steps (nz floats)
     const int nz = g.nz, nr = g.nr;
     const int i = blockIdx.x;
     float local32 = 3.0e38f;
@@ -1877,27 +1878,22 @@ __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const 
                                          ph.adiabatic ? E[c] : 1.0,
                                          ph.stabilize == 2 ? corr_phi[c] : 0.0,
                                          ph.stabilize == 2 ? corr_r[c] : 0.0);
+            d32s[j] = d32;
             local32 = fminf(local32, d32);
         }
     }
     if (cfl_ring) {
         // the FP64 dt of the cells the FP32 screen puts within 2^-15 of the
         // ring's FP32 minimum; that set holds the FP64 minimum, since the
-        // screen's error is below 2^-19
+        // screen's error is below 2^-19 (each thread reads back the screen
+        // values it wrote, and c_s, nu as it wrote them)
         const float ringmin = block_min_f(local32, redf);
         const float thr = ringmin * (1.0f + 0x1p-15f);
         for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+            if (!(d32s[j] <= thr)) continue;
             const size_t c = row + j;
             const double c_s = ((mode & 1) && !ph.adiabatic) ? t.CsIso[i] : cs[c];
             const double n = nu[c];
-            const float d32 = cfl_cell32(t32, ph, sn, c_s, n, vr[c], vr[c + nz], vaz[c],
-                                         vaz[row + (j == nz - 1 ? 0 : j + 1)], vm0,
-                                         ph.adiabatic ? qplus[c] : 0.0,
-                                         ph.adiabatic ? qminus[c] : 0.0,
-                                         ph.adiabatic ? E[c] : 1.0,
-                                         ph.stabilize == 2 ? corr_phi[c] : 0.0,
-                                         ph.stabilize == 2 ? corr_r[c] : 0.0);
-            if (!(d32 <= thr)) continue;
             double inv[6];
             const double dt_cell = cfl_cell64(g, t, ph, sn, i, j, c_s, n, vr, vaz, vm0, qplus,
                                               qminus, E, corr_phi, corr_r, inv);
@@ -2464,9 +2460,9 @@ void launch_cfl_cells(const Launch &L, const State &s, double *out)
 void launch_derived_cfl(const Launch &L, int mode, const State &s, unsigned long long *dt_min)
 {
     auto k = L.pair ? k_derived_cfl<true> : k_derived_cfl<false>;
-    k<<<L.g.nr, 256, 0, L.stream>>>(L.g, L.t, L.ph, mode, L.ph.art_visc_sn, s.sigma, s.energy,
-                                    s.vr, s.vaz, s.qplus, s.qminus, s.cs, s.H, s.P, s.T, s.nu,
-                                    s.corr_phi, s.corr_r, dt_min);
+    k<<<L.g.nr, 256, (size_t)L.g.nz * sizeof(float), L.stream>>>(
+        L.g, L.t, L.ph, mode, L.ph.art_visc_sn, s.sigma, s.energy, s.vr, s.vaz, s.qplus,
+        s.qminus, s.cs, s.H, s.P, s.T, s.nu, s.corr_phi, s.corr_r, dt_min);
 }
 
 void launch_gas_quantities(const Launch &L, double radius, double omf, const double *S,
