@@ -51,9 +51,10 @@ STEP_BYTES_PER_CELL = {"adiabatic": 64, "isothermal": 48}   # one read + write o
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant
 # kernels from one-kernel ncu captures (profiles/ names the capture of each)
 NCU_DRAM_BYTES = {
-    # 2048 x 6144 three-planet adiabatic disk (profiles/traffic_c5_transports.md)
-    ("c5", "fp64", "transport_azimuthal"): 719267072 + 986360320,
-    ("c5", "fp64", "transport_radial"): 403436800 + 552501504,
+    # 2048 x 6144 three-planet adiabatic disk (profiles/traffic_c5_transports.md;
+    # the FP64 form's float-pair kernels)
+    ("c5", "fp64", "transport_azimuthal"): 707886592 + 645737472,
+    ("c5", "fp64", "transport_radial"): 412882432 + 549269504,
     ("c5", "fp32", "transport_azimuthal"): 403144448 + 288285952,
     ("c5", "fp32", "transport_radial"): 260210688 + 302722816,
     # 512 x 1536 adiabatic disk (--set full captures)
@@ -491,9 +492,12 @@ def main():
     value = world * cells * args.steps / (vals[0] * 1e-3)
     e2e = world * cells * args.steps / vals[1]
     rl, rls = roofline(r64, args.steps, 1.0, "fp64", args.config)
-    # the FP64 kernels are bound by the FP64 pipe (72-80% busy, DRAM at 1%
-    # of peak in the same captures)
-    rl["fp64_pipe_busy_pct_ncu"] = {"transport_azimuthal": 72.5, "transport_radial": 79.7}
+    # what bounds the float-pair transports (ncu --set full on 256 rings of
+    # 6144 cells, profiles/transport_kernels_c5_fp64_pair.md): issue and
+    # latency, not the FP64 pipe or DRAM
+    rl["ncu_pipes_pct"] = {
+        "transport_azimuthal": {"issue_active": 41.1, "fp64_pipe": 38.2, "fma_pipe": 18.9},
+        "transport_radial": {"issue_active": 51.3, "fp64_pipe": 33.8, "fma_pipe": 26.1}}
     fp32 = None
     if r32 is not None:
         value32 = world * cells * args.steps / (vals[2] * 1e-3)

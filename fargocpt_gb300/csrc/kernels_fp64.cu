@@ -163,6 +163,13 @@ __device__ __forceinline__ bool maybe_inside(f2 dsm, float rsm_f)
     return dsm.h < __fmul_rn(rsm_f, 1.0f + 0x1p-20f);
 }
 
+// PAIR and a central object at the origin without Klahr smoothing (the
+// heliocentric frame's usual case, a uniform branch): its distance^2 is
+// Rmed^2 + smooth^2, since cos^2 + sin^2 = 1 within the tables' rounding, so
+// the FP64 work per cell is one product, one fused multiply-add, the
+// Newton-finished 1/sqrt and the final sums; the indirect term, linear in
+// the cell position, joins the planets' pair sum.
+template <bool PAIR>
 __global__ void k_potential(Geo g, Tables t, Phys ph, Bodies b, const double *__restrict__ H,
                             double *__restrict__ pot)
 {
@@ -170,6 +177,40 @@ __global__ void k_potential(Geo g, Tables t, Phys ph, Bodies b, const double *__
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.y;
     if (j >= nz) return;
+    if (PAIR && b.n > 0 && b.x[0] == 0.0 && b.y[0] == 0.0 && !(b.rsm[0] > 0.0)) {
+        const double smooth = ph.eps_smooth * H[CELL(i, j)];
+        const double rm = t.Rmed[i];
+        const double acc = -ph.G * b.m[0] * rsqrt_fp64(fma(smooth, smooth, rm * rm));
+        const f2 rmp{t.RmedHi[i], t.RmedLo[i]};
+        const f2 xc = f2_smul(rmp, f2{t.cosHi[j], t.cosLo[j]});
+        const f2 yc = f2_smul(rmp, f2{t.sinHi[j], t.sinLo[j]});
+        const f2 s2 = f2_split(smooth * smooth);
+        float ah = 0.f, al = 0.f;
+        for (int k = 1; k < b.n; ++k) {
+            const f2 dx = f2_ssub(xc, f2{b.xh[k], b.xl[k]});
+            const f2 dy = f2_ssub(yc, f2{b.yh[k], b.yl[k]});
+            const f2 d2 = f2_sadd(f2_sadd(f2_smul(dx, dx), f2_smul(dy, dy)), s2);
+            const f2 inv_d = f2_rsqrt(d2);
+            f2 term = f2_smul(inv_d, f2{b.gmh[k], b.gml[k]});
+            const double r_sm = b.rsm[k];
+            if (r_sm > 0.0) {
+                // Klahr's cubic inside r_sm (Pframeforce.cpp:57-66): rare, in FP64
+                const f2 dsm = f2_smul(d2, inv_d);
+                if (maybe_inside(dsm, f2_split(r_sm).h)) {
+                    const double d_sm = f2_to_double(dsm);
+                    if (d_sm < r_sm) {
+                        const double q = d_sm / r_sm;
+                        const double fk = q * q * q * q - 2.0 * (q * q * q) + 2.0 * q;
+                        term = f2_split(f2_to_double(term) * fk);
+                    }
+                }
+            }
+            f2_accumulate(ah, al, term);
+        }
+        const f2 ind = f2_neg(f2_sadd(f2_smul(f2_split(b.ix), xc), f2_smul(f2_split(b.iy), yc)));
+        pot[CELL(i, j)] = acc + f2_to_double(f2_sadd(f2{ah, al}, ind));
+        return;
+    }
     const double smooth = ph.eps_smooth * H[CELL(i, j)];
     const double s2d = smooth * smooth;
     const double x = t.Rmed[i] * t.cosj[j];
@@ -1771,6 +1812,101 @@ __device__ __forceinline__ double cfl_cell64(const Geo &g, const Tables &t, cons
     return dt_cell;
 }
 
+// The time step of cell (i, j) in float pairs: cfl_cell64's six inverse
+// times and CFL / sqrt of their squares (LeapFrog's 0.6 on the last three),
+// within a few 2^-46 of the FP64 value, far inside the CFL step's bar.  The
+// differences of stored velocities and Q+ - Q- are FP64 subtractions (they
+// cancel); StabilizeViscosity 2 is served by the FP64 path.
+__device__ __forceinline__ f2 cfl_cell_f2(const Geo &g, const Tables &t, const Phys &ph, int sn,
+                                          int i, int j, f2 c_s, f2 n,
+                                          const double *__restrict__ vr,
+                                          const double *__restrict__ vaz, double vm0,
+                                          const double *__restrict__ qplus,
+                                          const double *__restrict__ qminus,
+                                          const double *__restrict__ E)
+{
+    const int nz = g.nz;
+    const size_t row = (size_t)i * nz;
+    const size_t c = row + j;
+    auto tp = [&](const double *tab) {
+        const float2 v = t.ptab[(tab - t.tbase) + i];
+        return f2{v.x, v.y};
+    };
+    auto fmax2 = [](f2 a, f2 b) {  // a, b >= 0
+        return (a.h > b.h || (a.h == b.h && a.l > b.l)) ? a : b;
+    };
+    const double va = vaz[c], vr0 = vr[c], vr1 = vr[c + nz];
+    const double va1 = vaz[row + (j == nz - 1 ? 0 : j + 1)];
+    const f2 inv_drsup = tp(t.InvDiffRsup), inv_dxt = tp(t.InvDxTheta);
+    const f2 i1 = f2_smul(c_s, tp(t.InvCell));
+    const f2 i2 = f2_smul(f2_split(vr0), inv_drsup);
+    const f2 i3 = f2_smul(f2_split(ph.fast_transport ? va - vm0 : va), inv_dxt);
+    f2 i4;
+    if (sn) {
+        const double dvR = vr1 - vr0, dvA = va1 - va;
+        const f2 a = f2_smul(f2_split(positive(dvR) ? 0.0 : -dvR), inv_drsup);
+        const f2 b = f2_smul(f2_split(positive(dvA) ? 0.0 : -dvA), inv_dxt);
+        i4 = f2_smul(f2_split(ph.four_C2), fmax2(a, b));
+    } else {
+        const f2 eps_rr = f2_smul(f2_split(vr1 - vr0), inv_drsup);
+        const f2 h = f2_split(0.5 * (vr1 + vr0));
+        const f2 eps_pp = f2_smul(tp(t.InvRmed),
+                                  f2_sadd(f2_smul(f2_split(va1 - va), f2_split(g.invdphi)), h));
+        const f2 d = f2_sadd(eps_rr, eps_pp);
+        i4 = f2_smul(f2_split(ph.four_C2), d.h < 0.f ? f2_neg(d) : f2{0.f, 0.f});
+    }
+    f2 i5 = f2_smul(n, tp(t.InvCell2));
+    i5 = f2{__fmul_rn(4.0f, i5.h), __fmul_rn(4.0f, i5.l)};
+    f2 i6{0.f, 0.f};
+    if (ph.adiabatic) {
+        const f2 q = f2_sdiv(f2_split(qplus[c] - qminus[c]), f2_split(E[c]));
+        i6 = f2_smul(f2_split(ph.inv_hc_limit), q.h < 0.f ? f2_neg(q) : q);
+    }
+    if (ph.leapfrog) {
+        const f2 k = f2_split(0.6);
+        i4 = f2_smul(i4, k);
+        i5 = f2_smul(i5, k);
+        i6 = f2_smul(i6, k);
+    }
+    f2 sum = f2_smul(i1, i1);
+    sum = f2_sadd(sum, f2_smul(i2, i2));
+    sum = f2_sadd(sum, f2_smul(i3, i3));
+    sum = f2_sadd(sum, f2_smul(i4, i4));
+    sum = f2_sadd(sum, f2_smul(i5, i5));
+    sum = f2_sadd(sum, f2_smul(i6, i6));
+    return f2_sdiv(f2_split(ph.cfl), f2_sqrt(sum));
+}
+
+// the smaller of two positive pairs
+__device__ __forceinline__ f2 pair_min(f2 a, f2 b)
+{
+    return (b.h < a.h || (b.h == a.h && b.l < a.l)) ? b : a;
+}
+__device__ f2 block_min_f2(f2 v, float *red)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+    for (int o = 16; o > 0; o >>= 1)
+        v = pair_min(v, f2{__shfl_down_sync(0xffffffffu, v.h, o), __shfl_down_sync(0xffffffffu, v.l, o)});
+    __syncthreads();
+    if (lane == 0) {
+        red[2 * wid] = v.h;
+        red[2 * wid + 1] = v.l;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        f2 x = lane < nw ? f2{red[2 * lane], red[2 * lane + 1]} : f2{3.0e38f, 0.f};
+        for (int o = 16; o > 0; o >>= 1)
+            x = pair_min(x, f2{__shfl_down_sync(0xffffffffu, x.h, o), __shfl_down_sync(0xffffffffu, x.l, o)});
+        if (lane == 0) {
+            red[64] = x.h;
+            red[65] = x.l;
+        }
+    }
+    __syncthreads();
+    return f2{red[64], red[65]};
+}
+
 // PAIR: the ideal-EOS derived quantities (T, c_s, H, nu) in float-pair
 // arithmetic (P = (gamma - 1) e stays one FP64 product: the source terms
 // difference it)
@@ -1786,8 +1922,13 @@ __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const 
                               unsigned long long *__restrict__ dt_min)
 {
     __shared__ double red[33];
-    __shared__ float redf[33];
+    __shared__ float redf[66];
     extern __shared__ float d32s[];  // the ring's FP32 cell steps (nz floats)
+    // PAIR: every cell's step in float pairs, the ring's smallest kept as a
+    // pair (no FP32 screen: in a nearly axisymmetric ring most cells fall
+    // inside any screen's margin, and each would then take FP64)
+    const bool pair_cfl = PAIR && ph.stabilize != 2;
+    f2 local2{3.0e38f, 0.f};
     const int nz = g.nz, nr = g.nr;
     const int i = blockIdx.x;
     float local32 = 3.0e38f;
@@ -1829,6 +1970,8 @@ __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const 
     for (int j = threadIdx.x; j < nz; j += blockDim.x) {
         const size_t c = row + j;
         double c_s, n;
+        f2 cp2{0.f, 0.f};  // c_s as a pair where the pair path formed it
+        bool have_cp2 = false;
         if (mode & 1) {
             const double sg = S[c];
             if (ph.adiabatic && PAIR) {
@@ -1838,6 +1981,8 @@ __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const 
                 const f2 cp = f2_sqrt(f2_smul(f2_split(ph.g_gm1), es));
                 const float2 hf = t.ptab[(t.HFacAdi - t.tbase) + i];
                 const f2 hp = f2_smul(cp, f2{hf.x, hf.y});
+                cp2 = cp;
+                have_cp2 = true;
                 c_s = f2_to_double(cp);
                 cs[c] = c_s;
                 H[c] = f2_to_double(hp);
@@ -1870,7 +2015,11 @@ __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const 
             c_s = cs[c];
             n = nu[c];
         }
-        if (cfl_ring) {
+        if (cfl_ring && pair_cfl) {
+            const f2 cpair = have_cp2 ? cp2 : f2_split(c_s);
+            local2 = pair_min(local2, cfl_cell_f2(g, t, ph, sn, i, j, cpair, f2_split(n), vr, vaz,
+                                                  vm0, qplus, qminus, E));
+        } else if (cfl_ring) {
             const float d32 = cfl_cell32(t32, ph, sn, c_s, n, vr[c], vr[c + nz], vaz[c],
                                          vaz[row + (j == nz - 1 ? 0 : j + 1)], vm0,
                                          ph.adiabatic ? qplus[c] : 0.0,
@@ -1882,7 +2031,11 @@ __global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const 
             local32 = fminf(local32, d32);
         }
     }
-    if (cfl_ring) {
+    if (cfl_ring && pair_cfl) {
+        const f2 m = block_min_f2(local2, redf);
+        const double d = f2_to_double(m);
+        if (dbits(d) < dbits(local)) local = d;
+    } else if (cfl_ring) {
         // the FP64 dt of the cells the FP32 screen puts within 2^-15 of the
         // ring's FP32 minimum; that set holds the FP64 minimum, since the
         // screen's error is below 2^-19 (each thread reads back the screen
@@ -2142,7 +2295,8 @@ static inline dim3 grid2d(int nz, int rows, int bx) { return dim3((nz + bx - 1) 
 
 void launch_potential(const Launch &L, const Bodies &b, const double *H, double *pot)
 {
-    k_potential<<<grid2d(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(L.g, L.t, L.ph, b, H, pot);
+    auto k = L.pair ? k_potential<true> : k_potential<false>;
+    k<<<grid2d(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(L.g, L.t, L.ph, b, H, pot);
 }
 
 void launch_source(const Launch &L, double dt, double omf, const double *S, const double *P,
@@ -2278,20 +2432,23 @@ cudaError_t prepare_azimuthal(size_t smem)
     if (e == cudaSuccess) e = raise_smem_limit((const void *)k_transport_azimuthal<16>, smem);
 #define AZ2_FN(P, T, Q, X) (const void *)k_transport_azimuthal_f2<P, T, Q, false, X>
     const void *pair_kernels[12] = {
-        AZ2_FN(4, 512, 4, false), AZ2_FN(4, 512, 5, false), AZ2_FN(8, 768, 4, false),
-        AZ2_FN(8, 768, 5, false), AZ2_FN(16, 512, 4, false), AZ2_FN(16, 512, 5, false),
-        AZ2_FN(4, 512, 4, true), AZ2_FN(4, 512, 5, true), AZ2_FN(8, 768, 4, true),
-        AZ2_FN(8, 768, 5, true), AZ2_FN(16, 512, 4, true), AZ2_FN(16, 512, 5, true)};
+        AZ2_FN(2, 1024, 4, false), AZ2_FN(2, 1024, 5, false), AZ2_FN(2, 1024, 4, true),
+        AZ2_FN(2, 1024, 5, true), AZ2_FN(6, 1024, 4, false), AZ2_FN(6, 1024, 5, false),
+        AZ2_FN(6, 1024, 4, true), AZ2_FN(6, 1024, 5, true), AZ2_FN(16, 512, 4, false),
+        AZ2_FN(16, 512, 5, false), AZ2_FN(16, 512, 4, true), AZ2_FN(16, 512, 5, true)};
 #undef AZ2_FN
     for (const void *fn : pair_kernels)
         if (e == cudaSuccess) e = raise_smem_limit(fn, smem);
     return e;
 }
 
-// Cells per thread of the pair kernel: 4 up to 2048 cells (<= 512 threads),
-// 8 up to 6144 (<= 768), 16 beyond (<= 512 threads for 8192 cells); the
-// thread count is the ring length over that, in whole warps.
-int azimuthal_pair_cells_per_thread(int nz) { return nz <= 2048 ? 4 : (nz <= 6144 ? 8 : 16); }
+// Cells per thread of the pair kernel: 2 up to 1024 cells (<= 512 threads),
+// 6 up to 6144 (<= 1024), 16 beyond (<= 512 threads for 8192 cells); the
+// thread count is the ring length over that, in whole warps.  Measured
+// (ms per azimuthal pass): 384-cell rings 0.021 with 2 cells per thread
+// (4: 0.029, 6: 0.039); 1536: 0.127 with 6 (4: 0.132, 8: 0.135, 2: 0.169);
+// 3072: 0.378 with 6 (8: 0.412); 6144: 1.87 with 6 (8: 2.01, 12: 2.55).
+int azimuthal_pair_cells_per_thread(int nz) { return nz <= 1024 ? 2 : (nz <= 6144 ? 6 : 16); }
 
 void launch_transport_azimuthal(const Launch &L, double dt, int block, double *const mom[4],
                                 double *E, double *S, const double *vaz, double *ring_ws,
@@ -2316,10 +2473,10 @@ void launch_transport_azimuthal(const Launch &L, double dt, int block, double *c
             // rings beyond the shared memory: 16 cells per thread
             if (nq == 5) AZ2_LAUNCH1(16, 512, 5, true, false);
             else AZ2_LAUNCH1(16, 512, 4, true, false);
-        } else if (per == 4) {
-            AZ2_LAUNCH(4, 512);
-        } else if (per == 8) {
-            AZ2_LAUNCH(8, 768);
+        } else if (per == 2) {
+            AZ2_LAUNCH(2, 1024);
+        } else if (per == 6) {
+            AZ2_LAUNCH(6, 1024);
         } else {
             AZ2_LAUNCH(16, 512);
         }

@@ -117,6 +117,11 @@ CONFIGS = {
     # large adiabatic 2048 x 6144 disk with three planets
     "c5": dict(nrad=2048, naz=6144, rmin=0.3, rmax=5.0, adiabatic=True, slope=1.0,
                flaring=0.25, planets=[(1e-3, 1.0, 0.0), (3e-4, 1.6, 2.1), (1e-4, 2.5, 4.2)]),
+    # the large disk's set-up with a quarter of its rings (512 x 6144): the
+    # same 6144-cell rings for profiler captures that stay small (25 MB per
+    # FP64 field, about 0.8 GB on the device)
+    "c5s": dict(nrad=512, naz=6144, rmin=0.3, rmax=5.0, adiabatic=True, slope=1.0,
+                flaring=0.25, planets=[(1e-3, 1.0, 0.0), (3e-4, 1.6, 2.1), (1e-4, 2.5, 4.2)]),
 }
 
 
