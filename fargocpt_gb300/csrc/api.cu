@@ -1224,11 +1224,15 @@ extern "C" int fgpu_set_bodies(fgpu_engine *eng, int n, const fgpu_body *bodies,
         h = (float)v;
         l = (float)(v - (double)h);
     };
+    b.klahr = 0;
     for (int k = 0; k < n; ++k) {
         split(b.x[k], b.xh[k], b.xl[k]);
         split(b.y[k], b.yh[k], b.yl[k]);
         split(-eng->p.G * b.m[k], b.gmh[k], b.gml[k]);
+        if (b.rsm[k] > 0.0) b.klahr |= 1u << k;
     }
+    b.star_plain = n > 0 && b.x[0] == 0.0 && b.y[0] == 0.0 && !(b.rsm[0] > 0.0);
+    b.gm0 = n > 0 ? -eng->p.G * b.m[0] : 0.0;
     if (eng->e32) {
         if (omega_frame != 0.0 && eng->batch_owned) {
             eng->err = "the batched form runs in the fixed (non-rotating) frame";

@@ -87,6 +87,12 @@ struct Bodies {
     float gmh[kMaxBodies], gml[kMaxBodies];
     double ix, iy;        // indirect term
     double omega_frame;
+    // decided on the host, so that no kernel compares doubles per cell:
+    // bit k set when body k has Klahr smoothing (rsm[k] > 0); the central
+    // object at the origin without it; -G m of the central object
+    unsigned klahr;
+    int star_plain;
+    double gm0;
 };
 
 // Ghost-ring hooks of one step (FGPU_BC_* per field and side).  val_in /

@@ -177,10 +177,10 @@ __global__ void k_potential(Geo g, Tables t, Phys ph, Bodies b, const double *__
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.y;
     if (j >= nz) return;
-    if (PAIR && b.n > 0 && b.x[0] == 0.0 && b.y[0] == 0.0 && !(b.rsm[0] > 0.0)) {
+    if (PAIR && b.star_plain) {
         const double smooth = ph.eps_smooth * H[CELL(i, j)];
         const double rm = t.Rmed[i];
-        const double acc = -ph.G * b.m[0] * rsqrt_fp64(fma(smooth, smooth, rm * rm));
+        const double acc = b.gm0 * rsqrt_fp64(fma(smooth, smooth, rm * rm));
         const f2 rmp{t.RmedHi[i], t.RmedLo[i]};
         const f2 xc = f2_smul(rmp, f2{t.cosHi[j], t.cosLo[j]});
         const f2 yc = f2_smul(rmp, f2{t.sinHi[j], t.sinLo[j]});
@@ -192,9 +192,9 @@ __global__ void k_potential(Geo g, Tables t, Phys ph, Bodies b, const double *__
             const f2 d2 = f2_sadd(f2_sadd(f2_smul(dx, dx), f2_smul(dy, dy)), s2);
             const f2 inv_d = f2_rsqrt(d2);
             f2 term = f2_smul(inv_d, f2{b.gmh[k], b.gml[k]});
-            const double r_sm = b.rsm[k];
-            if (r_sm > 0.0) {
+            if ((b.klahr >> k) & 1u) {
                 // Klahr's cubic inside r_sm (Pframeforce.cpp:57-66): rare, in FP64
+                const double r_sm = b.rsm[k];
                 const f2 dsm = f2_smul(d2, inv_d);
                 if (maybe_inside(dsm, f2_split(r_sm).h)) {
                     const double d_sm = f2_to_double(dsm);
@@ -925,6 +925,9 @@ __device__ __forceinline__ f2 lim_f2(f2 a, f2 b, int mc)
 // their FP64 values.  The upwind choice and the interpolation distance come
 // from the FP64 velocity.
 // ---------------------------------------------------------------------------
+// The specific quantities of ring i (slots 0 .. NQ - 1: the two radial
+// momenta's velocities, the two angular momenta's, energy / sigma) and sigma
+// (slot NQ); sig = sigma as a double
 template <int NQ>
 __device__ __forceinline__ void rad_ring_f2(int i, int j, int nz, const double *S, const double *vr,
                                             const double *vaz, const double *E, double omf,
@@ -933,37 +936,43 @@ __device__ __forceinline__ void rad_ring_f2(int i, int j, int nz, const double *
     sig = S[CELL(i, j)];
     const f2 sg = f2_split(sig);
     const f2 r{t.RmedHi[i], t.RmedLo[i]};
-    w[0] = f2_split(vr[CELL(i + 1, j)]);
-    w[1] = f2_split(vr[CELL(i, j)]);
-    f2 a = f2_split(vaz[CELL(i, jnext(j, nz))]), b = f2_split(vaz[CELL(i, j)]);
-    if (omf != 0.0) {
-        const f2 ro = f2_split(t.Rmed[i] * omf);
-        a = f2_sadd(a, ro);
-        b = f2_sadd(b, ro);
+#pragma unroll
+    for (int s = 0; s < NQ; ++s) {
+        const int q = s;
+        if (q == 0) w[s] = f2_split(vr[CELL(i + 1, j)]);
+        if (q == 1) w[s] = f2_split(vr[CELL(i, j)]);
+        if (q == 2 || q == 3) {
+            f2 v = f2_split(vaz[CELL(i, q == 2 ? jnext(j, nz) : j)]);
+            if (omf != 0.0) v = f2_sadd(v, f2_split(t.Rmed[i] * omf));
+            w[s] = f2_smul(v, r);
+        }
+        if (q == 4) w[s] = f2_sdiv(f2_split(E[CELL(i, j)]), sg);
     }
-    w[2] = f2_smul(a, r);
-    w[3] = f2_smul(b, r);
-    if (NQ == 5) w[4] = f2_sdiv(f2_split(E[CELL(i, j)]), sg);
     w[NQ] = sg;
 }
 
 template <int NQ>
-__global__ void k_transport_radial_f2(Geo g, Tables t, double dt, double omf, int mc, int chunk,
-                                      const double *__restrict__ S, const double *__restrict__ vr,
-                                      const double *__restrict__ vaz, const double *__restrict__ E,
-                                      double *__restrict__ mom0, double *__restrict__ mom1,
-                                      double *__restrict__ mom2, double *__restrict__ mom3,
-                                      double *__restrict__ E_out, double *__restrict__ S_out)
+__device__ __forceinline__ void radial_sweep_f2(const Geo &g, const Tables &t, double dt,
+                                                double omf, int mc, int chunk, int j,
+                                                const double *__restrict__ S,
+                                                const double *__restrict__ vr,
+                                                const double *__restrict__ vaz,
+                                                const double *__restrict__ E,
+                                                double *__restrict__ mom0,
+                                                double *__restrict__ mom1,
+                                                double *__restrict__ mom2,
+                                                double *__restrict__ mom3,
+                                                double *__restrict__ E_out,
+                                                double *__restrict__ S_out)
 {
-    constexpr int NW = NQ + 1;
+    constexpr int NW = NQ + 1, NH = NQ;
     const int nz = g.nz, nr = g.nr;
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= nz) return;
     const int i0 = blockIdx.y * chunk;
     if (i0 >= nr) return;
     const int i1 = min(i0 + chunk, nr);
     const double dtdphi = dt * g.dphi;
     const f2 zero{0.f, 0.f};
+    double *const outq[5] = {mom0, mom1, mom2, mom3, E_out};
 
     // rolling state as in k_transport_radial: rings k-1 (wa, da), k (wb, db,
     // ub: its upward difference) and k+1 (wn); sigma of k-1 / k / k+1
@@ -1008,7 +1017,7 @@ __global__ void k_transport_radial_f2(Geo g, Tables t, double dt, double omf, in
             ub[q] = up;
         }
     }
-    f2 flux_prev[NW], q_prev[4];
+    f2 flux_prev[NW], q_prev[NH];
     double e_prev = 0.0;
     for (int k = i0; k <= i1; ++k) {
         // flux through the interface k (between rings k-1 and k)
@@ -1029,33 +1038,32 @@ __global__ void k_transport_radial_f2(Geo g, Tables t, double dt, double omf, in
             for (int q = 0; q < NW; ++q)
                 star[q] = f2_sfma(up ? wa[q] : wb[q], f, up ? da[q] : db[q]);
             // base sigma* v, the factor every quantity's flux shares
-            const f2 bsv = f2_smul(f2_smul(f2_split(dtdphi * t.Rinf[k]), star[NQ]), f2_split(v));
+            const f2 bsv = f2_smul(f2_smul(f2_split(dtdphi * t.Rinf[k]), star[NH]), f2_split(v));
 #pragma unroll
-            for (int q = 0; q < NQ; ++q) flux[q] = f2_smul(star[q], bsv);
-            flux[NQ] = bsv;
+            for (int q = 0; q < NH; ++q) flux[q] = f2_smul(star[q], bsv);
+            flux[NH] = bsv;
         }
         if (k > i0) {
             // VanLeerRadial update of ring k-1 (:586-591)
             const int i = k - 1;
             const f2 invs{t.InvSurfHi[i], t.InvSurfLo[i]};
             const size_t c = CELL(i, j);
-            f2 dq[NW];
 #pragma unroll
-            for (int q = 0; q < NW; ++q) dq[q] = f2_smul(f2_ssub(flux_prev[q], flux[q]), invs);
-            mom0[c] = f2_to_double(f2_sadd(q_prev[0], dq[0]));
-            mom1[c] = f2_to_double(f2_sadd(q_prev[1], dq[1]));
-            mom2[c] = f2_to_double(f2_sadd(q_prev[2], dq[2]));
-            mom3[c] = f2_to_double(f2_sadd(q_prev[3], dq[3]));
-            if (NQ == 5) E_out[c] = e_prev + f2_to_double(dq[4]);
-            S_out[c] = sa + f2_to_double(dq[NQ]);
+            for (int s = 0; s < NW; ++s) {
+                const f2 dq = f2_smul(f2_ssub(flux_prev[s], flux[s]), invs);
+                if (s < 4 && s < NH) outq[s][c] = f2_to_double(f2_sadd(q_prev[s], dq));
+                else if (s == 4 && NQ == 5) E_out[c] = e_prev + f2_to_double(dq);
+                else S_out[c] = sa + f2_to_double(dq);
+            }
         }
         if (k < i1) {
             // conserved quantities of ring k for its update at interface k+1
 #pragma unroll
             for (int q = 0; q < NW; ++q) flux_prev[q] = flux[q];
-            const f2 sp = wb[NQ];
+            const f2 sp = wb[NH];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) q_prev[q] = f2_smul(sp, wb[q]);
+            for (int s = 0; s < NH; ++s)
+                if (s < 4) q_prev[s] = f2_smul(sp, wb[s]);
             if (NQ == 5) e_prev = E[CELL(k, j)];
             // advance: ring k becomes k-1, ring k+1 becomes k
             const bool more = k + 2 < nr;
@@ -1079,6 +1087,20 @@ __global__ void k_transport_radial_f2(Geo g, Tables t, double dt, double omf, in
             sn = s2;
         }
     }
+}
+
+template <int NQ>
+__global__ void k_transport_radial_f2(Geo g, Tables t, double dt, double omf, int mc, int chunk,
+                                      const double *__restrict__ S, const double *__restrict__ vr,
+                                      const double *__restrict__ vaz, const double *__restrict__ E,
+                                      double *__restrict__ mom0, double *__restrict__ mom1,
+                                      double *__restrict__ mom2, double *__restrict__ mom3,
+                                      double *__restrict__ E_out, double *__restrict__ S_out)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= g.nz) return;
+    radial_sweep_f2<NQ>(g, t, dt, omf, mc, chunk, j, S, vr, vaz, E, mom0, mom1, mom2, mom3,
+                           E_out, S_out);
 }
 
 // ---------------------------------------------------------------------------
@@ -2147,6 +2169,7 @@ __global__ void k_accrete(Geo g, Tables t, Phys ph, AccretionSpec a, double *__r
 // ---------------------------------------------------------------------------
 struct ForceBodies {
     int n;  // bodies in this pass (1 .. kForceBodies)
+    unsigned klahr;  // bit b: body b has Klahr smoothing (rsm > 0)
     double a[kForceBodies], rsm[kForceBodies];
     float xh[kForceBodies], xl[kForceBodies], yh[kForceBodies], yl[kForceBodies];
 };
@@ -2188,7 +2211,7 @@ __global__ void k_disk_force_bodies(Geo g, Tables t, Phys ph, ForceBodies fb,
                 const f2 dsm2 = f2_add(f2_add(f2_mul(dx, dx), f2_mul(dy, dy)), s2);
                 const f2 rinv = f2_rsqrt(dsm2);
                 f2 w = f2_mul(dsig, f2_mul(f2_mul(rinv, rinv), rinv));
-                if (fb.rsm[b] > 0.0) {
+                if ((fb.klahr >> b) & 1u) {
                     // Klahr's factor inside r_sm (Force.cpp:88-100): rare, in FP64
                     const f2 dsm_p = f2_mul(dsm2, rinv);
                     if (maybe_inside(dsm_p, rsm_f[b])) {
@@ -2652,6 +2675,7 @@ void launch_disk_force(const Launch &L, int n, const double *px, const double *p
             fb.yl[b] = (float)(py[b0 + b] - (double)fb.yh[b]);
             fb.a[b] = pa[b0 + b];
             fb.rsm[b] = rsm[b0 + b];
+            if (fb.rsm[b] > 0.0) fb.klahr |= 1u << b;
         }
         const int width = 5 * fb.n;
         k_disk_force_bodies<<<rows, 256, 0, L.stream>>>(L.g, L.t, L.ph, fb, S, H, partial, width);
