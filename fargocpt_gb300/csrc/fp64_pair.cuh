@@ -123,15 +123,25 @@ __device__ __forceinline__ f2 f2_split(double x)
 __device__ __forceinline__ double f_to_d(float f)
 {
     const unsigned b = __float_as_uint(f);
-    const unsigned ef = (b >> 23) & 0xffu, sign = b & 0x80000000u;
-    const bool normal = ef - 1u < 254u;
-    const unsigned w1 = normal ? (sign | (((b & 0x7fffffffu) >> 3) + (896u << 20)))
-                               : (sign | (ef ? 0x7ff80000u : 0u));
+    const unsigned mag = b & 0x7fffffffu, sign = b & 0x80000000u;
+    const bool normal = mag - 0x00800000u < 0x7f000000u;
+    const unsigned w1 = normal ? (sign | ((mag >> 3) + (896u << 20)))
+                               : (sign | (mag < 0x00800000u ? 0u : 0x7ff80000u));
     return __hiloint2double((int)w1, (int)(normal ? b << 29 : 0u));
+}
+// the same for the low part of a pair, which is finite when the high part
+// is (a NaN pair has a NaN high part): zero and subnormals give zero
+__device__ __forceinline__ double f_to_d_lo(float f)
+{
+    const unsigned b = __float_as_uint(f);
+    const unsigned mag = b & 0x7fffffffu;
+    const bool tiny = mag < 0x00800000u;
+    const unsigned w1 = (b & 0x80000000u) | (tiny ? 0u : (mag >> 3) + (896u << 20));
+    return __hiloint2double((int)w1, (int)(tiny ? 0u : b << 29));
 }
 
 // h + l as a double (one FP64 addition of the two exact conversions)
-__device__ __forceinline__ double f2_to_double(f2 a) { return f_to_d(a.h) + f_to_d(a.l); }
+__device__ __forceinline__ double f2_to_double(f2 a) { return f_to_d(a.h) + f_to_d_lo(a.l); }
 
 // ---------------------------------------------------------------------------
 // Cheaper pair operations for the transports, whose error bars are relative

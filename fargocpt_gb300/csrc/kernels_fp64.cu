@@ -899,7 +899,10 @@ __device__ __forceinline__ bool f2_abs_less(f2 a, f2 b)
     if (ah != bh) return ah < bh;
     return (a.h < 0.f ? -a.l : a.l) < (b.h < 0.f ? -b.l : b.l);
 }
-// flux_limiter_unscaled in pairs
+// flux_limiter_unscaled in pairs, of two normalised differences (a
+// difference whose low part were not folded in would carry most of the
+// product a b in its low part, and the quotient's one-step correction would
+// then keep only float precision of it)
 __device__ __forceinline__ f2 lim_f2(f2 a, f2 b, int mc)
 {
     const f2 zero{0.f, 0.f};
@@ -1433,11 +1436,18 @@ __device__ void ring_advection_pass_f2(double *Sg, f2 *SP, f2 *W, f2 *CF, f2 *F,
     unsigned pos = 0;  // bit n: the upwind cell of face tid + n bs is its left neighbour
     auto cell = [&](int n) { return EXACT ? tid + n * bs : min(tid + n * bs, nz - 1); };
     auto owned = [&](int n) { return EXACT || tid + n * bs < nz; };
-    // X[j] and its halo copy (cells nz - 2, nz - 1 at -2, -1; cell 0 at nz)
-    auto put = [&](f2 *X, int j, f2 x) {
+    // X[j] and its halo copy (cells nz - 2, nz - 1 at -2, -1; cell 0 at nz);
+    // n is the compile-time cell slot of j, so that in an exact ring only the
+    // first and last slots test for the halo
+    auto put = [&](f2 *X, int j, f2 x, int n) {
         X[j] = x;
-        if (j >= nz - 2) X[j - nz] = x;
-        if (j == 0) X[nz] = x;
+        if (EXACT) {
+            if (n == 0 && tid == 0) X[nz] = x;
+            if (n == PER - 1 && tid >= bs - 2) X[j - nz] = x;
+        } else {
+            if (j >= nz - 2) X[j - nz] = x;
+            if (j == 0) X[nz] = x;
+        }
     };
     // the star value at a face of the quantity X from its upwind cell u
     // (u in -1 .. nz - 1)
@@ -1458,7 +1468,7 @@ __device__ void ring_advection_pass_f2(double *Sg, f2 *SP, f2 *W, f2 *CF, f2 *F,
         am[n] = uniform ? au : f2_split(p ? dxk - vk : -(dxk + vk));
         pos |= (unsigned)p << n;
         const f2 c = f2_smul(f2_smul(cvel, star(SP, p ? j - 1 : j, am[n])), f2_split(vk));
-        if (owned(n)) put(CF, j, c);
+        if (owned(n)) put(CF, j, c, n);
     }
     // per quantity: specific values (with the previous quantity's update),
     // then the fluxes
@@ -1474,7 +1484,7 @@ __device__ void ring_advection_pass_f2(double *Sg, f2 *SP, f2 *W, f2 *CF, f2 *F,
             }
             if (q < NQ) {
                 const f2 w = f2_sdiv(f2_split(qrow[q][j]), SP[j]);
-                if (owned(n)) put(W, j, w);
+                if (owned(n)) put(W, j, w, n);
             }
         }
         if (q == NQ) break;
@@ -1483,7 +1493,7 @@ __device__ void ring_advection_pass_f2(double *Sg, f2 *SP, f2 *W, f2 *CF, f2 *F,
         for (int n = 0; n < PER; ++n) {
             const int j = cell(n);
             const f2 f = f2_smul(star(W, (pos >> n) & 1u ? j - 1 : j, am[n]), CF[j]);
-            if (owned(n)) put(F, j, f);
+            if (owned(n)) put(F, j, f, n);
         }
         __syncthreads();
     }
@@ -1499,7 +1509,7 @@ __device__ void ring_advection_pass_f2(double *Sg, f2 *SP, f2 *W, f2 *CF, f2 *F,
         const f2 sp = f2_split(s);
         if (owned(n)) {
             Sg[j] = s;
-            put(SP, j, sp);
+            put(SP, j, sp, n);
         }
     }
     __syncthreads();
