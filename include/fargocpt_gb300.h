@@ -101,6 +101,13 @@ enum { FGPU_ARTVISC_NONE = 0, FGPU_ARTVISC_SN = 1, FGPU_ARTVISC_TW = 2 };
 enum { FGPU_LIMITER_VANLEER = 0, FGPU_LIMITER_MC = 1 };
 enum { FGPU_BETA_REF_ZERO = 0, FGPU_BETA_REF_REFERENCE = 1,
        FGPU_BETA_REF_DISKMODEL = 2, FGPU_BETA_REF_FLOOR = 3 };
+/* FGPU_PRECISION_FP64: FargoCPT's FP64 fields and FP64 state updates; the
+ * kernels compute in float pairs (48 significant bits) unless the environment
+ * variable FARGO_GB300_FP64_ARITH is "fp64" when fgpu_create runs (then in
+ * FP64; "pair" or unset: pairs; any other value: FGPU_ERR_BAD_ARG).
+ * FGPU_PRECISION_FP32_MIXED: FP32 fields in HBM (v_phi and the potential
+ * relative to the Keplerian disk), FargoCPT's FP64 fields on upload and
+ * download. */
 enum { FGPU_PRECISION_FP64 = 0, FGPU_PRECISION_FP32_MIXED = 1 };
 enum { FGPU_INTEGRATOR_EULER = 0, FGPU_INTEGRATOR_LEAPFROG = 1 };
 /* composite boundaries (boundary_conditions/config.cpp:344-430): "individual"
