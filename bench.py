@@ -332,6 +332,20 @@ def measure_batch(args, torch, dist):
     ms = e0.elapsed_time(e1)
     s1 = steps()
     updates = float(np.sum((s1 - s0) * cells))
+    # the same steps with the gas kick's and the closing substeps each as one
+    # persistent cooperative launch (fgpu_batch_set_mode); then back
+    b.set_mode(True)
+    b.run(args.steps, steps_per_graph=args.steps)   # captures its graph
+    torch.cuda.synchronize()
+    p0 = steps()
+    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2.record(stream)
+    b.run(args.steps, steps_per_graph=args.steps)
+    e3.record(stream)
+    e3.synchronize()
+    pers_ms = e2.elapsed_time(e3)
+    pers_updates = float(np.sum((steps() - p0) * cells))
+    b.set_mode(False)
     # end to end through the C ABI with host buffers: per step, every disk's
     # CFL dt read back, its bodies and (dt, t) sent (fgpu_batch_step)
     dts = np.empty(b.n)
@@ -351,6 +365,7 @@ def measure_batch(args, torch, dist):
     for e in b.disks:
         assert e.check_finite() is None, "non-finite state after the batched benchmark"
     out = dict(ms=ms, updates=updates, e2e_s=e2e_s, e2e_updates=e2e_updates, tiles=tiles,
+               pers_ms=pers_ms, pers_updates=pers_updates,
                tune_s=tune_s, cells=float(np.sum(cells)), n=b.n,
                nr=sorted(set(int(x[0].nrad) for x in disks)))
     b.close()
@@ -480,6 +495,12 @@ def main():
                               "peak_source": peak_src},
             "tiles": rb["tiles"], "autotune_s": rb["tune_s"],
             "gpu_launches": 14 * args.steps,
+            # the same steps with the substeps of the gas kick and of the
+            # step's close each as one persistent cooperative launch
+            "persistent_sequences": {
+                "value": world * rb["pers_updates"] / (rb["pers_ms"] * 1e-3),
+                "unit": "cell-updates/s", "ms_per_step": rb["pers_ms"] / args.steps,
+                "launches_per_step": "clock, 2 persistent sequences, transports"},
             "error": "per disk the FP32-mixed arithmetic (bit-identical to the single-disk "
                      "FP32-mixed engine); python -m fargocpt_gb300.accuracy gives its error",
         }

@@ -206,7 +206,12 @@ EXPORTED_SYMBOLS = [
     "fgpu_batch_create", "fgpu_batch_destroy", "fgpu_batch_last_error", "fgpu_batch_size",
     "fgpu_batch_disk", "fgpu_batch_get_tiles", "fgpu_batch_set_tiles", "fgpu_batch_autotune",
     "fgpu_batch_step", "fgpu_batch_set_clock", "fgpu_batch_get_clock", "fgpu_batch_run",
+    "fgpu_batch_set_mode", "fgpu_batch_get_mode",
 ]
+
+
+# fgpu_batch_set_mode: one launch per substep, or the persistent sequences
+BATCH_LAUNCHES, BATCH_PERSISTENT = 0, 1
 
 
 def _declare(lib: C.CDLL) -> C.CDLL:
@@ -266,6 +271,8 @@ def _declare(lib: C.CDLL) -> C.CDLL:
         "fgpu_batch_set_clock": ([vp, C.c_int, P(FgpuClock)], C.c_int),
         "fgpu_batch_get_clock": ([vp, C.c_int, P(FgpuClock)], C.c_int),
         "fgpu_batch_run": ([vp, C.c_int, C.c_int, P(C.c_int)], C.c_int),
+        "fgpu_batch_set_mode": ([vp, C.c_int], C.c_int),
+        "fgpu_batch_get_mode": ([vp, P(C.c_int)], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -92,6 +92,18 @@ class Batch:
         t = FgpuTiles.from_dict(tiles)
         self._check(self.lib.fgpu_batch_set_tiles(self.h, C.byref(t)), "fgpu_batch_set_tiles")
 
+    def set_mode(self, persistent: bool):
+        """One launch per substep (False), or the gas kick's and the closing
+        substeps each as one persistent cooperative launch (True)."""
+        self._check(self.lib.fgpu_batch_set_mode(self.h, 1 if persistent else 0),
+                    "fgpu_batch_set_mode")
+
+    @property
+    def persistent(self) -> bool:
+        m = C.c_int()
+        self._check(self.lib.fgpu_batch_get_mode(self.h, C.byref(m)), "fgpu_batch_get_mode")
+        return m.value == 1
+
     def autotune(self, reps: int = 5, cache: str | None = None, device: str = "cuda") -> dict:
         """Times candidate tile shapes of every kernel on the current state and
         keeps the fastest (the state is restored).  With ``cache``, a JSON file

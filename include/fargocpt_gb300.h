@@ -548,6 +548,20 @@ int fgpu_batch_get_tiles(const fgpu_batch *b, fgpu_tiles *tiles);
 int fgpu_batch_set_tiles(fgpu_batch *b, const fgpu_tiles *tiles);
 int fgpu_batch_autotune(fgpu_batch *b, int reps, fgpu_tiles *best);
 
+/* How a step's substeps are launched.  FGPU_BATCH_LAUNCHES (the default):
+ * one grid-stride launch over all disks per substep, each with its
+ * autotuned tile shape.  FGPU_BATCH_PERSISTENT: the gas kick's substeps
+ * (potential, source terms, artificial viscosity, stress, viscous update,
+ * the mid-step ghost rings) as one persistent cooperative launch, the
+ * closing substeps (velocities from momenta, damping, ghost rings, CFL) as
+ * another, the grid synchronising between substeps (256 threads per block,
+ * the autotuned rings per tile); the transports stay separate launches.
+ * Both give the same bits.  A captured step sequence is rebuilt;
+ * FGPU_ERR_UNSUPPORTED without cooperative launch. */
+enum { FGPU_BATCH_LAUNCHES = 0, FGPU_BATCH_PERSISTENT = 1 };
+int fgpu_batch_set_mode(fgpu_batch *b, int mode);
+int fgpu_batch_get_mode(const fgpu_batch *b, int *mode);
+
 /* One step of every disk with host-given dt[k] and t[k] (dt[k] = 0 skips
  * disk k) and the bodies last given to each disk's handle: fgpu_step_euler
  * of all disks at once. */

@@ -302,3 +302,48 @@ def test_register_blocked_groups_match_strided_pass(monkeypatch):
     for k in range(len(disks)):
         for f in EVOLVED:
             assert np.array_equal(out[0][k][f], out[1][k][f]), (k, f)
+
+
+def test_persistent_substep_sequences_give_the_same_bits():
+    """FGPU_BATCH_PERSISTENT runs the gas kick's substeps and the closing
+    substeps as two cooperative launches with grid-wide synchronisation
+    between substeps: bit-identical to one launch per substep, with the
+    host clock (isothermal and adiabatic disks, a disk sitting a step out)
+    and with the device clock in CUDA graphs."""
+    from fargocpt_gb300.batch import Batch, start_disks
+
+    small = _small_disks()
+    host = []
+    for persistent in (False, True):
+        b = Batch([p for p, *_ in small], [r for _, _, r, _ in small])
+        b.set_mode(persistent)
+        assert b.persistent == persistent
+        b0 = _bodies(0.0)
+        for be, (_, _, _, st) in zip(b.disks, small):
+            _load(be, st, b0)
+        t = np.zeros(len(small))
+        for n in range(10):
+            dts = np.array([be.condition_cfl() for be in b.disks])
+            if n == 4:
+                dts[1] = 0.0
+            for k, be in enumerate(b.disks):
+                be.set_bodies(_bodies(float(t[k])), 0.0, 0.0, 0.0)
+            b.step(dts, t)
+            t += dts
+        host.append([{f: e.get_field(f) for f in EVOLVED} for e in b.disks])
+        b.close()
+    disks = _sweep(4, seed=31)
+    dev = []
+    for persistent in (False, True):
+        b = Batch([x[0] for x in disks], [x[2] for x in disks])
+        b.set_mode(persistent)
+        start_disks(b, disks, t_end=1.0, monitor_dt=0.1)
+        b.run(24, steps_per_graph=8)
+        dev.append([{f: e.get_field(f) for f in EVOLVED} for e in b.disks])
+        steps = [b.clock(k)["steps"] for k in range(len(disks))]
+        b.close()
+        assert all(s == 24 for s in steps)
+    for out in (host, dev):
+        for k in range(len(out[0])):
+            for f in EVOLVED:
+                assert np.array_equal(out[0][k][f], out[1][k][f]), (k, f)
