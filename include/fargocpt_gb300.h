@@ -554,10 +554,11 @@ int fgpu_batch_autotune(fgpu_batch *b, int reps, fgpu_tiles *best);
  * (potential, source terms, artificial viscosity, stress, viscous update,
  * the mid-step ghost rings) as one persistent cooperative launch, the
  * closing substeps (velocities from momenta, damping, ghost rings, CFL) as
- * another, the grid synchronising between substeps (256 threads per block,
+ * another, the grid synchronising between substeps (128 threads per block,
  * the autotuned rings per tile); the transports stay separate launches.
- * Both give the same bits.  A captured step sequence is rebuilt;
- * FGPU_ERR_UNSUPPORTED without cooperative launch. */
+ * Both give the same bits; the persistent form is the slower on GB300 (one
+ * block shape and register budget for every substep).  A captured step
+ * sequence is rebuilt; FGPU_ERR_UNSUPPORTED without cooperative launch. */
 enum { FGPU_BATCH_LAUNCHES = 0, FGPU_BATCH_PERSISTENT = 1 };
 int fgpu_batch_set_mode(fgpu_batch *b, int mode);
 int fgpu_batch_get_mode(const fgpu_batch *b, int *mode);
