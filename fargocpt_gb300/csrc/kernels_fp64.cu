@@ -2209,18 +2209,18 @@ __global__ void k_disk_force_bodies(Geo g, Tables t, Phys ph, ForceBodies fb,
     for (int j = threadIdx.x; j < nz; j += blockDim.x) {
         const f2 smooth = f2_smul(eps, f2_split(H[row + j]));
         const f2 s2 = f2_smul(smooth, smooth);
-        const f2 xc = f2_mul(rm, f2{t.cosHi[j], t.cosLo[j]});
-        const f2 yc = f2_mul(rm, f2{t.sinHi[j], t.sinLo[j]});
+        const f2 xc = f2_smul(rm, f2{t.cosHi[j], t.cosLo[j]});
+        const f2 yc = f2_smul(rm, f2{t.sinHi[j], t.sinLo[j]});
         // sigma less the ring mean: the FP64 difference (they agree closely)
         const f2 dsig = f2_split(S[row + j] - sigma1d);
 #pragma unroll
         for (int b = 0; b < kForceBodies; ++b) {
             if (b < fb.n) {
-                const f2 dx = f2_sub(xc, f2{fb.xh[b], fb.xl[b]});
-                const f2 dy = f2_sub(yc, f2{fb.yh[b], fb.yl[b]});
-                const f2 dsm2 = f2_add(f2_add(f2_mul(dx, dx), f2_mul(dy, dy)), s2);
+                const f2 dx = f2_ssub(xc, f2{fb.xh[b], fb.xl[b]});
+                const f2 dy = f2_ssub(yc, f2{fb.yh[b], fb.yl[b]});
+                const f2 dsm2 = f2_sadd(f2_sadd(f2_smul(dx, dx), f2_smul(dy, dy)), s2);
                 const f2 rinv = f2_rsqrt(dsm2);
-                f2 w = f2_mul(dsig, f2_mul(f2_mul(rinv, rinv), rinv));
+                f2 w = f2_smul(dsig, f2_smul(f2_smul(rinv, rinv), rinv));
                 if ((fb.klahr >> b) & 1u) {
                     // Klahr's factor inside r_sm (Force.cpp:88-100): rare, in FP64
                     const f2 dsm_p = f2_mul(dsm2, rinv);
@@ -2233,8 +2233,8 @@ __global__ void k_disk_force_bodies(Geo g, Tables t, Phys ph, ForceBodies fb,
                         }
                     }
                 }
-                f2_accumulate(axh[b], axl[b], f2_mul(w, dx));
-                f2_accumulate(ayh[b], ayl[b], f2_mul(w, dy));
+                f2_accumulate(axh[b], axl[b], f2_smul(w, dx));
+                f2_accumulate(ayh[b], ayl[b], f2_smul(w, dy));
             }
         }
     }
