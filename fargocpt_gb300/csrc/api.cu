@@ -36,6 +36,7 @@ struct fgpu_engine {
     double *sigma_alt = nullptr, *vr_alt = nullptr, *vaz_alt = nullptr, *energy_alt = nullptr;
     double *mom[4] = {};
     double *ring_ws = nullptr;
+    int *ring_shift = nullptr;  // the pair azimuthal pass's shift per ring
     size_t az_smem = 0;
     int az_block = 256;
     bool pair_arith = true;  // the kernels' arithmetic in float pairs (else FP64)
@@ -972,6 +973,12 @@ static int create_engine(const fgpu_params *params, const double *radii, cudaStr
         const int per = azimuthal_cells_per_thread(eng->nz);
         eng->az_block = std::max(128, std::min(512, ((eng->nz + per - 1) / per + 31) / 32 * 32));
     }
+    if (cudaMalloc(&eng->ring_shift, sizeof(int) * (size_t)eng->nr) != cudaSuccess ||
+        cudaMemsetAsync(eng->ring_shift, 0, sizeof(int) * (size_t)eng->nr, eng->stream) !=
+            cudaSuccess) {
+        eng->err = "out of device memory (ring shifts)";
+        return fail(FGPU_ERR_OOM);
+    }
     eng->az_smem = azimuthal_smem_bytes(eng->nz);
     if (eng->az_smem > 220 * 1024) {
         if (cudaMalloc(&eng->ring_ws, eng->az_smem * (size_t)eng->nr) != cudaSuccess) {
@@ -1008,7 +1015,8 @@ extern "C" int fgpu_destroy(fgpu_engine *eng)
     for (int f = 0; f < FGPU_FIELD_COUNT; ++f) cudaFree(eng->field[f]);
     cudaFree(eng->sigma_alt); cudaFree(eng->vr_alt); cudaFree(eng->vaz_alt); cudaFree(eng->energy_alt);
     for (int k = 0; k < 4; ++k) cudaFree(eng->mom[k]);
-    cudaFree(eng->ring_ws); cudaFree(eng->tables_mem); cudaFree(eng->damp_mem);
+    cudaFree(eng->ring_ws); cudaFree(eng->ring_shift); cudaFree(eng->tables_mem);
+    cudaFree(eng->damp_mem);
     cudaFree(eng->damp_rings); cudaFree(eng->partial); cudaFree(eng->red_out);
     cudaFree(eng->pair_mem);
     cudaFree(eng->com_mem);
@@ -1577,10 +1585,10 @@ static void transport(fgpu_engine *eng, double dt)
                             eng->mom, eng->energy_alt, eng->sigma_alt);
     mark(eng, 7);
     launch_transport_azimuthal(L, dt, eng->az_block, eng->mom, eng->energy_alt, eng->sigma_alt,
-                               s.vaz, eng->ring_ws, eng->az_smem);
+                               s.vaz, eng->ring_ws, eng->az_smem, eng->ring_shift);
     mark(eng, 8);
     launch_finish(L, omf, eng->mom, eng->sigma_alt, eng->energy_alt, s.vr, eng->vr_alt,
-                  eng->vaz_alt, s.sigma, s.energy);
+                  eng->vaz_alt, s.sigma, s.energy, eng->ring_shift);
     std::swap(f[FGPU_V_RADIAL], eng->vr_alt);
     std::swap(f[FGPU_V_AZIMUTHAL], eng->vaz_alt);
     mark(eng, 9);

@@ -46,12 +46,15 @@ size_t azimuthal_smem_bytes(int nz);
 int azimuthal_cells_per_thread(int nz);
 cudaError_t prepare_azimuthal(size_t smem);
 // block: threads of the FP64 kernel (the pair kernel chooses its own)
+// ring_shift (nr ints): the pair kernel leaves AdvectSHIFT to the velocity
+// rebuild and writes each ring's shift there
 void launch_transport_azimuthal(const Launch &L, double dt, int block, double *const mom[4],
                                 double *E, double *S, const double *vaz, double *ring_ws,
-                                size_t smem);
+                                size_t smem, int *ring_shift);
+// ring_shift: the azimuthal shifts the pair rebuild applies (pair form)
 void launch_finish(const Launch &L, double omf, double *const mom[4], const double *S_t,
                    const double *E_t, const double *vr_in, double *vr_out, double *vaz_out,
-                   double *S_out, double *E_out);
+                   double *S_out, double *E_out, const int *ring_shift);
 void launch_damping(const Launch &L, const Damping &dm, double dt, const int *rings, int nrings,
                     const State &s);
 void launch_derived_cfl(const Launch &L, int mode, const State &s, unsigned long long *dt_min);
@@ -71,7 +74,7 @@ void launch_stress_pair(const Launch &L, const double *S, const double *vr, cons
 void launch_viscous_pair(const Launch &L, double dt, double beta_inv, int mode, const State &s);
 void launch_finish_pair(const Launch &L, double omf, double *const mom[4], const double *S_t,
                         const double *E_t, const double *vr_in, double *vr_out, double *vaz_out,
-                        double *S_out, double *E_out);
+                        double *S_out, double *E_out, const int *ring_shift);
 // bodies one disk-force pass handles
 constexpr int kForceBodies = 4;
 

@@ -1521,10 +1521,14 @@ __host__ __device__ constexpr size_t pair_ring_f2s(int nz) { return (size_t)4 * 
 
 // WS: the ring's arrays in the per-ring global workspace (rings beyond the
 // shared memory), else in shared memory
+// The integer shift of AdvectSHIFT is not applied here: ring_shift[i]
+// receives it (in [0, nz)), and the velocity rebuild (k_finish_p) reads each
+// ring's transported cells at their shifted places.
 template <int PER, int MAXT, int NQ, bool WS, bool EXACT>
 __global__ void __launch_bounds__(MAXT) k_transport_azimuthal_f2(
     Geo g, Tables t, double dt, int mc, int fast, const double *__restrict__ vaz, double *mom0,
-    double *mom1, double *mom2, double *mom3, double *E, double *S, double *ring_ws)
+    double *mom1, double *mom2, double *mom3, double *E, double *S, double *ring_ws,
+    int *__restrict__ ring_shift)
 {
     extern __shared__ double smem[];
     __shared__ double red[33];
@@ -1582,28 +1586,9 @@ __global__ void __launch_bounds__(MAXT) k_transport_azimuthal_f2(
         ring_advection_pass_f2<PER, NQ, EXACT>(Sg, SP, W, CF, F, qrow, vown, dt, dxtheta,
                                                half_invdx, dxrad * invsurf, nz, mc, true, vt);
     }
-    // AdvectSHIFT of every quantity, sigma last, staged through W's doubles
-    double *stage = reinterpret_cast<double *>(W);
-#pragma unroll
-    for (int q = 0; q <= NQ; ++q) {
-        double *Q = q < NQ ? qrow[q] : Sg;
-#pragma unroll
-        for (int n = 0; n < PER; ++n) {
-            const int j = tid + n * bs;
-            if (owned(n)) stage[j] = Q[j];
-        }
-        __syncthreads();
-#pragma unroll
-        for (int n = 0; n < PER; ++n) {
-            const int j = tid + n * bs;
-            if (owned(n)) {
-                int ji = (j - nshift) % nz;
-                if (ji < 0) ji += nz;
-                Q[j] = stage[ji];
-            }
-        }
-        __syncthreads();
-    }
+    // AdvectSHIFT (:238-268) is the rebuild's: it reads cell j of this ring
+    // from cell j - nshift
+    if (threadIdx.x == 0) ring_shift[i] = ((nshift % nz) + nz) % nz;
 }
 
 // ---------------------------------------------------------------------------
@@ -2485,7 +2470,7 @@ int azimuthal_pair_cells_per_thread(int nz) { return nz <= 1024 ? 2 : (nz <= 614
 
 void launch_transport_azimuthal(const Launch &L, double dt, int block, double *const mom[4],
                                 double *E, double *S, const double *vaz, double *ring_ws,
-                                size_t smem)
+                                size_t smem, int *ring_shift)
 {
     const bool pair = L.pair;
     const int nq = L.ph.adiabatic ? 5 : 4;
@@ -2497,7 +2482,7 @@ void launch_transport_azimuthal(const Launch &L, double dt, int block, double *c
 #define AZ2_LAUNCH1(P, T, Q, WS, X)                                                             \
     k_transport_azimuthal_f2<P, T, Q, WS, X><<<L.g.nr, threads, dyn, L.stream>>>(                \
         L.g, L.t, dt, L.ph.limiter_mc, L.ph.fast_transport, vaz, mom[0], mom[1], mom[2], mom[3], \
-        E, S, ring_ws)
+        E, S, ring_ws, ring_shift)
 #define AZ2_LAUNCH2(P, T, Q)                                                                    \
     if (exact) AZ2_LAUNCH1(P, T, Q, false, true); else AZ2_LAUNCH1(P, T, Q, false, false)
 #define AZ2_LAUNCH(P, T)                                                                        \
@@ -2535,10 +2520,11 @@ void launch_transport_azimuthal(const Launch &L, double dt, int block, double *c
 
 void launch_finish(const Launch &L, double omf, double *const mom[4], const double *S_t,
                    const double *E_t, const double *vr_in, double *vr_out, double *vaz_out,
-                   double *S_out, double *E_out)
+                   double *S_out, double *E_out, const int *ring_shift)
 {
     if (L.pair)
-        return launch_finish_pair(L, omf, mom, S_t, E_t, vr_in, vr_out, vaz_out, S_out, E_out);
+        return launch_finish_pair(L, omf, mom, S_t, E_t, vr_in, vr_out, vaz_out, S_out, E_out,
+                                  ring_shift);
     k_finish<<<grid2d(L.g.nz, L.g.nr + 1, L.bx), L.bx, 0, L.stream>>>(
         L.g, L.t, L.ph, omf, mom[0], mom[1], mom[2], mom[3], S_t, E_t, vr_in, vr_out, vaz_out,
         S_out, E_out);

@@ -404,13 +404,16 @@ __global__ void k_viscous_p(Geo g, Tables t, Phys ph, double dt, double beta_inv
 }
 
 // compute_velocities_from_momenta (TransportEuler.cpp:498-535), the sigma
-// floor (SourceEuler.cpp:102-134) and the temperature floor, as k_finish
+// floor (SourceEuler.cpp:102-134) and the temperature floor, as k_finish,
+// with the azimuthal transport's AdvectSHIFT (:238-268): the transported
+// fields of ring i are read at j - shift[i]
 __global__ void k_finish_p(Geo g, Tables t, Phys ph, double omf, const double *__restrict__ mom0,
                            const double *__restrict__ mom1, const double *__restrict__ mom2,
                            const double *__restrict__ mom3, const double *__restrict__ S_t,
                            const double *__restrict__ E_t, const double *__restrict__ vr_in,
                            double *__restrict__ vr_out, double *__restrict__ vaz_out,
-                           double *__restrict__ S_out, double *__restrict__ E_out)
+                           double *__restrict__ S_out, double *__restrict__ E_out,
+                           const int *__restrict__ shift)
 {
     const int nz = g.nz, nr = g.nr;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -421,16 +424,23 @@ __global__ void k_finish_p(Geo g, Tables t, Phys ph, double omf, const double *_
         vr_out[c] = vr_in[c];
         return;
     }
-    const double s = S_t[c];
+    // cell j of ring k before the shift
+    auto at = [&](int k, int jj) {
+        int a = jj - __ldg(shift + k);
+        if (a < 0) a += nz;
+        return CELL(k, a);
+    };
+    const size_t cs = at(i, j);
+    const double s = S_t[cs];
     const f2 sp = P(s);
     if (i == 0) {
         vr_out[c] = 0.0;
     } else {
-        const size_t cm = CELL(i - 1, j);
-        vr_out[c] = f2_to_double((P(mom0[cm]) + P(mom1[c])) / (P(S_t[cm]) + sp));
+        const size_t cm = at(i - 1, j);
+        vr_out[c] = f2_to_double((P(mom0[cm]) + P(mom1[cs])) / (P(S_t[cm]) + sp));
     }
-    const size_t cjm = CELL(i, prv(j, nz));
-    vaz_out[c] = f2_to_double((P(mom2[cjm]) + P(mom3[c])) / (P(S_t[cjm]) + sp) *
+    const size_t cjm = at(i, prv(j, nz));
+    vaz_out[c] = f2_to_double((P(mom2[cjm]) + P(mom3[cs])) / (P(S_t[cjm]) + sp) *
                                   T(t, t.InvRmed, i) -
                               T(t, t.Rmed, i) * P(omf));
     // s < sigma_min on the bit patterns (sigma_min >= 0; a NaN stays)
@@ -438,7 +448,7 @@ __global__ void k_finish_p(Geo g, Tables t, Phys ph, double omf, const double *_
     const bool nan = (bs & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
     const double sf = (!nan && bs < __double_as_longlong(ph.sigma_min)) ? ph.sigma_min : s;
     S_out[c] = sf;
-    if (ph.adiabatic) E_out[c] = floor_e(E_t[c], sf, ph);
+    if (ph.adiabatic) E_out[c] = floor_e(E_t[cs], sf, ph);
 }
 
 dim3 grid2(int nz, int rows, int bx) { return dim3((nz + bx - 1) / bx, rows); }
@@ -484,11 +494,11 @@ void launch_viscous_pair(const Launch &L, double dt, double beta_inv, int mode, 
 
 void launch_finish_pair(const Launch &L, double omf, double *const mom[4], const double *S_t,
                         const double *E_t, const double *vr_in, double *vr_out, double *vaz_out,
-                        double *S_out, double *E_out)
+                        double *S_out, double *E_out, const int *ring_shift)
 {
     k_finish_p<<<grid2(L.g.nz, L.g.nr + 1, L.bx), L.bx, 0, L.stream>>>(
         L.g, L.t, L.ph, omf, mom[0], mom[1], mom[2], mom[3], S_t, E_t, vr_in, vr_out, vaz_out,
-        S_out, E_out);
+        S_out, E_out, ring_shift);
 }
 
 }  // namespace fgpu
