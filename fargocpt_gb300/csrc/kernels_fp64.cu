@@ -1418,12 +1418,42 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(Geo g, Tables t, do
 // EXACT (nz == PER blockDim.x): every thread owns PER cells; otherwise the
 // loops compute with the index clamped into the ring and guard only their
 // stores.  Either way the loop bodies have no branch.
-template <int PER, int NQ, bool EXACT>
+// The quantity rows, chosen by a select chain: an indexed array of their
+// pointers would sit in local memory and put a load before every row access.
+struct QRows {
+    double *r0, *r1, *r2, *r3, *r4;
+    __device__ __forceinline__ double *operator[](int q) const
+    {
+        return q == 0 ? r0 : q == 1 ? r1 : q == 2 ? r2 : q == 3 ? r3 : r4;
+    }
+};
+
+// The face fluxes of an exact ring with whole warps (SHFL): each cell's
+// update F[j] - F[j + 1] takes the right neighbour's flux from the next lane
+// by a shuffle, so no flux array exists.  Its shared memory holds instead
+// the quantity's FP64 value of each cell, read from global memory once per
+// quantity and pass (the specific value and the update both use it).  Lane
+// 31's right neighbour is lane 0 of the next warp (of the next slot after
+// the last warp, cell 0 after the last cell): lane 0 publishes its flux, lane
+// 31 its flux and value, and after the quantity's closing barrier threads
+// 0 .. K - 1 (K = PER x warps, one per lane-31 cell) complete those updates.
+// The exchange buffers alternate with the quantity, so that the next
+// quantity's writes never meet this one's deferred reads.
+template <int K>
+struct PairEdges {
+    f2 first[2][K];   // lane 0's flux, slot-major: n x warps + warp
+    f2 last[2][K];    // lane 31's flux
+    double val[2][K]; // lane 31's quantity value
+};
+
+template <int PER, int NQ, bool EXACT, bool SHFL, int K>
 __device__ void ring_advection_pass_f2(double *Sg, f2 *SP, f2 *W, f2 *CF, f2 *F,
-                                       double *const *qrow, const double *v, double dt,
-                                       double dxtheta, double half_invdx, double dxrad_invsurf,
-                                       int nz, int mc, bool uniform, double vconst)
+                                       PairEdges<K> &xe, const QRows &qrow, const double *v,
+                                       double dt, double dxtheta, double half_invdx,
+                                       double dxrad_invsurf, int nz, int mc, bool uniform,
+                                       double vconst)
 {
+    static_assert(!SHFL || EXACT, "the shuffled fluxes need an exact ring");
     const int tid = threadIdx.x, bs = blockDim.x;
     // the slopes carry no constant factor; the distance does (as in
     // ring_advection_pass): k (dx - v dt) or -k (dx + v dt), k = 1 / dx
@@ -1470,6 +1500,48 @@ __device__ void ring_advection_pass_f2(double *Sg, f2 *SP, f2 *W, f2 *CF, f2 *F,
         const f2 c = f2_smul(f2_smul(cvel, star(SP, p ? j - 1 : j, am[n])), f2_split(vk));
         if (owned(n)) put(CF, j, c, n);
     }
+    if constexpr (SHFL) {
+        double *Qs = reinterpret_cast<double *>(F);
+        const int lane = tid & 31, w = tid >> 5, nw = bs >> 5, kk = PER * nw;
+        // the lane-31 cells' updates of quantity q (slot n, warp ww: cell
+        // n bs + 32 ww + 31; the next entry is its right neighbour's lane 0)
+        auto complete = [&](int q) {
+            if (tid < kk) {
+                const int b = q & 1, nx = tid + 1 == kk ? 0 : tid + 1;
+                const int n = tid / nw, ww = tid - n * nw;
+                qrow[q][n * bs + 32 * ww + 31] =
+                    xe.val[b][tid] + f2_to_double(f2_ssub(xe.last[b][tid], xe.first[b][nx]));
+            }
+        };
+#pragma unroll 1
+        for (int q = 0; q < NQ; ++q) {
+            if (q > 0) complete(q - 1);
+            double *Q = qrow[q];
+            const int b = q & 1;
+#pragma unroll
+            for (int n = 0; n < PER; ++n) {
+                const int j = tid + n * bs;
+                const double x = Q[j];
+                Qs[j] = x;
+                if (lane == 31) xe.val[b][n * nw + w] = x;
+                put(W, j, f2_sdiv(f2_split(x), SP[j]), n);
+            }
+            __syncthreads();
+#pragma unroll
+            for (int n = 0; n < PER; ++n) {
+                const int j = tid + n * bs;
+                const f2 f = f2_smul(star(W, (pos >> n) & 1u ? j - 1 : j, am[n]), CF[j]);
+                const f2 fr{__shfl_down_sync(0xffffffffu, f.h, 1),
+                            __shfl_down_sync(0xffffffffu, f.l, 1)};
+                if (lane == 0) xe.first[b][n * nw + w] = f;
+                if (lane == 31) xe.last[b][n * nw + w] = f;
+                const double qn = Qs[j] + f2_to_double(f2_ssub(f, fr));
+                if (lane != 31) Q[j] = qn;
+            }
+            __syncthreads();
+        }
+        if (NQ > 0) complete(NQ - 1);
+    } else {
     // per quantity: specific values (with the previous quantity's update),
     // then the fluxes
 #pragma unroll 1
@@ -1496,6 +1568,7 @@ __device__ void ring_advection_pass_f2(double *Sg, f2 *SP, f2 *W, f2 *CF, f2 *F,
             if (owned(n)) put(F, j, f, n);
         }
         __syncthreads();
+    }
     }
     // sigma: QRStar == 1, the flux is the face factor itself (CF is
     // complete: the barriers of the quantities, or this one when there are
@@ -1530,8 +1603,13 @@ __global__ void __launch_bounds__(MAXT) k_transport_azimuthal_f2(
     double *mom1, double *mom2, double *mom3, double *E, double *S, double *ring_ws,
     int *__restrict__ ring_shift)
 {
+    // the shuffled fluxes on exact rings of up to 6 cells per thread (their
+    // exchange buffers, 9 KB at 6 x 1024, fit beside the ring's arrays)
+    constexpr bool SHFL = EXACT && !WS && PER <= 6;
+    constexpr int K = SHFL ? PER * (MAXT / 32) : 1;
     extern __shared__ double smem[];
     __shared__ double red[33];
+    __shared__ PairEdges<K> xe;
     const int nz = g.nz;
     const int i = blockIdx.x;
     const int tid = threadIdx.x, bs = blockDim.x;
@@ -1541,6 +1619,19 @@ __global__ void __launch_bounds__(MAXT) k_transport_azimuthal_f2(
     f2 *SP = base + 2, *W = SP + (nz + 4), *CF = W + (nz + 4), *F = CF + (nz + 4);
     double *Sg = S + row;
     auto owned = [&](int n) { return EXACT || tid + n * bs < nz; };
+    // the ring's transported rows come from DRAM (the radial pass wrote the
+    // whole disk since): ask L2 for all of them now, so that their reads in
+    // the first pass, one quantity after the other, find them there
+    {
+        const int lines = (nz + 15) >> 4;  // 128-byte lines of a row
+        const double *rows[6] = {Sg, mom0 + row, mom1 + row, mom2 + row, mom3 + row, E + row};
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+            if (r == 5 && NQ < 5) break;
+            for (int l = tid; l < lines; l += bs)
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(rows[r] + min(16 * l, nz - 1)));
+        }
+    }
 
     // compute_average_azimuthal_velocity, :174-189
     double vown[PER];
@@ -1575,16 +1666,17 @@ __global__ void __launch_bounds__(MAXT) k_transport_azimuthal_f2(
     }
     __syncthreads();
 
-    double *qrow[5] = {mom0 + row, mom1 + row, mom2 + row, mom3 + row, E + row};
+    const QRows qrow{mom0 + row, mom1 + row, mom2 + row, mom3 + row, E + row};
     const double dxtheta = g.dphi * t.Rmed[i];
     const double half_invdx = 0.5 * (1.0 / dxtheta);
     const double dxrad = (t.Rsup[i] - t.Rinf[i]) * dt;
     const double invsurf = t.InvSurf[i];
-    ring_advection_pass_f2<PER, NQ, EXACT>(Sg, SP, W, CF, F, qrow, vown, dt, dxtheta, half_invdx,
-                                           dxrad * invsurf, nz, mc, false, 0.0);
+    ring_advection_pass_f2<PER, NQ, EXACT, SHFL>(Sg, SP, W, CF, F, xe, qrow, vown, dt, dxtheta,
+                                                 half_invdx, dxrad * invsurf, nz, mc, false, 0.0);
     if (fast) {
-        ring_advection_pass_f2<PER, NQ, EXACT>(Sg, SP, W, CF, F, qrow, vown, dt, dxtheta,
-                                               half_invdx, dxrad * invsurf, nz, mc, true, vt);
+        ring_advection_pass_f2<PER, NQ, EXACT, SHFL>(Sg, SP, W, CF, F, xe, qrow, vown, dt,
+                                                     dxtheta, half_invdx, dxrad * invsurf, nz,
+                                                     mc, true, vt);
     }
     // AdvectSHIFT (:238-268) is the rebuild's: it reads cell j of this ring
     // from cell j - nshift
