@@ -930,14 +930,13 @@ __device__ __forceinline__ f2 lim_f2(f2 a, f2 b, int mc)
 // ---------------------------------------------------------------------------
 // The specific quantities of ring i (slots 0 .. NQ - 1: the two radial
 // momenta's velocities, the two angular momenta's, energy / sigma) and sigma
-// (slot NQ); sig = sigma as a double
+// (slot NQ)
 template <int NQ>
 __device__ __forceinline__ void rad_ring_f2(int i, int j, int nz, const double *S, const double *vr,
                                             const double *vaz, const double *E, double omf,
-                                            const Tables &t, f2 *w, double &sig)
+                                            const Tables &t, f2 *w)
 {
-    sig = S[CELL(i, j)];
-    const f2 sg = f2_split(sig);
+    const f2 sg = f2_split(S[CELL(i, j)]);
     const f2 r{t.RmedHi[i], t.RmedLo[i]};
 #pragma unroll
     for (int s = 0; s < NQ; ++s) {
@@ -978,11 +977,10 @@ __device__ __forceinline__ void radial_sweep_f2(const Geo &g, const Tables &t, d
     double *const outq[5] = {mom0, mom1, mom2, mom3, E_out};
 
     // rolling state as in k_transport_radial: rings k-1 (wa, da), k (wb, db,
-    // ub: its upward difference) and k+1 (wn); sigma of k-1 / k / k+1
+    // ub: its upward difference) and k+1 (wn)
     f2 wa[NW], wb[NW], wn[NW], da[NW], db[NW], ub[NW];
 #pragma unroll
     for (int q = 0; q < NW; ++q) wa[q] = wb[q] = wn[q] = da[q] = db[q] = ub[q] = zero;
-    double sa = 0.0, sb = 0.0, sn = 0.0;
 
     // slope of a ring from its up/down differences (zero on the first and
     // last ring), without van Leer's factor 2
@@ -997,13 +995,12 @@ __device__ __forceinline__ void radial_sweep_f2(const Geo &g, const Tables &t, d
     // prime rings k-1 = i0-1 and k = i0 (their slopes need rings i0-2 .. i0+1)
     {
         f2 wm2[NW];
-        double s_tmp = 0.0;
 #pragma unroll
         for (int q = 0; q < NW; ++q) wm2[q] = zero;
         const int r0 = i0 - 1;
-        if (r0 - 1 >= 0) rad_ring_f2<NQ>(r0 - 1, j, nz, S, vr, vaz, E, omf, t, wm2, s_tmp);
-        if (r0 >= 0) rad_ring_f2<NQ>(r0, j, nz, S, vr, vaz, E, omf, t, wa, sa);
-        rad_ring_f2<NQ>(i0, j, nz, S, vr, vaz, E, omf, t, wb, sb);
+        if (r0 - 1 >= 0) rad_ring_f2<NQ>(r0 - 1, j, nz, S, vr, vaz, E, omf, t, wm2);
+        if (r0 >= 0) rad_ring_f2<NQ>(r0, j, nz, S, vr, vaz, E, omf, t, wa);
+        rad_ring_f2<NQ>(i0, j, nz, S, vr, vaz, E, omf, t, wb);
         f2 downa[NW];
 #pragma unroll
         for (int q = 0; q < NW; ++q) {
@@ -1011,7 +1008,7 @@ __device__ __forceinline__ void radial_sweep_f2(const Geo &g, const Tables &t, d
             ub[q] = r0 >= 0 ? dif(i0, wb[q], wa[q]) : zero;  // up of k-1 = down of k
         }
         const bool has_next = i0 + 1 < nr;
-        if (has_next) rad_ring_f2<NQ>(i0 + 1, j, nz, S, vr, vaz, E, omf, t, wn, sn);
+        if (has_next) rad_ring_f2<NQ>(i0 + 1, j, nz, S, vr, vaz, E, omf, t, wn);
 #pragma unroll
         for (int q = 0; q < NW; ++q) {
             da[q] = r0 >= 0 ? lim(r0, ub[q], downa[q]) : zero;
@@ -1020,8 +1017,7 @@ __device__ __forceinline__ void radial_sweep_f2(const Geo &g, const Tables &t, d
             ub[q] = up;
         }
     }
-    f2 flux_prev[NW], q_prev[NH];
-    double e_prev = 0.0;
+    f2 flux_prev[NW];
     for (int k = i0; k <= i1; ++k) {
         // flux through the interface k (between rings k-1 and k)
         f2 flux[NW];
@@ -1047,34 +1043,32 @@ __device__ __forceinline__ void radial_sweep_f2(const Geo &g, const Tables &t, d
             flux[NH] = bsv;
         }
         if (k > i0) {
-            // VanLeerRadial update of ring k-1 (:586-591)
+            // VanLeerRadial update of ring k-1 (:586-591), whose specific
+            // quantities are wa; its conserved momenta sigma w are formed
+            // here and its sigma and energy re-read (cache hits), so that
+            // the walk carries none of them
             const int i = k - 1;
             const f2 invs{t.InvSurfHi[i], t.InvSurfLo[i]};
             const size_t c = CELL(i, j);
 #pragma unroll
             for (int s = 0; s < NW; ++s) {
                 const f2 dq = f2_smul(f2_ssub(flux_prev[s], flux[s]), invs);
-                if (s < 4 && s < NH) outq[s][c] = f2_to_double(f2_sadd(q_prev[s], dq));
-                else if (s == 4 && NQ == 5) E_out[c] = e_prev + f2_to_double(dq);
-                else S_out[c] = sa + f2_to_double(dq);
+                if (s < 4 && s < NH)
+                    outq[s][c] = f2_to_double(f2_sadd(f2_smul(wa[NH], wa[s]), dq));
+                else if (s == 4 && NQ == 5) E_out[c] = E[c] + f2_to_double(dq);
+                else S_out[c] = S[c] + f2_to_double(dq);
             }
         }
         if (k < i1) {
-            // conserved quantities of ring k for its update at interface k+1
+            // the fluxes through interface k, for ring k's update at k+1
 #pragma unroll
             for (int q = 0; q < NW; ++q) flux_prev[q] = flux[q];
-            const f2 sp = wb[NH];
-#pragma unroll
-            for (int s = 0; s < NH; ++s)
-                if (s < 4) q_prev[s] = f2_smul(sp, wb[s]);
-            if (NQ == 5) e_prev = E[CELL(k, j)];
             // advance: ring k becomes k-1, ring k+1 becomes k
             const bool more = k + 2 < nr;
             f2 w2[NW];
-            double s2 = 0.0;
 #pragma unroll
             for (int q = 0; q < NW; ++q) w2[q] = zero;
-            if (more) rad_ring_f2<NQ>(k + 2, j, nz, S, vr, vaz, E, omf, t, w2, s2);
+            if (more) rad_ring_f2<NQ>(k + 2, j, nz, S, vr, vaz, E, omf, t, w2);
 #pragma unroll
             for (int q = 0; q < NW; ++q) {
                 wa[q] = wb[q];
@@ -1085,15 +1079,15 @@ __device__ __forceinline__ void radial_sweep_f2(const Geo &g, const Tables &t, d
                 ub[q] = up;
                 wn[q] = w2[q];
             }
-            sa = sb;
-            sb = sn;
-            sn = s2;
         }
     }
 }
 
+// 64-thread blocks, 8 per SM: 128 registers (84 bytes of spills, to L1,
+// which this kernel leaves unshared).  Measured on the 2048 x 6144 disk,
+// ms per pass: 0.708 at 128 registers, 0.761 at 156 (no spills), 0.780 at 96.
 template <int NQ>
-__global__ void k_transport_radial_f2(Geo g, Tables t, double dt, double omf, int mc, int chunk,
+__global__ void __launch_bounds__(64, 8) k_transport_radial_f2(Geo g, Tables t, double dt, double omf, int mc, int chunk,
                                       const double *__restrict__ S, const double *__restrict__ vr,
                                       const double *__restrict__ vaz, const double *__restrict__ E,
                                       double *__restrict__ mom0, double *__restrict__ mom1,
