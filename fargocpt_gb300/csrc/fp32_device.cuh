@@ -766,7 +766,7 @@ __device__ __forceinline__ void radial_col(const GeoF &g, const TablesF &t, floa
             ub[q] = upb;
         }
     }
-    float flux_prev[NW] = {}, q_prev[NW] = {};
+    float flux_prev[NW] = {};
     float kep_prev = 0.f;  // Keplerian term of ring k-1 from interface k-1
     for (int k = i0; k <= i1; ++k) {
         float flux[NW];
@@ -798,15 +798,20 @@ __device__ __forceinline__ void radial_col(const GeoF &g, const TablesF &t, floa
             else kep_lower = -t.DJ[k] * fs;
         }
         if (k > i0) {
+            // ring k-1's update; its conserved values are formed here from
+            // its specific values (wa, the products rounded as stored
+            // values) and its energy re-read, so that the walk carries none
+            // of them
             const int i = k - 1;
             const float invs = t.InvSurf[i];
             const size_t c = CELL(i, j);
-            m0[c] = q_prev[0] + (flux_prev[0] - flux[0]) * invs;
-            m1[c] = q_prev[1] + (flux_prev[1] - flux[1]) * invs;
-            m2[c] = q_prev[2] + (flux_prev[2] + kep_prev - flux[2] - kep_lower) * invs;
-            m3[c] = q_prev[3] + (flux_prev[3] + kep_prev - flux[3] - kep_lower) * invs;
-            if (NQ == 5) E_out[c] = q_prev[4] + (flux_prev[4] - flux[4]) * invs;
-            float hi = q_prev[NQ], lo = S_lo[c];
+            const float sa = wa[NQ];
+            m0[c] = __fmul_rn(sa, wa[0]) + (flux_prev[0] - flux[0]) * invs;
+            m1[c] = __fmul_rn(sa, wa[1]) + (flux_prev[1] - flux[1]) * invs;
+            m2[c] = __fmul_rn(sa, wa[2]) + (flux_prev[2] + kep_prev - flux[2] - kep_lower) * invs;
+            m3[c] = __fmul_rn(sa, wa[3]) + (flux_prev[3] + kep_prev - flux[3] - kep_lower) * invs;
+            if (NQ == 5) E_out[c] = E[c] + (flux_prev[4] - flux[4]) * invs;
+            float hi = sa, lo = S_lo[c];
             comp_add(hi, lo, (flux_prev[NQ] - flux[NQ]) * invs);
             S_out[c] = hi;
             S_lo_out[c] = lo;
@@ -815,13 +820,6 @@ __device__ __forceinline__ void radial_col(const GeoF &g, const TablesF &t, floa
 #pragma unroll
             for (int q = 0; q < NW; ++q) flux_prev[q] = flux[q];
             kep_prev = kep_upper;
-            const float sb = wb[NQ];
-            q_prev[0] = sb * wb[0];
-            q_prev[1] = sb * wb[1];
-            q_prev[2] = sb * wb[2];
-            q_prev[3] = sb * wb[3];
-            if (NQ == 5) q_prev[4] = E[CELL(k, j)];
-            q_prev[NQ] = sb;
             const bool more = k + 2 < nr;
             float w2[NW] = {};
             if (more) rad_ring_f<NQ>(k + 2, j, nz, S, vr, dv, E, t, w2);

@@ -2013,8 +2013,11 @@ __device__ f2 block_min_f2(f2 v, float *red)
 // PAIR: the ideal-EOS derived quantities (T, c_s, H, nu) in float-pair
 // arithmetic (P = (gamma - 1) e stays one FP64 product: the source terms
 // difference it)
+// 256-thread blocks; the pair form held to 64 registers, 4 blocks per SM (at
+// its free choice of 121 registers, 2 blocks: 0.67 ms on the 2048 x 6144
+// disk, at 80: 0.557, at 64: 0.502)
 template <bool PAIR>
-__global__ void k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const double *__restrict__ S,
+__global__ void __launch_bounds__(256, PAIR ? 4 : 3) k_derived_cfl(Geo g, Tables t, Phys ph, int mode, int sn, const double *__restrict__ S,
                               const double *__restrict__ E, const double *__restrict__ vr,
                               const double *__restrict__ vaz, const double *__restrict__ qplus,
                               const double *__restrict__ qminus, double *__restrict__ cs,
