@@ -546,7 +546,7 @@ static int setup_tables(fgpu_engine *eng, const double *radii)
     const int R = nr + 2;
     const double dphi = 2.0 * M_PI / (double)nz;      // Interpret.cpp:230
     const double invdphi = (double)nz / (2.0 * M_PI); // Interpret.cpp:231
-    eng->geo = Geo{nr, nz, dphi, invdphi};
+    eng->geo = Geo{nr, nz, dphi, invdphi, split_pair_host(invdphi)};
     enum { RINF, RSUP, RMED, SURF, INVRMED, INVSURF, INVDIFFRMED, INVDIFFRSUP, INVDIFFRSUPRB,
            INVRINF, RINFSQ, TWOOVER, OMEGAK, INVOMEGAK, CSISO, INVDXSRC, INVDXTHETA, EMODEL,
            HFACADI, INVCELL, INVCELL2, TWOOVERRMEDSUM, LSQTW, TWOOVERDRMED2, DIFFRMED,
@@ -841,6 +841,15 @@ static int setup_tables(fgpu_engine *eng, const double *radii)
     ph.emax_fac = p.maximum_temperature / p.mu * p.R_gas / (p.gamma - 1.0);
     ph.emin_fac_f = (float)ph.emin_fac;
     ph.emax_fac_f = (float)ph.emax_fac;  // may round to infinity: the screen then has no upper bound
+    ph.pk_gm1 = split_pair_host(ph.gm1);
+    ph.pk_g_gm1 = split_pair_host(ph.g_gm1);
+    ph.pk_alpha = split_pair_host(ph.alpha);
+    ph.pk_C2 = split_pair_host(ph.C2);
+    ph.pk_rvf = split_pair_host(ph.rvf);
+    ph.pk_hvf = split_pair_host(ph.hvf);
+    ph.pk_mu_gm1_over_R = split_pair_host(ph.mu_gm1_over_R);
+    ph.pk_cool_const = split_pair_host(ph.cool_const);
+    ph.pk_emin_fac = split_pair_host(ph.emin_fac);
     return FGPU_OK;
 }
 
@@ -1232,6 +1241,8 @@ extern "C" int fgpu_set_bodies(fgpu_engine *eng, int n, const fgpu_body *bodies,
     }
     b.ix = ix;
     b.iy = iy;
+    b.pk_ix = split_pair_host(ix);
+    b.pk_iy = split_pair_host(iy);
     b.omega_frame = omega_frame;
     auto split = [](double v, float &h, float &l) {
         h = (float)v;

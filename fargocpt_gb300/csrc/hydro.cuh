@@ -7,6 +7,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "com_boundary.cuh"
 
@@ -55,7 +56,35 @@ struct Tables {
 struct Geo {
     int nr, nz;
     double dphi, invdphi;
+    float2 pk_invdphi;    // invdphi as a float pair (split_pair_host)
 };
+
+// x as the float pair hi + lo of the float-pair kernels, computed on the
+// host with the device split's bits (f2_split in fp64_pair.cuh: hi the top 24
+// significant bits, lo the remaining 29 rounded to a float; zero below
+// 2^-74, NaN from 2^128), so that a constant split once here is the pair
+// those kernels would form from it.
+inline float2 split_pair_host(double x)
+{
+    uint64_t b;
+    memcpy(&b, &x, sizeof b);
+    const uint32_t w1 = (uint32_t)(b >> 32), w0 = (uint32_t)b;
+    const uint32_t ax = w1 & 0x7fffffffu, sign = w1 & 0x80000000u;
+    const uint32_t hb = ((ax - (896u << 20)) << 3) | (w0 >> 29);
+    const uint32_t sbits = (hb & 0x7f800000u) - (52u << 23);
+    float scale;
+    memcpy(&scale, &sbits, sizeof scale);
+    const float lf = (float)(w0 & 0x1fffffffu) * scale;
+    uint32_t lb;
+    memcpy(&lb, &lf, sizeof lb);
+    const bool in = ax - (949u << 20) < (202u << 20);
+    const uint32_t out = ax < (949u << 20) ? 0u : (0x7fc00000u | sign);
+    const uint32_t rh = in ? (hb | sign) : out, rl = in ? (lb | sign) : out;
+    float2 r;
+    memcpy(&r.x, &rh, sizeof rh);
+    memcpy(&r.y, &rl, sizeof rl);
+    return r;
+}
 
 // Physics switches and constants (a flat copy of the fgpu_params subset the
 // kernels read, plus host-precomputed products).
@@ -77,6 +106,9 @@ struct Phys {
     double mu_gm1_over_R; // mu (gamma - 1) / R
     double emin_fac, emax_fac; // Tmin|Tmax / mu * R / (gamma - 1)
     float emin_fac_f, emax_fac_f;  // the same rounded to float (FP32 screens)
+    // constants of the float-pair kernels as pairs (split_pair_host)
+    float2 pk_gm1, pk_g_gm1, pk_alpha, pk_C2, pk_rvf, pk_hvf, pk_mu_gm1_over_R, pk_cool_const,
+        pk_emin_fac;
 };
 
 struct Bodies {
@@ -86,6 +118,7 @@ struct Bodies {
     float xh[kMaxBodies], xl[kMaxBodies], yh[kMaxBodies], yl[kMaxBodies];
     float gmh[kMaxBodies], gml[kMaxBodies];
     double ix, iy;        // indirect term
+    float2 pk_ix, pk_iy;  // the same as float pairs (split_pair_host)
     double omega_frame;
     // decided on the host, so that no kernel compares doubles per cell:
     // bit k set when body k has Klahr smoothing (rsm[k] > 0); the central

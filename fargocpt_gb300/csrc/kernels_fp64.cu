@@ -207,7 +207,8 @@ __global__ void k_potential(Geo g, Tables t, Phys ph, Bodies b, const double *__
             }
             f2_accumulate(ah, al, term);
         }
-        const f2 ind = f2_neg(f2_sadd(f2_smul(f2_split(b.ix), xc), f2_smul(f2_split(b.iy), yc)));
+        const f2 ind = f2_neg(f2_sadd(f2_smul(f2{b.pk_ix.x, b.pk_ix.y}, xc),
+                                      f2_smul(f2{b.pk_iy.x, b.pk_iy.y}, yc)));
         pot[CELL(i, j)] = acc + f2_to_double(f2_sadd(f2{ah, al}, ind));
         return;
     }
@@ -2258,7 +2259,7 @@ struct ForceBodies {
     float xh[kForceBodies], xl[kForceBodies], yh[kForceBodies], yl[kForceBodies];
 };
 
-__global__ void k_disk_force_bodies(Geo g, Tables t, Phys ph, ForceBodies fb,
+__global__ void __launch_bounds__(256, 4) k_disk_force_bodies(Geo g, Tables t, Phys ph, ForceBodies fb,
                                     const double *__restrict__ S, const double *__restrict__ H,
                                     double *__restrict__ partial, int width)
 {

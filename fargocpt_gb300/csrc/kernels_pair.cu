@@ -48,6 +48,8 @@ __device__ __forceinline__ f2 T(const Tables &t, const double *tab, int i)
     const float2 v = t.ptab[(tab - t.tbase) + i];
     return f2{v.x, v.y};
 }
+// a constant the host split (split_pair_host)
+__device__ __forceinline__ f2 K(float2 v) { return f2{v.x, v.y}; }
 // the FP64 difference of two stored values, as a pair
 __device__ __forceinline__ f2 D(double a, double b) { return f2_split(a - b); }
 // x s for a power of two s (exact)
@@ -104,7 +106,7 @@ __device__ __forceinline__ f2 f2_expm1_small(f2 x)
 
 // update_with_sourceterms (SourceEuler.cpp:369-450): the momentum updates
 // from the pressure gradient, the potential and the centrifugal term
-__global__ void k_source_p(Geo g, Tables t, double dt, double omega_frame,
+__global__ void k_source_p(Geo g, Tables t, float2 dtp, float2 omega_frame,
                            const double *__restrict__ S, const double *__restrict__ Pr,
                            const double *__restrict__ pot, const double *__restrict__ vr_in,
                            const double *__restrict__ vaz_in, double *__restrict__ vr_out,
@@ -114,7 +116,7 @@ __global__ void k_source_p(Geo g, Tables t, double dt, double omega_frame,
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.y;  // 0 .. nr
     if (j >= nz) return;
-    const f2 pdt = P(dt);
+    const f2 pdt = K(dtp);
     double vr = vr_in[CELL(i, j)];
     if (i >= 2 && i < nr - 1) {
         const size_t c = CELL(i, j), cm = CELL(i - 1, j);
@@ -124,7 +126,7 @@ __global__ void k_source_p(Geo g, Tables t, double dt, double omega_frame,
         const int jn = nxt(j, nz);
         const f2 vsum = (P(vaz_in[c]) + P(vaz_in[CELL(i, jn)])) +
                         (P(vaz_in[cm]) + P(vaz_in[CELL(i - 1, jn)]));
-        const f2 vt = sc(vsum, 0.25f) + T(t, t.Rinf, i) * P(omega_frame);
+        const f2 vt = sc(vsum, 0.25f) + T(t, t.Rinf, i) * K(omega_frame);
         const f2 centrifugal = vt * vt * T(t, t.InvRinf, i);
         vr = upd(vr, pdt * (centrifugal - (gradp + gradphi)));
     }
@@ -145,7 +147,7 @@ __global__ void k_source_p(Geo g, Tables t, double dt, double omega_frame,
 // compression heating (SourceEuler.cpp:1045-1092) and the artificial
 // pressures with their dissipation (artificial_viscosity.cpp:35-91,
 // 141-230), as k_artvisc_q
-__global__ void k_artvisc_q_p(Geo g, Tables t, Phys ph, double dt, const double *__restrict__ S,
+__global__ void k_artvisc_q_p(Geo g, Tables t, Phys ph, float2 dtp, const double *__restrict__ S,
                               const double *__restrict__ vr, const double *__restrict__ vaz,
                               double *__restrict__ E, double *__restrict__ Qr,
                               double *__restrict__ Qp)
@@ -156,10 +158,10 @@ __global__ void k_artvisc_q_p(Geo g, Tables t, Phys ph, double dt, const double 
     if (j >= nz) return;
     const int jn = nxt(j, nz);
     const size_t c = CELL(i, j);
-    const f2 pdt = P(dt);
+    const f2 pdt = K(dtp);
     const f2 vr0 = P(vr[c]), vr1 = P(vr[CELL(i + 1, j)]);
     const f2 va0 = P(vaz[c]), va1 = P(vaz[CELL(i, jn)]);
-    const f2 invdphi = P(g.invdphi);
+    const f2 invdphi = K(g.pk_invdphi);
     double e = 0.0;
     f2 de{0.f, 0.f};  // the energy's increment beyond the compression factor
     if (ph.adiabatic) {
@@ -168,7 +170,7 @@ __global__ void k_artvisc_q_p(Geo g, Tables t, Phys ph, double dt, const double 
             const f2 div_v = (vr1 * T(t, t.Rinf, i + 1) - vr0 * T(t, t.Rinf, i)) *
                                  T(t, t.InvDiffRsupRb, i) +
                              (va1 - va0) * invdphi * T(t, t.InvRmed, i);
-            const f2 x = -(P(ph.gm1) * pdt * div_v);
+            const f2 x = -(K(ph.pk_gm1) * pdt * div_v);
             if (fabsf(x.h) <= 0.015625f) {
                 de = P(e) * f2_expm1_small(x);
             } else {
@@ -178,7 +180,7 @@ __global__ void k_artvisc_q_p(Geo g, Tables t, Phys ph, double dt, const double 
     }
     if (ph.art_visc_sn) {
         const f2 sig = P(S[c]);
-        const f2 C2 = P(ph.C2);
+        const f2 C2 = K(ph.pk_C2);
         const f2 dv_r = vr1 - vr0;
         const f2 qr = negative(dv_r) ? C2 * sig * (dv_r * dv_r) : f2{0.f, 0.f};
         const f2 dv_p = va1 - va0;
@@ -218,7 +220,7 @@ __global__ void k_artvisc_q_p(Geo g, Tables t, Phys ph, double dt, const double 
 // 93-139, 232-290) and the derived c_s, H, nu of the ideal EOS
 // (compute_sound_speed_normal, compute_scale_height_old, update_viscosity),
 // as k_artvisc_v
-__global__ void k_artvisc_v_p(Geo g, Tables t, Phys ph, double dt, const double *__restrict__ S,
+__global__ void k_artvisc_v_p(Geo g, Tables t, Phys ph, float2 dtp, const double *__restrict__ S,
                               const double *__restrict__ E, const double *__restrict__ Qr,
                               const double *__restrict__ Qp, double *__restrict__ vr,
                               double *__restrict__ vaz, double *__restrict__ cs,
@@ -229,7 +231,7 @@ __global__ void k_artvisc_v_p(Geo g, Tables t, Phys ph, double dt, const double 
     const int i = blockIdx.y;  // 0 .. nr - 1
     if (j >= nz) return;
     const size_t c = CELL(i, j);
-    const f2 pdt = P(dt);
+    const f2 pdt = K(dtp);
     if (ph.art_visc_sn) {
         if (i >= 2 && i < nr - 1) {
             const size_t cm = CELL(i - 1, j);
@@ -253,15 +255,15 @@ __global__ void k_artvisc_v_p(Geo g, Tables t, Phys ph, double dt, const double 
             const f2 avg = sc(P(S[c]) + P(S[cm]), 0.5f);
             const f2 br = (P(Qr[c]) * T(t, t.Rmed, i) - P(Qr[cm]) * T(t, t.Rmed, i - 1)) -
                           sc(P(Qp[c]) + P(Qp[cm]), 0.5f) * T(t, t.DiffRmed, i);
-            vr[c] = upd(vr[c], P(ph.rvf) * (pdt / avg) * T(t, t.TwoOverDRmed2, i) * br);
+            vr[c] = upd(vr[c], K(ph.pk_rvf) * (pdt / avg) * T(t, t.TwoOverDRmed2, i) * br);
         }
     }
     if (ph.adiabatic) {
-        const f2 c_s = f2_sqrt(P(ph.g_gm1) * (P(E[c]) / P(S[c])));
+        const f2 c_s = f2_sqrt(K(ph.pk_g_gm1) * (P(E[c]) / P(S[c])));
         const f2 h = c_s * T(t, t.HFacAdi, i);
         cs[c] = f2_to_double(c_s);
         H[c] = f2_to_double(h);
-        nu[c] = ph.alpha > 0 ? f2_to_double(P(ph.alpha) * h * c_s) : ph.constant_viscosity;
+        nu[c] = ph.alpha > 0 ? f2_to_double(K(ph.pk_alpha) * h * c_s) : ph.constant_viscosity;
     }
 }
 
@@ -281,7 +283,7 @@ __global__ void k_stress_p(Geo g, Tables t, const double *__restrict__ S,
     const f2 vr0 = P(vr[c]), vr1 = P(vr[CELL(i + 1, j)]);
     const f2 va0 = P(vaz[c]), va1 = P(vaz[CELL(i, jn)]);
     const f2 n = P(nu[c]), sg = P(S[c]);
-    const f2 invdphi = P(g.invdphi);
+    const f2 invdphi = K(g.pk_invdphi);
     const f2 irm = T(t, t.InvRmed, i);
     const f2 third = P(1.0 / 3.0);
     const f2 dv = (vr1 * T(t, t.Rinf, i + 1) - vr0 * T(t, t.Rinf, i)) * T(t, t.InvDiffRsupRb, i) +
@@ -309,7 +311,7 @@ __global__ void k_stress_p(Geo g, Tables t, const double *__restrict__ S,
 // StabilizeViscosity, which the FP64 kernel serves) and SubStep3:
 // thermal relaxation (SourceEuler.cpp:632-690), viscous heating (:496-536),
 // the radiative alpha factor (:905-912) and the energy update, as k_viscous
-__global__ void k_viscous_p(Geo g, Tables t, Phys ph, double dt, double beta_inv, int mode,
+__global__ void k_viscous_p(Geo g, Tables t, Phys ph, float2 dtp, float2 beta_inv, int mode,
                             const double *__restrict__ S, const double *__restrict__ trr,
                             const double *__restrict__ tpp, const double *__restrict__ trp,
                             const double *__restrict__ divv, const double *__restrict__ nu,
@@ -324,8 +326,8 @@ __global__ void k_viscous_p(Geo g, Tables t, Phys ph, double dt, double beta_inv
     if (j >= nz) return;
     const size_t c = CELL(i, j);
     const int jp = prv(j, nz), jn = nxt(j, nz);
-    const f2 pdt = P(dt);
-    const f2 invdphi = P(g.invdphi);
+    const f2 pdt = K(dtp);
+    const f2 invdphi = K(g.pk_invdphi);
     if (mode & 1) {
         if (i >= 1 && i < nr - 1) {
             const f2 avg = sc(P(S[c]) + P(S[CELL(i, jp)]), 0.5f);
@@ -338,7 +340,7 @@ __global__ void k_viscous_p(Geo g, Tables t, Phys ph, double dt, double beta_inv
         if (i >= 2 && i < nr - 1) {
             const size_t cm = CELL(i - 1, j);
             const f2 avg = sc(P(S[c]) + P(S[cm]), 0.5f);
-            const f2 dVr = pdt / avg * P(ph.rvf) * T(t, t.TwoOverRmedSum, i) *
+            const f2 dVr = pdt / avg * K(ph.pk_rvf) * T(t, t.TwoOverRmedSum, i) *
                            ((T(t, t.Rmed, i) * P(trr[c]) - T(t, t.Rmed, i - 1) * P(trr[cm])) *
                                 T(t, t.InvDiffRmed, i) +
                             (P(trp[CELL(i, jn)]) - P(trp[c])) * invdphi -
@@ -361,9 +363,9 @@ __global__ void k_viscous_p(Geo g, Tables t, Phys ph, double dt, double beta_inv
             } else if (ph.beta_ref == 2) {
                 delta_E = delta_E - T(t, t.EModel, i) * sig;
             } else if (ph.beta_ref == 3) {
-                delta_E = delta_E - sig * P(ph.emin_fac);
+                delta_E = delta_E - sig * K(ph.pk_emin_fac);
             }
-            qm = delta_E * T(t, t.OmegaK, i) * P(beta_inv);
+            qm = delta_E * T(t, t.OmegaK, i) * K(beta_inv);
         }
         if (ph.heating_viscous) {
             const double nd = nu[c];
@@ -376,12 +378,12 @@ __global__ void k_viscous_p(Geo g, Tables t, Phys ph, double dt, double beta_inv
                 const f2 ns = n * sig;
                 f2 q = (t_rr * t_rr + sc(tau_r_phi * tau_r_phi, 2.0f) + t_pp * t_pp) / sc(ns, 2.0f);
                 q = q + P(2.0 / 9.0) * ns * (d * d);
-                qp = q * P(ph.hvf);
+                qp = q * K(ph.pk_hvf);
             }
         }
-        const f2 x = P(ph.mu_gm1_over_R) / sig;
+        const f2 x = K(ph.pk_mu_gm1_over_R) / sig;
         const f2 x2 = x * x;
-        const f2 alpha = P(1.0) + P(H[c]) * P(ph.cool_const) * (x2 * x2) * (ep * ep * ep);
+        const f2 alpha = P(1.0) + P(H[c]) * K(ph.pk_cool_const) * (x2 * x2) * (ep * ep * ep);
         const f2 inv_alpha = f2_rcp(alpha);
         qp = qp * inv_alpha;
         qm = qm * inv_alpha;
@@ -407,7 +409,7 @@ __global__ void k_viscous_p(Geo g, Tables t, Phys ph, double dt, double beta_inv
 // floor (SourceEuler.cpp:102-134) and the temperature floor, as k_finish,
 // with the azimuthal transport's AdvectSHIFT (:238-268): the transported
 // fields of ring i are read at j - shift[i]
-__global__ void k_finish_p(Geo g, Tables t, Phys ph, double omf, const double *__restrict__ mom0,
+__global__ void k_finish_p(Geo g, Tables t, Phys ph, float2 omf, const double *__restrict__ mom0,
                            const double *__restrict__ mom1, const double *__restrict__ mom2,
                            const double *__restrict__ mom3, const double *__restrict__ S_t,
                            const double *__restrict__ E_t, const double *__restrict__ vr_in,
@@ -442,7 +444,7 @@ __global__ void k_finish_p(Geo g, Tables t, Phys ph, double omf, const double *_
     const size_t cjm = at(i, prv(j, nz));
     vaz_out[c] = f2_to_double((P(mom2[cjm]) + P(mom3[cs])) / (P(S_t[cjm]) + sp) *
                                   T(t, t.InvRmed, i) -
-                              T(t, t.Rmed, i) * P(omf));
+                              T(t, t.Rmed, i) * K(omf));
     // s < sigma_min on the bit patterns (sigma_min >= 0; a NaN stays)
     const long long bs = __double_as_longlong(s);
     const bool nan = (bs & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
@@ -460,22 +462,23 @@ void launch_source_pair(const Launch &L, double dt, double omf, const double *S,
                         double *vr_out, double *vaz_out)
 {
     k_source_p<<<grid2(L.g.nz, L.g.nr + 1, L.bx), L.bx, 0, L.stream>>>(
-        L.g, L.t, dt, omf, S, Pr, pot, vr_in, vaz_in, vr_out, vaz_out);
+        L.g, L.t, split_pair_host(dt), split_pair_host(omf), S, Pr, pot, vr_in, vaz_in, vr_out,
+        vaz_out);
 }
 
 void launch_artvisc_q_pair(const Launch &L, double dt, const double *S, const double *vr,
                            const double *vaz, double *E, double *Qr, double *Qp)
 {
-    k_artvisc_q_p<<<grid2(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(L.g, L.t, L.ph, dt, S, vr,
-                                                                      vaz, E, Qr, Qp);
+    k_artvisc_q_p<<<grid2(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(
+        L.g, L.t, L.ph, split_pair_host(dt), S, vr, vaz, E, Qr, Qp);
 }
 
 void launch_artvisc_v_pair(const Launch &L, double dt, const double *S, const double *E,
                            const double *Qr, const double *Qp, double *vr, double *vaz, double *cs,
                            double *H, double *nu)
 {
-    k_artvisc_v_p<<<grid2(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(L.g, L.t, L.ph, dt, S, E, Qr,
-                                                                      Qp, vr, vaz, cs, H, nu);
+    k_artvisc_v_p<<<grid2(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(
+        L.g, L.t, L.ph, split_pair_host(dt), S, E, Qr, Qp, vr, vaz, cs, H, nu);
 }
 
 void launch_stress_pair(const Launch &L, const double *S, const double *vr, const double *vaz,
@@ -488,7 +491,8 @@ void launch_stress_pair(const Launch &L, const double *S, const double *vr, cons
 void launch_viscous_pair(const Launch &L, double dt, double beta_inv, int mode, const State &s)
 {
     k_viscous_p<<<grid2(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(
-        L.g, L.t, L.ph, dt, beta_inv, mode, s.sigma, s.trr, s.tpp, s.trp, s.divv, s.nu, s.H,
+        L.g, L.t, L.ph, split_pair_host(dt), split_pair_host(beta_inv), mode, s.sigma, s.trr,
+        s.tpp, s.trp, s.divv, s.nu, s.H,
         s.sigma0, s.energy0, s.vr, s.vaz, s.energy, s.qplus, s.qminus);
 }
 
@@ -497,7 +501,8 @@ void launch_finish_pair(const Launch &L, double omf, double *const mom[4], const
                         double *S_out, double *E_out, const int *ring_shift)
 {
     k_finish_p<<<grid2(L.g.nz, L.g.nr + 1, L.bx), L.bx, 0, L.stream>>>(
-        L.g, L.t, L.ph, omf, mom[0], mom[1], mom[2], mom[3], S_t, E_t, vr_in, vr_out, vaz_out,
+        L.g, L.t, L.ph, split_pair_host(omf), mom[0], mom[1], mom[2], mom[3], S_t, E_t, vr_in,
+        vr_out, vaz_out,
         S_out, E_out, ring_shift);
 }
 
