@@ -40,6 +40,9 @@ struct fgpu_engine {
     size_t az_smem = 0;
     int az_block = 256;
     bool pair_arith = true;  // the kernels' arithmetic in float pairs (else FP64)
+    // div v and the stress tensor hold the stress kernel's float pairs
+    // (stress_as_pairs) until join_stress_pairs turns them into doubles
+    bool stress_pairs = false;
     int radial_chunk = 16;
 
     double *tables_mem = nullptr;
@@ -148,6 +151,28 @@ static bool is_vector_field(int f)
 }
 
 static int field_rows(const fgpu_engine *e, int f) { return is_vector_field(f) ? e->nr + 1 : e->nr; }
+
+static bool is_stress_field(int f)
+{
+    return f == FGPU_DIV_V || f == FGPU_TAU_R_R || f == FGPU_TAU_PHI_PHI || f == FGPU_TAU_R_PHI;
+}
+
+// div v and the stress tensor as doubles again where the last stress
+// evaluation left float pairs, before anything outside the step reads or
+// overwrites them: the rows that evaluation wrote (every ring of div v,
+// tau_rr, tau_phiphi; rings 1 .. nr - 1 of tau_rphi)
+static int join_stress_pairs(fgpu_engine *eng)
+{
+    if (!eng->stress_pairs) return FGPU_OK;
+    const size_t nz = eng->nz, rows = eng->nr;
+    launch_join_pairs(eng->stream, eng->field[FGPU_DIV_V], rows * nz);
+    launch_join_pairs(eng->stream, eng->field[FGPU_TAU_R_R], rows * nz);
+    launch_join_pairs(eng->stream, eng->field[FGPU_TAU_PHI_PHI], rows * nz);
+    launch_join_pairs(eng->stream, eng->field[FGPU_TAU_R_PHI] + nz, (rows - 1) * nz);
+    eng->stress_pairs = false;
+    CK(cudaGetLastError());
+    return FGPU_OK;
+}
 
 extern "C" int fgpu_grid_radii(int spacing, double rmin, double rmax, int nrad, double *radii)
 {
@@ -1118,6 +1143,10 @@ extern "C" int fgpu_upload_field(fgpu_engine *eng, int field, const double *host
         if (rc) eng->err = eng->e32->err;
         return rc;
     }
+    if (is_stress_field(field)) {
+        const int rc = join_stress_pairs(eng);
+        if (rc) return rc;
+    }
     CK(cudaMemcpyAsync(eng->field[field], host, sizeof(double) * (size_t)rows * cols,
                        cudaMemcpyHostToDevice, eng->stream));
     CK(cudaStreamSynchronize(eng->stream));
@@ -1136,6 +1165,10 @@ extern "C" int fgpu_download_field(fgpu_engine *eng, int field, double *host, in
         int rc = eng->e32->download(field, host, rows);
         if (rc) eng->err = eng->e32->err;
         return rc;
+    }
+    if (is_stress_field(field)) {
+        const int rc = join_stress_pairs(eng);
+        if (rc) return rc;
     }
     CK(cudaMemcpyAsync(host, eng->field[field], sizeof(double) * (size_t)rows * cols,
                        cudaMemcpyDeviceToHost, eng->stream));
@@ -1196,6 +1229,13 @@ extern "C" int fgpu_snapshot_begin(fgpu_engine *eng, int n, const int *fields,
             return FGPU_ERR_OOM;
         }
         eng->snap_capacity = need;
+    }
+    for (int k = 0; k < n && !eng->e32; ++k) {
+        if (is_stress_field(fields[k])) {
+            rc = join_stress_pairs(eng);
+            if (rc) return rc;
+            break;
+        }
     }
     // the staging copies are ordered with the steps on the engine's stream
     for (int k = 0; k < n; ++k) {
@@ -1296,6 +1336,7 @@ extern "C" int fgpu_init_euler(fgpu_engine *eng, double t)
     if (eng->ph.adiabatic) {
         // compute_heating_cooling_for_CFL, SourceEuler.cpp:1410-1450
         launch_stress(L, s.sigma, s.vr, s.vaz, s.nu, s.divv, s.trr, s.tpp, s.trp);
+        eng->stress_pairs = stress_as_pairs(L);
         if (eng->ph.stabilize) launch_visc_corr(L, s);
         launch_viscous(L, 0.0, beta_inv_at(eng->p, t), 2, s);
     }
@@ -1579,6 +1620,7 @@ static void gas_kick(fgpu_engine *eng, double dt, double t)
     }
     // viscous stress and velocity update, SubStep3 (simulation.cpp:196-203)
     launch_stress(L, s.sigma, s.vr, s.vaz, s.nu, s.divv, s.trr, s.tpp, s.trp);
+    eng->stress_pairs = stress_as_pairs(L);
     if (eng->ph.stabilize) launch_visc_corr(L, s);
     mark(eng, 4);
     launch_viscous(L, dt, beta_inv_at(eng->p, t), adi ? 7 : 1, s);

@@ -72,6 +72,14 @@ void launch_artvisc_v_pair(const Launch &L, double dt, const double *S, const do
 void launch_stress_pair(const Launch &L, const double *S, const double *vr, const double *vaz,
                         const double *nu, double *divv, double *trr, double *tpp, double *trp);
 void launch_viscous_pair(const Launch &L, double dt, double beta_inv, int mode, const State &s);
+// Whether the stress kernel leaves div v and the stress tensor as float pairs
+// (hi, lo in the 8 bytes of each double) for the float-pair viscous kernel,
+// which reads them so, instead of joined doubles; StabilizeViscosity 1's
+// viscous update is the FP64 kernel's, which reads doubles.
+inline bool stress_as_pairs(const Launch &L) { return L.pair && L.ph.stabilize != 1; }
+// the pairs of n cells joined into doubles in place (div v and the stress
+// tensor before they are read as doubles)
+void launch_join_pairs(cudaStream_t stream, double *x, size_t n);
 void launch_finish_pair(const Launch &L, double omf, double *const mom[4], const double *S_t,
                         const double *E_t, const double *vr_in, double *vr_out, double *vaz_out,
                         double *S_out, double *E_out, const int *ring_shift);

@@ -26,6 +26,8 @@
 
 #include <math.h>
 
+#include <algorithm>
+
 namespace fgpu {
 namespace {
 
@@ -160,7 +162,8 @@ __global__ void k_artvisc_q_p(Geo g, Tables t, Phys ph, float2 dtp, const double
     const size_t c = CELL(i, j);
     const f2 pdt = K(dtp);
     const f2 vr0 = P(vr[c]), vr1 = P(vr[CELL(i + 1, j)]);
-    const f2 va0 = P(vaz[c]), va1 = P(vaz[CELL(i, jn)]);
+    // the FP64 difference of neighbouring v_phi (they cancel to many digits)
+    const f2 dva = D(vaz[CELL(i, jn)], vaz[c]);
     const f2 invdphi = K(g.pk_invdphi);
     double e = 0.0;
     f2 de{0.f, 0.f};  // the energy's increment beyond the compression factor
@@ -169,7 +172,7 @@ __global__ void k_artvisc_q_p(Geo g, Tables t, Phys ph, float2 dtp, const double
         if (i < nr - 1) {
             const f2 div_v = (vr1 * T(t, t.Rinf, i + 1) - vr0 * T(t, t.Rinf, i)) *
                                  T(t, t.InvDiffRsupRb, i) +
-                             (va1 - va0) * invdphi * T(t, t.InvRmed, i);
+                             dva * invdphi * T(t, t.InvRmed, i);
             const f2 x = -(K(ph.pk_gm1) * pdt * div_v);
             if (fabsf(x.h) <= 0.015625f) {
                 de = P(e) * f2_expm1_small(x);
@@ -183,7 +186,7 @@ __global__ void k_artvisc_q_p(Geo g, Tables t, Phys ph, float2 dtp, const double
         const f2 C2 = K(ph.pk_C2);
         const f2 dv_r = vr1 - vr0;
         const f2 qr = negative(dv_r) ? C2 * sig * (dv_r * dv_r) : f2{0.f, 0.f};
-        const f2 dv_p = va1 - va0;
+        const f2 dv_p = dva;
         const f2 qp = negative(dv_p) ? C2 * sig * (dv_p * dv_p) : f2{0.f, 0.f};
         Qr[c] = f2_to_double(qr);
         Qp[c] = f2_to_double(qp);
@@ -195,7 +198,7 @@ __global__ void k_artvisc_q_p(Geo g, Tables t, Phys ph, float2 dtp, const double
         // update_with_artificial_viscosity_TW, artificial_viscosity.cpp:52-91
         const f2 sig = P(S[c]);
         const f2 eps_rr = (vr1 - vr0) * T(t, t.InvDiffRsup, i);
-        const f2 eps_pp = T(t, t.InvRmed, i) * ((va1 - va0) * invdphi + sc(vr1 + vr0, 0.5f));
+        const f2 eps_pp = T(t, t.InvRmed, i) * (dva * invdphi + sc(vr1 + vr0, 0.5f));
         const f2 sum = eps_rr + eps_pp;
         const f2 div_V = negative(sum) ? sum : f2{0.f, 0.f};
         const f2 third = P(1.0 / 3.0);
@@ -267,7 +270,21 @@ __global__ void k_artvisc_v_p(Geo g, Tables t, Phys ph, float2 dtp, const double
     }
 }
 
+// div v and the stress tensor as the viscous kernel reads them: the pair
+// itself in the double's 8 bytes (PT), else the joined double
+template <bool PT>
+__device__ __forceinline__ void put_t(double *x, size_t c, f2 v)
+{
+    if (PT) reinterpret_cast<f2 *>(x)[c] = v;
+    else x[c] = f2_to_double(v);
+}
+__device__ __forceinline__ f2 get_t(const double *x, size_t c)
+{
+    return reinterpret_cast<const f2 *>(x)[c];
+}
+
 // the viscous stress tensor (viscosity.cpp:60-247), as k_stress
+template <bool PT>
 __global__ void k_stress_p(Geo g, Tables t, const double *__restrict__ S,
                            const double *__restrict__ vr, const double *__restrict__ vaz,
                            const double *__restrict__ nu, double *__restrict__ divv,
@@ -281,29 +298,32 @@ __global__ void k_stress_p(Geo g, Tables t, const double *__restrict__ S,
     const size_t c = CELL(i, j);
     const int jn = nxt(j, nz);
     const f2 vr0 = P(vr[c]), vr1 = P(vr[CELL(i + 1, j)]);
-    const f2 va0 = P(vaz[c]), va1 = P(vaz[CELL(i, jn)]);
+    const double va0d = vaz[c];
+    // v_phi of neighbouring cells of a ring agree to many digits (the orbital
+    // speed cancels): their FP64 difference, exact as in the reference
+    const f2 dva = D(vaz[CELL(i, jn)], va0d);
     const f2 n = P(nu[c]), sg = P(S[c]);
     const f2 invdphi = K(g.pk_invdphi);
     const f2 irm = T(t, t.InvRmed, i);
     const f2 third = P(1.0 / 3.0);
     const f2 dv = (vr1 * T(t, t.Rinf, i + 1) - vr0 * T(t, t.Rinf, i)) * T(t, t.InvDiffRsupRb, i) +
-                  (va1 - va0) * invdphi * irm;
-    divv[c] = f2_to_double(dv);
+                  dva * invdphi * irm;
+    put_t<PT>(divv, c, dv);
     const f2 two_n_sg = sc(n * sg, 2.0f);
     const f2 drr = (vr1 - vr0) * T(t, t.InvDiffRsup, i);
-    trr[c] = f2_to_double(two_n_sg * (drr - third * dv));
-    const f2 dpp = (va1 - va0) * invdphi * irm + sc(vr1 + vr0, 0.5f) * irm;
-    tpp[c] = f2_to_double(two_n_sg * (dpp - third * dv));
+    put_t<PT>(trr, c, two_n_sg * (drr - third * dv));
+    const f2 dpp = dva * invdphi * irm + sc(vr1 + vr0, 0.5f) * irm;
+    put_t<PT>(tpp, c, two_n_sg * (dpp - third * dv));
     if (i >= 1) {
         const int jp = prv(j, nz);
         const size_t cm = CELL(i - 1, j), cp = CELL(i, jp), cmp = CELL(i - 1, jp);
-        const f2 dvazirdr = (va0 * irm - P(vaz[cm]) * T(t, t.InvRmed, i - 1)) *
+        const f2 dvazirdr = (P(va0d) * irm - P(vaz[cm]) * T(t, t.InvRmed, i - 1)) *
                             T(t, t.InvDiffRmed, i);
         const f2 dvrdphi = (vr0 - P(vr[cp])) * invdphi;
         const f2 drp = T(t, t.Rinf, i) * dvazirdr + dvrdphi * T(t, t.InvRinf, i);
         const f2 n4 = sc((n + P(nu[cm])) + (P(nu[cp]) + P(nu[cmp])), 0.25f);
         const f2 s4 = sc((sg + P(S[cm])) + (P(S[cp]) + P(S[cmp])), 0.25f);
-        trp[c] = f2_to_double(n4 * s4 * drp);
+        put_t<PT>(trp, c, n4 * s4 * drp);
     }
 }
 
@@ -332,19 +352,19 @@ __global__ void k_viscous_p(Geo g, Tables t, Phys ph, float2 dtp, float2 beta_in
         if (i >= 1 && i < nr - 1) {
             const f2 avg = sc(P(S[c]) + P(S[CELL(i, jp)]), 0.5f);
             const f2 dVp = pdt * T(t, t.InvRmed, i) / avg *
-                           (T(t, t.TwoOverDRa2, i) * (T(t, t.RinfSq, i + 1) * P(trp[CELL(i + 1, j)]) -
-                                                      T(t, t.RinfSq, i) * P(trp[c])) +
-                            (P(tpp[c]) - P(tpp[CELL(i, jp)])) * invdphi);
+                           (T(t, t.TwoOverDRa2, i) * (T(t, t.RinfSq, i + 1) * get_t(trp, CELL(i + 1, j)) -
+                                                      T(t, t.RinfSq, i) * get_t(trp, c)) +
+                            (get_t(tpp, c) - get_t(tpp, CELL(i, jp))) * invdphi);
             vaz[c] = upd(vaz[c], dVp);
         }
         if (i >= 2 && i < nr - 1) {
             const size_t cm = CELL(i - 1, j);
             const f2 avg = sc(P(S[c]) + P(S[cm]), 0.5f);
             const f2 dVr = pdt / avg * K(ph.pk_rvf) * T(t, t.TwoOverRmedSum, i) *
-                           ((T(t, t.Rmed, i) * P(trr[c]) - T(t, t.Rmed, i - 1) * P(trr[cm])) *
+                           ((T(t, t.Rmed, i) * get_t(trr, c) - T(t, t.Rmed, i - 1) * get_t(trr, cm)) *
                                 T(t, t.InvDiffRmed, i) +
-                            (P(trp[CELL(i, jn)]) - P(trp[c])) * invdphi -
-                            sc(P(tpp[c]) + P(tpp[cm]), 0.5f));
+                            (get_t(trp, CELL(i, jn)) - get_t(trp, c)) * invdphi -
+                            sc(get_t(tpp, c) + get_t(tpp, cm), 0.5f));
             vr[c] = upd(vr[c], dVr);
         }
     }
@@ -371,10 +391,10 @@ __global__ void k_viscous_p(Geo g, Tables t, Phys ph, float2 dtp, float2 beta_in
             const double nd = nu[c];
             if (nd != 0.0) {
                 const f2 n = P(nd);
-                const f2 tau_r_phi = sc((P(trp[c]) + P(trp[CELL(i + 1, j)])) +
-                                            (P(trp[CELL(i, jn)]) + P(trp[CELL(i + 1, jn)])),
+                const f2 tau_r_phi = sc((get_t(trp, c) + get_t(trp, CELL(i + 1, j))) +
+                                            (get_t(trp, CELL(i, jn)) + get_t(trp, CELL(i + 1, jn))),
                                         0.25f);
-                const f2 t_rr = P(trr[c]), t_pp = P(tpp[c]), d = P(divv[c]);
+                const f2 t_rr = get_t(trr, c), t_pp = get_t(tpp, c), d = get_t(divv, c);
                 const f2 ns = n * sig;
                 f2 q = (t_rr * t_rr + sc(tau_r_phi * tau_r_phi, 2.0f) + t_pp * t_pp) / sc(ns, 2.0f);
                 q = q + P(2.0 / 9.0) * ns * (d * d);
@@ -453,6 +473,13 @@ __global__ void k_finish_p(Geo g, Tables t, Phys ph, float2 omf, const double *_
     if (ph.adiabatic) E_out[c] = floor_e(E_t[cs], sf, ph);
 }
 
+__global__ void k_join_pairs(double *__restrict__ x, size_t n)
+{
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+         k += (size_t)gridDim.x * blockDim.x)
+        x[k] = f2_to_double(reinterpret_cast<const f2 *>(x)[k]);
+}
+
 dim3 grid2(int nz, int rows, int bx) { return dim3((nz + bx - 1) / bx, rows); }
 
 }  // namespace
@@ -484,8 +511,15 @@ void launch_artvisc_v_pair(const Launch &L, double dt, const double *S, const do
 void launch_stress_pair(const Launch &L, const double *S, const double *vr, const double *vaz,
                         const double *nu, double *divv, double *trr, double *tpp, double *trp)
 {
-    k_stress_p<<<grid2(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(L.g, L.t, S, vr, vaz, nu, divv,
-                                                                   trr, tpp, trp);
+    auto k = stress_as_pairs(L) ? k_stress_p<true> : k_stress_p<false>;
+    k<<<grid2(L.g.nz, L.g.nr, L.bx), L.bx, 0, L.stream>>>(L.g, L.t, S, vr, vaz, nu, divv, trr, tpp,
+                                                          trp);
+}
+
+void launch_join_pairs(cudaStream_t stream, double *x, size_t n)
+{
+    const unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, 8192);
+    k_join_pairs<<<blocks, 256, 0, stream>>>(x, n);
 }
 
 void launch_viscous_pair(const Launch &L, double dt, double beta_inv, int mode, const State &s)

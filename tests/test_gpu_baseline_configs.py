@@ -95,3 +95,77 @@ def test_transport_arithmetic_request_is_checked(monkeypatch, capfd):
     with pytest.raises(EngineError, match="BAD_ARG"):
         Engine(params, radii)
     assert "FARGO_GB300_FP64_ARITH=fp128" in capfd.readouterr().err
+
+
+STRESS = ("DIV_V", "TAU_R_R", "TAU_PHI_PHI", "TAU_R_PHI")
+
+
+def _perturbed(cls, seed=7):
+    """The 512 x 1536 adiabatic disk with seeded relative noise of 1e-3 on
+    v_phi and noise of 1e-3 of the orbital speed on v_r, so that div v and
+    the stress tensor are of the velocities' own order (in the smooth initial
+    disk they vanish or nearly so), after init_euler's stress evaluation."""
+    from fargocpt_gb300 import setups
+
+    params, d, radii, fields, nbody = setups.build("c2")
+    rng = np.random.default_rng(seed)
+    f = dict(fields)
+    vaz = f["V_AZIMUTHAL"]
+    f["V_AZIMUTHAL"] = vaz * (1.0 + 1e-3 * rng.standard_normal(vaz.shape))
+    f["V_RADIAL"] = f["V_RADIAL"] + 1e-3 * float(np.max(np.abs(vaz))) * \
+        rng.standard_normal(f["V_RADIAL"].shape)
+    h = cls(params, radii)
+    for k, a in f.items():
+        h.set_field(k, a)
+        h.set_field(k + "0", a)
+    b = nbody.bodies(0.0)
+    h.set_bodies(b, *nbody.indirect(b), 0.0)
+    h.init_euler(0.0)
+    return h
+
+
+def _stress_err(got, ref, f, nr):
+    # rows a stress evaluation writes (tau_r_phi: rings 1 .. nr - 1)
+    rows = slice(1, nr) if f == "TAU_R_PHI" else slice(0, nr)
+    scale = float(np.max(np.abs(ref[rows])))
+    assert scale > 0.0, f
+    return float(np.max(np.abs(got[rows] - ref[rows]))) / scale
+
+
+@pytest.mark.parametrize("arith", ["pair", "fp64"])
+def test_stress_fields_read_back_as_doubles(arith, monkeypatch):
+    """div v and the viscous stress tensor, which the float-pair kernels pass
+    between them as pairs, read back as the oracle's doubles through
+    fgpu_download_field and fgpu_snapshot_begin; after a step, an upload of
+    one of them (before anything read them) leaves the others as the step
+    left them.  Relative L-infinity bars: 1e-11 on the same state, 1e-9
+    after one step of both."""
+    from fargocpt_gb300.engine import Engine
+    from fargocpt_gb300.output import Snapshotter
+    from oracle.oracle_py import OracleState, set_threads
+
+    monkeypatch.setenv("FARGO_GB300_FP64_ARITH", arith)
+    set_threads(os.cpu_count() or 1)
+    o = _perturbed(OracleState)
+    g = _perturbed(Engine)
+    snap = Snapshotter(g, fields=STRESS + ("SIGMA",))
+    try:
+        snap.begin()
+        staged = {f: a.copy() for f, a in snap.wait().items()}
+    finally:
+        snap.close()
+    for f in STRESS:
+        got = g.get_field(f)
+        err = _stress_err(got, o.get_field(f), f, g.nr)
+        assert err <= 1e-11, f"{f}: rel Linf {err:.3e}"
+        assert np.array_equal(staged[f], got), f
+    dt = g.condition_cfl()
+    o.condition_cfl()
+    g.step_euler(dt, 0.0)
+    o.step_euler(dt, 0.0)
+    mark = np.full((g.nr, g.nz), 0.25)
+    g.set_field("TAU_R_R", mark)
+    assert np.array_equal(g.get_field("TAU_R_R"), mark)
+    for f in ("DIV_V", "TAU_PHI_PHI", "TAU_R_PHI"):
+        err = _stress_err(g.get_field(f), o.get_field(f), f, g.nr)
+        assert err <= 1e-9, f"{f} after a step and an upload of TAU_R_R: {err:.3e}"
