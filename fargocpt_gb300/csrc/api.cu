@@ -41,8 +41,9 @@ struct fgpu_engine {
     int az_block = 256;
     bool pair_arith = true;  // the kernels' arithmetic in float pairs (else FP64)
     // div v and the stress tensor hold the stress kernel's float pairs
-    // (stress_as_pairs) until join_stress_pairs turns them into doubles
-    bool stress_pairs = false;
+    // (stress_as_pairs), the artificial pressures those of the float-pair
+    // artificial viscosity, until join_pair_fields turns them into doubles
+    bool stress_pairs = false, q_pairs = false;
     int radial_chunk = 16;
 
     double *tables_mem = nullptr;
@@ -152,24 +153,31 @@ static bool is_vector_field(int f)
 
 static int field_rows(const fgpu_engine *e, int f) { return is_vector_field(f) ? e->nr + 1 : e->nr; }
 
-static bool is_stress_field(int f)
+static bool is_pair_field(int f)
 {
-    return f == FGPU_DIV_V || f == FGPU_TAU_R_R || f == FGPU_TAU_PHI_PHI || f == FGPU_TAU_R_PHI;
+    return f == FGPU_DIV_V || f == FGPU_TAU_R_R || f == FGPU_TAU_PHI_PHI || f == FGPU_TAU_R_PHI ||
+           f == FGPU_Q_R || f == FGPU_Q_PHI;
 }
 
-// div v and the stress tensor as doubles again where the last stress
-// evaluation left float pairs, before anything outside the step reads or
-// overwrites them: the rows that evaluation wrote (every ring of div v,
-// tau_rr, tau_phiphi; rings 1 .. nr - 1 of tau_rphi)
-static int join_stress_pairs(fgpu_engine *eng)
+// The fields the float-pair kernels pass on as pairs, as doubles again
+// before anything outside the step reads or overwrites them: the rows the
+// last evaluation wrote (every ring of div v, tau_rr, tau_phiphi and the
+// artificial pressures; rings 1 .. nr - 1 of tau_rphi)
+static int join_pair_fields(fgpu_engine *eng)
 {
-    if (!eng->stress_pairs) return FGPU_OK;
     const size_t nz = eng->nz, rows = eng->nr;
-    launch_join_pairs(eng->stream, eng->field[FGPU_DIV_V], rows * nz);
-    launch_join_pairs(eng->stream, eng->field[FGPU_TAU_R_R], rows * nz);
-    launch_join_pairs(eng->stream, eng->field[FGPU_TAU_PHI_PHI], rows * nz);
-    launch_join_pairs(eng->stream, eng->field[FGPU_TAU_R_PHI] + nz, (rows - 1) * nz);
-    eng->stress_pairs = false;
+    if (eng->stress_pairs) {
+        launch_join_pairs(eng->stream, eng->field[FGPU_DIV_V], rows * nz);
+        launch_join_pairs(eng->stream, eng->field[FGPU_TAU_R_R], rows * nz);
+        launch_join_pairs(eng->stream, eng->field[FGPU_TAU_PHI_PHI], rows * nz);
+        launch_join_pairs(eng->stream, eng->field[FGPU_TAU_R_PHI] + nz, (rows - 1) * nz);
+        eng->stress_pairs = false;
+    }
+    if (eng->q_pairs) {
+        launch_join_pairs(eng->stream, eng->field[FGPU_Q_R], rows * nz);
+        launch_join_pairs(eng->stream, eng->field[FGPU_Q_PHI], rows * nz);
+        eng->q_pairs = false;
+    }
     CK(cudaGetLastError());
     return FGPU_OK;
 }
@@ -1143,8 +1151,8 @@ extern "C" int fgpu_upload_field(fgpu_engine *eng, int field, const double *host
         if (rc) eng->err = eng->e32->err;
         return rc;
     }
-    if (is_stress_field(field)) {
-        const int rc = join_stress_pairs(eng);
+    if (is_pair_field(field)) {
+        const int rc = join_pair_fields(eng);
         if (rc) return rc;
     }
     CK(cudaMemcpyAsync(eng->field[field], host, sizeof(double) * (size_t)rows * cols,
@@ -1166,8 +1174,8 @@ extern "C" int fgpu_download_field(fgpu_engine *eng, int field, double *host, in
         if (rc) eng->err = eng->e32->err;
         return rc;
     }
-    if (is_stress_field(field)) {
-        const int rc = join_stress_pairs(eng);
+    if (is_pair_field(field)) {
+        const int rc = join_pair_fields(eng);
         if (rc) return rc;
     }
     CK(cudaMemcpyAsync(host, eng->field[field], sizeof(double) * (size_t)rows * cols,
@@ -1231,8 +1239,8 @@ extern "C" int fgpu_snapshot_begin(fgpu_engine *eng, int n, const int *fields,
         eng->snap_capacity = need;
     }
     for (int k = 0; k < n && !eng->e32; ++k) {
-        if (is_stress_field(fields[k])) {
-            rc = join_stress_pairs(eng);
+        if (is_pair_field(fields[k])) {
+            rc = join_pair_fields(eng);
             if (rc) return rc;
             break;
         }
@@ -1611,6 +1619,7 @@ static void gas_kick(fgpu_engine *eng, double dt, double t)
     // compression heating + artificial viscosity (simulation.cpp:190-194)
     if (adi || eng->ph.art_visc_sn || eng->ph.art_visc_tw) {
         launch_artvisc_q(L, dt, s.sigma, s.vr, s.vaz, s.energy, s.qr, s.qphi);
+        if (L.pair && (eng->ph.art_visc_sn || eng->ph.art_visc_tw)) eng->q_pairs = true;
         mark(eng, 2);
         launch_artvisc_v(L, dt, s.sigma, s.energy, s.qr, s.qphi, s.vr, s.vaz, s.cs, s.H, s.nu);
         mark(eng, 3);

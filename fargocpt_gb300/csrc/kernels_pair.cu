@@ -146,6 +146,20 @@ __global__ void k_source_p(Geo g, Tables t, float2 dtp, float2 omega_frame,
     }
 }
 
+// Fields one float-pair kernel leaves for the next (the artificial
+// pressures, div v and the stress tensor): the pair itself in the double's
+// 8 bytes (PT), else the joined double
+template <bool PT>
+__device__ __forceinline__ void put_t(double *x, size_t c, f2 v)
+{
+    if (PT) reinterpret_cast<f2 *>(x)[c] = v;
+    else x[c] = f2_to_double(v);
+}
+__device__ __forceinline__ f2 get_t(const double *x, size_t c)
+{
+    return reinterpret_cast<const f2 *>(x)[c];
+}
+
 // compression heating (SourceEuler.cpp:1045-1092) and the artificial
 // pressures with their dissipation (artificial_viscosity.cpp:35-91,
 // 141-230), as k_artvisc_q
@@ -188,8 +202,8 @@ __global__ void k_artvisc_q_p(Geo g, Tables t, Phys ph, float2 dtp, const double
         const f2 qr = negative(dv_r) ? C2 * sig * (dv_r * dv_r) : f2{0.f, 0.f};
         const f2 dv_p = dva;
         const f2 qp = negative(dv_p) ? C2 * sig * (dv_p * dv_p) : f2{0.f, 0.f};
-        Qr[c] = f2_to_double(qr);
-        Qp[c] = f2_to_double(qp);
+        put_t<true>(Qr, c, qr);
+        put_t<true>(Qp, c, qp);
         if (ph.adiabatic && ph.dissipation && i >= 1 && i < nr - 1) {
             de = de - pdt * (qr * dv_r * T(t, t.InvDiffRsup, i) + qp * dv_p * T(t, t.InvDxTheta, i));
         }
@@ -203,8 +217,8 @@ __global__ void k_artvisc_q_p(Geo g, Tables t, Phys ph, float2 dtp, const double
         const f2 div_V = negative(sum) ? sum : f2{0.f, 0.f};
         const f2 third = P(1.0 / 3.0);
         const f2 lsig = T(t, t.LSqTW, i) * sig;
-        Qr[c] = f2_to_double(-(lsig * div_V) * (eps_rr - third * div_V));
-        Qp[c] = f2_to_double(-(lsig * div_V) * (eps_pp - third * div_V));
+        put_t<true>(Qr, c, -(lsig * div_V) * (eps_rr - third * div_V));
+        put_t<true>(Qp, c, -(lsig * div_V) * (eps_pp - third * div_V));
         if (ph.adiabatic && ph.dissipation && i >= 1 && i < nr - 1) {
             const f2 d = eps_rr - eps_pp;
             const f2 qplus = -(T(t, t.LSqTW, i) * div_V * sig * third) *
@@ -239,25 +253,25 @@ __global__ void k_artvisc_v_p(Geo g, Tables t, Phys ph, float2 dtp, const double
         if (i >= 2 && i < nr - 1) {
             const size_t cm = CELL(i - 1, j);
             const f2 a = sc(pdt, 2.0f) / (P(S[c]) + P(S[cm]));
-            vr[c] = upd(vr[c], -(a * (P(Qr[c]) - P(Qr[cm])) * T(t, t.InvDiffRmed, i)));
+            vr[c] = upd(vr[c], -(a * (get_t(Qr, c) - get_t(Qr, cm)) * T(t, t.InvDiffRmed, i)));
         }
         if (i >= 1 && i < nr - 1) {
             const size_t cp = CELL(i, prv(j, nz));
             const f2 a = sc(pdt, 2.0f) / (P(S[c]) + P(S[cp]));
-            vaz[c] = upd(vaz[c], -(a * (P(Qp[c]) - P(Qp[cp])) * T(t, t.InvDxTheta, i)));
+            vaz[c] = upd(vaz[c], -(a * (get_t(Qp, c) - get_t(Qp, cp)) * T(t, t.InvDxTheta, i)));
         }
     }
     if (ph.art_visc_tw) {
         if (i >= 1 && i < nr - 1) {
             const size_t cp = CELL(i, prv(j, nz));
             const f2 avg = sc(P(S[c]) + P(S[cp]), 0.5f);
-            vaz[c] = upd(vaz[c], pdt / avg * T(t, t.InvDxSrc, i) * (P(Qp[c]) - P(Qp[cp])));
+            vaz[c] = upd(vaz[c], pdt / avg * T(t, t.InvDxSrc, i) * (get_t(Qp, c) - get_t(Qp, cp)));
         }
         if (i >= 2 && i < nr - 1) {
             const size_t cm = CELL(i - 1, j);
             const f2 avg = sc(P(S[c]) + P(S[cm]), 0.5f);
-            const f2 br = (P(Qr[c]) * T(t, t.Rmed, i) - P(Qr[cm]) * T(t, t.Rmed, i - 1)) -
-                          sc(P(Qp[c]) + P(Qp[cm]), 0.5f) * T(t, t.DiffRmed, i);
+            const f2 br = (get_t(Qr, c) * T(t, t.Rmed, i) - get_t(Qr, cm) * T(t, t.Rmed, i - 1)) -
+                          sc(get_t(Qp, c) + get_t(Qp, cm), 0.5f) * T(t, t.DiffRmed, i);
             vr[c] = upd(vr[c], K(ph.pk_rvf) * (pdt / avg) * T(t, t.TwoOverDRmed2, i) * br);
         }
     }
@@ -268,19 +282,6 @@ __global__ void k_artvisc_v_p(Geo g, Tables t, Phys ph, float2 dtp, const double
         H[c] = f2_to_double(h);
         nu[c] = ph.alpha > 0 ? f2_to_double(K(ph.pk_alpha) * h * c_s) : ph.constant_viscosity;
     }
-}
-
-// div v and the stress tensor as the viscous kernel reads them: the pair
-// itself in the double's 8 bytes (PT), else the joined double
-template <bool PT>
-__device__ __forceinline__ void put_t(double *x, size_t c, f2 v)
-{
-    if (PT) reinterpret_cast<f2 *>(x)[c] = v;
-    else x[c] = f2_to_double(v);
-}
-__device__ __forceinline__ f2 get_t(const double *x, size_t c)
-{
-    return reinterpret_cast<const f2 *>(x)[c];
 }
 
 // the viscous stress tensor (viscosity.cpp:60-247), as k_stress

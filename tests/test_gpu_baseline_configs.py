@@ -134,12 +134,12 @@ def _stress_err(got, ref, f, nr):
 
 @pytest.mark.parametrize("arith", ["pair", "fp64"])
 def test_stress_fields_read_back_as_doubles(arith, monkeypatch):
-    """div v and the viscous stress tensor, which the float-pair kernels pass
-    between them as pairs, read back as the oracle's doubles through
-    fgpu_download_field and fgpu_snapshot_begin; after a step, an upload of
-    one of them (before anything read them) leaves the others as the step
-    left them.  Relative L-infinity bars: 1e-11 on the same state, 1e-9
-    after one step of both."""
+    """div v, the viscous stress tensor and the artificial pressures, which
+    the float-pair kernels pass between them as pairs, read back as the
+    oracle's doubles through fgpu_download_field and fgpu_snapshot_begin;
+    after a step, an upload of one of them (before anything read them) leaves
+    the others as the step left them.  Relative L-infinity bars: 1e-11 on the
+    same state, 1e-9 after one step of both."""
     from fargocpt_gb300.engine import Engine
     from fargocpt_gb300.output import Snapshotter
     from oracle.oracle_py import OracleState, set_threads
@@ -166,6 +166,6 @@ def test_stress_fields_read_back_as_doubles(arith, monkeypatch):
     mark = np.full((g.nr, g.nz), 0.25)
     g.set_field("TAU_R_R", mark)
     assert np.array_equal(g.get_field("TAU_R_R"), mark)
-    for f in ("DIV_V", "TAU_PHI_PHI", "TAU_R_PHI"):
+    for f in ("DIV_V", "TAU_PHI_PHI", "TAU_R_PHI", "Q_R", "Q_PHI"):
         err = _stress_err(g.get_field(f), o.get_field(f), f, g.nr)
         assert err <= 1e-9, f"{f} after a step and an upload of TAU_R_R: {err:.3e}"
