@@ -53,10 +53,10 @@ STEP_BYTES_PER_CELL = {"adiabatic": 64, "isothermal": 48}   # one read + write o
 NCU_DRAM_BYTES = {
     # 2048 x 6144 three-planet adiabatic disk (profiles/traffic_c5_transports.md;
     # the FP64 form's float-pair kernels)
-    ("c5", "fp64", "transport_azimuthal"): 707886592 + 645737472,
-    ("c5", "fp64", "transport_radial"): 412882432 + 549269504,
-    ("c5", "fp32", "transport_azimuthal"): 403144448 + 288285952,
-    ("c5", "fp32", "transport_radial"): 260210688 + 302722816,
+    ("c5", "fp64", "transport_azimuthal"): 713425664 + 602434048,
+    ("c5", "fp64", "transport_radial"): 453888256 + 557087488,
+    ("c5", "fp32", "transport_azimuthal"): 402961408 + 288184320,
+    ("c5", "fp32", "transport_radial"): 295241216 + 318492928,
     # 512 x 1536 adiabatic disk (--set full captures)
     ("c2", "fp64", "transport_azimuthal"): 44.127e6 + 0.422e6,
     ("c2", "fp64", "transport_radial"): 25.252e6 + 0.738e6,
@@ -513,12 +513,12 @@ def main():
     value = world * cells * args.steps / (vals[0] * 1e-3)
     e2e = world * cells * args.steps / vals[1]
     rl, rls = roofline(r64, args.steps, 1.0, "fp64", args.config)
-    # what bounds the float-pair transports (ncu --set full on 256 rings of
-    # 6144 cells, profiles/transport_kernels_c5_fp64_pair.md): issue and
-    # latency, not the FP64 pipe or DRAM
+    # what bounds the float-pair transports (ncu --set full on 512 rings of
+    # 6144 cells, profiles/transport_kernels_c5_fp64_pair.md): issue, the
+    # FP64 pipe and latency, not DRAM
     rl["ncu_pipes_pct"] = {
-        "transport_azimuthal": {"issue_active": 41.1, "fp64_pipe": 38.2, "fma_pipe": 18.9},
-        "transport_radial": {"issue_active": 51.3, "fp64_pipe": 33.8, "fma_pipe": 26.1}}
+        "transport_azimuthal": {"issue_active": 53.4, "fp64_pipe": 54.5, "fma_pipe": 26.4},
+        "transport_radial": {"issue_active": 58.8, "fp64_pipe": 42.7, "fma_pipe": 31.6}}
     fp32 = None
     if r32 is not None:
         value32 = world * cells * args.steps / (vals[2] * 1e-3)
