@@ -883,6 +883,7 @@ static int setup_tables(fgpu_engine *eng, const double *radii)
     ph.pk_mu_gm1_over_R = split_pair_host(ph.mu_gm1_over_R);
     ph.pk_cool_const = split_pair_host(ph.cool_const);
     ph.pk_emin_fac = split_pair_host(ph.emin_fac);
+    ph.pk_eps_smooth = split_pair_host(ph.eps_smooth);
     return FGPU_OK;
 }
 

@@ -108,7 +108,7 @@ struct Phys {
     float emin_fac_f, emax_fac_f;  // the same rounded to float (FP32 screens)
     // constants of the float-pair kernels as pairs (split_pair_host)
     float2 pk_gm1, pk_g_gm1, pk_alpha, pk_C2, pk_rvf, pk_hvf, pk_mu_gm1_over_R, pk_cool_const,
-        pk_emin_fac;
+        pk_emin_fac, pk_eps_smooth;
 };
 
 struct Bodies {

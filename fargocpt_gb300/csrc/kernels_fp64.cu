@@ -165,9 +165,15 @@ __device__ __forceinline__ bool maybe_inside(f2 dsm, float rsm_f)
 
 // PAIR and a central object at the origin without Klahr smoothing (the
 // heliocentric frame's usual case, a uniform branch): its distance^2 is
-// Rmed^2 + smooth^2, since cos^2 + sin^2 = 1 within the tables' rounding, so
-// the FP64 work per cell is one product, one fused multiply-add, the
-// Newton-finished 1/sqrt and the final sums; the indirect term, linear in
+// R^2 + s^2 (R = Rmed, s = eps H; cos^2 + sin^2 = 1 within the tables'
+// rounding), and its potential -G m / sqrt(R^2 + s^2) = C (1 + g(u)) with
+// C = -G m / R in FP64 and, u = (s / R)^2,
+//     g(u) = (1 + u)^(-1/2) - 1 = -u / (sqrt(1 + u) (1 + sqrt(1 + u))),
+// a form without cancellation.  g is small (u is about (eps h)^2), so C g in
+// pairs carries an absolute error of a few 2^-46 |C g|, far below the
+// rounding of C itself: the FP64 work per cell is the product C and the
+// final sum.  The source terms' FP64 differences of the potential see C's
+// per-ring values and the smooth correction.  The indirect term, linear in
 // the cell position, joins the planets' pair sum.
 template <bool PAIR>
 __global__ void k_potential(Geo g, Tables t, Phys ph, Bodies b, const double *__restrict__ H,
@@ -178,13 +184,19 @@ __global__ void k_potential(Geo g, Tables t, Phys ph, Bodies b, const double *__
     const int i = blockIdx.y;
     if (j >= nz) return;
     if (PAIR && b.star_plain) {
-        const double smooth = ph.eps_smooth * H[CELL(i, j)];
-        const double rm = t.Rmed[i];
-        const double acc = b.gm0 * rsqrt_fp64(fma(smooth, smooth, rm * rm));
+        const double C = b.gm0 * t.InvRmed[i];
+        const f2 sp = f2_smul(f2_split(H[CELL(i, j)]), f2{ph.pk_eps_smooth.x, ph.pk_eps_smooth.y});
+        const float2 ir = t.ptab[(t.InvRmed - t.tbase) + i];
+        const f2 q = f2_smul(sp, f2{ir.x, ir.y});
+        const f2 u = f2_smul(q, q);
+        const f2 one{1.f, 0.f};
+        const f2 sq = f2_sqrt(f2_sadd(one, u));
+        const f2 g1 = f2_neg(f2_sdiv(u, f2_smul(sq, f2_sadd(one, sq))));
+        const f2 star = f2_smul(f2_split(C), g1);
         const f2 rmp{t.RmedHi[i], t.RmedLo[i]};
         const f2 xc = f2_smul(rmp, f2{t.cosHi[j], t.cosLo[j]});
         const f2 yc = f2_smul(rmp, f2{t.sinHi[j], t.sinLo[j]});
-        const f2 s2 = f2_split(smooth * smooth);
+        const f2 s2 = f2_smul(sp, sp);
         float ah = 0.f, al = 0.f;
         for (int k = 1; k < b.n; ++k) {
             const f2 dx = f2_ssub(xc, f2{b.xh[k], b.xl[k]});
@@ -209,7 +221,7 @@ __global__ void k_potential(Geo g, Tables t, Phys ph, Bodies b, const double *__
         }
         const f2 ind = f2_neg(f2_sadd(f2_smul(f2{b.pk_ix.x, b.pk_ix.y}, xc),
                                       f2_smul(f2{b.pk_iy.x, b.pk_iy.y}, yc)));
-        pot[CELL(i, j)] = acc + f2_to_double(f2_sadd(f2{ah, al}, ind));
+        pot[CELL(i, j)] = C + f2_to_double(f2_sadd(f2_sadd(f2{ah, al}, ind), star));
         return;
     }
     const double smooth = ph.eps_smooth * H[CELL(i, j)];
