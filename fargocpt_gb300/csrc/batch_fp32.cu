@@ -144,7 +144,8 @@ __global__ void b_finish(const DiskF *__restrict__ D, const StepF *__restrict__ 
 {
     for_cells(D, S, start, nd, rpb, 1, [&](const DiskF &k, const StepF &, int i, int j) {
         finish_cell(k.g, k.t, k.ph, k.mom[0], k.mom[1], k.mom[2], k.mom[3], k.sigma_t, k.energy_t,
-                    k.vr_b, k.s.vr, k.s.dv, k.s.sigma, k.s.energy, k.sigma_lo_t, k.s.sigma_lo, i,
+                    k.vr_b, k.s.vr, k.s.dv, k.s.sigma, k.s.energy, k.sigma_lo_t, k.s.sigma_lo,
+                    k.ring_shift, i,
                     j);
     });
 }
@@ -219,7 +220,8 @@ __global__ void __launch_bounds__(PER <= 4 ? 384 : 512, PER <= 4 ? 2 : 1)
         const int i = item - __ldg(start + d);
         azimuthal_ring<PER, NQ, true>(k.g, k.t, S[d].dt, k.ph.limiter_mc, k.ph.fast_transport,
                                       k.dv_b, k.mom[0], k.mom[1], k.mom[2], k.mom[3], k.energy_t,
-                                      k.sigma_t, k.sigma_lo_t, i, smf, redf, redl);
+                                      k.sigma_t, k.sigma_lo_t, i, smf, redf, redl,
+                                      k.ring_shift);
     }
 }
 
@@ -242,7 +244,8 @@ __global__ void __launch_bounds__(rb_max_threads(PER))
         const int i = item - __ldg(start + d);
         azimuthal_ring_rb<PER, NQ>(k.g, k.t, S[d].dt, k.ph.limiter_mc, k.ph.fast_transport,
                                    k.dv_b, k.mom[0], k.mom[1], k.mom[2], k.mom[3], k.energy_t,
-                                   k.sigma_t, k.sigma_lo_t, i, smf, redf, redl);
+                                   k.sigma_t, k.sigma_lo_t, i, smf, redf, redl,
+                                   k.ring_shift);
     }
 }
 
@@ -391,7 +394,7 @@ __global__ void b_close_sequence(const DiskF *__restrict__ D, const StepF *__res
               [&](const DiskF &k, const StepF &, int i, int j) {
                   finish_cell(k.g, k.t, k.ph, k.mom[0], k.mom[1], k.mom[2], k.mom[3], k.sigma_t,
                               k.energy_t, k.vr_b, k.s.vr, k.s.dv, k.s.sigma, k.s.energy,
-                              k.sigma_lo_t, k.s.sigma_lo, i, j);
+                              k.sigma_lo_t, k.s.sigma_lo, k.ring_shift, i, j);
               });
     grid.sync();
     // damping zones, as b_damping (its block reductions are block-wide)

@@ -44,7 +44,11 @@ __device__ __forceinline__ void comp_add(float &hi, float &lo, float inc)
 // The star values and fluxes of the azimuthal passes with the rounding of
 // every operation fixed (an explicit FMA where the value is interpolated),
 // so that the strided and the register-blocked ring kernels, whose code the
-// compiler would otherwise contract differently, give the same bits.
+// compiler would otherwise contract differently, give the same bits; the
+// passes spell out the specific values (q / sigma as q times 1 / sigma) and
+// the slopes' differences and scaling for the same reason (the blocked kernel
+// holds a specific value in a register where it is differenced, the strided
+// one reloads it from shared memory, and only the former may fuse the two).
 //   upwind value on the positive side: W_jm + (dx - ksi) D_jm
 //   on the negative side:              W_j  - (dx + ksi) D_j
 __device__ __forceinline__ float star_pos(float w, float d, float dx, float ksi)
@@ -864,7 +868,7 @@ __device__ __forceinline__ void ring_pass_f(float *S, float *W, float *D, float 
         const int j = tid + n * bs;
         if (j < nz) {
             const int jp = j == nz - 1 ? 0 : j + 1, jm = j == 0 ? nz - 1 : j - 1;
-            D[j] = lim_f(S[jp] - S[j], S[j] - S[jm], mc) * half_invdx;
+            D[j] = __fmul_rn(lim_f(__fsub_rn(S[jp], S[j]), __fsub_rn(S[j], S[jm]), mc), half_invdx);
             invs[n] = __frcp_rn(S[j]);
         }
     }
@@ -888,7 +892,7 @@ __device__ __forceinline__ void ring_pass_f(float *S, float *W, float *D, float 
 #pragma unroll
         for (int n = 0; n < PER; ++n) {
             const int j = tid + n * bs;
-            if (j < nz) W[j] = Q[j] * invs[n];
+            if (j < nz) W[j] = __fmul_rn(Q[j], invs[n]);
         }
         __syncthreads();
 #pragma unroll
@@ -896,7 +900,7 @@ __device__ __forceinline__ void ring_pass_f(float *S, float *W, float *D, float 
             const int j = tid + n * bs;
             if (j < nz) {
                 const int jp = j == nz - 1 ? 0 : j + 1, jm = j == 0 ? nz - 1 : j - 1;
-                D[j] = lim_f(W[jp] - W[j], W[j] - W[jm], mc) * half_invdx;
+                D[j] = __fmul_rn(lim_f(__fsub_rn(W[jp], W[j]), __fsub_rn(W[j], W[jm]), mc), half_invdx);
             }
         }
         __syncthreads();
@@ -966,7 +970,7 @@ __device__ __forceinline__ void ring_pass_uniform_f(float *S, float *W, float *D
         const int j = tid + n * bs;
         if (j < nz) {
             const int jp = j == nz - 1 ? 0 : j + 1, jm = j == 0 ? nz - 1 : j - 1;
-            D[j] = lim_f(S[jp] - S[j], S[j] - S[jm], mc) * half_invdx;
+            D[j] = __fmul_rn(lim_f(__fsub_rn(S[jp], S[j]), __fsub_rn(S[j], S[jm]), mc), half_invdx);
             invs[n] = __frcp_rn(S[j]);
         }
     }
@@ -988,7 +992,7 @@ __device__ __forceinline__ void ring_pass_uniform_f(float *S, float *W, float *D
 #pragma unroll
         for (int n = 0; n < PER; ++n) {
             const int j = tid + n * bs;
-            if (j < nz) W[j] = Q[j] * invs[n];
+            if (j < nz) W[j] = __fmul_rn(Q[j], invs[n]);
         }
         __syncthreads();
 #pragma unroll
@@ -996,7 +1000,7 @@ __device__ __forceinline__ void ring_pass_uniform_f(float *S, float *W, float *D
             const int j = tid + n * bs;
             if (j < nz) {
                 const int jp = j == nz - 1 ? 0 : j + 1, jm = j == 0 ? nz - 1 : j - 1;
-                D[j] = lim_f(W[jp] - W[j], W[j] - W[jm], mc) * half_invdx;
+                D[j] = __fmul_rn(lim_f(__fsub_rn(W[jp], W[j]), __fsub_rn(W[j], W[jm]), mc), half_invdx);
             }
         }
         __syncthreads();
@@ -1029,8 +1033,8 @@ __device__ __forceinline__ void ring_pass_uniform_f(float *S, float *W, float *D
 // specific quantity, its slope and the flux, a fifth for the per-face factors
 // on rings up to 2048 cells (where at most 4 cells per thread leave no
 // registers for them), plus the nq quantity rows when STAGE (then every row
-// is read from HBM once, up front, and the passes and the shift work in
-// shared memory).
+// is read from HBM once, up front, the passes work in shared memory and the
+// rows go back once at the end).
 __host__ __device__ constexpr int azimuthal_work_rows(int nz) { return nz <= 2048 ? 5 : 4; }
 __host__ __device__ constexpr size_t azimuthal_smem_floats(int nz, int nq, bool stage)
 {
@@ -1044,7 +1048,7 @@ __device__ __forceinline__ void azimuthal_ring(const GeoF &g, const TablesF &t, 
                                                int fast, const float *__restrict__ dv,
                                                float *m0, float *m1, float *m2, float *m3,
                                                float *E, float *S, float *S_lo, int i, float *smf,
-                                               float *redf, long long *redl)
+                                               float *redf, long long *redl, int *ring_shift)
 {
     const int nz = g.nz;
     const int tid = threadIdx.x, bs = blockDim.x;
@@ -1113,59 +1117,28 @@ __device__ __forceinline__ void azimuthal_ring(const GeoF &g, const TablesF &t, 
                                      pos ? dxtheta - ksi : -(dxtheta + ksi),
                                      dxrad * vt * invsurf, half_invdx, nz, mc);
     }
-    // the integer shift (AdvectSHIFT, :238-268): cell j takes cell j - nshift
-    const int ns = nshift % nz;
-    int src[PER];
+    // AdvectSHIFT (:238-268) is the velocity rebuild's: it reads cell j of
+    // this ring from cell j - nshift, so the rows go back unshifted (the
+    // quantities are already in place unless staged)
 #pragma unroll
     for (int n = 0; n < PER; ++n) {
-        int ji = tid + n * bs - ns;
-        if (ji < 0) ji += nz;
-        else if (ji >= nz) ji -= nz;
-        src[n] = ji;
+        const int j = tid + n * bs;
+        if (j < nz) {
+            S[row + j] = Sr[j];
+            S_lo[row + j] = slo[n];
+        }
     }
     if (STAGE) {
-        // all rows are in shared memory: shift straight out of it
 #pragma unroll
-        for (int q = 0; q <= NQ; ++q) {
-            const float *from = q < NQ ? qrow[q] : Sr;
-            float *to = q < NQ ? grow[q] : S + row;
+        for (int q = 0; q < NQ; ++q) {
 #pragma unroll
             for (int n = 0; n < PER; ++n) {
                 const int j = tid + n * bs;
-                if (j < nz) to[j] = from[src[n]];
+                if (j < nz) grow[q][j] = qrow[q][j];
             }
         }
-    } else {
-#pragma unroll
-        for (int q = 0; q <= NQ; ++q) {
-            float *Q = q < NQ ? grow[q] : S + row;
-            const float *from = q < NQ ? grow[q] : Sr;
-#pragma unroll
-            for (int n = 0; n < PER; ++n) {
-                const int j = tid + n * bs;
-                if (j < nz) W[j] = from[j];
-            }
-            __syncthreads();
-#pragma unroll
-            for (int n = 0; n < PER; ++n) {
-                const int j = tid + n * bs;
-                if (j < nz) Q[j] = W[src[n]];
-            }
-            __syncthreads();
-        }
     }
-    // the low part of sigma moves with it
-#pragma unroll
-    for (int n = 0; n < PER; ++n) {
-        const int j = tid + n * bs;
-        if (j < nz) W[j] = slo[n];
-    }
-    __syncthreads();
-#pragma unroll
-    for (int n = 0; n < PER; ++n) {
-        const int j = tid + n * bs;
-        if (j < nz) S_lo[row + j] = W[src[n]];
-    }
+    if (tid == 0) ring_shift[i] = ((nshift % nz) + nz) % nz;
     // the caller may reuse smf for the next ring
     __syncthreads();
 }
@@ -1184,19 +1157,19 @@ __device__ __forceinline__ void azimuthal_ring(const GeoF &g, const TablesF &t, 
 // the exchange in between, which every thread reaches only after reading
 // buffer b, so no write overtakes a read.  Every cell's arithmetic is the
 // strided kernel's (ring_pass_f, ring_pass_uniform_f, the exact-sum ring mean,
-// the shift), expression for expression, so both give the same bits.
+// the shift phase), expression for expression, so both give the same bits.
 //
-// Shared memory (rb_smem_floats): the NQ transported rows (each thread's
-// segment; their shifted copy-out reads across the ring), one spare row for
-// sigma and its low part at the shift, and 2 x 5 x blockDim.x floats for the
-// exchanges.
+// Shared memory (rb_smem_floats): the NQ transported rows between the two
+// passes (staged coalesced from HBM; the last pass writes each segment back
+// to its row in place, the integer shift being the velocity rebuild's) and
+// 2 x 5 x blockDim.x floats for the exchanges.
 // ---------------------------------------------------------------------------
 // threads per ring block of the register-blocked kernel: 16 cells per thread
 // need more registers than 128 (the budget at 512 threads)
 __host__ __device__ constexpr int rb_max_threads(int per) { return per >= 16 ? 384 : 512; }
 __host__ __device__ constexpr size_t rb_smem_floats(int nz, int nq, int threads)
 {
-    return (size_t)(nq + 1) * (size_t)nz + (size_t)10 * (size_t)threads;
+    return (size_t)nq * (size_t)nz + (size_t)10 * (size_t)threads;
 }
 // whether a ring of nz cells splits into segments of per cells with between
 // min_threads and the kernel's bound of threads, within max_smem bytes
@@ -1227,7 +1200,8 @@ __device__ __forceinline__ void azimuthal_ring_rb(const GeoF &g, const TablesF &
                                                   int mc, int fast, const float *__restrict__ dv,
                                                   float *m0, float *m1, float *m2, float *m3,
                                                   float *E, float *S, float *S_lo, int i,
-                                                  float *smf, float *redf, long long *redl)
+                                                  float *smf, float *redf, long long *redl,
+                                                  int *ring_shift)
 {
     static_assert(PER % 4 == 0 && PER >= 4, "segments of whole 128-bit words");
     const int nz = g.nz;  // == PER * blockDim.x
@@ -1236,8 +1210,7 @@ __device__ __forceinline__ void azimuthal_ring_rb(const GeoF &g, const TablesF &
     const int j0 = tid * PER;
     const int left = tid == 0 ? bs - 1 : tid - 1, right = tid == bs - 1 ? 0 : tid + 1;
     float *qsm = smf;                               // NQ rows
-    float *spare = smf + (size_t)NQ * nz;           // one row
-    float *xs = spare + nz;                         // [2][5][bs]
+    float *xs = smf + (size_t)NQ * nz;              // [2][5][bs]
     float *grow[5] = {m0 + row, m1 + row, m2 + row, m3 + row, E + row};
     int buf = 0;
     // publishes a0, a1 (first two), a2, a3 (last two) and a4; returns the
@@ -1321,7 +1294,8 @@ __device__ __forceinline__ void azimuthal_ring_rb(const GeoF &g, const TablesF &
     auto slopes = [&]() {
 #pragma unroll
         for (int c = -1; c <= PER; ++c)
-            D[c + 1] = lim_f(X[c + 3] - X[c + 2], X[c + 2] - X[c + 1], mc) * half_invdx;
+            D[c + 1] = __fmul_rn(lim_f(__fsub_rn(X[c + 3], X[c + 2]), __fsub_rn(X[c + 2], X[c + 1]), mc),
+                                 half_invdx);
     };
     auto sigma_ends = [&](float a4, float &r4) {
         float l2, l3, r0, r1;
@@ -1335,7 +1309,7 @@ __device__ __forceinline__ void azimuthal_ring_rb(const GeoF &g, const TablesF &
     };
     auto specific = [&](const float *q) {
 #pragma unroll
-        for (int n = 0; n < PER; ++n) X[n + 2] = q[n] * invs[n];
+        for (int n = 0; n < PER; ++n) X[n + 2] = __fmul_rn(q[n], invs[n]);
         float l2, l3, r0, r1, r4;
         exchange(X[2], X[3], X[PER], X[PER + 1], 0.f, l2, l3, r0, r1, r4);
         X[0] = l2;
@@ -1375,7 +1349,8 @@ __device__ __forceinline__ void azimuthal_ring_rb(const GeoF &g, const TablesF &
             }
 #pragma unroll
             for (int n = 0; n < PER; ++n) qv[n] = __fadd_rn(qv[n], __fsub_rn(F[n], F[n + 1]));
-            store_seg(qsm + (size_t)q * nz, qv);
+            // the last pass writes the segment back to its row in place
+            store_seg(fast ? qsm + (size_t)q * nz : grow[q], qv);
         }
 #pragma unroll
         for (int n = 0; n < PER; ++n) comp_add(s[n], slo[n], cf[n] - cf[n + 1]);
@@ -1416,33 +1391,18 @@ __device__ __forceinline__ void azimuthal_ring_rb(const GeoF &g, const TablesF &
                 const float dqs = star_diff(xu, xu1, du, du1, a);
                 qv[n] = uniform_update(qv[n], c, qs, dss[n], Fs[n], dqs);
             }
-            store_seg(qsm + (size_t)q * nz, qv);
+            store_seg(grow[q], qv);
         }
 #pragma unroll
         for (int n = 0; n < PER; ++n) comp_add(s[n], slo[n], __fmul_rn(c, dss[n]));
     }
 
-    // the integer shift (AdvectSHIFT, :238-268): cell j takes cell j - nshift,
-    // copied out in the strided order so that both sides stay coalesced
-    const int ns = nshift % nz;
-    auto src_of = [&](int j) {
-        int ji = j - ns;
-        if (ji < 0) ji += nz;
-        else if (ji >= nz) ji -= nz;
-        return ji;
-    };
-    __syncthreads();  // every segment of the rows is final
-#pragma unroll
-    for (int q = 0; q < NQ; ++q)
-        for (int j = tid; j < nz; j += bs) grow[q][j] = qsm[(size_t)q * nz + src_of(j)];
-    store_seg(spare, s);
-    __syncthreads();
-    for (int j = tid; j < nz; j += bs) S[row + j] = spare[src_of(j)];
-    __syncthreads();
-    // the low part of sigma moves with it
-    store_seg(spare, slo);
-    __syncthreads();
-    for (int j = tid; j < nz; j += bs) S_lo[row + j] = spare[src_of(j)];
+    // AdvectSHIFT (:238-268) is the velocity rebuild's: it reads cell j of
+    // this ring from cell j - nshift; the last pass wrote the quantities'
+    // segments in place, sigma and its low part follow
+    store_seg(S + row, s);
+    store_seg(S_lo + row, slo);
+    if (tid == 0) ring_shift[i] = ((nshift % nz) + nz) % nz;
     // the caller may reuse smf for the next ring
     __syncthreads();
 }
@@ -1469,8 +1429,8 @@ __device__ __forceinline__ void finish_cell(
     const float *__restrict__ m1, const float *__restrict__ m2, const float *__restrict__ m3,
     const float *__restrict__ S_t, const float *__restrict__ E_t, const float *__restrict__ vr_in,
     float *__restrict__ vr_out, float *__restrict__ dv_out, float *__restrict__ S_out,
-    float *__restrict__ E_out, const float *__restrict__ Slo_t, float *__restrict__ Slo_out, int i,
-    int j)
+    float *__restrict__ E_out, const float *__restrict__ Slo_t, float *__restrict__ Slo_out,
+    const int *__restrict__ shift, int i, int j)
 {
     const int nz = g.nz, nr = g.nr;
     const size_t c = CELL(i, j);
@@ -1478,26 +1438,33 @@ __device__ __forceinline__ void finish_cell(
         vr_out[c] = vr_in[c];
         return;
     }
-    const float s = S_t[c];
+    // AdvectSHIFT: the transported cell j of ring k sits at j - shift[k]
+    auto at = [&](int k, int jj) {
+        int a = jj - __ldg(shift + k);
+        if (a < 0) a += nz;
+        return CELL(k, a);
+    };
+    const size_t cs = at(i, j);
+    const float s = S_t[cs];
     if (i == 0) {
         vr_out[c] = 0.f;
     } else {
-        const size_t cm = CELL(i - 1, j);
-        vr_out[c] = __fdiv_rn(m0[cm] + m1[c], S_t[cm] + s);
+        const size_t cm = at(i - 1, j);
+        vr_out[c] = __fdiv_rn(m0[cm] + m1[cs], S_t[cm] + s);
     }
-    const size_t cjm = CELL(i, jprev(j, nz));
+    const size_t cjm = at(i, jprev(j, nz));
     // the residual angular momenta were formed as sigma (dv Rmed) with the
     // FP32 Rmed of the ring: dividing by that same Rmed returns dv without
     // bias, where multiplying by the FP32 1/Rmed would scale every ring's
     // residual by Rmed 1/Rmed - 1 (up to ~6e-8) in every step, a drift that
     // accumulates over tens of thousands of steps; the divisions are
     // correctly rounded for the same reason
-    dv_out[c] = __fdiv_rn(m2[cjm] + m3[c], __fmul_rn(S_t[cjm] + s, t.Rmed[i]));
+    dv_out[c] = __fdiv_rn(m2[cjm] + m3[cs], __fmul_rn(S_t[cjm] + s, t.Rmed[i]));
     const bool floored = s < ph.sigma_min;
     const float sf = floored ? ph.sigma_min : s;
     S_out[c] = sf;
-    Slo_out[c] = floored ? 0.f : Slo_t[c];
-    if (ph.adiabatic) E_out[c] = tfloor(E_t[c], sf, ph);
+    Slo_out[c] = floored ? 0.f : Slo_t[cs];
+    if (ph.adiabatic) E_out[c] = tfloor(E_t[cs], sf, ph);
 }
 
 // damping zones (damping.cpp:311-776); block-wide over ring i

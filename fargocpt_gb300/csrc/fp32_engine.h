@@ -145,6 +145,7 @@ struct DiskF {
     StateF s;
     float *vr_b, *dv_b;
     float *sigma_t, *energy_t, *sigma_lo_t;  // after radial transport
+    int *ring_shift;  // the azimuthal pass's integer shift per ring (AdvectSHIFT)
     float *mom[4];
     float *pot, *P, *cs, *H, *nu, *T, *Qr, *Qp, *divv, *trr, *tpp, *trp, *qplus, *qminus;
     unsigned int *dtmin;
@@ -261,6 +262,7 @@ class Engine32 {
     float *alt_sigma = nullptr, *alt_vr = nullptr, *alt_dv = nullptr, *alt_e = nullptr;
     float *vr_a = nullptr, *dv_a = nullptr;  // v_r, v_phi buffers at creation
     float *sigma_lo = nullptr, *alt_sigma_lo = nullptr;
+    int *ring_shift = nullptr;  // AdvectSHIFT per ring, applied by the velocity rebuild
     float *mom[4] = {};
     float *tab_f = nullptr;
     double *tab_d = nullptr;

@@ -148,13 +148,13 @@ __global__ void __launch_bounds__(512) f_transport_azimuthal(GeoF g, TablesF t, 
                                                              const float *__restrict__ dv,
                                                              float *m0, float *m1, float *m2,
                                                              float *m3, float *E, float *S,
-                                                             float *S_lo)
+                                                             float *S_lo, int *ring_shift)
 {
     extern __shared__ __align__(16) float smf[];
     __shared__ float redf[33];
     __shared__ long long redl[33];
     azimuthal_ring<PER, NQ, STAGE>(g, t, dt, mc, fast, dv, m0, m1, m2, m3, E, S, S_lo,
-                                   blockIdx.x, smf, redf, redl);
+                                   blockIdx.x, smf, redf, redl, ring_shift);
 }
 
 // the register-blocked ring transport (azimuthal_ring_rb): nz = PER x blockDim.x
@@ -164,13 +164,13 @@ __global__ void __launch_bounds__(rb_max_threads(PER)) f_transport_azimuthal_rb(
                                                                 const float *__restrict__ dv,
                                                                 float *m0, float *m1, float *m2,
                                                                 float *m3, float *E, float *S,
-                                                                float *S_lo)
+                                                                float *S_lo, int *ring_shift)
 {
     extern __shared__ __align__(16) float smf[];
     __shared__ float redf[33];
     __shared__ long long redl[33];
     azimuthal_ring_rb<PER, NQ>(g, t, dt, mc, fast, dv, m0, m1, m2, m3, E, S, S_lo, blockIdx.x,
-                               smf, redf, redl);
+                               smf, redf, redl, ring_shift);
 }
 
 __global__ void f_pressure(GeoF g, TablesF t, PhysF ph, const float *__restrict__ S,
@@ -187,12 +187,13 @@ __global__ void f_finish(GeoF g, TablesF t, PhysF ph, const float *__restrict__ 
                          const float *__restrict__ E_t, const float *__restrict__ vr_in,
                          float *__restrict__ vr_out, float *__restrict__ dv_out,
                          float *__restrict__ S_out, float *__restrict__ E_out,
-                         const float *__restrict__ Slo_t, float *__restrict__ Slo_out)
+                         const float *__restrict__ Slo_t, float *__restrict__ Slo_out,
+                         const int *__restrict__ shift)
 {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= g.nz) return;
     finish_cell(g, t, ph, m0, m1, m2, m3, S_t, E_t, vr_in, vr_out, dv_out, S_out, E_out, Slo_t,
-                Slo_out, blockIdx.y, j);
+                Slo_out, shift, blockIdx.y, j);
 }
 
 __global__ void f_damping(GeoF g, DampingF dm, float dt, const int *__restrict__ rings, StateF s)
@@ -648,6 +649,8 @@ int Engine32::create(const fgpu_params &prm, const double *radii, cudaStream_t s
     CKF(cudaMemset(sigma_lo, 0, cells * sizeof(float)));
     CKF(cudaMalloc(&alt_sigma_lo, cells * sizeof(float)));
     CKF(cudaMemset(alt_sigma_lo, 0, cells * sizeof(float)));
+    CKF(cudaMalloc(&ring_shift, sizeof(int) * (size_t)nr));
+    CKF(cudaMemset(ring_shift, 0, sizeof(int) * (size_t)nr));
     for (int k = 0; k < 4; ++k) CKF(cudaMalloc(&mom[k], cells * sizeof(float)));
     CKF(cudaMalloc(&partial, sizeof(double) * 5 * kForceBodies32 * (size_t)nr));
     CKF(cudaMalloc(&red_out, sizeof(double) * (8 + 5 * kMaxBodies)));
@@ -854,7 +857,7 @@ void Engine32::destroy()
 {
     for (int f = 0; f < FGPU_FIELD_COUNT; ++f) cudaFree(fld[f]);
     cudaFree(alt_sigma); cudaFree(alt_vr); cudaFree(alt_dv); cudaFree(alt_e);
-    cudaFree(sigma_lo); cudaFree(alt_sigma_lo);
+    cudaFree(sigma_lo); cudaFree(alt_sigma_lo); cudaFree(ring_shift);
     for (int k = 0; k < 4; ++k) cudaFree(mom[k]);
     cudaFree(partial); cudaFree(red_out); cudaFree(d_dtmin); cudaFree(d_bad); cudaFree(stage);
     cudaFree(corr_phi); cudaFree(corr_r);
@@ -886,6 +889,7 @@ DiskF Engine32::describe()
     d.sigma_t = alt_sigma;
     d.energy_t = alt_e;
     d.sigma_lo_t = alt_sigma_lo;
+    d.ring_shift = ring_shift;
     for (int k = 0; k < 4; ++k) d.mom[k] = mom[k];
     d.pot = fld[FGPU_POTENTIAL];
     d.P = fld[FGPU_PRESSURE];
@@ -1224,7 +1228,7 @@ int Engine32::transport(double dt)
 #define AZ32(P, NQ, ST)                                                                          \
     f_transport_azimuthal<P, NQ, ST><<<nr, az_block, az_smem, stream>>>(                         \
         geo, tabs, dt, phys.limiter_mc, phys.fast_transport, s.dv, mom[0], mom[1], mom[2],      \
-        mom[3], alt_e, alt_sigma, alt_sigma_lo)
+        mom[3], alt_e, alt_sigma, alt_sigma_lo, ring_shift)
 #define AZ32_NQ(NQ)                                      \
     if (az_stage) {                                      \
         if (per == 4) AZ32(4, NQ, true);                 \
@@ -1240,7 +1244,7 @@ int Engine32::transport(double dt)
 #define AZRB(P, NQ)                                                                              \
     f_transport_azimuthal_rb<P, NQ><<<nr, nz / P, rb_smem, stream>>>(                            \
         geo, tabs, dt, phys.limiter_mc, phys.fast_transport, s.dv, mom[0], mom[1], mom[2],      \
-        mom[3], alt_e, alt_sigma, alt_sigma_lo)
+        mom[3], alt_e, alt_sigma, alt_sigma_lo, ring_shift)
 #define AZRB_NQ(NQ)                         \
     if (rb_per == 4) AZRB(4, NQ);           \
     else if (rb_per == 8) AZRB(8, NQ);      \
@@ -1267,7 +1271,7 @@ int Engine32::transport(double dt)
     f_finish<<<grid2(nz, nr + 1), 128, 0, stream>>>(geo, tabs, phys, mom[0], mom[1], mom[2],
                                                     mom[3], alt_sigma, alt_e, s.vr, alt_vr,
                                                     alt_dv, s.sigma, s.energy, alt_sigma_lo,
-                                                    sigma_lo);
+                                                    sigma_lo, ring_shift);
     CKL("finish");
     std::swap(fld[FGPU_V_RADIAL], alt_vr);
     std::swap(fld[FGPU_V_AZIMUTHAL], alt_dv);
