@@ -1,5 +1,5 @@
 """The FP64 drop-in against the oracle on the benchmark disks themselves,
-over 100 CFL-limited steps (the spec parity bar):
+over 100 CFL-limited steps (the FP64 parity bar, 1e-10):
 
 * the locally isothermal 128 x 384 disk (r in [0.4, 2.5], one planet of mass
   ratio 1e-3 at r = 1, FARGO, reference damping, CFL 0.5);
