@@ -2738,7 +2738,11 @@ void launch_cfl_cells(const Launch &L, const State &s, double *out)
 void launch_derived_cfl(const Launch &L, int mode, const State &s, unsigned long long *dt_min)
 {
     auto k = L.pair ? k_derived_cfl<true> : k_derived_cfl<false>;
-    k<<<L.g.nr, 256, (size_t)L.g.nz * sizeof(float), L.stream>>>(
+    // the FP32 screen's per-cell steps: only the FP64-arithmetic kernel and
+    // StabilizeViscosity 2 use them (the pair kernel keeps the shared memory
+    // for L1)
+    const bool screen = !L.pair || L.ph.stabilize == 2;
+    k<<<L.g.nr, 256, screen ? (size_t)L.g.nz * sizeof(float) : 0, L.stream>>>(
         L.g, L.t, L.ph, mode, L.ph.art_visc_sn, s.sigma, s.energy, s.vr, s.vaz, s.qplus,
         s.qminus, s.cs, s.H, s.P, s.T, s.nu, s.corr_phi, s.corr_r, dt_min);
 }
