@@ -169,3 +169,29 @@ def test_stress_fields_read_back_as_doubles(arith, monkeypatch):
     for f in ("DIV_V", "TAU_PHI_PHI", "TAU_R_PHI", "Q_R", "Q_PHI"):
         err = _stress_err(g.get_field(f), o.get_field(f), f, g.nr)
         assert err <= 1e-9, f"{f} after a step and an upload of TAU_R_R: {err:.3e}"
+
+
+@pytest.mark.parametrize("arith", ["pair", "fp64"])
+def test_fp64_full_size_disk_against_oracle(arith, monkeypatch):
+    """The 2048 x 6144 three-planet adiabatic disk of the bench line, 10 CFL
+    steps against the oracle: the production kernel variants at their full
+    size (6 cells per thread on 1024-thread ring blocks with the shuffled
+    fluxes, the radial walk's 32-ring chunks, the four-body disk force).
+    Bars as for the 100-step runs: dt within 1e-12, fields within 1e-10
+    relative L-infinity, the force on the first planet within 1e-9."""
+    from fargocpt_gb300.engine import Engine
+    from oracle.oracle_py import OracleState, set_threads
+
+    monkeypatch.setenv("FARGO_GB300_FP64_ARITH", arith)
+    set_threads(os.cpu_count() or 1)
+    o, co, _, _ = _run(OracleState, "c5", 10)
+    g, cg, _, _ = _run(Engine, "c5", 10)
+    np.testing.assert_allclose(cg.dts, co.dts, rtol=1e-12, atol=0)
+    for f in EVOLVED:
+        ref = o.get_field(f)
+        if not np.any(ref):
+            continue
+        err = rel_linf(g.get_field(f), ref)
+        assert err <= 1e-10, f"c5 {f}: rel Linf {err:.3e}"
+    np.testing.assert_allclose(g.disk_on_planet_accel(1), o.disk_on_planet_accel(1),
+                               rtol=1e-9, atol=0)
