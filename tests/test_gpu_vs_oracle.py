@@ -54,11 +54,16 @@ def test_gpu_vs_oracle_cfl_steps(adiabatic, nrad, naz):
     assert abs(g.total_mass() - o.total_mass()) <= 1e-13 * abs(o.total_mass())
 
 
-@pytest.mark.parametrize("naz", [1536, 7680])
-def test_azimuthal_kernel_variants(naz):
-    # naz = 1536 runs the ring in > 48 KB of shared memory, 7680 in 180 KB
-    # (one block per SM, 16 cells per thread)
-    params, d = make_params(8, naz, adiabatic=True)
+@pytest.mark.parametrize("adiabatic", [True, False])
+@pytest.mark.parametrize("naz", [1000, 1536, 4608, 6000, 6150, 7680])
+def test_azimuthal_kernel_variants(naz, adiabatic):
+    # the float-pair ring pass's variants: 1000 cells, 2 per thread on 512
+    # threads with clamped loops; 1536 and 4608, 6 per thread on whole warps
+    # (256 and 768 threads) with the shuffled fluxes; 6000, 6 per thread on
+    # 1024 threads, clamped; 6150, 16 per thread, clamped, the ring in 197 KB
+    # of shared memory; 7680, the ring's arrays in the global workspace (the
+    # FP64-arithmetic pass: > 48 KB of shared memory from 1536 cells on)
+    params, d = make_params(8, naz, adiabatic=adiabatic)
     (o, dto), (g, dtg) = run_both(params, d, steps=3, planet=False)
     np.testing.assert_allclose(dtg, dto, rtol=1e-12)
     for f in EVOLVED:
