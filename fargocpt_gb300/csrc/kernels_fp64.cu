@@ -1928,9 +1928,11 @@ __device__ __forceinline__ double cfl_cell64(const Geo &g, const Tables &t, cons
     return dt_cell;
 }
 
-// The time step of cell (i, j) in float pairs: cfl_cell64's six inverse
-// times and CFL / sqrt of their squares (LeapFrog's 0.6 on the last three),
-// within a few 2^-46 of the FP64 value, far inside the CFL step's bar.  The
+// The sum of the squares of cell (i, j)'s six inverse times in float pairs
+// (cfl_cell64's; LeapFrog's 0.6 on the last three): the cell's step is CFL
+// over its square root, so the ring's smallest step is CFL / sqrt of the
+// ring's largest sum, formed once per ring; within a few 2^-46 of the FP64
+// value, far inside the CFL step's bar.  The
 // differences of stored velocities and Q+ - Q- are FP64 subtractions (they
 // cancel); StabilizeViscosity 2 is served by the FP64 path.
 __device__ __forceinline__ f2 cfl_cell_f2(const Geo &g, const Tables &t, const Phys &ph, int sn,
@@ -1990,20 +1992,20 @@ __device__ __forceinline__ f2 cfl_cell_f2(const Geo &g, const Tables &t, const P
     sum = f2_sadd(sum, f2_smul(i4, i4));
     sum = f2_sadd(sum, f2_smul(i5, i5));
     sum = f2_sadd(sum, f2_smul(i6, i6));
-    return f2_sdiv(f2_split(ph.cfl), f2_sqrt(sum));
+    return sum;
 }
 
-// the smaller of two positive pairs
-__device__ __forceinline__ f2 pair_min(f2 a, f2 b)
+// the larger of two non-negative pairs
+__device__ __forceinline__ f2 pair_max(f2 a, f2 b)
 {
-    return (b.h < a.h || (b.h == a.h && b.l < a.l)) ? b : a;
+    return (b.h > a.h || (b.h == a.h && b.l > a.l)) ? b : a;
 }
-__device__ f2 block_min_f2(f2 v, float *red)
+__device__ f2 block_max_f2(f2 v, float *red)
 {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int nw = (blockDim.x + 31) >> 5;
     for (int o = 16; o > 0; o >>= 1)
-        v = pair_min(v, f2{__shfl_down_sync(0xffffffffu, v.h, o), __shfl_down_sync(0xffffffffu, v.l, o)});
+        v = pair_max(v, f2{__shfl_down_sync(0xffffffffu, v.h, o), __shfl_down_sync(0xffffffffu, v.l, o)});
     __syncthreads();
     if (lane == 0) {
         red[2 * wid] = v.h;
@@ -2011,9 +2013,9 @@ __device__ f2 block_min_f2(f2 v, float *red)
     }
     __syncthreads();
     if (wid == 0) {
-        f2 x = lane < nw ? f2{red[2 * lane], red[2 * lane + 1]} : f2{3.0e38f, 0.f};
+        f2 x = lane < nw ? f2{red[2 * lane], red[2 * lane + 1]} : f2{0.f, 0.f};
         for (int o = 16; o > 0; o >>= 1)
-            x = pair_min(x, f2{__shfl_down_sync(0xffffffffu, x.h, o), __shfl_down_sync(0xffffffffu, x.l, o)});
+            x = pair_max(x, f2{__shfl_down_sync(0xffffffffu, x.h, o), __shfl_down_sync(0xffffffffu, x.l, o)});
         if (lane == 0) {
             red[64] = x.h;
             red[65] = x.l;
@@ -2022,6 +2024,7 @@ __device__ f2 block_min_f2(f2 v, float *red)
     __syncthreads();
     return f2{red[64], red[65]};
 }
+
 
 // PAIR: the ideal-EOS derived quantities (T, c_s, H, nu) in float-pair
 // arithmetic (P = (gamma - 1) e stays one FP64 product: the source terms
@@ -2043,11 +2046,12 @@ __global__ void __launch_bounds__(256, PAIR ? 4 : 3) k_derived_cfl(Geo g, Tables
     __shared__ double red[33];
     __shared__ float redf[66];
     extern __shared__ float d32s[];  // the ring's FP32 cell steps (nz floats)
-    // PAIR: every cell's step in float pairs, the ring's smallest kept as a
-    // pair (no FP32 screen: in a nearly axisymmetric ring most cells fall
-    // inside any screen's margin, and each would then take FP64)
+    // PAIR: every cell's squared inverse step in float pairs, the ring's
+    // largest kept as a pair and turned into the ring's step once (no FP32
+    // screen: in a nearly axisymmetric ring most cells fall inside any
+    // screen's margin, and each would then take FP64)
     const bool pair_cfl = PAIR && ph.stabilize != 2;
-    f2 local2{3.0e38f, 0.f};
+    f2 local2{0.f, 0.f};
     const int nz = g.nz, nr = g.nr;
     const int i = blockIdx.x;
     float local32 = 3.0e38f;
@@ -2136,7 +2140,7 @@ __global__ void __launch_bounds__(256, PAIR ? 4 : 3) k_derived_cfl(Geo g, Tables
         }
         if (cfl_ring && pair_cfl) {
             const f2 cpair = have_cp2 ? cp2 : f2_split(c_s);
-            local2 = pair_min(local2, cfl_cell_f2(g, t, ph, sn, i, j, cpair, f2_split(n), vr, vaz,
+            local2 = pair_max(local2, cfl_cell_f2(g, t, ph, sn, i, j, cpair, f2_split(n), vr, vaz,
                                                   vm0, qplus, qminus, E));
         } else if (cfl_ring) {
             const float d32 = cfl_cell32(t32, ph, sn, c_s, n, vr[c], vr[c + nz], vaz[c],
@@ -2151,8 +2155,8 @@ __global__ void __launch_bounds__(256, PAIR ? 4 : 3) k_derived_cfl(Geo g, Tables
         }
     }
     if (cfl_ring && pair_cfl) {
-        const f2 m = block_min_f2(local2, redf);
-        const double d = f2_to_double(m);
+        const f2 m = block_max_f2(local2, redf);
+        const double d = f2_to_double(f2_sdiv(f2_split(ph.cfl), f2_sqrt(m)));
         if (dbits(d) < dbits(local)) local = d;
     } else if (cfl_ring) {
         // the FP64 dt of the cells the FP32 screen puts within 2^-15 of the
