@@ -912,11 +912,6 @@ static int create_engine(const fgpu_params *params, const double *radii, cudaStr
     eng->nz = params->naz;
     eng->cells = (size_t)eng->nr * eng->nz;
     eng->vcells = (size_t)(eng->nr + 1) * eng->nz;
-    // rings per radial sweep chunk: longer chunks prime fewer rings, shorter
-    // ones give more blocks (measured, ms per radial transport: 2048x6144
-    // 0.811 with 32, 0.830 with 16, 0.844 with 64; 512x1536 0.064 with 16,
-    // 0.068 with 8, 0.098 with 32)
-    eng->radial_chunk = eng->cells >= ((size_t)8 << 20) ? 32 : 16;
     eng->host_radii.assign(radii, radii + eng->nr + 2);
     auto fail = [&](int code) {
         fprintf(stderr, "fgpu_create: %s\n", eng->err.c_str());
@@ -1011,6 +1006,13 @@ static int create_engine(const fgpu_params *params, const double *radii, cudaStr
             return fail(FGPU_ERR_BAD_ARG);
         }
     }
+    // rings per radial sweep chunk (radial_chunk_for): longer chunks prime
+    // fewer rings, shorter ones give more blocks; 16 below 8M cells
+    // (measured, ms per radial pass on 512x1536: 0.064 with 16, 0.068 with
+    // 8, 0.098 with 32), else the chunk whose grid fills the fewest waves of
+    // resident blocks (2048x6144 in float pairs: 0.707 ms with 32 rings, six
+    // waves; 0.694 with 33 and 0.683 with 34, five)
+    eng->radial_chunk = radial_chunk_for(eng->pair_arith, eng->ph.adiabatic, eng->nr, eng->nz);
     // azimuthal transport: whole ring in shared memory when it fits
     {
         const int per = azimuthal_cells_per_thread(eng->nz);

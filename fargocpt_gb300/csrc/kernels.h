@@ -39,6 +39,8 @@ void launch_com_boundary(const Launch &L, const ComSpec &c, const State &s);
 void launch_correct_vaz(const Launch &L, double domega, double *vaz);
 void launch_cfl_cells(const Launch &L, const State &s, double *out);
 void launch_com_damping(const Launch &L, const ComSpec &c, double dt, const State &s);
+// rings per radial sweep chunk for this device and disk
+int radial_chunk_for(bool pair, bool adiabatic, int nr, int nz);
 void launch_transport_radial(const Launch &L, double dt, double omf, int chunk, const double *S,
                              const double *vr, const double *vaz, const double *E,
                              double *const mom[4], double *E_out, double *S_out);

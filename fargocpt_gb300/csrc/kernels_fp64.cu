@@ -2511,6 +2511,39 @@ void launch_ghost(const Launch &L, const BcSpec &bc, double omf, const State &s)
     k_ghost<<<(L.g.nz + 127) / 128, 128, 0, L.stream>>>(L.g, L.t, bc, omf, s);
 }
 
+int radial_chunk_for(bool pair, bool adiabatic, int nr, int nz)
+{
+    // resident 64-thread blocks per SM of the kernel this engine launches
+    const void *fn = pair ? (adiabatic ? (const void *)k_transport_radial_f2<5>
+                                       : (const void *)k_transport_radial_f2<4>)
+                          : (adiabatic ? (const void *)k_transport_radial<5>
+                                       : (const void *)k_transport_radial<4>);
+    int per_sm = 0, dev = 0, nsm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 64, 0) != cudaSuccess ||
+        cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        per_sm <= 0 || nsm <= 0) {
+        cudaGetLastError();
+        return (size_t)nr * nz >= ((size_t)8 << 20) ? 32 : 16;
+    }
+    if ((size_t)nr * nz < ((size_t)8 << 20)) return 16;
+    // large disks: the chunk of 28 .. 40 rings whose grid fills the fewest
+    // waves of resident blocks for the rings walked (each chunk also primes
+    // about three rings)
+    const long long cols = (nz + 63) / 64, slots = (long long)per_sm * nsm;
+    int best = 32;
+    long long best_cost = -1;
+    for (int c = 28; c <= 40; ++c) {
+        const long long blocks = cols * ((nr + c - 1) / c);
+        const long long cost = (blocks + slots - 1) / slots * (c + 3);
+        if (best_cost < 0 || cost < best_cost) {
+            best = c;
+            best_cost = cost;
+        }
+    }
+    return best;
+}
+
 void launch_transport_radial(const Launch &L, double dt, double omf, int chunk, const double *S,
                              const double *vr, const double *vaz, const double *E,
                              double *const mom[4], double *E_out, double *S_out)
